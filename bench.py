@@ -1,0 +1,313 @@
+"""Benchmark: cell-steps/s of the GeodesicODIS LTE time loop on one GB300.
+
+Workload (configs[1] of the benchmark set): icosahedral mesh level 6 (40962 cells,
+122880 faces), Enceladus-like body (r = 252.1 km, g = 0.113 m/s^2, rotation
+5.307e-5 rad/s -> P = 118394 s), h = 10 km, linear drag 1e-5 1/s, eccentricity
+tide e = 0.0047, self-gravity/loading to l_max = 16 with per-degree factors
+drawn from U[0.5, 1.5] (seed 1), 4000 steps per orbit (dt = 29.5985 s).  The
+FP64 method is the headline; the FP32-state variant and the run without the
+self-gravity term are reported beside it.
+
+A bench "step" is one orbit of the time loop (4000 LTE steps); L2 is flushed
+(256 MB write) before every timed orbit.  Inputs are synthetic (the reference
+has no dataset): the state starts from rest, forcing is the analytic tide.
+
+  python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the FP64
+C restatement in oracle/, built with OpenMP, all host cores) on bounded samples
+of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+RADIUS, GRAV, ANGVEL_IN = 252.1e3, 0.113, 5.307e-5
+H, ALPHA, ECC = 1e4, 1e-5, 0.0047
+LEVEL, LMAX, DT_TARGET = 6, 16, 29.5985
+METRIC = "cell-steps/s at level 6"
+
+
+def sh_factors(lmax: int, seed: int = 1) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    f = np.zeros(lmax + 1)
+    f[2:] = rng.uniform(0.5, 1.5, lmax - 1)
+    return f
+
+
+def workload_config(steps_per_orbit: int, n_cells: int, n_faces: int) -> dict:
+    return {"workload": f"LTE time loop, icosahedral level {LEVEL} ({n_cells} cells, {n_faces} faces), "
+                        f"ECC tide + SH self-gravity l_max={LMAX}, one orbit = {steps_per_orbit} steps per bench step",
+            "level": LEVEL, "cells": n_cells, "faces": n_faces, "steps_per_orbit": steps_per_orbit,
+            "sh_lmax": LMAX, "h_m": H, "alpha": ALPHA, "ecc": ECC,
+            "l2": "flushed (256 MB write) before each timed orbit; within an orbit the per-step working set "
+                  "stays L2-resident as in the real run"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1])); smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(n_steps: int, threads: int | None, with_sh: bool = True):
+    """The oracle (FP64 C restatement, OpenMP rows) on n_steps of the workload; returns cell-steps/s."""
+    from oracle import pyoracle as O
+    env_threads = str(threads or os.cpu_count())
+    os.environ["OMP_NUM_THREADS"] = env_threads
+    angvel, P, dt, n = O.derive_time(ANGVEL_IN, DT_TARGET)
+    with tempfile.TemporaryDirectory() as d:
+        grid = os.path.join(d, f"grid_{LEVEL}.txt")
+        import geodesicodis_gb300 as g
+        g.generate_grid_file(LEVEL, grid)
+        mesh = O.OracleMesh(grid, RADIUS)
+    kw = dict(radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt, potential=O.ECC)
+    if with_sh:
+        kw.update(sh_lmax=LMAX, sh_factors=sh_factors(LMAX))
+    sol = O.OracleSolver(mesh, **kw)
+    sol.run(2)
+    t = time.perf_counter()
+    sol.run(n_steps)
+    el = time.perf_counter() - t
+    return mesh.n_cells * n_steps / el, mesh
+
+
+def run_reference(args) -> dict:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return {}
+    threads = os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import pyoracle as O
+    import geodesicodis_gb300 as g
+    angvel, P, dt, n = O.derive_time(ANGVEL_IN, DT_TARGET)
+    with tempfile.TemporaryDirectory() as d:
+        grid = os.path.join(d, f"grid_{LEVEL}.txt")
+        g.generate_grid_file(LEVEL, grid)
+        mesh = O.OracleMesh(grid, RADIUS)
+    sol = O.OracleSolver(mesh, radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt,
+                         potential=O.ECC, sh_lmax=LMAX, sh_factors=sh_factors(LMAX))
+    sample = args.ref_sample_steps
+    for _ in range(args.warmup):
+        sol.run(sample)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        sol.run(sample)
+    el = time.perf_counter() - t
+    value = mesh.n_cells * sample * args.steps / el
+    desc = (f"{sample} LTE steps of the level-6 FP64 + l_max=16 workload per bench step, "
+            f"oracle C restatement (the reference build needs Eigen/HDF5, absent), OpenMP {threads} threads")
+    return {"metric": METRIC, "value": value, "unit": "cell-steps/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(n, mesh.n_cells, mesh.n_edges) | {"parallelism": "cpu-openmp",
+                                                                        "ref_sample_steps": sample},
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_ours(args) -> dict:
+    import torch
+    import geodesicodis_gb300 as g
+    from geodesicodis_gb300 import build_ext
+
+    build_ext.build()
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    angvel, P, dt, n = g.derive_time(ANGVEL_IN, DT_TARGET)
+    mesh = g.Mesh.generate(LEVEL, RADIUS)
+    N, E = mesh.n_cells, mesh.n_edges
+    fac = sh_factors(LMAX)
+
+    def solver(precision, lmax):
+        p = g.make_params(radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt,
+                          potential=g.POT_ECC, precision=precision, sh_lmax=lmax, sh_factors=fac if lmax else None)
+        s = g.Solver(p, mesh)
+        return s
+
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
+
+    def timed_orbits(sol, k, w):
+        sol.set_stream(stream.cuda_stream)
+        zero_state = (0, np.zeros(E), np.zeros(N), np.zeros((E, 3)), np.zeros((N, 3)))
+        sol.set_state(*zero_state)
+        with torch.cuda.stream(stream):
+            for _ in range(w):
+                sol.run_device(n, None)
+            torch.cuda.synchronize()
+            l0 = sol.launch_count()
+            total = 0.0
+            for _ in range(k):
+                flush.fill_(1.0)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                sol.run_device(n, None)
+                b.record(stream)
+                b.synchronize()
+                total += a.elapsed_time(b) / 1e3
+            launches = sol.launch_count() - l0
+        return total, launches
+
+    results = {}
+    clocks = ClockSampler()
+    clocks.start()
+    main = solver(g.FP64, LMAX)
+    t_main, launches = timed_orbits(main, args.steps, args.warmup)
+    clk = clocks.stop()
+    value = N * n * args.steps / t_main
+    results["fp64_sh16"] = value
+    # variants (fewer orbits)
+    kv = max(1, args.steps // 4)
+    for key, prec, lmax in (("fp32_sh16", g.FP32, LMAX), ("fp64_plain", g.FP64, 0), ("fp32_plain", g.FP32, 0)):
+        s = solver(prec, lmax)
+        t, _ = timed_orbits(s, kv, 1)
+        results[key] = N * n * kv / t
+        s.close()
+
+    # end-to-end through the C ABI with host buffers (pinned), copies inside the timed region
+    hv = torch.zeros(E, dtype=torch.float64).pin_memory()
+    he = torch.zeros(N, dtype=torch.float64).pin_memory()
+    hdv = torch.zeros(E * 3, dtype=torch.float64).pin_memory()
+    hde = torch.zeros(N * 3, dtype=torch.float64).pin_memory()
+    hp = torch.zeros(n, dtype=torch.float64).pin_memory()
+    e2e_sol = solver(g.FP64, LMAX)
+    e2e_sol.set_stream(stream.cuda_stream)
+    it = 0
+    for _ in range(args.warmup):
+        e2e_sol.set_state_ptrs(it, hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
+        e2e_sol.run_host_ptr(n, hp.data_ptr())
+        it = e2e_sol.get_state_ptrs(hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
+    torch.cuda.synchronize()
+    e2e_time = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        # each call below returns only after its copies and kernels are complete
+        e2e_sol.set_state_ptrs(it, hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
+        e2e_sol.run_host_ptr(n, hp.data_ptr())
+        it = e2e_sol.get_state_ptrs(hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
+        e2e_time += time.perf_counter() - ta
+    e2e_sol.close()
+    h2d = (E + N + 3 * E + 3 * N) * 8
+    d2h = (E + N + 3 * E + 3 * N) * 8 + n * 8
+
+    # per-kernel device times (graphs of back-to-back launches, CUDA events)
+    prof = solver(g.FP64, LMAX)
+    prof.set_stream(stream.cuda_stream)
+    ms = prof.profile_kernels(200)
+    prof.close()
+    s_bytes = 8
+    face_bytes = E * (19 * s_bytes + 48)
+    cell_bytes = N * (13 * s_bytes + 24)
+    K = (LMAX + 1) ** 2
+    sh_bytes = 2 * K * N * s_bytes + 2 * N * s_bytes
+    per_step = {"face_step": ms[0], "cell_step": ms[1], "sh_self_gravity": ms[2]}
+    dominant = max(per_step, key=per_step.get)
+    alg = {"face_step": face_bytes, "cell_step": cell_bytes, "sh_self_gravity": sh_bytes}[dominant]
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg / (per_step[dominant] / 1e3) / 1e9
+
+    out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_main / args.steps * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": workload_config(n, N, E) | {"parallelism": "single-gpu", "global_batch": 1},
+           "variants_cell_steps_per_s": results,
+           "kernel_ms_per_launch": per_step,
+           "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": None,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)" if peaks else "fallback 6800"},
+           "clocks": clk, "gpu_launches": launches,
+           "e2e": {"value": N * n * args.steps / e2e_time, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h,
+                   "how": "per orbit: odis_set_state from pinned host buffers, odis_run_steps(4000) with the "
+                          "power series copied to host, odis_get_state back to host; wall clock"}}
+    if not args.no_cpu_baseline:
+        v, _ = cpu_sample(args.cpu_sample_steps, None)
+        out["cpu_baseline"] = {"value": v, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"{args.cpu_sample_steps} LTE steps of the same level-6 FP64 + l_max=16 "
+                                         f"workload, oracle C restatement with OpenMP over rows/cells"}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ref-sample-steps", type=int, default=40)
+    ap.add_argument("--cpu-sample-steps", type=int, default=200)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        out = run_reference(args)
+        if out:
+            print(json.dumps(out))
+        return
+    out = run_ours(args)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,308 @@
+"""GB300-native GeodesicODIS LTE timestep.
+
+Python view of libodis_gpu.so (C ABI in include/odis_gpu.h).  The names
+mirror the reference's free functions (updateMomentum, updateEta, forcing,
+integrateAB3scalar, interpolateVelocity, updateEnergy) and its time loop
+(ab3Explicit), with the same argument meaning; errors raise OdisError with
+the library's status code instead of the reference's exit(0).
+
+The CUDA library is required: importing works without a GPU (the mesh and
+input.in code is host C++), but every call that computes on the device fails
+loudly when no GPU or no built library is present.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+__all__ = [
+    "OdisError", "lib", "Params", "Input", "Mesh", "Solver", "generate_grid_file", "derive_time",
+    "read_input", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL", "FP64", "FP32",
+]
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "lib" / "libodis_gpu.so"
+
+OK, ERR_ARG, ERR_CUDA, ERR_OOB, ERR_NONFINITE, ERR_TIMEOUT, ERR_IO, ERR_MESH, ERR_NOMEM = range(9)
+_NAMES = {1: "ODIS_ERR_ARG", 2: "ODIS_ERR_CUDA", 3: "ODIS_ERR_OOB", 4: "ODIS_ERR_NONFINITE",
+          5: "ODIS_ERR_TIMEOUT", 6: "ODIS_ERR_IO", 7: "ODIS_ERR_MESH", 8: "ODIS_ERR_NOMEM"}
+POT_NONE, POT_ECC, POT_OBLIQ, POT_OBLIQ_WEST, POT_FULL = range(5)
+FP64, FP32 = 0, 1
+MEM_HOST, MEM_DEVICE = 0, 1
+
+
+class OdisError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        super().__init__(f"{where}: {_NAMES.get(code, code)}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("radius", C.c_double), ("g", C.c_double), ("angvel", C.c_double), ("h", C.c_double),
+                ("alpha", C.c_double), ("ecc", C.c_double), ("obliq", C.c_double), ("love_reduct", C.c_double),
+                ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int), ("precision", C.c_int),
+                ("sh_lmax", C.c_int), ("sh_factors", C.POINTER(C.c_double))]
+
+
+class Input(C.Structure):
+    _fields_ = [("params", Params), ("period", C.c_double), ("end_time", C.c_double),
+                ("steps_per_orbit", C.c_int), ("grid_level", C.c_int), ("output_time", C.c_int),
+                ("sh_degree", C.c_int), ("advection", C.c_int), ("fric_linear", C.c_int),
+                ("surface_free", C.c_int), ("init_kind", C.c_int), ("out_flags", C.c_int),
+                ("potential_name", C.c_char * 32), ("friction_name", C.c_char * 32),
+                ("surface_name", C.c_char * 32), ("solver_name", C.c_char * 32), ("init_name", C.c_char * 32)]
+
+
+_lib = None
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_V = C.c_void_p
+
+_SIGS = {
+    "odis_grid_generate_file": ([C.c_int, C.c_char_p], C.c_int),
+    "odis_mesh_from_file": ([C.c_char_p, C.c_double, C.POINTER(_V)], C.c_int),
+    "odis_mesh_generate": ([C.c_int, C.c_double, C.POINTER(_V)], C.c_int),
+    "odis_mesh_from_arrays": ([C.c_int, _D, _I, _D, C.c_double, C.POINTER(_V)], C.c_int),
+    "odis_mesh_sizes": ([_V, _I, _I, _I], C.c_int),
+    "odis_mesh_field": ([_V, C.c_int, _D], C.c_int),
+    "odis_mesh_topology": ([_V, _I, _I, _I, _I, _D, _I], C.c_int),
+    "odis_mesh_destroy": ([_V], None),
+    "odis_derive_time": ([C.c_double, C.c_double, _D, _D, _D, _I], C.c_int),
+    "odis_params_from_input": ([C.c_char_p, C.POINTER(Input)], C.c_int),
+    "odis_create": ([C.POINTER(Params), _V, C.POINTER(_V)], C.c_int),
+    "odis_destroy": ([_V], None),
+    "odis_set_stream": ([_V, _V], C.c_int),
+    "odis_synchronize": ([_V], C.c_int),
+    "odis_device_status": ([_V], C.c_int),
+    "odis_update_momentum": ([_V, _V, _V, _V, C.c_int], C.c_int),
+    "odis_update_eta": ([_V, _V, _V, C.c_int], C.c_int),
+    "odis_forcing": ([_V, _V, C.c_int, C.c_double, C.c_int], C.c_int),
+    "odis_ab3": ([_V, _V, _V, C.c_int, C.c_int, C.c_int], C.c_int),
+    "odis_interpolate_velocity": ([_V, _V, _V, C.c_int], C.c_int),
+    "odis_update_energy": ([_V, _V, _V, _V, C.c_int], C.c_int),
+    "odis_run_steps": ([_V, C.c_int, _V, C.c_int], C.c_int),
+    "odis_get_state": ([_V, _I, _D, _D, _D, _D], C.c_int),
+    "odis_set_state": ([_V, C.c_int, _D, _D, _D, _D], C.c_int),
+    "odis_launch_count": ([_V, C.POINTER(C.c_longlong)], C.c_int),
+    "odis_profile_kernels": ([_V, C.c_int, _D], C.c_int),
+}
+
+
+def lib() -> C.CDLL:
+    """Load libodis_gpu.so (built in-tree by build_ext.build())."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise OdisError(ERR_CUDA, f"{LIB_PATH} is missing; build it with geodesicodis_gb300.build_ext.build()")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (args, res) in _SIGS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _ck(code: int, where: str) -> None:
+    if code != OK:
+        raise OdisError(code, where)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def _vp(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+def generate_grid_file(level: int, path: str | os.PathLike) -> None:
+    """Icosahedral grid at `level` (10*4^level+2 cells) in the reference grid-file format."""
+    _ck(lib().odis_grid_generate_file(int(level), os.fsencode(str(path))), "odis_grid_generate_file")
+
+
+def derive_time(angvel_in: float, dt_target: float):
+    """(angvel, period, dt, steps_per_orbit) after period rounding and dt snapping."""
+    a, p, d, n = C.c_double(), C.c_double(), C.c_double(), C.c_int()
+    _ck(lib().odis_derive_time(angvel_in, dt_target, C.byref(a), C.byref(p), C.byref(d), C.byref(n)),
+        "odis_derive_time")
+    return a.value, p.value, d.value, n.value
+
+
+def read_input(path: str | os.PathLike) -> Input:
+    inp = Input()
+    _ck(lib().odis_params_from_input(os.fsencode(str(path)), C.byref(inp)), "odis_params_from_input")
+    return inp
+
+
+class Mesh:
+    """Geometry and operators of an icosahedral-geodesic mesh (the reference's Mesh)."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+        n, e, v = C.c_int(), C.c_int(), C.c_int()
+        _ck(lib().odis_mesh_sizes(self._h, C.byref(n), C.byref(e), C.byref(v)), "odis_mesh_sizes")
+        self.n_cells, self.n_edges, self.n_vertices = n.value, e.value, v.value
+
+    @classmethod
+    def from_file(cls, path: str | os.PathLike, radius: float) -> "Mesh":
+        h = C.c_void_p()
+        _ck(lib().odis_mesh_from_file(os.fsencode(str(path)), radius, C.byref(h)), "odis_mesh_from_file")
+        return cls(h.value)
+
+    @classmethod
+    def generate(cls, level: int, radius: float) -> "Mesh":
+        h = C.c_void_p()
+        _ck(lib().odis_mesh_generate(int(level), radius, C.byref(h)), "odis_mesh_generate")
+        return cls(h.value)
+
+    def field(self, which: int) -> np.ndarray:
+        n = self.n_cells if which == 3 else self.n_edges
+        out = np.zeros(n)
+        _ck(lib().odis_mesh_field(self._h, which, _dp(out)), "odis_mesh_field")
+        return out
+
+    def topology(self):
+        E, N = self.n_edges, self.n_cells
+        fn = np.zeros((E, 2), np.int32)
+        faces = np.zeros((N, 6), np.int32)
+        nfd = np.zeros((N, 6), np.int32)
+        ifr = np.zeros((E, 10), np.int32)
+        iw = np.zeros((E, 10))
+        inn = np.zeros(E, np.int32)
+        ip = lambda a: a.ctypes.data_as(_I)  # noqa: E731
+        _ck(lib().odis_mesh_topology(self._h, ip(fn), ip(faces), ip(nfd), ip(ifr), _dp(iw), ip(inn)),
+            "odis_mesh_topology")
+        return dict(face_nodes=fn, faces=faces, node_face_dir=nfd, interp_friends=ifr, interp_w=iw, interp_n=inn)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.odis_mesh_destroy(h)
+            self._h = C.c_void_p()
+
+
+def make_params(*, radius, g, angvel, h, alpha, ecc=0.0, obliq=0.0, love_reduct=1.0, dt, potential=POT_ECC,
+                init_load=0, precision=FP64, sh_lmax=0, sh_factors=None) -> Params:
+    p = Params(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load, precision, sh_lmax, None)
+    if sh_lmax:
+        arr = np.ascontiguousarray(sh_factors, dtype=np.float64)
+        p._factors = arr  # keep alive
+        p.sh_factors = arr.ctypes.data_as(_D)
+    return p
+
+
+class Solver:
+    """One ocean instance on the GPU: the reference's per-operator functions and its AB3 time loop."""
+
+    def __init__(self, params: Params, mesh: Mesh):
+        self.params = params
+        self.mesh = mesh
+        h = C.c_void_p()
+        _ck(lib().odis_create(C.byref(params), mesh._h, C.byref(h)), "odis_create")
+        self._h = h
+        self.E, self.N = mesh.n_edges, mesh.n_cells
+
+    # -- the reference's free functions (host arrays) --------------------------------
+    def updateMomentum(self, v: np.ndarray, eta: np.ndarray) -> np.ndarray:
+        out = np.zeros(self.E)
+        v, eta = np.ascontiguousarray(v, np.float64), np.ascontiguousarray(eta, np.float64)
+        _ck(lib().odis_update_momentum(self._h, _vp(out), _vp(v), _vp(eta), MEM_HOST), "odis_update_momentum")
+        return out
+
+    def updateEta(self, v: np.ndarray) -> np.ndarray:
+        out = np.zeros(self.N)
+        v = np.ascontiguousarray(v, np.float64)
+        _ck(lib().odis_update_eta(self._h, _vp(out), _vp(v), MEM_HOST), "odis_update_eta")
+        return out
+
+    def forcing(self, type_: int, t: float) -> np.ndarray:
+        out = np.zeros(self.N)
+        _ck(lib().odis_forcing(self._h, _vp(out), int(type_), float(t), MEM_HOST), "odis_forcing")
+        return out
+
+    def integrateAB3scalar(self, s: np.ndarray, ds_dt: np.ndarray, it: int) -> None:
+        """In place on s[num] and ds_dt[num][3], as the reference."""
+        assert s.dtype == np.float64 and ds_dt.dtype == np.float64 and s.flags.c_contiguous and ds_dt.flags.c_contiguous
+        _ck(lib().odis_ab3(self._h, _vp(s), _vp(ds_dt), int(it), int(s.shape[0]), MEM_HOST), "odis_ab3")
+
+    def interpolateVelocity(self, v: np.ndarray) -> np.ndarray:
+        out = np.zeros((self.E, 2))
+        v = np.ascontiguousarray(v, np.float64)
+        _ck(lib().odis_interpolate_velocity(self._h, _vp(out), _vp(v), MEM_HOST), "odis_interpolate_velocity")
+        return out
+
+    def updateEnergy(self, uv: np.ndarray):
+        """(area-mean dissipation W/m^2, per-face dissipation)."""
+        e = np.zeros(self.E)
+        avg = np.zeros(1)
+        uv = np.ascontiguousarray(uv, np.float64)
+        _ck(lib().odis_update_energy(self._h, _vp(avg), _vp(e), _vp(uv), MEM_HOST), "odis_update_energy")
+        return float(avg[0]), e
+
+    # -- the time loop -------------------------------------------------------------
+    def run(self, nsteps: int, power: bool = True) -> np.ndarray | None:
+        out = np.zeros(nsteps) if power else None
+        ptr = _vp(out) if power else None
+        _ck(lib().odis_run_steps(self._h, int(nsteps), ptr, MEM_HOST), "odis_run_steps")
+        return out
+
+    def run_device(self, nsteps: int, power_dev_ptr: int | None) -> None:
+        _ck(lib().odis_run_steps(self._h, int(nsteps), C.c_void_p(power_dev_ptr) if power_dev_ptr else None,
+                                 MEM_DEVICE), "odis_run_steps")
+
+    def get_state(self):
+        it = C.c_int()
+        v, eta = np.zeros(self.E), np.zeros(self.N)
+        dv, de = np.zeros((self.E, 3)), np.zeros((self.N, 3))
+        _ck(lib().odis_get_state(self._h, C.byref(it), _dp(v), _dp(eta), _dp(dv), _dp(de)), "odis_get_state")
+        return it.value, v, eta, dv, de
+
+    def set_state(self, it: int, v, eta, dvdt, detadt) -> None:
+        a = [np.ascontiguousarray(x, np.float64) for x in (v, eta, dvdt, detadt)]
+        _ck(lib().odis_set_state(self._h, int(it), *[_dp(x) for x in a]), "odis_set_state")
+
+    def set_stream(self, stream_ptr: int) -> None:
+        _ck(lib().odis_set_stream(self._h, C.c_void_p(stream_ptr)), "odis_set_stream")
+
+    def launch_count(self) -> int:
+        n = C.c_longlong()
+        _ck(lib().odis_launch_count(self._h, C.byref(n)), "odis_launch_count")
+        return n.value
+
+    def profile_kernels(self, reps: int = 200):
+        ms = np.zeros(3)
+        _ck(lib().odis_profile_kernels(self._h, int(reps), _dp(ms)), "odis_profile_kernels")
+        return ms
+
+    def set_state_ptrs(self, it: int, v: int, eta: int, dvdt: int, detadt: int) -> None:
+        """set_state from raw host addresses (e.g. pinned buffers)."""
+        _ck(lib().odis_set_state(self._h, int(it), C.cast(v, _D), C.cast(eta, _D), C.cast(dvdt, _D),
+                                 C.cast(detadt, _D)), "odis_set_state")
+
+    def get_state_ptrs(self, v: int, eta: int, dvdt: int, detadt: int) -> int:
+        it = C.c_int()
+        _ck(lib().odis_get_state(self._h, C.byref(it), C.cast(v, _D), C.cast(eta, _D), C.cast(dvdt, _D),
+                                 C.cast(detadt, _D)), "odis_get_state")
+        return it.value
+
+    def run_host_ptr(self, nsteps: int, power_ptr: int) -> None:
+        _ck(lib().odis_run_steps(self._h, int(nsteps), C.c_void_p(power_ptr), MEM_HOST), "odis_run_steps")
+
+    def synchronize(self) -> None:
+        _ck(lib().odis_synchronize(self._h), "odis_synchronize")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib().odis_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

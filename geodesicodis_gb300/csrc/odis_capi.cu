@@ -1,0 +1,820 @@
+// C ABI of libodis_gpu.so (declared in include/odis_gpu.h).
+//
+// A context owns: the device copy of the mesh operators in the layout of
+// odis_device.cuh (FP64, or FP32 for the FP32-state variant), the state of
+// one ocean instance, a stream, and a CUDA graph of kGraphSteps fused steps
+// that odis_run_steps replays.  The per-step kernels read the step index
+// from a device counter, so one instantiated graph serves every chunk of
+// every run.
+#include "odis_internal.h"
+#include "odis_device.cuh"
+#include "odis_kernels.cuh"
+#include "odis_sh.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <vector>
+
+using namespace odis;
+
+namespace {
+
+constexpr double kPi = 3.1415926535897932384626433832795028841971693993751058;
+constexpr int kGraphSteps = 64;
+
+int pad128(int n) { return (n + 127) / 128 * 128; }
+
+#define ODIS_CK(call)                                  \
+    do {                                               \
+        cudaError_t _e = (call);                       \
+        if (_e != cudaSuccess) return ODIS_ERR_CUDA;   \
+    } while (0)
+
+// device allocation list freed with the context
+struct DevArena {
+    std::vector<void*> ptrs;
+    template <class T>
+    T* alloc(size_t n) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, n * sizeof(T) + 16) != cudaSuccess) return nullptr;
+        cudaMemset(p, 0, n * sizeof(T) + 16);
+        ptrs.push_back(p);
+        return (T*)p;
+    }
+    template <class T>
+    T* upload(const std::vector<T>& h) {
+        T* d = alloc<T>(h.size());
+        if (d && !h.empty()) cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+        return d;
+    }
+    ~DevArena() { for (void* p : ptrs) cudaFree(p); }
+};
+
+template <class T>
+struct Operators {
+    FaceCoef<T> fc{};
+    CellCoef<T> cc{};
+};
+
+}  // namespace
+
+struct odis_ctx {
+    odis_params p{};
+    std::vector<double> sh_factors;
+    int E = 0, N = 0, Ep = 0, Np = 0, eb = 0;
+    double r = 0.0;
+    DevArena mem;
+    Operators<double> op64;      // always present: per-operator calls are FP64
+    Operators<float> op32;       // FP32-state variant
+    double* nrm = nullptr;       // [2][Ep]
+    double* area = nullptr;      // [Ep]
+    double* trig = nullptr;      // [10][Np]
+    State<double> s64{};
+    State<float> s32{};
+    long long* d_iter = nullptr;
+    long long* d_run_first = nullptr;
+    int* d_status = nullptr;
+    double* d_partial = nullptr;
+    double* d_power = nullptr;
+    int power_cap = 0;
+    long long iter = 0;
+    std::vector<double> slot0_saved;    // reference history slot 0 before the first step
+    StepConst sc{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaGraphExec_t graph = nullptr;
+    double* stage[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t stage_n = 0;
+    ShLoading* sh = nullptr;
+    long long launches = 0;      // kernels of this library launched by this context
+    ~odis_ctx() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (sh) sh_destroy(sh);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// grid / mesh
+// ---------------------------------------------------------------------------
+extern "C" odis_status odis_grid_generate_file(int level, const char* path)
+{
+    if (!path) return ODIS_ERR_ARG;
+    GridArrays g;
+    int st = generate_grid(level, g);
+    if (st != ODIS_OK) return st;
+    return write_grid(g, path);
+}
+
+static odis_status mesh_from_grid(const GridArrays& g, double radius, odis_mesh** out)
+{
+    const double rc = kPi / 180.0;
+    std::vector<double> ns(g.node_deg.size()), cs(g.cent_deg.size());
+    for (size_t k = 0; k < ns.size(); k++) ns[k] = g.node_deg[k] * rc;
+    for (size_t k = 0; k < cs.size(); k++) cs[k] = g.cent_deg[k] * rc;
+    return odis_mesh_from_arrays(g.N, ns.data(), g.friends.data(), cs.data(), radius, out);
+}
+
+extern "C" odis_status odis_mesh_from_arrays(int n_nodes, const double* node_sph, const int* friends,
+                                             const double* cent_sph, double radius, odis_mesh** out)
+{
+    if (!out) return ODIS_ERR_ARG;
+    *out = nullptr;
+    odis_mesh* m = new (std::nothrow) odis_mesh;
+    if (!m) return ODIS_ERR_NOMEM;
+    int st = build_mesh(n_nodes, node_sph, friends, cent_sph, radius, m->m);
+    if (st != ODIS_OK) { delete m; return st; }
+    *out = m;
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_mesh_from_file(const char* path, double radius, odis_mesh** out)
+{
+    if (!path || !out) return ODIS_ERR_ARG;
+    GridArrays g;
+    int st = read_grid(path, g);
+    if (st != ODIS_OK) return st;
+    return mesh_from_grid(g, radius, out);
+}
+
+extern "C" odis_status odis_mesh_generate(int level, double radius, odis_mesh** out)
+{
+    if (!out) return ODIS_ERR_ARG;
+    GridArrays g;
+    int st = generate_grid(level, g);
+    if (st != ODIS_OK) return st;
+    return mesh_from_grid(g, radius, out);
+}
+
+extern "C" odis_status odis_mesh_sizes(const odis_mesh* m, int* n_cells, int* n_edges, int* n_vertices)
+{
+    if (!m) return ODIS_ERR_ARG;
+    if (n_cells) *n_cells = m->m.N;
+    if (n_edges) *n_edges = m->m.E;
+    if (n_vertices) *n_vertices = m->m.V;
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_mesh_field(const odis_mesh* mp, int which, double* out)
+{
+    if (!mp || !out) return ODIS_ERR_ARG;
+    const Mesh& m = mp->m;
+    const int E = m.E;
+    auto col = [&](const std::vector<double>& v, int c) { for (int i = 0; i < E; i++) out[i] = v[(size_t)i * 2 + c]; };
+    switch (which) {
+    case 0: std::memcpy(out, m.face_len.data(), sizeof(double) * E); break;
+    case 1: std::memcpy(out, m.face_dist.data(), sizeof(double) * E); break;
+    case 2: std::memcpy(out, m.face_area.data(), sizeof(double) * E); break;
+    case 3: std::memcpy(out, m.cv_area.data(), sizeof(double) * m.N); break;
+    case 4: col(m.face_centre, 0); break;
+    case 5: col(m.face_centre, 1); break;
+    case 6: col(m.face_m, 0); break;
+    case 7: col(m.face_m, 1); break;
+    case 8: col(m.face_normal, 0); break;
+    case 9: col(m.face_normal, 1); break;
+    case 10: col(m.face_int, 0); break;
+    case 11: col(m.face_int, 1); break;
+    default: return ODIS_ERR_ARG;
+    }
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_mesh_topology(const odis_mesh* mp, int* face_nodes, int* faces, int* node_face_dir,
+                                          int* interp_friends, double* interp_w, int* interp_n)
+{
+    if (!mp) return ODIS_ERR_ARG;
+    const Mesh& m = mp->m;
+    if (face_nodes) std::memcpy(face_nodes, m.face_nodes.data(), sizeof(int) * m.E * 2);
+    if (faces) std::memcpy(faces, m.faces.data(), sizeof(int) * m.N * 6);
+    if (node_face_dir) std::memcpy(node_face_dir, m.node_face_dir.data(), sizeof(int) * m.N * 6);
+    if (interp_friends) std::memcpy(interp_friends, m.interp_friends.data(), sizeof(int) * m.E * 10);
+    if (interp_w) std::memcpy(interp_w, m.interp_w.data(), sizeof(double) * m.E * 10);
+    if (interp_n) std::memcpy(interp_n, m.interp_n.data(), sizeof(int) * m.E);
+    return ODIS_OK;
+}
+
+extern "C" void odis_mesh_destroy(odis_mesh* m) { delete m; }
+
+// ---------------------------------------------------------------------------
+// parameters
+// ---------------------------------------------------------------------------
+extern "C" odis_status odis_derive_time(double angvel_in, double dt_target, double* angvel, double* period,
+                                        double* dt, int* steps_per_orbit)
+{
+    if (!(angvel_in > 0.0) || !(dt_target > 0.0) || !angvel || !period || !dt || !steps_per_orbit) return ODIS_ERR_ARG;
+    double P = 2. * kPi / angvel_in;
+    int it = (int)std::round(P / 2) * 2;
+    *period = (double)it;
+    *angvel = 2 * kPi / (double)it;
+    double d = *period;
+    int n = 100;
+    while (d > dt_target) { d = *period / n; n += 100; }
+    n -= 100;
+    *dt = d;
+    *steps_per_orbit = n;
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_params_from_input(const char* path, odis_input* out)
+{
+    if (!path || !out) return ODIS_ERR_ARG;
+    return parse_input(path, *out);
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+template <class T>
+static int build_operators(odis_ctx* c, const Mesh& m, const std::vector<double>& Ua, const std::vector<double>& Ub,
+                           Operators<T>& op)
+{
+    const int E = c->E, N = c->N, Ep = c->Ep, Np = c->Np;
+    const odis_params& p = c->p;
+    std::vector<int> nbr((size_t)kTrisk * Ep), n0(Ep), n1(Ep), edge((size_t)kCellFaces * Np);
+    std::vector<T> w((size_t)kTrisk * Ep, T(0)), gg0(Ep, T(0)), gg1(Ep, T(0)), cor(Ep, T(0));
+    std::vector<T> fP(Ep, T(0)), fQ(Ep, T(0)), diss(Ep, T(0)), hw((size_t)kCellFaces * Np, T(0));
+    const double four_pi_r2 = 4 * kPi * std::pow(m.r, 2.0);
+    for (int e = 0; e < Ep; e++) {
+        const int ee = e < E ? e : 0;
+        for (int k = 0; k < kTrisk; k++) {
+            const bool ok = e < E && k < m.interp_n[ee];
+            const int f = ok ? m.interp_friends[(size_t)ee * 10 + k] : ee;
+            nbr[(size_t)k * Ep + e] = f;
+            w[(size_t)k * Ep + e] = ok ? (T)(m.interp_w[(size_t)ee * 10 + k] * m.face_len[f] / m.face_dist[ee]) : T(0);
+        }
+        const int a = m.face_nodes[(size_t)ee * 2], b = m.face_nodes[(size_t)ee * 2 + 1];
+        n0[e] = a;
+        n1[e] = b;
+        if (e >= E) continue;
+        const double d = m.face_dist[e];
+        const double g0 = (-m.face_m[(size_t)e * 2]) / d, g1 = (m.face_m[(size_t)e * 2 + 1]) / d;
+        gg0[e] = (T)(-p.g * g0);
+        gg1[e] = (T)(-p.g * g1);
+        cor[e] = (T)(-2.0 * p.angvel * std::sin(m.face_centre[(size_t)e * 2]));
+        fP[e] = (T)(g0 * Ua[a] + g1 * Ua[b]);
+        fQ[e] = (T)(g0 * Ub[a] + g1 * Ub[b]);
+        diss[e] = (T)(p.alpha * 1000.0 * p.h * m.face_area[e] / four_pi_r2);
+    }
+    for (int i = 0; i < Np; i++) {
+        const int ii = i < N ? i : 0;
+        const int k5 = i < N ? m.nfriends(ii) : 0;
+        for (int k = 0; k < kCellFaces; k++) {
+            const bool ok = k < k5;
+            const int f = ok ? m.faces[(size_t)ii * 6 + k] : m.faces[(size_t)ii * 6];
+            edge[(size_t)k * Np + i] = f;
+            if (ok) {
+                const double dv = -m.node_face_dir[(size_t)ii * 6 + k] * m.face_len[f] / m.cv_area[ii];
+                hw[(size_t)k * Np + i] = (T)(p.h * dv);
+            }
+        }
+    }
+    // host-side range check of every index the kernels gather through
+    for (int x : nbr) if (x < 0 || x >= E) return ODIS_ERR_MESH;
+    for (int x : n0) if (x < 0 || x >= N) return ODIS_ERR_MESH;
+    for (int x : n1) if (x < 0 || x >= N) return ODIS_ERR_MESH;
+    for (int x : edge) if (x < 0 || x >= E) return ODIS_ERR_MESH;
+    DevArena& A = c->mem;
+    op.fc.nbr = A.upload(nbr);
+    op.fc.w = A.upload(w);
+    op.fc.n0 = A.upload(n0);
+    op.fc.n1 = A.upload(n1);
+    op.fc.gg0 = A.upload(gg0);
+    op.fc.gg1 = A.upload(gg1);
+    op.fc.cor = A.upload(cor);
+    op.fc.fP = A.upload(fP);
+    op.fc.fQ = A.upload(fQ);
+    op.fc.diss = A.upload(diss);
+    op.cc.edge = A.upload(edge);
+    op.cc.hw = A.upload(hw);
+    if (!op.fc.nbr || !op.fc.w || !op.fc.n0 || !op.fc.n1 || !op.fc.gg0 || !op.fc.gg1 || !op.fc.cor || !op.fc.fP ||
+        !op.fc.fQ || !op.fc.diss || !op.cc.edge || !op.cc.hw)
+        return ODIS_ERR_NOMEM;
+    return ODIS_OK;
+}
+
+template <class T>
+static int alloc_state(odis_ctx* c, State<T>& s, bool split)
+{
+    DevArena& A = c->mem;
+    for (int k = 0; k < 2; k++) {
+        s.v[k] = A.alloc<T>(c->Ep);
+        s.hv[k] = A.alloc<T>(c->Ep);
+        s.he[k] = A.alloc<T>(c->Np);
+        s.vlo[k] = split ? A.alloc<T>(c->Ep) : nullptr;
+        if (!s.v[k] || !s.hv[k] || !s.he[k] || (split && !s.vlo[k])) return ODIS_ERR_NOMEM;
+    }
+    s.eta = A.alloc<T>(c->Np);
+    s.etalo = split ? A.alloc<T>(c->Np) : nullptr;
+    if (!s.eta || (split && !s.etalo)) return ODIS_ERR_NOMEM;
+    s.usg = nullptr;
+    s.iter = c->d_iter;
+    s.run_first = c->d_run_first;
+    s.partial = c->d_partial;
+    s.power = nullptr;
+    s.status = c->d_status;
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, odis_ctx** out)
+{
+    if (!p || !mp || !out) return ODIS_ERR_ARG;
+    *out = nullptr;
+    if (p->precision != ODIS_FP64 && p->precision != ODIS_FP32) return ODIS_ERR_ARG;
+    if (p->potential < ODIS_POT_NONE || p->potential > ODIS_POT_FULL) return ODIS_ERR_ARG;
+    if (!(p->dt > 0.0) || !(p->g > 0.0) || !(p->h > 0.0) || !(p->radius > 0.0) || p->alpha < 0.0) return ODIS_ERR_ARG;
+    if (p->sh_lmax < 0 || p->sh_lmax > 64 || (p->sh_lmax > 0 && !p->sh_factors)) return ODIS_ERR_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return ODIS_ERR_CUDA;
+    std::unique_ptr<odis_ctx> c(new (std::nothrow) odis_ctx);
+    if (!c) return ODIS_ERR_NOMEM;
+    const Mesh& m = mp->m;
+    c->p = *p;
+    if (p->sh_lmax > 0) c->sh_factors.assign(p->sh_factors, p->sh_factors + p->sh_lmax + 1);
+    c->p.sh_factors = c->sh_factors.empty() ? nullptr : c->sh_factors.data();
+    c->E = m.E;
+    c->N = m.N;
+    c->Ep = pad128(m.E);
+    c->Np = pad128(m.N);
+    c->r = m.r;
+    c->eb = (m.E + kStepThreads - 1) / kStepThreads;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return ODIS_ERR_CUDA;
+    c->own_stream = true;
+    DevArena& A = c->mem;
+    c->d_iter = A.alloc<long long>(1);
+    c->d_run_first = A.alloc<long long>(1);
+    c->d_status = A.alloc<int>(1);
+    c->d_partial = A.alloc<double>(c->eb + 32);
+    if (!c->d_iter || !c->d_run_first || !c->d_status || !c->d_partial) return ODIS_ERR_NOMEM;
+
+    std::vector<double> Ua, Ub;
+    int st = forcing_basis(m, c->p, Ua, Ub);
+    if (st != ODIS_OK) return st;
+    st = build_operators<double>(c.get(), m, Ua, Ub, c->op64);
+    if (st != ODIS_OK) return st;
+    if (p->precision == ODIS_FP32) {
+        st = build_operators<float>(c.get(), m, Ua, Ub, c->op32);
+        if (st != ODIS_OK) return st;
+    }
+    // geometry needed by the per-operator calls
+    std::vector<double> nrm((size_t)2 * c->Ep, 0.0), area(c->Ep, 0.0), trig((size_t)10 * c->Np, 0.0);
+    for (int e = 0; e < m.E; e++) {
+        nrm[e] = m.face_normal[(size_t)e * 2];
+        nrm[(size_t)c->Ep + e] = m.face_normal[(size_t)e * 2 + 1];
+        area[e] = m.face_area[e];
+    }
+    for (int i = 0; i < m.N; i++) {
+        const double lat = m.node_sph[(size_t)i * 2], lon = m.node_sph[(size_t)i * 2 + 1];
+        const double t[10] = {std::cos(lat), std::sin(lat), std::cos(lon), std::sin(lon), std::cos(2.0 * lat),
+                              std::sin(2.0 * lat), std::cos(2.0 * lon), std::sin(2.0 * lon),
+                              std::pow(std::cos(lat), 2.0), std::pow(std::sin(lat), 2.0)};
+        for (int k = 0; k < 10; k++) trig[(size_t)k * c->Np + i] = t[k];
+    }
+    c->nrm = A.upload(nrm);
+    c->area = A.upload(area);
+    c->trig = A.upload(trig);
+    if (!c->nrm || !c->area || !c->trig) return ODIS_ERR_NOMEM;
+
+    st = alloc_state<double>(c.get(), c->s64, false);
+    if (st != ODIS_OK) return st;
+    if (p->precision == ODIS_FP32) {
+        st = alloc_state<float>(c.get(), c->s32, true);
+        if (st != ODIS_OK) return st;
+    }
+    if (p->sh_lmax > 0) {
+        st = sh_create(&c->sh, m, p->sh_lmax, c->p.sh_factors, p->precision, c->Np);
+        if (st != ODIS_OK) return st;
+        c->s64.usg = sh_usg64(c->sh);
+        c->s32.usg = sh_usg32(c->sh);
+    }
+    StepConst& sc = c->sc;
+    sc.E = m.E;
+    sc.N = m.N;
+    sc.Ep = c->Ep;
+    sc.Np = c->Np;
+    sc.dt = p->dt;
+    sc.alpha = p->alpha;
+    sc.angvel = p->angvel;
+    sc.ab3a = 23. / 12.;
+    sc.ab3b = -16. / 12.;
+    sc.ab3c = 5. / 12.;
+    sc.init_load = p->init_load ? 1 : 0;
+    sc.use_sg = p->sh_lmax > 0 ? 1 : 0;
+    c->stage_n = (size_t)3 * std::max(c->Ep, c->Np);
+    for (int k = 0; k < 4; k++) {
+        c->stage[k] = A.alloc<double>(c->stage_n);
+        if (!c->stage[k]) return ODIS_ERR_NOMEM;
+    }
+    c->slot0_saved.assign((size_t)(m.E + m.N), 0.0);
+    if (cudaDeviceSynchronize() != cudaSuccess) return ODIS_ERR_CUDA;
+    *out = c.release();
+    return ODIS_OK;
+}
+
+extern "C" void odis_destroy(odis_ctx* c)
+{
+    if (!c) return;
+    cudaStreamSynchronize(c->stream);
+    delete c;
+}
+
+extern "C" odis_status odis_set_stream(odis_ctx* c, void* s)
+{
+    if (!c) return ODIS_ERR_ARG;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return ODIS_ERR_CUDA;
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    c->own_stream = false;
+    c->stream = (cudaStream_t)s;
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_synchronize(odis_ctx* c)
+{
+    if (!c) return ODIS_ERR_ARG;
+    return cudaStreamSynchronize(c->stream) == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
+}
+
+extern "C" odis_status odis_device_status(odis_ctx* c)
+{
+    if (!c) return ODIS_ERR_ARG;
+    int h = 0;
+    ODIS_CK(cudaMemcpyAsync(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    ODIS_CK(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+    ODIS_CK(cudaStreamSynchronize(c->stream));
+    for (int b = 1; b < 16; b++)
+        if (h & (1 << b)) return b;
+    return ODIS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// per-operator calls
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Io {
+    odis_ctx* c;
+    int mem;
+    int slot = 0;
+    // device view of a caller buffer of n doubles (copied in if `in`)
+    double* in(const double* p, size_t n) {
+        if (mem == ODIS_MEM_DEVICE) return const_cast<double*>(p);
+        double* d = c->stage[slot++];
+        if (n && cudaMemcpyAsync(d, p, n * sizeof(double), cudaMemcpyHostToDevice, c->stream) != cudaSuccess) return nullptr;
+        return d;
+    }
+    double* out(double* p) { return mem == ODIS_MEM_DEVICE ? p : c->stage[slot++]; }
+    int back(double* host, const double* dev, size_t n) {
+        if (mem == ODIS_MEM_DEVICE || !host) return ODIS_OK;
+        ODIS_CK(cudaMemcpyAsync(host, dev, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        return ODIS_OK;
+    }
+    int done() {
+        ODIS_CK(cudaGetLastError());
+        ODIS_CK(cudaStreamSynchronize(c->stream));
+        return ODIS_OK;
+    }
+};
+
+bool mem_ok(int mem) { return mem == ODIS_MEM_HOST || mem == ODIS_MEM_DEVICE; }
+
+}  // namespace
+
+extern "C" odis_status odis_update_momentum(odis_ctx* c, double* dvdt, const double* v, const double* eta, int mem)
+{
+    if (!c || !dvdt || !v || !eta || !mem_ok(mem)) return ODIS_ERR_ARG;
+    Io io{c, mem};
+    const double* dv = io.in(v, c->E);
+    const double* de = io.in(eta, c->N);
+    double* dout = io.out(dvdt);
+    if (!dv || !de) return ODIS_ERR_CUDA;
+    launch_momentum(c->op64.fc, c->E, c->Ep, dout, dv, de, c->stream);
+    int st = io.back(dvdt, dout, c->E);
+    return st != ODIS_OK ? st : io.done();
+}
+
+extern "C" odis_status odis_update_eta(odis_ctx* c, double* detadt, const double* v, int mem)
+{
+    if (!c || !detadt || !v || !mem_ok(mem)) return ODIS_ERR_ARG;
+    Io io{c, mem};
+    const double* dv = io.in(v, c->E);
+    double* dout = io.out(detadt);
+    if (!dv) return ODIS_ERR_CUDA;
+    launch_divergence(c->op64.cc, c->N, c->Np, dout, dv, c->stream);
+    int st = io.back(detadt, dout, c->N);
+    return st != ODIS_OK ? st : io.done();
+}
+
+extern "C" odis_status odis_forcing(odis_ctx* c, double* U, int type, double t, int mem)
+{
+    if (!c || !U || !mem_ok(mem) || type < ODIS_POT_NONE || type > ODIS_POT_FULL) return ODIS_ERR_ARG;
+    Io io{c, mem};
+    double* dout = io.out(U);
+    launch_forcing(c->trig, c->N, c->Np, dout, type, t, c->p.angvel, c->p.radius, c->p.love_reduct, c->p.ecc,
+                   c->p.obliq, c->stream);
+    int st = io.back(U, dout, c->N);
+    return st != ODIS_OK ? st : io.done();
+}
+
+extern "C" odis_status odis_ab3(odis_ctx* c, double* s, double* hist, int iter, int num, int mem)
+{
+    if (!c || !s || !hist || num < 0 || iter < 0 || !mem_ok(mem)) return ODIS_ERR_ARG;
+    if ((size_t)num * 3 > c->stage_n) return ODIS_ERR_ARG;
+    Io io{c, mem};
+    double* ds = io.in(s, num);
+    double* dh = io.in(hist, (size_t)num * 3);
+    if (!ds || !dh) return ODIS_ERR_CUDA;
+    launch_ab3_ref(ds, dh, iter, num, c->p.dt, c->p.init_load, c->stream);
+    int st = io.back(s, ds, num);
+    if (st == ODIS_OK) st = io.back(hist, dh, (size_t)num * 3);
+    return st != ODIS_OK ? st : io.done();
+}
+
+extern "C" odis_status odis_interpolate_velocity(odis_ctx* c, double* uv, const double* v, int mem)
+{
+    if (!c || !uv || !v || !mem_ok(mem)) return ODIS_ERR_ARG;
+    Io io{c, mem};
+    const double* dv = io.in(v, c->E);
+    double* dout = io.out(uv);
+    if (!dv) return ODIS_ERR_CUDA;
+    launch_interp(c->op64.fc, c->nrm, c->E, c->Ep, dout, dv, c->stream);
+    int st = io.back(uv, dout, (size_t)c->E * 2);
+    return st != ODIS_OK ? st : io.done();
+}
+
+extern "C" odis_status odis_update_energy(odis_ctx* c, double* avg, double* e, const double* uv, int mem)
+{
+    if (!c || !avg || !uv || !mem_ok(mem)) return ODIS_ERR_ARG;
+    Io io{c, mem};
+    const double* duv = io.in(uv, (size_t)c->E * 2);
+    double* de = e ? io.out(e) : nullptr;
+    double* davg = mem == ODIS_MEM_DEVICE ? avg : c->stage[3];
+    if (!duv) return ODIS_ERR_CUDA;
+    launch_energy(c->area, c->E, c->p.alpha * 1000.0 * c->p.h, 4 * kPi * std::pow(c->r, 2.0), duv, de, c->d_partial,
+                  davg, c->stream);
+    int st = e ? io.back(e, de, c->E) : ODIS_OK;
+    if (st == ODIS_OK) st = io.back(avg, davg, 1);
+    return st != ODIS_OK ? st : io.done();
+}
+
+// ---------------------------------------------------------------------------
+// fused time loop
+// ---------------------------------------------------------------------------
+static int kernels_per_step(const odis_ctx* c) { return 2 + (c->sh ? 3 : 0); }
+
+static void enqueue_steps(odis_ctx* c, int n)
+{
+    c->launches += (long long)n * kernels_per_step(c) + 1;
+    for (int k = 0; k < n; k++) {
+        if (c->sh) sh_enqueue(c->sh, c->p.precision == ODIS_FP32 ? (const void*)c->s32.eta : (const void*)c->s64.eta,
+                              c->stream);
+        if (c->p.precision == ODIS_FP64) launch_step<double, false>(c->op64.fc, c->op64.cc, c->s64, c->sc, k, c->stream);
+        else launch_step<float, true>(c->op32.fc, c->op32.cc, c->s32, c->sc, k, c->stream);
+    }
+    launch_bump(c->d_iter, n, c->stream);
+}
+
+static int ensure_graph(odis_ctx* c)
+{
+    if (c->graph) return ODIS_OK;
+    cudaGraph_t g = nullptr;
+    const long long before = c->launches;
+    ODIS_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_steps(c, kGraphSteps);
+    c->launches = before;     // capture launches nothing; replays are counted
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return ODIS_ERR_CUDA; }
+    e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { c->graph = nullptr; return ODIS_ERR_CUDA; }
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem)
+{
+    if (!c || n < 0 || !mem_ok(mem)) return ODIS_ERR_ARG;
+    if (n == 0) return ODIS_OK;
+    double* dpow = nullptr;
+    if (power) {
+        if (mem == ODIS_MEM_DEVICE) dpow = power;
+        else {
+            if (n > c->power_cap) {
+                if (c->d_power) cudaFree(c->d_power);
+                c->d_power = nullptr;
+                c->power_cap = 0;
+                ODIS_CK(cudaMalloc(&c->d_power, sizeof(double) * n));
+                c->power_cap = n;
+            }
+            dpow = c->d_power;
+        }
+    }
+    // the graph bakes in the state struct, so the power pointer lives in the
+    // state only for eager launches; graphs are rebuilt if it changes
+    const long long first = c->iter;
+    ODIS_CK(cudaMemcpyAsync(c->d_run_first, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    ODIS_CK(cudaMemcpyAsync(c->d_iter, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    if (c->s64.power != dpow || c->s32.power != dpow) {
+        c->s64.power = dpow;
+        c->s32.power = dpow;
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    }
+    int done = 0;
+    if (n >= kGraphSteps) {
+        int st = ensure_graph(c);
+        if (st != ODIS_OK) return st;
+        for (; done + kGraphSteps <= n; done += kGraphSteps) {
+            ODIS_CK(cudaGraphLaunch(c->graph, c->stream));
+            c->launches += (long long)kGraphSteps * kernels_per_step(c) + 1;
+        }
+    }
+    if (done < n) enqueue_steps(c, n - done);
+    if (c->p.precision == ODIS_FP64) launch_power_tail<double>(c->op64.fc, c->s64, c->sc, c->stream);
+    else launch_power_tail<float>(c->op32.fc, c->s32, c->sc, c->stream);
+    c->launches += 2;
+    ODIS_CK(cudaGetLastError());
+    if (power && mem == ODIS_MEM_HOST)
+        ODIS_CK(cudaMemcpyAsync(power, dpow, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    ODIS_CK(cudaStreamSynchronize(c->stream));
+    c->iter += n;
+    int h = 0;
+    ODIS_CK(cudaMemcpy(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) ODIS_CK(cudaMemset(c->d_status, 0, sizeof(int)));
+    if (h & (1 << ODIS_ERR_NONFINITE)) return ODIS_ERR_NONFINITE;
+    return ODIS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// state in the reference's layout
+// ---------------------------------------------------------------------------
+template <class T>
+static int get_vec(odis_ctx* c, const T* hi, const T* lo, size_t n, double* out)
+{
+    std::vector<T> a(n), b;
+    ODIS_CK(cudaMemcpy(a.data(), hi, n * sizeof(T), cudaMemcpyDeviceToHost));
+    if (lo) { b.resize(n); ODIS_CK(cudaMemcpy(b.data(), lo, n * sizeof(T), cudaMemcpyDeviceToHost)); }
+    for (size_t i = 0; i < n; i++) out[i] = lo ? (double)a[i] + (double)b[i] : (double)a[i];
+    (void)c;
+    return ODIS_OK;
+}
+
+template <class T>
+static int set_vec(T* hi, T* lo, size_t n, const double* in)
+{
+    std::vector<T> a(n), b(n);
+    for (size_t i = 0; i < n; i++) {
+        a[i] = (T)in[i];
+        b[i] = (T)(in[i] - (double)a[i]);
+    }
+    ODIS_CK(cudaMemcpy(hi, a.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+    if (lo) ODIS_CK(cudaMemcpy(lo, b.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+    return ODIS_OK;
+}
+
+template <class T>
+static int get_state_t(odis_ctx* c, State<T>& s, double* v, double* eta, double* dvdt, double* detadt)
+{
+    const long long k = c->iter;
+    const size_t E = c->E, N = c->N;
+    int st = ODIS_OK;
+    if (v) st = get_vec<T>(c, s.v[k & 1], s.vlo[0] ? s.vlo[k & 1] : nullptr, E, v);
+    if (st == ODIS_OK && eta) st = get_vec<T>(c, s.eta, s.etalo, N, eta);
+    for (int which = 0; which < 2 && st == ODIS_OK; which++) {
+        double* out = which == 0 ? dvdt : detadt;
+        if (!out) continue;
+        const size_t n = which == 0 ? E : N;
+        T* const* h = which == 0 ? s.hv : s.he;
+        std::vector<double> a(n), b(n);
+        st = get_vec<T>(c, h[0], nullptr, n, a.data());
+        if (st == ODIS_OK) st = get_vec<T>(c, h[1], nullptr, n, b.data());
+        const std::vector<double>& h0 = a;    // hv[0]
+        const std::vector<double>& h1 = b;    // hv[1]
+        const double* saved = c->slot0_saved.data() + (which == 0 ? 0 : E);
+        for (size_t i = 0; i < n; i++) {
+            double s0, s1, s2;
+            if (k == 0) { s0 = saved[i]; s1 = h1[i]; s2 = h0[i]; }
+            else if (k == 1 && !c->p.init_load) { s0 = h0[i]; s1 = h1[i]; s2 = h0[i]; }
+            else {
+                const double fl = ((k + 1) & 1) ? h1[i] : h0[i];
+                const double fo = (k & 1) ? h1[i] : h0[i];
+                s0 = fl; s1 = fl; s2 = fo;
+            }
+            out[i * 3] = s0; out[i * 3 + 1] = s1; out[i * 3 + 2] = s2;
+        }
+    }
+    return st;
+}
+
+template <class T>
+static int set_state_t(odis_ctx* c, State<T>& s, long long k, const double* v, const double* eta, const double* dvdt,
+                       const double* detadt)
+{
+    const size_t E = c->E, N = c->N;
+    int st = ODIS_OK;
+    for (int q = 0; q < 2; q++) {
+        ODIS_CK(cudaMemset(s.v[q], 0, sizeof(T) * c->Ep));
+        if (s.vlo[q]) ODIS_CK(cudaMemset(s.vlo[q], 0, sizeof(T) * c->Ep));
+    }
+    if (v) st = set_vec<T>(s.v[k & 1], s.vlo[0] ? s.vlo[k & 1] : nullptr, E, v);
+    ODIS_CK(cudaMemset(s.eta, 0, sizeof(T) * c->Np));
+    if (s.etalo) ODIS_CK(cudaMemset(s.etalo, 0, sizeof(T) * c->Np));
+    if (st == ODIS_OK && eta) st = set_vec<T>(s.eta, s.etalo, N, eta);
+    for (int which = 0; which < 2 && st == ODIS_OK; which++) {
+        const double* in = which == 0 ? dvdt : detadt;
+        const size_t n = which == 0 ? E : N;
+        T* const* h = which == 0 ? s.hv : s.he;
+        std::vector<double> h0(n, 0.0), h1(n, 0.0);
+        double* saved = c->slot0_saved.data() + (which == 0 ? 0 : E);
+        for (size_t i = 0; i < n; i++) {
+            const double s0 = in ? in[i * 3] : 0.0, s1 = in ? in[i * 3 + 1] : 0.0, s2 = in ? in[i * 3 + 2] : 0.0;
+            saved[i] = s0;
+            if (k == 1 && !c->p.init_load) { h0[i] = s2; h1[i] = s1; }
+            else if ((k + 1) & 1) { h1[i] = s1; h0[i] = s2; }
+            else { h0[i] = s1; h1[i] = s2; }
+        }
+        st = set_vec<T>(h[0], nullptr, n, h0.data());
+        if (st == ODIS_OK) st = set_vec<T>(h[1], nullptr, n, h1.data());
+    }
+    return st;
+}
+
+extern "C" odis_status odis_get_state(odis_ctx* c, int* iter, double* v, double* eta, double* dvdt, double* detadt)
+{
+    if (!c) return ODIS_ERR_ARG;
+    ODIS_CK(cudaStreamSynchronize(c->stream));
+    if (iter) *iter = (int)c->iter;
+    return c->p.precision == ODIS_FP64 ? get_state_t<double>(c, c->s64, v, eta, dvdt, detadt)
+                                       : get_state_t<float>(c, c->s32, v, eta, dvdt, detadt);
+}
+
+extern "C" odis_status odis_set_state(odis_ctx* c, int iter, const double* v, const double* eta, const double* dvdt,
+                                      const double* detadt)
+{
+    if (!c || iter < 0) return ODIS_ERR_ARG;
+    ODIS_CK(cudaStreamSynchronize(c->stream));
+    c->iter = iter;
+    return c->p.precision == ODIS_FP64 ? set_state_t<double>(c, c->s64, iter, v, eta, dvdt, detadt)
+                                       : set_state_t<float>(c, c->s32, iter, v, eta, dvdt, detadt);
+}
+
+// ---------------------------------------------------------------------------
+// measurement helpers
+// ---------------------------------------------------------------------------
+extern "C" odis_status odis_launch_count(odis_ctx* c, long long* n)
+{
+    if (!c || !n) return ODIS_ERR_ARG;
+    *n = c->launches;
+    return ODIS_OK;
+}
+
+// Average device time of each kernel group, each launched `reps` times back to
+// back inside one CUDA graph and timed with events on the context stream:
+// ms[0] face kernel, ms[1] cell kernel, ms[2] SH analysis+solve+synthesis
+// (0 without self-gravity).  Leaves the state undefined.
+extern "C" odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms)
+{
+    if (!c || reps <= 0 || !ms) return ODIS_ERR_ARG;
+    ODIS_CK(cudaStreamSynchronize(c->stream));
+    cudaEvent_t a, b;
+    ODIS_CK(cudaEventCreate(&a));
+    ODIS_CK(cudaEventCreate(&b));
+    int st = ODIS_OK;
+    for (int which = 0; which < 3 && st == ODIS_OK; which++) {
+        ms[which] = 0.0;
+        if (which == 2 && !c->sh) continue;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
+        for (int r = 0; r < reps; r++) {
+            const bool f32 = c->p.precision == ODIS_FP32;
+            if (which == 0) {
+                if (f32) launch_edge<float, true>(c->op32.fc, c->s32, c->sc, 2, c->stream);
+                else launch_edge<double, false>(c->op64.fc, c->s64, c->sc, 2, c->stream);
+            } else if (which == 1) {
+                if (f32) launch_cell<float, true>(c->op32.cc, c->s32, c->sc, 2, c->stream);
+                else launch_cell<double, false>(c->op64.cc, c->s64, c->sc, 2, c->stream);
+            } else {
+                sh_enqueue(c->sh, f32 ? (const void*)c->s32.eta : (const void*)c->s64.eta, c->stream);
+            }
+        }
+        if (cudaStreamEndCapture(c->stream, &g) != cudaSuccess || cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) {
+            st = ODIS_ERR_CUDA;
+        } else {
+            cudaGraphLaunch(ge, c->stream);                 // warm-up
+            cudaEventRecord(a, c->stream);
+            cudaGraphLaunch(ge, c->stream);
+            cudaEventRecord(b, c->stream);
+            if (cudaEventSynchronize(b) != cudaSuccess) st = ODIS_ERR_CUDA;
+            float t = 0.f;
+            cudaEventElapsedTime(&t, a, b);
+            ms[which] = (double)t / reps;
+            c->launches += 2LL * reps * (which == 2 ? 3 : 1);
+        }
+        if (ge) cudaGraphExecDestroy(ge);
+        if (g) cudaGraphDestroy(g);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return st;
+}

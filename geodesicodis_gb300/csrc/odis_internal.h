@@ -1,0 +1,63 @@
+// Internal declarations shared by the host (C++) and device (CUDA) parts of
+// libodis_gpu.so.  Nothing here crosses the C ABI.
+#pragma once
+
+#include "../../include/odis_gpu.h"
+
+#include <cstdint>
+#include <vector>
+
+namespace odis {
+
+// Grid in the reference's file layout, angles in degrees.
+struct GridArrays {
+    int N = 0;
+    std::vector<double> node_deg;   // [N][2]
+    std::vector<int> friends;       // [N][6]
+    std::vector<double> cent_deg;   // [N][6][2]
+};
+
+int generate_grid(int level, GridArrays& g);
+int write_grid(const GridArrays& g, const char* path);
+int read_grid(const char* path, GridArrays& g);
+
+// Host-side geometry and operator data, numbered exactly as the reference
+// numbers cells (file order) and faces (AssignFaces loop order).
+struct Mesh {
+    int N = 0, E = 0, V = 0;
+    double r = 0.0;
+    std::vector<double> node_sph;      // [N][2] rad
+    std::vector<int> friends;          // [N][6]
+    std::vector<double> cent_sph;      // [N][6][2] rad
+    std::vector<double> cv_area;       // [N]
+    std::vector<int> vertexes;         // [N][6]
+    std::vector<double> vert_sph;      // [V][2]
+    std::vector<int> faces;            // [N][6]
+    std::vector<int> node_face_dir;    // [N][6]
+    std::vector<int> face_nodes;       // [E][2]
+    std::vector<double> face_len, face_dist, face_area;  // [E]
+    std::vector<double> face_centre;   // [E][2]
+    std::vector<double> face_m;        // [E][2]
+    std::vector<double> face_normal;   // [E][2]
+    std::vector<double> face_int;      // [E][2]
+    std::vector<int> interp_friends;   // [E][10]
+    std::vector<double> interp_w;      // [E][10]
+    std::vector<int> interp_n;         // [E]
+    int nfriends(int i) const { return friends[i * 6 + 5] < 0 ? 5 : 6; }
+};
+
+int build_mesh(int N, const double* node_sph, const int* friends, const double* cent_sph,
+               double radius, Mesh& m);
+
+// Forcing as a single-frequency pair: U_i(t) = cos(M) Ua_i + sin(M) Ub_i with
+// M = angvel * t, for the ECC / OBLIQ / OBLIQ_WEST / FULL potentials.
+int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, std::vector<double>& Ub);
+
+// Parse input.in (src/globals.cpp:325-477 semantics).
+int parse_input(const char* path, odis_input& out);
+
+}  // namespace odis
+
+struct odis_mesh {
+    odis::Mesh m;
+};

@@ -1,0 +1,392 @@
+// sm_103a kernels of the LTE timestep (src/timeIntegrator.cpp:205-272 of the
+// reference, linear branch).
+//
+// One step is two launches:
+//   k_edge_step : per face e (one thread each)
+//       T_e   = sum_k w_ek v_nbr(e,k)                  TRiSK tangential velocity of v^n
+//       P^{n-1} partial: diss_e (v_e^2 + T_e^2)         (dissipation of v^n, block partial)
+//       f_e   = -g (G eta^n)_e - 2 Omega sin(phi_e) T_e  (updateMomentum, linear branch)
+//       v^{n+1} = v^n + dt AB3(f) + dt (-alpha v^n + (G U(t^{n+1}))_e)
+//   k_cell_step : per cell i
+//       q_i   = h (D v^{n+1})_i                         (updateEta, linear branch)
+//       eta^{n+1} = eta^n + dt AB3(q)
+//       block 0 also folds the face kernel's block partials into P^{n-1}
+// The tangential reconstruction of v^{n+1} is needed twice in the reference
+// (Coriolis of step n+1 and the dissipation of step n); it is computed once,
+// in the next step's face kernel, so the dissipation of the last step of a
+// run is finished by k_power_tail.
+//
+// Reductions are deterministic: fixed-shape warp shuffles inside a block,
+// then one warp summing the per-block partials in block order.
+#include "../../include/odis_gpu.h"
+#include "odis_device.cuh"
+#include "odis_kernels.cuh"
+
+#include <cmath>
+
+namespace odis {
+
+namespace {
+
+template <class T> __device__ __forceinline__ T fmaT(T a, T b, T c);
+template <> __device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+__device__ __forceinline__ double warp_sum(double x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// Sum of one double per thread over the block; the result is valid in thread 0.
+template <int kThreads>
+__device__ __forceinline__ double block_sum(double x, double* smem)
+{
+    x = warp_sum(x);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) smem[wid] = x;
+    __syncthreads();
+    double s = 0.0;
+    if (wid == 0) {
+        s = lane < kThreads / 32 ? smem[lane] : 0.0;
+        s = warp_sum(s);
+    }
+    return s;
+}
+
+// One warp sums n partials in a fixed order; result in lane 0.
+__device__ __forceinline__ double fold_partials(const double* p, int n)
+{
+    const int lane = threadIdx.x & 31;
+    double s = 0.0;
+    for (int k = lane; k < n; k += 32) s += p[k];
+    return warp_sum(s);
+}
+
+__device__ __forceinline__ bool finite_d(double x) { return fabs(x) <= 1.7976931348623157e308; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// fused step, face part
+// ---------------------------------------------------------------------------
+template <class T, bool kSplit>
+__global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, State<T> st, StepConst sc, int offset)
+{
+    __shared__ double s_cs[2];
+    __shared__ double s_red[kStepThreads / 32];
+    const long long it = *st.iter + offset;
+    if (threadIdx.x == 0) {
+        // forcing phase at t^{n+1} = dt*n + dt, as src/timeIntegrator.cpp:218
+        double t = sc.dt * (double)it + sc.dt, s, c;
+        sincos(sc.angvel * t, &s, &c);
+        s_cs[0] = c;
+        s_cs[1] = s;
+    }
+    __syncthreads();
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Ep = sc.Ep;
+    const T* __restrict__ vin = st.v[it & 1];
+    double pw = 0.0;
+    if (e < sc.E) {
+        T tsum = T(0);
+#pragma unroll
+        for (int k = 0; k < kTrisk; k++) tsum = fmaT<T>(__ldg(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
+        const T ve = vin[e];
+        const int i0 = __ldg(&fc.n0[e]), i1 = __ldg(&fc.n1[e]);
+        const T d = __ldg(&fc.diss[e]);
+        pw = (double)(d * fmaT<T>(ve, ve, tsum * tsum));
+        // updateMomentum: -g G eta + C v
+        const T f0 = fmaT<T>(__ldg(&fc.cor[e]), tsum, fmaT<T>(__ldg(&fc.gg0[e]), st.eta[i0], __ldg(&fc.gg1[e]) * st.eta[i1]));
+        // forcing gradient G U(t^{n+1}) (+ self-gravity), then linear drag
+        T gu = fmaT<T>((T)s_cs[0], __ldg(&fc.fP[e]), (T)s_cs[1] * __ldg(&fc.fQ[e]));
+        if (sc.use_sg) gu -= fmaT<T>(__ldg(&fc.gg0[e]), st.usg[i0], __ldg(&fc.gg1[e]) * st.usg[i1]);
+        const T drag = fmaT<T>((T)(-sc.alpha), ve, gu);
+        T* hcur = st.hv[it & 1];
+        T inc = f0;
+        if (sc.init_load || it > 1) {
+            const T f1 = st.hv[(it + 1) & 1][e];
+            const T f2 = hcur[e];
+            inc = fmaT<T>((T)sc.ab3c, f2, fmaT<T>((T)sc.ab3b, f1, (T)sc.ab3a * f0));
+        }
+        hcur[e] = f0;
+        if constexpr (kSplit) {
+            double vd = (double)ve + (double)st.vlo[it & 1][e];
+            vd = fma(sc.dt, (double)inc, vd);
+            vd = fma(sc.dt, (double)drag, vd);
+            const T hi = (T)vd;
+            st.v[(it + 1) & 1][e] = hi;
+            st.vlo[(it + 1) & 1][e] = (T)(vd - (double)hi);
+            if (!finite_d(vd)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
+        } else {
+            T vn = fmaT<T>(inc, (T)sc.dt, ve);
+            vn = fmaT<T>((T)sc.dt, drag, vn);
+            st.v[(it + 1) & 1][e] = vn;
+            if (!finite_d((double)vn)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
+        }
+    }
+    const double bs = block_sum<kStepThreads>(pw, s_red);
+    if (threadIdx.x == 0) st.partial[blockIdx.x] = bs;
+}
+
+// ---------------------------------------------------------------------------
+// fused step, cell part
+// ---------------------------------------------------------------------------
+template <class T, bool kSplit>
+__global__ void __launch_bounds__(kStepThreads) k_cell_step(CellCoef<T> cc, State<T> st, StepConst sc, int offset, int n_partial)
+{
+    const long long it = *st.iter + offset;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Np = sc.Np;
+    const T* __restrict__ vn = st.v[(it + 1) & 1];
+    if (i < sc.N) {
+        T q = T(0);
+#pragma unroll
+        for (int k = 0; k < kCellFaces; k++) q = fmaT<T>(__ldg(&cc.hw[k * Np + i]), vn[__ldg(&cc.edge[k * Np + i])], q);
+        T* hcur = st.he[it & 1];
+        T inc = q;
+        if (sc.init_load || it > 1) {
+            const T f1 = st.he[(it + 1) & 1][i];
+            const T f2 = hcur[i];
+            inc = fmaT<T>((T)sc.ab3c, f2, fmaT<T>((T)sc.ab3b, f1, (T)sc.ab3a * q));
+        }
+        hcur[i] = q;
+        if constexpr (kSplit) {
+            double ed = (double)st.eta[i] + (double)st.etalo[i];
+            ed = fma(sc.dt, (double)inc, ed);
+            const T hi = (T)ed;
+            st.eta[i] = hi;
+            st.etalo[i] = (T)(ed - (double)hi);
+        } else {
+            st.eta[i] = fmaT<T>(inc, (T)sc.dt, st.eta[i]);
+        }
+    }
+    // dissipation of v^n (the state this step started from) = power of step n-1
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
+        const double s = fold_partials(st.partial, n_partial);
+        const long long k = it - 1 - *st.run_first;
+        if (threadIdx.x == 0 && k >= 0 && st.power) st.power[k] = s;
+    }
+}
+
+// Dissipation of the current v (after the last step of a run).
+template <class T>
+__global__ void __launch_bounds__(kStepThreads) k_power_partial(FaceCoef<T> fc, State<T> st, StepConst sc)
+{
+    __shared__ double s_red[kStepThreads / 32];
+    const long long it = *st.iter;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Ep = sc.Ep;
+    const T* __restrict__ vin = st.v[it & 1];
+    double pw = 0.0;
+    if (e < sc.E) {
+        T tsum = T(0);
+#pragma unroll
+        for (int k = 0; k < kTrisk; k++) tsum = fmaT<T>(__ldg(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
+        const T ve = vin[e];
+        pw = (double)(__ldg(&fc.diss[e]) * fmaT<T>(ve, ve, tsum * tsum));
+    }
+    const double bs = block_sum<kStepThreads>(pw, s_red);
+    if (threadIdx.x == 0) st.partial[blockIdx.x] = bs;
+}
+
+template <class T>
+__global__ void k_power_tail(State<T> st, int n_partial)
+{
+    const double s = fold_partials(st.partial, n_partial);
+    const long long k = *st.iter - 1 - *st.run_first;
+    if (threadIdx.x == 0 && k >= 0 && st.power) st.power[k] = s;
+}
+
+__global__ void k_bump_iter(long long* iter, int n)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *iter += n;
+}
+
+// ---------------------------------------------------------------------------
+// per-operator kernels (the reference's free functions)
+// ---------------------------------------------------------------------------
+// updateMomentum (linear): dvdt = -g G eta + C v
+__global__ void k_momentum(FaceCoef<double> fc, int E, int Ep, double* dvdt, const double* v, const double* eta)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < kTrisk; k++) t = fma(fc.w[k * Ep + e], v[fc.nbr[k * Ep + e]], t);
+    dvdt[e] = fma(fc.cor[e], t, fma(fc.gg0[e], eta[fc.n0[e]], fc.gg1[e] * eta[fc.n1[e]]));
+}
+
+// updateEta (linear): detadt = h D v
+__global__ void k_divergence(CellCoef<double> cc, int N, int Np, double* q, const double* v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < kCellFaces; k++) s = fma(cc.hw[k * Np + i], v[cc.edge[k * Np + i]], s);
+    q[i] = s;
+}
+
+// forcing (src/tidalPotentials.cpp:29-174), from the node trig tables
+// trig[10][Np]: cosLat sinLat cosLon sinLon cos2Lat sin2Lat cos2Lon sin2Lon cos^2Lat sin^2Lat
+__global__ void k_forcing(const double* trig, int N, int Np, double* U, int type, double t,
+                          double omega, double radius, double love, double ecc, double obl)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double sinM, cosM;
+    sincos(omega * t, &sinM, &cosM);
+    const double cosLat = trig[0 * Np + i], sinLat = trig[1 * Np + i], cosLon = trig[2 * Np + i];
+    const double sinLon = trig[3 * Np + i], sin2Lat = trig[5 * Np + i];
+    const double cos2Lon = trig[6 * Np + i], sin2Lon = trig[7 * Np + i], cosSq = trig[8 * Np + i], sinSq = trig[9 * Np + i];
+    const double w2r2 = omega * omega * (radius * radius);
+    double u = 0.0;
+    if (type == ODIS_POT_ECC || type == ODIS_POT_FULL) {
+        const double f = 0.75 * love * w2r2 * ecc;
+        u = f * ((1. - 3. * sinSq) * cosM + cosSq * (3. * cosM * cos2Lon + 4. * sinM * sin2Lon));
+    }
+    if (type == ODIS_POT_OBLIQ || type == ODIS_POT_FULL) {
+        const double f = -3. / 2. * love * w2r2 * obl;
+        u += f * cosM * sin2Lat * cosLon;
+    }
+    if (type == ODIS_POT_OBLIQ_WEST) {
+        const double f = 0.5 * love * w2r2 * obl;
+        u = 3 * f * sinLat * cosLat * (cosLon * cosM - sinLon * sinM);
+    }
+    U[i] = u;
+}
+
+// integrateAB3scalar with the reference's [num][3] history layout
+__global__ void k_ab3_ref(double* s, double* h, int iter, int num, double dt, int init_load)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num) return;
+    const double a = 23. / 12., b = -16. / 12., c = 5. / 12.;
+    double* hi = h + (size_t)i * 3;
+    if (iter > 1 || init_load) {
+        s[i] += (a * hi[0] + b * hi[1] + c * hi[2]) * dt;
+        hi[2] = hi[1];
+        hi[1] = hi[0];
+    } else if (iter == 0) {
+        s[i] += hi[0] * dt;
+        hi[2] = hi[0];
+    } else if (iter == 1) {
+        s[i] += hi[0] * dt;
+        hi[1] = hi[0];
+    }
+}
+
+// interpolateVelocity: uv[e] = n v_e + t v_t,e with t = (n_y, -n_x)
+__global__ void k_interp(FaceCoef<double> fc, const double* nrm, int E, int Ep, double* uv, const double* v)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < kTrisk; k++) t = fma(fc.w[k * Ep + e], v[fc.nbr[k * Ep + e]], t);
+    const double nx = nrm[e], ny = nrm[Ep + e];
+    uv[2 * e] = nx * v[e] + ny * t;
+    uv[2 * e + 1] = ny * v[e] + (-nx) * t;
+}
+
+// updateEnergy (LINEAR): e_i = alpha 1000 h |uv_i|^2, block partials of e_i * A_i
+__global__ void __launch_bounds__(kStepThreads) k_energy_partial(const double* area, int E, double coef, const double* uv,
+                                                                 double* e_out, double* partial)
+{
+    __shared__ double s_red[kStepThreads / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double x = 0.0;
+    if (i < E) {
+        const double u = uv[2 * i], w = uv[2 * i + 1];
+        const double ei = coef * (u * u + w * w);
+        if (e_out) e_out[i] = ei;
+        x = ei * area[i];
+    }
+    const double bs = block_sum<kStepThreads>(x, s_red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = bs;
+}
+
+__global__ void k_fold(const double* partial, int n, double divisor, double* out)
+{
+    const double s = fold_partials(partial, n);
+    if (threadIdx.x == 0) *out = s / divisor;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <class T, bool kSplit>
+void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
+{
+    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
+    k_edge_step<T, kSplit><<<eb, kStepThreads, 0, s>>>(fc, st, sc, offset);
+}
+
+template <class T, bool kSplit>
+void launch_cell(const CellCoef<T>& cc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
+{
+    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
+    const int cb = (sc.N + kStepThreads - 1) / kStepThreads;
+    k_cell_step<T, kSplit><<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset, eb);
+}
+
+template <class T, bool kSplit>
+void launch_step(const FaceCoef<T>& fc, const CellCoef<T>& cc, const State<T>& st, const StepConst& sc,
+                 int offset, cudaStream_t s)
+{
+    launch_edge<T, kSplit>(fc, st, sc, offset, s);
+    launch_cell<T, kSplit>(cc, st, sc, offset, s);
+}
+
+template <class T>
+void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, cudaStream_t s)
+{
+    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
+    k_power_partial<T><<<eb, kStepThreads, 0, s>>>(fc, st, sc);
+    k_power_tail<T><<<1, 32, 0, s>>>(st, eb);
+}
+
+void launch_bump(long long* iter, int n, cudaStream_t s) { k_bump_iter<<<1, 32, 0, s>>>(iter, n); }
+
+template void launch_edge<double, false>(const FaceCoef<double>&, const State<double>&, const StepConst&, int, cudaStream_t);
+template void launch_edge<float, true>(const FaceCoef<float>&, const State<float>&, const StepConst&, int, cudaStream_t);
+template void launch_cell<double, false>(const CellCoef<double>&, const State<double>&, const StepConst&, int, cudaStream_t);
+template void launch_cell<float, true>(const CellCoef<float>&, const State<float>&, const StepConst&, int, cudaStream_t);
+template void launch_step<double, false>(const FaceCoef<double>&, const CellCoef<double>&, const State<double>&,
+                                         const StepConst&, int, cudaStream_t);
+template void launch_step<float, true>(const FaceCoef<float>&, const CellCoef<float>&, const State<float>&,
+                                       const StepConst&, int, cudaStream_t);
+template void launch_power_tail<double>(const FaceCoef<double>&, const State<double>&, const StepConst&, cudaStream_t);
+template void launch_power_tail<float>(const FaceCoef<float>&, const State<float>&, const StepConst&, cudaStream_t);
+
+static inline int blocks(int n, int t) { return (n + t - 1) / t; }
+
+void launch_momentum(const FaceCoef<double>& fc, int E, int Ep, double* dvdt, const double* v, const double* eta, cudaStream_t s)
+{ k_momentum<<<blocks(E, 256), 256, 0, s>>>(fc, E, Ep, dvdt, v, eta); }
+
+void launch_divergence(const CellCoef<double>& cc, int N, int Np, double* q, const double* v, cudaStream_t s)
+{ k_divergence<<<blocks(N, 256), 256, 0, s>>>(cc, N, Np, q, v); }
+
+void launch_forcing(const double* trig, int N, int Np, double* U, int type, double t, double omega, double radius,
+                    double love, double ecc, double obl, cudaStream_t s)
+{ k_forcing<<<blocks(N, 256), 256, 0, s>>>(trig, N, Np, U, type, t, omega, radius, love, ecc, obl); }
+
+void launch_ab3_ref(double* x, double* h, int iter, int num, double dt, int init_load, cudaStream_t s)
+{ k_ab3_ref<<<blocks(num, 256), 256, 0, s>>>(x, h, iter, num, dt, init_load); }
+
+void launch_interp(const FaceCoef<double>& fc, const double* nrm, int E, int Ep, double* uv, const double* v, cudaStream_t s)
+{ k_interp<<<blocks(E, 256), 256, 0, s>>>(fc, nrm, E, Ep, uv, v); }
+
+int energy_blocks(int E) { return blocks(E, kStepThreads); }
+
+void launch_energy(const double* area, int E, double coef, double divisor, const double* uv, double* e_out,
+                   double* partial, double* out, cudaStream_t s)
+{
+    const int nb = energy_blocks(E);
+    k_energy_partial<<<nb, kStepThreads, 0, s>>>(area, E, coef, uv, e_out, partial);
+    k_fold<<<1, 32, 0, s>>>(partial, nb, divisor, out);
+}
+
+}  // namespace odis

@@ -1,0 +1,33 @@
+// Launchers of the LTE kernels (odis_kernels.cu), called by the C ABI.
+#pragma once
+
+#include "odis_device.cuh"
+
+namespace odis {
+
+constexpr int kStepThreads = 256;
+
+template <class T, bool kSplit>
+void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s);
+template <class T, bool kSplit>
+void launch_cell(const CellCoef<T>& cc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s);
+template <class T, bool kSplit>
+void launch_step(const FaceCoef<T>& fc, const CellCoef<T>& cc, const State<T>& st, const StepConst& sc,
+                 int offset, cudaStream_t s);
+template <class T>
+void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, cudaStream_t s);
+void launch_bump(long long* iter, int n, cudaStream_t s);
+
+void launch_momentum(const FaceCoef<double>& fc, int E, int Ep, double* dvdt, const double* v, const double* eta,
+                     cudaStream_t s);
+void launch_divergence(const CellCoef<double>& cc, int N, int Np, double* q, const double* v, cudaStream_t s);
+void launch_forcing(const double* trig, int N, int Np, double* U, int type, double t, double omega, double radius,
+                    double love, double ecc, double obl, cudaStream_t s);
+void launch_ab3_ref(double* x, double* h, int iter, int num, double dt, int init_load, cudaStream_t s);
+void launch_interp(const FaceCoef<double>& fc, const double* nrm, int E, int Ep, double* uv, const double* v,
+                   cudaStream_t s);
+int energy_blocks(int E);
+void launch_energy(const double* area, int E, double coef, double divisor, const double* uv, double* e_out,
+                   double* partial, double* out, cudaStream_t s);
+
+}  // namespace odis

@@ -1,0 +1,34 @@
+// Self-gravity / ocean-loading potential through spherical harmonics.
+//
+// The reference's form (commented-out pressureGradientSH,
+// src/spatialOperators.cpp:387-462, with the basis of CalcLegendreFuncs,
+// src/mesh.cpp:2154-2258): eta is expanded to degree L in 4pi-normalised real
+// harmonics with the Condon-Shortley phase (SHTOOLS PlmBar csphase=-1,
+// src/legendre.f95:20) by least squares over the cells (SHExpandLSQ,
+// src/extractSHCoeffGG.f95:17), each degree l >= 2 is scaled by a factor f_l
+// and the field is synthesised back and added to the tidal potential times g.
+//
+// Per step:  t = Y^T eta  (K sums over the cells),  c = F (Y^T Y)^-1 t  (K x K),
+//            usg = Y c    (N dot products of length K);
+// the face kernel then adds G (g usg) to the forcing gradient.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "odis_internal.h"
+
+namespace odis {
+
+struct ShLoading;
+
+int sh_create(ShLoading** out, const Mesh& m, int lmax, const double* factors, int precision, int Np);
+void sh_destroy(ShLoading* s);
+// usg buffer ([Np], FP64 or FP32 according to the precision)
+const double* sh_usg64(ShLoading* s);
+const float* sh_usg32(ShLoading* s);
+// enqueue analysis + synthesis of the current eta (double* or float*)
+void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t stream);
+// host helpers for checks: real SH basis at the nodes, [N][K]
+void sh_basis_host(const Mesh& m, int lmax, std::vector<double>& Y);
+
+}  // namespace odis

@@ -1,0 +1,177 @@
+/*
+ * odis_gpu.h -- C ABI of libodis_gpu.so, the GB300 (sm_103a) implementation of
+ * the GeodesicODIS linear Laplace Tidal Equation timestep.
+ *
+ * Plain pointers and sizes only.  Every call returns an odis_status; nothing
+ * throws across the boundary.  One context per host thread; each context owns
+ * one CUDA stream (or uses the one given by odis_set_stream).
+ *
+ * Reference interfaces replaced (hamishHay/GeodesicODIS v1.11):
+ *   odis_update_momentum   <- updateMomentum      include/updateMomentum.h:8,   src/updateMomentum.cpp:16-46
+ *   odis_update_eta        <- updateEta           include/updateEta.h:8,        src/updateEta.cpp:7-44
+ *   odis_forcing           <- forcing             include/tidalPotentials.h:16, src/tidalPotentials.cpp:29-334
+ *   odis_ab3               <- integrateAB3scalar  include/temporalOperators.h:14, src/temporalOperators.cpp:17-68
+ *   odis_interpolate_velocity <- interpolateVelocity include/interpolation.h:12, src/interpolation.cpp:26-62
+ *   odis_update_energy     <- updateEnergy        include/energy.h:10,          src/energy.cpp:13-61
+ *   odis_run_steps         <- the body of ab3Explicit's time loop, src/timeIntegrator.cpp:205-313
+ *   odis_get_state / odis_set_state <- writeInitialConditions / loadInitialConditions,
+ *                                      src/initialConditions.cpp:19,209
+ *   odis_mesh_*            <- Mesh::Mesh + ReadMeshFile + AssignFaces + Calc*OperatorCoeffs,
+ *                             src/mesh.cpp:32-197, :508-1154, :2808-3288, :4016-4089
+ *   odis_params_from_input <- Globals::Globals + ReadGlobals + CalcMaxTimeStep,
+ *                             src/globals.cpp:35-323,325-477; src/mesh.cpp:1566-1621
+ */
+#ifndef ODIS_GPU_H
+#define ODIS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int odis_status;
+#define ODIS_OK 0
+#define ODIS_ERR_ARG 1          /* bad argument or unsupported option */
+#define ODIS_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define ODIS_ERR_OOB 3          /* index outside the mesh seen by a kernel */
+#define ODIS_ERR_NONFINITE 4    /* NaN/Inf appeared in the state */
+#define ODIS_ERR_TIMEOUT 5      /* a bounded device wait ran out */
+#define ODIS_ERR_IO 6           /* file could not be read/written/parsed */
+#define ODIS_ERR_MESH 7         /* inconsistent grid */
+#define ODIS_ERR_NOMEM 8        /* allocation failed */
+
+/* forcing types (the reference's `potential` keys) */
+#define ODIS_POT_NONE 0
+#define ODIS_POT_ECC 1
+#define ODIS_POT_OBLIQ 2
+#define ODIS_POT_OBLIQ_WEST 3
+#define ODIS_POT_FULL 4
+
+/* arithmetic of the state and stencils */
+#define ODIS_FP64 0             /* everything in FP64 (the reference's method) */
+#define ODIS_FP32 1             /* FP32 state and stencils; FP64 time accumulation and reductions */
+
+/* where the pointers passed to per-operator calls live */
+#define ODIS_MEM_HOST 0
+#define ODIS_MEM_DEVICE 1
+
+typedef struct odis_mesh odis_mesh;
+typedef struct odis_ctx odis_ctx;
+
+/* Physical and numerical parameters, in the units of input.in after the
+ * reference's own post-processing (obliquity in radians, angvel after the
+ * period has been rounded, dt after snapping).  odis_params_from_input fills
+ * one from an input.in file. */
+typedef struct odis_params {
+    double radius;          /* m */
+    double g;               /* m s^-2 */
+    double angvel;          /* rad s^-1 */
+    double h;               /* ocean thickness, m */
+    double alpha;           /* linear drag, s^-1 */
+    double ecc;             /* eccentricity */
+    double obliq;           /* obliquity, rad */
+    double love_reduct;     /* 1 + k2 - h2 */
+    double dt;              /* s */
+    int potential;          /* ODIS_POT_* */
+    int init_load;          /* 1: AB3 from the first step (initial conditions LOAD) */
+    int precision;          /* ODIS_FP64 or ODIS_FP32 */
+    int sh_lmax;            /* 0: no self-gravity/loading; else maximum degree (<= 64) */
+    const double* sh_factors; /* [sh_lmax+1] per-degree factors (0 and 1 unused); may be NULL if sh_lmax == 0 */
+} odis_params;
+
+/* Parsed input.in (src/globals.cpp:58-203 keys).  Strings are fixed-size. */
+typedef struct odis_input {
+    odis_params params;
+    double period;           /* s, after rounding */
+    double end_time;         /* orbits */
+    int steps_per_orbit;     /* totalIter after CalcMaxTimeStep */
+    int grid_level;          /* "geodesic grid level" as written in the file */
+    int output_time;         /* dumps per orbit */
+    int sh_degree;           /* "sh degree" */
+    int advection;           /* 1 if advection true (unsupported by this library) */
+    int fric_linear;         /* 1 LINEAR, 0 QUADRATIC */
+    int surface_free;        /* 1 FREE */
+    int init_kind;           /* 0 NONE, 1 LOAD, 2 ANALYTICAL */
+    int out_flags;           /* bit0 velocity, 1 cartesian, 2 displacement, 3 dissipation,
+                                4 dissipation avg, 5 kinetic avg, 6 dummy1 */
+    char potential_name[32];
+    char friction_name[32];
+    char surface_name[32];
+    char solver_name[32];
+    char init_name[32];
+} odis_input;
+
+/* ---- grid -------------------------------------------------------------- */
+/* Icosahedral grid at level n (10*4^n+2 cells), written in the reference's
+ * grid-file format. */
+odis_status odis_grid_generate_file(int level, const char* path);
+
+/* ---- mesh (host side geometry, operators and device-ready layout) ------ */
+odis_status odis_mesh_from_file(const char* path, double radius, odis_mesh** out);
+odis_status odis_mesh_generate(int level, double radius, odis_mesh** out);
+/* node_sph [N][2] and cent_sph [N][6][2] in radians, friends [N][6] (-1 in slot 5 for pentagons) */
+odis_status odis_mesh_from_arrays(int n_nodes, const double* node_sph, const int* friends,
+                                  const double* cent_sph, double radius, odis_mesh** out);
+odis_status odis_mesh_sizes(const odis_mesh* m, int* n_cells, int* n_edges, int* n_vertices);
+/* Geometry the operators are built from (for checks): which = 0 face_len,
+ * 1 face_node_dist, 2 face_area, 3 control-volume area [N], 4 face-centre lat,
+ * 5 face-centre lon, 6 map factor at node 0, 7 map factor at node 1,
+ * 8/9 face normal (x, y), 10/11 intercept (lat, lon). */
+odis_status odis_mesh_field(const odis_mesh* m, int which, double* out);
+/* face_nodes [E][2], faces [N][6], node_face_dir [N][6], interp_friends [E][10],
+ * interp_w [E][10], interp_n [E]; any may be NULL */
+odis_status odis_mesh_topology(const odis_mesh* m, int* face_nodes, int* faces, int* node_face_dir,
+                               int* interp_friends, double* interp_w, int* interp_n);
+void odis_mesh_destroy(odis_mesh* m);
+
+/* ---- parameters -------------------------------------------------------- */
+/* Period rounding (src/globals.cpp:209-214) and dt snapping (src/mesh.cpp:1566-1621). */
+odis_status odis_derive_time(double angvel_in, double dt_target, double* angvel, double* period,
+                             double* dt, int* steps_per_orbit);
+odis_status odis_params_from_input(const char* input_in_path, odis_input* out);
+
+/* ---- context ----------------------------------------------------------- */
+odis_status odis_create(const odis_params* p, const odis_mesh* m, odis_ctx** out);
+void odis_destroy(odis_ctx* c);
+/* Use the caller's stream (a cudaStream_t) instead of the context's own. */
+odis_status odis_set_stream(odis_ctx* c, void* cuda_stream);
+odis_status odis_synchronize(odis_ctx* c);
+/* Last status recorded by a kernel's own checks (OOB / NONFINITE / TIMEOUT), 0 if none; clears it. */
+odis_status odis_device_status(odis_ctx* c);
+
+/* ---- per-operator calls (mirror the reference's free functions) -------- */
+/* dvdt[E] = -g*G*eta + C*v */
+odis_status odis_update_momentum(odis_ctx* c, double* dvdt, const double* v, const double* eta, int mem);
+/* detadt[N] = h*D*v */
+odis_status odis_update_eta(odis_ctx* c, double* detadt, const double* v, int mem);
+/* U[N] = tidal potential of type `type` at time t (s) */
+odis_status odis_forcing(odis_ctx* c, double* U, int type, double t, int mem);
+/* integrateAB3scalar on s[num] with history hist[num][3] at iteration iter */
+odis_status odis_ab3(odis_ctx* c, double* s, double* hist, int iter, int num, int mem);
+/* uv[E][2] = (east, north) velocity at faces from normal velocity v[E] */
+odis_status odis_interpolate_velocity(odis_ctx* c, double* uv, const double* v, int mem);
+/* e[E] (nullable) per-face dissipation and *avg area-mean (W m^-2) from uv[E][2] */
+odis_status odis_update_energy(odis_ctx* c, double* avg, double* e, const double* uv, int mem);
+
+/* ---- the fused time loop ----------------------------------------------- */
+/* Advance n steps.  power (nullable, ODIS_MEM_HOST or ODIS_MEM_DEVICE per
+ * `mem`) receives the dissipated power (W m^-2) after each step. */
+odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem);
+/* State in the reference's layout: v[E], eta[N], dvdt[E][3], detadt[N][3]
+ * (history slot 0 = latest tendency).  iter = steps taken. Host pointers. */
+odis_status odis_get_state(odis_ctx* c, int* iter, double* v, double* eta, double* dvdt, double* detadt);
+odis_status odis_set_state(odis_ctx* c, int iter, const double* v, const double* eta,
+                           const double* dvdt, const double* detadt);
+
+/* ---- measurement ------------------------------------------------------- */
+/* Number of this library's kernels launched so far by the context. */
+odis_status odis_launch_count(odis_ctx* c, long long* n);
+/* Average device time (ms) per launch of each kernel group, each launched
+ * `reps` times back to back in a CUDA graph on the context stream:
+ * ms[0] face step kernel, ms[1] cell step kernel, ms[2] self-gravity
+ * analysis+solve+synthesis (0 if off).  Leaves the state undefined. */
+odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ODIS_GPU_H */

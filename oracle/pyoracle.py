@@ -1,0 +1,217 @@
+"""ctypes view of the FP64 CPU oracle (odis_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
+bench.py's CPU baseline / reference arm.  The product library never loads it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libodis_oracle.so"
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_V = C.c_void_p
+
+ECC, OBLIQ, OBLIQ_WEST, FULL, FULL2, NONE = 1, 2, 3, 4, 5, 0
+
+
+class OrcParams(C.Structure):
+    _fields_ = [("radius", C.c_double), ("g", C.c_double), ("angvel", C.c_double), ("h", C.c_double),
+                ("alpha", C.c_double), ("ecc", C.c_double), ("obliq", C.c_double), ("love_reduct", C.c_double),
+                ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int)]
+
+
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = C.CDLL(str(LIB))
+        sig = {
+            "orc_mesh_load": ([C.c_char_p, C.c_double, _I], _V),
+            "orc_mesh_from_arrays": ([C.c_int, _D, _I, _D, C.c_double, _I], _V),
+            "orc_mesh_free": ([_V], None),
+            "orc_mesh_sizes": ([_V, _I, _I, _I], None),
+            "orc_mesh_get_field": ([_V, C.c_int, _D], C.c_int),
+            "orc_mesh_get_topology": ([_V, _I, _I, _I, _I, _D, _I], None),
+            "orc_mesh_get_csr": ([_V, C.c_int, _I, _I, _D], C.c_int),
+            "orc_derive_time": ([C.c_double, C.c_double, _D, _D, _D, _I], None),
+            "orc_solver_create": ([_V, C.POINTER(OrcParams)], _V),
+            "orc_solver_free": ([_V], None),
+            "orc_solver_set_loading": ([_V, C.c_int, _D], C.c_int),
+            "orc_update_momentum": ([_V, _D, _D, _D], None),
+            "orc_update_eta": ([_V, _D, _D], None),
+            "orc_forcing": ([_V, _D, C.c_int, C.c_double], None),
+            "orc_ab3": ([C.c_double, _D, _D, C.c_int, C.c_int, C.c_int], None),
+            "orc_interpolate_velocity": ([_V, _D, _D], None),
+            "orc_update_energy": ([_V, C.c_double, C.c_double, _D, _D], C.c_double),
+            "orc_plmbar": ([C.c_int, C.c_double, _D], None),
+            "orc_sh_basis": ([_V, C.c_int, _D], None),
+            "orc_sh_analysis": ([_V, _D, _D], None),
+            "orc_sim_create": ([_V], _V),
+            "orc_sim_free": ([_V], None),
+            "orc_sim_set_state": ([_V, C.c_int, _D, _D, _D, _D], None),
+            "orc_sim_get_state": ([_V, _I, _D, _D, _D, _D], None),
+            "orc_sim_step": ([_V], C.c_double),
+            "orc_sim_run": ([_V, C.c_int, _D], C.c_int),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(_D)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_I)
+
+
+def derive_time(angvel_in, dt_target):
+    a, p, d, n = C.c_double(), C.c_double(), C.c_double(), C.c_int()
+    lib().orc_derive_time(angvel_in, dt_target, C.byref(a), C.byref(p), C.byref(d), C.byref(n))
+    return a.value, p.value, d.value, n.value
+
+
+class OracleMesh:
+    def __init__(self, path: str | os.PathLike, radius: float):
+        st = C.c_int()
+        h = lib().orc_mesh_load(os.fsencode(str(path)), radius, C.byref(st))
+        if not h:
+            raise RuntimeError(f"oracle could not load {path}: status {st.value}")
+        self._h = C.c_void_p(h)
+        n, e, v = C.c_int(), C.c_int(), C.c_int()
+        lib().orc_mesh_sizes(self._h, C.byref(n), C.byref(e), C.byref(v))
+        self.n_cells, self.n_edges, self.n_vertices = n.value, e.value, v.value
+
+    def field(self, which: int) -> np.ndarray:
+        out = np.zeros(self.n_cells if which == 3 else self.n_edges)
+        lib().orc_mesh_get_field(self._h, which, _dp(out))
+        return out
+
+    def topology(self):
+        E, N = self.n_edges, self.n_cells
+        fn = np.zeros((E, 2), np.int32)
+        faces = np.zeros((N, 6), np.int32)
+        nfd = np.zeros((N, 6), np.int32)
+        ifr = np.zeros((E, 10), np.int32)
+        iw = np.zeros((E, 10))
+        inn = np.zeros(E, np.int32)
+        lib().orc_mesh_get_topology(self._h, _ip(fn), _ip(faces), _ip(nfd), _ip(ifr), _dp(iw), _ip(inn))
+        return dict(face_nodes=fn, faces=faces, node_face_dir=nfd, interp_friends=ifr, interp_w=iw, interp_n=inn)
+
+    def csr(self, op: int):
+        """op 0 gradient (E x N), 1 divergence (N x E), 2 Coriolis with Omega = 1 (E x E)."""
+        rows = self.n_edges if op != 1 else self.n_cells
+        nnz = lib().orc_mesh_get_csr(self._h, op, None, None, None)
+        rp = np.zeros(rows + 1, np.int32)
+        col = np.zeros(nnz, np.int32)
+        val = np.zeros(nnz)
+        lib().orc_mesh_get_csr(self._h, op, _ip(rp), _ip(col), _dp(val))
+        return rp, col, val
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _lib is not None:
+            _lib.orc_mesh_free(self._h)
+            self._h = C.c_void_p()
+
+
+class OracleSolver:
+    """FP64 restatement of the reference step (see odis_oracle.c)."""
+
+    def __init__(self, mesh: OracleMesh, *, radius, g, angvel, h, alpha, ecc=0.0, obliq=0.0, love_reduct=1.0,
+                 dt, potential=ECC, init_load=0, sh_lmax=0, sh_factors=None):
+        self.mesh = mesh
+        self.p = OrcParams(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load)
+        self._s = C.c_void_p(lib().orc_solver_create(mesh._h, C.byref(self.p)))
+        if sh_lmax:
+            f = np.ascontiguousarray(sh_factors, np.float64)
+            st = lib().orc_solver_set_loading(self._s, int(sh_lmax), _dp(f))
+            if st != 0:
+                raise RuntimeError(f"oracle SH setup failed: {st}")
+        self._x = C.c_void_p(lib().orc_sim_create(self._s))
+        self.E, self.N = mesh.n_edges, mesh.n_cells
+
+    def updateMomentum(self, v, eta):
+        out = np.zeros(self.E)
+        lib().orc_update_momentum(self._s, _dp(out), _dp(np.ascontiguousarray(v, np.float64)),
+                                  _dp(np.ascontiguousarray(eta, np.float64)))
+        return out
+
+    def updateEta(self, v):
+        out = np.zeros(self.N)
+        lib().orc_update_eta(self._s, _dp(out), _dp(np.ascontiguousarray(v, np.float64)))
+        return out
+
+    def forcing(self, type_, t):
+        out = np.zeros(self.N)
+        lib().orc_forcing(self._s, _dp(out), int(type_), float(t))
+        return out
+
+    def integrateAB3scalar(self, s, ds_dt, it):
+        lib().orc_ab3(self.p.dt, _dp(s), _dp(ds_dt), int(it), int(s.shape[0]), int(self.p.init_load))
+
+    def interpolateVelocity(self, v):
+        out = np.zeros((self.E, 2))
+        lib().orc_interpolate_velocity(self.mesh._h, _dp(out), _dp(np.ascontiguousarray(v, np.float64)))
+        return out
+
+    def updateEnergy(self, uv):
+        e = np.zeros(self.E)
+        avg = lib().orc_update_energy(self.mesh._h, self.p.alpha, self.p.h, _dp(e),
+                                      _dp(np.ascontiguousarray(uv, np.float64)))
+        return avg, e
+
+    def sh_analysis(self, eta):
+        raise NotImplementedError
+
+    def run(self, nsteps):
+        out = np.zeros(nsteps)
+        lib().orc_sim_run(self._x, int(nsteps), _dp(out))
+        return out
+
+    def get_state(self):
+        it = C.c_int()
+        v, eta = np.zeros(self.E), np.zeros(self.N)
+        dv, de = np.zeros((self.E, 3)), np.zeros((self.N, 3))
+        lib().orc_sim_get_state(self._x, C.byref(it), _dp(v), _dp(eta), _dp(dv), _dp(de))
+        return it.value, v, eta, dv, de
+
+    def set_state(self, it, v, eta, dvdt, detadt):
+        a = [np.ascontiguousarray(x, np.float64) for x in (v, eta, dvdt, detadt)]
+        lib().orc_sim_set_state(self._x, int(it), *[_dp(x) for x in a])
+
+    def __del__(self):
+        if _lib is None:
+            return
+        if getattr(self, "_x", None) and self._x.value:
+            _lib.orc_sim_free(self._x)
+            self._x = C.c_void_p()
+        if getattr(self, "_s", None) and self._s.value:
+            _lib.orc_solver_free(self._s)
+            self._s = C.c_void_p()
+
+
+def plmbar(L: int, z: float) -> np.ndarray:
+    out = np.zeros((L + 1) * (L + 2) // 2)
+    lib().orc_plmbar(int(L), float(z), _dp(out))
+    return out

@@ -1,0 +1,72 @@
+"""Shared fixtures.  GPU tests are marked `gpu`; everything else runs on CPU."""
+from __future__ import annotations
+
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+
+REF_INPUT = Path("/root/reference/input_files")   # present only where the reference is mounted
+
+# Enceladus-like body of the benchmark configurations
+RADIUS = 252.1e3
+GRAV = 0.113
+ANGVEL_IN = 5.307e-5
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libodis_gpu.so")
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Build the product library and the oracle once per session (idempotent)."""
+    from geodesicodis_gb300 import build_ext
+    from oracle import pyoracle
+    build_ext.build()
+    pyoracle.build()
+    return True
+
+
+@pytest.fixture(scope="session")
+def grid_dir(tmp_path_factory, built):
+    import geodesicodis_gb300 as g
+    d = tmp_path_factory.mktemp("grids")
+    for lvl in range(0, 6):
+        g.generate_grid_file(lvl, d / f"grid_{lvl}.txt")
+    return d
+
+
+def ref_grid(level_baseline: int) -> Path:
+    """The reference's shipped grid with 10*4^level+2 cells (its file is named one level higher)."""
+    return REF_INPUT / f"grid_l{level_baseline + 1}.txt"
+
+
+def rel_err(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    s = max(np.max(np.abs(b)), 1e-300)
+    return float(np.max(np.abs(a - b)) / s)
+
+
+def config0_params(**over):
+    """configs[0]: h = 10 km, alpha = 1e-5, ECC e = 0.0047, 2000 steps/orbit."""
+    from oracle import pyoracle as O
+    angvel, P, dt, n = O.derive_time(ANGVEL_IN, 59.197)
+    p = dict(radius=RADIUS, g=GRAV, angvel=angvel, h=1e4, alpha=1e-5, ecc=0.0047, obliq=0.0, love_reduct=1.0,
+             dt=dt, potential=1, init_load=0)
+    p.update(over)
+    return p
+
+
+def gpu_available() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False

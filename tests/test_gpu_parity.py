@@ -1,0 +1,159 @@
+"""GPU parity: libodis_gpu.so (sm_103a kernels, through the C ABI) against the FP64 oracle.
+
+Tolerances:
+  * per-operator calls (FP64): 1e-12 relative to the field's max-abs
+  * fused FP64 time loop after N steps: eta, v and dissipated power within 1e-10
+    relative (max-abs normalised), as the reference parity target states
+  * FP32-state variant: dissipated power within 1e-4 relative of the FP64 oracle
+"""
+import numpy as np
+import pytest
+
+from conftest import RADIUS, config0_params, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(path, precision=0, **over):
+    import geodesicodis_gb300 as g
+    from oracle import pyoracle as O
+    p = config0_params(**over)
+    om = O.OracleMesh(path, RADIUS)
+    orc = O.OracleSolver(om, **p)
+    gm = g.Mesh.from_file(path, RADIUS)
+    gp = g.make_params(precision=precision, **p)
+    return orc, g.Solver(gp, gm)
+
+
+@pytest.fixture(scope="module")
+def level3(grid_dir):
+    return _pair(grid_dir / "grid_3.txt")
+
+
+def test_update_momentum(level3):
+    orc, gpu = level3
+    rng = np.random.default_rng(1)
+    v, eta = rng.standard_normal(orc.E) * 0.1, rng.standard_normal(orc.N)
+    assert rel_err(gpu.updateMomentum(v, eta), orc.updateMomentum(v, eta)) < 1e-12
+
+
+def test_update_eta(level3):
+    orc, gpu = level3
+    v = np.random.default_rng(2).standard_normal(orc.E)
+    assert rel_err(gpu.updateEta(v), orc.updateEta(v)) < 1e-12
+
+
+@pytest.mark.parametrize("ptype", [1, 2, 3, 4])
+def test_forcing(level3, ptype):
+    orc, gpu = level3
+    for t in (0.0, 1234.5, 7.7e5):
+        assert rel_err(gpu.forcing(ptype, t), orc.forcing(ptype, t)) < 1e-12
+
+
+@pytest.mark.parametrize("it", [0, 1, 2, 7])
+def test_ab3(level3, it):
+    orc, gpu = level3
+    rng = np.random.default_rng(3 + it)
+    s, h = rng.standard_normal(500), rng.standard_normal((500, 3))
+    s2, h2 = s.copy(), h.copy()
+    orc.integrateAB3scalar(s, h, it)
+    gpu.integrateAB3scalar(s2, h2, it)
+    assert rel_err(s2, s) < 1e-14 and rel_err(h2, h) == 0.0
+
+
+def test_interpolate_and_energy(level3):
+    orc, gpu = level3
+    v = np.random.default_rng(4).standard_normal(orc.E)
+    uv_o, uv_g = orc.interpolateVelocity(v), gpu.interpolateVelocity(v)
+    assert rel_err(uv_g, uv_o) < 1e-12
+    a_o, e_o = orc.updateEnergy(uv_o)
+    a_g, e_g = gpu.updateEnergy(uv_o)
+    assert rel_err(e_g, e_o) < 1e-14
+    assert abs(a_g - a_o) / abs(a_o) < 1e-12
+
+
+@pytest.mark.parametrize("level,steps", [(2, 700), (3, 2500)])
+def test_fused_fp64_parity(grid_dir, level, steps):
+    orc, gpu = _pair(grid_dir / f"grid_{level}.txt")
+    po = orc.run(steps)
+    pg = gpu.run(steps)
+    _, vo, eo, dvo, deo = orc.get_state()
+    it, vg, eg, dvg, deg = gpu.get_state()
+    assert it == steps
+    assert rel_err(eg, eo) < 1e-10
+    assert rel_err(vg, vo) < 1e-10
+    assert rel_err(pg, po) < 1e-10
+    assert rel_err(dvg, dvo) < 1e-10 and rel_err(deg, deo) < 1e-10
+
+
+def test_config0_full_run_parity(grid_dir):
+    """configs[0]: level 4 (2562 cells), ECC e=0.0047, h=10 km, alpha=1e-5, 10 orbits x 2000 steps."""
+    orc, gpu = _pair(grid_dir / "grid_4.txt")
+    po = orc.run(20000)
+    pg = gpu.run(20000)
+    _, vo, eo, _, _ = orc.get_state()
+    _, vg, eg, _, _ = gpu.get_state()
+    assert rel_err(eg, eo) < 1e-10
+    assert rel_err(vg, vo) < 1e-10
+    assert rel_err(pg, po) < 1e-10
+    assert po[-1] > 0
+
+
+def test_fp32_variant_power(grid_dir):
+    """FP32 state and stencils, FP64 time accumulation and reductions: power within 1e-4 of FP64."""
+    orc, gpu = _pair(grid_dir / "grid_3.txt", precision=1)
+    po = orc.run(4000)
+    pg = gpu.run(4000)
+    _, vo, eo, _, _ = orc.get_state()
+    _, vg, eg, _, _ = gpu.get_state()
+    assert rel_err(pg[-2000:], po[-2000:]) < 1e-4
+    assert abs(pg[-2000:].mean() / po[-2000:].mean() - 1) < 1e-4
+    assert rel_err(eg, eo) < 1e-3 and rel_err(vg, vo) < 1e-3
+
+
+def test_graph_and_eager_paths_agree(grid_dir):
+    """Chunks replayed from the CUDA graph and eager launches give identical bits; runs are deterministic."""
+    _, a = _pair(grid_dir / "grid_2.txt")
+    _, b = _pair(grid_dir / "grid_2.txt")
+    pa = np.concatenate([a.run(64 * 3 + 5)])
+    pb = np.concatenate([b.run(10), b.run(63), b.run(64 * 2 + 3 - 1), b.run(0 + 1)])
+    assert pa.shape == pb.shape
+    np.testing.assert_array_equal(pa, pb)
+    np.testing.assert_array_equal(a.get_state()[1], b.get_state()[1])
+
+
+def test_state_round_trip_and_load_mode(grid_dir):
+    """get/set in the reference's [n][3] history layout; LOAD runs AB3 from the first step."""
+    orc, gpu = _pair(grid_dir / "grid_2.txt")
+    orc.run(37)
+    gpu.run(37)
+    st = gpu.get_state()
+    orc_l, gpu_l = _pair(grid_dir / "grid_2.txt", init_load=1)
+    _, v, eta, dv, de = orc.get_state()
+    orc_l.set_state(0, v, eta, dv, de)
+    gpu_l.set_state(0, *st[1:])
+    assert rel_err(gpu_l.get_state()[1], v) < 1e-10
+    po, pg = orc_l.run(300), gpu_l.run(300)
+    assert rel_err(pg, po) < 1e-10
+    assert rel_err(gpu_l.get_state()[2], orc_l.get_state()[2]) < 1e-10
+    # round trip of a mid-run state at odd and even step counts
+    for k in (1, 2, 5):
+        orc2, gpu2 = _pair(grid_dir / "grid_2.txt")
+        orc2.run(k); gpu2.run(k)
+        s = gpu2.get_state()
+        gpu3 = _pair(grid_dir / "grid_2.txt")[1]
+        gpu3.set_state(*s)
+        a, b = gpu2.run(50), gpu3.run(50)
+        np.testing.assert_array_equal(a, b)
+        assert rel_err(b, orc2.run(50)) < 1e-10
+
+
+def test_nonfinite_state_is_reported(grid_dir):
+    import geodesicodis_gb300 as g
+    _, gpu = _pair(grid_dir / "grid_1.txt")
+    it, v, eta, dv, de = gpu.get_state()
+    v[3] = np.nan
+    gpu.set_state(0, v, eta, dv, de)
+    with pytest.raises(g.OdisError) as ei:
+        gpu.run(3)
+    assert ei.value.code == g.ERR_NONFINITE

@@ -1,0 +1,76 @@
+"""Icosahedral grid generator: topology, orientation and vertex placement."""
+import numpy as np
+import pytest
+
+from conftest import REF_INPUT, ref_grid
+
+
+def read_grid(path):
+    lat, lon, fr, cent = [], [], [], []
+    with open(path) as f:
+        next(f)
+        for line in f:
+            a, b = line.split("{", 1)
+            p = a.split()
+            lat.append(float(p[1])); lon.append(float(p[2]))
+            f_part, c_part = b.split("}", 1)
+            fr.append([int(x) for x in f_part.split(",")])
+            nums = c_part.replace("(", " ").replace(")", " ").replace(",", " ").replace("{", " ").replace("}", " ").split()
+            cent.append([float(x) for x in nums])
+    rc = np.pi / 180
+    return np.array(lat) * rc, np.array(lon) * rc, np.array(fr), np.array(cent).reshape(-1, 6, 2) * rc
+
+
+def xyz(lat, lon):
+    return np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], -1)
+
+
+@pytest.mark.parametrize("level", [0, 1, 2, 3, 4, 5])
+def test_counts_and_symmetry(grid_dir, level):
+    lat, lon, fr, cent = read_grid(grid_dir / f"grid_{level}.txt")
+    N = 10 * 4 ** level + 2
+    assert len(lat) == N
+    pent = fr[:, 5] < 0
+    assert pent.sum() == 12
+    for i in range(N):
+        k = 5 if pent[i] else 6
+        for j in range(k):
+            f = fr[i, j]
+            assert 0 <= f < N and f != i
+            assert i in fr[f]                      # friendship is symmetric
+    edges = (6 * (N - 12) + 60) // 2
+    assert edges == 3 * N - 6
+
+
+@pytest.mark.parametrize("level", [1, 3, 5])
+def test_clockwise_and_circumcentres(grid_dir, level):
+    lat, lon, fr, cent = read_grid(grid_dir / f"grid_{level}.txt")
+    P = xyz(lat, lon)
+    for i in range(0, len(lat), max(1, len(lat) // 400)):
+        k = 5 if fr[i, 5] < 0 else 6
+        for j in range(k):
+            a, b = P[fr[i, j]], P[fr[i, (j + 1) % k]]
+            # clockwise seen from outside: (a - p) x (b - p) points inwards
+            assert np.dot(np.cross(a - P[i], b - P[i]), P[i]) < 0
+            c = xyz(cent[i, j, 0], cent[i, j, 1])
+            d = [np.arccos(np.clip(np.dot(c, q), -1, 1)) for q in (P[i], a, b)]
+            assert max(d) - min(d) < 1e-12
+
+
+@pytest.mark.skipif(not REF_INPUT.exists(), reason="reference grids not mounted")
+@pytest.mark.parametrize("level", [2, 3, 4])
+def test_same_layout_as_reference_files(grid_dir, level):
+    """Generated and shipped grids agree in size, pentagon count and orientation convention."""
+    lat, lon, fr, cent = read_grid(ref_grid(level))
+    lat2, lon2, fr2, cent2 = read_grid(grid_dir / f"grid_{level}.txt")
+    assert len(lat) == len(lat2)
+    assert (fr[:, 5] < 0).sum() == (fr2[:, 5] < 0).sum() == 12
+    P = xyz(lat, lon)
+    i = 100
+    k = 6 if fr[i, 5] >= 0 else 5
+    assert np.dot(np.cross(P[fr[i, 0]] - P[i], P[fr[i, 1]] - P[i]), P[i]) < 0
+    # cell sizes of the two grids have the same mean (equal-count grids on the unit sphere)
+    def mean_spacing(lat, lon, fr):
+        P = xyz(lat, lon)
+        return np.mean([np.arccos(np.clip(np.dot(P[i], P[fr[i, 0]]), -1, 1)) for i in range(len(lat))])
+    assert abs(mean_spacing(lat, lon, fr) / mean_spacing(lat2, lon2, fr2) - 1) < 0.05

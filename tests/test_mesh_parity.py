@@ -1,0 +1,49 @@
+"""The product's host-side mesh builder (libodis_gpu.so, no GPU needed) against the oracle:
+geometry and TRiSK weights must be bit-identical, since both follow the reference's formulas."""
+import numpy as np
+import pytest
+
+from conftest import RADIUS, REF_INPUT, ref_grid
+
+
+def _compare(path):
+    import geodesicodis_gb300 as g
+    from oracle import pyoracle as O
+    om = O.OracleMesh(path, RADIUS)
+    pm = g.Mesh.from_file(path, RADIUS)
+    assert (om.n_cells, om.n_edges, om.n_vertices) == (pm.n_cells, pm.n_edges, pm.n_vertices)
+    for w in range(12):
+        np.testing.assert_array_equal(om.field(w), pm.field(w), err_msg=f"field {w}")
+    ta, tb = om.topology(), pm.topology()
+    for k in ta:
+        np.testing.assert_array_equal(ta[k], tb[k], err_msg=k)
+    return om, pm
+
+
+@pytest.mark.parametrize("level", [0, 1, 2, 3, 4])
+def test_generated_grids(grid_dir, level):
+    _compare(grid_dir / f"grid_{level}.txt")
+
+
+@pytest.mark.skipif(not REF_INPUT.exists(), reason="reference grids not mounted")
+@pytest.mark.parametrize("level", [2, 3, 4, 5])
+def test_reference_grids(built, level):
+    _compare(ref_grid(level))
+
+
+def test_generate_in_memory_equals_file(grid_dir):
+    import geodesicodis_gb300 as g
+    a = g.Mesh.generate(3, RADIUS)
+    b = g.Mesh.from_file(grid_dir / "grid_3.txt", RADIUS)
+    for w in range(12):
+        np.testing.assert_array_equal(a.field(w), b.field(w))
+
+
+def test_bad_grid_is_rejected(tmp_path, built):
+    import geodesicodis_gb300 as g
+    p = tmp_path / "bad.txt"
+    p.write_text("header\n0 0.0 0.0 {1, 2, 3, 4, 5, 99}, {(0,0), (0,0), (0,0), (0,0), (0,0), (0,0)}\n")
+    with pytest.raises(g.OdisError):
+        g.Mesh.from_file(p, RADIUS)
+    with pytest.raises(g.OdisError):
+        g.Mesh.from_file(tmp_path / "missing.txt", RADIUS)

@@ -1,0 +1,152 @@
+"""Pins of the CPU oracle.
+
+The reference ships no golden vectors; its own tests of this path are the
+operator tests of src/tests.cpp (analytic fields projected on face normals,
+error norms of G, D and C, :38-195, :246-319, :413-526), run over its grid
+files.  They are re-expressed here as convergence assertions on the shipped
+grids (when mounted) and on generated grids, together with the structural
+properties of the TRiSK weights and the Legendre normalisation used by the
+self-gravity term (SHTOOLS 4pi normalisation, csphase=-1)."""
+import numpy as np
+import pytest
+
+from conftest import ANGVEL_IN, RADIUS, REF_INPUT, ref_grid
+
+
+def spmv(csr, x):
+    rp, col, val = csr
+    y = np.add.reduceat(val * x[col], rp[:-1]) if len(val) else np.zeros(len(rp) - 1)
+    y[np.diff(rp) == 0] = 0.0
+    return y
+
+
+def node_latlon(path):
+    lat, lon = [], []
+    with open(path) as f:
+        next(f)
+        for line in f:
+            p = line.split()
+            lat.append(float(p[1])); lon.append(float(p[2]))
+    return np.radians(lat), np.radians(lon)
+
+
+def operator_errors(path):
+    """L1 error norms of G, -D and C (Omega = 1) against the analytic fields of src/tests.cpp (m = n = 1)."""
+    from oracle import pyoracle as O
+    m = O.OracleMesh(path, RADIUS)
+    lat, lon = node_latlon(path)
+    clat, clon, nx, ny, ilat = m.field(4), m.field(5), m.field(8), m.field(9), m.field(10)
+    R = RADIUS
+    beta = 1e8 * np.cos(lon) * np.cos(lat)                        # setBeta
+    ge = -1e8 * np.cos(clat) * np.sin(clon) / (R * np.cos(clat))   # setGradBeta (curl-free form)
+    gn = -1e8 * np.cos(clon) * np.sin(clat) / R
+    grad_an = ge * nx + gn * ny
+    grad = spmv(m.csr(0), beta)
+    div = -spmv(m.csr(1), grad_an)                                 # -D (src/tests.cpp:457)
+    div_an = -2.0 * beta / R ** 2                                  # Laplacian of the degree-1 field
+    ue = 1e8 * np.cos(clon) * np.sin(clat) / R                     # setU (div-free form)
+    un = -1e8 * np.cos(clat) * np.sin(clon) / (R * np.cos(clat))
+    vn, vt = ue * nx + un * ny, ue * ny - un * nx
+    cor = spmv(m.csr(2), vn)
+    cor_an = -2.0 * np.sin(ilat) * vt                              # src/tests.cpp:285
+    l1 = lambda a, b: np.mean(np.abs(a - b)) / np.max(np.abs(b))   # noqa: E731
+    return l1(grad, grad_an), l1(div, div_an), l1(cor, cor_an)
+
+
+def _convergence(paths, min_ratio):
+    errs = np.array([operator_errors(p) for p in paths])
+    ratios = errs[:-1] / errs[1:]
+    assert np.all(ratios > np.asarray(min_ratio)), ratios
+    assert errs[-1, 0] < 1e-4 and errs[-1, 1] < 1e-3 and errs[-1, 2] < 2e-2, errs
+    return errs
+
+
+@pytest.mark.skipif(not REF_INPUT.exists(), reason="reference grids not mounted")
+def test_operator_convergence_reference_grids(built):
+    # the shipped (tweaked) grids: second order for G and D, close to it for C
+    _convergence([ref_grid(k) for k in (2, 3, 4, 5)], (3.5, 3.5, 2.5))
+
+
+def test_operator_convergence_generated_grids(grid_dir):
+    # plain recursive bisection: G second order, D a little below, C first order
+    _convergence([grid_dir / f"grid_{k}.txt" for k in (2, 3, 4, 5)], (3.5, 3.0, 1.4))
+
+
+@pytest.mark.parametrize("level", [2, 3, 4])
+def test_trisk_antisymmetry(grid_dir, level):
+    """l_e w_ee' l_e' = -l_e' w_e'e l_e (energy-neutral Coriolis, Thuburn et al. 2009)."""
+    from oracle import pyoracle as O
+    m = O.OracleMesh(grid_dir / f"grid_{level}.txt", RADIUS)
+    t = m.topology()
+    fl = m.field(0)
+    W = {}
+    for e in range(m.n_edges):
+        for k in range(t["interp_n"][e]):
+            W[(e, int(t["interp_friends"][e, k]))] = t["interp_w"][e, k]
+    worst = max(abs(W[(e, f)] + W[(f, e)]) for (e, f) in W)
+    assert worst < 1e-8
+    # each face has 10 neighbours, 9 next to a pentagon
+    assert set(np.unique(t["interp_n"])) <= {8, 9, 10}
+
+
+def test_derive_time_matches_reference_rules(built):
+    """Period rounded to an even number of seconds; dt = P/n, n the first multiple of 100 with P/n <= target."""
+    from oracle import pyoracle as O
+    import geodesicodis_gb300 as g
+    for target, n_expect in ((59.197, 2000), (29.5985, 4000), (14.79925, 8000), (30.0, 4000), (1e9, 0)):
+        a, P, dt, n = O.derive_time(ANGVEL_IN, target)
+        assert P == 118394.0 and n == n_expect
+        assert (a, P, dt, n) == g.derive_time(ANGVEL_IN, target)
+
+
+def test_legendre_normalisation(built):
+    from oracle import pyoracle as O
+    z = 0.3
+    s = np.sqrt(1 - z * z)
+    P = O.plmbar(4, z)
+    idx = lambda l, m: l * (l + 1) // 2 + m  # noqa: E731
+    assert abs(P[idx(0, 0)] - 1) < 1e-15
+    assert abs(P[idx(1, 1)] + np.sqrt(3) * s) < 1e-15                       # Condon-Shortley phase
+    assert abs(P[idx(2, 0)] - np.sqrt(5) * (3 * z * z - 1) / 2) < 1e-14
+    assert abs(P[idx(2, 1)] - np.sqrt(5 / 3) * (-3 * z * s)) < 1e-14
+    assert abs(P[idx(2, 2)] - np.sqrt(5 / 12) * 3 * s * s) < 1e-14
+    # 4pi normalisation: (1/2) int_{-1}^{1} Pbar_lm^2 dz = 2 - delta_m0
+    xg, wg = np.polynomial.legendre.leggauss(40)
+    for l, m in ((3, 0), (3, 2), (4, 4), (4, 1)):
+        v = np.array([O.plmbar(4, x)[idx(l, m)] for x in xg])
+        assert abs(0.5 * np.sum(wg * v * v) - (1.0 if m == 0 else 2.0)) < 1e-12
+
+
+def test_sh_lsq_round_trip(grid_dir):
+    """Analysis of a band-limited field recovers its coefficients exactly (LSQ, as SHExpandLSQ)."""
+    import ctypes as C
+    from oracle import pyoracle as O
+    L = 6
+    K = (L + 1) ** 2
+    m = O.OracleMesh(grid_dir / "grid_3.txt", RADIUS)
+    s = O.OracleSolver(m, radius=RADIUS, g=0.113, angvel=1e-5, h=1e3, alpha=1e-6, dt=10.0,
+                       sh_lmax=L, sh_factors=np.ones(L + 1))
+    Y = np.zeros((m.n_cells, K))
+    O.lib().orc_sh_basis(m._h, L, Y.ctypes.data_as(C.POINTER(C.c_double)))
+    c = np.random.default_rng(0).standard_normal(K)
+    eta = Y @ c
+    out = np.zeros(K)
+    O.lib().orc_sh_analysis(s._s, eta.ctypes.data_as(C.POINTER(C.c_double)), out.ctypes.data_as(C.POINTER(C.c_double)))
+    np.testing.assert_allclose(out, c, atol=1e-10)
+
+
+def test_oracle_rest_state_and_linearity(grid_dir):
+    """No forcing and a zero state stay at rest; doubling the forcing doubles the response."""
+    from oracle import pyoracle as O
+    from conftest import config0_params
+    m = O.OracleMesh(grid_dir / "grid_2.txt", RADIUS)
+    s0 = O.OracleSolver(m, **config0_params(potential=O.NONE))
+    p = s0.run(50)
+    assert np.all(p == 0.0)
+    a = O.OracleSolver(m, **config0_params())
+    b = O.OracleSolver(m, **config0_params(ecc=2 * 0.0047))
+    a.run(200); b.run(200)
+    _, va, ea, _, _ = a.get_state()
+    _, vb, eb, _, _ = b.get_state()
+    np.testing.assert_allclose(vb, 2 * va, rtol=1e-12, atol=1e-14 * np.abs(va).max())
+    np.testing.assert_allclose(eb, 2 * ea, rtol=1e-12, atol=1e-14 * np.abs(ea).max())
