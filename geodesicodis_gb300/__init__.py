@@ -71,6 +71,9 @@ _SIGS = {
     "odis_mesh_field": ([_V, C.c_int, _D], C.c_int),
     "odis_mesh_topology": ([_V, _I, _I, _I, _I, _D, _I], C.c_int),
     "odis_mesh_destroy": ([_V], None),
+    "odis_mesh_gravity_wave_omega": ([_V, C.c_double, C.c_double, C.c_int, _D], C.c_int),
+    "odis_stable_steps_per_orbit": ([C.c_double, C.c_double, C.c_double, _I], C.c_int),
+    "odis_loading_factors": ([C.c_double, C.c_double, C.c_int, _D], C.c_int),
     "odis_derive_time": ([C.c_double, C.c_double, _D, _D, _D, _I], C.c_int),
     "odis_params_from_input": ([C.c_char_p, C.POINTER(Input)], C.c_int),
     "odis_create": ([C.POINTER(Params), _V, C.POINTER(_V)], C.c_int),
@@ -133,6 +136,31 @@ def derive_time(angvel_in: float, dt_target: float):
     return a.value, p.value, d.value, n.value
 
 
+STABILITY_LIMIT = 6.0 / 11.0   # omega_max * dt bound of the reference's forward-backward AB3 loop
+
+
+def stable_steps_per_orbit(period: float, omega_max: float, margin: float = 0.95) -> int:
+    """Smallest multiple of 100 steps per orbit with omega_max * dt <= margin * 6/11."""
+    n = C.c_int()
+    _ck(lib().odis_stable_steps_per_orbit(period, omega_max, margin, C.byref(n)), "odis_stable_steps_per_orbit")
+    return n.value
+
+
+def loading_factors(g: float, radius: float, lmax: int) -> np.ndarray:
+    """gamma_l of the reference's FREE_LOADING surface, l = 0..lmax."""
+    out = np.zeros(lmax + 1)
+    _ck(lib().odis_loading_factors(g, radius, int(lmax), _dp(out)), "odis_loading_factors")
+    return out
+
+
+def benchmark_sh_factors(g: float, radius: float, lmax: int, seed: int = 1) -> np.ndarray:
+    """Per-degree self-gravity factors of the level-6 benchmark: f_l * gamma_l with
+    f_l ~ U[0.5, 1.5] (numpy default_rng(seed), degrees 2..lmax in order)."""
+    f = np.zeros(lmax + 1)
+    f[2:] = np.random.default_rng(seed).uniform(0.5, 1.5, lmax - 1)
+    return f * loading_factors(g, radius, lmax)
+
+
 def read_input(path: str | os.PathLike) -> Input:
     inp = Input()
     _ck(lib().odis_params_from_input(os.fsencode(str(path)), C.byref(inp)), "odis_params_from_input")
@@ -165,6 +193,12 @@ class Mesh:
         out = np.zeros(n)
         _ck(lib().odis_mesh_field(self._h, which, _dp(out)), "odis_mesh_field")
         return out
+
+    def gravity_wave_omega(self, g: float, h: float, iters: int = 300) -> float:
+        """sqrt of the largest eigenvalue of -g h D G (rad/s)."""
+        w = C.c_double()
+        _ck(lib().odis_mesh_gravity_wave_omega(self._h, g, h, int(iters), C.byref(w)), "odis_mesh_gravity_wave_omega")
+        return w.value
 
     def topology(self):
         E, N = self.n_edges, self.n_cells

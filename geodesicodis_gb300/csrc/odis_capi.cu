@@ -199,6 +199,46 @@ extern "C" odis_status odis_mesh_topology(const odis_mesh* mp, int* face_nodes, 
 
 extern "C" void odis_mesh_destroy(odis_mesh* m) { delete m; }
 
+extern "C" odis_status odis_mesh_gravity_wave_omega(const odis_mesh* m, double g, double h, int iters, double* omega)
+{
+    if (!m || !omega || !(g > 0.0) || !(h > 0.0) || iters <= 0) return ODIS_ERR_ARG;
+    *omega = gravity_wave_omega(m->m, g, h, iters);
+    return ODIS_OK;
+}
+
+// FREE_LOADING degree factors of src/boundaryConditions.cpp:29-76: loading
+// Love numbers from a uniform elastic body (rigidity 40 GPa, bulk density
+// 1609.22 kg/m^3, ocean 1000 kg/m^3) and gamma_l = (1 + k_l - h_l) 3 rho_o / ((2l+1) rho_b).
+extern "C" odis_status odis_loading_factors(double g, double radius, int lmax, double* out)
+{
+    if (!out || lmax < 0 || !(g > 0.0) || !(radius > 0.0)) return ODIS_ERR_ARG;
+    const double ocean_den = 1000.0, bulk_den = 1609.22, rig = 40e9;
+    out[0] = 0.0;
+    for (int l = 1; l <= lmax; l++) {
+        double eff_rig = (double)(2 * l * l + 4 * l + 3);
+        eff_rig /= (double)l;
+        eff_rig *= rig / (bulk_den * g * radius);
+        const double k_l = -(1.0 / (1.0 + eff_rig));
+        const double h_l = -(1.0 / (1.0 + eff_rig)) * (2.0 * (double)l + 1.0) / 3.0;
+        double f = (1.0 + k_l - h_l);
+        f *= 3. * ocean_den / ((2. * (double)l + 1.0) * bulk_den);
+        out[l] = f;
+    }
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_stable_steps_per_orbit(double period, double omega_max, double margin, int* steps)
+{
+    if (!steps || !(period > 0.0) || !(omega_max >= 0.0) || !(margin > 0.0 && margin <= 1.0)) return ODIS_ERR_ARG;
+    // omega*dt <= margin * 6/11 with dt = period/n, n a multiple of 100 (src/mesh.cpp:1601-1618)
+    const double nmin = period * omega_max / (margin * 6.0 / 11.0);
+    long long n = ((long long)std::ceil(nmin / 100.0)) * 100;
+    if (n < 100) n = 100;
+    if (n > 2000000000LL) return ODIS_ERR_ARG;
+    *steps = (int)n;
+    return ODIS_OK;
+}
+
 // ---------------------------------------------------------------------------
 // parameters
 // ---------------------------------------------------------------------------

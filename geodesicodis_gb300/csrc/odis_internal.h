@@ -53,6 +53,9 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
 // M = angvel * t, for the ECC / OBLIQ / OBLIQ_WEST / FULL potentials.
 int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, std::vector<double>& Ub);
 
+// sqrt(largest eigenvalue of -g h D G), power iteration
+double gravity_wave_omega(const Mesh& m, double g, double h, int iters);
+
 // Parse input.in (src/globals.cpp:325-477 semantics).
 int parse_input(const char* path, odis_input& out);
 

@@ -346,6 +346,44 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
     return bad ? ODIS_ERR_MESH : ODIS_OK;
 }
 
+// Largest gravity-wave frequency of the discrete operator: sqrt of the largest
+// eigenvalue of -g h D G (G gradient, D divergence as assembled in
+// src/mesh.cpp:3005-3288), by power iteration.  The time loop of the
+// reference (AB3 for v with the old eta, then AB3 for eta with the new v,
+// src/timeIntegrator.cpp:213-253) is stable for omega_max * dt <= 6/11.
+double gravity_wave_omega(const Mesh& m, double g, double h, int iters)
+{
+    const int N = m.N, E = m.E;
+    std::vector<double> x(N), y(N), gv(E);
+    for (int i = 0; i < N; i++) x[i] = ((i * 2654435761u) % 1000u) / 1000.0 - 0.5;   // deterministic start
+    double lam = 0.0;
+    for (int it = 0; it < iters; it++) {
+        double nx = 0.0;
+        for (int i = 0; i < N; i++) nx += x[i] * x[i];
+        nx = std::sqrt(nx);
+        for (int i = 0; i < N; i++) x[i] /= nx;
+#pragma omp parallel for schedule(static)
+        for (int e = 0; e < E; e++) {
+            const int a = m.face_nodes[(size_t)e * 2], b = m.face_nodes[(size_t)e * 2 + 1];
+            gv[e] = (-m.face_m[(size_t)e * 2] * x[a] + m.face_m[(size_t)e * 2 + 1] * x[b]) / m.face_dist[e];
+        }
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < N; i++) {
+            double s = 0.0;
+            for (int j = 0; j < m.nfriends(i); j++) {
+                const int f = m.faces[(size_t)i * 6 + j];
+                s += -m.node_face_dir[(size_t)i * 6 + j] * m.face_len[f] / m.cv_area[i] * gv[f];
+            }
+            y[i] = -g * h * s;
+        }
+        double r = 0.0;
+        for (int i = 0; i < N; i++) r += x[i] * y[i];
+        lam = r;
+        x.swap(y);
+    }
+    return std::sqrt(std::fabs(lam));
+}
+
 // U(t) = cos(M) Ua + sin(M) Ub for the single-frequency potentials of
 // src/tidalPotentials.cpp:82-174 (ECC, OBLIQ, OBLIQ_WEST, FULL), using the
 // node trig tables of src/mesh.cpp:2122-2152.

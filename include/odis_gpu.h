@@ -122,6 +122,20 @@ odis_status odis_mesh_field(const odis_mesh* m, int which, double* out);
 odis_status odis_mesh_topology(const odis_mesh* m, int* face_nodes, int* faces, int* node_face_dir,
                                int* interp_friends, double* interp_w, int* interp_n);
 void odis_mesh_destroy(odis_mesh* m);
+/* Largest gravity-wave frequency (rad/s) of the discrete operator: sqrt of the
+ * largest eigenvalue of -g h D G, by `iters` power iterations (host).  The
+ * reference's time loop (AB3 momentum with the old eta, then AB3 continuity
+ * with the new velocity, src/timeIntegrator.cpp:213-253) is stable only for
+ * omega_max * dt <= 6/11; the reference itself never checks this
+ * (src/mesh.cpp:1566-1621 only snaps dt). */
+odis_status odis_mesh_gravity_wave_omega(const odis_mesh* m, double g, double h, int iters, double* omega_max);
+/* Self-attraction/loading factor gamma_l (l = 0..lmax) of the FREE_LOADING
+ * surface (src/boundaryConditions.cpp:29-76, elastic body of rigidity 40 GPa).
+ * odis_params.sh_factors[l] = gamma_l reproduces the reference's loading term;
+ * a per-degree scaling f_l multiplies it (sh_factors[l] = f_l * gamma_l). */
+odis_status odis_loading_factors(double g, double radius, int lmax, double* out);
+/* Smallest multiple of 100 steps per orbit with omega_max * dt <= margin * 6/11. */
+odis_status odis_stable_steps_per_orbit(double period, double omega_max, double margin, int* steps);
 
 /* ---- parameters -------------------------------------------------------- */
 /* Period rounding (src/globals.cpp:209-214) and dt snapping (src/mesh.cpp:1566-1621). */

@@ -115,8 +115,8 @@ def test_graph_and_eager_paths_agree(grid_dir):
     """Chunks replayed from the CUDA graph and eager launches give identical bits; runs are deterministic."""
     _, a = _pair(grid_dir / "grid_2.txt")
     _, b = _pair(grid_dir / "grid_2.txt")
-    pa = np.concatenate([a.run(64 * 3 + 5)])
-    pb = np.concatenate([b.run(10), b.run(63), b.run(64 * 2 + 3 - 1), b.run(0 + 1)])
+    pa = a.run(64 * 3 + 5)                                   # 3 graph chunks + 5 eager steps
+    pb = np.concatenate([b.run(10), b.run(63), b.run(64 * 2 - 5), b.run(1)])   # mixed chunking, 197 steps
     assert pa.shape == pb.shape
     np.testing.assert_array_equal(pa, pb)
     np.testing.assert_array_equal(a.get_state()[1], b.get_state()[1])
@@ -157,3 +157,20 @@ def test_nonfinite_state_is_reported(grid_dir):
     with pytest.raises(g.OdisError) as ei:
         gpu.run(3)
     assert ei.value.code == g.ERR_NONFINITE
+
+
+@pytest.mark.parametrize("precision,lmax,tol", [(0, 8, 1e-10), (1, 8, 1e-4)])
+def test_self_gravity_loading_parity(grid_dir, precision, lmax, tol):
+    """Self-gravity/loading (least-squares SH analysis to l_max, per-degree factor, synthesis) vs the oracle."""
+    import geodesicodis_gb300 as g
+    fac = g.benchmark_sh_factors(0.113, RADIUS, lmax, seed=1)
+    orc, gpu = _pair(grid_dir / "grid_3.txt", precision=precision, sh_lmax=lmax, sh_factors=fac)
+    po, pg = orc.run(1500), gpu.run(1500)
+    _, vo, eo, _, _ = orc.get_state()
+    _, vg, eg, _, _ = gpu.get_state()
+    assert rel_err(pg[-500:], po[-500:]) < tol
+    if precision == 0:
+        assert rel_err(eg, eo) < tol and rel_err(vg, vo) < tol
+    # the term matters: the run without it differs well above the tolerance
+    orc0 = _pair(grid_dir / "grid_3.txt")[0]
+    assert rel_err(orc0.run(1500)[-500:], po[-500:]) > 1e3 * tol
