@@ -176,6 +176,23 @@ odis_status odis_get_state(odis_ctx* c, int* iter, double* v, double* eta, doubl
 odis_status odis_set_state(odis_ctx* c, int iter, const double* v, const double* eta,
                            const double* dvdt, const double* detadt);
 
+/* ---- allocation-free dissipation --------------------------------------- */
+/* Same result as odis_update_energy, for callers that cannot allocate device
+ * memory (host callbacks or graph host nodes, fixed-budget real-time loops,
+ * plugins handed only device buffers): no context, no cudaMalloc/cudaFree.
+ * No counterpart in the reference (its updateEnergy, src/energy.cpp:13-61, is
+ * the computation, not this calling convention).  All pointers are device
+ * pointers: uv [n_faces][2], area [n_faces], e_out [n_faces] (nullable),
+ * avg_out [1]; the area-mean dissipation alpha*1000*h*|uv|^2*area/(4 pi r^2)
+ * is written to *avg_out on `stream` (a cudaStream_t, NULL = legacy default).
+ * The reduction scratch is a fixed 64 KiB __device__ array held by every GPU
+ * that loads the library until exit: n_faces above 2,097,152 returns
+ * ODIS_ERR_ARG.  The first call on a device sets up that device's scratch
+ * address (make it before any stream capture).  Calls share the scratch, so
+ * calls that overlap on the GPU race: serialise them. */
+odis_status odis_update_energy_noalloc(const double* uv, const double* area, int n_faces, double alpha, double h,
+                                       double radius, double* e_out, double* avg_out, void* stream);
+
 /* ---- measurement ------------------------------------------------------- */
 /* Number of this library's kernels launched so far by the context. */
 odis_status odis_launch_count(odis_ctx* c, long long* n);
