@@ -20,7 +20,7 @@ import numpy as np
 
 __all__ = [
     "OdisError", "lib", "Params", "Input", "Mesh", "Solver", "generate_grid_file", "derive_time",
-    "read_input", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL", "FP64", "FP32",
+    "read_input", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL", "FP64", "FP32", "DF64",
 ]
 
 _PKG = Path(__file__).resolve().parent
@@ -30,7 +30,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_OOB, ERR_NONFINITE, ERR_TIMEOUT, ERR_IO, ERR_MESH, ER
 _NAMES = {1: "ODIS_ERR_ARG", 2: "ODIS_ERR_CUDA", 3: "ODIS_ERR_OOB", 4: "ODIS_ERR_NONFINITE",
           5: "ODIS_ERR_TIMEOUT", 6: "ODIS_ERR_IO", 7: "ODIS_ERR_MESH", 8: "ODIS_ERR_NOMEM"}
 POT_NONE, POT_ECC, POT_OBLIQ, POT_OBLIQ_WEST, POT_FULL = range(5)
-FP64, FP32 = 0, 1
+FP64, FP32, DF64 = 0, 1, 2
 MEM_HOST, MEM_DEVICE = 0, 1
 
 

@@ -10,6 +10,7 @@
 #include "odis_device.cuh"
 #include "odis_kernels.cuh"
 #include "odis_sh.cuh"
+#include "odis_df64.cuh"
 
 #include <cuda_runtime.h>
 
@@ -54,6 +55,13 @@ struct DevArena {
     ~DevArena() { for (void* p : ptrs) cudaFree(p); }
 };
 
+// value conversions between the host's FP64 and each method's storage type
+template <class T> T cvt(double x) { return (T)x; }
+template <> float2 cvt<float2>(double x) { return df_from_double(x); }
+inline double to_d(double x) { return x; }
+inline double to_d(float x) { return (double)x; }
+inline double to_d(float2 x) { return df_to_double(x); }
+
 template <class T>
 struct Operators {
     FaceCoef<T> fc{};
@@ -70,11 +78,13 @@ struct odis_ctx {
     DevArena mem;
     Operators<double> op64;      // always present: per-operator calls are FP64
     Operators<float> op32;       // FP32-state variant
+    Operators<float2> opdf;      // double-float method
     double* nrm = nullptr;       // [2][Ep]
     double* area = nullptr;      // [Ep]
     double* trig = nullptr;      // [10][Np]
     State<double> s64{};
     State<float> s32{};
+    State<float2> sdf{};
     long long* d_iter = nullptr;
     long long* d_run_first = nullptr;
     int* d_status = nullptr;
@@ -275,8 +285,9 @@ static int build_operators(odis_ctx* c, const Mesh& m, const std::vector<double>
     const int E = c->E, N = c->N, Ep = c->Ep, Np = c->Np;
     const odis_params& p = c->p;
     std::vector<int> nbr((size_t)kTrisk * Ep), n0(Ep), n1(Ep), edge((size_t)kCellFaces * Np);
-    std::vector<T> w((size_t)kTrisk * Ep, T(0)), gg0(Ep, T(0)), gg1(Ep, T(0)), cor(Ep, T(0));
-    std::vector<T> fP(Ep, T(0)), fQ(Ep, T(0)), diss(Ep, T(0)), hw((size_t)kCellFaces * Np, T(0));
+    const T zero = cvt<T>(0.0);
+    std::vector<T> w((size_t)kTrisk * Ep, zero), gg0(Ep, zero), gg1(Ep, zero), cor(Ep, zero);
+    std::vector<T> fP(Ep, zero), fQ(Ep, zero), diss(Ep, zero), hw((size_t)kCellFaces * Np, zero);
     const double four_pi_r2 = 4 * kPi * std::pow(m.r, 2.0);
     for (int e = 0; e < Ep; e++) {
         const int ee = e < E ? e : 0;
@@ -284,7 +295,7 @@ static int build_operators(odis_ctx* c, const Mesh& m, const std::vector<double>
             const bool ok = e < E && k < m.interp_n[ee];
             const int f = ok ? m.interp_friends[(size_t)ee * 10 + k] : ee;
             nbr[(size_t)k * Ep + e] = f;
-            w[(size_t)k * Ep + e] = ok ? (T)(m.interp_w[(size_t)ee * 10 + k] * m.face_len[f] / m.face_dist[ee]) : T(0);
+            w[(size_t)k * Ep + e] = ok ? cvt<T>(m.interp_w[(size_t)ee * 10 + k] * m.face_len[f] / m.face_dist[ee]) : zero;
         }
         const int a = m.face_nodes[(size_t)ee * 2], b = m.face_nodes[(size_t)ee * 2 + 1];
         n0[e] = a;
@@ -292,12 +303,12 @@ static int build_operators(odis_ctx* c, const Mesh& m, const std::vector<double>
         if (e >= E) continue;
         const double d = m.face_dist[e];
         const double g0 = (-m.face_m[(size_t)e * 2]) / d, g1 = (m.face_m[(size_t)e * 2 + 1]) / d;
-        gg0[e] = (T)(-p.g * g0);
-        gg1[e] = (T)(-p.g * g1);
-        cor[e] = (T)(-2.0 * p.angvel * std::sin(m.face_centre[(size_t)e * 2]));
-        fP[e] = (T)(g0 * Ua[a] + g1 * Ua[b]);
-        fQ[e] = (T)(g0 * Ub[a] + g1 * Ub[b]);
-        diss[e] = (T)(p.alpha * 1000.0 * p.h * m.face_area[e] / four_pi_r2);
+        gg0[e] = cvt<T>(-p.g * g0);
+        gg1[e] = cvt<T>(-p.g * g1);
+        cor[e] = cvt<T>(-2.0 * p.angvel * std::sin(m.face_centre[(size_t)e * 2]));
+        fP[e] = cvt<T>(g0 * Ua[a] + g1 * Ua[b]);
+        fQ[e] = cvt<T>(g0 * Ub[a] + g1 * Ub[b]);
+        diss[e] = cvt<T>(p.alpha * 1000.0 * p.h * m.face_area[e] / four_pi_r2);
     }
     for (int i = 0; i < Np; i++) {
         const int ii = i < N ? i : 0;
@@ -308,7 +319,7 @@ static int build_operators(odis_ctx* c, const Mesh& m, const std::vector<double>
             edge[(size_t)k * Np + i] = f;
             if (ok) {
                 const double dv = -m.node_face_dir[(size_t)ii * 6 + k] * m.face_len[f] / m.cv_area[ii];
-                hw[(size_t)k * Np + i] = (T)(p.h * dv);
+                hw[(size_t)k * Np + i] = cvt<T>(p.h * dv);
             }
         }
     }
@@ -344,12 +355,12 @@ static int alloc_state(odis_ctx* c, State<T>& s, bool split)
         s.v[k] = A.alloc<T>(c->Ep);
         s.hv[k] = A.alloc<T>(c->Ep);
         s.he[k] = A.alloc<T>(c->Np);
-        s.vlo[k] = split ? A.alloc<T>(c->Ep) : nullptr;
-        if (!s.v[k] || !s.hv[k] || !s.he[k] || (split && !s.vlo[k])) return ODIS_ERR_NOMEM;
+        if (!s.v[k] || !s.hv[k] || !s.he[k]) return ODIS_ERR_NOMEM;
     }
+    s.vm = split ? A.alloc<double>(c->Ep) : nullptr;
     s.eta = A.alloc<T>(c->Np);
-    s.etalo = split ? A.alloc<T>(c->Np) : nullptr;
-    if (!s.eta || (split && !s.etalo)) return ODIS_ERR_NOMEM;
+    s.etam = split ? A.alloc<double>(c->Np) : nullptr;
+    if (!s.eta || (split && (!s.vm || !s.etam))) return ODIS_ERR_NOMEM;
     s.usg = nullptr;
     s.iter = c->d_iter;
     s.run_first = c->d_run_first;
@@ -363,7 +374,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
 {
     if (!p || !mp || !out) return ODIS_ERR_ARG;
     *out = nullptr;
-    if (p->precision != ODIS_FP64 && p->precision != ODIS_FP32) return ODIS_ERR_ARG;
+    if (p->precision != ODIS_FP64 && p->precision != ODIS_FP32 && p->precision != ODIS_DF64) return ODIS_ERR_ARG;
     if (p->potential < ODIS_POT_NONE || p->potential > ODIS_POT_FULL) return ODIS_ERR_ARG;
     if (!(p->dt > 0.0) || !(p->g > 0.0) || !(p->h > 0.0) || !(p->radius > 0.0) || p->alpha < 0.0) return ODIS_ERR_ARG;
     if (p->sh_lmax < 0 || p->sh_lmax > 64 || (p->sh_lmax > 0 && !p->sh_factors)) return ODIS_ERR_ARG;
@@ -399,6 +410,10 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
         st = build_operators<float>(c.get(), m, Ua, Ub, c->op32);
         if (st != ODIS_OK) return st;
     }
+    if (p->precision == ODIS_DF64) {
+        st = build_operators<float2>(c.get(), m, Ua, Ub, c->opdf);
+        if (st != ODIS_OK) return st;
+    }
     // geometry needed by the per-operator calls
     std::vector<double> nrm((size_t)2 * c->Ep, 0.0), area(c->Ep, 0.0), trig((size_t)10 * c->Np, 0.0);
     for (int e = 0; e < m.E; e++) {
@@ -424,11 +439,16 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
         st = alloc_state<float>(c.get(), c->s32, true);
         if (st != ODIS_OK) return st;
     }
+    if (p->precision == ODIS_DF64) {
+        st = alloc_state<float2>(c.get(), c->sdf, false);
+        if (st != ODIS_OK) return st;
+    }
     if (p->sh_lmax > 0) {
         st = sh_create(&c->sh, m, p->sh_lmax, c->p.sh_factors, p->precision, c->Np);
         if (st != ODIS_OK) return st;
         c->s64.usg = sh_usg64(c->sh);
         c->s32.usg = sh_usg32(c->sh);
+        c->sdf.usg = sh_usgdf(c->sh);
     }
     StepConst& sc = c->sc;
     sc.E = m.E;
@@ -443,6 +463,11 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     sc.ab3c = 5. / 12.;
     sc.init_load = p->init_load ? 1 : 0;
     sc.use_sg = p->sh_lmax > 0 ? 1 : 0;
+    sc.df_dt = df_from_double(p->dt);
+    sc.df_malpha = df_from_double(-p->alpha);
+    sc.df_a = df_from_double(sc.ab3a);
+    sc.df_b = df_from_double(sc.ab3b);
+    sc.df_c = df_from_double(sc.ab3c);
     c->stage_n = (size_t)3 * std::max(c->Ep, c->Np);
     for (int k = 0; k < 4; k++) {
         c->stage[k] = A.alloc<double>(c->stage_n);
@@ -602,16 +627,25 @@ extern "C" odis_status odis_update_energy(odis_ctx* c, double* avg, double* e, c
 // ---------------------------------------------------------------------------
 // fused time loop
 // ---------------------------------------------------------------------------
+static const void* state_eta(const odis_ctx* c)
+{
+    return c->p.precision == ODIS_FP32 ? (const void*)c->s32.eta
+         : c->p.precision == ODIS_DF64 ? (const void*)c->sdf.eta : (const void*)c->s64.eta;
+}
+
 static int kernels_per_step(const odis_ctx* c) { return 2 + (c->sh ? 3 : 0); }
 
 static void enqueue_steps(odis_ctx* c, int n)
 {
     c->launches += (long long)n * kernels_per_step(c) + 1;
     for (int k = 0; k < n; k++) {
-        if (c->sh) sh_enqueue(c->sh, c->p.precision == ODIS_FP32 ? (const void*)c->s32.eta : (const void*)c->s64.eta,
-                              c->stream);
+        if (c->sh) sh_enqueue(c->sh, state_eta(c), c->stream);
         if (c->p.precision == ODIS_FP64) launch_step<double, false>(c->op64.fc, c->op64.cc, c->s64, c->sc, k, c->stream);
-        else launch_step<float, true>(c->op32.fc, c->op32.cc, c->s32, c->sc, k, c->stream);
+        else if (c->p.precision == ODIS_FP32) launch_step<float, true>(c->op32.fc, c->op32.cc, c->s32, c->sc, k, c->stream);
+        else {
+            launch_edge_df(c->opdf.fc, c->sdf, c->sc, k, c->stream);
+            launch_cell_df(c->opdf.cc, c->sdf, c->sc, k, c->stream);
+        }
     }
     launch_bump(c->d_iter, n, c->stream);
 }
@@ -655,9 +689,10 @@ extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem
     const long long first = c->iter;
     ODIS_CK(cudaMemcpyAsync(c->d_run_first, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
     ODIS_CK(cudaMemcpyAsync(c->d_iter, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
-    if (c->s64.power != dpow || c->s32.power != dpow) {
+    if (c->s64.power != dpow || c->s32.power != dpow || c->sdf.power != dpow) {
         c->s64.power = dpow;
         c->s32.power = dpow;
+        c->sdf.power = dpow;
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     }
     int done = 0;
@@ -671,7 +706,8 @@ extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem
     }
     if (done < n) enqueue_steps(c, n - done);
     if (c->p.precision == ODIS_FP64) launch_power_tail<double>(c->op64.fc, c->s64, c->sc, c->stream);
-    else launch_power_tail<float>(c->op32.fc, c->s32, c->sc, c->stream);
+    else if (c->p.precision == ODIS_FP32) launch_power_tail<float>(c->op32.fc, c->s32, c->sc, c->stream);
+    else launch_power_tail_df(c->opdf.fc, c->sdf, c->sc, c->stream);
     c->launches += 2;
     ODIS_CK(cudaGetLastError());
     if (power && mem == ODIS_MEM_HOST)
@@ -688,27 +724,29 @@ extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem
 // ---------------------------------------------------------------------------
 // state in the reference's layout
 // ---------------------------------------------------------------------------
+// device vector (or its FP64 master, when present) -> host doubles
 template <class T>
-static int get_vec(odis_ctx* c, const T* hi, const T* lo, size_t n, double* out)
+static int get_vec(odis_ctx* c, const T* v, const double* master, size_t n, double* out)
 {
-    std::vector<T> a(n), b;
-    ODIS_CK(cudaMemcpy(a.data(), hi, n * sizeof(T), cudaMemcpyDeviceToHost));
-    if (lo) { b.resize(n); ODIS_CK(cudaMemcpy(b.data(), lo, n * sizeof(T), cudaMemcpyDeviceToHost)); }
-    for (size_t i = 0; i < n; i++) out[i] = lo ? (double)a[i] + (double)b[i] : (double)a[i];
     (void)c;
+    if (master) {
+        ODIS_CK(cudaMemcpy(out, master, n * sizeof(double), cudaMemcpyDeviceToHost));
+        return ODIS_OK;
+    }
+    std::vector<T> a(n);
+    ODIS_CK(cudaMemcpy(a.data(), v, n * sizeof(T), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) out[i] = to_d(a[i]);
     return ODIS_OK;
 }
 
+// host doubles -> device vector (rounded to T) and its FP64 master, when present
 template <class T>
-static int set_vec(T* hi, T* lo, size_t n, const double* in)
+static int set_vec(T* v, double* master, size_t n, const double* in)
 {
-    std::vector<T> a(n), b(n);
-    for (size_t i = 0; i < n; i++) {
-        a[i] = (T)in[i];
-        b[i] = (T)(in[i] - (double)a[i]);
-    }
-    ODIS_CK(cudaMemcpy(hi, a.data(), n * sizeof(T), cudaMemcpyHostToDevice));
-    if (lo) ODIS_CK(cudaMemcpy(lo, b.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+    std::vector<T> a(n);
+    for (size_t i = 0; i < n; i++) a[i] = cvt<T>(in[i]);
+    ODIS_CK(cudaMemcpy(v, a.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+    if (master) ODIS_CK(cudaMemcpy(master, in, n * sizeof(double), cudaMemcpyHostToDevice));
     return ODIS_OK;
 }
 
@@ -718,8 +756,8 @@ static int get_state_t(odis_ctx* c, State<T>& s, double* v, double* eta, double*
     const long long k = c->iter;
     const size_t E = c->E, N = c->N;
     int st = ODIS_OK;
-    if (v) st = get_vec<T>(c, s.v[k & 1], s.vlo[0] ? s.vlo[k & 1] : nullptr, E, v);
-    if (st == ODIS_OK && eta) st = get_vec<T>(c, s.eta, s.etalo, N, eta);
+    if (v) st = get_vec<T>(c, s.v[k & 1], s.vm, E, v);
+    if (st == ODIS_OK && eta) st = get_vec<T>(c, s.eta, s.etam, N, eta);
     for (int which = 0; which < 2 && st == ODIS_OK; which++) {
         double* out = which == 0 ? dvdt : detadt;
         if (!out) continue;
@@ -752,14 +790,12 @@ static int set_state_t(odis_ctx* c, State<T>& s, long long k, const double* v, c
 {
     const size_t E = c->E, N = c->N;
     int st = ODIS_OK;
-    for (int q = 0; q < 2; q++) {
-        ODIS_CK(cudaMemset(s.v[q], 0, sizeof(T) * c->Ep));
-        if (s.vlo[q]) ODIS_CK(cudaMemset(s.vlo[q], 0, sizeof(T) * c->Ep));
-    }
-    if (v) st = set_vec<T>(s.v[k & 1], s.vlo[0] ? s.vlo[k & 1] : nullptr, E, v);
+    for (int q = 0; q < 2; q++) ODIS_CK(cudaMemset(s.v[q], 0, sizeof(T) * c->Ep));
+    if (s.vm) ODIS_CK(cudaMemset(s.vm, 0, sizeof(double) * c->Ep));
+    if (v) st = set_vec<T>(s.v[k & 1], s.vm, E, v);
     ODIS_CK(cudaMemset(s.eta, 0, sizeof(T) * c->Np));
-    if (s.etalo) ODIS_CK(cudaMemset(s.etalo, 0, sizeof(T) * c->Np));
-    if (st == ODIS_OK && eta) st = set_vec<T>(s.eta, s.etalo, N, eta);
+    if (s.etam) ODIS_CK(cudaMemset(s.etam, 0, sizeof(double) * c->Np));
+    if (st == ODIS_OK && eta) st = set_vec<T>(s.eta, s.etam, N, eta);
     for (int which = 0; which < 2 && st == ODIS_OK; which++) {
         const double* in = which == 0 ? dvdt : detadt;
         const size_t n = which == 0 ? E : N;
@@ -784,6 +820,7 @@ extern "C" odis_status odis_get_state(odis_ctx* c, int* iter, double* v, double*
     if (!c) return ODIS_ERR_ARG;
     ODIS_CK(cudaStreamSynchronize(c->stream));
     if (iter) *iter = (int)c->iter;
+    if (c->p.precision == ODIS_DF64) return get_state_t<float2>(c, c->sdf, v, eta, dvdt, detadt);
     return c->p.precision == ODIS_FP64 ? get_state_t<double>(c, c->s64, v, eta, dvdt, detadt)
                                        : get_state_t<float>(c, c->s32, v, eta, dvdt, detadt);
 }
@@ -794,6 +831,7 @@ extern "C" odis_status odis_set_state(odis_ctx* c, int iter, const double* v, co
     if (!c || iter < 0) return ODIS_ERR_ARG;
     ODIS_CK(cudaStreamSynchronize(c->stream));
     c->iter = iter;
+    if (c->p.precision == ODIS_DF64) return set_state_t<float2>(c, c->sdf, iter, v, eta, dvdt, detadt);
     return c->p.precision == ODIS_FP64 ? set_state_t<double>(c, c->s64, iter, v, eta, dvdt, detadt)
                                        : set_state_t<float>(c, c->s32, iter, v, eta, dvdt, detadt);
 }
@@ -827,15 +865,17 @@ extern "C" odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms)
         cudaGraphExec_t ge = nullptr;
         if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
         for (int r = 0; r < reps; r++) {
-            const bool f32 = c->p.precision == ODIS_FP32;
+            const bool f32 = c->p.precision == ODIS_FP32, fdf = c->p.precision == ODIS_DF64;
             if (which == 0) {
-                if (f32) launch_edge<float, true>(c->op32.fc, c->s32, c->sc, 2, c->stream);
+                if (fdf) launch_edge_df(c->opdf.fc, c->sdf, c->sc, 2, c->stream);
+                else if (f32) launch_edge<float, true>(c->op32.fc, c->s32, c->sc, 2, c->stream);
                 else launch_edge<double, false>(c->op64.fc, c->s64, c->sc, 2, c->stream);
             } else if (which == 1) {
-                if (f32) launch_cell<float, true>(c->op32.cc, c->s32, c->sc, 2, c->stream);
+                if (fdf) launch_cell_df(c->opdf.cc, c->sdf, c->sc, 2, c->stream);
+                else if (f32) launch_cell<float, true>(c->op32.cc, c->s32, c->sc, 2, c->stream);
                 else launch_cell<double, false>(c->op64.cc, c->s64, c->sc, 2, c->stream);
             } else {
-                sh_enqueue(c->sh, f32 ? (const void*)c->s32.eta : (const void*)c->s64.eta, c->stream);
+                sh_enqueue(c->sh, state_eta(c), c->stream);
             }
         }
         if (cudaStreamEndCapture(c->stream, &g) != cudaSuccess || cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) {

@@ -45,19 +45,25 @@ struct StepConst {
     double ab3a, ab3b, ab3c;  // 23/12, -16/12, 5/12
     int init_load;            // 1: AB3 from the first step
     int use_sg;               // 1: add the self-gravity / loading potential
+    // the same constants as double-float (hi, lo) pairs for the ODIS_DF64 method
+    float2 df_dt, df_malpha, df_a, df_b, df_c;
 };
 
 // Mutable state of one instance.  The time level of v alternates between
 // v[0] and v[1]; the AB3 history alternates between hv[0] and hv[1]:
 // step `it` reads v[it&1], writes v[(it+1)&1], reads f(it-1) from
 // hv[(it+1)&1] and f(it-2) from hv[it&1] and then stores f(it) in hv[it&1].
+// The FP32-state variant keeps an FP64 master copy of v and eta (vm, etam)
+// that only the owning thread reads and writes: the AB3 increment, formed in
+// FP32 from FP32 stencils, is accumulated in FP64 and the FP32 copies the
+// stencils gather from are rounded from the master each step.
 template <class T>
 struct State {
     T* v[2];
-    T* vlo[2];           // FP32 variant: low-order part of v (v ~= v + vlo)
+    double* vm;          // FP32 variant: FP64 master of v (nullptr in the FP64 method)
     T* hv[2];
     T* eta;
-    T* etalo;            // FP32 variant: low-order part of eta
+    double* etam;        // FP32 variant: FP64 master of eta
     T* he[2];
     const T* usg;        // [N] self-gravity potential / g (nullable)
     const long long* iter;   // device step counter (base of the current chunk)

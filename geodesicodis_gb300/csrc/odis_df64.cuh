@@ -1,0 +1,87 @@
+// Double-float ("df64") arithmetic: a value is an unevaluated sum hi + lo of
+// two FP32 numbers (|lo| <= ulp(hi)/2), a 48-bit significand.  GB300 runs FP64
+// at 1/74 of its FP32 rate (measured 1.0 vs 74 TFLOP/s), so the ODIS_DF64
+// method evaluates the FP64 step on the FP32 pipes with these error-free
+// transformations (Dekker 1971; Knuth TAOCP vol. 2, 4.2.2; the FMA form of
+// the exact product):
+//   two_sum(a, b):       s = a + b exactly as s + e           (6 flops)
+//   quick_two_sum(a, b): same for |a| >= |b|                   (3 flops)
+//   exact product:       p = a*b, e = fma(a, b, -p)            (2 flops)
+// Additions are the "sloppy" form (one two_sum on the high parts), which keeps
+// an absolute error of ~2^-48 of the larger operand -- enough for the 1e-10
+// parity of the time loop, which is verified against the FP64 oracle.
+// The compiler must not reassociate: these files are built without fast-math.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace odis {
+
+using df64 = float2;      // .x = hi, .y = lo
+
+__host__ __device__ __forceinline__ df64 df_make(float hi, float lo) { return make_float2(hi, lo); }
+
+// exact split of a double into a df64 (host, or device on cold paths)
+__host__ __device__ __forceinline__ df64 df_from_double(double x)
+{
+    const float hi = (float)x;
+    const float lo = (float)(x - (double)hi);
+    return make_float2(hi, lo);
+}
+
+__host__ __device__ __forceinline__ double df_to_double(df64 a) { return (double)a.x + (double)a.y; }
+
+__device__ __forceinline__ df64 df_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return make_float2(s, e);
+}
+
+__device__ __forceinline__ df64 df_quick_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float e = __fsub_rn(b, __fsub_rn(s, a));
+    return make_float2(s, e);
+}
+
+__device__ __forceinline__ df64 df_add(df64 a, df64 b)
+{
+    const df64 s = df_two_sum(a.x, b.x);
+    const float e = __fadd_rn(s.y, __fadd_rn(a.y, b.y));
+    return df_quick_two_sum(s.x, e);
+}
+
+__device__ __forceinline__ df64 df_neg(df64 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ df64 df_sub(df64 a, df64 b) { return df_add(a, df_neg(b)); }
+
+__device__ __forceinline__ df64 df_mul(df64 a, df64 b)
+{
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+    return df_quick_two_sum(p, e);
+}
+
+// a*b + c
+__device__ __forceinline__ df64 df_fma(df64 a, df64 b, df64 c)
+{
+    const float p = __fmul_rn(a.x, b.x);
+    float pe = __fmaf_rn(a.x, b.x, -p);
+    pe = __fmaf_rn(a.x, b.y, pe);
+    pe = __fmaf_rn(a.y, b.x, pe);
+    const df64 s = df_two_sum(p, c.x);
+    const float e = __fadd_rn(s.y, __fadd_rn(pe, c.y));
+    return df_quick_two_sum(s.x, e);
+}
+
+__device__ __forceinline__ df64 df_shfl_down(df64 a, int o)
+{
+    return make_float2(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o));
+}
+
+__device__ __forceinline__ bool df_finite(df64 a) { return (__float_as_int(a.x) & 0x7f800000) != 0x7f800000; }
+
+}  // namespace odis

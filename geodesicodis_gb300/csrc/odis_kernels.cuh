@@ -7,16 +7,21 @@ namespace odis {
 
 constexpr int kStepThreads = 256;
 
-template <class T, bool kSplit>
+template <class T, bool kMaster>
 void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s);
-template <class T, bool kSplit>
+template <class T, bool kMaster>
 void launch_cell(const CellCoef<T>& cc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s);
-template <class T, bool kSplit>
+template <class T, bool kMaster>
 void launch_step(const FaceCoef<T>& fc, const CellCoef<T>& cc, const State<T>& st, const StepConst& sc,
                  int offset, cudaStream_t s);
 template <class T>
 void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, cudaStream_t s);
 void launch_bump(long long* iter, int n, cudaStream_t s);
+
+// ODIS_DF64 method (odis_kernels_df.cu)
+void launch_edge_df(const FaceCoef<float2>& fc, const State<float2>& st, const StepConst& sc, int offset, cudaStream_t s);
+void launch_cell_df(const CellCoef<float2>& cc, const State<float2>& st, const StepConst& sc, int offset, cudaStream_t s);
+void launch_power_tail_df(const FaceCoef<float2>& fc, const State<float2>& st, const StepConst& sc, cudaStream_t s);
 
 void launch_momentum(const FaceCoef<double>& fc, int E, int Ep, double* dvdt, const double* v, const double* eta,
                      cudaStream_t s);

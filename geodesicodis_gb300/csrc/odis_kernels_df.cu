@@ -1,0 +1,168 @@
+// Step kernels of the ODIS_DF64 method: the FP64 time loop of
+// src/timeIntegrator.cpp:205-272 (linear branch) evaluated in double-float
+// arithmetic on the FP32 pipes (odis_df64.cuh).  Same data flow as the FP64
+// kernels of odis_kernels.cu -- face kernel (TRiSK tangential velocity,
+// dissipation of v^n, -g G eta + C v, forcing gradient, drag, AB3) then cell
+// kernel (h D v^{n+1}, AB3) -- with every coefficient and state value stored as
+// a float2 (hi, lo) pair: one 8-byte load per value, as for FP64.
+#include "../../include/odis_gpu.h"
+#include "odis_device.cuh"
+#include "odis_df64.cuh"
+#include "odis_kernels.cuh"
+
+namespace odis {
+
+namespace {
+
+__device__ __forceinline__ double warp_sum_dd(double x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// block sum of a df64 per thread; the result (as FP64) is valid in thread 0
+__device__ __forceinline__ double block_sum_df(df64 x, df64* smem)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = df_add(x, df_shfl_down(x, o));
+    if (lane == 0) smem[wid] = x;
+    __syncthreads();
+    df64 s = df_make(0.f, 0.f);
+    if (wid == 0) {
+        s = lane < kStepThreads / 32 ? smem[lane] : df_make(0.f, 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
+    }
+    return df_to_double(s);
+}
+
+__device__ __forceinline__ df64 ldg2(const df64* p) { return __ldg(p); }
+
+}  // namespace
+
+__global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc, State<df64> st, StepConst sc, int offset)
+{
+    __shared__ df64 s_cs[2];
+    __shared__ df64 s_red[kStepThreads / 32];
+    const long long it = *st.iter + offset;
+    if (threadIdx.x == 0) {
+        double t = sc.dt * (double)it + sc.dt, s, c;     // forcing phase at t^{n+1}
+        sincos(sc.angvel * t, &s, &c);
+        s_cs[0] = df_from_double(c);
+        s_cs[1] = df_from_double(s);
+    }
+    __syncthreads();
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Ep = sc.Ep;
+    const df64* __restrict__ vin = st.v[it & 1];
+    df64 pw = df_make(0.f, 0.f);
+    if (e < sc.E) {
+        df64 tsum = df_make(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < kTrisk; k++) tsum = df_fma(ldg2(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
+        const df64 ve = vin[e];
+        const int i0 = __ldg(&fc.n0[e]), i1 = __ldg(&fc.n1[e]);
+        pw = df_mul(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)));
+        const df64 g0 = ldg2(&fc.gg0[e]), g1 = ldg2(&fc.gg1[e]);
+        const df64 f0 = df_fma(ldg2(&fc.cor[e]), tsum, df_fma(g0, st.eta[i0], df_mul(g1, st.eta[i1])));
+        df64 gu = df_fma(s_cs[0], ldg2(&fc.fP[e]), df_mul(s_cs[1], ldg2(&fc.fQ[e])));
+        if (sc.use_sg) gu = df_sub(gu, df_fma(g0, st.usg[i0], df_mul(g1, st.usg[i1])));
+        const df64 drag = df_fma(sc.df_malpha, ve, gu);
+        df64* hcur = st.hv[it & 1];
+        df64 inc = f0;
+        if (sc.init_load || it > 1) {
+            const df64 f1 = st.hv[(it + 1) & 1][e];
+            const df64 f2 = hcur[e];
+            inc = df_fma(sc.df_c, f2, df_fma(sc.df_b, f1, df_mul(sc.df_a, f0)));
+        }
+        hcur[e] = f0;
+        df64 vn = df_fma(inc, sc.df_dt, ve);
+        vn = df_fma(sc.df_dt, drag, vn);
+        st.v[(it + 1) & 1][e] = vn;
+        if (!df_finite(vn)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
+    }
+    const double bs = block_sum_df(pw, s_red);
+    if (threadIdx.x == 0) st.partial[blockIdx.x] = bs;
+}
+
+__global__ void __launch_bounds__(kStepThreads) k_cell_step_df(CellCoef<df64> cc, State<df64> st, StepConst sc, int offset,
+                                                               int n_partial)
+{
+    const long long it = *st.iter + offset;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Np = sc.Np;
+    const df64* __restrict__ vn = st.v[(it + 1) & 1];
+    if (i < sc.N) {
+        df64 q = df_make(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < kCellFaces; k++) q = df_fma(ldg2(&cc.hw[k * Np + i]), vn[__ldg(&cc.edge[k * Np + i])], q);
+        df64* hcur = st.he[it & 1];
+        df64 inc = q;
+        if (sc.init_load || it > 1) {
+            const df64 f1 = st.he[(it + 1) & 1][i];
+            const df64 f2 = hcur[i];
+            inc = df_fma(sc.df_c, f2, df_fma(sc.df_b, f1, df_mul(sc.df_a, q)));
+        }
+        hcur[i] = q;
+        st.eta[i] = df_fma(inc, sc.df_dt, st.eta[i]);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
+        double s = 0.0;
+        for (int k = threadIdx.x; k < n_partial; k += 32) s += st.partial[k];
+        s = warp_sum_dd(s);
+        const long long k = it - 1 - *st.run_first;
+        if (threadIdx.x == 0 && k >= 0 && st.power) st.power[k] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64> fc, State<df64> st, StepConst sc)
+{
+    __shared__ df64 s_red[kStepThreads / 32];
+    const long long it = *st.iter;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Ep = sc.Ep;
+    const df64* __restrict__ vin = st.v[it & 1];
+    df64 pw = df_make(0.f, 0.f);
+    if (e < sc.E) {
+        df64 tsum = df_make(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < kTrisk; k++) tsum = df_fma(ldg2(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
+        const df64 ve = vin[e];
+        pw = df_mul(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)));
+    }
+    const double bs = block_sum_df(pw, s_red);
+    if (threadIdx.x == 0) st.partial[blockIdx.x] = bs;
+}
+
+__global__ void k_power_tail_df(State<df64> st, int n_partial)
+{
+    double s = 0.0;
+    for (int k = threadIdx.x; k < n_partial; k += 32) s += st.partial[k];
+    s = warp_sum_dd(s);
+    const long long k = *st.iter - 1 - *st.run_first;
+    if (threadIdx.x == 0 && k >= 0 && st.power) st.power[k] = s;
+}
+
+void launch_edge_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
+{
+    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
+    k_edge_step_df<<<eb, kStepThreads, 0, s>>>(fc, st, sc, offset);
+}
+
+void launch_cell_df(const CellCoef<df64>& cc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
+{
+    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
+    const int cb = (sc.N + kStepThreads - 1) / kStepThreads;
+    k_cell_step_df<<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset, eb);
+}
+
+void launch_power_tail_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, cudaStream_t s)
+{
+    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
+    k_power_partial_df<<<eb, kStepThreads, 0, s>>>(fc, st, sc);
+    k_power_tail_df<<<1, 32, 0, s>>>(st, eb);
+}
+
+}  // namespace odis

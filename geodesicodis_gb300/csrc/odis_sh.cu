@@ -8,6 +8,7 @@
 // Featherstone 2002) and the Gram matrix Y^T Y is inverted in FP64 (Cholesky);
 // the FP32-state variant stores Y in FP32 and accumulates in FP64.
 #include "odis_sh.cuh"
+#include "odis_df64.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -18,8 +19,8 @@ namespace odis {
 namespace {
 
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993751058;
-constexpr int kChunk = 2048;          // cells per analysis block
 constexpr int kShThreads = 256;
+constexpr int kSynthThreads = 128;
 
 // fully normalised (4pi) associated Legendre functions with the Condon-Shortley
 // phase, P[l(l+1)/2 + m], argument z = cos(colatitude)
@@ -55,72 +56,139 @@ __device__ __forceinline__ double warp_sum_d(double x)
     return x;
 }
 
-// t_partial[k][chunk] = sum over the chunk's cells of Y[k][i] eta[i]
+// Accumulator type of the transforms: FP64 for the FP64 method, FP32 inside a
+// thread for the FP32-state variant (block and global sums are FP64 in both).
+template <class T> struct Acc { using type = double; };
+template <> struct Acc<float> { using type = float; };
+
+// t[k] = sum_i Y[k][i] eta[i]: one block per harmonic, four independent
+// accumulators per thread, FP64 block sum in a fixed order.
 template <class T>
 __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict__ Y, const T* __restrict__ eta, int N,
-                                                            int Np, int nchunk, double* __restrict__ part)
+                                                            int Np, double* __restrict__ t)
 {
+    using A = typename Acc<T>::type;
     __shared__ double red[kShThreads / 32];
-    const int k = blockIdx.y, ch = blockIdx.x;
+    const int k = blockIdx.x;
     const T* row = Y + (size_t)k * Np;
-    const int i0 = ch * kChunk, i1 = min(N, i0 + kChunk);
-    double acc = 0.0;
-    for (int i = i0 + threadIdx.x; i < i1; i += kShThreads) acc = fma((double)row[i], (double)eta[i], acc);
+    A a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    int i = threadIdx.x;
+    for (; i + 3 * kShThreads < N; i += 4 * kShThreads) {
+        a0 = fma((A)row[i], (A)eta[i], a0);
+        a1 = fma((A)row[i + kShThreads], (A)eta[i + kShThreads], a1);
+        a2 = fma((A)row[i + 2 * kShThreads], (A)eta[i + 2 * kShThreads], a2);
+        a3 = fma((A)row[i + 3 * kShThreads], (A)eta[i + 3 * kShThreads], a3);
+    }
+    for (; i < N; i += kShThreads) a0 = fma((A)row[i], (A)eta[i], a0);
+    double acc = (double)((a0 + a1) + (a2 + a3));
     acc = warp_sum_d(acc);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x < 32) {
         double s = threadIdx.x < kShThreads / 32 ? red[threadIdx.x] : 0.0;
         s = warp_sum_d(s);
-        if (threadIdx.x == 0) part[(size_t)k * nchunk + ch] = s;
+        if (threadIdx.x == 0) t[k] = s;
     }
 }
 
-// c = F Ginv t, one block; t_k folded from the chunk partials in order
-__global__ void __launch_bounds__(kShThreads) k_sh_solve(const double* __restrict__ part, int nchunk, int K,
-                                                         const double* __restrict__ FGinv, double* __restrict__ coef)
+// c = (F G^-1) t: one warp per coefficient
+__global__ void __launch_bounds__(32) k_sh_coef(const double* __restrict__ t, int K, const double* __restrict__ FGinv,
+                                                double* __restrict__ coef)
 {
-    extern __shared__ double t[];
-    for (int k = threadIdx.x; k < K; k += kShThreads) {
-        double s = 0.0;
-        for (int ch = 0; ch < nchunk; ch++) s += part[(size_t)k * nchunk + ch];
-        t[k] = s;
-    }
-    __syncthreads();
-    for (int a = threadIdx.x; a < K; a += kShThreads) {
-        const double* row = FGinv + (size_t)a * K;
-        double s = 0.0;
-        for (int b = 0; b < K; b++) s = fma(row[b], t[b], s);
-        coef[a] = s;
-    }
-}
-
-// usg[i] = sum_k Y[k][i] c[k]   (harmonics l >= 2 only; c is zero below)
-template <class T>
-__global__ void __launch_bounds__(kShThreads) k_sh_synth(const T* __restrict__ Y, const double* __restrict__ coef,
-                                                         int N, int Np, int K, T* __restrict__ usg)
-{
-    extern __shared__ double c[];
-    for (int k = threadIdx.x; k < K; k += kShThreads) c[k] = coef[k];
-    __syncthreads();
-    const int i = blockIdx.x * kShThreads + threadIdx.x;
-    if (i >= N) return;
+    const int a = blockIdx.x;
+    const double* row = FGinv + (size_t)a * K;
     double s = 0.0;
-    for (int k = 4; k < K; k++) s = fma((double)Y[(size_t)k * Np + i], c[k], s);
-    usg[i] = (T)s;
+    for (int b = threadIdx.x; b < K; b += 32) s = fma(row[b], t[b], s);
+    s = warp_sum_d(s);
+    if (threadIdx.x == 0) coef[a] = s;
+}
+
+// usg[i] = sum_{k >= 4} Y[k][i] c[k]  (c is zero below degree 2)
+template <class T>
+__global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict__ Y, const double* __restrict__ coef,
+                                                            int N, int Np, int K, T* __restrict__ usg)
+{
+    using A = typename Acc<T>::type;
+    extern __shared__ double c_sh[];
+    A* c = reinterpret_cast<A*>(c_sh);
+    for (int k = threadIdx.x; k < K; k += kSynthThreads) c[k] = (A)coef[k];
+    __syncthreads();
+    const int i = blockIdx.x * kSynthThreads + threadIdx.x;
+    if (i >= N) return;
+    A a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    int k = 4;
+    for (; k + 3 < K; k += 4) {
+        a0 = fma((A)Y[(size_t)k * Np + i], c[k], a0);
+        a1 = fma((A)Y[(size_t)(k + 1) * Np + i], c[k + 1], a1);
+        a2 = fma((A)Y[(size_t)(k + 2) * Np + i], c[k + 2], a2);
+        a3 = fma((A)Y[(size_t)(k + 3) * Np + i], c[k + 3], a3);
+    }
+    for (; k < K; k++) a0 = fma((A)Y[(size_t)k * Np + i], c[k], a0);
+    usg[i] = (T)((a0 + a1) + (a2 + a3));
+}
+
+// double-float forms of the two transforms (ODIS_DF64 method)
+__global__ void __launch_bounds__(kShThreads) k_sh_analysis_df(const df64* __restrict__ Y, const df64* __restrict__ eta,
+                                                               int N, int Np, double* __restrict__ t)
+{
+    __shared__ df64 red[kShThreads / 32];
+    const int k = blockIdx.x;
+    const df64* row = Y + (size_t)k * Np;
+    df64 a0 = df_make(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
+    int i = threadIdx.x;
+    for (; i + 3 * kShThreads < N; i += 4 * kShThreads) {
+        a0 = df_fma(row[i], eta[i], a0);
+        a1 = df_fma(row[i + kShThreads], eta[i + kShThreads], a1);
+        a2 = df_fma(row[i + 2 * kShThreads], eta[i + 2 * kShThreads], a2);
+        a3 = df_fma(row[i + 3 * kShThreads], eta[i + 3 * kShThreads], a3);
+    }
+    for (; i < N; i += kShThreads) a0 = df_fma(row[i], eta[i], a0);
+    df64 acc = df_add(df_add(a0, a1), df_add(a2, a3));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_down(acc, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        df64 s = threadIdx.x < kShThreads / 32 ? red[threadIdx.x] : df_make(0.f, 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
+        if (threadIdx.x == 0) t[k] = df_to_double(s);
+    }
+}
+
+__global__ void __launch_bounds__(kSynthThreads) k_sh_synth_df(const df64* __restrict__ Y, const double* __restrict__ coef,
+                                                               int N, int Np, int K, df64* __restrict__ usg)
+{
+    extern __shared__ df64 cdf[];
+    for (int k = threadIdx.x; k < K; k += kSynthThreads) cdf[k] = df_from_double(coef[k]);
+    __syncthreads();
+    const int i = blockIdx.x * kSynthThreads + threadIdx.x;
+    if (i >= N) return;
+    df64 a0 = df_make(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
+    int k = 4;
+    for (; k + 3 < K; k += 4) {
+        a0 = df_fma(Y[(size_t)k * Np + i], cdf[k], a0);
+        a1 = df_fma(Y[(size_t)(k + 1) * Np + i], cdf[k + 1], a1);
+        a2 = df_fma(Y[(size_t)(k + 2) * Np + i], cdf[k + 2], a2);
+        a3 = df_fma(Y[(size_t)(k + 3) * Np + i], cdf[k + 3], a3);
+    }
+    for (; k < K; k++) a0 = df_fma(Y[(size_t)k * Np + i], cdf[k], a0);
+    usg[i] = df_add(df_add(a0, a1), df_add(a2, a3));
 }
 
 }  // namespace
 
 struct ShLoading {
-    int L = 0, K = 0, N = 0, Np = 0, nchunk = 0, precision = ODIS_FP64;
+    int L = 0, K = 0, N = 0, Np = 0, precision = ODIS_FP64;
     double* Y64 = nullptr;
     float* Y32 = nullptr;
     double* FGinv = nullptr;
-    double* part = nullptr;
+    double* t = nullptr;
     double* coef = nullptr;
     double* usg64 = nullptr;
     float* usg32 = nullptr;
+    df64* Ydf = nullptr;
+    df64* usgdf = nullptr;
 };
 
 void sh_basis_host(const Mesh& m, int L, std::vector<double>& Y)
@@ -206,7 +274,6 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
         }
     ShLoading* s = new ShLoading;
     s->L = L; s->K = K; s->N = m.N; s->Np = Np; s->precision = precision;
-    s->nchunk = (m.N + kChunk - 1) / kChunk;
     std::vector<double> Yt((size_t)K * Np, 0.0);
     for (int i = 0; i < m.N; i++)
         for (int k = 0; k < K; k++) Yt[(size_t)k * Np + i] = Y[(size_t)i * K + k];
@@ -219,13 +286,18 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
     if (precision == ODIS_FP64) {
         up((void**)&s->Y64, Yt.data(), sizeof(double) * Yt.size());
         up((void**)&s->usg64, nullptr, sizeof(double) * Np);
+    } else if (precision == ODIS_DF64) {
+        std::vector<df64> Yd(Yt.size());
+        for (size_t q = 0; q < Yt.size(); q++) Yd[q] = df_from_double(Yt[q]);
+        up((void**)&s->Ydf, Yd.data(), sizeof(df64) * Yd.size());
+        up((void**)&s->usgdf, nullptr, sizeof(df64) * Np);
     } else {
         std::vector<float> Yf(Yt.begin(), Yt.end());
         up((void**)&s->Y32, Yf.data(), sizeof(float) * Yf.size());
         up((void**)&s->usg32, nullptr, sizeof(float) * Np);
     }
     up((void**)&s->FGinv, G.data(), sizeof(double) * G.size());
-    up((void**)&s->part, nullptr, sizeof(double) * (size_t)K * s->nchunk);
+    up((void**)&s->t, nullptr, sizeof(double) * K);
     up((void**)&s->coef, nullptr, sizeof(double) * K);
     if (!ok) { sh_destroy(s); return ODIS_ERR_NOMEM; }
     *out = s;
@@ -235,27 +307,30 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
 void sh_destroy(ShLoading* s)
 {
     if (!s) return;
-    cudaFree(s->Y64); cudaFree(s->Y32); cudaFree(s->FGinv); cudaFree(s->part); cudaFree(s->coef);
-    cudaFree(s->usg64); cudaFree(s->usg32);
+    cudaFree(s->Y64); cudaFree(s->Y32); cudaFree(s->FGinv); cudaFree(s->t); cudaFree(s->coef);
+    cudaFree(s->usg64); cudaFree(s->usg32); cudaFree(s->Ydf); cudaFree(s->usgdf);
     delete s;
 }
 
 const double* sh_usg64(ShLoading* s) { return s ? s->usg64 : nullptr; }
 const float* sh_usg32(ShLoading* s) { return s ? s->usg32 : nullptr; }
+const float2* sh_usgdf(ShLoading* s) { return s ? s->usgdf : nullptr; }
 
 void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)
 {
-    dim3 ga(s->nchunk, s->K);
-    const size_t smem = sizeof(double) * s->K;
-    const int sb = (s->N + kShThreads - 1) / kShThreads;
+    const int sb = (s->N + kSynthThreads - 1) / kSynthThreads;
     if (s->precision == ODIS_FP64) {
-        k_sh_analysis<double><<<ga, kShThreads, 0, st>>>(s->Y64, (const double*)eta, s->N, s->Np, s->nchunk, s->part);
-        k_sh_solve<<<1, kShThreads, smem, st>>>(s->part, s->nchunk, s->K, s->FGinv, s->coef);
-        k_sh_synth<double><<<sb, kShThreads, smem, st>>>(s->Y64, s->coef, s->N, s->Np, s->K, s->usg64);
+        k_sh_analysis<double><<<s->K, kShThreads, 0, st>>>(s->Y64, (const double*)eta, s->N, s->Np, s->t);
+        k_sh_coef<<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, s->coef);
+        k_sh_synth<double><<<sb, kSynthThreads, sizeof(double) * s->K, st>>>(s->Y64, s->coef, s->N, s->Np, s->K, s->usg64);
+    } else if (s->precision == ODIS_DF64) {
+        k_sh_analysis_df<<<s->K, kShThreads, 0, st>>>(s->Ydf, (const df64*)eta, s->N, s->Np, s->t);
+        k_sh_coef<<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, s->coef);
+        k_sh_synth_df<<<sb, kSynthThreads, sizeof(df64) * s->K, st>>>(s->Ydf, s->coef, s->N, s->Np, s->K, s->usgdf);
     } else {
-        k_sh_analysis<float><<<ga, kShThreads, 0, st>>>(s->Y32, (const float*)eta, s->N, s->Np, s->nchunk, s->part);
-        k_sh_solve<<<1, kShThreads, smem, st>>>(s->part, s->nchunk, s->K, s->FGinv, s->coef);
-        k_sh_synth<float><<<sb, kShThreads, smem, st>>>(s->Y32, s->coef, s->N, s->Np, s->K, s->usg32);
+        k_sh_analysis<float><<<s->K, kShThreads, 0, st>>>(s->Y32, (const float*)eta, s->N, s->Np, s->t);
+        k_sh_coef<<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, s->coef);
+        k_sh_synth<float><<<sb, kSynthThreads, sizeof(float) * s->K, st>>>(s->Y32, s->coef, s->N, s->Np, s->K, s->usg32);
     }
 }
 

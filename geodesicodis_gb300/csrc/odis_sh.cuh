@@ -26,6 +26,7 @@ void sh_destroy(ShLoading* s);
 // usg buffer ([Np], FP64 or FP32 according to the precision)
 const double* sh_usg64(ShLoading* s);
 const float* sh_usg32(ShLoading* s);
+const float2* sh_usgdf(ShLoading* s);
 // enqueue analysis + synthesis of the current eta (double* or float*)
 void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t stream);
 // host helpers for checks: real SH basis at the nodes, [N][K]

@@ -49,6 +49,8 @@ typedef int odis_status;
 /* arithmetic of the state and stencils */
 #define ODIS_FP64 0             /* everything in FP64 (the reference's method) */
 #define ODIS_FP32 1             /* FP32 state and stencils; FP64 time accumulation and reductions */
+#define ODIS_DF64 2             /* the FP64 method in double-float (2 x FP32, 48-bit significand) on the
+                                   FP32 pipes; meets the FP64 parity bar (1e-10 against the FP64 oracle) */
 
 /* where the pointers passed to per-operator calls live */
 #define ODIS_MEM_HOST 0

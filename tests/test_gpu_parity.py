@@ -174,3 +174,32 @@ def test_self_gravity_loading_parity(grid_dir, precision, lmax, tol):
     # the term matters: the run without it differs well above the tolerance
     orc0 = _pair(grid_dir / "grid_3.txt")[0]
     assert rel_err(orc0.run(1500)[-500:], po[-500:]) > 1e3 * tol
+
+
+@pytest.mark.parametrize("level,steps", [(2, 700), (3, 2500)])
+def test_df64_parity(grid_dir, level, steps):
+    """ODIS_DF64 (the FP64 method in double-float on the FP32 pipes) meets the FP64 parity bar."""
+    orc, gpu = _pair(grid_dir / f"grid_{level}.txt", precision=2)
+    po, pg = orc.run(steps), gpu.run(steps)
+    _, vo, eo, dvo, deo = orc.get_state()
+    _, vg, eg, dvg, deg = gpu.get_state()
+    assert rel_err(eg, eo) < 1e-10 and rel_err(vg, vo) < 1e-10 and rel_err(pg, po) < 1e-10
+    assert rel_err(dvg, dvo) < 1e-10 and rel_err(deg, deo) < 1e-10
+
+
+def test_df64_config0_full_run(grid_dir):
+    orc, gpu = _pair(grid_dir / "grid_4.txt", precision=2)
+    po, pg = orc.run(20000), gpu.run(20000)
+    _, vo, eo, _, _ = orc.get_state()
+    _, vg, eg, _, _ = gpu.get_state()
+    assert rel_err(eg, eo) < 1e-10 and rel_err(vg, vo) < 1e-10 and rel_err(pg, po) < 1e-10
+
+
+def test_df64_self_gravity_parity(grid_dir):
+    import geodesicodis_gb300 as g
+    fac = g.benchmark_sh_factors(0.113, RADIUS, 8, seed=1)
+    orc, gpu = _pair(grid_dir / "grid_3.txt", precision=2, sh_lmax=8, sh_factors=fac)
+    po, pg = orc.run(1500), gpu.run(1500)
+    _, vo, eo, _, _ = orc.get_state()
+    _, vg, eg, _, _ = gpu.get_state()
+    assert rel_err(pg, po) < 1e-10 and rel_err(eg, eo) < 1e-10 and rel_err(vg, vo) < 1e-10
