@@ -633,7 +633,7 @@ static const void* state_eta(const odis_ctx* c)
          : c->p.precision == ODIS_DF64 ? (const void*)c->sdf.eta : (const void*)c->s64.eta;
 }
 
-static int kernels_per_step(const odis_ctx* c) { return 2 + (c->sh ? 3 : 0); }
+static int kernels_per_step(const odis_ctx* c) { return 2 + (c->sh ? sh_kernels_per_step() : 0); }
 
 static void enqueue_steps(odis_ctx* c, int n)
 {
@@ -889,7 +889,7 @@ extern "C" odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms)
             float t = 0.f;
             cudaEventElapsedTime(&t, a, b);
             ms[which] = (double)t / reps;
-            c->launches += 2LL * reps * (which == 2 ? 3 : 1);
+            c->launches += 2LL * reps * (which == 2 ? sh_kernels_per_step() : 1);
         }
         if (ge) cudaGraphExecDestroy(ge);
         if (g) cudaGraphDestroy(g);

@@ -1,12 +1,24 @@
 // Spherical-harmonic self-gravity / loading kernels (see odis_sh.cuh).
 //
-// Layout: Y is stored [K][Np] (one harmonic per row, cells contiguous), so the
-// analysis (t_k = sum_i Y_ki eta_i) streams each row with coalesced loads and
-// the synthesis (usg_i = sum_k Y_ki c_k) reads one coalesced column slice per
-// k.  The normalised Legendre functions are evaluated in FP64 on the host
-// (three-term recurrences of the fully normalised functions, Holmes &
-// Featherstone 2002) and the Gram matrix Y^T Y is inverted in FP64 (Cholesky);
-// the FP32-state variant stores Y in FP32 and accumulates in FP64.
+// Storage: the real harmonic Y_lm(cos|sin) = Pbar_lm(sin lat) * (cos|sin)(m lon)
+// is never stored.  Each cell keeps the (L+1)(L+2)/2 normalised Legendre values
+// Pbar_lm in rows ordered by order m (P[row(l,m)][Np]) plus cos(m lon) and
+// sin(m lon) rows; at level 6 with L = 16 that is 187 rows (61 MB in FP64/DF64)
+// instead of 289 rows of Y, small enough to stay L2-resident next to the
+// stencil data across steps.
+//
+// Per step:
+//   k_sh_analysis: blocks of (order m, up to 8 degrees, chunk of cells);
+//                  partial sums of Pbar_lm * (cos|sin)(m lon) * eta per chunk
+//   k_sh_fold:     t_k = fixed-order sum of the chunk partials
+//   k_sh_coef:     c = F (Y^T Y)^-1 t  (least squares as SHExpandLSQ, factors F)
+//   k_sh_synth:    usg_i = sum_m cos(m lon) sum_l Pbar_lm c_lm,cos + sin(m lon) sum_l Pbar_lm c_lm,sin
+//                  with cos/sin(m lon) advanced by angle addition in registers
+// The Legendre values are computed in FP64 on the host (three-term recurrences
+// of the fully normalised functions, Holmes & Featherstone 2002), the Gram
+// matrix Y^T Y in FP64 on the device, its inverse in FP64 (Cholesky) on the
+// host.  The arithmetic of the per-step transforms follows the method: FP64,
+// double-float (DF64) or FP32 (FP32-state variant; block sums in FP64).
 #include "odis_sh.cuh"
 #include "odis_df64.cuh"
 
@@ -21,6 +33,8 @@ namespace {
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993751058;
 constexpr int kShThreads = 256;
 constexpr int kSynthThreads = 128;
+constexpr int kTileL = 8;          // degrees per analysis block
+constexpr int kChunks = 16;        // cell chunks of the analysis
 
 // fully normalised (4pi) associated Legendre functions with the Condon-Shortley
 // phase, P[l(l+1)/2 + m], argument z = cos(colatitude)
@@ -47,48 +61,104 @@ void plm_bar(int L, double z, std::vector<double>& P)
 }
 
 // column of harmonic (l, m, cos|sin): l^2 for m=0, l^2 + 2m-1 (cos), l^2 + 2m (sin)
-inline int sh_col(int l, int m, int is_sin) { return l * l + (m == 0 ? 0 : 2 * m - 1 + is_sin); }
+__host__ __device__ inline int sh_col(int l, int m, int is_sin) { return l * l + (m == 0 ? 0 : 2 * m - 1 + is_sin); }
+// Legendre row of (l, m), rows ordered by m then l
+__host__ __device__ inline int p_row(int L, int l, int m) { return m * (L + 1) - m * (m - 1) / 2 + (l - m); }
 
-__device__ __forceinline__ double warp_sum_d(double x)
+// ---- arithmetic of each method ---------------------------------------------
+template <class T> struct Ar;
+template <> struct Ar<double> {
+    using V = double;
+    __device__ static V zero() { return 0.0; }
+    __device__ static V fma(V a, V b, V c) { return ::fma(a, b, c); }
+    __device__ static V mul(V a, V b) { return a * b; }
+    __device__ static V add(V a, V b) { return a + b; }
+    __device__ static V sub(V a, V b) { return a - b; }
+    __device__ static V from(double x) { return x; }
+    __device__ static double to(V a) { return a; }
+    __device__ static V shfl(V a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
+};
+template <> struct Ar<float> {
+    using V = float;
+    __device__ static V zero() { return 0.f; }
+    __device__ static V fma(V a, V b, V c) { return fmaf(a, b, c); }
+    __device__ static V mul(V a, V b) { return a * b; }
+    __device__ static V add(V a, V b) { return a + b; }
+    __device__ static V sub(V a, V b) { return a - b; }
+    __device__ static V from(double x) { return (float)x; }
+    __device__ static double to(V a) { return (double)a; }
+    __device__ static V shfl(V a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
+};
+template <> struct Ar<df64> {
+    using V = df64;
+    __device__ static V zero() { return df_make(0.f, 0.f); }
+    __device__ static V fma(V a, V b, V c) { return df_fma(a, b, c); }
+    __device__ static V mul(V a, V b) { return df_mul(a, b); }
+    __device__ static V add(V a, V b) { return df_add(a, b); }
+    __device__ static V sub(V a, V b) { return df_sub(a, b); }
+    __device__ static V from(double x) { return df_from_double(x); }
+    __device__ static double to(V a) { return df_to_double(a); }
+    __device__ static V shfl(V a, int o) { return df_shfl_down(a, o); }
+};
+
+// partial[k][chunk] = sum over the chunk's cells of Pbar_lm (cos|sin)(m lon) eta,
+// for the degrees l0 .. l0+nl-1 of order m of this block's tile
+template <class T>
+__global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict__ P, const T* __restrict__ trig,
+                                                            const T* __restrict__ eta, int N, int Np, int L,
+                                                            const int* __restrict__ tiles, double* __restrict__ part)
 {
+    using A = Ar<T>;
+    __shared__ double red[kShThreads / 32][2 * kTileL];
+    const int m = tiles[3 * blockIdx.x], l0 = tiles[3 * blockIdx.x + 1], nl = tiles[3 * blockIdx.x + 2];
+    const int chunk = blockIdx.y;
+    const int per = (N + kChunks - 1) / kChunks;
+    const int i0 = chunk * per, i1 = min(N, i0 + per);
+    T ac[kTileL], as[kTileL];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    return x;
+    for (int j = 0; j < kTileL; j++) { ac[j] = A::zero(); as[j] = A::zero(); }
+    const T* cm = trig + (size_t)(2 * m) * Np;
+    const T* sm = trig + (size_t)(2 * m + 1) * Np;
+    const T* prow = P + (size_t)p_row(L, l0, m) * Np;
+    for (int i = i0 + threadIdx.x; i < i1; i += kShThreads) {
+        const T e = eta[i];
+        const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
+#pragma unroll
+        for (int j = 0; j < kTileL; j++) {
+            if (j < nl) {
+                const T p = prow[(size_t)j * Np + i];
+                ac[j] = A::fma(p, ec, ac[j]);
+                as[j] = A::fma(p, es, as[j]);
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < kTileL; j++) {
+        if (j < nl) {
+            T c = ac[j], s = as[j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) { c = A::add(c, A::shfl(c, o)); s = A::add(s, A::shfl(s, o)); }
+            if (lane == 0) { red[wid][2 * j] = A::to(c); red[wid][2 * j + 1] = A::to(s); }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * nl) {
+        double s = 0.0;
+        for (int w = 0; w < kShThreads / 32; w++) s += red[w][threadIdx.x];
+        const int j = threadIdx.x >> 1, is_sin = threadIdx.x & 1;
+        if (m > 0 || !is_sin) part[(size_t)sh_col(l0 + j, m, is_sin) * kChunks + chunk] = s;
+    }
 }
 
-// Accumulator type of the transforms: FP64 for the FP64 method, FP32 inside a
-// thread for the FP32-state variant (block and global sums are FP64 in both).
-template <class T> struct Acc { using type = double; };
-template <> struct Acc<float> { using type = float; };
-
-// t[k] = sum_i Y[k][i] eta[i]: one block per harmonic, four independent
-// accumulators per thread, FP64 block sum in a fixed order.
-template <class T>
-__global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict__ Y, const T* __restrict__ eta, int N,
-                                                            int Np, double* __restrict__ t)
+// t_k = sum over chunks in a fixed order
+__global__ void k_sh_fold(const double* __restrict__ part, int K, double* __restrict__ t)
 {
-    using A = typename Acc<T>::type;
-    __shared__ double red[kShThreads / 32];
-    const int k = blockIdx.x;
-    const T* row = Y + (size_t)k * Np;
-    A a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    int i = threadIdx.x;
-    for (; i + 3 * kShThreads < N; i += 4 * kShThreads) {
-        a0 = fma((A)row[i], (A)eta[i], a0);
-        a1 = fma((A)row[i + kShThreads], (A)eta[i + kShThreads], a1);
-        a2 = fma((A)row[i + 2 * kShThreads], (A)eta[i + 2 * kShThreads], a2);
-        a3 = fma((A)row[i + 3 * kShThreads], (A)eta[i + 3 * kShThreads], a3);
-    }
-    for (; i < N; i += kShThreads) a0 = fma((A)row[i], (A)eta[i], a0);
-    double acc = (double)((a0 + a1) + (a2 + a3));
-    acc = warp_sum_d(acc);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double s = threadIdx.x < kShThreads / 32 ? red[threadIdx.x] : 0.0;
-        s = warp_sum_d(s);
-        if (threadIdx.x == 0) t[k] = s;
-    }
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    double s = 0.0;
+    for (int c = 0; c < kChunks; c++) s += part[(size_t)k * kChunks + c];
+    t[k] = s;
 }
 
 // c = (F G^-1) t: one warp per coefficient
@@ -99,96 +169,100 @@ __global__ void __launch_bounds__(32) k_sh_coef(const double* __restrict__ t, in
     const double* row = FGinv + (size_t)a * K;
     double s = 0.0;
     for (int b = threadIdx.x; b < K; b += 32) s = fma(row[b], t[b], s);
-    s = warp_sum_d(s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (threadIdx.x == 0) coef[a] = s;
 }
 
-// usg[i] = sum_{k >= 4} Y[k][i] c[k]  (c is zero below degree 2)
+// usg_i = sum_{m} [cos(m lon) sum_{l>=max(m,2)} Pbar_lm c_lm,cos + sin(m lon) sum_l Pbar_lm c_lm,sin]
+// kSynthLanes consecutive threads share a cell and split the orders m between
+// them (m = j, j + kSynthLanes, ...); their sums meet by shuffles in a fixed
+// order.  Two independent accumulator pairs keep two loads in flight per lane.
+constexpr int kSynthLanes = 4;
+
 template <class T>
-__global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict__ Y, const double* __restrict__ coef,
-                                                            int N, int Np, int K, T* __restrict__ usg)
+__global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict__ P, const T* __restrict__ trig,
+                                                            const double* __restrict__ coef, int N, int Np, int L, int K,
+                                                            T* __restrict__ usg)
 {
-    using A = typename Acc<T>::type;
-    extern __shared__ double c_sh[];
-    A* c = reinterpret_cast<A*>(c_sh);
-    for (int k = threadIdx.x; k < K; k += kSynthThreads) c[k] = (A)coef[k];
+    using A = Ar<T>;
+    extern __shared__ unsigned char c_raw[];
+    T* c = reinterpret_cast<T*>(c_raw);
+    for (int k = threadIdx.x; k < K; k += kSynthThreads) c[k] = A::from(coef[k]);
     __syncthreads();
-    const int i = blockIdx.x * kSynthThreads + threadIdx.x;
-    if (i >= N) return;
-    A a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    int k = 4;
-    for (; k + 3 < K; k += 4) {
-        a0 = fma((A)Y[(size_t)k * Np + i], c[k], a0);
-        a1 = fma((A)Y[(size_t)(k + 1) * Np + i], c[k + 1], a1);
-        a2 = fma((A)Y[(size_t)(k + 2) * Np + i], c[k + 2], a2);
-        a3 = fma((A)Y[(size_t)(k + 3) * Np + i], c[k + 3], a3);
+    const int gt = blockIdx.x * kSynthThreads + threadIdx.x;
+    const int i = gt / kSynthLanes, j = gt % kSynthLanes;
+    T u = A::zero();
+    if (i < N) {
+        for (int m = j; m <= L; m += kSynthLanes) {
+            T a0 = A::zero(), b0 = A::zero(), a1 = A::zero(), b1 = A::zero();
+            const int lstart = m < 2 ? 2 : m;
+            const T* prow = P + (size_t)p_row(L, lstart, m) * Np + i;
+            int l = lstart;
+            for (; l + 1 <= L; l += 2) {
+                const T p0 = prow[(size_t)(l - lstart) * Np];
+                const T p1 = prow[(size_t)(l + 1 - lstart) * Np];
+                a0 = A::fma(p0, c[sh_col(l, m, 0)], a0);
+                a1 = A::fma(p1, c[sh_col(l + 1, m, 0)], a1);
+                if (m > 0) {
+                    b0 = A::fma(p0, c[sh_col(l, m, 1)], b0);
+                    b1 = A::fma(p1, c[sh_col(l + 1, m, 1)], b1);
+                }
+            }
+            if (l <= L) {
+                const T p0 = prow[(size_t)(l - lstart) * Np];
+                a0 = A::fma(p0, c[sh_col(l, m, 0)], a0);
+                if (m > 0) b0 = A::fma(p0, c[sh_col(l, m, 1)], b0);
+            }
+            const T cm = trig[(size_t)(2 * m) * Np + i], sm = trig[(size_t)(2 * m + 1) * Np + i];
+            u = A::fma(cm, A::add(a0, a1), A::fma(sm, A::add(b0, b1), u));
+        }
     }
-    for (; k < K; k++) a0 = fma((A)Y[(size_t)k * Np + i], c[k], a0);
-    usg[i] = (T)((a0 + a1) + (a2 + a3));
+#pragma unroll
+    for (int o = kSynthLanes / 2; o > 0; o >>= 1) u = A::add(u, A::shfl(u, o));
+    if (i < N && j == 0) usg[i] = u;
 }
 
-// double-float forms of the two transforms (ODIS_DF64 method)
-__global__ void __launch_bounds__(kShThreads) k_sh_analysis_df(const df64* __restrict__ Y, const df64* __restrict__ eta,
-                                                               int N, int Np, double* __restrict__ t)
+// Gram matrix G = Y^T Y in FP64 (setup only): 32x32 output tiles, lower triangle
+__global__ void __launch_bounds__(256) k_gram(const double* __restrict__ Y, int K, int N, int Np, double* __restrict__ G)
 {
-    __shared__ df64 red[kShThreads / 32];
-    const int k = blockIdx.x;
-    const df64* row = Y + (size_t)k * Np;
-    df64 a0 = df_make(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
-    int i = threadIdx.x;
-    for (; i + 3 * kShThreads < N; i += 4 * kShThreads) {
-        a0 = df_fma(row[i], eta[i], a0);
-        a1 = df_fma(row[i + kShThreads], eta[i + kShThreads], a1);
-        a2 = df_fma(row[i + 2 * kShThreads], eta[i + 2 * kShThreads], a2);
-        a3 = df_fma(row[i + 3 * kShThreads], eta[i + 3 * kShThreads], a3);
+    __shared__ double ya[32][33], yb[32][33];
+    const int ta = blockIdx.y, tb = blockIdx.x;
+    if (tb > ta) return;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;      // 8 rows of threads
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int i0 = 0; i0 < N; i0 += 32) {
+        for (int r = ty; r < 32; r += 8) {
+            const int ka = ta * 32 + r, kb = tb * 32 + r, i = i0 + tx;
+            ya[r][tx] = (ka < K && i < N) ? Y[(size_t)ka * Np + i] : 0.0;
+            yb[r][tx] = (kb < K && i < N) ? Y[(size_t)kb * Np + i] : 0.0;
+        }
+        __syncthreads();
+        for (int q = 0; q < 4; q++) {
+            const int r = ty + 8 * q;
+#pragma unroll 8
+            for (int x = 0; x < 32; x++) acc[q] = fma(ya[r][x], yb[tx][x], acc[q]);
+        }
+        __syncthreads();
     }
-    for (; i < N; i += kShThreads) a0 = df_fma(row[i], eta[i], a0);
-    df64 acc = df_add(df_add(a0, a1), df_add(a2, a3));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc = df_add(acc, df_shfl_down(acc, o));
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        df64 s = threadIdx.x < kShThreads / 32 ? red[threadIdx.x] : df_make(0.f, 0.f);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
-        if (threadIdx.x == 0) t[k] = df_to_double(s);
+    for (int q = 0; q < 4; q++) {
+        const int a = ta * 32 + ty + 8 * q, b = tb * 32 + tx;
+        if (a < K && b < K) { G[(size_t)a * K + b] = acc[q]; G[(size_t)b * K + a] = acc[q]; }
     }
-}
-
-__global__ void __launch_bounds__(kSynthThreads) k_sh_synth_df(const df64* __restrict__ Y, const double* __restrict__ coef,
-                                                               int N, int Np, int K, df64* __restrict__ usg)
-{
-    extern __shared__ df64 cdf[];
-    for (int k = threadIdx.x; k < K; k += kSynthThreads) cdf[k] = df_from_double(coef[k]);
-    __syncthreads();
-    const int i = blockIdx.x * kSynthThreads + threadIdx.x;
-    if (i >= N) return;
-    df64 a0 = df_make(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
-    int k = 4;
-    for (; k + 3 < K; k += 4) {
-        a0 = df_fma(Y[(size_t)k * Np + i], cdf[k], a0);
-        a1 = df_fma(Y[(size_t)(k + 1) * Np + i], cdf[k + 1], a1);
-        a2 = df_fma(Y[(size_t)(k + 2) * Np + i], cdf[k + 2], a2);
-        a3 = df_fma(Y[(size_t)(k + 3) * Np + i], cdf[k + 3], a3);
-    }
-    for (; k < K; k++) a0 = df_fma(Y[(size_t)k * Np + i], cdf[k], a0);
-    usg[i] = df_add(df_add(a0, a1), df_add(a2, a3));
 }
 
 }  // namespace
 
 struct ShLoading {
-    int L = 0, K = 0, N = 0, Np = 0, precision = ODIS_FP64;
-    double* Y64 = nullptr;
-    float* Y32 = nullptr;
-    double* FGinv = nullptr;
+    int L = 0, K = 0, MP = 0, N = 0, Np = 0, precision = ODIS_FP64, ntiles = 0;
+    void* P = nullptr;           // [MP][Np] Legendre rows, method type
+    void* trig = nullptr;        // [2(L+1)][Np] cos(m lon), sin(m lon), method type
+    int* tiles = nullptr;        // [ntiles][3] (m, l0, nl)
+    double* part = nullptr;      // [K][kChunks]
+    double* FGinv = nullptr;     // [K][K]
     double* t = nullptr;
     double* coef = nullptr;
-    double* usg64 = nullptr;
-    float* usg32 = nullptr;
-    df64* Ydf = nullptr;
-    df64* usgdf = nullptr;
+    void* usg = nullptr;         // [Np] method type
 };
 
 void sh_basis_host(const Mesh& m, int L, std::vector<double>& Y)
@@ -222,6 +296,7 @@ static int chol_inverse(std::vector<double>& A, int n)
         if (!(d > 0.0)) return ODIS_ERR_ARG;
         d = std::sqrt(d);
         Lw[(size_t)j * n + j] = d;
+#pragma omp parallel for schedule(static)
         for (int i = j + 1; i < n; i++) {
             double s = Lw[(size_t)i * n + j];
             for (int k = 0; k < j; k++) s -= Lw[(size_t)i * n + k] * Lw[(size_t)j * n + k];
@@ -248,57 +323,96 @@ static int chol_inverse(std::vector<double>& A, int n)
     return ODIS_OK;
 }
 
+template <class T>
+static T host_cvt(double x);
+template <> double host_cvt<double>(double x) { return x; }
+template <> float host_cvt<float>(double x) { return (float)x; }
+template <> df64 host_cvt<df64>(double x) { return df_from_double(x); }
+
+template <class T>
+static bool upload_rows(void** d, const std::vector<double>& h)
+{
+    std::vector<T> v(h.size());
+    for (size_t q = 0; q < h.size(); q++) v[q] = host_cvt<T>(h[q]);
+    if (cudaMalloc(d, sizeof(T) * v.size()) != cudaSuccess) { *d = nullptr; return false; }
+    return cudaMemcpy(*d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+}
+
 int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int precision, int Np)
 {
     *out = nullptr;
-    const int K = (L + 1) * (L + 1);
+    const int K = (L + 1) * (L + 1), MP = (L + 1) * (L + 2) / 2;
     if (L < 2 || m.N < K) return ODIS_ERR_ARG;
-    std::vector<double> Y;
-    sh_basis_host(m, L, Y);
-    // Gram matrix Y^T Y (FP64), inverted
-    std::vector<double> G((size_t)K * K, 0.0);
-#pragma omp parallel for schedule(dynamic)
-    for (int a = 0; a < K; a++)
-        for (int b = 0; b <= a; b++) {
-            double s = 0.0;
-            for (int i = 0; i < m.N; i++) s += Y[(size_t)i * K + a] * Y[(size_t)i * K + b];
-            G[(size_t)a * K + b] = s;
-            G[(size_t)b * K + a] = s;
+    const int N = m.N;
+    // Legendre rows, trig rows (host, FP64)
+    std::vector<double> P((size_t)MP * Np, 0.0), trig((size_t)2 * (L + 1) * Np, 0.0);
+#pragma omp parallel
+    {
+        std::vector<double> pl;
+#pragma omp for schedule(static)
+        for (int i = 0; i < N; i++) {
+            const double lat = m.node_sph[(size_t)i * 2], lon = m.node_sph[(size_t)i * 2 + 1];
+            plm_bar(L, std::cos(kPi * 0.5 - lat), pl);
+            for (int mm = 0; mm <= L; mm++) {
+                for (int l = mm; l <= L; l++) P[(size_t)p_row(L, l, mm) * Np + i] = pl[(size_t)l * (l + 1) / 2 + mm];
+                trig[(size_t)(2 * mm) * Np + i] = std::cos((double)mm * lon);
+                trig[(size_t)(2 * mm + 1) * Np + i] = std::sin((double)mm * lon);
+            }
         }
+    }
+    // Gram matrix on the device from the full basis Y[K][Np] (FP64, setup only)
+    std::vector<double> G((size_t)K * K, 0.0);
+    {
+        std::vector<double> Yt((size_t)K * Np, 0.0);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < N; i++)
+            for (int mm = 0; mm <= L; mm++)
+                for (int l = mm; l <= L; l++) {
+                    const double p = P[(size_t)p_row(L, l, mm) * Np + i];
+                    Yt[(size_t)sh_col(l, mm, 0) * Np + i] = p * trig[(size_t)(2 * mm) * Np + i];
+                    if (mm > 0) Yt[(size_t)sh_col(l, mm, 1) * Np + i] = p * trig[(size_t)(2 * mm + 1) * Np + i];
+                }
+        double *dY = nullptr, *dG = nullptr;
+        if (cudaMalloc(&dY, sizeof(double) * Yt.size()) != cudaSuccess) return ODIS_ERR_NOMEM;
+        if (cudaMalloc(&dG, sizeof(double) * G.size()) != cudaSuccess) { cudaFree(dY); return ODIS_ERR_NOMEM; }
+        cudaMemcpy(dY, Yt.data(), sizeof(double) * Yt.size(), cudaMemcpyHostToDevice);
+        const int nt = (K + 31) / 32;
+        k_gram<<<dim3(nt, nt), 256>>>(dY, K, N, Np, dG);
+        const cudaError_t e = cudaMemcpy(G.data(), dG, sizeof(double) * G.size(), cudaMemcpyDeviceToHost);
+        cudaFree(dY);
+        cudaFree(dG);
+        if (e != cudaSuccess) return ODIS_ERR_CUDA;
+    }
     if (chol_inverse(G, K) != ODIS_OK) return ODIS_ERR_ARG;
-    // fold the per-degree factors (zero below degree 2)
     for (int l = 0; l <= L; l++)
         for (int a = l * l; a < (l + 1) * (l + 1); a++) {
             const double f = l >= 2 ? factors[l] : 0.0;
             for (int b = 0; b < K; b++) G[(size_t)a * K + b] *= f;
         }
+    // analysis tiles: (m, l0, nl) with nl <= kTileL
+    std::vector<int> tiles;
+    for (int mm = 0; mm <= L; mm++)
+        for (int l0 = mm; l0 <= L; l0 += kTileL) {
+            tiles.push_back(mm);
+            tiles.push_back(l0);
+            tiles.push_back(std::min(kTileL, L - l0 + 1));
+        }
     ShLoading* s = new ShLoading;
-    s->L = L; s->K = K; s->N = m.N; s->Np = Np; s->precision = precision;
-    std::vector<double> Yt((size_t)K * Np, 0.0);
-    for (int i = 0; i < m.N; i++)
-        for (int k = 0; k < K; k++) Yt[(size_t)k * Np + i] = Y[(size_t)i * K + k];
+    s->L = L; s->K = K; s->MP = MP; s->N = N; s->Np = Np; s->precision = precision;
+    s->ntiles = (int)tiles.size() / 3;
     bool ok = true;
-    auto up = [&](void** d, const void* h, size_t bytes) {
-        if (cudaMalloc(d, bytes) != cudaSuccess) { ok = false; *d = nullptr; return; }
-        if (h) cudaMemcpy(*d, h, bytes, cudaMemcpyHostToDevice);
-        else cudaMemset(*d, 0, bytes);
-    };
-    if (precision == ODIS_FP64) {
-        up((void**)&s->Y64, Yt.data(), sizeof(double) * Yt.size());
-        up((void**)&s->usg64, nullptr, sizeof(double) * Np);
-    } else if (precision == ODIS_DF64) {
-        std::vector<df64> Yd(Yt.size());
-        for (size_t q = 0; q < Yt.size(); q++) Yd[q] = df_from_double(Yt[q]);
-        up((void**)&s->Ydf, Yd.data(), sizeof(df64) * Yd.size());
-        up((void**)&s->usgdf, nullptr, sizeof(df64) * Np);
-    } else {
-        std::vector<float> Yf(Yt.begin(), Yt.end());
-        up((void**)&s->Y32, Yf.data(), sizeof(float) * Yf.size());
-        up((void**)&s->usg32, nullptr, sizeof(float) * Np);
-    }
-    up((void**)&s->FGinv, G.data(), sizeof(double) * G.size());
-    up((void**)&s->t, nullptr, sizeof(double) * K);
-    up((void**)&s->coef, nullptr, sizeof(double) * K);
+    if (precision == ODIS_FP64) ok = upload_rows<double>(&s->P, P) && upload_rows<double>(&s->trig, trig);
+    else if (precision == ODIS_DF64) ok = upload_rows<df64>(&s->P, P) && upload_rows<df64>(&s->trig, trig);
+    else ok = upload_rows<float>(&s->P, P) && upload_rows<float>(&s->trig, trig);
+    const size_t esz = precision == ODIS_FP32 ? sizeof(float) : sizeof(double);
+    ok = ok && cudaMalloc(&s->usg, esz * Np) == cudaSuccess && cudaMemset(s->usg, 0, esz * Np) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->tiles, sizeof(int) * tiles.size()) == cudaSuccess &&
+         cudaMemcpy(s->tiles, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->part, sizeof(double) * (size_t)K * kChunks) == cudaSuccess &&
+         cudaMemset(s->part, 0, sizeof(double) * (size_t)K * kChunks) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->FGinv, sizeof(double) * G.size()) == cudaSuccess &&
+         cudaMemcpy(s->FGinv, G.data(), sizeof(double) * G.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->t, sizeof(double) * K) == cudaSuccess && cudaMalloc(&s->coef, sizeof(double) * K) == cudaSuccess;
     if (!ok) { sh_destroy(s); return ODIS_ERR_NOMEM; }
     *out = s;
     return ODIS_OK;
@@ -307,31 +421,35 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
 void sh_destroy(ShLoading* s)
 {
     if (!s) return;
-    cudaFree(s->Y64); cudaFree(s->Y32); cudaFree(s->FGinv); cudaFree(s->t); cudaFree(s->coef);
-    cudaFree(s->usg64); cudaFree(s->usg32); cudaFree(s->Ydf); cudaFree(s->usgdf);
+    cudaFree(s->P); cudaFree(s->trig); cudaFree(s->tiles); cudaFree(s->part); cudaFree(s->FGinv);
+    cudaFree(s->t); cudaFree(s->coef); cudaFree(s->usg);
     delete s;
 }
 
-const double* sh_usg64(ShLoading* s) { return s ? s->usg64 : nullptr; }
-const float* sh_usg32(ShLoading* s) { return s ? s->usg32 : nullptr; }
-const float2* sh_usgdf(ShLoading* s) { return s ? s->usgdf : nullptr; }
+const double* sh_usg64(ShLoading* s) { return s && s->precision == ODIS_FP64 ? (const double*)s->usg : nullptr; }
+const float* sh_usg32(ShLoading* s) { return s && s->precision == ODIS_FP32 ? (const float*)s->usg : nullptr; }
+const float2* sh_usgdf(ShLoading* s) { return s && s->precision == ODIS_DF64 ? (const float2*)s->usg : nullptr; }
+
+template <class T>
+static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st)
+{
+    const T* P = (const T*)s->P;
+    const T* trig = (const T*)s->trig;
+    k_sh_analysis<T><<<dim3(s->ntiles, kChunks), kShThreads, 0, st>>>(P, trig, (const T*)eta, s->N, s->Np, s->L,
+                                                                       s->tiles, s->part);
+    k_sh_fold<<<(s->K + 127) / 128, 128, 0, st>>>(s->part, s->K, s->t);
+    k_sh_coef<<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, s->coef);
+    const int sb = (s->N * kSynthLanes + kSynthThreads - 1) / kSynthThreads;
+    k_sh_synth<T><<<sb, kSynthThreads, sizeof(T) * s->K, st>>>(P, trig, s->coef, s->N, s->Np, s->L, s->K, (T*)s->usg);
+}
 
 void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)
 {
-    const int sb = (s->N + kSynthThreads - 1) / kSynthThreads;
-    if (s->precision == ODIS_FP64) {
-        k_sh_analysis<double><<<s->K, kShThreads, 0, st>>>(s->Y64, (const double*)eta, s->N, s->Np, s->t);
-        k_sh_coef<<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, s->coef);
-        k_sh_synth<double><<<sb, kSynthThreads, sizeof(double) * s->K, st>>>(s->Y64, s->coef, s->N, s->Np, s->K, s->usg64);
-    } else if (s->precision == ODIS_DF64) {
-        k_sh_analysis_df<<<s->K, kShThreads, 0, st>>>(s->Ydf, (const df64*)eta, s->N, s->Np, s->t);
-        k_sh_coef<<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, s->coef);
-        k_sh_synth_df<<<sb, kSynthThreads, sizeof(df64) * s->K, st>>>(s->Ydf, s->coef, s->N, s->Np, s->K, s->usgdf);
-    } else {
-        k_sh_analysis<float><<<s->K, kShThreads, 0, st>>>(s->Y32, (const float*)eta, s->N, s->Np, s->t);
-        k_sh_coef<<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, s->coef);
-        k_sh_synth<float><<<sb, kSynthThreads, sizeof(float) * s->K, st>>>(s->Y32, s->coef, s->N, s->Np, s->K, s->usg32);
-    }
+    if (s->precision == ODIS_FP64) enqueue_t<double>(s, eta, st);
+    else if (s->precision == ODIS_DF64) enqueue_t<df64>(s, eta, st);
+    else enqueue_t<float>(s, eta, st);
 }
+
+int sh_kernels_per_step() { return 4; }
 
 }  // namespace odis

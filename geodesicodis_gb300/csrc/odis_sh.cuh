@@ -29,6 +29,8 @@ const float* sh_usg32(ShLoading* s);
 const float2* sh_usgdf(ShLoading* s);
 // enqueue analysis + synthesis of the current eta (double* or float*)
 void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t stream);
+// kernels launched by one sh_enqueue
+int sh_kernels_per_step();
 // host helpers for checks: real SH basis at the nodes, [N][K]
 void sh_basis_host(const Mesh& m, int lmax, std::vector<double>& Y);
 
