@@ -301,7 +301,27 @@ def main():
     ap.add_argument("--ref-sample-steps", type=int, default=40)
     ap.add_argument("--cpu-sample-steps", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", choices=["fp64", "df64", "fp32"], default=None,
+                    help="run a short level-6 case for an ncu capture (no timing, no JSON)")
+    ap.add_argument("--case-sh", type=int, default=0, help="self-gravity degree of --profile-case")
+    ap.add_argument("--case-steps", type=int, default=30)
+    ap.add_argument("--case-graph", action="store_true", help="--profile-case: force the graph-replayed kernels")
     args = ap.parse_args()
+    if args.profile_case:
+        import geodesicodis_gb300 as g
+        angvel, P, dt, n = g.derive_time(ANGVEL_IN, DT_TARGET)
+        mesh = g.Mesh.generate(LEVEL, RADIUS)
+        prec = {"fp64": g.FP64, "df64": g.DF64, "fp32": g.FP32}[args.profile_case]
+        p = g.make_params(radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt, potential=g.POT_ECC,
+                          precision=prec, sh_lmax=args.case_sh, sh_factors=sh_factors(args.case_sh) if args.case_sh else None)
+        sol = g.Solver(p, mesh)
+        if args.case_graph:
+            sol.set_persistent(False)
+        for _ in range(3):
+            sol.run(max(1, args.case_steps // 3))
+        sol.synchronize()
+        print("profile case done", sol.get_state()[0])
+        return
     if args.impl == "reference":
         out = run_reference(args)
         if out:

@@ -92,6 +92,7 @@ _SIGS = {
     "odis_set_state": ([_V, C.c_int, _D, _D, _D, _D], C.c_int),
     "odis_launch_count": ([_V, C.POINTER(C.c_longlong)], C.c_int),
     "odis_profile_kernels": ([_V, C.c_int, _D], C.c_int),
+    "odis_set_persistent": ([_V, C.c_int, _I], C.c_int),
 }
 
 
@@ -302,6 +303,14 @@ class Solver:
 
     def set_stream(self, stream_ptr: int) -> None:
         _ck(lib().odis_set_stream(self._h, C.c_void_p(stream_ptr)), "odis_set_stream")
+
+    def set_persistent(self, enable) -> bool:
+        """Use (True) or forbid (False) the persistent single-launch loop, or None for
+        the faster of the two paths as timed at creation; returns whether runs will use it."""
+        a = C.c_int()
+        flag = -1 if enable is None else int(bool(enable))
+        _ck(lib().odis_set_persistent(self._h, flag, C.byref(a)), "odis_set_persistent")
+        return bool(a.value)
 
     def launch_count(self) -> int:
         n = C.c_longlong()

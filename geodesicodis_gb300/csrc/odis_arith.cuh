@@ -1,0 +1,58 @@
+// Arithmetic policies shared by kernels templated on the method's number type:
+// double (FP64 method), float2 = df64 (double-float method), float (FP32 state).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "odis_df64.cuh"
+
+namespace odis {
+
+template <class T> struct Ar;
+template <> struct Ar<double> {
+    using V = double;
+    __device__ static V zero() { return 0.0; }
+    __device__ static V fma(V a, V b, V c) { return ::fma(a, b, c); }
+    __device__ static V mul(V a, V b) { return a * b; }
+    __device__ static V add(V a, V b) { return a + b; }
+    __device__ static V sub(V a, V b) { return a - b; }
+    __device__ static V neg(V a) { return -a; }
+    __device__ static V from(double x) { return x; }
+    __device__ static double to(V a) { return a; }
+    __device__ static V shfl(V a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
+    __device__ static bool finite(V a) { return (__double2hiint(a) & 0x7ff00000) != 0x7ff00000; }
+    __device__ static V ldcg(const V* p) { return __ldcg(p); }
+    __device__ static void stcg(V* p, V v) { __stcg(p, v); }
+};
+template <> struct Ar<float> {
+    using V = float;
+    __device__ static V zero() { return 0.f; }
+    __device__ static V fma(V a, V b, V c) { return fmaf(a, b, c); }
+    __device__ static V mul(V a, V b) { return a * b; }
+    __device__ static V add(V a, V b) { return a + b; }
+    __device__ static V sub(V a, V b) { return a - b; }
+    __device__ static V neg(V a) { return -a; }
+    __device__ static V from(double x) { return (float)x; }
+    __device__ static double to(V a) { return (double)a; }
+    __device__ static V shfl(V a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
+    __device__ static bool finite(V a) { return (__float_as_int(a) & 0x7f800000) != 0x7f800000; }
+    __device__ static V ldcg(const V* p) { return __ldcg(p); }
+    __device__ static void stcg(V* p, V v) { __stcg(p, v); }
+};
+template <> struct Ar<df64> {
+    using V = df64;
+    __device__ static V zero() { return df_make(0.f, 0.f); }
+    __device__ static V fma(V a, V b, V c) { return df_fma(a, b, c); }
+    __device__ static V mul(V a, V b) { return df_mul(a, b); }
+    __device__ static V add(V a, V b) { return df_add(a, b); }
+    __device__ static V sub(V a, V b) { return df_sub(a, b); }
+    __device__ static V neg(V a) { return df_neg(a); }
+    __device__ static V from(double x) { return df_from_double(x); }
+    __device__ static double to(V a) { return df_to_double(a); }
+    __device__ static V shfl(V a, int o) { return df_shfl_down(a, o); }
+    __device__ static bool finite(V a) { return df_finite(a); }
+    __device__ static V ldcg(const V* p) { return __ldcg(p); }
+    __device__ static void stcg(V* p, V v) { __stcg(p, v); }
+};
+
+}  // namespace odis

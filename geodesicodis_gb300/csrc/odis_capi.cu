@@ -11,6 +11,10 @@
 #include "odis_kernels.cuh"
 #include "odis_sh.cuh"
 #include "odis_df64.cuh"
+#include "odis_persistent.cuh"
+
+#include <algorithm>
+#include <chrono>
 
 #include <cuda_runtime.h>
 
@@ -91,6 +95,8 @@ struct odis_ctx {
     double* d_partial = nullptr;
     double* d_power = nullptr;
     int power_cap = 0;
+    void* d_phase = nullptr;     // forcing-phase table of the current run (method type)
+    int phase_cap = 0;
     long long iter = 0;
     std::vector<double> slot0_saved;    // reference history slot 0 before the first step
     StepConst sc{};
@@ -100,10 +106,20 @@ struct odis_ctx {
     double* stage[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t stage_n = 0;
     ShLoading* sh = nullptr;
+    PersistPlan plan{};          // persistent single-launch loop (FP64 / DF64 without self-gravity)
+    bool persist_ok = false;     // the plan fits one CTA per SM and cooperative launch is available
+    bool persist_on = true;      // odis_set_persistent
+    bool persist_auto = true;    // the faster path as timed by choose_exec_path at creation
+    double exec_ms[2] = {0, 0};  // those timings: graph-replayed pair, persistent loop (ms per step)
+    int part_cap = 0;            // steps the plan's partial buffer holds
+    double persist_frac = 0.0;   // fraction of faces interior to their CTA
     long long launches = 0;      // kernels of this library launched by this context
     ~odis_ctx() {
         if (graph) cudaGraphExecDestroy(graph);
         if (sh) sh_destroy(sh);
+        if (d_power) cudaFree(d_power);
+        if (d_phase) cudaFree(d_phase);
+        if (plan.part) cudaFree(plan.part);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
@@ -370,6 +386,111 @@ static int alloc_state(odis_ctx* c, State<T>& s, bool split)
     return ODIS_OK;
 }
 
+// Partition of faces and cells over one CTA per SM for the persistent loop,
+// with each CTA's producer sets (see odis_persistent.cu).  If the partition's
+// coefficients do not fit one CTA's shared memory, or the device cannot do a
+// cooperative launch, the context keeps to the graph-replayed two-kernel step.
+static int build_persist_plan(odis_ctx* c, const Mesh& m)
+{
+    int dev = 0, sms = 0, coop = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return ODIS_ERR_CUDA;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop || sms <= 0) return ODIS_OK;
+    const int P = sms, E = m.E, N = m.N;
+    if (E < 4 * P || N < 4 * P) return ODIS_OK;          // too small to partition usefully
+    std::vector<int> fstart(P + 1), cstart(P + 1), fown(E), cown(N);
+    for (int b = 0; b <= P; b++) {
+        fstart[b] = (int)((long long)E * b / P);
+        cstart[b] = (int)((long long)N * b / P);
+    }
+    int nf_max = 0, nc_max = 0;
+    for (int b = 0; b < P; b++) {
+        for (int e = fstart[b]; e < fstart[b + 1]; e++) fown[e] = b;
+        for (int i = cstart[b]; i < cstart[b + 1]; i++) cown[i] = b;
+        nf_max = std::max(nf_max, fstart[b + 1] - fstart[b]);
+        nc_max = std::max(nc_max, cstart[b + 1] - cstart[b]);
+    }
+    std::vector<int> aptr(P + 1, 0), cptr(P + 1, 0), alist, clist;
+    std::vector<int> mark(P, -1);
+    for (int b = 0; b < P; b++) {
+        auto add = [&](int q, std::vector<int>& lst) {
+            if (q != b && mark[q] != b) { mark[q] = b; lst.push_back(q); }
+        };
+        for (int e = fstart[b]; e < fstart[b + 1]; e++) {
+            for (int k = 0; k < m.interp_n[e]; k++) add(fown[m.interp_friends[(size_t)e * 10 + k]], alist);
+            add(cown[m.face_nodes[(size_t)e * 2]], alist);
+            add(cown[m.face_nodes[(size_t)e * 2 + 1]], alist);
+        }
+        aptr[b + 1] = (int)alist.size();
+        std::fill(mark.begin(), mark.end(), -1);
+        for (int i = cstart[b]; i < cstart[b + 1]; i++)
+            for (int k = 0; k < m.nfriends(i); k++) add(fown[m.faces[(size_t)i * 6 + k]], clist);
+        cptr[b + 1] = (int)clist.size();
+        std::fill(mark.begin(), mark.end(), -1);
+    }
+    // interior-first order inside each CTA: a face is interior when its TRiSK
+    // neighbours and both end cells are owned by its CTA, a cell when all its
+    // faces are
+    std::vector<int> forder(E), fpos(E), corder(N), cpos(N), fint(P), cint(P);
+    for (int b = 0; b < P; b++) {
+        int lo = fstart[b], hi = fstart[b + 1];
+        std::vector<int> in, bd;
+        for (int e = lo; e < hi; e++) {
+            bool interior = cown[m.face_nodes[(size_t)e * 2]] == b && cown[m.face_nodes[(size_t)e * 2 + 1]] == b;
+            for (int k = 0; k < m.interp_n[e] && interior; k++) interior = fown[m.interp_friends[(size_t)e * 10 + k]] == b;
+            (interior ? in : bd).push_back(e);
+        }
+        fint[b] = (int)in.size();
+        in.insert(in.end(), bd.begin(), bd.end());
+        for (int q = 0; q < (int)in.size(); q++) { forder[lo + q] = in[q]; fpos[in[q]] = q; }
+        lo = cstart[b]; hi = cstart[b + 1];
+        in.clear(); bd.clear();
+        for (int i = lo; i < hi; i++) {
+            bool interior = true;
+            for (int k = 0; k < m.nfriends(i) && interior; k++) interior = fown[m.faces[(size_t)i * 6 + k]] == b;
+            (interior ? in : bd).push_back(i);
+        }
+        cint[b] = (int)in.size();
+        in.insert(in.end(), bd.begin(), bd.end());
+        for (int q = 0; q < (int)in.size(); q++) { corder[lo + q] = in[q]; cpos[in[q]] = q; }
+    }
+    PersistPlan pl;
+    pl.P = P;
+    pl.nf_max = nf_max;
+    pl.nc_max = nc_max;
+    if (!persistent_fits(c->p.precision, pl, nullptr)) return ODIS_OK;
+    DevArena& A = c->mem;
+    if (alist.empty()) alist.push_back(0);
+    if (clist.empty()) clist.push_back(0);
+    pl.fstart = A.upload(fstart);
+    pl.cstart = A.upload(cstart);
+    pl.fint = A.upload(fint);
+    pl.cint = A.upload(cint);
+    pl.forder = A.upload(forder);
+    pl.corder = A.upload(corder);
+    pl.fpos = A.upload(fpos);
+    pl.cpos = A.upload(cpos);
+    pl.fowner = A.upload(fown);
+    pl.cowner = A.upload(cown);
+    pl.depA_ptr = A.upload(aptr);
+    pl.depA = A.upload(alist);
+    pl.depC_ptr = A.upload(cptr);
+    pl.depC = A.upload(clist);
+    pl.flag_e = A.alloc<unsigned>(P);
+    pl.flag_c = A.alloc<unsigned>(P);
+    if (!pl.fstart || !pl.cstart || !pl.fint || !pl.cint || !pl.forder || !pl.corder || !pl.fpos || !pl.cpos ||
+        !pl.fowner || !pl.cowner || !pl.depA_ptr || !pl.depA || !pl.depC_ptr || !pl.depC || !pl.flag_e || !pl.flag_c)
+        return ODIS_ERR_NOMEM;
+    c->persist_frac = 0.0;
+    for (int b = 0; b < P; b++) c->persist_frac += (double)fint[b] / E;
+    c->plan = pl;
+    c->persist_ok = true;
+    return ODIS_OK;
+}
+
+static int choose_exec_path(odis_ctx* c);
+
 extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, odis_ctx** out)
 {
     if (!p || !mp || !out) return ODIS_ERR_ARG;
@@ -468,6 +589,15 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     sc.df_a = df_from_double(sc.ab3a);
     sc.df_b = df_from_double(sc.ab3b);
     sc.df_c = df_from_double(sc.ab3c);
+    sc.f_dt = (float)p->dt;
+    sc.f_malpha = (float)(-p->alpha);
+    sc.f_a = (float)sc.ab3a;
+    sc.f_b = (float)sc.ab3b;
+    sc.f_c = (float)sc.ab3c;
+    if ((p->precision == ODIS_FP64 || p->precision == ODIS_DF64) && p->sh_lmax == 0) {
+        st = build_persist_plan(c.get(), m);
+        if (st != ODIS_OK) return st;
+    }
     c->stage_n = (size_t)3 * std::max(c->Ep, c->Np);
     for (int k = 0; k < 4; k++) {
         c->stage[k] = A.alloc<double>(c->stage_n);
@@ -475,6 +605,8 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     }
     c->slot0_saved.assign((size_t)(m.E + m.N), 0.0);
     if (cudaDeviceSynchronize() != cudaSuccess) return ODIS_ERR_CUDA;
+    st = choose_exec_path(c.get());
+    if (st != ODIS_OK) return st;
     *out = c.release();
     return ODIS_OK;
 }
@@ -666,6 +798,29 @@ static int ensure_graph(odis_ctx* c)
     return ODIS_OK;
 }
 
+// Forcing-phase table for steps first .. first+n-1 (grown as needed; a new
+// buffer invalidates the instantiated graph, which bakes in the pointer).
+static int prepare_phase(odis_ctx* c, long long first, int n)
+{
+    const size_t esz = c->p.precision == ODIS_FP32 ? sizeof(float) : c->p.precision == ODIS_DF64 ? sizeof(float2)
+                                                                                              : sizeof(double);
+    if (n > c->phase_cap) {
+        if (c->d_phase) cudaFree(c->d_phase);
+        c->d_phase = nullptr;
+        c->phase_cap = 0;
+        const int cap = std::max(n, 4096);
+        ODIS_CK(cudaMalloc(&c->d_phase, esz * 2 * (size_t)cap));
+        c->phase_cap = cap;
+        c->s64.phase = (const double*)c->d_phase;
+        c->s32.phase = (const float*)c->d_phase;
+        c->sdf.phase = (const float2*)c->d_phase;
+        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    }
+    launch_phase(c->d_phase, c->p.precision, first, n, c->p.dt, c->p.angvel, c->stream);
+    c->launches += 1;
+    return cudaGetLastError() == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
+}
+
 extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem)
 {
     if (!c || n < 0 || !mem_ok(mem)) return ODIS_ERR_ARG;
@@ -689,26 +844,57 @@ extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem
     const long long first = c->iter;
     ODIS_CK(cudaMemcpyAsync(c->d_run_first, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
     ODIS_CK(cudaMemcpyAsync(c->d_iter, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    {
+        const int st = prepare_phase(c, first, n);
+        if (st != ODIS_OK) return st;
+    }
     if (c->s64.power != dpow || c->s32.power != dpow || c->sdf.power != dpow) {
         c->s64.power = dpow;
         c->s32.power = dpow;
         c->sdf.power = dpow;
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     }
-    int done = 0;
-    if (n >= kGraphSteps) {
-        int st = ensure_graph(c);
-        if (st != ODIS_OK) return st;
-        for (; done + kGraphSteps <= n; done += kGraphSteps) {
-            ODIS_CK(cudaGraphLaunch(c->graph, c->stream));
-            c->launches += (long long)kGraphSteps * kernels_per_step(c) + 1;
+    bool persisted = false;
+    if (c->persist_ok && c->persist_on) {
+        // one cooperative launch for the whole run
+        if (n + 1 > c->part_cap) {
+            if (c->plan.part) cudaFree(c->plan.part);
+            c->plan.part = nullptr;
+            c->part_cap = 0;
+            const int cap = std::max(n + 1, 4097);
+            ODIS_CK(cudaMalloc(&c->plan.part, sizeof(double) * (size_t)cap * c->plan.P));
+            c->part_cap = cap;
+        }
+        const void* fc = c->p.precision == ODIS_FP64 ? (const void*)&c->op64.fc : (const void*)&c->opdf.fc;
+        const void* cc = c->p.precision == ODIS_FP64 ? (const void*)&c->op64.cc : (const void*)&c->opdf.cc;
+        const void* stp = c->p.precision == ODIS_FP64 ? (const void*)&c->s64 : (const void*)&c->sdf;
+        const int st = launch_persistent(c->p.precision, fc, cc, stp, c->sc, c->plan, n, first, dpow, c->stream);
+        if (st == ODIS_OK) {
+            persisted = true;
+            c->launches += 2;
+        } else {
+            // the device refused the cooperative launch (e.g. SMs taken by other
+            // work): nothing ran, keep to the graph-replayed step from now on
+            cudaGetLastError();
+            c->persist_ok = false;
         }
     }
-    if (done < n) enqueue_steps(c, n - done);
-    if (c->p.precision == ODIS_FP64) launch_power_tail<double>(c->op64.fc, c->s64, c->sc, c->stream);
-    else if (c->p.precision == ODIS_FP32) launch_power_tail<float>(c->op32.fc, c->s32, c->sc, c->stream);
-    else launch_power_tail_df(c->opdf.fc, c->sdf, c->sc, c->stream);
-    c->launches += 2;
+    if (!persisted) {
+        int done = 0;
+        if (n >= kGraphSteps) {
+            int st = ensure_graph(c);
+            if (st != ODIS_OK) return st;
+            for (; done + kGraphSteps <= n; done += kGraphSteps) {
+                ODIS_CK(cudaGraphLaunch(c->graph, c->stream));
+                c->launches += (long long)kGraphSteps * kernels_per_step(c) + 1;
+            }
+        }
+        if (done < n) enqueue_steps(c, n - done);
+        if (c->p.precision == ODIS_FP64) launch_power_tail<double>(c->op64.fc, c->s64, c->sc, c->stream);
+        else if (c->p.precision == ODIS_FP32) launch_power_tail<float>(c->op32.fc, c->s32, c->sc, c->stream);
+        else launch_power_tail_df(c->opdf.fc, c->sdf, c->sc, c->stream);
+        c->launches += 2;
+    }
     ODIS_CK(cudaGetLastError());
     if (power && mem == ODIS_MEM_HOST)
         ODIS_CK(cudaMemcpyAsync(power, dpow, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
@@ -717,6 +903,7 @@ extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem
     int h = 0;
     ODIS_CK(cudaMemcpy(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
     if (h) ODIS_CK(cudaMemset(c->d_status, 0, sizeof(int)));
+    if (h & (1 << ODIS_ERR_TIMEOUT)) return ODIS_ERR_TIMEOUT;
     if (h & (1 << ODIS_ERR_NONFINITE)) return ODIS_ERR_NONFINITE;
     return ODIS_OK;
 }
@@ -836,6 +1023,35 @@ extern "C" odis_status odis_set_state(odis_ctx* c, int iter, const double* v, co
                                        : set_state_t<float>(c, c->s32, iter, v, eta, dvdt, detadt);
 }
 
+// Times the persistent loop against the graph-replayed kernel pair (best of two
+// runs of 3 graph chunks each, after one warm-up run of each, host clock around
+// the synchronising run call), keeps the faster one as the default and puts the
+// context back in its freshly created state (zero state, step 0, no launches).
+static int choose_exec_path(odis_ctx* c)
+{
+    if (!c->persist_ok) return ODIS_OK;
+    const int n = 3 * kGraphSteps;
+    double best[2] = {1e300, 1e300};
+    for (int rep = 0; rep < 3; rep++) {
+        for (int mode = 0; mode < 2 && c->persist_ok; mode++) {
+            c->persist_on = mode == 1;
+            const auto t0 = std::chrono::steady_clock::now();
+            const int st = odis_run_steps(c, n, nullptr, ODIS_MEM_DEVICE);
+            const auto t1 = std::chrono::steady_clock::now();
+            // a NaN from an unstable dt is the caller's to find on a real run
+            if (st == ODIS_ERR_TIMEOUT && mode == 1) { c->persist_ok = false; break; }
+            if (st != ODIS_OK && st != ODIS_ERR_NONFINITE) return st;
+            if (rep > 0) best[mode] = std::min(best[mode], std::chrono::duration<double, std::milli>(t1 - t0).count() / n);
+        }
+    }
+    c->exec_ms[0] = best[0];
+    c->exec_ms[1] = best[1];
+    c->persist_auto = c->persist_ok && best[1] < best[0];
+    c->persist_on = c->persist_auto;
+    c->launches = 0;
+    return odis_set_state(c, 0, nullptr, nullptr, nullptr, nullptr);
+}
+
 // ---------------------------------------------------------------------------
 // measurement helpers
 // ---------------------------------------------------------------------------
@@ -853,6 +1069,14 @@ extern "C" odis_status odis_launch_count(odis_ctx* c, long long* n)
 extern "C" odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms)
 {
     if (!c || reps <= 0 || !ms) return ODIS_ERR_ARG;
+    // the kernels below run at step offset 2 of a run starting at the current step
+    const long long first = c->iter;
+    ODIS_CK(cudaMemcpyAsync(c->d_run_first, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    ODIS_CK(cudaMemcpyAsync(c->d_iter, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    {
+        const int pst = prepare_phase(c, first, 8);
+        if (pst != ODIS_OK) return pst;
+    }
     ODIS_CK(cudaStreamSynchronize(c->stream));
     cudaEvent_t a, b;
     ODIS_CK(cudaEventCreate(&a));
@@ -897,4 +1121,12 @@ extern "C" odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms)
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     return st;
+}
+
+extern "C" odis_status odis_set_persistent(odis_ctx* c, int enable, int* active)
+{
+    if (!c || enable < -1 || enable > 1) return ODIS_ERR_ARG;
+    c->persist_on = enable < 0 ? c->persist_auto : enable != 0;
+    if (active) *active = (c->persist_ok && c->persist_on) ? 1 : 0;
+    return ODIS_OK;
 }

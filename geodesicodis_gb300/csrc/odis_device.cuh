@@ -47,6 +47,8 @@ struct StepConst {
     int use_sg;               // 1: add the self-gravity / loading potential
     // the same constants as double-float (hi, lo) pairs for the ODIS_DF64 method
     float2 df_dt, df_malpha, df_a, df_b, df_c;
+    // and rounded to FP32 for the FP32-state variant (no per-thread conversions)
+    float f_dt, f_malpha, f_a, f_b, f_c;
 };
 
 // Mutable state of one instance.  The time level of v alternates between
@@ -68,6 +70,7 @@ struct State {
     const T* usg;        // [N] self-gravity potential / g (nullable)
     const long long* iter;   // device step counter (base of the current chunk)
     const long long* run_first;  // first step index of the current run
+    const T* phase;      // [2n] cos, sin of the forcing phase Omega*t^{n+1} for each step of the current run
     double* partial;     // [edge blocks] per-block dissipation partial sums
     double* power;       // [n] output power series of the current run (nullable)
     int* status;         // device status word

@@ -20,6 +20,7 @@
 // then one warp summing the per-block partials in block order.
 #include "../../include/odis_gpu.h"
 #include "odis_device.cuh"
+#include "odis_df64.cuh"
 #include "odis_kernels.cuh"
 
 #include <cmath>
@@ -64,6 +65,11 @@ __device__ __forceinline__ double fold_partials(const double* p, int n)
     return warp_sum(s);
 }
 
+// step constants in the kernel's type: the double itself, or its FP32 copy
+template <class T> __device__ __forceinline__ T kc(double d, float f);
+template <> __device__ __forceinline__ double kc<double>(double d, float) { return d; }
+template <> __device__ __forceinline__ float kc<float>(double, float f) { return f; }
+
 // finiteness from the exponent bits (integer pipe, no FP64 compare)
 __device__ __forceinline__ bool finite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
 
@@ -93,20 +99,14 @@ __device__ __forceinline__ double block_power(T pw, double* smem)
 template <class T, bool kMaster>
 __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, State<T> st, StepConst sc, int offset)
 {
-    __shared__ double s_cs[2];
     __shared__ double s_red[kStepThreads / 32];
     const long long it = *st.iter + offset;
-    if (threadIdx.x == 0) {
-        // forcing phase at t^{n+1} = dt*n + dt, as src/timeIntegrator.cpp:218
-        double t = sc.dt * (double)it + sc.dt, s, c;
-        sincos(sc.angvel * t, &s, &c);
-        s_cs[0] = c;
-        s_cs[1] = s;
-    }
-    __syncthreads();
+    // forcing phase at t^{n+1} (precomputed per run by k_phase)
+    const long long kstep = it - *st.run_first;
+    const T cosM = st.phase[2 * kstep], sinM = st.phase[2 * kstep + 1];
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int Ep = sc.Ep;
-    const T* __restrict__ vin = st.v[it & 1];
+    const T* __restrict__ vin = ((it & 1) ? st.v[1] : st.v[0]);
     T pw = T(0);
     if (e < sc.E) {
         T tsum = T(0);
@@ -119,27 +119,28 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, Stat
         const T g0 = __ldg(&fc.gg0[e]), g1 = __ldg(&fc.gg1[e]);
         const T f0 = fmaT<T>(__ldg(&fc.cor[e]), tsum, fmaT<T>(g0, st.eta[i0], g1 * st.eta[i1]));
         // forcing gradient G U(t^{n+1}) (+ self-gravity), then linear drag
-        T gu = fmaT<T>((T)s_cs[0], __ldg(&fc.fP[e]), (T)s_cs[1] * __ldg(&fc.fQ[e]));
+        T gu = fmaT<T>(cosM, __ldg(&fc.fP[e]), sinM * __ldg(&fc.fQ[e]));
         if (sc.use_sg) gu -= fmaT<T>(g0, st.usg[i0], g1 * st.usg[i1]);
-        const T drag = fmaT<T>((T)(-sc.alpha), ve, gu);
-        T* hcur = st.hv[it & 1];
+        const T kdt = kc<T>(sc.dt, sc.f_dt);
+        const T drag = fmaT<T>(kc<T>(-sc.alpha, sc.f_malpha), ve, gu);
+        T* hcur = ((it & 1) ? st.hv[1] : st.hv[0]);
         T inc = f0;
         if (sc.init_load || it > 1) {
-            const T f1 = st.hv[(it + 1) & 1][e];
+            const T f1 = ((it & 1) ? st.hv[0] : st.hv[1])[e];
             const T f2 = hcur[e];
-            inc = fmaT<T>((T)sc.ab3c, f2, fmaT<T>((T)sc.ab3b, f1, (T)sc.ab3a * f0));
+            inc = fmaT<T>(kc<T>(sc.ab3c, sc.f_c), f2, fmaT<T>(kc<T>(sc.ab3b, sc.f_b), f1, kc<T>(sc.ab3a, sc.f_a) * f0));
         }
         hcur[e] = f0;
         if constexpr (kMaster) {
             // FP32 increment, FP64 accumulation in the master copy
-            const double vm = st.vm[e] + (double)((T)sc.dt * (inc + drag));
+            const double vm = st.vm[e] + (double)(kdt * (inc + drag));
             st.vm[e] = vm;
-            st.v[(it + 1) & 1][e] = (T)vm;
+            ((it & 1) ? st.v[0] : st.v[1])[e] = (T)vm;
             if (!finite_bits(vm)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
         } else {
-            T vn = fmaT<T>(inc, (T)sc.dt, ve);
-            vn = fmaT<T>((T)sc.dt, drag, vn);
-            st.v[(it + 1) & 1][e] = vn;
+            T vn = fmaT<T>(inc, kdt, ve);
+            vn = fmaT<T>(kdt, drag, vn);
+            ((it & 1) ? st.v[0] : st.v[1])[e] = vn;
             if (!finite_bits((double)vn)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
         }
     }
@@ -156,25 +157,26 @@ __global__ void __launch_bounds__(kStepThreads) k_cell_step(CellCoef<T> cc, Stat
     const long long it = *st.iter + offset;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int Np = sc.Np;
-    const T* __restrict__ vn = st.v[(it + 1) & 1];
+    const T* __restrict__ vn = ((it & 1) ? st.v[0] : st.v[1]);
     if (i < sc.N) {
         T q = T(0);
 #pragma unroll
         for (int k = 0; k < kCellFaces; k++) q = fmaT<T>(__ldg(&cc.hw[k * Np + i]), vn[__ldg(&cc.edge[k * Np + i])], q);
-        T* hcur = st.he[it & 1];
+        T* hcur = ((it & 1) ? st.he[1] : st.he[0]);
+        const T kdt = kc<T>(sc.dt, sc.f_dt);
         T inc = q;
         if (sc.init_load || it > 1) {
-            const T f1 = st.he[(it + 1) & 1][i];
+            const T f1 = ((it & 1) ? st.he[0] : st.he[1])[i];
             const T f2 = hcur[i];
-            inc = fmaT<T>((T)sc.ab3c, f2, fmaT<T>((T)sc.ab3b, f1, (T)sc.ab3a * q));
+            inc = fmaT<T>(kc<T>(sc.ab3c, sc.f_c), f2, fmaT<T>(kc<T>(sc.ab3b, sc.f_b), f1, kc<T>(sc.ab3a, sc.f_a) * q));
         }
         hcur[i] = q;
         if constexpr (kMaster) {
-            const double em = st.etam[i] + (double)((T)sc.dt * inc);
+            const double em = st.etam[i] + (double)(kdt * inc);
             st.etam[i] = em;
             st.eta[i] = (T)em;
         } else {
-            st.eta[i] = fmaT<T>(inc, (T)sc.dt, st.eta[i]);
+            st.eta[i] = fmaT<T>(inc, kdt, st.eta[i]);
         }
     }
     // dissipation of v^n (the state this step started from) = power of step n-1
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial(FaceCoef<T> fc, 
     const long long it = *st.iter;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int Ep = sc.Ep;
-    const T* __restrict__ vin = st.v[it & 1];
+    const T* __restrict__ vin = ((it & 1) ? st.v[1] : st.v[0]);
     double pw = 0.0;
     if (e < sc.E) {
         T tsum = T(0);
@@ -217,6 +219,33 @@ __global__ void k_power_tail(State<T> st, int n_partial)
 __global__ void k_bump_iter(long long* iter, int n)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) *iter += n;
+}
+
+template <class T> __device__ __forceinline__ T from_double_dev(double x) { return (T)x; }
+template <> __device__ __forceinline__ float2 from_double_dev<float2>(double x) { return df_from_double(x); }
+
+// cos, sin of the forcing phase Omega * t^{n+1}, t^{n+1} = dt*n + dt
+// (src/timeIntegrator.cpp:218), for the steps first .. first+n-1, stored in
+// the method's own number type; one thread per step, so no step's critical
+// path carries a serial FP64 sincos.
+template <class T>
+__global__ void k_phase(T* out, long long first, int n, double dt, double angvel)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double t = dt * (double)(first + k) + dt;
+    double s, c;
+    sincos(angvel * t, &s, &c);
+    out[2 * k] = from_double_dev<T>(c);
+    out[2 * k + 1] = from_double_dev<T>(s);
+}
+
+void launch_phase(void* out, int precision, long long first, int n, double dt, double angvel, cudaStream_t s)
+{
+    const int nb = (n + 255) / 256;
+    if (precision == ODIS_FP64) k_phase<double><<<nb, 256, 0, s>>>((double*)out, first, n, dt, angvel);
+    else if (precision == ODIS_FP32) k_phase<float><<<nb, 256, 0, s>>>((float*)out, first, n, dt, angvel);
+    else k_phase<float2><<<nb, 256, 0, s>>>((float2*)out, first, n, dt, angvel);
 }
 
 // ---------------------------------------------------------------------------

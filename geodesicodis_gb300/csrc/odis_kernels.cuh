@@ -17,6 +17,8 @@ void launch_step(const FaceCoef<T>& fc, const CellCoef<T>& cc, const State<T>& s
 template <class T>
 void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, cudaStream_t s);
 void launch_bump(long long* iter, int n, cudaStream_t s);
+// forcing-phase table of a run: out[2k], out[2k+1] = cos, sin of Omega*(dt*(first+k) + dt)
+void launch_phase(void* out, int precision, long long first, int n, double dt, double angvel, cudaStream_t s);
 
 // ODIS_DF64 method (odis_kernels_df.cu)
 void launch_edge_df(const FaceCoef<float2>& fc, const State<float2>& st, const StepConst& sc, int offset, cudaStream_t s);

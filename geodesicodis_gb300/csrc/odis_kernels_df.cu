@@ -44,19 +44,13 @@ __device__ __forceinline__ df64 ldg2(const df64* p) { return __ldg(p); }
 
 __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc, State<df64> st, StepConst sc, int offset)
 {
-    __shared__ df64 s_cs[2];
     __shared__ df64 s_red[kStepThreads / 32];
     const long long it = *st.iter + offset;
-    if (threadIdx.x == 0) {
-        double t = sc.dt * (double)it + sc.dt, s, c;     // forcing phase at t^{n+1}
-        sincos(sc.angvel * t, &s, &c);
-        s_cs[0] = df_from_double(c);
-        s_cs[1] = df_from_double(s);
-    }
-    __syncthreads();
+    const long long kstep = it - *st.run_first;        // forcing phase at t^{n+1}, precomputed per run
+    const df64 cosM = st.phase[2 * kstep], sinM = st.phase[2 * kstep + 1];
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int Ep = sc.Ep;
-    const df64* __restrict__ vin = st.v[it & 1];
+    const df64* __restrict__ vin = ((it & 1) ? st.v[1] : st.v[0]);
     df64 pw = df_make(0.f, 0.f);
     if (e < sc.E) {
         df64 tsum = df_make(0.f, 0.f);
@@ -67,20 +61,20 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc
         pw = df_mul(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)));
         const df64 g0 = ldg2(&fc.gg0[e]), g1 = ldg2(&fc.gg1[e]);
         const df64 f0 = df_fma(ldg2(&fc.cor[e]), tsum, df_fma(g0, st.eta[i0], df_mul(g1, st.eta[i1])));
-        df64 gu = df_fma(s_cs[0], ldg2(&fc.fP[e]), df_mul(s_cs[1], ldg2(&fc.fQ[e])));
+        df64 gu = df_fma(cosM, ldg2(&fc.fP[e]), df_mul(sinM, ldg2(&fc.fQ[e])));
         if (sc.use_sg) gu = df_sub(gu, df_fma(g0, st.usg[i0], df_mul(g1, st.usg[i1])));
         const df64 drag = df_fma(sc.df_malpha, ve, gu);
-        df64* hcur = st.hv[it & 1];
+        df64* hcur = ((it & 1) ? st.hv[1] : st.hv[0]);
         df64 inc = f0;
         if (sc.init_load || it > 1) {
-            const df64 f1 = st.hv[(it + 1) & 1][e];
+            const df64 f1 = ((it & 1) ? st.hv[0] : st.hv[1])[e];
             const df64 f2 = hcur[e];
             inc = df_fma(sc.df_c, f2, df_fma(sc.df_b, f1, df_mul(sc.df_a, f0)));
         }
         hcur[e] = f0;
         df64 vn = df_fma(inc, sc.df_dt, ve);
         vn = df_fma(sc.df_dt, drag, vn);
-        st.v[(it + 1) & 1][e] = vn;
+        ((it & 1) ? st.v[0] : st.v[1])[e] = vn;
         if (!df_finite(vn)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
     }
     const double bs = block_sum_df(pw, s_red);
@@ -93,15 +87,15 @@ __global__ void __launch_bounds__(kStepThreads) k_cell_step_df(CellCoef<df64> cc
     const long long it = *st.iter + offset;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int Np = sc.Np;
-    const df64* __restrict__ vn = st.v[(it + 1) & 1];
+    const df64* __restrict__ vn = ((it & 1) ? st.v[0] : st.v[1]);
     if (i < sc.N) {
         df64 q = df_make(0.f, 0.f);
 #pragma unroll
         for (int k = 0; k < kCellFaces; k++) q = df_fma(ldg2(&cc.hw[k * Np + i]), vn[__ldg(&cc.edge[k * Np + i])], q);
-        df64* hcur = st.he[it & 1];
+        df64* hcur = ((it & 1) ? st.he[1] : st.he[0]);
         df64 inc = q;
         if (sc.init_load || it > 1) {
-            const df64 f1 = st.he[(it + 1) & 1][i];
+            const df64 f1 = ((it & 1) ? st.he[0] : st.he[1])[i];
             const df64 f2 = hcur[i];
             inc = df_fma(sc.df_c, f2, df_fma(sc.df_b, f1, df_mul(sc.df_a, q)));
         }
@@ -123,7 +117,7 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64
     const long long it = *st.iter;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int Ep = sc.Ep;
-    const df64* __restrict__ vin = st.v[it & 1];
+    const df64* __restrict__ vin = ((it & 1) ? st.v[1] : st.v[0]);
     df64 pw = df_make(0.f, 0.f);
     if (e < sc.E) {
         df64 tsum = df_make(0.f, 0.f);

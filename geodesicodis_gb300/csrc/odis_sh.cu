@@ -33,8 +33,7 @@ namespace {
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993751058;
 constexpr int kShThreads = 256;
 constexpr int kSynthThreads = 128;
-constexpr int kTileL = 8;          // degrees per analysis block
-constexpr int kChunks = 16;        // cell chunks of the analysis
+constexpr int kMaxChunks = 64;     // largest cell-chunk count the autotuner tries
 
 // fully normalised (4pi) associated Legendre functions with the Condon-Shortley
 // phase, P[l(l+1)/2 + m], argument z = cos(colatitude)
@@ -103,16 +102,17 @@ template <> struct Ar<df64> {
 
 // partial[k][chunk] = sum over the chunk's cells of Pbar_lm (cos|sin)(m lon) eta,
 // for the degrees l0 .. l0+nl-1 of order m of this block's tile
-template <class T>
+template <class T, int kTileL>
 __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict__ P, const T* __restrict__ trig,
                                                             const T* __restrict__ eta, int N, int Np, int L,
-                                                            const int* __restrict__ tiles, double* __restrict__ part)
+                                                            const int* __restrict__ tiles, int nchunk,
+                                                            T* __restrict__ part)
 {
     using A = Ar<T>;
-    __shared__ double red[kShThreads / 32][2 * kTileL];
+    __shared__ T red[kShThreads / 32][2 * kTileL];
     const int m = tiles[3 * blockIdx.x], l0 = tiles[3 * blockIdx.x + 1], nl = tiles[3 * blockIdx.x + 2];
     const int chunk = blockIdx.y;
-    const int per = (N + kChunks - 1) / kChunks;
+    const int per = (N + nchunk - 1) / nchunk;
     const int i0 = chunk * per, i1 = min(N, i0 + per);
     T ac[kTileL], as[kTileL];
 #pragma unroll
@@ -139,31 +139,35 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
             T c = ac[j], s = as[j];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) { c = A::add(c, A::shfl(c, o)); s = A::add(s, A::shfl(s, o)); }
-            if (lane == 0) { red[wid][2 * j] = A::to(c); red[wid][2 * j + 1] = A::to(s); }
+            if (lane == 0) { red[wid][2 * j] = c; red[wid][2 * j + 1] = s; }
         }
     }
     __syncthreads();
     if (threadIdx.x < 2 * nl) {
-        double s = 0.0;
-        for (int w = 0; w < kShThreads / 32; w++) s += red[w][threadIdx.x];
+        T s = A::zero();
+        for (int w = 0; w < kShThreads / 32; w++) s = A::add(s, red[w][threadIdx.x]);
         const int j = threadIdx.x >> 1, is_sin = threadIdx.x & 1;
-        if (m > 0 || !is_sin) part[(size_t)sh_col(l0 + j, m, is_sin) * kChunks + chunk] = s;
+        if (m > 0 || !is_sin) part[(size_t)sh_col(l0 + j, m, is_sin) * nchunk + chunk] = s;
     }
 }
 
-// t_k = sum over chunks in a fixed order
-__global__ void k_sh_fold(const double* __restrict__ part, int K, double* __restrict__ t)
+// t_k = sum over chunks in a fixed order (in the method's arithmetic; one
+// conversion to FP64 per coefficient)
+template <class T>
+__global__ void k_sh_fold(const T* __restrict__ part, int K, int nchunk, double* __restrict__ t)
 {
+    using A = Ar<T>;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
-    double s = 0.0;
-    for (int c = 0; c < kChunks; c++) s += part[(size_t)k * kChunks + c];
-    t[k] = s;
+    T s = A::zero();
+    for (int c = 0; c < nchunk; c++) s = A::add(s, part[(size_t)k * nchunk + c]);
+    t[k] = A::to(s);
 }
 
-// c = (F G^-1) t: one warp per coefficient
+// c = (F G^-1) t in FP64, one warp per coefficient, stored in the method's type
+template <class T>
 __global__ void __launch_bounds__(32) k_sh_coef(const double* __restrict__ t, int K, const double* __restrict__ FGinv,
-                                                double* __restrict__ coef)
+                                                T* __restrict__ coef)
 {
     const int a = blockIdx.x;
     const double* row = FGinv + (size_t)a * K;
@@ -171,24 +175,22 @@ __global__ void __launch_bounds__(32) k_sh_coef(const double* __restrict__ t, in
     for (int b = threadIdx.x; b < K; b += 32) s = fma(row[b], t[b], s);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (threadIdx.x == 0) coef[a] = s;
+    if (threadIdx.x == 0) coef[a] = Ar<T>::from(s);
 }
 
 // usg_i = sum_{m} [cos(m lon) sum_{l>=max(m,2)} Pbar_lm c_lm,cos + sin(m lon) sum_l Pbar_lm c_lm,sin]
 // kSynthLanes consecutive threads share a cell and split the orders m between
 // them (m = j, j + kSynthLanes, ...); their sums meet by shuffles in a fixed
 // order.  Two independent accumulator pairs keep two loads in flight per lane.
-constexpr int kSynthLanes = 4;
-
-template <class T>
+template <class T, int kSynthLanes>
 __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict__ P, const T* __restrict__ trig,
-                                                            const double* __restrict__ coef, int N, int Np, int L, int K,
+                                                            const T* __restrict__ coef, int N, int Np, int L, int K,
                                                             T* __restrict__ usg)
 {
     using A = Ar<T>;
     extern __shared__ unsigned char c_raw[];
     T* c = reinterpret_cast<T*>(c_raw);
-    for (int k = threadIdx.x; k < K; k += kSynthThreads) c[k] = A::from(coef[k]);
+    for (int k = threadIdx.x; k < K; k += kSynthThreads) c[k] = coef[k];
     __syncthreads();
     const int gt = blockIdx.x * kSynthThreads + threadIdx.x;
     const int i = gt / kSynthLanes, j = gt % kSynthLanes;
@@ -253,15 +255,18 @@ __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ Y, int 
 
 }  // namespace
 
+int sh_autotune(ShLoading* s);
+
 struct ShLoading {
     int L = 0, K = 0, MP = 0, N = 0, Np = 0, precision = ODIS_FP64, ntiles = 0;
+    int tl = 8, nchunk = 16, lanes = 4;   // tile shapes chosen by the autotuner
     void* P = nullptr;           // [MP][Np] Legendre rows, method type
     void* trig = nullptr;        // [2(L+1)][Np] cos(m lon), sin(m lon), method type
     int* tiles = nullptr;        // [ntiles][3] (m, l0, nl)
-    double* part = nullptr;      // [K][kChunks]
+    void* part = nullptr;        // [K][nchunk] chunk partials, method type
     double* FGinv = nullptr;     // [K][K]
     double* t = nullptr;
-    double* coef = nullptr;
+    void* coef = nullptr;        // [K] coefficients, method type
     void* usg = nullptr;         // [Np] method type
 };
 
@@ -389,31 +394,22 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
             const double f = l >= 2 ? factors[l] : 0.0;
             for (int b = 0; b < K; b++) G[(size_t)a * K + b] *= f;
         }
-    // analysis tiles: (m, l0, nl) with nl <= kTileL
-    std::vector<int> tiles;
-    for (int mm = 0; mm <= L; mm++)
-        for (int l0 = mm; l0 <= L; l0 += kTileL) {
-            tiles.push_back(mm);
-            tiles.push_back(l0);
-            tiles.push_back(std::min(kTileL, L - l0 + 1));
-        }
     ShLoading* s = new ShLoading;
     s->L = L; s->K = K; s->MP = MP; s->N = N; s->Np = Np; s->precision = precision;
-    s->ntiles = (int)tiles.size() / 3;
     bool ok = true;
     if (precision == ODIS_FP64) ok = upload_rows<double>(&s->P, P) && upload_rows<double>(&s->trig, trig);
     else if (precision == ODIS_DF64) ok = upload_rows<df64>(&s->P, P) && upload_rows<df64>(&s->trig, trig);
     else ok = upload_rows<float>(&s->P, P) && upload_rows<float>(&s->trig, trig);
     const size_t esz = precision == ODIS_FP32 ? sizeof(float) : sizeof(double);
     ok = ok && cudaMalloc(&s->usg, esz * Np) == cudaSuccess && cudaMemset(s->usg, 0, esz * Np) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->tiles, sizeof(int) * tiles.size()) == cudaSuccess &&
-         cudaMemcpy(s->tiles, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->part, sizeof(double) * (size_t)K * kChunks) == cudaSuccess &&
-         cudaMemset(s->part, 0, sizeof(double) * (size_t)K * kChunks) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->part, 8 * (size_t)K * kMaxChunks) == cudaSuccess &&
+         cudaMemset(s->part, 0, 8 * (size_t)K * kMaxChunks) == cudaSuccess;
     ok = ok && cudaMalloc(&s->FGinv, sizeof(double) * G.size()) == cudaSuccess &&
          cudaMemcpy(s->FGinv, G.data(), sizeof(double) * G.size(), cudaMemcpyHostToDevice) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->t, sizeof(double) * K) == cudaSuccess && cudaMalloc(&s->coef, sizeof(double) * K) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->t, sizeof(double) * K) == cudaSuccess && cudaMalloc(&s->coef, 8 * (size_t)K) == cudaSuccess;
     if (!ok) { sh_destroy(s); return ODIS_ERR_NOMEM; }
+    const int st = sh_autotune(s);
+    if (st != ODIS_OK) { sh_destroy(s); return st; }
     *out = s;
     return ODIS_OK;
 }
@@ -430,17 +426,129 @@ const double* sh_usg64(ShLoading* s) { return s && s->precision == ODIS_FP64 ? (
 const float* sh_usg32(ShLoading* s) { return s && s->precision == ODIS_FP32 ? (const float*)s->usg : nullptr; }
 const float2* sh_usgdf(ShLoading* s) { return s && s->precision == ODIS_DF64 ? (const float2*)s->usg : nullptr; }
 
+// analysis tiles (m, l0, nl) with nl <= tl
+static std::vector<int> make_tiles(int L, int tl)
+{
+    std::vector<int> tiles;
+    for (int mm = 0; mm <= L; mm++)
+        for (int l0 = mm; l0 <= L; l0 += tl) {
+            tiles.push_back(mm);
+            tiles.push_back(l0);
+            tiles.push_back(std::min(tl, L - l0 + 1));
+        }
+    return tiles;
+}
+
+template <class T>
+static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int ntiles, int nchunk, const void* eta,
+                            cudaStream_t st)
+{
+    const dim3 grid(ntiles, nchunk);
+    const T* P = (const T*)s->P;
+    const T* trig = (const T*)s->trig;
+    if (tl == 2) k_sh_analysis<T, 2><<<grid, kShThreads, 0, st>>>(P, trig, (const T*)eta, s->N, s->Np, s->L, tiles, nchunk, (T*)s->part);
+    else if (tl == 4) k_sh_analysis<T, 4><<<grid, kShThreads, 0, st>>>(P, trig, (const T*)eta, s->N, s->Np, s->L, tiles, nchunk, (T*)s->part);
+    else k_sh_analysis<T, 8><<<grid, kShThreads, 0, st>>>(P, trig, (const T*)eta, s->N, s->Np, s->L, tiles, nchunk, (T*)s->part);
+}
+
+template <class T>
+static void launch_synth(const ShLoading* s, int lanes, cudaStream_t st)
+{
+    const int sb = (s->N * lanes + kSynthThreads - 1) / kSynthThreads;
+    const size_t sm = sizeof(T) * s->K;
+    const T* P = (const T*)s->P;
+    const T* trig = (const T*)s->trig;
+    const T* c = (const T*)s->coef;
+    T* u = (T*)s->usg;
+    if (lanes == 1) k_sh_synth<T, 1><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u);
+    else if (lanes == 2) k_sh_synth<T, 2><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u);
+    else if (lanes == 4) k_sh_synth<T, 4><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u);
+    else k_sh_synth<T, 8><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u);
+}
+
+// Self-tuning of the transform tiles: every candidate is timed on this mesh
+// and this device (CUDA events, warm L2, median of three runs of 10 launches)
+// and the fastest is kept.  Results do not depend on the choice of the
+// synthesis lanes; the analysis's chunking changes only the order of the
+// partial sums.
+template <class T>
+static int autotune_t(ShLoading* s)
+{
+    void* eta = nullptr;
+    if (cudaMalloc(&eta, sizeof(T) * s->Np) != cudaSuccess) return ODIS_ERR_NOMEM;
+    cudaMemset(eta, 0, sizeof(T) * s->Np);
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    auto timeit = [&](auto&& body) {
+        float best = 1e30f;
+        body();
+        for (int r = 0; r < 3; r++) {
+            cudaEventRecord(a);
+            for (int q = 0; q < 10; q++) body();
+            cudaEventRecord(b);
+            cudaEventSynchronize(b);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            best = std::min(best, ms);
+        }
+        return best;
+    };
+    float best = 1e30f;
+    int best_tl = 8, best_ch = 16;
+    std::vector<int> best_tiles;
+    int* dt = nullptr;
+    cudaMalloc(&dt, sizeof(int) * 3 * (size_t)(s->L + 1) * (s->L + 1));
+    for (int tl : {2, 4, 8}) {
+        const std::vector<int> tiles = make_tiles(s->L, tl);
+        cudaMemcpy(dt, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice);
+        for (int ch : {8, 16, 32, 64}) {
+            const float ms = timeit([&] { launch_analysis<T>(s, tl, dt, (int)tiles.size() / 3, ch, eta, 0); });
+            if (ms < best) { best = ms; best_tl = tl; best_ch = ch; best_tiles = tiles; }
+        }
+    }
+    cudaFree(dt);
+    s->tl = best_tl;
+    s->nchunk = best_ch;
+    s->ntiles = (int)best_tiles.size() / 3;
+    int st = ODIS_OK;
+    if (cudaMalloc(&s->tiles, sizeof(int) * best_tiles.size()) != cudaSuccess ||
+        cudaMemcpy(s->tiles, best_tiles.data(), sizeof(int) * best_tiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        st = ODIS_ERR_NOMEM;
+    best = 1e30f;
+    for (int lanes : {1, 2, 4, 8}) {
+        const float ms = timeit([&] { launch_synth<T>(s, lanes, 0); });
+        if (ms < best) { best = ms; s->lanes = lanes; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(eta);
+    cudaMemset(s->usg, 0, (s->precision == ODIS_FP32 ? sizeof(float) : sizeof(double)) * s->Np);
+    if (cudaDeviceSynchronize() != cudaSuccess) st = ODIS_ERR_CUDA;
+    return st;
+}
+
+int sh_autotune(ShLoading* s)
+{
+    if (s->precision == ODIS_FP64) return autotune_t<double>(s);
+    if (s->precision == ODIS_DF64) return autotune_t<df64>(s);
+    return autotune_t<float>(s);
+}
+
+void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes)
+{
+    if (tl) *tl = s->tl;
+    if (nchunk) *nchunk = s->nchunk;
+    if (lanes) *lanes = s->lanes;
+}
+
 template <class T>
 static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st)
 {
-    const T* P = (const T*)s->P;
-    const T* trig = (const T*)s->trig;
-    k_sh_analysis<T><<<dim3(s->ntiles, kChunks), kShThreads, 0, st>>>(P, trig, (const T*)eta, s->N, s->Np, s->L,
-                                                                       s->tiles, s->part);
-    k_sh_fold<<<(s->K + 127) / 128, 128, 0, st>>>(s->part, s->K, s->t);
-    k_sh_coef<<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, s->coef);
-    const int sb = (s->N * kSynthLanes + kSynthThreads - 1) / kSynthThreads;
-    k_sh_synth<T><<<sb, kSynthThreads, sizeof(T) * s->K, st>>>(P, trig, s->coef, s->N, s->Np, s->L, s->K, (T*)s->usg);
+    launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, eta, st);
+    k_sh_fold<T><<<(s->K + 127) / 128, 128, 0, st>>>((const T*)s->part, s->K, s->nchunk, s->t);
+    k_sh_coef<T><<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, (T*)s->coef);
+    launch_synth<T>(s, s->lanes, st);
 }
 
 void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)

@@ -31,6 +31,8 @@ const float2* sh_usgdf(ShLoading* s);
 void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t stream);
 // kernels launched by one sh_enqueue
 int sh_kernels_per_step();
+// tile shapes chosen by the setup-time autotuner
+void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes);
 // host helpers for checks: real SH basis at the nodes, [N][K]
 void sh_basis_host(const Mesh& m, int lmax, std::vector<double>& Y);
 

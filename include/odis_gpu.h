@@ -195,6 +195,19 @@ odis_status odis_set_state(odis_ctx* c, int iter, const double* v, const double*
 odis_status odis_update_energy_noalloc(const double* uv, const double* area, int n_faces, double alpha, double h,
                                        double radius, double* e_out, double* avg_out, void* stream);
 
+/* ---- execution strategy ------------------------------------------------ */
+/* FP64 and DF64 runs without self-gravity execute a whole odis_run_steps call
+ * as one persistent cooperative launch (one CTA per SM, coefficients and AB3
+ * histories resident in shared memory, neighbour-only step synchronisation
+ * with bounded waits) when the mesh partition fits; otherwise, and for the
+ * other methods, steps are CUDA-graph-replayed pairs of face and cell kernels.
+ * Where both are possible, odis_create times each over 192 steps from the
+ * zero state on this device, keeps the faster one and restores the zero
+ * state.  enable = 0 forces the graph path, 1 the persistent loop (where
+ * possible), -1 returns to the choice made at creation.  *active (nullable)
+ * reports whether runs will use the persistent loop. */
+odis_status odis_set_persistent(odis_ctx* c, int enable, int* active);
+
 /* ---- measurement ------------------------------------------------------- */
 /* Number of this library's kernels launched so far by the context. */
 odis_status odis_launch_count(odis_ctx* c, long long* n);

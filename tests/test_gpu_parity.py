@@ -203,3 +203,37 @@ def test_df64_self_gravity_parity(grid_dir):
     _, vo, eo, _, _ = orc.get_state()
     _, vg, eg, _, _ = gpu.get_state()
     assert rel_err(pg, po) < 1e-10 and rel_err(eg, eo) < 1e-10 and rel_err(vg, vo) < 1e-10
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_persistent_loop_matches_graph_path(grid_dir, precision):
+    """The single-launch persistent loop and the graph-replayed kernel pairs give the same state bits;
+    the power series differs only in the order of the block sums."""
+    orc, a = _pair(grid_dir / "grid_4.txt", precision=precision)
+    _, b = _pair(grid_dir / "grid_4.txt", precision=precision)
+    assert a.set_persistent(True) is True
+    assert b.set_persistent(False) is False
+    pa = np.concatenate([a.run(37), a.run(300), a.run(1)])
+    pb = np.concatenate([b.run(37), b.run(300), b.run(1)])
+    sa, sb = a.get_state(), b.get_state()
+    for x, y in zip(sa[1:], sb[1:]):
+        np.testing.assert_array_equal(x, y)
+    assert rel_err(pa, pb) < 1e-13
+    assert rel_err(pa, orc.run(338)) < 1e-10
+
+
+def test_persistent_loop_load_mode_and_state_round_trip(grid_dir):
+    orc, gpu = _pair(grid_dir / "grid_3.txt", precision=2, init_load=1)
+    rng = np.random.default_rng(11)
+    v = rng.standard_normal(orc.E) * 1e-3
+    eta = rng.standard_normal(orc.N) * 1e-2
+    dv = rng.standard_normal((orc.E, 3)) * 1e-8
+    de = rng.standard_normal((orc.N, 3)) * 1e-7
+    orc.set_state(5, v, eta, dv, de)
+    gpu.set_state(5, v, eta, dv, de)
+    assert gpu.set_persistent(True)
+    po, pg = orc.run(400), gpu.run(400)
+    assert rel_err(pg, po) < 1e-10
+    _, vo, eo, dvo, deo = orc.get_state()
+    it, vg, eg, dvg, deg = gpu.get_state()
+    assert it == 405 and rel_err(vg, vo) < 1e-10 and rel_err(eg, eo) < 1e-10 and rel_err(dvg, dvo) < 1e-10
