@@ -20,7 +20,7 @@ import numpy as np
 
 __all__ = [
     "OdisError", "lib", "Params", "Input", "Mesh", "Solver", "generate_grid_file", "derive_time",
-    "read_input", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL", "FP64", "FP32", "DF64",
+    "read_input", "Batch", "BatchMember", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL", "FP64", "FP32", "DF64",
 ]
 
 _PKG = Path(__file__).resolve().parent
@@ -45,6 +45,11 @@ class Params(C.Structure):
                 ("alpha", C.c_double), ("ecc", C.c_double), ("obliq", C.c_double), ("love_reduct", C.c_double),
                 ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int), ("precision", C.c_int),
                 ("sh_lmax", C.c_int), ("sh_factors", C.POINTER(C.c_double))]
+
+
+class BatchMember(C.Structure):
+    _fields_ = [("mesh", C.c_int), ("steps_per_orbit", C.c_int), ("h", C.c_double), ("alpha", C.c_double),
+                ("ecc", C.c_double), ("obliq", C.c_double)]
 
 
 class Input(C.Structure):
@@ -93,6 +98,13 @@ _SIGS = {
     "odis_launch_count": ([_V, C.POINTER(C.c_longlong)], C.c_int),
     "odis_profile_kernels": ([_V, C.c_int, _D], C.c_int),
     "odis_set_persistent": ([_V, C.c_int, _I], C.c_int),
+    "odis_sh_tiles": ([_V, _I, _I, _I], C.c_int),
+    "odis_batch_create": ([C.POINTER(Params), C.POINTER(_V), C.c_int, _V, C.c_int, C.POINTER(_V)], C.c_int),
+    "odis_batch_destroy": ([_V], None),
+    "odis_batch_run": ([_V, C.c_double, C.c_int, _D, C.c_int, _D, C.c_int, C.c_int], C.c_int),
+    "odis_batch_get_member": ([_V, C.c_int, _I, _D, _D], C.c_int),
+    "odis_batch_set_member": ([_V, C.c_int, _D, _D], C.c_int),
+    "odis_batch_info": ([_V, _I, _I, _I, C.POINTER(C.c_longlong)], C.c_int),
 }
 
 
@@ -312,6 +324,12 @@ class Solver:
         _ck(lib().odis_set_persistent(self._h, flag, C.byref(a)), "odis_set_persistent")
         return bool(a.value)
 
+    def sh_tiles(self) -> tuple:
+        """(tile_l, chunks, lanes) of the self-gravity transforms chosen at creation."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _ck(lib().odis_sh_tiles(self._h, C.byref(a), C.byref(b), C.byref(c)), "odis_sh_tiles")
+        return a.value, b.value, c.value
+
     def launch_count(self) -> int:
         n = C.c_longlong()
         _ck(lib().odis_launch_count(self._h, C.byref(n)), "odis_launch_count")
@@ -349,3 +367,69 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """Many configurations of the time loop advanced by one persistent launch per chunk of steps.
+
+    `meshes` is a list of Mesh; `members` a list of dicts (or BatchMember) with keys
+    mesh (index into `meshes`), steps_per_orbit (even), h, alpha, ecc, obliq.  The
+    common parameters (radius, g, angvel, potential, love_reduct, init_load) come
+    from `params`.
+    """
+
+    def __init__(self, params: Params, meshes, members):
+        self.params = params
+        self.meshes = list(meshes)
+        arr = (BatchMember * len(members))()
+        for i, m in enumerate(members):
+            if isinstance(m, BatchMember):
+                arr[i] = m
+            else:
+                arr[i] = BatchMember(int(m["mesh"]), int(m["steps_per_orbit"]), float(m["h"]), float(m["alpha"]),
+                                     float(m.get("ecc", 0.0)), float(m.get("obliq", 0.0)))
+        self.members = arr
+        self.count = len(members)
+        handles = (C.c_void_p * len(self.meshes))(*[mm._h.value for mm in self.meshes])
+        h = C.c_void_p()
+        _ck(lib().odis_batch_create(C.byref(params), handles, len(self.meshes), C.cast(arr, C.c_void_p), self.count,
+                                    C.byref(h)), "odis_batch_create")
+        self._h = h
+
+    def run(self, orbits: float = 0, steps: int = 0, step_power: bool = False, chunk: int = 0):
+        """Advance every member; returns (orbit_power [count, n_orbits], step_power [count, n_steps] or None)."""
+        spo = np.array([m.steps_per_orbit for m in self.members])
+        runs = np.rint(orbits * spo).astype(np.int64) if orbits > 0 else np.full(self.count, steps)
+        n_orb = int(np.max((runs + spo - 1) // spo))
+        op = np.zeros((self.count, n_orb))
+        sp = np.zeros((self.count, int(np.max(runs)))) if step_power else None
+        _ck(lib().odis_batch_run(self._h, float(orbits), int(steps), _dp(op), n_orb,
+                                 _dp(sp) if sp is not None else None, sp.shape[1] if sp is not None else 0, int(chunk)),
+            "odis_batch_run")
+        return op, sp
+
+    def get_member(self, i: int):
+        m = self.members[i]
+        mesh = self.meshes[m.mesh]
+        v, eta, it = np.zeros(mesh.n_edges), np.zeros(mesh.n_cells), C.c_int()
+        _ck(lib().odis_batch_get_member(self._h, int(i), C.byref(it), _dp(v), _dp(eta)), "odis_batch_get_member")
+        return it.value, v, eta
+
+    def set_member(self, i: int, v=None, eta=None) -> None:
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        ee = None if eta is None else np.ascontiguousarray(eta, dtype=np.float64)
+        _ck(lib().odis_batch_set_member(self._h, int(i), _dp(vv) if vv is not None else None,
+                                        _dp(ee) if ee is not None else None), "odis_batch_set_member")
+
+    def info(self) -> dict:
+        g, p, gr, n = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        _ck(lib().odis_batch_info(self._h, C.byref(g), C.byref(p), C.byref(gr), C.byref(n)), "odis_batch_info")
+        return {"groups": g.value, "padded_members": p.value, "grid": gr.value, "launches": n.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value and _lib is not None:
+            _lib.odis_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        self.close()

@@ -1123,6 +1123,17 @@ extern "C" odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms)
     return st;
 }
 
+extern "C" odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes)
+{
+    if (!c) return ODIS_ERR_ARG;
+    int a = 0, b = 0, d = 0;
+    if (c->sh) sh_tuning(c->sh, &a, &b, &d);
+    if (tile_l) *tile_l = a;
+    if (chunks) *chunks = b;
+    if (lanes) *lanes = d;
+    return ODIS_OK;
+}
+
 extern "C" odis_status odis_set_persistent(odis_ctx* c, int enable, int* active)
 {
     if (!c || enable < -1 || enable > 1) return ODIS_ERR_ARG;

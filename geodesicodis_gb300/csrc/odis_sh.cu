@@ -24,6 +24,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 namespace odis {
@@ -471,6 +473,21 @@ static void launch_synth(const ShLoading* s, int lanes, cudaStream_t st)
 // and the fastest is kept.  Results do not depend on the choice of the
 // synthesis lanes; the analysis's chunking changes only the order of the
 // partial sums.
+// ODIS_SH_TILES="tile_l,chunks,lanes" (tile_l in {2,4,8}, chunks in {8,16,32,64},
+// lanes in {1,2,4,8}) fixes the tiles instead of timing them, e.g. to reproduce
+// a run bit for bit or to profile a given variant.  Anything else is ignored.
+static bool forced_tiles(int* f)
+{
+    const char* e = std::getenv("ODIS_SH_TILES");
+    if (!e) return false;
+    int a = 0, b = 0, c = 0;
+    if (std::sscanf(e, "%d,%d,%d", &a, &b, &c) != 3) return false;
+    const bool ok = (a == 2 || a == 4 || a == 8) && (b == 8 || b == 16 || b == 32 || b == 64) &&
+                    (c == 1 || c == 2 || c == 4 || c == 8);
+    if (ok) { f[0] = a; f[1] = b; f[2] = c; }
+    return ok;
+}
+
 template <class T>
 static int autotune_t(ShLoading* s)
 {
@@ -497,13 +514,17 @@ static int autotune_t(ShLoading* s)
     float best = 1e30f;
     int best_tl = 8, best_ch = 16;
     std::vector<int> best_tiles;
+    int forced[3] = {0, 0, 0};
+    const bool force = forced_tiles(forced);
     int* dt = nullptr;
     cudaMalloc(&dt, sizeof(int) * 3 * (size_t)(s->L + 1) * (s->L + 1));
     for (int tl : {2, 4, 8}) {
+        if (force && tl != forced[0]) continue;
         const std::vector<int> tiles = make_tiles(s->L, tl);
         cudaMemcpy(dt, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice);
         for (int ch : {8, 16, 32, 64}) {
-            const float ms = timeit([&] { launch_analysis<T>(s, tl, dt, (int)tiles.size() / 3, ch, eta, 0); });
+            if (force && ch != forced[1]) continue;
+            const float ms = force ? 0.f : timeit([&] { launch_analysis<T>(s, tl, dt, (int)tiles.size() / 3, ch, eta, 0); });
             if (ms < best) { best = ms; best_tl = tl; best_ch = ch; best_tiles = tiles; }
         }
     }
@@ -517,7 +538,8 @@ static int autotune_t(ShLoading* s)
         st = ODIS_ERR_NOMEM;
     best = 1e30f;
     for (int lanes : {1, 2, 4, 8}) {
-        const float ms = timeit([&] { launch_synth<T>(s, lanes, 0); });
+        if (force && lanes != forced[2]) continue;
+        const float ms = force ? 0.f : timeit([&] { launch_synth<T>(s, lanes, 0); });
         if (ms < best) { best = ms; s->lanes = lanes; }
     }
     cudaEventDestroy(a);

@@ -216,6 +216,53 @@ odis_status odis_launch_count(odis_ctx* c, long long* n);
  * ms[0] face step kernel, ms[1] cell step kernel, ms[2] self-gravity
  * analysis+solve+synthesis (0 if off).  Leaves the state undefined. */
 odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms);
+/* Tiles of the self-gravity transforms (0 without self-gravity): the analysis
+ * covers tile_l degrees per block with the cells split in `chunks`, the
+ * synthesis gives each cell `lanes` threads.  odis_create times every
+ * combination on this device and keeps the fastest, unless the environment
+ * variable ODIS_SH_TILES="tile_l,chunks,lanes" names one. */
+odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes);
+
+/* ---- batched sweep ----------------------------------------------------- */
+/* Many configurations of the LTE time loop (src/timeIntegrator.cpp:57-322,
+ * linear branch) advanced together by one persistent cooperative kernel.  No
+ * reference counterpart: it replaces running the reference binary once per
+ * configuration.  State FP32 with double-float (FP64-accurate) AB3
+ * accumulation; dissipated power summed in FP64 across tiles.  Members share
+ * the `common` parameters (radius, g, angvel, potential, love_reduct,
+ * init_load; the rest is ignored) and each has its own mesh (an index into
+ * `meshes`, which must outlive odis_batch_create only), thickness, drag,
+ * eccentricity, obliquity and steps per orbit. */
+typedef struct odis_batch odis_batch;
+typedef struct odis_batch_member {
+    int mesh;                /* index into the meshes array */
+    int steps_per_orbit;     /* even; dt = (2 pi / angvel) / steps_per_orbit */
+    double h;                /* ocean thickness, m */
+    double alpha;            /* linear drag, s^-1 */
+    double ecc;              /* eccentricity */
+    double obliq;            /* obliquity, radians */
+} odis_batch_member;
+odis_status odis_batch_create(const odis_params* common, const odis_mesh* const* meshes, int n_meshes,
+                              const odis_batch_member* members, int count, odis_batch** out);
+void odis_batch_destroy(odis_batch* b);
+/* Advances every member by orbits * steps_per_orbit steps (orbits > 0, steps = 0;
+ * fractions allowed where that is a whole even number for every member) or by
+ * `steps` steps (orbits = 0, steps > 0 and even).  Host outputs, nullable:
+ * orbit_power[member * orbit_stride + o] = mean dissipated power (W/m^2 as
+ * updateEnergy, src/energy.cpp:13-61) over orbit o of this run;
+ * step_power[member * step_stride + k] = power after step k of this run.
+ * chunk = steps per cooperative launch (0: 2048).  Returns ODIS_ERR_NONFINITE
+ * if a member's state became non-finite, ODIS_ERR_TIMEOUT if a grid barrier
+ * wait ran out. */
+odis_status odis_batch_run(odis_batch* b, double orbits, int steps, double* orbit_power, int orbit_stride,
+                           double* step_power, int step_stride, int chunk);
+/* One member's v[E] and eta[N] (FP64 from the double-float master) and its step count. */
+odis_status odis_batch_get_member(odis_batch* b, int member, int* iter, double* v, double* eta);
+/* Sets one member's v and eta (nullable: zero), clears its AB3 history and
+ * restarts its step count at 0 (forcing phase 0, forward-Euler start): the
+ * warm-start entry point. */
+odis_status odis_batch_set_member(odis_batch* b, int member, const double* v, const double* eta);
+odis_status odis_batch_info(const odis_batch* b, int* n_groups, int* padded_members, int* grid, long long* launches);
 
 #ifdef __cplusplus
 }
