@@ -20,7 +20,7 @@ import numpy as np
 
 __all__ = [
     "OdisError", "lib", "Params", "Input", "Mesh", "Solver", "generate_grid_file", "derive_time",
-    "read_input", "Batch", "BatchMember", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL", "FP64", "FP32", "DF64",
+    "read_input", "Batch", "BatchMember", "MLP", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL", "FP64", "FP32", "DF64",
 ]
 
 _PKG = Path(__file__).resolve().parent
@@ -105,6 +105,17 @@ _SIGS = {
     "odis_batch_get_member": ([_V, C.c_int, _I, _D, _D], C.c_int),
     "odis_batch_set_member": ([_V, C.c_int, _D, _D], C.c_int),
     "odis_batch_info": ([_V, _I, _I, _I, C.POINTER(C.c_longlong)], C.c_int),
+    "odis_batch_get_mesh_members": ([_V, C.c_int, _D, _D], C.c_int),
+    "odis_batch_set_mesh_members": ([_V, C.c_int, _D, _D], C.c_int),
+    "odis_batch_project": ([_V, C.c_int, _V, C.c_int, _V, C.c_int, _D, C.c_int], C.c_int),
+    "odis_mlp_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_V)], C.c_int),
+    "odis_mlp_destroy": ([_V], None),
+    "odis_mlp_num_params": ([_V, C.POINTER(C.c_longlong)], C.c_int),
+    "odis_mlp_get_params": ([_V, _V], C.c_int),
+    "odis_mlp_set_params": ([_V, _V], C.c_int),
+    "odis_mlp_predict": ([_V, _V, _V, C.c_int, _V], C.c_int),
+    "odis_mlp_gradient": ([_V, _V, _V, _V, _V, C.c_int, _D, _V], C.c_int),
+    "odis_mlp_train": ([_V, _V, _V, _V, _V, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong, _D], C.c_int),
 }
 
 
@@ -421,6 +432,33 @@ class Batch:
         _ck(lib().odis_batch_set_member(self._h, int(i), _dp(vv) if vv is not None else None,
                                         _dp(ee) if ee is not None else None), "odis_batch_set_member")
 
+    def mesh_members(self, mesh: int) -> np.ndarray:
+        return np.array([i for i in range(self.count) if self.members[i].mesh == mesh], dtype=np.int64)
+
+    def get_mesh_members(self, mesh: int):
+        """(v [m, E], eta [m, N]) of the members on `mesh`, in member order."""
+        m = len(self.mesh_members(mesh))
+        ms = self.meshes[mesh]
+        v, eta = np.zeros((m, ms.n_edges)), np.zeros((m, ms.n_cells))
+        _ck(lib().odis_batch_get_mesh_members(self._h, int(mesh), _dp(v), _dp(eta)), "odis_batch_get_mesh_members")
+        return v, eta
+
+    def set_mesh_members(self, mesh: int, v=None, eta=None) -> None:
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
+        ee = None if eta is None else np.ascontiguousarray(eta, dtype=np.float64)
+        _ck(lib().odis_batch_set_mesh_members(self._h, int(mesh), _dp(vv) if vv is not None else None,
+                                              _dp(ee) if ee is not None else None), "odis_batch_set_mesh_members")
+
+    def project(self, mesh: int, basis_v: np.ndarray, basis_eta: np.ndarray) -> np.ndarray:
+        """[m, kv + ke] projections of the members on `mesh` (member order) onto the row bases."""
+        bv = np.ascontiguousarray(basis_v, dtype=np.float32)
+        be = np.ascontiguousarray(basis_eta, dtype=np.float32)
+        kv, ke = bv.shape[0], be.shape[0]
+        out = np.zeros((self.count, kv + ke))
+        _ck(lib().odis_batch_project(self._h, int(mesh), C.c_void_p(bv.ctypes.data), kv, C.c_void_p(be.ctypes.data), ke,
+                                     _dp(out), kv + ke), "odis_batch_project")
+        return out[self.mesh_members(mesh)]
+
     def info(self) -> dict:
         g, p, gr, n = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
         _ck(lib().odis_batch_info(self._h, C.byref(g), C.byref(p), C.byref(gr), C.byref(n)), "odis_batch_info")
@@ -429,6 +467,69 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value and _lib is not None:
             _lib.odis_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+
+def _fp(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class MLP:
+    """The warm-start network (odis_mlp_*): n_in -> width x depth (GELU) -> n_mix * n_out, mixed per sample."""
+
+    def __init__(self, n_in: int, width: int, depth: int, n_out: int, n_mix: int = 0, seed: int = 0):
+        self.n_in, self.width, self.depth, self.n_out, self.n_mix = n_in, width, depth, n_out, n_mix
+        h = C.c_void_p()
+        _ck(lib().odis_mlp_create(n_in, width, depth, n_out, n_mix, seed, C.byref(h)), "odis_mlp_create")
+        self._h = h
+        n = C.c_longlong()
+        _ck(lib().odis_mlp_num_params(self._h, C.byref(n)), "odis_mlp_num_params")
+        self.n_params = n.value
+
+    def _rows(self, x, mix, t=None, w=None):
+        x = np.ascontiguousarray(x, np.float32)
+        mix = None if mix is None else np.ascontiguousarray(mix, np.float32)
+        t = None if t is None else np.ascontiguousarray(t, np.float32)
+        w = None if w is None else np.ascontiguousarray(w, np.float32)
+        return x, mix, t, w
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, np.float32)
+        _ck(lib().odis_mlp_get_params(self._h, _fp(p)), "odis_mlp_get_params")
+        return p
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        _ck(lib().odis_mlp_set_params(self._h, _fp(p)), "odis_mlp_set_params")
+
+    def predict(self, x, mix=None) -> np.ndarray:
+        x, mix, _, _ = self._rows(x, mix)
+        y = np.zeros((x.shape[0], self.n_out), np.float32)
+        _ck(lib().odis_mlp_predict(self._h, _fp(x), _fp(mix), x.shape[0], _fp(y)), "odis_mlp_predict")
+        return y
+
+    def gradient(self, x, t, mix=None, w=None):
+        x, mix, t, w = self._rows(x, mix, t, w)
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_double()
+        _ck(lib().odis_mlp_gradient(self._h, _fp(x), _fp(mix), _fp(t), _fp(w), x.shape[0], C.byref(loss), _fp(g)),
+            "odis_mlp_gradient")
+        return loss.value, g
+
+    def train(self, x, t, mix=None, w=None, epochs=100, batch=256, lr=1e-3, seed=0) -> np.ndarray:
+        x, mix, t, w = self._rows(x, mix, t, w)
+        losses = np.zeros(epochs)
+        _ck(lib().odis_mlp_train(self._h, _fp(x), _fp(mix), _fp(t), _fp(w), x.shape[0], int(epochs), int(batch),
+                                 float(lr), int(seed), _dp(losses)), "odis_mlp_train")
+        return losses
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value and _lib is not None:
+            _lib.odis_mlp_destroy(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

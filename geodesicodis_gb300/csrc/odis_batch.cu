@@ -850,3 +850,191 @@ extern "C" odis_status odis_batch_set_member(odis_batch* b, int member, const do
     if (st == ODIS_OK) b->base[s] = 0;
     return st;
 }
+
+// ---------------------------------------------------------------------------
+// bulk state access and projections (one mesh's members at a time)
+// ---------------------------------------------------------------------------
+namespace odis {
+namespace {
+
+constexpr int kProjK = 8;        // basis rows per thread
+constexpr int kProjQ = 32;       // member quads per block (threadIdx.x)
+constexpr int kProjS = 8;        // row slices per block (threadIdx.y)
+
+// out[k][4 q + c] = sum_r basis[k][r] * state[r][4 q + c] for one group: each
+// thread sums kProjK basis rows for one quad over a slice of the rows (FP32),
+// the slices are added in FP64.
+__global__ void __launch_bounds__(kProjQ * kProjS) k_project(const float* __restrict__ basis, int K, int rows,
+                                                            const float4* __restrict__ state, int Bq,
+                                                            double* __restrict__ out)
+{
+    __shared__ float4 s_acc[kProjS][kProjK][kProjQ];
+    const int x = threadIdx.x, y = threadIdx.y;
+    const int q = blockIdx.x * kProjQ + x, k0 = blockIdx.y * kProjK;
+    float4 acc[kProjK];
+#pragma unroll
+    for (int kk = 0; kk < kProjK; kk++) acc[kk] = f4(0.f);
+    if (q < Bq) {
+        for (int r = y; r < rows; r += kProjS) {
+            const float4 v = state[(size_t)r * Bq + q];
+#pragma unroll
+            for (int kk = 0; kk < kProjK; kk++) {
+                const float bk = k0 + kk < K ? __ldg(&basis[(size_t)(k0 + kk) * rows + r]) : 0.f;
+                acc[kk] = fma4(bk, v, acc[kk]);
+            }
+        }
+    }
+#pragma unroll
+    for (int kk = 0; kk < kProjK; kk++) s_acc[y][kk][x] = acc[kk];
+    __syncthreads();
+    if (y == 0 && q < Bq) {
+        for (int kk = 0; kk < kProjK && k0 + kk < K; kk++) {
+            double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+            for (int yy = 0; yy < kProjS; yy++) {
+                const float4 a = s_acc[yy][kk][x];
+                s0 += a.x; s1 += a.y; s2 += a.z; s3 += a.w;
+            }
+            double* o = out + (size_t)(k0 + kk) * 4 * Bq + 4 * q;
+            o[0] = s0; o[1] = s1; o[2] = s2; o[3] = s3;
+        }
+    }
+}
+
+}  // namespace
+}  // namespace odis
+
+static std::vector<int> mesh_members(const odis_batch* b, int mesh)
+{
+    std::vector<int> out;
+    for (int i = 0; i < b->count; i++)
+        if (b->members[i].mesh == mesh) out.push_back(i);
+    return out;
+}
+
+extern "C" odis_status odis_batch_project(odis_batch* b, int mesh, const float* basis_v, int kv, const float* basis_eta,
+                                          int ke, double* out, int out_stride)
+{
+    if (!b || !out || kv < 0 || ke < 0 || (kv && !basis_v) || (ke && !basis_eta) || out_stride < kv + ke) return ODIS_ERR_ARG;
+    const std::vector<int> mem = mesh_members(b, mesh);
+    if (mem.empty()) return ODIS_ERR_ARG;
+    const GroupDev& G0 = b->groups[b->group_of[mem[0]]];
+    const int E = G0.E, N = G0.N;
+    ODIS_BCK(cudaStreamSynchronize(b->stream));
+    float* d_basis = nullptr;
+    double* d_out = nullptr;
+    const int K = std::max(kv, ke);
+    int maxBq = 0;
+    for (size_t g = 0; g < b->groups.size(); g++) maxBq = std::max(maxBq, b->groups[g].Bq);
+    const size_t bn = std::max((size_t)kv * E, (size_t)ke * N);
+    if (cudaMalloc(&d_basis, sizeof(float) * std::max<size_t>(bn, 1)) != cudaSuccess) return ODIS_ERR_NOMEM;
+    if (cudaMalloc(&d_out, sizeof(double) * (size_t)std::max(K, 1) * 4 * maxBq) != cudaSuccess) { cudaFree(d_basis); return ODIS_ERR_NOMEM; }
+    int st = ODIS_OK;
+    std::vector<double> h;
+    for (int which = 0; which < 2 && st == ODIS_OK; which++) {
+        const int k = which == 0 ? kv : ke;
+        if (!k) continue;
+        const int rows = which == 0 ? E : N;
+        if (cudaMemcpy(d_basis, which == 0 ? basis_v : basis_eta, sizeof(float) * (size_t)k * rows, cudaMemcpyHostToDevice) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
+        for (size_t g = 0; g < b->groups.size() && st == ODIS_OK; g++) {
+            const GroupDev& G = b->groups[g];
+            bool mine = false;
+            for (int i : mem) mine |= b->group_of[i] == (int)g;
+            if (!mine) continue;
+            const float4* state = reinterpret_cast<const float4*>(which == 0 ? G.vhi[0] : G.ehi);
+            dim3 grid((G.Bq + kProjQ - 1) / kProjQ, (k + kProjK - 1) / kProjK), block(kProjQ, kProjS);
+            k_project<<<grid, block, 0, b->stream>>>(d_basis, k, rows, state, G.Bq, d_out);
+            h.assign((size_t)k * 4 * G.Bq, 0.0);
+            if (cudaMemcpyAsync(h.data(), d_out, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, b->stream) != cudaSuccess ||
+                cudaStreamSynchronize(b->stream) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
+            b->launches++;
+            for (int i : mem) {
+                if (b->group_of[i] != (int)g) continue;
+                const int col = b->slot_of[i] - G.moff;
+                for (int kk = 0; kk < k; kk++) out[(size_t)i * out_stride + (which == 0 ? 0 : kv) + kk] = h[(size_t)kk * 4 * G.Bq + col];
+            }
+        }
+    }
+    cudaFree(d_basis);
+    cudaFree(d_out);
+    return st;
+}
+
+// Members on `mesh`, in increasing member index: v [m][E], eta [m][N].
+extern "C" odis_status odis_batch_get_mesh_members(odis_batch* b, int mesh, double* v, double* eta)
+{
+    if (!b) return ODIS_ERR_ARG;
+    const std::vector<int> mem = mesh_members(b, mesh);
+    if (mem.empty()) return ODIS_ERR_ARG;
+    ODIS_BCK(cudaStreamSynchronize(b->stream));
+    std::vector<float> hi, lo;
+    for (int which = 0; which < 2; which++) {
+        double* out = which == 0 ? v : eta;
+        if (!out) continue;
+        for (size_t g = 0; g < b->groups.size(); g++) {
+            const GroupDev& G = b->groups[g];
+            std::vector<int> here;
+            for (size_t k = 0; k < mem.size(); k++) if (b->group_of[mem[k]] == (int)g) here.push_back((int)k);
+            if (here.empty()) continue;
+            const int rows = which == 0 ? G.E : G.N, pitch = 4 * G.Bq;
+            hi.resize((size_t)rows * pitch);
+            lo.resize((size_t)rows * pitch);
+            ODIS_BCK(cudaMemcpy(hi.data(), which == 0 ? G.vhi[0] : G.ehi, sizeof(float) * hi.size(), cudaMemcpyDeviceToHost));
+            ODIS_BCK(cudaMemcpy(lo.data(), which == 0 ? G.vlo : G.elo, sizeof(float) * lo.size(), cudaMemcpyDeviceToHost));
+            for (int k : here) {
+                const int col = b->slot_of[mem[k]] - G.moff;
+                double* o = out + (size_t)k * rows;
+                for (int r = 0; r < rows; r++) o[r] = (double)hi[(size_t)r * pitch + col] + (double)lo[(size_t)r * pitch + col];
+            }
+        }
+    }
+    return ODIS_OK;
+}
+
+// Sets every member on `mesh` (increasing member index; v [m][E], eta [m][N],
+// nullable: zero), clears their AB3 histories and restarts their step counts
+// at 0 (forcing phase 0, forward-Euler start): the bulk warm-start entry point.
+extern "C" odis_status odis_batch_set_mesh_members(odis_batch* b, int mesh, const double* v, const double* eta)
+{
+    if (!b) return ODIS_ERR_ARG;
+    const std::vector<int> mem = mesh_members(b, mesh);
+    if (mem.empty()) return ODIS_ERR_ARG;
+    ODIS_BCK(cudaStreamSynchronize(b->stream));
+    std::vector<float> hi, lo;
+    for (size_t g = 0; g < b->groups.size(); g++) {
+        GroupDev& G = b->groups[g];
+        std::vector<int> here;
+        for (size_t k = 0; k < mem.size(); k++) if (b->group_of[mem[k]] == (int)g) here.push_back((int)k);
+        if (here.empty()) continue;
+        const int pitch = 4 * G.Bq;
+        for (int which = 0; which < 2; which++) {
+            const double* in = which == 0 ? v : eta;
+            const int rows = which == 0 ? G.E : G.N;
+            float* dhi = which == 0 ? G.vhi[0] : G.ehi;
+            float* dlo = which == 0 ? G.vlo : G.elo;
+            hi.resize((size_t)rows * pitch);
+            lo.resize((size_t)rows * pitch);
+            // keep the columns of members on other meshes (none share a group) and of padding
+            ODIS_BCK(cudaMemcpy(hi.data(), dhi, sizeof(float) * hi.size(), cudaMemcpyDeviceToHost));
+            ODIS_BCK(cudaMemcpy(lo.data(), dlo, sizeof(float) * lo.size(), cudaMemcpyDeviceToHost));
+            for (int k : here) {
+                const int col = b->slot_of[mem[k]] - G.moff;
+                for (int r = 0; r < rows; r++) {
+                    const double x = in ? in[(size_t)k * rows + r] : 0.0;
+                    const float xh = (float)x;
+                    hi[(size_t)r * pitch + col] = xh;
+                    lo[(size_t)r * pitch + col] = (float)(x - (double)xh);
+                }
+            }
+            ODIS_BCK(cudaMemcpy(dhi, hi.data(), sizeof(float) * hi.size(), cudaMemcpyHostToDevice));
+            ODIS_BCK(cudaMemcpy(dlo, lo.data(), sizeof(float) * lo.size(), cudaMemcpyHostToDevice));
+        }
+        const size_t ev = (size_t)G.E * pitch, cv = (size_t)G.N * pitch;
+        ODIS_BCK(cudaMemset(G.vhi[1], 0, sizeof(float) * ev));
+        for (int k = 0; k < 2; k++) {
+            ODIS_BCK(cudaMemset(G.hv[k], 0, sizeof(float) * ev));
+            ODIS_BCK(cudaMemset(G.he[k], 0, sizeof(float) * cv));
+        }
+        for (int k : here) b->base[b->slot_of[mem[k]]] = 0;
+    }
+    return ODIS_OK;
+}

@@ -263,6 +263,41 @@ odis_status odis_batch_get_member(odis_batch* b, int member, int* iter, double* 
  * warm-start entry point. */
 odis_status odis_batch_set_member(odis_batch* b, int member, const double* v, const double* eta);
 odis_status odis_batch_info(const odis_batch* b, int* n_groups, int* padded_members, int* grid, long long* launches);
+/* Bulk state access for the members on mesh `mesh`, in increasing member index
+ * (v [m][E], eta [m][N]).  set_mesh_members also clears their AB3 histories
+ * and restarts their step counts at 0, as odis_batch_set_member. */
+odis_status odis_batch_get_mesh_members(odis_batch* b, int mesh, double* v, double* eta);
+odis_status odis_batch_set_mesh_members(odis_batch* b, int mesh, const double* v, const double* eta);
+/* Projections of the current state of the members on `mesh` onto row bases:
+ * out[member * out_stride + k] = sum_e basis_v[k][e] v_e (k < kv), then
+ * sum_i basis_eta[k][i] eta_i (kv <= k < kv + ke); FP32 products and slice
+ * sums, FP64 across slices.  Members on other meshes are left untouched. */
+odis_status odis_batch_project(odis_batch* b, int mesh, const float* basis_v, int kv, const float* basis_eta, int ke,
+                               double* out, int out_stride);
+
+/* ---- warm-start surrogate network -------------------------------------- */
+/* No reference counterpart.  MLP n_in -> width (GELU) x depth -> n_mix * n_out,
+ * output y = sum_k mix[k] * R_k (n_mix = 0: y = R).  FP32 master weights,
+ * BF16 operands with FP32 accumulation in every GEMM (tensor cores), FP32
+ * bias/GELU/loss/Adam.  Loss = sum_i w_i ||y_i - t_i||^2 / n (w nullable: 1).
+ * Host arrays, row-major: x [n][n_in], mix [n][n_mix], t/y [n][n_out], w [n].
+ * Parameters flat: for each layer W [out][in] then b [out]. */
+typedef struct odis_mlp odis_mlp;
+odis_status odis_mlp_create(int n_in, int width, int depth, int n_out, int n_mix, unsigned long long seed,
+                            odis_mlp** out);
+void odis_mlp_destroy(odis_mlp* m);
+odis_status odis_mlp_num_params(const odis_mlp* m, long long* n);
+odis_status odis_mlp_get_params(odis_mlp* m, float* out);
+/* also resets the Adam state */
+odis_status odis_mlp_set_params(odis_mlp* m, const float* in);
+odis_status odis_mlp_predict(odis_mlp* m, const float* x, const float* mix, int n, float* y);
+/* one forward + backward pass over n rows: loss and the gradient (flat, FP32) */
+odis_status odis_mlp_gradient(odis_mlp* m, const float* x, const float* mix, const float* t, const float* w, int n,
+                              double* loss, float* grad);
+/* Adam (0.9, 0.999, 1e-8), shuffled minibatches (whole batches only), cosine
+ * learning-rate decay from lr; loss_per_epoch (nullable) = mean minibatch loss. */
+odis_status odis_mlp_train(odis_mlp* m, const float* x, const float* mix, const float* t, const float* w, int n,
+                           int epochs, int batch, float lr, unsigned long long seed, double* loss_per_epoch);
 
 #ifdef __cplusplus
 }

@@ -130,3 +130,28 @@ def test_batch_nonfinite_member_is_reported(grid_dir):
     orc.run(400)
     assert rel_err(b.get_member(0)[2], orc.get_state()[2]) < 1e-3
     b.close()
+
+
+def test_batch_bulk_state_and_projection(grid_dir):
+    g, O, angvel, P, paths, meshes, members, common = _setup(grid_dir, count=10, seed=13)
+    b = g.Batch(common, meshes, members)
+    b.run(steps=200)
+    for mesh in (0, 1):
+        idx = b.mesh_members(mesh)
+        v, eta = b.get_mesh_members(mesh)
+        for k, i in enumerate(idx):
+            _, vi, ei = b.get_member(int(i))
+            np.testing.assert_array_equal(v[k], vi)
+            np.testing.assert_array_equal(eta[k], ei)
+        rng = np.random.default_rng(mesh)
+        bv = rng.standard_normal((13, v.shape[1])).astype(np.float32)
+        be = rng.standard_normal((9, eta.shape[1])).astype(np.float32)
+        pr = b.project(mesh, bv, be)
+        ref = np.concatenate([v @ bv.T.astype(np.float64), eta @ be.T.astype(np.float64)], axis=1)
+        assert np.max(np.abs(pr - ref)) / np.max(np.abs(ref)) < 1e-5
+        # bulk set: a scaled copy, then the members restart from step 0
+        b.set_mesh_members(mesh, 2 * v, 3 * eta)
+        v2, eta2 = b.get_mesh_members(mesh)
+        assert rel_err(v2, 2 * v) < 1e-12 and rel_err(eta2, 3 * eta) < 1e-12
+        assert all(b.get_member(int(i))[0] == 0 for i in idx)
+    b.close()
