@@ -320,12 +320,55 @@ def run_ours(args) -> dict:
                    "d2h_bytes_per_step": d2h,
                    "how": f"per orbit: odis_set_state from pinned host buffers, odis_run_steps({n}) with the "
                           "power series copied to host, odis_get_state back to host; wall clock"}}
+    if not args.no_sweep:
+        out["sweep"] = run_sweep(args, results["fp64_plain"], peak)
     if not args.no_cpu_baseline:
         v, _ = cpu_sample(args.cpu_sample_steps, None)
         out["cpu_baseline"] = {"value": v, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
                                "sample": f"{args.cpu_sample_steps} LTE steps of the same level-6 FP64 + l_max=16 "
                                          f"workload, oracle C restatement with OpenMP over rows/cells"}
     return out
+
+
+def run_sweep(args, fp64_plain: float, peak: float) -> dict:
+    """Batched sweep: 256 seeded configurations (levels 4-6, thickness, drag, eccentricity, obliquity;
+    FULL tide), FP32 state with double-float accumulation, `args.sweep_orbits` orbits each, in one
+    persistent cooperative launch per chunk of steps (odis_batch_run)."""
+    from geodesicodis_gb300 import sweep as S
+    t0 = time.perf_counter()
+    batch, members, meshes, period = S.make_sweep(256, 2, (4, 5, 6))
+    t_create = time.perf_counter() - t0
+    batch.run(steps=200)                                   # warm-up (then the members restart from rest)
+    for mesh in range(len(meshes.levels)):
+        batch.set_mesh_members(mesh)
+    l0 = batch.info()["launches"]
+    t = time.perf_counter()
+    op, _ = batch.run(orbits=args.sweep_orbits)            # synchronous: returns when the device is done
+    el = time.perf_counter() - t
+    cs = S.cell_steps(members, meshes, args.sweep_orbits)
+    # all members active: a uniform 2000-step run
+    uni = sum(meshes.meshes[meshes.levels[m["mesh"]]].n_cells for m in members) * 2000
+    t = time.perf_counter()
+    batch.run(steps=2000)
+    el_u = time.perf_counter() - t
+    spo = np.array([m["steps_per_orbit"] for m in members])
+    info = batch.info()
+    batch.close()
+    # algorithmic bytes per cell-step of the batched step (FP32 hi + lo state, FP32 history):
+    # per face 28 B (v hi r/w, v lo r/w, two history reads, one write), per cell 28 B, faces = 3 cells
+    bytes_per_cell_step = 3 * 28 + 28
+    return {"workload": f"256 members, levels 4/5/6, {args.sweep_orbits} orbits each at max(2000, stable) steps/orbit",
+            "cell_steps_per_s": cs / el, "seconds": el, "cell_steps": cs,
+            "uniform_2000_steps_cell_steps_per_s": uni / el_u,
+            "vs_fp64_plain_single_instance": cs / el / fp64_plain,
+            "steps_per_orbit_range": [int(spo.min()), int(spo.max())], "members_at_2000": int(np.sum(spo == 2000)),
+            "nonfinite_members": int(np.sum(~np.isfinite(op).all(axis=1))),
+            "launches": info["launches"] - l0, "grid": info["grid"], "padded_members": info["padded_members"],
+            "create_seconds": t_create,
+            "hbm_roofline_uniform": {"bytes_per_cell_step": bytes_per_cell_step,
+                                     "achieved_gbs": uni / el_u * bytes_per_cell_step / 1e9,
+                                     "frac": uni / el_u * bytes_per_cell_step / 1e9 / peak},
+            "timing": "host wall clock around the synchronous run call; inputs resident on the device"}
 
 
 def profiled_traffic(kernel: str):
@@ -352,12 +395,23 @@ def main():
     ap.add_argument("--ref-sample-steps", type=int, default=40)
     ap.add_argument("--cpu-sample-steps", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile-case", choices=["fp64", "df64", "fp32"], default=None,
+    ap.add_argument("--no-sweep", action="store_true", help="skip the batched 256-configuration sweep")
+    ap.add_argument("--sweep-orbits", type=float, default=10.0)
+    ap.add_argument("--profile-case", choices=["fp64", "df64", "fp32", "batch"], default=None,
                     help="run a short level-6 case for an ncu capture (no timing, no JSON)")
     ap.add_argument("--case-sh", type=int, default=0, help="self-gravity degree of --profile-case")
     ap.add_argument("--case-steps", type=int, default=30)
     ap.add_argument("--case-graph", action="store_true", help="--profile-case: force the graph-replayed kernels")
     args = ap.parse_args()
+    if args.profile_case == "batch":
+        # one cooperative launch of `case-steps` steps of the 256-member sweep
+        from geodesicodis_gb300 import sweep as S
+        batch, members, meshes, period = S.make_sweep(256, 2, (4, 5, 6))
+        steps = args.case_steps + (args.case_steps & 1)
+        batch.run(steps=steps, chunk=steps + 1)
+        batch.run(steps=steps, chunk=steps + 1)
+        print("profile case done", batch.info())
+        return
     if args.profile_case:
         import geodesicodis_gb300 as g
         angvel, P, dt, n = g.derive_time(ANGVEL_IN, DT_TARGET)

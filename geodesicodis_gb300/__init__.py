@@ -213,7 +213,7 @@ class Mesh:
         return cls(h.value)
 
     def field(self, which: int) -> np.ndarray:
-        n = self.n_cells if which == 3 else self.n_edges
+        n = self.n_cells if which in (3, 12, 13) else self.n_edges
         out = np.zeros(n)
         _ck(lib().odis_mesh_field(self._h, which, _dp(out)), "odis_mesh_field")
         return out

@@ -204,6 +204,8 @@ extern "C" odis_status odis_mesh_field(const odis_mesh* mp, int which, double* o
     case 9: col(m.face_normal, 1); break;
     case 10: col(m.face_int, 0); break;
     case 11: col(m.face_int, 1); break;
+    case 12: for (int i = 0; i < m.N; i++) out[i] = m.node_sph[(size_t)i * 2]; break;
+    case 13: for (int i = 0; i < m.N; i++) out[i] = m.node_sph[(size_t)i * 2 + 1]; break;
     default: return ODIS_ERR_ARG;
     }
     return ODIS_OK;

@@ -372,7 +372,7 @@ extern "C" odis_status odis_mlp_create(int n_in, int width, int depth, int n_out
         off += m->dim[l + 1];
     }
     m->n_params = off;
-    // He-uniform weights (GELU layers), zero biases; splitmix64 stream from `seed`
+    // weights and biases uniform in +-1/sqrt(fan_in); splitmix64 stream from `seed`
     std::vector<float> h(off, 0.f);
     uint64_t x = seed;
     auto next = [&]() {
@@ -383,8 +383,9 @@ extern "C" odis_status odis_mlp_create(int n_in, int width, int depth, int n_out
         return (double)(z >> 11) * (1.0 / 9007199254740992.0);
     };
     for (int l = 0; l < L; l++) {
-        const double a = std::sqrt(6.0 / m->dim[l]) * (l + 1 < L ? 1.0 : 0.5);
+        const double a = 1.0 / std::sqrt((double)m->dim[l]);
         for (long k = 0; k < (long)m->dim[l + 1] * m->dim[l]; k++) h[m->woff[l] + k] = (float)((2.0 * next() - 1.0) * a);
+        for (long k = 0; k < m->dim[l + 1]; k++) h[m->boff[l] + k] = (float)((2.0 * next() - 1.0) * a);
     }
     ODIS_MCK(cudaStreamCreateWithFlags(&m->s, cudaStreamNonBlocking));
     ODIS_MCK(cudaMalloc(&m->p, sizeof(float) * off));

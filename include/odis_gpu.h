@@ -117,7 +117,7 @@ odis_status odis_mesh_sizes(const odis_mesh* m, int* n_cells, int* n_edges, int*
 /* Geometry the operators are built from (for checks): which = 0 face_len,
  * 1 face_node_dist, 2 face_area, 3 control-volume area [N], 4 face-centre lat,
  * 5 face-centre lon, 6 map factor at node 0, 7 map factor at node 1,
- * 8/9 face normal (x, y), 10/11 intercept (lat, lon). */
+ * 8/9 face normal (x, y), 10/11 intercept (lat, lon), 12/13 node lat/lon [N]. */
 odis_status odis_mesh_field(const odis_mesh* m, int which, double* out);
 /* face_nodes [E][2], faces [N][6], node_face_dir [N][6], interp_friends [E][10],
  * interp_w [E][10], interp_n [E]; any may be NULL */
