@@ -8,7 +8,7 @@
 // kept at FP64 accuracy as a double-float master (hi, lo) pair: hi is the FP32
 // value the stencils read, lo the rounding residual that only the owning thread
 // reads and writes.  The dissipated-power reduction is FP32 over at most
-// kBatchRows * 64 non-negative terms per tile and FP64 beyond.
+// 4 * 64 non-negative terms per tile and FP64 beyond.
 //
 // Layout.  Members are grouped by mesh; inside a group they are sorted by
 // steps per orbit (descending) and padded to a multiple of four.  Every state
@@ -31,7 +31,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -42,7 +44,7 @@ namespace odis {
 namespace {
 
 constexpr int kBatchThreads = 256;
-constexpr int kBatchRows = 4;            // face / cell rows per thread per tile
+constexpr int kRowChoices[3] = {1, 2, 4};  // face / cell rows per thread per tile: a template choice, timed at creation
 constexpr int kMaxQuads = kBatchThreads; // members per group <= 4 * 256
 constexpr int kMaxGroups = 32;
 constexpr unsigned kBarrierSpins = 1u << 22;
@@ -190,34 +192,47 @@ __device__ bool grid_barrier(const BatchArgs& a, int* s_ok)
 }
 
 struct QuadInfo {
-    float4 dt, malpha, h, ecc, obl, dah, cosM, sinM;
-    int4 upd;      // member advances at this step
-    int4 pow_on;   // member's power of v^j is recorded
-    int4 euler;    // AB3 start-up (forward Euler) at this step
-    bool any_upd, any_pow;
+    float4 dt, malpha, ce, co, se, so;   // forcing weights: cos/sin of the phase times eccentricity/obliquity
+    float4 w;                            // face phase: alpha * h (dissipation); cell phase: h
+    unsigned mask;                       // bits 0-3 member advances, 4-7 its power is recorded, 8-11 forward-Euler step
 };
 
+__device__ __forceinline__ int4 bits4(unsigned m, int shift)
+{
+    return make_int4((m >> shift) & 1u, (m >> (shift + 1)) & 1u, (m >> (shift + 2)) & 1u, (m >> (shift + 3)) & 1u);
+}
+
 __device__ __forceinline__ QuadInfo quad_info(const BatchArgs& a, int slot, int j, const float* s_cos,
-                                              const float* s_sin)
+                                              const float* s_sin, bool face)
 {
     QuadInfo q;
     const MemberDev& m = a.mem;
     const int4 S = __ldg(reinterpret_cast<const int4*>(m.S + slot));
     const int4 b = __ldg(reinterpret_cast<const int4*>(m.base + slot));
-    q.upd = make_int4(j < S.x, j < S.y, j < S.z, j < S.w);
-    q.pow_on = make_int4(j >= 1 && j <= S.x, j >= 1 && j <= S.y, j >= 1 && j <= S.z, j >= 1 && j <= S.w);
-    q.any_upd = q.upd.x | q.upd.y | q.upd.z | q.upd.w;
-    q.any_pow = q.pow_on.x | q.pow_on.y | q.pow_on.z | q.pow_on.w;
-    const int il = a.init_load;
-    q.euler = make_int4(!(il || b.x + j > 1), !(il || b.y + j > 1), !(il || b.z + j > 1), !(il || b.w + j > 1));
+    const int Sv[4] = {S.x, S.y, S.z, S.w}, bv[4] = {b.x, b.y, b.z, b.w};
+    unsigned mask = 0;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        mask |= (unsigned)(j < Sv[c]) << c;
+        mask |= (unsigned)(j >= 1 && j <= Sv[c]) << (4 + c);
+        mask |= (unsigned)!(a.init_load || bv[c] + j > 1) << (8 + c);
+    }
+    q.mask = mask;
     q.dt = __ldg(reinterpret_cast<const float4*>(m.dt + slot));
-    q.malpha = __ldg(reinterpret_cast<const float4*>(m.malpha + slot));
-    q.h = __ldg(reinterpret_cast<const float4*>(m.h + slot));
-    q.ecc = __ldg(reinterpret_cast<const float4*>(m.ecc + slot));
-    q.obl = __ldg(reinterpret_cast<const float4*>(m.obl + slot));
-    q.dah = __ldg(reinterpret_cast<const float4*>(m.dah + slot));
-    q.cosM = *reinterpret_cast<const float4*>(s_cos + slot);
-    q.sinM = *reinterpret_cast<const float4*>(s_sin + slot);
+    if (face) {
+        q.malpha = __ldg(reinterpret_cast<const float4*>(m.malpha + slot));
+        const float4 ecc = __ldg(reinterpret_cast<const float4*>(m.ecc + slot));
+        const float4 obl = __ldg(reinterpret_cast<const float4*>(m.obl + slot));
+        const float4 cm = *reinterpret_cast<const float4*>(s_cos + slot);
+        const float4 sm = *reinterpret_cast<const float4*>(s_sin + slot);
+        q.ce = mul4v(cm, ecc);
+        q.co = mul4v(cm, obl);
+        q.se = mul4v(sm, ecc);
+        q.so = mul4v(sm, obl);
+        q.w = __ldg(reinterpret_cast<const float4*>(m.dah + slot));
+    } else {
+        q.w = __ldg(reinterpret_cast<const float4*>(m.h + slot));
+    }
     return q;
 }
 
@@ -225,6 +240,7 @@ __device__ __forceinline__ QuadInfo quad_info(const BatchArgs& a, int slot, int 
 // thread's quad (components outside pow_on are zero).  State arrays are read
 // with plain (L1-cacheable) loads: the grid barrier before each phase is an
 // acquire at GPU scope, so no line cached before it is used after it.
+template <int R>
 __device__ __forceinline__ float4 face_tile(const BatchArgs& a, const GroupDev& G, const QuadInfo& q, int x, int y,
                                             int ny, int e0, int j, bool& bad)
 {
@@ -239,7 +255,7 @@ __device__ __forceinline__ float4 face_tile(const BatchArgs& a, const GroupDev& 
     const float* __restrict__ w = G.w;
     float4 pw = f4(0.f);
 #pragma unroll
-    for (int r = 0; r < kBatchRows; r++) {
+    for (int r = 0; r < R; r++) {
         const int e = e0 + y + ny * r;
         if (e < E) {
             float4 ts = f4(0.f);
@@ -247,35 +263,36 @@ __device__ __forceinline__ float4 face_tile(const BatchArgs& a, const GroupDev& 
             for (int k = 0; k < 10; k++) ts = fma4(__ldg(&w[k * E + e]), vcur[(size_t)__ldg(&nbr[k * E + e]) * Bq + x], ts);
             const size_t o = (size_t)e * Bq + x;
             const float4 ve = vcur[o];
-            if (q.any_pow) {
+            if (q.mask & 0xF0u) {
                 const float4 ke = fma4v(ve, ve, mul4v(ts, ts));
-                const float4 d = mul4(__ldg(&G.dbase[e]), mul4v(q.dah, ke));
-                pw = add4v(pw, sel4(q.pow_on, d, f4(0.f)));
+                const float4 d = mul4(__ldg(&G.dbase[e]), mul4v(q.w, ke));
+                pw = add4v(pw, sel4(bits4(q.mask, 4), d, f4(0.f)));
             }
-            if (q.any_upd) {
+            if (q.mask & 0xFu) {
+                const int4 upd = bits4(q.mask, 0);
                 const int i0 = __ldg(&G.n0[e]), i1 = __ldg(&G.n1[e]);
                 const float g0 = __ldg(&G.gg0[e]), g1 = __ldg(&G.gg1[e]);
                 const float4 f0 = fma4(__ldg(&G.cor[e]), ts, fma4(g0, eta[(size_t)i0 * Bq + x], mul4(g1, eta[(size_t)i1 * Bq + x])));
-                const float4 fp = fma4v(q.ecc, f4(__ldg(&G.pe[e])), mul4v(q.obl, f4(__ldg(&G.po[e]))));
-                const float4 fq = fma4v(q.ecc, f4(__ldg(&G.qe[e])), mul4v(q.obl, f4(__ldg(&G.qo[e]))));
-                const float4 gu = fma4v(q.cosM, fp, mul4v(q.sinM, fq));
+                const float4 gu = fma4v(q.ce, f4(__ldg(&G.pe[e])), fma4v(q.co, f4(__ldg(&G.po[e])),
+                                        fma4v(q.se, f4(__ldg(&G.qe[e])), mul4v(q.so, f4(__ldg(&G.qo[e]))))));
                 const float4 drag = fma4v(q.malpha, ve, gu);
                 const float4 f1 = hprev[o], f2 = hcur[o];
                 const float4 ab = fma4(a.ab3c, f2, fma4(a.ab3b, f1, mul4(a.ab3a, f0)));
-                const float4 inc = sel4(q.euler, f0, ab);
-                st4m(&hcur[o], f0, q.upd);
+                const float4 inc = sel4(bits4(q.mask, 8), f0, ab);
+                st4m(&hcur[o], f0, upd);
                 float4 hi = ve, lo = vlo[o];
                 df_acc4(hi, lo, mul4v(q.dt, add4v(inc, drag)));
-                st4m(&vnext[o], hi, q.upd);
-                st4m(&vlo[o], lo, q.upd);
-                bad |= (q.upd.x && !isfinite(hi.x)) || (q.upd.y && !isfinite(hi.y)) || (q.upd.z && !isfinite(hi.z)) ||
-                       (q.upd.w && !isfinite(hi.w));
+                st4m(&vnext[o], hi, upd);
+                st4m(&vlo[o], lo, upd);
+                bad |= (upd.x && !isfinite(hi.x)) || (upd.y && !isfinite(hi.y)) || (upd.z && !isfinite(hi.z)) ||
+                       (upd.w && !isfinite(hi.w));
             }
         }
     }
     return pw;
 }
 
+template <int R>
 __device__ __forceinline__ void cell_tile(const GroupDev& G, const QuadInfo& q, const BatchArgs& a, int x, int y,
                                           int ny, int c0, int j)
 {
@@ -288,22 +305,23 @@ __device__ __forceinline__ void cell_tile(const GroupDev& G, const QuadInfo& q, 
     const int* __restrict__ edge = G.edge;
     const float* __restrict__ dv = G.dv;
 #pragma unroll
-    for (int r = 0; r < kBatchRows; r++) {
+    for (int r = 0; r < R; r++) {
         const int i = c0 + y + ny * r;
         if (i < N) {
             float4 qd = f4(0.f);
 #pragma unroll
             for (int k = 0; k < 6; k++) qd = fma4(__ldg(&dv[k * N + i]), vn[(size_t)__ldg(&edge[k * N + i]) * Bq + x], qd);
-            qd = mul4v(q.h, qd);
+            qd = mul4v(q.w, qd);
             const size_t o = (size_t)i * Bq + x;
             const float4 f1 = hprev[o], f2 = hcur[o];
             const float4 ab = fma4(a.ab3c, f2, fma4(a.ab3b, f1, mul4(a.ab3a, qd)));
-            const float4 inc = sel4(q.euler, qd, ab);
-            st4m(&hcur[o], qd, q.upd);
+            const int4 upd = bits4(q.mask, 0);
+            const float4 inc = sel4(bits4(q.mask, 8), qd, ab);
+            st4m(&hcur[o], qd, upd);
             float4 hi = ehi[o], lo = elo[o];
             df_acc4(hi, lo, mul4v(q.dt, inc));
-            st4m(&ehi[o], hi, q.upd);
-            st4m(&elo[o], lo, q.upd);
+            st4m(&ehi[o], hi, upd);
+            st4m(&elo[o], lo, upd);
         }
     }
 }
@@ -323,7 +341,8 @@ __device__ __forceinline__ int active_quads(const BatchArgs& a, const GroupDev& 
     return lo;
 }
 
-__global__ void __launch_bounds__(kBatchThreads, 2) k_batch(BatchArgs a, int j0, int j1)
+template <int R>
+__global__ void __launch_bounds__(kBatchThreads) k_batch(BatchArgs a, int j0, int j1)
 {
     extern __shared__ double s_dyn[];
     double* s_acc = s_dyn;                                   // [P] power of this CTA's tiles, per member slot
@@ -349,7 +368,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(BatchArgs a, int j0,
             const GroupDev& G = a.groups[tid];
             const int qa = active_quads(a, G, j);
             const int ny = qa ? kBatchThreads / qa : 1;
-            const int rows = ny * kBatchRows;
+            const int rows = ny * R;
             s_qa[tid] = qa;
             s_ny[tid] = ny;
             s_ft0[tid + 1] = qa ? (G.E + rows - 1) / rows : 0;
@@ -375,9 +394,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(BatchArgs a, int j0,
             const int x = tid % qa, y = tid / qa;
             float4 pw = f4(0.f);
             if (y < ny) {
-                const QuadInfo q = quad_info(a, G.moff + 4 * x, j, s_cos, s_sin);
-                if (q.any_upd || q.any_pow)
-                    pw = face_tile(a, G, q, x, y, ny, (t - s_ft0[g]) * ny * kBatchRows, j, bad);
+                const QuadInfo q = quad_info(a, G.moff + 4 * x, j, s_cos, s_sin, true);
+                if (q.mask & 0xFFu)
+                    pw = face_tile<R>(a, G, q, x, y, ny, (t - s_ft0[g]) * ny * R, j, bad);
             }
             s_pw[tid] = pw;
             __syncthreads();
@@ -426,8 +445,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(BatchArgs a, int j0,
             const int qa = s_qa[g], ny = s_ny[g];
             const int x = tid % qa, y = tid / qa;
             if (y < ny) {
-                const QuadInfo q = quad_info(a, G.moff + 4 * x, j, s_cos, s_sin);
-                if (q.any_upd) cell_tile(G, q, a, x, y, ny, (t - s_ct0[g]) * ny * kBatchRows, j);
+                const QuadInfo q = quad_info(a, G.moff + 4 * x, j, s_cos, s_sin, false);
+                if (q.mask & 0xFu) cell_tile<R>(G, q, a, x, y, ny, (t - s_ct0[g]) * ny * R, j);
             }
         }
         if (j + 1 < j1 && !grid_barrier(a, &s_ok)) return;
@@ -482,7 +501,9 @@ struct odis_batch {
     double* d_part = nullptr;
     unsigned* d_bar = nullptr;           // [0] count, [1] generation
     int* d_status = nullptr;
-    int grid = 0;
+    int grid = 0;                        // CTAs of the chosen variant
+    int variant = 2;                     // index into kRowChoices
+    int grid_v[3] = {0, 0, 0};           // co-resident CTAs of each variant (0: cannot launch)
     int ftiles = 0, ctiles = 0;
     cudaStream_t stream = nullptr;
     long long launches = 0;
@@ -496,6 +517,57 @@ struct odis_batch {
         cudaError_t _e = (call);                       \
         if (_e != cudaSuccess) return ODIS_ERR_CUDA;   \
     } while (0)
+
+static const void* batch_kernel(int v)
+{
+    return v == 0 ? (const void*)k_batch<1> : v == 1 ? (const void*)k_batch<2> : (const void*)k_batch<4>;
+}
+
+static int zero_state(odis_batch* b)
+{
+    for (GroupDev& G : b->groups) {
+        const size_t ev = (size_t)G.E * 4 * G.Bq, cv = (size_t)G.N * 4 * G.Bq;
+        for (int k = 0; k < 2; k++) {
+            ODIS_BCK(cudaMemset(G.vhi[k], 0, sizeof(float) * ev));
+            ODIS_BCK(cudaMemset(G.hv[k], 0, sizeof(float) * ev));
+            ODIS_BCK(cudaMemset(G.he[k], 0, sizeof(float) * cv));
+        }
+        ODIS_BCK(cudaMemset(G.vlo, 0, sizeof(float) * ev));
+        ODIS_BCK(cudaMemset(G.ehi, 0, sizeof(float) * cv));
+        ODIS_BCK(cudaMemset(G.elo, 0, sizeof(float) * cv));
+    }
+    std::fill(b->base.begin(), b->base.end(), 0);
+    return ODIS_OK;
+}
+
+// Rows per thread per tile: ODIS_BATCH_ROWS=1|2|4 fixes it; otherwise each
+// variant runs 24 steps from rest (after a 4-step warm-up) and the fastest is
+// kept.  The members are then put back at rest, step 0.
+static int choose_rows(odis_batch* b)
+{
+    const char* e = std::getenv("ODIS_BATCH_ROWS");
+    int forced = -1;
+    if (e) for (int v = 0; v < 3; v++) if (std::atoi(e) == kRowChoices[v]) forced = v;
+    double best = 1e300;
+    int pick = -1;
+    for (int v = 0; v < 3; v++) {
+        if (!b->grid_v[v] || (forced >= 0 && v != forced)) continue;
+        b->variant = v;
+        b->grid = b->grid_v[v];
+        if (forced >= 0) { pick = v; break; }
+        int st = odis_batch_run(b, 0.0, 4, nullptr, 0, nullptr, 0, 0);
+        const auto t0 = std::chrono::steady_clock::now();
+        if (st == ODIS_OK || st == ODIS_ERR_NONFINITE) st = odis_batch_run(b, 0.0, 24, nullptr, 0, nullptr, 0, 0);
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (st != ODIS_OK && st != ODIS_ERR_NONFINITE) return st;
+        if (ms < best) { best = ms; pick = v; }
+    }
+    if (pick < 0) return ODIS_ERR_CUDA;
+    b->variant = pick;
+    b->grid = b->grid_v[pick];
+    b->launches = 0;
+    return zero_state(b);
+}
 
 static int build_group(odis_batch* b, const Mesh& m, GroupDev& G)
 {
@@ -634,7 +706,7 @@ extern "C" odis_status odis_batch_create(const odis_params* common, const odis_m
         P += 4 * G.Bq;
         const int st = build_group(b.get(), m, G);
         if (st != ODIS_OK) return st;
-        const int rows = G.ny * kBatchRows;
+        const int rows = G.ny * 4;
         G.ftile0 = ft;
         G.ftiles = (G.E + rows - 1) / rows;
         ft += G.ftiles;
@@ -687,14 +759,21 @@ extern "C" odis_status odis_batch_create(const odis_params* common, const odis_m
     ODIS_BCK(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) return ODIS_ERR_CUDA;
     const size_t smem = (sizeof(double) + 2 * sizeof(float)) * (size_t)P;
-    if (smem > 48 * 1024) ODIS_BCK(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ODIS_BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kBatchThreads, smem));
-    if (per_sm < 1) return ODIS_ERR_CUDA;
-    b->grid = sms * std::min(per_sm, 4);
-    b->d_part = A.alloc<double>((size_t)2 * b->grid * P);
+    int gmax = 0;
+    for (int v = 0; v < 3; v++) {
+        const void* f = batch_kernel(v);
+        if (smem > 48 * 1024) ODIS_BCK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        ODIS_BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kBatchThreads, smem));
+        b->grid_v[v] = per_sm >= 1 ? sms * std::min(per_sm, 4) : 0;
+        gmax = std::max(gmax, b->grid_v[v]);
+    }
+    if (gmax < 1) return ODIS_ERR_CUDA;
+    b->d_part = A.alloc<double>((size_t)2 * gmax * P);
     if (!b->d_part) return ODIS_ERR_NOMEM;
     ODIS_BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     ODIS_BCK(cudaDeviceSynchronize());
+    const int st = choose_rows(b.get());
+    if (st != ODIS_OK) return st;
     *out = b.release();
     return ODIS_OK;
 }
@@ -777,7 +856,7 @@ extern "C" odis_status odis_batch_run(odis_batch* b, double orbits, int steps, d
         for (int j0 = 0; j0 <= smax && st == ODIS_OK; j0 += chunk) {
             int j1 = std::min(smax + 1, j0 + chunk);
             void* args[] = {&a, &j0, &j1};
-            if (cudaLaunchCooperativeKernel((const void*)k_batch, dim3(b->grid), dim3(kBatchThreads), args, smem, s) !=
+            if (cudaLaunchCooperativeKernel(batch_kernel(b->variant), dim3(b->grid), dim3(kBatchThreads), args, smem, s) !=
                 cudaSuccess) { st = ODIS_ERR_CUDA; break; }
             b->launches++;
             int h = 0;

@@ -113,6 +113,7 @@ struct odis_ctx {
     double exec_ms[2] = {0, 0};  // those timings: graph-replayed pair, persistent loop (ms per step)
     int part_cap = 0;            // steps the plan's partial buffer holds
     double persist_frac = 0.0;   // fraction of faces interior to their CTA
+    int fold_rows = 0;           // steps per run chunk (rows of the partial table minus one)
     long long launches = 0;      // kernels of this library launched by this context
     ~odis_ctx() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -521,7 +522,9 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     c->d_iter = A.alloc<long long>(1);
     c->d_run_first = A.alloc<long long>(1);
     c->d_status = A.alloc<int>(1);
-    c->d_partial = A.alloc<double>(c->eb + 32);
+    // per-run table of the face kernels' dissipation partials, one row per step, folded once per run chunk
+    c->fold_rows = std::max(kGraphSteps, std::min(4096, (int)((64ll << 20) / (8ll * c->eb)) / kGraphSteps * kGraphSteps));
+    c->d_partial = A.alloc<double>((size_t)(c->fold_rows + 1) * c->eb + 32);
     if (!c->d_iter || !c->d_run_first || !c->d_status || !c->d_partial) return ODIS_ERR_NOMEM;
 
     std::vector<double> Ua, Ub;
@@ -823,26 +826,9 @@ static int prepare_phase(odis_ctx* c, long long first, int n)
     return cudaGetLastError() == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
 }
 
-extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem)
+// One chunk of at most fold_rows steps; dpow (device, nullable) receives its power series.
+static int run_chunk(odis_ctx* c, int n, double* dpow)
 {
-    if (!c || n < 0 || !mem_ok(mem)) return ODIS_ERR_ARG;
-    if (n == 0) return ODIS_OK;
-    double* dpow = nullptr;
-    if (power) {
-        if (mem == ODIS_MEM_DEVICE) dpow = power;
-        else {
-            if (n > c->power_cap) {
-                if (c->d_power) cudaFree(c->d_power);
-                c->d_power = nullptr;
-                c->power_cap = 0;
-                ODIS_CK(cudaMalloc(&c->d_power, sizeof(double) * n));
-                c->power_cap = n;
-            }
-            dpow = c->d_power;
-        }
-    }
-    // the graph bakes in the state struct, so the power pointer lives in the
-    // state only for eager launches; graphs are rebuilt if it changes
     const long long first = c->iter;
     ODIS_CK(cudaMemcpyAsync(c->d_run_first, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
     ODIS_CK(cudaMemcpyAsync(c->d_iter, &first, sizeof(long long), cudaMemcpyHostToDevice, c->stream));
@@ -850,15 +836,14 @@ extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem
         const int st = prepare_phase(c, first, n);
         if (st != ODIS_OK) return st;
     }
-    if (c->s64.power != dpow || c->s32.power != dpow || c->sdf.power != dpow) {
-        c->s64.power = dpow;
-        c->s32.power = dpow;
-        c->sdf.power = dpow;
-        if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-    }
+    // only the end-of-chunk fold writes the power series (the step kernels write
+    // partials), so the instantiated graph does not depend on dpow
+    c->s64.power = dpow;
+    c->s32.power = dpow;
+    c->sdf.power = dpow;
     bool persisted = false;
     if (c->persist_ok && c->persist_on) {
-        // one cooperative launch for the whole run
+        // one cooperative launch for the whole chunk
         if (n + 1 > c->part_cap) {
             if (c->plan.part) cudaFree(c->plan.part);
             c->plan.part = nullptr;
@@ -892,16 +877,43 @@ extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem
             }
         }
         if (done < n) enqueue_steps(c, n - done);
-        if (c->p.precision == ODIS_FP64) launch_power_tail<double>(c->op64.fc, c->s64, c->sc, c->stream);
-        else if (c->p.precision == ODIS_FP32) launch_power_tail<float>(c->op32.fc, c->s32, c->sc, c->stream);
-        else launch_power_tail_df(c->opdf.fc, c->sdf, c->sc, c->stream);
-        c->launches += 2;
+        if (c->p.precision == ODIS_FP64) launch_power_tail<double>(c->op64.fc, c->s64, c->sc, n, c->stream);
+        else if (c->p.precision == ODIS_FP32) launch_power_tail<float>(c->op32.fc, c->s32, c->sc, n, c->stream);
+        else launch_power_tail_df(c->opdf.fc, c->sdf, c->sc, n, c->stream);
+        c->launches += dpow ? 2 : 1;
     }
     ODIS_CK(cudaGetLastError());
+    c->iter += n;
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem)
+{
+    if (!c || n < 0 || !mem_ok(mem)) return ODIS_ERR_ARG;
+    if (n == 0) return ODIS_OK;
+    double* dpow = nullptr;
+    if (power) {
+        if (mem == ODIS_MEM_DEVICE) dpow = power;
+        else {
+            if (n > c->power_cap) {
+                if (c->d_power) cudaFree(c->d_power);
+                c->d_power = nullptr;
+                c->power_cap = 0;
+                ODIS_CK(cudaMalloc(&c->d_power, sizeof(double) * n));
+                c->power_cap = n;
+            }
+            dpow = c->d_power;
+        }
+    }
+    for (int done = 0; done < n;) {
+        const int k = std::min(n - done, c->fold_rows);
+        const int st = run_chunk(c, k, dpow ? dpow + done : nullptr);
+        if (st != ODIS_OK) return st;
+        done += k;
+    }
     if (power && mem == ODIS_MEM_HOST)
         ODIS_CK(cudaMemcpyAsync(power, dpow, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     ODIS_CK(cudaStreamSynchronize(c->stream));
-    c->iter += n;
     int h = 0;
     ODIS_CK(cudaMemcpy(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost));
     if (h) ODIS_CK(cudaMemset(c->d_status, 0, sizeof(int)));

@@ -71,8 +71,8 @@ struct State {
     const long long* iter;   // device step counter (base of the current chunk)
     const long long* run_first;  // first step index of the current run
     const T* phase;      // [2n] cos, sin of the forcing phase Omega*t^{n+1} for each step of the current run
-    double* partial;     // [edge blocks] per-block dissipation partial sums
-    double* power;       // [n] output power series of the current run (nullable)
+    double* partial;     // [steps of the run chunk + 1][edge blocks] per-block dissipation partial sums
+    double* power;       // [n] output power series of the current run chunk (nullable; written by the fold only)
     int* status;         // device status word
 };
 

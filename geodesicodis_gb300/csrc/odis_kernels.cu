@@ -145,14 +145,15 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, Stat
         }
     }
     const double bs = block_power<T>(pw, s_red);
-    if (threadIdx.x == 0) st.partial[blockIdx.x] = bs;
+    // row kstep of the run's partial table: the dissipation of v^it, the power after step it-1
+    if (threadIdx.x == 0) st.partial[kstep * gridDim.x + blockIdx.x] = bs;
 }
 
 // ---------------------------------------------------------------------------
 // fused step, cell part
 // ---------------------------------------------------------------------------
 template <class T, bool kMaster>
-__global__ void __launch_bounds__(kStepThreads) k_cell_step(CellCoef<T> cc, State<T> st, StepConst sc, int offset, int n_partial)
+__global__ void __launch_bounds__(kStepThreads) k_cell_step(CellCoef<T> cc, State<T> st, StepConst sc, int offset)
 {
     const long long it = *st.iter + offset;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -179,12 +180,6 @@ __global__ void __launch_bounds__(kStepThreads) k_cell_step(CellCoef<T> cc, Stat
             st.eta[i] = fmaT<T>(inc, kdt, st.eta[i]);
         }
     }
-    // dissipation of v^n (the state this step started from) = power of step n-1
-    if (blockIdx.x == 0 && threadIdx.x < 32) {
-        const double s = fold_partials(st.partial, n_partial);
-        const long long k = it - 1 - *st.run_first;
-        if (threadIdx.x == 0 && k >= 0 && st.power) st.power[k] = s;
-    }
 }
 
 // Dissipation of the current v (after the last step of a run).
@@ -205,15 +200,17 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial(FaceCoef<T> fc, 
         pw = (double)(__ldg(&fc.diss[e]) * fmaT<T>(ve, ve, tsum * tsum));
     }
     const double bs = block_sum<kStepThreads>(pw, s_red);
-    if (threadIdx.x == 0) st.partial[blockIdx.x] = bs;
+    if (threadIdx.x == 0) st.partial[(it - *st.run_first) * gridDim.x + blockIdx.x] = bs;
 }
 
-template <class T>
-__global__ void k_power_tail(State<T> st, int n_partial)
+// power[k] = sum of row k+1 of the run's partial table (k < n), one warp per step,
+// the partials of a row in a fixed order
+__global__ void k_power_fold(const double* __restrict__ part, int nb, int n, double* __restrict__ power)
 {
-    const double s = fold_partials(st.partial, n_partial);
-    const long long k = *st.iter - 1 - *st.run_first;
-    if (threadIdx.x == 0 && k >= 0 && st.power) st.power[k] = s;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (k >= n) return;
+    const double s = fold_partials(part + (size_t)(k + 1) * nb, nb);
+    if ((threadIdx.x & 31) == 0) power[k] = s;
 }
 
 __global__ void k_bump_iter(long long* iter, int n)
@@ -371,9 +368,8 @@ void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc,
 template <class T, bool kMaster>
 void launch_cell(const CellCoef<T>& cc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
-    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
     const int cb = (sc.N + kStepThreads - 1) / kStepThreads;
-    k_cell_step<T, kMaster><<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset, eb);
+    k_cell_step<T, kMaster><<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset);
 }
 
 template <class T, bool kMaster>
@@ -385,11 +381,17 @@ void launch_step(const FaceCoef<T>& fc, const CellCoef<T>& cc, const State<T>& s
 }
 
 template <class T>
-void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, cudaStream_t s)
+void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int n, cudaStream_t s)
 {
     const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
     k_power_partial<T><<<eb, kStepThreads, 0, s>>>(fc, st, sc);
-    k_power_tail<T><<<1, 32, 0, s>>>(st, eb);
+    launch_power_fold(st.partial, eb, n, st.power, s);
+}
+
+void launch_power_fold(const double* part, int nb, int n, double* power, cudaStream_t s)
+{
+    if (!power || n <= 0) return;
+    k_power_fold<<<(n * 32 + 255) / 256, 256, 0, s>>>(part, nb, n, power);
 }
 
 void launch_bump(long long* iter, int n, cudaStream_t s) { k_bump_iter<<<1, 32, 0, s>>>(iter, n); }
@@ -402,8 +404,8 @@ template void launch_step<double, false>(const FaceCoef<double>&, const CellCoef
                                          const StepConst&, int, cudaStream_t);
 template void launch_step<float, true>(const FaceCoef<float>&, const CellCoef<float>&, const State<float>&,
                                        const StepConst&, int, cudaStream_t);
-template void launch_power_tail<double>(const FaceCoef<double>&, const State<double>&, const StepConst&, cudaStream_t);
-template void launch_power_tail<float>(const FaceCoef<float>&, const State<float>&, const StepConst&, cudaStream_t);
+template void launch_power_tail<double>(const FaceCoef<double>&, const State<double>&, const StepConst&, int, cudaStream_t);
+template void launch_power_tail<float>(const FaceCoef<float>&, const State<float>&, const StepConst&, int, cudaStream_t);
 
 static inline int blocks(int n, int t) { return (n + t - 1) / t; }
 

@@ -15,7 +15,9 @@ template <class T, bool kMaster>
 void launch_step(const FaceCoef<T>& fc, const CellCoef<T>& cc, const State<T>& st, const StepConst& sc,
                  int offset, cudaStream_t s);
 template <class T>
-void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, cudaStream_t s);
+void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int n, cudaStream_t s);
+// power[k] = sum of row k+1 of a run's partial table [n+1][nb] (no-op without power)
+void launch_power_fold(const double* part, int nb, int n, double* power, cudaStream_t s);
 void launch_bump(long long* iter, int n, cudaStream_t s);
 // forcing-phase table of a run: out[2k], out[2k+1] = cos, sin of Omega*(dt*(first+k) + dt)
 void launch_phase(void* out, int precision, long long first, int n, double dt, double angvel, cudaStream_t s);
@@ -23,7 +25,7 @@ void launch_phase(void* out, int precision, long long first, int n, double dt, d
 // ODIS_DF64 method (odis_kernels_df.cu)
 void launch_edge_df(const FaceCoef<float2>& fc, const State<float2>& st, const StepConst& sc, int offset, cudaStream_t s);
 void launch_cell_df(const CellCoef<float2>& cc, const State<float2>& st, const StepConst& sc, int offset, cudaStream_t s);
-void launch_power_tail_df(const FaceCoef<float2>& fc, const State<float2>& st, const StepConst& sc, cudaStream_t s);
+void launch_power_tail_df(const FaceCoef<float2>& fc, const State<float2>& st, const StepConst& sc, int n, cudaStream_t s);
 
 void launch_momentum(const FaceCoef<double>& fc, int E, int Ep, double* dvdt, const double* v, const double* eta,
                      cudaStream_t s);

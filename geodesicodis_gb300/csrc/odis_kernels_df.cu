@@ -14,13 +14,6 @@ namespace odis {
 
 namespace {
 
-__device__ __forceinline__ double warp_sum_dd(double x)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    return x;
-}
-
 // block sum of a df64 per thread; the result (as FP64) is valid in thread 0
 __device__ __forceinline__ double block_sum_df(df64 x, df64* smem)
 {
@@ -78,11 +71,11 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc
         if (!df_finite(vn)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
     }
     const double bs = block_sum_df(pw, s_red);
-    if (threadIdx.x == 0) st.partial[blockIdx.x] = bs;
+    // row kstep of the run's partial table: the dissipation of v^it, the power after step it-1
+    if (threadIdx.x == 0) st.partial[kstep * gridDim.x + blockIdx.x] = bs;
 }
 
-__global__ void __launch_bounds__(kStepThreads) k_cell_step_df(CellCoef<df64> cc, State<df64> st, StepConst sc, int offset,
-                                                               int n_partial)
+__global__ void __launch_bounds__(kStepThreads) k_cell_step_df(CellCoef<df64> cc, State<df64> st, StepConst sc, int offset)
 {
     const long long it = *st.iter + offset;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -102,13 +95,6 @@ __global__ void __launch_bounds__(kStepThreads) k_cell_step_df(CellCoef<df64> cc
         hcur[i] = q;
         st.eta[i] = df_fma(inc, sc.df_dt, st.eta[i]);
     }
-    if (blockIdx.x == 0 && threadIdx.x < 32) {
-        double s = 0.0;
-        for (int k = threadIdx.x; k < n_partial; k += 32) s += st.partial[k];
-        s = warp_sum_dd(s);
-        const long long k = it - 1 - *st.run_first;
-        if (threadIdx.x == 0 && k >= 0 && st.power) st.power[k] = s;
-    }
 }
 
 __global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64> fc, State<df64> st, StepConst sc)
@@ -127,16 +113,7 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64
         pw = df_mul(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)));
     }
     const double bs = block_sum_df(pw, s_red);
-    if (threadIdx.x == 0) st.partial[blockIdx.x] = bs;
-}
-
-__global__ void k_power_tail_df(State<df64> st, int n_partial)
-{
-    double s = 0.0;
-    for (int k = threadIdx.x; k < n_partial; k += 32) s += st.partial[k];
-    s = warp_sum_dd(s);
-    const long long k = *st.iter - 1 - *st.run_first;
-    if (threadIdx.x == 0 && k >= 0 && st.power) st.power[k] = s;
+    if (threadIdx.x == 0) st.partial[(it - *st.run_first) * gridDim.x + blockIdx.x] = bs;
 }
 
 void launch_edge_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
@@ -147,16 +124,15 @@ void launch_edge_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepC
 
 void launch_cell_df(const CellCoef<df64>& cc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
-    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
     const int cb = (sc.N + kStepThreads - 1) / kStepThreads;
-    k_cell_step_df<<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset, eb);
+    k_cell_step_df<<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset);
 }
 
-void launch_power_tail_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, cudaStream_t s)
+void launch_power_tail_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, int n, cudaStream_t s)
 {
     const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
     k_power_partial_df<<<eb, kStepThreads, 0, s>>>(fc, st, sc);
-    k_power_tail_df<<<1, 32, 0, s>>>(st, eb);
+    launch_power_fold(st.partial, eb, n, st.power, s);
 }
 
 }  // namespace odis
