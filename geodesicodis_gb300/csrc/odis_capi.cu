@@ -376,10 +376,10 @@ static int alloc_state(odis_ctx* c, State<T>& s, bool split)
         s.he[k] = A.alloc<T>(c->Np);
         if (!s.v[k] || !s.hv[k] || !s.he[k]) return ODIS_ERR_NOMEM;
     }
-    s.vm = split ? A.alloc<double>(c->Ep) : nullptr;
+    s.vlo = split ? A.alloc<float>(c->Ep) : nullptr;
     s.eta = A.alloc<T>(c->Np);
-    s.etam = split ? A.alloc<double>(c->Np) : nullptr;
-    if (!s.eta || (split && (!s.vm || !s.etam))) return ODIS_ERR_NOMEM;
+    s.etalo = split ? A.alloc<float>(c->Np) : nullptr;
+    if (!s.eta || (split && (!s.vlo || !s.etalo))) return ODIS_ERR_NOMEM;
     s.usg = nullptr;
     s.iter = c->d_iter;
     s.run_first = c->d_run_first;
@@ -927,27 +927,32 @@ extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem
 // ---------------------------------------------------------------------------
 // device vector (or its FP64 master, when present) -> host doubles
 template <class T>
-static int get_vec(odis_ctx* c, const T* v, const double* master, size_t n, double* out)
+static int get_vec(odis_ctx* c, const T* v, const float* lo, size_t n, double* out)
 {
     (void)c;
-    if (master) {
-        ODIS_CK(cudaMemcpy(out, master, n * sizeof(double), cudaMemcpyDeviceToHost));
-        return ODIS_OK;
-    }
     std::vector<T> a(n);
     ODIS_CK(cudaMemcpy(a.data(), v, n * sizeof(T), cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < n; i++) out[i] = to_d(a[i]);
+    if (lo) {
+        std::vector<float> b(n);
+        ODIS_CK(cudaMemcpy(b.data(), lo, n * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; i++) out[i] += (double)b[i];
+    }
     return ODIS_OK;
 }
 
-// host doubles -> device vector (rounded to T) and its FP64 master, when present
+// host doubles -> device vector (rounded to T) and, when present, the rounding residual
 template <class T>
-static int set_vec(T* v, double* master, size_t n, const double* in)
+static int set_vec(T* v, float* lo, size_t n, const double* in)
 {
     std::vector<T> a(n);
     for (size_t i = 0; i < n; i++) a[i] = cvt<T>(in[i]);
     ODIS_CK(cudaMemcpy(v, a.data(), n * sizeof(T), cudaMemcpyHostToDevice));
-    if (master) ODIS_CK(cudaMemcpy(master, in, n * sizeof(double), cudaMemcpyHostToDevice));
+    if (lo) {
+        std::vector<float> b(n);
+        for (size_t i = 0; i < n; i++) b[i] = (float)(in[i] - to_d(a[i]));
+        ODIS_CK(cudaMemcpy(lo, b.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    }
     return ODIS_OK;
 }
 
@@ -957,8 +962,8 @@ static int get_state_t(odis_ctx* c, State<T>& s, double* v, double* eta, double*
     const long long k = c->iter;
     const size_t E = c->E, N = c->N;
     int st = ODIS_OK;
-    if (v) st = get_vec<T>(c, s.v[k & 1], s.vm, E, v);
-    if (st == ODIS_OK && eta) st = get_vec<T>(c, s.eta, s.etam, N, eta);
+    if (v) st = get_vec<T>(c, s.v[k & 1], s.vlo, E, v);
+    if (st == ODIS_OK && eta) st = get_vec<T>(c, s.eta, s.etalo, N, eta);
     for (int which = 0; which < 2 && st == ODIS_OK; which++) {
         double* out = which == 0 ? dvdt : detadt;
         if (!out) continue;
@@ -992,11 +997,11 @@ static int set_state_t(odis_ctx* c, State<T>& s, long long k, const double* v, c
     const size_t E = c->E, N = c->N;
     int st = ODIS_OK;
     for (int q = 0; q < 2; q++) ODIS_CK(cudaMemset(s.v[q], 0, sizeof(T) * c->Ep));
-    if (s.vm) ODIS_CK(cudaMemset(s.vm, 0, sizeof(double) * c->Ep));
-    if (v) st = set_vec<T>(s.v[k & 1], s.vm, E, v);
+    if (s.vlo) ODIS_CK(cudaMemset(s.vlo, 0, sizeof(float) * c->Ep));
+    if (v) st = set_vec<T>(s.v[k & 1], s.vlo, E, v);
     ODIS_CK(cudaMemset(s.eta, 0, sizeof(T) * c->Np));
-    if (s.etam) ODIS_CK(cudaMemset(s.etam, 0, sizeof(double) * c->Np));
-    if (st == ODIS_OK && eta) st = set_vec<T>(s.eta, s.etam, N, eta);
+    if (s.etalo) ODIS_CK(cudaMemset(s.etalo, 0, sizeof(float) * c->Np));
+    if (st == ODIS_OK && eta) st = set_vec<T>(s.eta, s.etalo, N, eta);
     for (int which = 0; which < 2 && st == ODIS_OK; which++) {
         const double* in = which == 0 ? dvdt : detadt;
         const size_t n = which == 0 ? E : N;

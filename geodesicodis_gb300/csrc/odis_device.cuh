@@ -55,17 +55,19 @@ struct StepConst {
 // v[0] and v[1]; the AB3 history alternates between hv[0] and hv[1]:
 // step `it` reads v[it&1], writes v[(it+1)&1], reads f(it-1) from
 // hv[(it+1)&1] and f(it-2) from hv[it&1] and then stores f(it) in hv[it&1].
-// The FP32-state variant keeps an FP64 master copy of v and eta (vm, etam)
-// that only the owning thread reads and writes: the AB3 increment, formed in
-// FP32 from FP32 stencils, is accumulated in FP64 and the FP32 copies the
-// stencils gather from are rounded from the master each step.
+// The FP32-state variant keeps v and eta as double-float pairs: the FP32 value
+// the stencils gather (v, eta) plus its rounding residual (vlo, etalo), which
+// only the owning thread reads and writes.  The AB3 increment, formed in FP32
+// from FP32 stencils, is accumulated into the pair with an error-free FP32
+// two-sum, i.e. at FP64 accuracy without FP64 instructions (GB300's FP64 and
+// FP64-conversion rates are a small fraction of its FP32 rate).
 template <class T>
 struct State {
     T* v[2];
-    double* vm;          // FP32 variant: FP64 master of v (nullptr in the FP64 method)
+    float* vlo;          // FP32 variant: rounding residual of v (nullptr otherwise)
     T* hv[2];
     T* eta;
-    double* etam;        // FP32 variant: FP64 master of eta
+    float* etalo;        // FP32 variant: rounding residual of eta
     T* he[2];
     const T* usg;        // [N] self-gravity potential / g (nullable)
     const long long* iter;   // device step counter (base of the current chunk)

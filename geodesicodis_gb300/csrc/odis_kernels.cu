@@ -23,6 +23,8 @@
 #include "odis_df64.cuh"
 #include "odis_kernels.cuh"
 
+#include <type_traits>
+
 #include <cmath>
 
 namespace odis {
@@ -69,6 +71,19 @@ __device__ __forceinline__ double fold_partials(const double* p, int n)
 template <class T> __device__ __forceinline__ T kc(double d, float f);
 template <> __device__ __forceinline__ double kc<double>(double d, float) { return d; }
 template <> __device__ __forceinline__ float kc<float>(double, float f) { return f; }
+
+// (hi, lo) += x exactly to double-float precision: Knuth two-sum, then renormalise
+// (explicit round-to-nearest adds, so no contraction can break the error terms)
+__device__ __forceinline__ void df_accumulate(float& hi, float& lo, float x)
+{
+    const float s = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    const float t = __fadd_rn(lo, err);
+    const float h2 = __fadd_rn(s, t);
+    lo = __fsub_rn(t, __fsub_rn(h2, s));
+    hi = h2;
+}
 
 // finiteness from the exponent bits (integer pipe, no FP64 compare)
 __device__ __forceinline__ bool finite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
@@ -132,11 +147,12 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, Stat
         }
         hcur[e] = f0;
         if constexpr (kMaster) {
-            // FP32 increment, FP64 accumulation in the master copy
-            const double vm = st.vm[e] + (double)(kdt * (inc + drag));
-            st.vm[e] = vm;
-            ((it & 1) ? st.v[0] : st.v[1])[e] = (T)vm;
-            if (!finite_bits(vm)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
+            // FP32 increment, double-float accumulation into (v, vlo)
+            float hi = ve, lo = st.vlo[e];
+            df_accumulate(hi, lo, kdt * (inc + drag));
+            st.vlo[e] = lo;
+            ((it & 1) ? st.v[0] : st.v[1])[e] = hi;
+            if (!isfinite(hi)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
         } else {
             T vn = fmaT<T>(inc, kdt, ve);
             vn = fmaT<T>(kdt, drag, vn);
@@ -147,6 +163,99 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, Stat
     const double bs = block_power<T>(pw, s_red);
     // row kstep of the run's partial table: the dissipation of v^it, the power after step it-1
     if (threadIdx.x == 0) st.partial[kstep * gridDim.x + blockIdx.x] = bs;
+}
+
+// ---------------------------------------------------------------------------
+// FP32-state variant, face part: two neighbouring faces per thread
+// ---------------------------------------------------------------------------
+// Same arithmetic per face as k_edge_step<float, true>, but each thread owns the
+// face pair (2p, 2p+1) and moves their coefficients and state with 8-byte
+// (float2 / int2) loads and stores.  With 4-byte values one face per thread
+// keeps only half the bytes in flight of the 8-byte methods, and the kernel is
+// latency bound well below the HBM rate once the working set leaves L2.  The
+// pad faces past E (Ep is a multiple of 128) have zero coefficients and point
+// at face 0, so the second face of an odd tail computes and stores zeros.
+__global__ void __launch_bounds__(kStepThreads) k_edge_step_f32x2(FaceCoef<float> fc, State<float> st, StepConst sc,
+                                                                     int offset)
+{
+    __shared__ double s_red[kStepThreads / 32];
+    const long long it = *st.iter + offset;
+    const long long kstep = it - *st.run_first;
+    const float cosM = st.phase[2 * kstep], sinM = st.phase[2 * kstep + 1];
+    const int e = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int Ep = sc.Ep;
+    const float* __restrict__ vin = ((it & 1) ? st.v[1] : st.v[0]);
+    float pw = 0.f;
+    if (e < sc.E) {
+        float tx = 0.f, ty = 0.f;
+#pragma unroll
+        for (int k = 0; k < kTrisk; k++) {
+            const float2 w = __ldg(reinterpret_cast<const float2*>(&fc.w[k * Ep + e]));
+            const int2 nb = __ldg(reinterpret_cast<const int2*>(&fc.nbr[k * Ep + e]));
+            tx = fmaf(w.x, vin[nb.x], tx);
+            ty = fmaf(w.y, vin[nb.y], ty);
+        }
+        const float2 ve = *reinterpret_cast<const float2*>(&vin[e]);
+        const float2 diss = __ldg(reinterpret_cast<const float2*>(&fc.diss[e]));
+        pw = diss.x * fmaf(ve.x, ve.x, tx * tx) + diss.y * fmaf(ve.y, ve.y, ty * ty);
+        const int2 n0 = __ldg(reinterpret_cast<const int2*>(&fc.n0[e]));
+        const int2 n1 = __ldg(reinterpret_cast<const int2*>(&fc.n1[e]));
+        const float2 g0 = __ldg(reinterpret_cast<const float2*>(&fc.gg0[e]));
+        const float2 g1 = __ldg(reinterpret_cast<const float2*>(&fc.gg1[e]));
+        const float2 cor = __ldg(reinterpret_cast<const float2*>(&fc.cor[e]));
+        const float2 fP = __ldg(reinterpret_cast<const float2*>(&fc.fP[e]));
+        const float2 fQ = __ldg(reinterpret_cast<const float2*>(&fc.fQ[e]));
+        float2 f0;
+        f0.x = fmaf(cor.x, tx, fmaf(g0.x, st.eta[n0.x], g1.x * st.eta[n1.x]));
+        f0.y = fmaf(cor.y, ty, fmaf(g0.y, st.eta[n0.y], g1.y * st.eta[n1.y]));
+        float2 gu = make_float2(fmaf(cosM, fP.x, sinM * fQ.x), fmaf(cosM, fP.y, sinM * fQ.y));
+        if (sc.use_sg) {
+            gu.x -= fmaf(g0.x, st.usg[n0.x], g1.x * st.usg[n1.x]);
+            gu.y -= fmaf(g0.y, st.usg[n0.y], g1.y * st.usg[n1.y]);
+        }
+        const float2 drag = make_float2(fmaf(sc.f_malpha, ve.x, gu.x), fmaf(sc.f_malpha, ve.y, gu.y));
+        float* hcur = ((it & 1) ? st.hv[1] : st.hv[0]);
+        float2 inc = f0;
+        if (sc.init_load || it > 1) {
+            const float2 f1 = *reinterpret_cast<const float2*>(&((it & 1) ? st.hv[0] : st.hv[1])[e]);
+            const float2 f2 = *reinterpret_cast<const float2*>(&hcur[e]);
+            inc.x = fmaf(sc.f_c, f2.x, fmaf(sc.f_b, f1.x, sc.f_a * f0.x));
+            inc.y = fmaf(sc.f_c, f2.y, fmaf(sc.f_b, f1.y, sc.f_a * f0.y));
+        }
+        *reinterpret_cast<float2*>(&hcur[e]) = f0;
+        float2 lo = *reinterpret_cast<const float2*>(&st.vlo[e]);
+        float2 hi = ve;
+        df_accumulate(hi.x, lo.x, sc.f_dt * (inc.x + drag.x));
+        df_accumulate(hi.y, lo.y, sc.f_dt * (inc.y + drag.y));
+        *reinterpret_cast<float2*>(&st.vlo[e]) = lo;
+        *reinterpret_cast<float2*>(&((it & 1) ? st.v[0] : st.v[1])[e]) = hi;
+        if (!isfinite(hi.x) || !isfinite(hi.y)) atomicOr(st.status, 1 << ODIS_ERR_NONFINITE);
+    }
+    const double bs = block_power<float>(pw, s_red);
+    if (threadIdx.x == 0) st.partial[kstep * gridDim.x + blockIdx.x] = bs;
+}
+
+// Dissipation of the current v after the last step of a run, in the pair layout of k_edge_step_f32x2.
+__global__ void __launch_bounds__(kStepThreads) k_power_partial_f32x2(FaceCoef<float> fc, State<float> st,
+                                                                      StepConst sc)
+{
+    __shared__ double s_red[kStepThreads / 32];
+    const long long it = *st.iter;
+    const int e = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int Ep = sc.Ep;
+    const float* __restrict__ vin = ((it & 1) ? st.v[1] : st.v[0]);
+    float pw = 0.f;
+    for (int c = 0; c < 2; c++) {
+        const int f = e + c;
+        if (f >= sc.E) break;
+        float tsum = 0.f;
+#pragma unroll
+        for (int k = 0; k < kTrisk; k++) tsum = fmaf(__ldg(&fc.w[k * Ep + f]), vin[__ldg(&fc.nbr[k * Ep + f])], tsum);
+        const float ve = vin[f];
+        pw += __ldg(&fc.diss[f]) * fmaf(ve, ve, tsum * tsum);
+    }
+    const double bs = block_power<float>(pw, s_red);
+    if (threadIdx.x == 0) st.partial[(it - *st.run_first) * gridDim.x + blockIdx.x] = bs;
 }
 
 // ---------------------------------------------------------------------------
@@ -173,9 +282,10 @@ __global__ void __launch_bounds__(kStepThreads) k_cell_step(CellCoef<T> cc, Stat
         }
         hcur[i] = q;
         if constexpr (kMaster) {
-            const double em = st.etam[i] + (double)(kdt * inc);
-            st.etam[i] = em;
-            st.eta[i] = (T)em;
+            float hi = st.eta[i], lo = st.etalo[i];
+            df_accumulate(hi, lo, kdt * inc);
+            st.etalo[i] = lo;
+            st.eta[i] = hi;
         } else {
             st.eta[i] = fmaT<T>(inc, kdt, st.eta[i]);
         }
@@ -361,8 +471,17 @@ __global__ void k_fold(const double* partial, int n, double divisor, double* out
 template <class T, bool kMaster>
 void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
-    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
-    k_edge_step<T, kMaster><<<eb, kStepThreads, 0, s>>>(fc, st, sc, offset);
+    if constexpr (kMaster) {
+        k_edge_step_f32x2<<<face_blocks(sc, true), kStepThreads, 0, s>>>(fc, st, sc, offset);
+    } else {
+        k_edge_step<T, kMaster><<<face_blocks(sc, false), kStepThreads, 0, s>>>(fc, st, sc, offset);
+    }
+}
+
+int face_blocks(const StepConst& sc, bool pairs)
+{
+    const int n = pairs ? (sc.E + 1) / 2 : sc.E;
+    return (n + kStepThreads - 1) / kStepThreads;
 }
 
 template <class T, bool kMaster>
@@ -383,8 +502,10 @@ void launch_step(const FaceCoef<T>& fc, const CellCoef<T>& cc, const State<T>& s
 template <class T>
 void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int n, cudaStream_t s)
 {
-    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
-    k_power_partial<T><<<eb, kStepThreads, 0, s>>>(fc, st, sc);
+    constexpr bool pairs = std::is_same<T, float>::value;
+    const int eb = face_blocks(sc, pairs);
+    if constexpr (pairs) k_power_partial_f32x2<<<eb, kStepThreads, 0, s>>>(fc, st, sc);
+    else k_power_partial<T><<<eb, kStepThreads, 0, s>>>(fc, st, sc);
     launch_power_fold(st.partial, eb, n, st.power, s);
 }
 

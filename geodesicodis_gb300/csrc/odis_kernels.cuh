@@ -18,6 +18,8 @@ template <class T>
 void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int n, cudaStream_t s);
 // power[k] = sum of row k+1 of a run's partial table [n+1][nb] (no-op without power)
 void launch_power_fold(const double* part, int nb, int n, double* power, cudaStream_t s);
+// CTAs of the face step kernel: one face per thread, or a face pair per thread (FP32 variant)
+int face_blocks(const StepConst& sc, bool pairs);
 void launch_bump(long long* iter, int n, cudaStream_t s);
 // forcing-phase table of a run: out[2k], out[2k+1] = cos, sin of Omega*(dt*(first+k) + dt)
 void launch_phase(void* out, int precision, long long first, int n, double dt, double angvel, cudaStream_t s);

@@ -48,7 +48,8 @@ typedef int odis_status;
 
 /* arithmetic of the state and stencils */
 #define ODIS_FP64 0             /* everything in FP64 (the reference's method) */
-#define ODIS_FP32 1             /* FP32 state and stencils; FP64 time accumulation and reductions */
+#define ODIS_FP32 1             /* FP32 state and stencils; time accumulation at FP64 accuracy (double-float
+                                   residual per unknown), power reductions FP64 across warps */
 #define ODIS_DF64 2             /* the FP64 method in double-float (2 x FP32, 48-bit significand) on the
                                    FP32 pipes; meets the FP64 parity bar (1e-10 against the FP64 oracle) */
 
