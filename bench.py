@@ -364,11 +364,64 @@ def run_sweep(args, fp64_plain: float, peak: float) -> dict:
             "steps_per_orbit_range": [int(spo.min()), int(spo.max())], "members_at_2000": int(np.sum(spo == 2000)),
             "nonfinite_members": int(np.sum(~np.isfinite(op).all(axis=1))),
             "launches": info["launches"] - l0, "grid": info["grid"], "padded_members": info["padded_members"],
+            "rows_per_thread": info["rows_per_thread"],
             "create_seconds": t_create,
             "hbm_roofline_uniform": {"bytes_per_cell_step": bytes_per_cell_step,
                                      "achieved_gbs": uni / el_u * bytes_per_cell_step / 1e9,
                                      "frac": uni / el_u * bytes_per_cell_step / 1e9 / peak},
             "timing": "host wall clock around the synchronous run call; inputs resident on the device"}
+
+
+def run_level8(args) -> dict:
+    """configs[4]: level 8 (655362 cells), eccentricity + obliquity tide, h = 20 km, drag 1e-6, self-gravity
+    l_max = 32; every method with and without self-gravity, `args.case_steps` timed steps each, errors of
+    FP32 and DF64 against FP64 after the same steps from rest."""
+    import geodesicodis_gb300 as g
+    h, alpha = 2e4, 1e-6
+    t = time.perf_counter()
+    mesh = g.Mesh.generate(8, RADIUS)
+    t_mesh = time.perf_counter() - t
+    angvel, P, _, _ = g.derive_time(ANGVEL_IN, 118394.0 / 8000)
+    w = mesh.gravity_wave_omega(GRAV, h)
+    n = g.stable_steps_per_orbit(P, w, 0.95)
+    fac = sh_factors(32)
+    E, N = mesh.n_edges, mesh.n_cells
+    out = {"workload": "level 8, FULL tide (e 0.0047, obliquity 0.2 deg), h 20 km, drag 1e-6, SH l_max 32",
+           "cells": N, "faces": E, "mesh_seconds": t_mesh, "steps_per_orbit_stable": n,
+           "omega_dt_at_8000_steps_per_orbit": w * P / 8000, "timed_steps": args.case_steps, "methods": {}}
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    finals = {}
+    for name, prec, lmax in (("fp32_sh32", g.FP32, 32), ("df64_sh32", g.DF64, 32), ("fp64_sh32", g.FP64, 32),
+                             ("fp32_plain", g.FP32, 0), ("df64_plain", g.DF64, 0), ("fp64_plain", g.FP64, 0)):
+        p = g.make_params(radius=RADIUS, g=GRAV, angvel=angvel, h=h, alpha=alpha, ecc=ECC, obliq=np.deg2rad(0.2),
+                          dt=P / n, potential=g.POT_FULL, precision=prec, sh_lmax=lmax,
+                          sh_factors=fac if lmax else None)
+        s = g.Solver(p, mesh)
+        s.run(50)
+        s.synchronize()
+        t = time.perf_counter()
+        pw = s.run(args.case_steps)
+        el = time.perf_counter() - t
+        _, v, eta, _, _ = s.get_state()
+        finals[name] = (v, eta, float(pw[-1]))
+        ms = s.profile_kernels(20)
+        sb = 4 if prec == g.FP32 else 8
+        fb, cb = E * (19 * sb + 48), N * (13 * sb + 24)
+        out["methods"][name] = {
+            "us_per_step": el / args.case_steps * 1e6, "cell_steps_per_s": N * args.case_steps / el,
+            "face_us": ms[0] * 1e3, "cell_us": ms[1] * 1e3, "sh_us": ms[2] * 1e3,
+            "face_hbm_frac": fb / (ms[0] * 1e-3) / 1e9 / peak, "cell_hbm_frac": cb / (ms[1] * 1e-3) / 1e9 / peak,
+            "sh_tiles": list(s.sh_tiles()) if lmax else None}
+        s.close()
+    for a, b in (("fp32_sh32", "fp64_sh32"), ("df64_sh32", "fp64_sh32"), ("fp32_plain", "fp64_plain")):
+        (va, ea, pa), (vb, eb_, pb) = finals[a], finals[b]
+        out[f"{a}_vs_{b}"] = {"v": _rel(va, vb), "eta": _rel(ea, eb_), "power": abs(pa - pb) / abs(pb),
+                              "steps": 50 + args.case_steps}
+    out["tensor_pipe"] = ("0: the Legendre contraction of one instance per step is two matrix-vector products, "
+                          "run on the FP32 (FP32, DF64) or FP64 pipes")
+    out["peak_gbs"] = peak
+    return out
 
 
 def profiled_traffic(kernel: str):
@@ -397,12 +450,30 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the batched 256-configuration sweep")
     ap.add_argument("--sweep-orbits", type=float, default=10.0)
+    ap.add_argument("--workload", choices=["level6", "level8", "surrogate"], default="level6",
+                    help="level8: the level-8 l_max=32 measurements; surrogate: the learned warm-start experiment")
     ap.add_argument("--profile-case", choices=["fp64", "df64", "fp32", "batch"], default=None,
                     help="run a short level-6 case for an ncu capture (no timing, no JSON)")
     ap.add_argument("--case-sh", type=int, default=0, help="self-gravity degree of --profile-case")
+    ap.add_argument("--sur-train", type=int, default=4096)
+    ap.add_argument("--sur-test", type=int, default=512)
+    ap.add_argument("--sur-level", type=int, default=5)
+    ap.add_argument("--sur-epochs", type=int, default=400)
     ap.add_argument("--case-steps", type=int, default=30)
     ap.add_argument("--case-graph", action="store_true", help="--profile-case: force the graph-replayed kernels")
     args = ap.parse_args()
+    if args.workload == "level8":
+        from geodesicodis_gb300 import build_ext
+        build_ext.build()
+        print(json.dumps(run_level8(args)))
+        return
+    if args.workload == "surrogate":
+        from geodesicodis_gb300 import build_ext, surrogate
+        build_ext.build()
+        res = surrogate.experiment(n_train=args.sur_train, n_test=args.sur_test, level=args.sur_level,
+                                   epochs=args.sur_epochs, log=lambda m: print(m, file=sys.stderr, flush=True))
+        print(json.dumps(res))
+        return
     if args.profile_case == "batch":
         # one cooperative launch of `case-steps` steps of the 256-member sweep
         from geodesicodis_gb300 import sweep as S

@@ -104,7 +104,7 @@ _SIGS = {
     "odis_batch_run": ([_V, C.c_double, C.c_int, _D, C.c_int, _D, C.c_int, C.c_int], C.c_int),
     "odis_batch_get_member": ([_V, C.c_int, _I, _D, _D], C.c_int),
     "odis_batch_set_member": ([_V, C.c_int, _D, _D], C.c_int),
-    "odis_batch_info": ([_V, _I, _I, _I, C.POINTER(C.c_longlong)], C.c_int),
+    "odis_batch_info": ([_V, _I, _I, _I, C.POINTER(C.c_longlong), _I], C.c_int),
     "odis_batch_get_mesh_members": ([_V, C.c_int, _D, _D], C.c_int),
     "odis_batch_set_mesh_members": ([_V, C.c_int, _D, _D], C.c_int),
     "odis_batch_project": ([_V, C.c_int, _V, C.c_int, _V, C.c_int, _D, C.c_int], C.c_int),
@@ -460,9 +460,11 @@ class Batch:
         return out[self.mesh_members(mesh)]
 
     def info(self) -> dict:
-        g, p, gr, n = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
-        _ck(lib().odis_batch_info(self._h, C.byref(g), C.byref(p), C.byref(gr), C.byref(n)), "odis_batch_info")
-        return {"groups": g.value, "padded_members": p.value, "grid": gr.value, "launches": n.value}
+        g, p, gr, n, r = C.c_int(), C.c_int(), C.c_int(), C.c_longlong(), C.c_int()
+        _ck(lib().odis_batch_info(self._h, C.byref(g), C.byref(p), C.byref(gr), C.byref(n), C.byref(r)),
+            "odis_batch_info")
+        return {"groups": g.value, "padded_members": p.value, "grid": gr.value, "launches": n.value,
+                "rows_per_thread": r.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value and _lib is not None:

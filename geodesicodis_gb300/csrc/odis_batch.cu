@@ -786,9 +786,10 @@ extern "C" void odis_batch_destroy(odis_batch* b)
 }
 
 extern "C" odis_status odis_batch_info(const odis_batch* b, int* n_groups, int* padded_members, int* grid,
-                                       long long* launches)
+                                       long long* launches, int* rows_per_thread)
 {
     if (!b) return ODIS_ERR_ARG;
+    if (rows_per_thread) *rows_per_thread = kRowChoices[b->variant];
     if (n_groups) *n_groups = (int)b->groups.size();
     if (padded_members) *padded_members = b->P;
     if (grid) *grid = b->grid;

@@ -263,7 +263,11 @@ odis_status odis_batch_get_member(odis_batch* b, int member, int* iter, double* 
  * restarts its step count at 0 (forcing phase 0, forward-Euler start): the
  * warm-start entry point. */
 odis_status odis_batch_set_member(odis_batch* b, int member, const double* v, const double* eta);
-odis_status odis_batch_info(const odis_batch* b, int* n_groups, int* padded_members, int* grid, long long* launches);
+/* Layout and launch facts: member groups, padded member slots, CTAs of the
+ * cooperative launch, launches so far, and the face/cell rows each thread
+ * handles per tile (1, 2 or 4: timed at creation, or ODIS_BATCH_ROWS). */
+odis_status odis_batch_info(const odis_batch* b, int* n_groups, int* padded_members, int* grid, long long* launches,
+                            int* rows_per_thread);
 /* Bulk state access for the members on mesh `mesh`, in increasing member index
  * (v [m][E], eta [m][N]).  set_mesh_members also clears their AB3 histories
  * and restarts their step counts at 0, as odis_batch_set_member. */
