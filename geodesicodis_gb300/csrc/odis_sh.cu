@@ -122,7 +122,29 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
     const T* cm = trig + (size_t)(2 * m) * Np;
     const T* sm = trig + (size_t)(2 * m + 1) * Np;
     const T* prow = P + (size_t)p_row(L, l0, m) * Np;
-    for (int i = i0 + threadIdx.x; i < i1; i += kShThreads) {
+    // two cells per iteration into separate accumulators: twice the loads in flight
+    T bc[kTileL], bs[kTileL];
+#pragma unroll
+    for (int j = 0; j < kTileL; j++) { bc[j] = A::zero(); bs[j] = A::zero(); }
+    int i = i0 + threadIdx.x;
+    for (; i + kShThreads < i1; i += 2 * kShThreads) {
+        const int i2 = i + kShThreads;
+        const T e = eta[i], e2 = eta[i2];
+        const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
+        const T ec2 = A::mul(cm[i2], e2), es2 = A::mul(sm[i2], e2);
+#pragma unroll
+        for (int j = 0; j < kTileL; j++) {
+            if (j < nl) {
+                const T p = prow[(size_t)j * Np + i];
+                const T p2 = prow[(size_t)j * Np + i2];
+                ac[j] = A::fma(p, ec, ac[j]);
+                as[j] = A::fma(p, es, as[j]);
+                bc[j] = A::fma(p2, ec2, bc[j]);
+                bs[j] = A::fma(p2, es2, bs[j]);
+            }
+        }
+    }
+    if (i < i1) {
         const T e = eta[i];
         const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
 #pragma unroll
@@ -134,6 +156,8 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
             }
         }
     }
+#pragma unroll
+    for (int j = 0; j < kTileL; j++) { ac[j] = A::add(ac[j], bc[j]); as[j] = A::add(as[j], bs[j]); }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j < kTileL; j++) {
