@@ -67,9 +67,29 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    _build_cli()
     if verbose:
         print(f"built {LIB}")
     return LIB
+
+
+CLI_SRC = PKG / "cli" / "odis_run.cpp"
+CLI = PKG / "bin" / "odis_run"
+
+
+def _build_cli() -> None:
+    """The run driver: host C++ over the C ABI, linked against the in-tree library."""
+    if not CLI_SRC.exists():
+        return
+    CLI.parent.mkdir(exist_ok=True)
+    if CLI.exists() and CLI.stat().st_mtime > max(CLI_SRC.stat().st_mtime, LIB.stat().st_mtime):
+        return
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(CLI_SRC), "-L", str(LIB.parent), "-lodis_gpu",
+           "-Wl,-rpath,$ORIGIN/../lib", "-o", str(CLI)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"building odis_run failed:\n{res.stdout}\n{res.stderr}")
 
 
 if __name__ == "__main__":
