@@ -218,37 +218,43 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
     T* c = reinterpret_cast<T*>(c_raw);
     for (int k = threadIdx.x; k < K; k += kSynthThreads) c[k] = coef[k];
     __syncthreads();
+    // each thread sums orders m = j, j + lanes, ... for the adjacent cells 2q and 2q+1
     const int gt = blockIdx.x * kSynthThreads + threadIdx.x;
-    const int i = gt / kSynthLanes, j = gt % kSynthLanes;
-    T u = A::zero();
+    const int q = gt / kSynthLanes, j = gt % kSynthLanes;
+    const int i = 2 * q, i2 = min(2 * q + 1, N - 1);
+    T u = A::zero(), u2 = A::zero();
     if (i < N) {
         for (int m = j; m <= L; m += kSynthLanes) {
             T a0 = A::zero(), b0 = A::zero(), a1 = A::zero(), b1 = A::zero();
             const int lstart = m < 2 ? 2 : m;
-            const T* prow = P + (size_t)p_row(L, lstart, m) * Np + i;
-            int l = lstart;
-            for (; l + 1 <= L; l += 2) {
-                const T p0 = prow[(size_t)(l - lstart) * Np];
-                const T p1 = prow[(size_t)(l + 1 - lstart) * Np];
-                a0 = A::fma(p0, c[sh_col(l, m, 0)], a0);
-                a1 = A::fma(p1, c[sh_col(l + 1, m, 0)], a1);
+            const T* prow = P + (size_t)p_row(L, lstart, m) * Np;
+            for (int l = lstart; l <= L; l++) {
+                const T* pr = prow + (size_t)(l - lstart) * Np;
+                const T p0 = pr[i], p1 = pr[i2];
+                const T cc = c[sh_col(l, m, 0)];
+                a0 = A::fma(p0, cc, a0);
+                a1 = A::fma(p1, cc, a1);
                 if (m > 0) {
-                    b0 = A::fma(p0, c[sh_col(l, m, 1)], b0);
-                    b1 = A::fma(p1, c[sh_col(l + 1, m, 1)], b1);
+                    const T cs = c[sh_col(l, m, 1)];
+                    b0 = A::fma(p0, cs, b0);
+                    b1 = A::fma(p1, cs, b1);
                 }
             }
-            if (l <= L) {
-                const T p0 = prow[(size_t)(l - lstart) * Np];
-                a0 = A::fma(p0, c[sh_col(l, m, 0)], a0);
-                if (m > 0) b0 = A::fma(p0, c[sh_col(l, m, 1)], b0);
-            }
-            const T cm = trig[(size_t)(2 * m) * Np + i], sm = trig[(size_t)(2 * m + 1) * Np + i];
-            u = A::fma(cm, A::add(a0, a1), A::fma(sm, A::add(b0, b1), u));
+            const T* cr = trig + (size_t)(2 * m) * Np;
+            const T* sr = trig + (size_t)(2 * m + 1) * Np;
+            u = A::fma(cr[i], a0, A::fma(sr[i], b0, u));
+            u2 = A::fma(cr[i2], a1, A::fma(sr[i2], b1, u2));
         }
     }
 #pragma unroll
-    for (int o = kSynthLanes / 2; o > 0; o >>= 1) u = A::add(u, A::shfl(u, o));
-    if (i < N && j == 0) usg[i] = u;
+    for (int o = kSynthLanes / 2; o > 0; o >>= 1) {
+        u = A::add(u, A::shfl(u, o));
+        u2 = A::add(u2, A::shfl(u2, o));
+    }
+    if (i < N && j == 0) {
+        usg[i] = u;
+        if (2 * q + 1 < N) usg[2 * q + 1] = u2;
+    }
 }
 
 // Gram matrix G = Y^T Y in FP64 (setup only): 32x32 output tiles, lower triangle
@@ -480,7 +486,7 @@ static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int nt
 template <class T>
 static void launch_synth(const ShLoading* s, int lanes, cudaStream_t st)
 {
-    const int sb = (s->N * lanes + kSynthThreads - 1) / kSynthThreads;
+    const int sb = ((s->N + 1) / 2 * lanes + kSynthThreads - 1) / kSynthThreads;
     const size_t sm = sizeof(T) * s->K;
     const T* P = (const T*)s->P;
     const T* trig = (const T*)s->trig;
