@@ -174,14 +174,56 @@ def _rel(a, b) -> float:
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
+def _max_over_ranks(D, x: float) -> float:
+    """The max of a host scalar over the replicas (gloo, CPU tensor); x itself with one process."""
+    if not D:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    D.all_reduce(t, op=D.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _replica_setup(cuda: bool = True):
+    """(rank, world, torch.distributed or None).  Under torchrun every rank is an independent replica of the
+    workload on its own GPU (the path does not shard): each process sees only its GPU, so the library's own
+    CUDA runtime and torch agree on device 0."""
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return 0, 1, None
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    vis = [x for x in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if x.strip()]
+    os.environ["CUDA_VISIBLE_DEVICES"] = vis[local % len(vis)] if vis else str(local)
+    import torch
+    import torch.distributed as D
+    if cuda:
+        torch.cuda.set_device(0)
+    # host-side barriers and one scalar max per measurement: gloo over CPU tensors, no GPU collective
+    D.init_process_group("gloo")
+    return rank, world, D
+
+
 def run_ours(args) -> dict:
+    rank, world, D = _replica_setup()
     import torch
     import geodesicodis_gb300 as g
     from geodesicodis_gb300 import build_ext
 
-    build_ext.build()
+    if rank == 0:
+        build_ext.build()
+    if D:
+        D.barrier()
     dev = torch.device("cuda:0")
     torch.cuda.set_device(dev)
+
+    def max_over_ranks(x: float) -> float:
+        return _max_over_ranks(D, x)
+
+    def barrier(collective: bool = True):
+        torch.cuda.synchronize()
+        if D and collective:
+            D.barrier()
+            torch.cuda.synchronize()
     angvel, P, dt, n = g.derive_time(ANGVEL_IN, DT_TARGET)
     mesh = g.Mesh.generate(LEVEL, RADIUS)
     N, E = mesh.n_cells, mesh.n_edges
@@ -195,14 +237,14 @@ def run_ours(args) -> dict:
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
 
-    def timed_orbits(sol, k, w):
+    def timed_orbits(sol, k, w, collective=True):
         """w untimed then k timed orbits from rest; device time of each orbit (CUDA events on the context stream)."""
         sol.set_stream(stream.cuda_stream)
         sol.set_state(0, np.zeros(E), np.zeros(N), np.zeros((E, 3)), np.zeros((N, 3)))
         with torch.cuda.stream(stream):
             for _ in range(w):
                 sol.run_device(n, None)
-            torch.cuda.synchronize()
+            barrier(collective)
             l0 = sol.launch_count()
             total = 0.0
             for _ in range(k):
@@ -215,6 +257,7 @@ def run_ours(args) -> dict:
                 b.synchronize()
                 total += a.elapsed_time(b) / 1e3
             launches = sol.launch_count() - l0
+            barrier(collective)
         return total, launches
 
     # headline: the FP64-parity double-float method (ODIS_DF64) on the level-6 + l_max=16 workload
@@ -225,7 +268,12 @@ def run_ours(args) -> dict:
     t_main, launches = timed_orbits(main_sol, args.steps, args.warmup)
     clk = clocks.stop()
     main_sol.close()
-    value = N * n * args.steps / t_main
+    t_main = max_over_ranks(t_main)
+    value = world * N * n * args.steps / t_main      # whole job: every replica ran the same orbits
+    e2e_value = run_e2e(g, solver, stream, flush, args, n, N, E, barrier, max_over_ranks, world)
+    if rank != 0:
+        barrier()
+        return {}
 
     # the other methods, 1 untimed + kv timed orbits each from rest; final states kept for the error report
     kv = max(1, args.steps // 4)
@@ -233,7 +281,7 @@ def run_ours(args) -> dict:
     for key, prec, lmax in (("df64_sh16", g.DF64, LMAX), ("fp64_sh16", g.FP64, LMAX), ("fp32_sh16", g.FP32, LMAX),
                             ("df64_plain", g.DF64, 0), ("fp64_plain", g.FP64, 0), ("fp32_plain", g.FP32, 0)):
         s = solver(prec, lmax)
-        t, _ = timed_orbits(s, kv, 1)
+        t, _ = timed_orbits(s, kv, 1, collective=False)     # rank 0 only
         if key != "df64_sh16":
             results[key] = N * n * kv / t
         _, v, eta, _, _ = s.get_state()
@@ -248,31 +296,6 @@ def run_ours(args) -> dict:
         errors[f"{key}_vs_{ref}"] = {"eta": _rel(ea, eb_), "velocity": _rel(va, vb), "power": abs(pa - pb) / abs(pb),
                                      "orbits": 1 + kv}
 
-    # end-to-end through the C ABI with host buffers (pinned), copies inside the timed region
-    hv = torch.zeros(E, dtype=torch.float64).pin_memory()
-    he = torch.zeros(N, dtype=torch.float64).pin_memory()
-    hdv = torch.zeros(E * 3, dtype=torch.float64).pin_memory()
-    hde = torch.zeros(N * 3, dtype=torch.float64).pin_memory()
-    hp = torch.zeros(n, dtype=torch.float64).pin_memory()
-    e2e_sol = solver(g.DF64, LMAX)
-    e2e_sol.set_stream(stream.cuda_stream)
-    it = 0
-    for _ in range(args.warmup):
-        e2e_sol.set_state_ptrs(it, hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
-        e2e_sol.run_host_ptr(n, hp.data_ptr())
-        it = e2e_sol.get_state_ptrs(hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
-    torch.cuda.synchronize()
-    e2e_time = 0.0
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        ta = time.perf_counter()
-        # each call below returns only after its copies and kernels are complete
-        e2e_sol.set_state_ptrs(it, hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
-        e2e_sol.run_host_ptr(n, hp.data_ptr())
-        it = e2e_sol.get_state_ptrs(hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
-        e2e_time += time.perf_counter() - ta
-    e2e_sol.close()
     h2d = (E + N + 3 * E + 3 * N) * 8
     d2h = (E + N + 3 * E + 3 * N) * 8 + n * 8
 
@@ -299,10 +322,11 @@ def run_ours(args) -> dict:
         gbs = b * results[key] / N / 1e9
         plain[key] = {"achieved_gbs": gbs, "frac": gbs / peak, "bytes_per_step": b}
 
-    out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+    out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_main / args.steps * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "df64", "data": "synthetic",
-           "config": workload_config(n, N, E) | {"parallelism": "single-gpu", "global_batch": 1,
+           "config": workload_config(n, N, E) | {"parallelism": "single-gpu" if world == 1 else f"{world} replicas",
+                                                 "global_batch": world,
                                                  "method": "ODIS_DF64: FP64-parity (1e-10) double-float arithmetic",
                                                  "sh_tiles_autotuned": tiles},
            "variants_cell_steps_per_s": results,
@@ -316,8 +340,8 @@ def run_ours(args) -> dict:
                                 "they stay L2-resident at level 6, and the kernel is FP32-pipe bound"
                                 if dominant == "sh_self_gravity" else ""},
            "plain_step_roofline": plain,
-           "clocks": clk, "gpu_launches": launches,
-           "e2e": {"value": N * n * args.steps / e2e_time, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+           "clocks": clk, "gpu_launches": launches * world,
+           "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": d2h,
                    "how": f"per orbit: odis_set_state from pinned host buffers, odis_run_steps({n}) with the "
                           "power series copied to host, odis_get_state back to host; wall clock"}}
@@ -328,7 +352,42 @@ def run_ours(args) -> dict:
         out["cpu_baseline"] = {"value": v, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
                                "sample": f"{args.cpu_sample_steps} LTE steps of the same level-6 FP64 + l_max=16 "
                                          f"workload, oracle C restatement with OpenMP over rows/cells"}
+    if D:
+        barrier()              # the other replicas wait here while rank 0 measures the extras
     return out
+
+
+def run_e2e(g, solver, stream, flush, args, n, N, E, barrier, max_over_ranks, world) -> float:
+    """The headline orbits end to end through the C ABI with pinned host buffers: per orbit
+    odis_set_state from host, odis_run_steps with the power series copied to host, odis_get_state back;
+    host wall clock; whole-job cell-steps/s (max over replicas)."""
+    import torch
+    hv = torch.zeros(E, dtype=torch.float64).pin_memory()
+    he = torch.zeros(N, dtype=torch.float64).pin_memory()
+    hdv = torch.zeros(E * 3, dtype=torch.float64).pin_memory()
+    hde = torch.zeros(N * 3, dtype=torch.float64).pin_memory()
+    hp = torch.zeros(n, dtype=torch.float64).pin_memory()
+    sol = solver(g.DF64, LMAX)
+    sol.set_stream(stream.cuda_stream)
+    it = 0
+    for _ in range(args.warmup):
+        sol.set_state_ptrs(it, hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
+        sol.run_host_ptr(n, hp.data_ptr())
+        it = sol.get_state_ptrs(hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
+    barrier()
+    total = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        # each call below returns only after its copies and kernels are complete
+        sol.set_state_ptrs(it, hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
+        sol.run_host_ptr(n, hp.data_ptr())
+        it = sol.get_state_ptrs(hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
+        total += time.perf_counter() - ta
+    sol.close()
+    barrier()
+    return world * N * n * args.steps / max_over_ranks(total)
 
 
 def run_sweep(args, fp64_plain: float, peak: float) -> dict:
@@ -505,7 +564,8 @@ def main():
             print(json.dumps(out))
         return
     out = run_ours(args)
-    print(json.dumps(out))
+    if out:
+        print(json.dumps(out))
 
 
 if __name__ == "__main__":
