@@ -91,6 +91,7 @@ _SIGS = {
     "odis_forcing": ([_V, _V, C.c_int, C.c_double, C.c_int], C.c_int),
     "odis_ab3": ([_V, _V, _V, C.c_int, C.c_int, C.c_int], C.c_int),
     "odis_interpolate_velocity": ([_V, _V, _V, C.c_int], C.c_int),
+    "odis_interpolate_cartesian": ([_V, _V, _V, C.c_int], C.c_int),
     "odis_update_energy": ([_V, _V, _V, _V, C.c_int], C.c_int),
     "odis_run_steps": ([_V, C.c_int, _V, C.c_int], C.c_int),
     "odis_get_state": ([_V, _I, _D, _D, _D, _D], C.c_int),
@@ -292,6 +293,13 @@ class Solver:
         out = np.zeros((self.E, 2))
         v = np.ascontiguousarray(v, np.float64)
         _ck(lib().odis_interpolate_velocity(self._h, _vp(out), _vp(v), MEM_HOST), "odis_interpolate_velocity")
+        return out
+
+    def interpolateVelocityCart(self, v: np.ndarray) -> np.ndarray:
+        """Cartesian velocity [N, 3] at the nodes (the reference's RBF reconstruction)."""
+        out = np.zeros((self.N, 3))
+        v = np.ascontiguousarray(v, np.float64)
+        _ck(lib().odis_interpolate_cartesian(self._h, _vp(out), _vp(v), MEM_HOST), "odis_interpolate_cartesian")
         return out
 
     def updateEnergy(self, uv: np.ndarray):

@@ -8,7 +8,9 @@
 // DISS: ... GW" line at every output interval (src/timeIntegrator.cpp:190-193)
 // to stdout and OUTPUT.txt, and writes the final state back in the
 // InitialConditions format.  DATA/power.txt gets one "orbit  W/m^2  GW" line
-// per output interval; the HDF5 field dumps (src/outFiles.cpp) are not written.
+// per output interval, DATA/final_nodes.txt the final displacement and Cartesian
+// velocity (RBF reconstruction) per node; the HDF5 field dumps (src/outFiles.cpp)
+// are not written.
 //
 //   odis_run [--dir D] [--grid FILE | --level N] [--precision fp64|df64|fp32] [--orbits X]
 //
@@ -149,6 +151,17 @@ int main(int argc, char** argv)
         mkdir((dir + "/InitialConditions").c_str(), 0755);
         write_state(dir + "/InitialConditions/vel_init.txt", E, v, dv);
         write_state(dir + "/InitialConditions/pres_init.txt", N, eta, de);
+        // final displacement and Cartesian velocity at the nodes (the "displacement" and
+        // "x/y/z velocity" fields of the reference's output)
+        std::vector<double> uxyz((size_t)3 * N);
+        if (odis_interpolate_cartesian(ctx, uxyz.data(), v.data(), ODIS_MEM_HOST) == ODIS_OK) {
+            FILE* f = std::fopen((dir + "/DATA/final_nodes.txt").c_str(), "w");
+            if (f) {
+                for (int i = 0; i < N; i++)
+                    std::fprintf(f, "%1.9E %1.9E %1.9E %1.9E\n", eta[i], uxyz[3 * i], uxyz[3 * i + 1], uxyz[3 * i + 2]);
+                std::fclose(f);
+            }
+        }
     }
     odis_destroy(ctx);
     odis_mesh_destroy(mesh);

@@ -86,6 +86,7 @@ struct odis_ctx {
     double* nrm = nullptr;       // [2][Ep]
     double* area = nullptr;      // [Ep]
     double* trig = nullptr;      // [10][Np]
+    double* rbf = nullptr;       // [3][6][Np] Cartesian reconstruction blocks
     State<double> s64{};
     State<float> s32{};
     State<float2> sdf{};
@@ -557,7 +558,14 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     c->nrm = A.upload(nrm);
     c->area = A.upload(area);
     c->trig = A.upload(trig);
-    if (!c->nrm || !c->area || !c->trig) return ODIS_ERR_NOMEM;
+    {
+        std::vector<double> blk, soa((size_t)18 * c->Np, 0.0);
+        build_rbf(m, blk);
+        for (int i = 0; i < m.N; i++)
+            for (int q = 0; q < 18; q++) soa[(size_t)q * c->Np + i] = blk[(size_t)i * 18 + q];
+        c->rbf = A.upload(soa);
+    }
+    if (!c->nrm || !c->area || !c->trig || !c->rbf) return ODIS_ERR_NOMEM;
 
     st = alloc_state<double>(c.get(), c->s64, false);
     if (st != ODIS_OK) return st;
@@ -694,6 +702,18 @@ extern "C" odis_status odis_update_momentum(odis_ctx* c, double* dvdt, const dou
     if (!dv || !de) return ODIS_ERR_CUDA;
     launch_momentum(c->op64.fc, c->E, c->Ep, dout, dv, de, c->stream);
     int st = io.back(dvdt, dout, c->E);
+    return st != ODIS_OK ? st : io.done();
+}
+
+extern "C" odis_status odis_interpolate_cartesian(odis_ctx* c, double* uxyz, const double* v, int mem)
+{
+    if (!c || !uxyz || !v || !mem_ok(mem)) return ODIS_ERR_ARG;
+    Io io{c, mem};
+    const double* dv = io.in(v, c->E);
+    double* dout = io.out(uxyz);
+    if (!dv) return ODIS_ERR_CUDA;
+    launch_rbf(c->rbf, c->op64.cc.edge, c->N, c->Np, dv, dout, c->stream);
+    int st = io.back(uxyz, dout, (size_t)3 * c->N);
     return st != ODIS_OK ? st : io.done();
 }
 

@@ -40,6 +40,7 @@ struct Mesh {
     std::vector<double> face_m;        // [E][2]
     std::vector<double> face_normal;   // [E][2]
     std::vector<double> face_int;      // [E][2]
+    std::vector<double> face_nxyz;     // [E][3] unit normal of the great circle through the face's vertices
     std::vector<int> interp_friends;   // [E][10]
     std::vector<double> interp_w;      // [E][10]
     std::vector<int> interp_n;         // [E]
@@ -52,6 +53,10 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
 // Forcing as a single-frequency pair: U_i(t) = cos(M) Ua_i + sin(M) Ub_i with
 // M = angvel * t, for the ECC / OBLIQ / OBLIQ_WEST / FULL potentials.
 int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, std::vector<double>& Ub);
+
+// RBF reconstruction of Cartesian velocity at the nodes from the face-normal
+// velocities: rbf[(i * 3 + c) * 6 + j] multiplies v at faces(i, j).
+void build_rbf(const Mesh& m, std::vector<double>& rbf);
 
 // sqrt(largest eigenvalue of -g h D G), power iteration
 double gravity_wave_omega(const Mesh& m, double g, double h, int iters);

@@ -459,6 +459,30 @@ __global__ void __launch_bounds__(kStepThreads) k_energy_partial(const double* a
     if (threadIdx.x == 0) partial[blockIdx.x] = bs;
 }
 
+// Cartesian velocity at the nodes from the face-normal velocities (RBF operator,
+// per node a 3 x 6 block over its faces; missing pentagon entries are zero).
+__global__ void k_rbf(const double* __restrict__ rbf, const int* __restrict__ edge, int N, int Np,
+                      const double* __restrict__ v, double* __restrict__ uxyz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double vf[kCellFaces];
+#pragma unroll
+    for (int j = 0; j < kCellFaces; j++) vf[j] = v[__ldg(&edge[j * Np + i])];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        double u = 0.0;
+#pragma unroll
+        for (int j = 0; j < kCellFaces; j++) u = fma(__ldg(&rbf[(c * kCellFaces + j) * Np + i]), vf[j], u);
+        uxyz[3 * i + c] = u;
+    }
+}
+
+void launch_rbf(const double* rbf, const int* edge, int N, int Np, const double* v, double* uxyz, cudaStream_t s)
+{
+    k_rbf<<<(N + 255) / 256, 256, 0, s>>>(rbf, edge, N, Np, v, uxyz);
+}
+
 __global__ void k_fold(const double* partial, int n, double divisor, double* out)
 {
     const double s = fold_partials(partial, n);

@@ -18,6 +18,8 @@ template <class T>
 void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int n, cudaStream_t s);
 // power[k] = sum of row k+1 of a run's partial table [n+1][nb] (no-op without power)
 void launch_power_fold(const double* part, int nb, int n, double* power, cudaStream_t s);
+// uxyz[i][c] = sum_j rbf[(c*6+j)*Np + i] * v[edge[j*Np + i]]
+void launch_rbf(const double* rbf, const int* edge, int N, int Np, const double* v, double* uxyz, cudaStream_t s);
 // CTAs of the face step kernel: one face per thread, or a face pair per thread (FP32 variant)
 int face_blocks(const StepConst& sc, bool pairs);
 void launch_bump(long long* iter, int n, cudaStream_t s);

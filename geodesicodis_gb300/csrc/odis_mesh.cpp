@@ -260,6 +260,7 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
     m.face_m.assign((size_t)E * 2, 0.0);
     m.face_normal.assign((size_t)E * 2, 0.0);
     m.face_int.assign((size_t)E * 2, 0.0);
+    m.face_nxyz.assign((size_t)E * 3, 0.0);
 #pragma omp parallel for schedule(static)
     for (int e = 0; e < E; e++) {
         int i = m.face_nodes[e * 2], f = m.face_nodes[e * 2 + 1], j = face_slot[e];
@@ -280,6 +281,19 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
         map_normal(v1, v2, n);
         m.face_normal[e * 2] = n[0];
         m.face_normal[e * 2 + 1] = n[1];
+        {
+            // Cartesian normal: the unit cross product of the vertex positions (include/mathRoutines.h:246-267)
+            double p1[3], p2[3];
+            to_xyz(v1, p1);
+            to_xyz(v2, p2);
+            double c0 = p1[1] * p2[2] - p1[2] * p2[1];
+            double c1 = -(p1[0] * p2[2] - p1[2] * p2[0]);
+            double c2 = p1[0] * p2[1] - p1[1] * p2[0];
+            const double mag = std::sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+            m.face_nxyz[e * 3] = c0 / mag;
+            m.face_nxyz[e * 3 + 1] = c1 / mag;
+            m.face_nxyz[e * 3 + 2] = c2 / mag;
+        }
         LL ip = intersect(v1, v2, node(i), node(f));
         m.face_int[e * 2] = ip.lat;
         m.face_int[e * 2 + 1] = ip.lon;
@@ -387,6 +401,71 @@ double gravity_wave_omega(const Mesh& m, double g, double h, int iters)
 // U(t) = cos(M) Ua + sin(M) Ub for the single-frequency potentials of
 // src/tidalPotentials.cpp:82-174 (ECC, OBLIQ, OBLIQ_WEST, FULL), using the
 // node trig tables of src/mesh.cpp:2122-2152.
+// Gaussian radial basis function of an arc on the unit sphere, shape parameter 1
+// (include/mathRoutines.h:431-439)
+static double rbf_phi(double d)
+{
+    return d < 1e-8 ? 1.0 : std::exp(-std::pow(d, 2.0));
+}
+
+// Inverse of a k x k matrix (k <= 6) by Gauss-Jordan elimination with partial pivoting.
+static bool invert_small(int k, double a[6][6], double inv[6][6])
+{
+    for (int r = 0; r < k; r++)
+        for (int c = 0; c < k; c++) inv[r][c] = r == c ? 1.0 : 0.0;
+    for (int c = 0; c < k; c++) {
+        int piv = c;
+        for (int r = c + 1; r < k; r++) if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (a[piv][c] == 0.0) return false;
+        if (piv != c)
+            for (int q = 0; q < k; q++) { std::swap(a[c][q], a[piv][q]); std::swap(inv[c][q], inv[piv][q]); }
+        const double d = a[c][c];
+        for (int q = 0; q < k; q++) { a[c][q] /= d; inv[c][q] /= d; }
+        for (int r = 0; r < k; r++) {
+            if (r == c) continue;
+            const double f = a[r][c];
+            if (f == 0.0) continue;
+            for (int q = 0; q < k; q++) { a[r][q] -= f * a[c][q]; inv[r][q] -= f * inv[c][q]; }
+        }
+    }
+    return true;
+}
+
+// RBF reconstruction (src/mesh.cpp:355-430 and :2263-2362, used by
+// interpolateVelocityCartRBF, src/interpolation.cpp:64-174): about node i with
+// faces j = 0..k-1, A[j1][j2] = phi(arc(f_j1, f_j2)) n_j1 . n_j2 and
+// w[j] = phi(arc(node i, f_j)); the Cartesian velocity is
+// u_c = sum_j1 w[j1] n_j1,c sum_j2 (A^-1)[j1][j2] v(f_j2).
+void build_rbf(const Mesh& m, std::vector<double>& rbf)
+{
+    const int N = m.N;
+    rbf.assign((size_t)N * 18, 0.0);
+    auto node = [&](int i) { return LL{m.node_sph[i * 2], m.node_sph[i * 2 + 1]}; };
+    auto fc = [&](int e) { return LL{m.face_centre[e * 2], m.face_centre[e * 2 + 1]}; };
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; i++) {
+        const int k = m.nfriends(i);
+        double A[6][6] = {}, Ai[6][6] = {}, w[6] = {};
+        for (int j1 = 0; j1 < k; j1++) {
+            const int f1 = m.faces[i * 6 + j1];
+            for (int j2 = 0; j2 < k; j2++) {
+                const int f2 = m.faces[i * 6 + j2];
+                const double dot = m.face_nxyz[f1 * 3] * m.face_nxyz[f2 * 3] + m.face_nxyz[f1 * 3 + 1] * m.face_nxyz[f2 * 3 + 1] +
+                                   m.face_nxyz[f1 * 3 + 2] * m.face_nxyz[f2 * 3 + 2];
+                A[j1][j2] = rbf_phi(arc_atan2(fc(f1), fc(f2))) * dot;
+            }
+            w[j1] = rbf_phi(arc_atan2(node(i), fc(f1)));
+        }
+        if (!invert_small(k, A, Ai)) continue;
+        for (int c = 0; c < 3; c++)
+            for (int j2 = 0; j2 < k; j2++) {
+                double s = 0.0;
+                for (int j1 = 0; j1 < k; j1++) s += w[j1] * m.face_nxyz[m.faces[i * 6 + j1] * 3 + c] * Ai[j1][j2];
+                rbf[((size_t)i * 3 + c) * 6 + j2] = s;
+            }
+    }
+}
+
 int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, std::vector<double>& Ub)
 {
     Ua.assign(m.N, 0.0);

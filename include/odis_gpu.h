@@ -12,6 +12,7 @@
  *   odis_forcing           <- forcing             include/tidalPotentials.h:16, src/tidalPotentials.cpp:29-334
  *   odis_ab3               <- integrateAB3scalar  include/temporalOperators.h:14, src/temporalOperators.cpp:17-68
  *   odis_interpolate_velocity <- interpolateVelocity include/interpolation.h:12, src/interpolation.cpp:26-62
+ *   odis_interpolate_cartesian <- interpolateVelocityCartRBF include/interpolation.h:16, src/interpolation.cpp:64-174
  *   odis_update_energy     <- updateEnergy        include/energy.h:10,          src/energy.cpp:13-61
  *   odis_run_steps         <- the body of ab3Explicit's time loop, src/timeIntegrator.cpp:205-313
  *   odis_get_state / odis_set_state <- writeInitialConditions / loadInitialConditions,
@@ -166,6 +167,12 @@ odis_status odis_forcing(odis_ctx* c, double* U, int type, double t, int mem);
 odis_status odis_ab3(odis_ctx* c, double* s, double* hist, int iter, int num, int mem);
 /* uv[E][2] = (east, north) velocity at faces from normal velocity v[E] */
 odis_status odis_interpolate_velocity(odis_ctx* c, double* uv, const double* v, int mem);
+/* interpolateVelocityCartRBF (src/interpolation.cpp:64-174; operatorRBFinterp,
+ * src/mesh.cpp:355-430 and :2263-2362): Cartesian velocity uxyz [N][3] at the
+ * nodes from the face-normal velocities v [E], by the reference's Gaussian
+ * radial-basis reconstruction over each node's faces (the "x/y/z velocity"
+ * output fields). */
+odis_status odis_interpolate_cartesian(odis_ctx* c, double* uxyz, const double* v, int mem);
 /* e[E] (nullable) per-face dissipation and *avg area-mean (W m^-2) from uv[E][2] */
 odis_status odis_update_energy(odis_ctx* c, double* avg, double* e, const double* uv, int mem);
 

@@ -255,6 +255,7 @@ typedef struct {
     double *face_m;       /* [E][2] */
     double *face_normal;  /* [E][2] */
     double *face_int;     /* [E][2] */
+    double *face_nxyz;    /* [E][3] Cartesian face normal */
     int *interp_friends;  /* [E][10] */
     double *interp_w;     /* [E][10] */
     int *interp_n;        /* [E] number of valid entries (10, 9 or 8) */
@@ -270,7 +271,7 @@ void orc_mesh_free(orc_mesh *M)
     free(M->node_sph); free(M->friends); free(M->cent_sph); free(M->cent_map); free(M->cv_area);
     free(M->vertexes); free(M->vert_sph); free(M->vert_nodes); free(M->faces); free(M->node_face_dir);
     free(M->face_nodes); free(M->face_len); free(M->face_dist); free(M->face_area); free(M->face_centre);
-    free(M->face_m); free(M->face_normal); free(M->face_int); free(M->interp_friends); free(M->interp_w);
+    free(M->face_m); free(M->face_normal); free(M->face_int); free(M->face_nxyz); free(M->interp_friends); free(M->interp_w);
     free(M->interp_n); free(M->trig);
     csr_free(&M->G); csr_free(&M->D); csr_free(&M->C0);
     free(M);
@@ -335,6 +336,7 @@ static int assign_faces(orc_mesh *M)
     M->face_centre = (double *)calloc((size_t)E * 2, sizeof(double));
     M->face_m = (double *)calloc((size_t)E * 2, sizeof(double));
     M->face_normal = (double *)calloc((size_t)E * 2, sizeof(double));
+    M->face_nxyz = (double *)calloc((size_t)E * 3, sizeof(double));
     M->face_int = (double *)calloc((size_t)E * 2, sizeof(double));
     M->interp_friends = (int *)calloc((size_t)E * 10, sizeof(int));
     M->interp_w = (double *)calloc((size_t)E * 10, sizeof(double));
@@ -371,6 +373,14 @@ static int assign_faces(orc_mesh *M)
             double nv[2];
             normal_map(nv, s1, s2);                                                /* :632-637 */
             M->face_normal[fc * 2] = nv[0]; M->face_normal[fc * 2 + 1] = nv[1];
+            {   /* normalVectorBetweenXYZ, include/mathRoutines.h:246-267; src/mesh.cpp:640-644 */
+                double a[3], b[3];
+                sph2cart(&a[0], &a[1], &a[2], 1.0, ORC_PI * 0.5 - s1[0], s1[1]);
+                sph2cart(&b[0], &b[1], &b[2], 1.0, ORC_PI * 0.5 - s2[0], s2[1]);
+                double nx = a[1] * b[2] - a[2] * b[1], ny = -(a[0] * b[2] - a[2] * b[0]), nz = a[0] * b[1] - a[1] * b[0];
+                double mag = sqrt(nx * nx + ny * ny + nz * nz);
+                M->face_nxyz[fc * 3] = nx / mag; M->face_nxyz[fc * 3 + 1] = ny / mag; M->face_nxyz[fc * 3 + 2] = nz / mag;
+            }
             for (int k = 0; k < 2; k++) { s3[k] = M->node_sph[i * 2 + k]; s4[k] = M->node_sph[f * 2 + k]; }
             intersect_sph(s1, s2, s3, s4, sc);                                     /* :660-670 */
             M->face_int[fc * 2] = sc[0]; M->face_int[fc * 2 + 1] = sc[1];
@@ -834,6 +844,58 @@ void orc_interpolate_velocity(const orc_mesh *M, double *uv, const double *vn)
         double ty = -nx, tx = ny;
         uv[i * 2] = nx * vn[i] + tx * vt;
         uv[i * 2 + 1] = ny * vn[i] + ty * vt;
+    }
+}
+
+/* interpolateVelocityCartRBF, src/interpolation.cpp:64-174, with the operator
+ * of src/mesh.cpp:355-430 and :2263-2362: per node i with faces j,
+ * A[j1][j2] = phi(arc(f_j1, f_j2)) n_j1 . n_j2, w[j] = phi(arc(i, f_j)),
+ * phi(d) = exp(-d^2) (1 below 1e-8, include/mathRoutines.h:431-439),
+ * u_c(i) = sum_j1 w[j1] n_j1,c (A^-1 v_faces)[j1].  The k x k systems are solved
+ * by Gaussian elimination with partial pivoting. */
+static double orc_rbf(double d) { return d < 1e-8 ? 1.0 : exp(-pow(d, 2.0)); }
+
+void orc_interpolate_cartesian(const orc_mesh *M, double *uxyz, const double *vn)
+{
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < M->N; i++) {
+        int k = nfriends(M, i);
+        double a[6][7], x[6];
+        double sn[2] = {M->node_sph[i * 2], M->node_sph[i * 2 + 1]};
+        double w[6];
+        for (int j1 = 0; j1 < k; j1++) {
+            int f1 = M->faces[i * 6 + j1];
+            double s1[2] = {M->face_centre[f1 * 2], M->face_centre[f1 * 2 + 1]};
+            for (int j2 = 0; j2 < k; j2++) {
+                int f2 = M->faces[i * 6 + j2];
+                double s2[2] = {M->face_centre[f2 * 2], M->face_centre[f2 * 2 + 1]};
+                double dot = M->face_nxyz[f1 * 3] * M->face_nxyz[f2 * 3] + M->face_nxyz[f1 * 3 + 1] * M->face_nxyz[f2 * 3 + 1] +
+                             M->face_nxyz[f1 * 3 + 2] * M->face_nxyz[f2 * 3 + 2];
+                a[j1][j2] = orc_rbf(dist_sph2(s1, s2)) * dot;
+            }
+            a[j1][k] = vn[f1];
+            w[j1] = orc_rbf(dist_sph2(sn, s1));
+        }
+        /* solve A x = v_faces */
+        for (int c = 0; c < k; c++) {
+            int piv = c;
+            for (int r = c + 1; r < k; r++) if (fabs(a[r][c]) > fabs(a[piv][c])) piv = r;
+            if (piv != c) for (int q = 0; q <= k; q++) { double t = a[c][q]; a[c][q] = a[piv][q]; a[piv][q] = t; }
+            for (int r = c + 1; r < k; r++) {
+                double f = a[r][c] / a[c][c];
+                for (int q = c; q <= k; q++) a[r][q] -= f * a[c][q];
+            }
+        }
+        for (int r = k - 1; r >= 0; r--) {
+            double t = a[r][k];
+            for (int q = r + 1; q < k; q++) t -= a[r][q] * x[q];
+            x[r] = t / a[r][r];
+        }
+        for (int c = 0; c < 3; c++) {
+            double u = 0.0;
+            for (int j = 0; j < k; j++) u += w[j] * M->face_nxyz[M->faces[i * 6 + j] * 3 + c] * x[j];
+            uxyz[i * 3 + c] = u;
+        }
     }
 }
 

@@ -59,6 +59,7 @@ def lib() -> C.CDLL:
             "orc_forcing": ([_V, _D, C.c_int, C.c_double], None),
             "orc_ab3": ([C.c_double, _D, _D, C.c_int, C.c_int, C.c_int], None),
             "orc_interpolate_velocity": ([_V, _D, _D], None),
+            "orc_interpolate_cartesian": ([_V, _D, _D], None),
             "orc_update_energy": ([_V, C.c_double, C.c_double, _D, _D], C.c_double),
             "orc_plmbar": ([C.c_int, C.c_double, _D], None),
             "orc_sh_basis": ([_V, C.c_int, _D], None),
@@ -173,6 +174,11 @@ class OracleSolver:
     def interpolateVelocity(self, v):
         out = np.zeros((self.E, 2))
         lib().orc_interpolate_velocity(self.mesh._h, _dp(out), _dp(np.ascontiguousarray(v, np.float64)))
+        return out
+
+    def interpolateVelocityCart(self, v):
+        out = np.zeros((self.N, 3))
+        lib().orc_interpolate_cartesian(self.mesh._h, _dp(out), _dp(np.ascontiguousarray(v, np.float64)))
         return out
 
     def updateEnergy(self, uv):

@@ -51,6 +51,9 @@ def test_cli_run_and_restart_match_the_library(built, tmp_path):
     assert np.max(np.abs(ef - eta)) <= 1e-6 * np.max(np.abs(eta))
     data = np.loadtxt(d / "DATA" / "power.txt", ndmin=2)
     assert abs(data[-1, 1] / pw.mean() - 1) < 1e-12
+    nodes = np.loadtxt(d / "DATA" / "final_nodes.txt")
+    ux = sol.interpolateVelocityCart(v)
+    assert np.max(np.abs(nodes[:, 1:] - ux)) <= 1e-8 * np.max(np.abs(ux))
     # restart from the written state (initial conditions LOAD) against the library run from the same numbers
     d2 = _rundir(tmp_path, "LOAD")
     r = subprocess.run([str(CLI), "--dir", str(d2), "--orbits", "0.1"], capture_output=True, text=True)

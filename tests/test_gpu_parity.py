@@ -61,6 +61,14 @@ def test_ab3(level3, it):
     assert rel_err(s2, s) < 1e-14 and rel_err(h2, h) == 0.0
 
 
+@pytest.mark.parametrize("level", [3, 4])
+def test_interpolate_cartesian(grid_dir, level):
+    """interpolateVelocityCartRBF: the GPU's explicit-inverse blocks against the oracle's per-node solves."""
+    orc, gpu = _pair(grid_dir / f"grid_{level}.txt")
+    v = np.random.default_rng(level).standard_normal(orc.E)
+    assert rel_err(gpu.interpolateVelocityCart(v), orc.interpolateVelocityCart(v)) < 1e-9
+
+
 def test_interpolate_and_energy(level3):
     orc, gpu = level3
     v = np.random.default_rng(4).standard_normal(orc.E)

@@ -150,3 +150,29 @@ def test_oracle_rest_state_and_linearity(grid_dir):
     _, vb, eb, _, _ = b.get_state()
     np.testing.assert_allclose(vb, 2 * va, rtol=1e-12, atol=1e-14 * np.abs(va).max())
     np.testing.assert_allclose(eb, 2 * ea, rtol=1e-12, atol=1e-14 * np.abs(ea).max())
+
+
+def test_rbf_cartesian_reconstruction_converges(grid_dir):
+    """The RBF reconstruction (operatorRBFinterp) recovers a solid-body rotation at the nodes, error falling with level."""
+    import geodesicodis_gb300 as g
+    from oracle import pyoracle as O
+
+    def xyz(lat, lon):
+        return np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], -1)
+
+    errs = []
+    for lv in (2, 3, 4):
+        om = O.OracleMesh(grid_dir / f"grid_{lv}.txt", RADIUS)
+        orc = O.OracleSolver(om, radius=RADIUS, g=0.113, angvel=5.3e-5, h=1e4, alpha=1e-5, dt=10.0)
+        fl, fo = om.field(4), om.field(5)
+        nx, ny = om.field(8), om.field(9)
+        east = np.stack([-np.sin(fo), np.cos(fo), 0 * fo], -1)
+        north = np.stack([-np.sin(fl) * np.cos(fo), -np.sin(fl) * np.sin(fo), np.cos(fl)], -1)
+        n = nx[:, None] * east + ny[:, None] * north
+        v = np.sum(n * np.cross([0.0, 0.0, 1.0], xyz(fl, fo)), axis=1)
+        u = orc.interpolateVelocityCart(v)
+        m = g.Mesh.from_file(grid_dir / f"grid_{lv}.txt", RADIUS)
+        exact = np.cross([0.0, 0.0, 1.0], xyz(m.field(12), m.field(13)))
+        errs.append(np.max(np.abs(u - exact)) / np.max(np.abs(exact)))
+    assert errs[0] < 0.04 and errs[1] < 0.012 and errs[2] < 0.004
+    assert errs[0] > errs[1] > errs[2]
