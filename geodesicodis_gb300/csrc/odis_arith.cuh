@@ -23,6 +23,8 @@ template <> struct Ar<double> {
     __device__ static bool finite(V a) { return (__double2hiint(a) & 0x7ff00000) != 0x7ff00000; }
     __device__ static V ldcg(const V* p) { return __ldcg(p); }
     __device__ static void stcg(V* p, V v) { __stcg(p, v); }
+    // two adjacent values in one aligned vector load (p[0] and p[1], p 16-byte aligned)
+    __device__ static void ld2(const V* p, V& a, V& b) { const double2 v = *reinterpret_cast<const double2*>(p); a = v.x; b = v.y; }
 };
 template <> struct Ar<float> {
     using V = float;
@@ -38,6 +40,7 @@ template <> struct Ar<float> {
     __device__ static bool finite(V a) { return (__float_as_int(a) & 0x7f800000) != 0x7f800000; }
     __device__ static V ldcg(const V* p) { return __ldcg(p); }
     __device__ static void stcg(V* p, V v) { __stcg(p, v); }
+    __device__ static void ld2(const V* p, V& a, V& b) { const float2 v = *reinterpret_cast<const float2*>(p); a = v.x; b = v.y; }
 };
 template <> struct Ar<df64> {
     using V = df64;
@@ -53,6 +56,12 @@ template <> struct Ar<df64> {
     __device__ static bool finite(V a) { return df_finite(a); }
     __device__ static V ldcg(const V* p) { return __ldcg(p); }
     __device__ static void stcg(V* p, V v) { __stcg(p, v); }
+    __device__ static void ld2(const V* p, V& a, V& b)
+    {
+        const float4 v = *reinterpret_cast<const float4*>(p);
+        a = make_float2(v.x, v.y);
+        b = make_float2(v.z, v.w);
+    }
 };
 
 }  // namespace odis

@@ -21,6 +21,7 @@
 // double-float (DF64) or FP32 (FP32-state variant; block sums in FP64).
 #include "odis_sh.cuh"
 #include "odis_df64.cuh"
+#include "odis_arith.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -66,41 +67,7 @@ __host__ __device__ inline int sh_col(int l, int m, int is_sin) { return l * l +
 // Legendre row of (l, m), rows ordered by m then l
 __host__ __device__ inline int p_row(int L, int l, int m) { return m * (L + 1) - m * (m - 1) / 2 + (l - m); }
 
-// ---- arithmetic of each method ---------------------------------------------
-template <class T> struct Ar;
-template <> struct Ar<double> {
-    using V = double;
-    __device__ static V zero() { return 0.0; }
-    __device__ static V fma(V a, V b, V c) { return ::fma(a, b, c); }
-    __device__ static V mul(V a, V b) { return a * b; }
-    __device__ static V add(V a, V b) { return a + b; }
-    __device__ static V sub(V a, V b) { return a - b; }
-    __device__ static V from(double x) { return x; }
-    __device__ static double to(V a) { return a; }
-    __device__ static V shfl(V a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
-};
-template <> struct Ar<float> {
-    using V = float;
-    __device__ static V zero() { return 0.f; }
-    __device__ static V fma(V a, V b, V c) { return fmaf(a, b, c); }
-    __device__ static V mul(V a, V b) { return a * b; }
-    __device__ static V add(V a, V b) { return a + b; }
-    __device__ static V sub(V a, V b) { return a - b; }
-    __device__ static V from(double x) { return (float)x; }
-    __device__ static double to(V a) { return (double)a; }
-    __device__ static V shfl(V a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
-};
-template <> struct Ar<df64> {
-    using V = df64;
-    __device__ static V zero() { return df_make(0.f, 0.f); }
-    __device__ static V fma(V a, V b, V c) { return df_fma(a, b, c); }
-    __device__ static V mul(V a, V b) { return df_mul(a, b); }
-    __device__ static V add(V a, V b) { return df_add(a, b); }
-    __device__ static V sub(V a, V b) { return df_sub(a, b); }
-    __device__ static V from(double x) { return df_from_double(x); }
-    __device__ static double to(V a) { return df_to_double(a); }
-    __device__ static V shfl(V a, int o) { return df_shfl_down(a, o); }
-};
+// arithmetic of each method: Ar<T> (odis_arith.cuh)
 
 // partial[k][chunk] = sum over the chunk's cells of Pbar_lm (cos|sin)(m lon) eta,
 // for the degrees l0 .. l0+nl-1 of order m of this block's tile
@@ -114,45 +81,45 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
     __shared__ T red[kShThreads / 32][2 * kTileL];
     const int m = tiles[3 * blockIdx.x], l0 = tiles[3 * blockIdx.x + 1], nl = tiles[3 * blockIdx.x + 2];
     const int chunk = blockIdx.y;
-    const int per = (N + nchunk - 1) / nchunk;
-    const int i0 = chunk * per, i1 = min(N, i0 + per);
-    T ac[kTileL], as[kTileL];
+    // chunk bounds are even, so cell pairs (i, i+1) stay inside one chunk and are 2-aligned
+    const int per = ((N + nchunk - 1) / nchunk + 1) & ~1;
+    const int i0 = min(N, chunk * per), i1 = min(N, i0 + per);
+    T ac[kTileL], as[kTileL], bc[kTileL], bs[kTileL];
 #pragma unroll
-    for (int j = 0; j < kTileL; j++) { ac[j] = A::zero(); as[j] = A::zero(); }
+    for (int j = 0; j < kTileL; j++) { ac[j] = A::zero(); as[j] = A::zero(); bc[j] = A::zero(); bs[j] = A::zero(); }
     const T* cm = trig + (size_t)(2 * m) * Np;
     const T* sm = trig + (size_t)(2 * m + 1) * Np;
     const T* prow = P + (size_t)p_row(L, l0, m) * Np;
-    // two cells per iteration into separate accumulators: twice the loads in flight
-    T bc[kTileL], bs[kTileL];
+    // two adjacent cells per thread and iteration, each row read with one vector load
+    for (int i = i0 + 2 * threadIdx.x; i < i1; i += 2 * kShThreads) {
+        if (i + 1 < i1) {
+            T e, e2, c1, c2, s1, s2;
+            A::ld2(eta + i, e, e2);
+            A::ld2(cm + i, c1, c2);
+            A::ld2(sm + i, s1, s2);
+            const T ec = A::mul(c1, e), es = A::mul(s1, e);
+            const T ec2 = A::mul(c2, e2), es2 = A::mul(s2, e2);
 #pragma unroll
-    for (int j = 0; j < kTileL; j++) { bc[j] = A::zero(); bs[j] = A::zero(); }
-    int i = i0 + threadIdx.x;
-    for (; i + kShThreads < i1; i += 2 * kShThreads) {
-        const int i2 = i + kShThreads;
-        const T e = eta[i], e2 = eta[i2];
-        const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
-        const T ec2 = A::mul(cm[i2], e2), es2 = A::mul(sm[i2], e2);
-#pragma unroll
-        for (int j = 0; j < kTileL; j++) {
-            if (j < nl) {
-                const T p = prow[(size_t)j * Np + i];
-                const T p2 = prow[(size_t)j * Np + i2];
-                ac[j] = A::fma(p, ec, ac[j]);
-                as[j] = A::fma(p, es, as[j]);
-                bc[j] = A::fma(p2, ec2, bc[j]);
-                bs[j] = A::fma(p2, es2, bs[j]);
+            for (int j = 0; j < kTileL; j++) {
+                if (j < nl) {
+                    T p, p2;
+                    A::ld2(prow + (size_t)j * Np + i, p, p2);
+                    ac[j] = A::fma(p, ec, ac[j]);
+                    as[j] = A::fma(p, es, as[j]);
+                    bc[j] = A::fma(p2, ec2, bc[j]);
+                    bs[j] = A::fma(p2, es2, bs[j]);
+                }
             }
-        }
-    }
-    if (i < i1) {
-        const T e = eta[i];
-        const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
+        } else {
+            const T e = eta[i];
+            const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
 #pragma unroll
-        for (int j = 0; j < kTileL; j++) {
-            if (j < nl) {
-                const T p = prow[(size_t)j * Np + i];
-                ac[j] = A::fma(p, ec, ac[j]);
-                as[j] = A::fma(p, es, as[j]);
+            for (int j = 0; j < kTileL; j++) {
+                if (j < nl) {
+                    const T p = prow[(size_t)j * Np + i];
+                    ac[j] = A::fma(p, ec, ac[j]);
+                    as[j] = A::fma(p, es, as[j]);
+                }
             }
         }
     }
@@ -222,6 +189,7 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
     const int gt = blockIdx.x * kSynthThreads + threadIdx.x;
     const int q = gt / kSynthLanes, j = gt % kSynthLanes;
     const int i = 2 * q, i2 = min(2 * q + 1, N - 1);
+    const bool pair = i2 == i + 1;          // i is even, so (i, i+1) is one aligned vector
     T u = A::zero(), u2 = A::zero();
     if (i < N) {
         for (int m = j; m <= L; m += kSynthLanes) {
@@ -230,7 +198,9 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
             const T* prow = P + (size_t)p_row(L, lstart, m) * Np;
             for (int l = lstart; l <= L; l++) {
                 const T* pr = prow + (size_t)(l - lstart) * Np;
-                const T p0 = pr[i], p1 = pr[i2];
+                T p0, p1;
+                if (pair) A::ld2(pr + i, p0, p1);
+                else { p0 = pr[i]; p1 = pr[i2]; }
                 const T cc = c[sh_col(l, m, 0)];
                 a0 = A::fma(p0, cc, a0);
                 a1 = A::fma(p1, cc, a1);
@@ -242,8 +212,11 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
             }
             const T* cr = trig + (size_t)(2 * m) * Np;
             const T* sr = trig + (size_t)(2 * m + 1) * Np;
-            u = A::fma(cr[i], a0, A::fma(sr[i], b0, u));
-            u2 = A::fma(cr[i2], a1, A::fma(sr[i2], b1, u2));
+            T c0, c1, s0, s1;
+            if (pair) { A::ld2(cr + i, c0, c1); A::ld2(sr + i, s0, s1); }
+            else { c0 = cr[i]; c1 = cr[i2]; s0 = sr[i]; s1 = sr[i2]; }
+            u = A::fma(c0, a0, A::fma(s0, b0, u));
+            u2 = A::fma(c1, a1, A::fma(s1, b1, u2));
         }
     }
 #pragma unroll
