@@ -7,8 +7,8 @@
 // state is FP32 (the stencils gather FP32 values) and the AB3 accumulation is
 // kept at FP64 accuracy as a double-float master (hi, lo) pair: hi is the FP32
 // value the stencils read, lo the rounding residual that only the owning thread
-// reads and writes.  The dissipated-power reduction is FP32 over at most
-// 4 * 64 non-negative terms per tile and FP64 beyond.
+// reads and writes.  The dissipated power is summed in FP32 per thread and per
+// quad within a CTA's share of a group (non-negative terms) and in FP64 beyond.
 //
 // Layout.  Members are grouped by mesh; inside a group they are sorted by
 // steps per orbit (descending) and padded to a multiple of four.  Every state
@@ -326,6 +326,26 @@ __device__ __forceinline__ void cell_tile(const GroupDev& G, const QuadInfo& q, 
     }
 }
 
+// Adds the per-thread FP32 power sums of group g's quads (threads x = tid % qa,
+// y = tid / qa < ny) to the CTA's FP64 accumulators.  Called by every thread.
+__device__ __forceinline__ void fold_group_power(const BatchArgs& a, int g, int qa, int ny, float4 pw, float4* s_pw,
+                                                 double* s_acc)
+{
+    const int tid = threadIdx.x;
+    s_pw[tid] = tid < qa * ny ? pw : f4(0.f);
+    __syncthreads();
+    if (tid < qa) {
+        float4 sm = f4(0.f);
+        for (int yy = 0; yy < ny; yy++) sm = add4v(sm, s_pw[yy * qa + tid]);
+        double* acc = s_acc + a.groups[g].moff + 4 * tid;
+        acc[0] += (double)sm.x;
+        acc[1] += (double)sm.y;
+        acc[2] += (double)sm.z;
+        acc[3] += (double)sm.w;
+    }
+    __syncthreads();
+}
+
 // Active quads of group g at step j: members are sorted by run length
 // (descending), so the quads whose first member still updates or records power
 // (S >= max(j, 1)) are a prefix; binary search over the quads' first slots.
@@ -385,32 +405,29 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(BatchArgs a, int j0, in
         }
         __syncthreads();
         // ---- face phase ----
+        // Power: each thread sums its quad's faces over all of this CTA's tiles of a group in FP32
+        // (non-negative terms); the block folds the threads of a quad once per group, into FP64.
         bool bad = false;
+        float4 pw = f4(0.f);
+        int cur = -1;
         for (int t = blockIdx.x; t < s_ft0[ng]; t += gridDim.x) {
             int g = 0;
             while (g + 1 < ng && t >= s_ft0[g + 1]) g++;
+            if (g != cur) {                                          // uniform over the CTA
+                if (cur >= 0) fold_group_power(a, cur, s_qa[cur], s_ny[cur], pw, s_pw, s_acc);
+                cur = g;
+                pw = f4(0.f);
+            }
             const GroupDev& G = a.groups[g];
             const int qa = s_qa[g], ny = s_ny[g];
             const int x = tid % qa, y = tid / qa;
-            float4 pw = f4(0.f);
             if (y < ny) {
                 const QuadInfo q = quad_info(a, G.moff + 4 * x, j, s_cos, s_sin, true);
                 if (q.mask & 0xFFu)
-                    pw = face_tile<R>(a, G, q, x, y, ny, (t - s_ft0[g]) * ny * R, j, bad);
+                    pw = add4v(pw, face_tile<R>(a, G, q, x, y, ny, (t - s_ft0[g]) * ny * R, j, bad));
             }
-            s_pw[tid] = pw;
-            __syncthreads();
-            if (tid < qa) {
-                float4 sm = f4(0.f);
-                for (int yy = 0; yy < ny; yy++) sm = add4v(sm, s_pw[yy * qa + tid]);
-                double* acc = s_acc + G.moff + 4 * tid;
-                acc[0] += (double)sm.x;
-                acc[1] += (double)sm.y;
-                acc[2] += (double)sm.z;
-                acc[3] += (double)sm.w;
-            }
-            __syncthreads();
         }
+        if (cur >= 0) fold_group_power(a, cur, s_qa[cur], s_ny[cur], pw, s_pw, s_acc);
         if (bad) s_bad = 1;
         double* part = a.part + (size_t)(j & 1) * gridDim.x * a.P + (size_t)blockIdx.x * a.P;
         for (int k = tid; k < a.P; k += blockDim.x) __stcg(&part[k], s_acc[k]);
