@@ -152,9 +152,9 @@ __global__ void k_sh_fold(const T* __restrict__ part, int K, int nchunk, double*
     using A = Ar<T>;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= K) return;
-    T s = A::zero();
-    for (int c = 0; c < nchunk; c++) s = A::add(s, part[(size_t)k * nchunk + c]);
-    t[k] = A::to(s);
+    double s = 0.0;                               // the chunk partials are added in FP64
+    for (int c = 0; c < nchunk; c++) s += A::to(part[(size_t)k * nchunk + c]);
+    t[k] = s;
 }
 
 // c = (F G^-1) t in FP64, one warp per coefficient, stored in the method's type
