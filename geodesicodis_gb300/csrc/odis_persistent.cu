@@ -66,14 +66,12 @@ __device__ bool wait_deps(const unsigned* flags, const int* dep, int nd, unsigne
     return __syncthreads_and(ok) != 0;
 }
 
-// CTA barrier, then one thread makes the CTA's writes visible and publishes v
+// CTA barrier, then one thread publishes v with a GPU-scope release: the barrier
+// orders the CTA's writes before it, and the release is cumulative over them
 __device__ __forceinline__ void signal(unsigned* flag, unsigned v)
 {
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        st_release_u32(flag, v);
-    }
+    if (threadIdx.x == 0) st_release_u32(flag, v);
 }
 
 template <class T>
