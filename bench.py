@@ -27,6 +27,7 @@ of the same workload.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import os
 import subprocess
@@ -51,6 +52,22 @@ def sh_factors(lmax: int, seed: int = 1) -> np.ndarray:
     """f_l * gamma_l: the reference's FREE_LOADING factor gamma_l scaled per degree by f_l ~ U[0.5, 1.5]."""
     import geodesicodis_gb300 as g
     return g.benchmark_sh_factors(GRAV, RADIUS, lmax, seed)
+
+
+@contextlib.contextmanager
+def sh_path(tc):
+    """ODIS_SH_TC around a context creation: "1" tensor-core SH transforms, "0" CUDA-core, None timed choice."""
+    old = os.environ.get("ODIS_SH_TC")
+    if tc is not None:
+        os.environ["ODIS_SH_TC"] = tc
+    try:
+        yield
+    finally:
+        if tc is not None:
+            if old is None:
+                os.environ.pop("ODIS_SH_TC", None)
+            else:
+                os.environ["ODIS_SH_TC"] = old
 
 
 def workload_config(steps_per_orbit: int, n_cells: int, n_faces: int) -> dict:
@@ -229,10 +246,11 @@ def run_ours(args) -> dict:
     N, E = mesh.n_cells, mesh.n_edges
     fac = sh_factors(LMAX)
 
-    def solver(precision, lmax):
+    def solver(precision, lmax, sh_tc=None):
         p = g.make_params(radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt,
                           potential=g.POT_ECC, precision=precision, sh_lmax=lmax, sh_factors=fac if lmax else None)
-        return g.Solver(p, mesh)
+        with sh_path(sh_tc):
+            return g.Solver(p, mesh)
 
     stream = torch.cuda.Stream(device=dev)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)   # 256 MB > L2
@@ -278,9 +296,11 @@ def run_ours(args) -> dict:
     # the other methods, 1 untimed + kv timed orbits each from rest; final states kept for the error report
     kv = max(1, args.steps // 4)
     results, finals = {"df64_sh16": value}, {}
-    for key, prec, lmax in (("df64_sh16", g.DF64, LMAX), ("fp64_sh16", g.FP64, LMAX), ("fp32_sh16", g.FP32, LMAX),
-                            ("df64_plain", g.DF64, 0), ("fp64_plain", g.FP64, 0), ("fp32_plain", g.FP32, 0)):
-        s = solver(prec, lmax)
+    for key, prec, lmax, tc in (("df64_sh16", g.DF64, LMAX, None), ("fp64_sh16", g.FP64, LMAX, None),
+                                ("fp32_sh16", g.FP32, LMAX, None), ("fp32_sh16_tc", g.FP32, LMAX, "1"),
+                                ("df64_plain", g.DF64, 0, None), ("fp64_plain", g.FP64, 0, None),
+                                ("fp32_plain", g.FP32, 0, None)):
+        s = solver(prec, lmax, tc)
         t, _ = timed_orbits(s, kv, 1, collective=False)     # rank 0 only
         if key != "df64_sh16":
             results[key] = N * n * kv / t
@@ -290,8 +310,8 @@ def run_ours(args) -> dict:
         finals[key] = (v, eta, float(pw[-1]))
         s.close()
     errors = {}
-    for key, ref in (("fp32_sh16", "fp64_sh16"), ("df64_sh16", "fp64_sh16"), ("fp32_plain", "fp64_plain"),
-                     ("df64_plain", "fp64_plain")):
+    for key, ref in (("fp32_sh16", "fp64_sh16"), ("fp32_sh16_tc", "fp64_sh16"), ("df64_sh16", "fp64_sh16"),
+                     ("fp32_plain", "fp64_plain"), ("df64_plain", "fp64_plain")):
         (va, ea, pa), (vb, eb_, pb) = finals[key], finals[ref]
         errors[f"{key}_vs_{ref}"] = {"eta": _rel(ea, eb_), "velocity": _rel(va, vb), "power": abs(pa - pb) / abs(pb),
                                      "orbits": 1 + kv}
@@ -452,12 +472,15 @@ def run_level8(args) -> dict:
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     finals = {}
-    for name, prec, lmax in (("fp32_sh32", g.FP32, 32), ("df64_sh32", g.DF64, 32), ("fp64_sh32", g.FP64, 32),
-                             ("fp32_plain", g.FP32, 0), ("df64_plain", g.DF64, 0), ("fp64_plain", g.FP64, 0)):
+    for name, prec, lmax, tc in (("fp32_sh32", g.FP32, 32, None), ("fp32_sh32_tc", g.FP32, 32, "1"),
+                                 ("df64_sh32", g.DF64, 32, None), ("fp64_sh32", g.FP64, 32, None),
+                                 ("fp32_plain", g.FP32, 0, None), ("df64_plain", g.DF64, 0, None),
+                                 ("fp64_plain", g.FP64, 0, None)):
         p = g.make_params(radius=RADIUS, g=GRAV, angvel=angvel, h=h, alpha=alpha, ecc=ECC, obliq=np.deg2rad(0.2),
                           dt=P / n, potential=g.POT_FULL, precision=prec, sh_lmax=lmax,
                           sh_factors=fac if lmax else None)
-        s = g.Solver(p, mesh)
+        with sh_path(tc):
+            s = g.Solver(p, mesh)
         s.run(50)
         s.synchronize()
         t = time.perf_counter()
@@ -474,12 +497,15 @@ def run_level8(args) -> dict:
             "face_hbm_frac": fb / (ms[0] * 1e-3) / 1e9 / peak, "cell_hbm_frac": cb / (ms[1] * 1e-3) / 1e9 / peak,
             "sh_tiles": list(s.sh_tiles()) if lmax else None}
         s.close()
-    for a, b in (("fp32_sh32", "fp64_sh32"), ("df64_sh32", "fp64_sh32"), ("fp32_plain", "fp64_plain")):
+    for a, b in (("fp32_sh32", "fp64_sh32"), ("fp32_sh32_tc", "fp64_sh32"), ("df64_sh32", "fp64_sh32"),
+                 ("fp32_plain", "fp64_plain")):
         (va, ea, pa), (vb, eb_, pb) = finals[a], finals[b]
         out[f"{a}_vs_{b}"] = {"v": _rel(va, vb), "eta": _rel(ea, eb_), "power": abs(pa - pb) / abs(pb),
                               "steps": 50 + args.case_steps}
-    out["tensor_pipe"] = ("0: the Legendre contraction of one instance per step is two matrix-vector products, "
-                          "run on the FP32 (FP32, DF64) or FP64 pipes")
+    out["tensor_pipe"] = ("fp32_sh32_tc runs the Legendre contraction as tcgen05 GEMMs (fp16 hi/lo operand pairs, "
+                          "FP32 accumulation in tensor memory); tensor-pipe activity from ncu in the profile summary. "
+                          "The setup-time timing keeps the CUDA-core transforms (fp32_sh32) when they are faster: "
+                          "both stream the same 4 bytes per Legendre value")
     out["peak_gbs"] = peak
     return out
 
@@ -515,6 +541,7 @@ def main():
     ap.add_argument("--profile-case", choices=["fp64", "df64", "fp32", "batch"], default=None,
                     help="run a short level-6 case for an ncu capture (no timing, no JSON)")
     ap.add_argument("--case-sh", type=int, default=0, help="self-gravity degree of --profile-case")
+    ap.add_argument("--case-level", type=int, default=LEVEL, help="mesh level of --profile-case (stable dt off level 6)")
     ap.add_argument("--sur-train", type=int, default=4096)
     ap.add_argument("--sur-test", type=int, default=512)
     ap.add_argument("--sur-level", type=int, default=5)
@@ -546,7 +573,9 @@ def main():
     if args.profile_case:
         import geodesicodis_gb300 as g
         angvel, P, dt, n = g.derive_time(ANGVEL_IN, DT_TARGET)
-        mesh = g.Mesh.generate(LEVEL, RADIUS)
+        mesh = g.Mesh.generate(args.case_level, RADIUS)
+        if args.case_level != LEVEL:
+            dt = P / g.stable_steps_per_orbit(P, mesh.gravity_wave_omega(GRAV, H), 0.95)
         prec = {"fp64": g.FP64, "df64": g.DF64, "fp32": g.FP32}[args.profile_case]
         p = g.make_params(radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt, potential=g.POT_ECC,
                           precision=prec, sh_lmax=args.case_sh, sh_factors=sh_factors(args.case_sh) if args.case_sh else None)

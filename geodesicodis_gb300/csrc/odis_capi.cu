@@ -578,7 +578,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
         if (st != ODIS_OK) return st;
     }
     if (p->sh_lmax > 0) {
-        st = sh_create(&c->sh, m, p->sh_lmax, c->p.sh_factors, p->precision, c->Np);
+        st = sh_create(&c->sh, m, p->sh_lmax, c->p.sh_factors, p->precision, c->Np, c->d_status);
         if (st != ODIS_OK) return st;
         c->s64.usg = sh_usg64(c->sh);
         c->s32.usg = sh_usg32(c->sh);
@@ -790,7 +790,7 @@ static const void* state_eta(const odis_ctx* c)
          : c->p.precision == ODIS_DF64 ? (const void*)c->sdf.eta : (const void*)c->s64.eta;
 }
 
-static int kernels_per_step(const odis_ctx* c) { return 2 + (c->sh ? sh_kernels_per_step() : 0); }
+static int kernels_per_step(const odis_ctx* c) { return 2 + (c->sh ? sh_kernels_per_step(c->sh) : 0); }
 
 static void enqueue_steps(odis_ctx* c, int n)
 {
@@ -1152,7 +1152,7 @@ extern "C" odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms)
             float t = 0.f;
             cudaEventElapsedTime(&t, a, b);
             ms[which] = (double)t / reps;
-            c->launches += 2LL * reps * (which == 2 ? sh_kernels_per_step() : 1);
+            c->launches += 2LL * reps * (which == 2 ? sh_kernels_per_step(c->sh) : 1);
         }
         if (ge) cudaGraphExecDestroy(ge);
         if (g) cudaGraphDestroy(g);

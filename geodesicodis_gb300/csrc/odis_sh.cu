@@ -20,6 +20,7 @@
 // host.  The arithmetic of the per-step transforms follows the method: FP64,
 // double-float (DF64) or FP32 (FP32-state variant; block sums in FP64).
 #include "odis_sh.cuh"
+#include "odis_sh_tc.cuh"
 #include "odis_df64.cuh"
 #include "odis_arith.cuh"
 
@@ -27,6 +28,7 @@
 #include <cstring>
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 namespace odis {
@@ -61,11 +63,6 @@ void plm_bar(int L, double z, std::vector<double>& P)
         }
     }
 }
-
-// column of harmonic (l, m, cos|sin): l^2 for m=0, l^2 + 2m-1 (cos), l^2 + 2m (sin)
-__host__ __device__ inline int sh_col(int l, int m, int is_sin) { return l * l + (m == 0 ? 0 : 2 * m - 1 + is_sin); }
-// Legendre row of (l, m), rows ordered by m then l
-__host__ __device__ inline int p_row(int L, int l, int m) { return m * (L + 1) - m * (m - 1) / 2 + (l - m); }
 
 // arithmetic of each method: Ar<T> (odis_arith.cuh)
 
@@ -144,17 +141,20 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
     }
 }
 
-// t_k = sum over chunks in a fixed order (in the method's arithmetic; one
-// conversion to FP64 per coefficient)
+// t_k = sum over the chunk partials of coefficient k in FP64, one warp per
+// coefficient: lane j adds chunks j, j+32, ... then the lanes meet in a fixed
+// shuffle tree (the order does not depend on timing)
 template <class T>
-__global__ void k_sh_fold(const T* __restrict__ part, int K, int nchunk, double* __restrict__ t)
+__global__ void __launch_bounds__(128) k_sh_fold(const T* __restrict__ part, int K, int nchunk, double* __restrict__ t)
 {
     using A = Ar<T>;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (k >= K) return;
-    double s = 0.0;                               // the chunk partials are added in FP64
-    for (int c = 0; c < nchunk; c++) s += A::to(part[(size_t)k * nchunk + c]);
-    t[k] = s;
+    double s = 0.0;
+    for (int c = lane; c < nchunk; c += 32) s += A::to(part[(size_t)k * nchunk + c]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) t[k] = s;
 }
 
 // c = (F G^-1) t in FP64, one warp per coefficient, stored in the method's type
@@ -273,6 +273,9 @@ struct ShLoading {
     double* t = nullptr;
     void* coef = nullptr;        // [K] coefficients, method type
     void* usg = nullptr;         // [Np] method type
+    ShTc* tc = nullptr;          // tensor-core transforms (FP32 method), when they fit
+    bool use_tc = false;         // setup-time choice between the tc and CUDA-core transforms
+    int* status = nullptr;       // context status word (device)
 };
 
 void sh_basis_host(const Mesh& m, int L, std::vector<double>& Y)
@@ -348,7 +351,7 @@ static bool upload_rows(void** d, const std::vector<double>& h)
     return cudaMemcpy(*d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) == cudaSuccess;
 }
 
-int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int precision, int Np)
+int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int precision, int Np, int* status)
 {
     *out = nullptr;
     const int K = (L + 1) * (L + 1), MP = (L + 1) * (L + 2) / 2;
@@ -400,7 +403,7 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
             for (int b = 0; b < K; b++) G[(size_t)a * K + b] *= f;
         }
     ShLoading* s = new ShLoading;
-    s->L = L; s->K = K; s->MP = MP; s->N = N; s->Np = Np; s->precision = precision;
+    s->L = L; s->K = K; s->MP = MP; s->N = N; s->Np = Np; s->precision = precision; s->status = status;
     bool ok = true;
     if (precision == ODIS_FP64) ok = upload_rows<double>(&s->P, P) && upload_rows<double>(&s->trig, trig);
     else if (precision == ODIS_DF64) ok = upload_rows<df64>(&s->P, P) && upload_rows<df64>(&s->trig, trig);
@@ -413,6 +416,12 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
          cudaMemcpy(s->FGinv, G.data(), sizeof(double) * G.size(), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMalloc(&s->t, sizeof(double) * K) == cudaSuccess && cudaMalloc(&s->coef, 8 * (size_t)K) == cudaSuccess;
     if (!ok) { sh_destroy(s); return ODIS_ERR_NOMEM; }
+    if (precision == ODIS_FP32) {
+        double pmax = 0.0;
+        for (double x : P) pmax = std::fmax(pmax, std::fabs(x));
+        const int tst = shtc_create(&s->tc, (const float*)s->P, (const float*)s->trig, pmax, L, N, Np, status);
+        if (tst != ODIS_OK && tst != ODIS_ERR_ARG) { sh_destroy(s); return tst; }
+    }
     const int st = sh_autotune(s);
     if (st != ODIS_OK) { sh_destroy(s); return st; }
     *out = s;
@@ -424,6 +433,7 @@ void sh_destroy(ShLoading* s)
     if (!s) return;
     cudaFree(s->P); cudaFree(s->trig); cudaFree(s->tiles); cudaFree(s->part); cudaFree(s->FGinv);
     cudaFree(s->t); cudaFree(s->coef); cudaFree(s->usg);
+    shtc_destroy(s->tc);
     delete s;
 }
 
@@ -492,6 +502,9 @@ static bool forced_tiles(int* f)
 }
 
 template <class T>
+static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st);
+
+template <class T>
 static int autotune_t(ShLoading* s)
 {
     void* eta = nullptr;
@@ -545,6 +558,35 @@ static int autotune_t(ShLoading* s)
         const float ms = force ? 0.f : timeit([&] { launch_synth<T>(s, lanes, 0); });
         if (ms < best) { best = ms; s->lanes = lanes; }
     }
+    if constexpr (std::is_same<T, float>::value) {
+        // tensor-core transforms against the CUDA-core ones, whole per-step sequence;
+        // ODIS_SH_TC=1 or 0 fixes the choice
+        if (s->tc && st == ODIS_OK) {
+            const char* e = std::getenv("ODIS_SH_TC");
+            const int want = (e && e[0] == '1') ? 1 : (e && e[0] == '0') ? 0 : -1;
+            s->use_tc = false;
+            const float cc = want < 0 ? timeit([&] { enqueue_t<float>(s, eta, 0); }) : 0.f;
+            float best_tc = 1e30f;
+            int best_tp = 2;
+            for (int tp : {1, 2}) {
+                if (!shtc_tiles_per_pass_ok(s->tc, tp)) continue;
+                shtc_set_tiles_per_pass(s->tc, tp);
+                s->use_tc = true;
+                const float ms = timeit([&] { enqueue_t<float>(s, eta, 0); });
+                if (ms < best_tc) { best_tc = ms; best_tp = tp; }
+            }
+            shtc_set_tiles_per_pass(s->tc, best_tp);
+            s->use_tc = want == 1 || (want < 0 && best_tc < cc);
+            int h = 0;
+            if (cudaMemcpy(&h, s->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) st = ODIS_ERR_CUDA;
+            else if (h & (1 << ODIS_ERR_TIMEOUT)) st = ODIS_ERR_TIMEOUT;
+            if (!s->use_tc) {          // the operand copies (4 B per Legendre value each) are not kept
+                cudaDeviceSynchronize();
+                shtc_destroy(s->tc);
+                s->tc = nullptr;
+            }
+        }
+    }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     cudaFree(eta);
@@ -562,16 +604,26 @@ int sh_autotune(ShLoading* s)
 
 void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes)
 {
-    if (tl) *tl = s->tl;
-    if (nchunk) *nchunk = s->nchunk;
-    if (lanes) *lanes = s->lanes;
+    if (tl) *tl = s->use_tc ? 0 : s->tl;
+    if (nchunk) *nchunk = s->use_tc ? shtc_chunks(s->tc) : s->nchunk;
+    if (lanes) *lanes = s->use_tc ? shtc_tiles_per_pass(s->tc) : s->lanes;
 }
 
 template <class T>
 static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st)
 {
+    if constexpr (std::is_same<T, float>::value) {
+        if (s->use_tc) {
+            shtc_analysis(s->tc, (const float*)eta, st);
+            k_sh_fold<float><<<(s->K + 3) / 4, 128, 0, st>>>(shtc_partials(s->tc), s->K, shtc_chunks(s->tc), s->t);
+            k_sh_coef<float><<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, (float*)s->coef);
+            shtc_pack(s->tc, (const float*)s->coef, st);
+            shtc_synth(s->tc, (float*)s->usg, st);
+            return;
+        }
+    }
     launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, eta, st);
-    k_sh_fold<T><<<(s->K + 127) / 128, 128, 0, st>>>((const T*)s->part, s->K, s->nchunk, s->t);
+    k_sh_fold<T><<<(s->K + 3) / 4, 128, 0, st>>>((const T*)s->part, s->K, s->nchunk, s->t);
     k_sh_coef<T><<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, (T*)s->coef);
     launch_synth<T>(s, s->lanes, st);
 }
@@ -583,6 +635,6 @@ void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)
     else enqueue_t<float>(s, eta, st);
 }
 
-int sh_kernels_per_step() { return 4; }
+int sh_kernels_per_step(const ShLoading* s) { return s && s->use_tc ? shtc_kernels_per_step() : 4; }
 
 }  // namespace odis

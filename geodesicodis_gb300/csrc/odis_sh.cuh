@@ -19,9 +19,15 @@
 
 namespace odis {
 
+// column of harmonic (l, m, cos|sin) in t and c: l^2 for m=0, l^2 + 2m-1 (cos), l^2 + 2m (sin)
+__host__ __device__ inline int sh_col(int l, int m, int is_sin) { return l * l + (m == 0 ? 0 : 2 * m - 1 + is_sin); }
+// stored Legendre row of (l, m): rows ordered by order m, then degree l
+__host__ __device__ inline int p_row(int L, int l, int m) { return m * (L + 1) - m * (m - 1) / 2 + (l - m); }
+
 struct ShLoading;
 
-int sh_create(ShLoading** out, const Mesh& m, int lmax, const double* factors, int precision, int Np);
+// status: the context's device status word (bounded waits record ODIS_ERR_TIMEOUT there)
+int sh_create(ShLoading** out, const Mesh& m, int lmax, const double* factors, int precision, int Np, int* status);
 void sh_destroy(ShLoading* s);
 // usg buffer ([Np], FP64 or FP32 according to the precision)
 const double* sh_usg64(ShLoading* s);
@@ -30,8 +36,9 @@ const float2* sh_usgdf(ShLoading* s);
 // enqueue analysis + synthesis of the current eta (double* or float*)
 void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t stream);
 // kernels launched by one sh_enqueue
-int sh_kernels_per_step();
-// tile shapes chosen by the setup-time autotuner
+int sh_kernels_per_step(const ShLoading* s);
+// tile shapes chosen by the setup-time autotuner; tl = 0 for the tensor-core
+// transforms (nchunk = analysis chunks, lanes = cell tiles per synthesis pass)
 void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes);
 // host helpers for checks: real SH basis at the nodes, [N][K]
 void sh_basis_host(const Mesh& m, int lmax, std::vector<double>& Y);

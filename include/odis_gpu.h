@@ -228,7 +228,12 @@ odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms);
  * covers tile_l degrees per block with the cells split in `chunks`, the
  * synthesis gives each cell `lanes` threads.  odis_create times every
  * combination on this device and keeps the fastest, unless the environment
- * variable ODIS_SH_TILES="tile_l,chunks,lanes" names one. */
+ * variable ODIS_SH_TILES="tile_l,chunks,lanes" names one.
+ * ODIS_FP32 also has tensor-core transforms (tcgen05, fp16 hi/lo operand pairs,
+ * FP32 accumulation); odis_create times them against the CUDA-core ones and
+ * keeps the faster, unless ODIS_SH_TC=1 (tensor cores) or ODIS_SH_TC=0 (CUDA
+ * cores) fixes the choice.  With the tensor-core transforms tile_l = 0, chunks
+ * = analysis chunks and lanes = 128-cell tiles per synthesis pass. */
 odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes);
 
 /* ---- batched sweep ----------------------------------------------------- */

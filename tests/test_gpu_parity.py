@@ -184,6 +184,24 @@ def test_self_gravity_loading_parity(grid_dir, precision, lmax, tol):
     assert rel_err(orc0.run(1500)[-500:], po[-500:]) > 1e3 * tol
 
 
+@pytest.mark.parametrize("tc", ["1", "0"])
+def test_fp32_self_gravity_transform_paths(grid_dir, monkeypatch, tc):
+    """FP32 method with self-gravity through each transform path, forced by ODIS_SH_TC:
+    the tensor-core (tcgen05, fp16 hi/lo operands, FP32 accumulation in tensor memory)
+    and the CUDA-core transforms.  Power within 1e-4 of the FP64 oracle, state within 1e-4."""
+    import geodesicodis_gb300 as g
+    monkeypatch.setenv("ODIS_SH_TC", tc)
+    fac = g.benchmark_sh_factors(0.113, RADIUS, 8, seed=1)
+    orc, gpu = _pair(grid_dir / "grid_3.txt", precision=1, sh_lmax=8, sh_factors=fac)
+    tl, chunks, lanes = gpu.sh_tiles()
+    assert (tl == 0) == (tc == "1") and chunks > 0 and lanes > 0
+    po, pg = orc.run(1500), gpu.run(1500)
+    _, vo, eo, _, _ = orc.get_state()
+    _, vg, eg, _, _ = gpu.get_state()
+    assert rel_err(pg[-500:], po[-500:]) < 1e-4
+    assert rel_err(eg, eo) < 1e-4 and rel_err(vg, vo) < 1e-4
+
+
 @pytest.mark.parametrize("level,steps", [(2, 700), (3, 2500)])
 def test_df64_parity(grid_dir, level, steps):
     """ODIS_DF64 (the FP64 method in double-float on the FP32 pipes) meets the FP64 parity bar."""
