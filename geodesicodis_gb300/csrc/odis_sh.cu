@@ -87,9 +87,12 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
     const T* cm = trig + (size_t)(2 * m) * Np;
     const T* sm = trig + (size_t)(2 * m + 1) * Np;
     const T* prow = P + (size_t)p_row(L, l0, m) * Np;
-    // two adjacent cells per thread and iteration, each row read with one vector load
-    for (int i = i0 + 2 * threadIdx.x; i < i1; i += 2 * kShThreads) {
-        if (i + 1 < i1) {
+    // two adjacent cells per thread and iteration, each row read with one vector load;
+    // two iterations unrolled so their loads are in flight together
+    int i = i0 + 2 * threadIdx.x;
+#pragma unroll 2
+    for (; i + 1 < i1; i += 2 * kShThreads) {
+        {
             T e, e2, c1, c2, s1, s2;
             A::ld2(eta + i, e, e2);
             A::ld2(cm + i, c1, c2);
@@ -107,7 +110,10 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
                     bs[j] = A::fma(p2, es2, bs[j]);
                 }
             }
-        } else {
+        }
+    }
+    if (i < i1) {           // the last cell of an odd-length final chunk
+        {
             const T e = eta[i];
             const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
 #pragma unroll
@@ -175,7 +181,7 @@ __global__ void __launch_bounds__(32) k_sh_coef(const double* __restrict__ t, in
 // kSynthLanes consecutive threads share a cell and split the orders m between
 // them (m = j, j + kSynthLanes, ...); their sums meet by shuffles in a fixed
 // order.  Two independent accumulator pairs keep two loads in flight per lane.
-template <class T, int kSynthLanes>
+template <class T, int kSynthLanes, int kCells>
 __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict__ P, const T* __restrict__ trig,
                                                             const T* __restrict__ coef, int N, int Np, int L, int K,
                                                             T* __restrict__ usg)
@@ -185,48 +191,66 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
     T* c = reinterpret_cast<T*>(c_raw);
     for (int k = threadIdx.x; k < K; k += kSynthThreads) c[k] = coef[k];
     __syncthreads();
-    // each thread sums orders m = j, j + lanes, ... for the adjacent cells 2q and 2q+1
+    // each thread sums orders m = j, j + lanes, ... for the cell q (kCells = 1) or the
+    // adjacent cells 2q and 2q+1 (kCells = 2)
     const int gt = blockIdx.x * kSynthThreads + threadIdx.x;
     const int q = gt / kSynthLanes, j = gt % kSynthLanes;
-    const int i = 2 * q, i2 = min(2 * q + 1, N - 1);
-    const bool pair = i2 == i + 1;          // i is even, so (i, i+1) is one aligned vector
+    const int i = kCells * q, i2 = kCells == 2 ? min(2 * q + 1, N - 1) : i;
+    const bool pair = kCells == 2 && i2 == i + 1;   // i is even, so (i, i+1) is one aligned vector
     T u = A::zero(), u2 = A::zero();
     if (i < N) {
         for (int m = j; m <= L; m += kSynthLanes) {
             T a0 = A::zero(), b0 = A::zero(), a1 = A::zero(), b1 = A::zero();
             const int lstart = m < 2 ? 2 : m;
             const T* prow = P + (size_t)p_row(L, lstart, m) * Np;
-            for (int l = lstart; l <= L; l++) {
-                const T* pr = prow + (size_t)(l - lstart) * Np;
-                T p0, p1;
-                if (pair) A::ld2(pr + i, p0, p1);
-                else { p0 = pr[i]; p1 = pr[i2]; }
-                const T cc = c[sh_col(l, m, 0)];
-                a0 = A::fma(p0, cc, a0);
-                a1 = A::fma(p1, cc, a1);
-                if (m > 0) {
-                    const T cs = c[sh_col(l, m, 1)];
-                    b0 = A::fma(p0, cs, b0);
-                    b1 = A::fma(p1, cs, b1);
-                }
-            }
+            // the order's trig values are loaded first and are in flight during the degree loop
             const T* cr = trig + (size_t)(2 * m) * Np;
             const T* sr = trig + (size_t)(2 * m + 1) * Np;
             T c0, c1, s0, s1;
             if (pair) { A::ld2(cr + i, c0, c1); A::ld2(sr + i, s0, s1); }
             else { c0 = cr[i]; c1 = cr[i2]; s0 = sr[i]; s1 = sr[i2]; }
+            auto step = [&](int l, T p0, T p1) {
+                const T cc = c[sh_col(l, m, 0)];
+                a0 = A::fma(p0, cc, a0);
+                if (kCells == 2) a1 = A::fma(p1, cc, a1);
+                if (m > 0) {
+                    const T cs = c[sh_col(l, m, 1)];
+                    b0 = A::fma(p0, cs, b0);
+                    if (kCells == 2) b1 = A::fma(p1, cs, b1);
+                }
+            };
+            int l = lstart;
+            // four rows' loads issued before their multiply-adds (four L2 requests in flight)
+            for (; l + 3 <= L; l += 4) {
+                T p0[4], p1[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const T* pr = prow + (size_t)(l + q - lstart) * Np;
+                    if (pair) A::ld2(pr + i, p0[q], p1[q]);
+                    else { p0[q] = pr[i]; p1[q] = kCells == 2 ? pr[i2] : p0[q]; }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) step(l + q, p0[q], p1[q]);
+            }
+            for (; l <= L; l++) {
+                const T* pr = prow + (size_t)(l - lstart) * Np;
+                T p0, p1;
+                if (pair) A::ld2(pr + i, p0, p1);
+                else { p0 = pr[i]; p1 = kCells == 2 ? pr[i2] : p0; }
+                step(l, p0, p1);
+            }
             u = A::fma(c0, a0, A::fma(s0, b0, u));
-            u2 = A::fma(c1, a1, A::fma(s1, b1, u2));
+            if (kCells == 2) u2 = A::fma(c1, a1, A::fma(s1, b1, u2));
         }
     }
 #pragma unroll
     for (int o = kSynthLanes / 2; o > 0; o >>= 1) {
         u = A::add(u, A::shfl(u, o));
-        u2 = A::add(u2, A::shfl(u2, o));
+        if (kCells == 2) u2 = A::add(u2, A::shfl(u2, o));
     }
     if (i < N && j == 0) {
         usg[i] = u;
-        if (2 * q + 1 < N) usg[2 * q + 1] = u2;
+        if (kCells == 2 && 2 * q + 1 < N) usg[2 * q + 1] = u2;
     }
 }
 
@@ -265,6 +289,7 @@ int sh_autotune(ShLoading* s);
 struct ShLoading {
     int L = 0, K = 0, MP = 0, N = 0, Np = 0, precision = ODIS_FP64, ntiles = 0;
     int tl = 8, nchunk = 16, lanes = 4;   // tile shapes chosen by the autotuner
+    int cells = 2;                        // synthesis cells per thread
     void* P = nullptr;           // [MP][Np] Legendre rows, method type
     void* trig = nullptr;        // [2(L+1)][Np] cos(m lon), sin(m lon), method type
     int* tiles = nullptr;        // [ntiles][3] (m, l0, nl)
@@ -467,18 +492,21 @@ static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int nt
 }
 
 template <class T>
-static void launch_synth(const ShLoading* s, int lanes, cudaStream_t st)
+static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t st)
 {
-    const int sb = ((s->N + 1) / 2 * lanes + kSynthThreads - 1) / kSynthThreads;
+    const int sb = ((s->N + cells - 1) / cells * lanes + kSynthThreads - 1) / kSynthThreads;
     const size_t sm = sizeof(T) * s->K;
     const T* P = (const T*)s->P;
     const T* trig = (const T*)s->trig;
     const T* c = (const T*)s->coef;
     T* u = (T*)s->usg;
-    if (lanes == 1) k_sh_synth<T, 1><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u);
-    else if (lanes == 2) k_sh_synth<T, 2><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u);
-    else if (lanes == 4) k_sh_synth<T, 4><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u);
-    else k_sh_synth<T, 8><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u);
+#define ODIS_SYNTH(LN, CL) k_sh_synth<T, LN, CL><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u)
+    if (cells == 2) {
+        if (lanes == 1) ODIS_SYNTH(1, 2); else if (lanes == 2) ODIS_SYNTH(2, 2); else if (lanes == 4) ODIS_SYNTH(4, 2); else ODIS_SYNTH(8, 2);
+    } else {
+        if (lanes == 1) ODIS_SYNTH(1, 1); else if (lanes == 2) ODIS_SYNTH(2, 1); else if (lanes == 4) ODIS_SYNTH(4, 1); else ODIS_SYNTH(8, 1);
+    }
+#undef ODIS_SYNTH
 }
 
 // Self-tuning of the transform tiles: every candidate is timed on this mesh
@@ -486,18 +514,20 @@ static void launch_synth(const ShLoading* s, int lanes, cudaStream_t st)
 // and the fastest is kept.  Results do not depend on the choice of the
 // synthesis lanes; the analysis's chunking changes only the order of the
 // partial sums.
-// ODIS_SH_TILES="tile_l,chunks,lanes" (tile_l in {2,4,8}, chunks in {8,16,32,64},
-// lanes in {1,2,4,8}) fixes the tiles instead of timing them, e.g. to reproduce
-// a run bit for bit or to profile a given variant.  Anything else is ignored.
+// ODIS_SH_TILES="tile_l,chunks,lanes[,cells]" (tile_l in {2,4,8}, chunks in
+// {8,16,32,64}, lanes in {1,2,4,8}, synthesis cells per thread in {1,2}, default
+// 2) fixes the tiles instead of timing them, e.g. to reproduce a run bit for bit
+// or to profile a given variant.  Anything else is ignored.
 static bool forced_tiles(int* f)
 {
     const char* e = std::getenv("ODIS_SH_TILES");
     if (!e) return false;
-    int a = 0, b = 0, c = 0;
-    if (std::sscanf(e, "%d,%d,%d", &a, &b, &c) != 3) return false;
+    int a = 0, b = 0, c = 0, d = 2;
+    const int n = std::sscanf(e, "%d,%d,%d,%d", &a, &b, &c, &d);
+    if (n != 3 && n != 4) return false;
     const bool ok = (a == 2 || a == 4 || a == 8) && (b == 8 || b == 16 || b == 32 || b == 64) &&
-                    (c == 1 || c == 2 || c == 4 || c == 8);
-    if (ok) { f[0] = a; f[1] = b; f[2] = c; }
+                    (c == 1 || c == 2 || c == 4 || c == 8) && (d == 1 || d == 2);
+    if (ok) { f[0] = a; f[1] = b; f[2] = c; f[3] = d; }
     return ok;
 }
 
@@ -530,7 +560,7 @@ static int autotune_t(ShLoading* s)
     float best = 1e30f;
     int best_tl = 8, best_ch = 16;
     std::vector<int> best_tiles;
-    int forced[3] = {0, 0, 0};
+    int forced[4] = {0, 0, 0, 2};
     const bool force = forced_tiles(forced);
     int* dt = nullptr;
     cudaMalloc(&dt, sizeof(int) * 3 * (size_t)(s->L + 1) * (s->L + 1));
@@ -553,11 +583,12 @@ static int autotune_t(ShLoading* s)
         cudaMemcpy(s->tiles, best_tiles.data(), sizeof(int) * best_tiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
         st = ODIS_ERR_NOMEM;
     best = 1e30f;
-    for (int lanes : {1, 2, 4, 8}) {
-        if (force && lanes != forced[2]) continue;
-        const float ms = force ? 0.f : timeit([&] { launch_synth<T>(s, lanes, 0); });
-        if (ms < best) { best = ms; s->lanes = lanes; }
-    }
+    for (int cells : {2, 1})
+        for (int lanes : {1, 2, 4, 8}) {
+            if (force && (lanes != forced[2] || cells != forced[3])) continue;
+            const float ms = force ? 0.f : timeit([&] { launch_synth<T>(s, lanes, cells, 0); });
+            if (ms < best) { best = ms; s->lanes = lanes; s->cells = cells; }
+        }
     if constexpr (std::is_same<T, float>::value) {
         // tensor-core transforms against the CUDA-core ones, whole per-step sequence;
         // ODIS_SH_TC=1 or 0 fixes the choice
@@ -625,7 +656,7 @@ static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st)
     launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, eta, st);
     k_sh_fold<T><<<(s->K + 3) / 4, 128, 0, st>>>((const T*)s->part, s->K, s->nchunk, s->t);
     k_sh_coef<T><<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, (T*)s->coef);
-    launch_synth<T>(s, s->lanes, st);
+    launch_synth<T>(s, s->lanes, s->cells, st);
 }
 
 void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)
