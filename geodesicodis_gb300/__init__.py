@@ -75,6 +75,8 @@ _SIGS = {
     "odis_mesh_sizes": ([_V, _I, _I, _I], C.c_int),
     "odis_mesh_field": ([_V, C.c_int, _D], C.c_int),
     "odis_mesh_topology": ([_V, _I, _I, _I, _I, _D, _I], C.c_int),
+    "odis_mesh_vertex_field": ([_V, C.c_int, _D], C.c_int),
+    "odis_mesh_vertex_topology": ([_V, _I, _I, _I, _I], C.c_int),
     "odis_mesh_destroy": ([_V], None),
     "odis_mesh_gravity_wave_omega": ([_V, C.c_double, C.c_double, C.c_int, _D], C.c_int),
     "odis_stable_steps_per_orbit": ([C.c_double, C.c_double, C.c_double, _I], C.c_int),
@@ -92,6 +94,7 @@ _SIGS = {
     "odis_ab3": ([_V, _V, _V, C.c_int, C.c_int, C.c_int], C.c_int),
     "odis_interpolate_velocity": ([_V, _V, _V, C.c_int], C.c_int),
     "odis_interpolate_cartesian": ([_V, _V, _V, C.c_int], C.c_int),
+    "odis_momentum_advection": ([_V, _V, _V, _V, _V, _V, C.c_int], C.c_int),
     "odis_update_energy": ([_V, _V, _V, _V, C.c_int], C.c_int),
     "odis_run_steps": ([_V, C.c_int, _V, C.c_int], C.c_int),
     "odis_get_state": ([_V, _I, _D, _D, _D, _D], C.c_int),
@@ -238,6 +241,22 @@ class Mesh:
             "odis_mesh_topology")
         return dict(face_nodes=fn, faces=faces, node_face_dir=nfd, interp_friends=ifr, interp_w=iw, interp_n=inn)
 
+    def vertex_field(self, which: int) -> np.ndarray:
+        """0 area of the vertex's node triangle, 1-3 kite fractions R(v, j), 4 sin(lat)."""
+        out = np.zeros(self.n_vertices)
+        _ck(lib().odis_mesh_vertex_field(self._h, which, _dp(out)), "odis_mesh_vertex_field")
+        return out
+
+    def vertex_topology(self):
+        V, E = self.n_vertices, self.n_edges
+        vn = np.zeros((V, 3), np.int32)
+        vf = np.zeros((V, 3), np.int32)
+        vd = np.zeros((V, 3), np.int32)
+        fv = np.zeros((E, 2), np.int32)
+        ip = lambda a: a.ctypes.data_as(_I)  # noqa: E731
+        _ck(lib().odis_mesh_vertex_topology(self._h, ip(vn), ip(vf), ip(vd), ip(fv)), "odis_mesh_vertex_topology")
+        return dict(vert_nodes=vn, vert_faces=vf, vert_face_dir=vd, face_verts=fv)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h and h.value and _lib is not None:
@@ -301,6 +320,16 @@ class Solver:
         v = np.ascontiguousarray(v, np.float64)
         _ck(lib().odis_interpolate_cartesian(self._h, _vp(out), _vp(v), MEM_HOST), "odis_interpolate_cartesian")
         return out
+
+    def calculateMomentumAdvection(self, dvdt: np.ndarray, v: np.ndarray, h_total: np.ndarray):
+        """(dvdt + PV flux - grad KE, KE at the nodes): the reference's calculateMomentumAdvection."""
+        out = np.array(dvdt, np.float64, copy=True)
+        ekin = np.zeros(self.N)
+        v = np.ascontiguousarray(v, np.float64)
+        h = np.ascontiguousarray(h_total, np.float64)
+        _ck(lib().odis_momentum_advection(self._h, self.mesh._h, _vp(out), _vp(v), _vp(h), _vp(ekin), MEM_HOST),
+            "odis_momentum_advection")
+        return out, ekin
 
     def updateEnergy(self, uv: np.ndarray):
         """(area-mean dissipation W/m^2, per-face dissipation)."""

@@ -1,0 +1,22 @@
+// Nonlinear momentum advection on the device (see odis_advection.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "odis_internal.h"
+
+namespace odis {
+
+struct AdvDev;
+
+int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np);
+void adv_destroy(AdvDev* a);
+// dvdt[E] += PV flux - G KE for velocity v[E] and column thickness h_total[N];
+// ekin[N] receives the kinetic energy (device; adv_ekin_scratch gives a buffer).
+// rbf / cell_face: the context's Cartesian reconstruction blocks and cell-face table.
+void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dvdt, const double* v,
+                  const double* h_total, double* ekin, cudaStream_t s);
+double* adv_ekin_scratch(AdvDev* a);
+int adv_kernels_per_call();
+
+}  // namespace odis

@@ -10,6 +10,7 @@
 #include "odis_device.cuh"
 #include "odis_kernels.cuh"
 #include "odis_sh.cuh"
+#include "odis_advection.cuh"
 #include "odis_df64.cuh"
 #include "odis_persistent.cuh"
 
@@ -107,6 +108,7 @@ struct odis_ctx {
     double* stage[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t stage_n = 0;
     ShLoading* sh = nullptr;
+    AdvDev* adv = nullptr;           // nonlinear advection operators (built on first use)
     PersistPlan plan{};          // persistent single-launch loop (FP64 / DF64 without self-gravity)
     bool persist_ok = false;     // the plan fits one CTA per SM and cooperative launch is available
     bool persist_on = true;      // odis_set_persistent
@@ -119,6 +121,7 @@ struct odis_ctx {
     ~odis_ctx() {
         if (graph) cudaGraphExecDestroy(graph);
         if (sh) sh_destroy(sh);
+        if (adv) adv_destroy(adv);
         if (d_power) cudaFree(d_power);
         if (d_phase) cudaFree(d_phase);
         if (plan.part) cudaFree(plan.part);
@@ -224,6 +227,31 @@ extern "C" odis_status odis_mesh_topology(const odis_mesh* mp, int* face_nodes, 
     if (interp_friends) std::memcpy(interp_friends, m.interp_friends.data(), sizeof(int) * m.E * 10);
     if (interp_w) std::memcpy(interp_w, m.interp_w.data(), sizeof(double) * m.E * 10);
     if (interp_n) std::memcpy(interp_n, m.interp_n.data(), sizeof(int) * m.E);
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_mesh_vertex_field(const odis_mesh* mp, int which, double* out)
+{
+    if (!mp || !out) return ODIS_ERR_ARG;
+    const Mesh& m = mp->m;
+    for (int v = 0; v < m.V; v++) {
+        if (which == 0) out[v] = m.vert_area[v];
+        else if (which >= 1 && which <= 3) out[v] = m.vert_R[(size_t)v * 3 + which - 1];
+        else if (which == 4) out[v] = std::sin(m.vert_sph[(size_t)v * 2]);
+        else return ODIS_ERR_ARG;
+    }
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_mesh_vertex_topology(const odis_mesh* mp, int* vert_nodes, int* vert_faces,
+                                                 int* vert_face_dir, int* face_verts)
+{
+    if (!mp) return ODIS_ERR_ARG;
+    const Mesh& m = mp->m;
+    if (vert_nodes) std::memcpy(vert_nodes, m.vert_nodes.data(), sizeof(int) * m.V * 3);
+    if (vert_faces) std::memcpy(vert_faces, m.vert_faces.data(), sizeof(int) * m.V * 3);
+    if (vert_face_dir) std::memcpy(vert_face_dir, m.vert_face_dir.data(), sizeof(int) * m.V * 3);
+    if (face_verts) std::memcpy(face_verts, m.face_verts.data(), sizeof(int) * m.E * 2);
     return ODIS_OK;
 }
 
@@ -714,6 +742,28 @@ extern "C" odis_status odis_interpolate_cartesian(odis_ctx* c, double* uxyz, con
     if (!dv) return ODIS_ERR_CUDA;
     launch_rbf(c->rbf, c->op64.cc.edge, c->N, c->Np, dv, dout, c->stream);
     int st = io.back(uxyz, dout, (size_t)3 * c->N);
+    return st != ODIS_OK ? st : io.done();
+}
+
+extern "C" odis_status odis_momentum_advection(odis_ctx* c, const odis_mesh* mesh, double* dvdt, const double* v,
+                                               const double* h_total, double* ekin, int mem)
+{
+    if (!c || !dvdt || !v || !h_total || !mem_ok(mem)) return ODIS_ERR_ARG;
+    if (!c->adv) {
+        if (!mesh || mesh->m.N != c->N || mesh->m.E != c->E) return ODIS_ERR_ARG;
+        const int st = adv_create(&c->adv, mesh->m, c->p.angvel, c->Ep, c->Np);
+        if (st != ODIS_OK) return st;
+    }
+    Io io{c, mem};
+    const double* dv = io.in(v, c->E);
+    const double* dh = io.in(h_total, c->N);
+    double* dd = io.in(dvdt, c->E);
+    double* dk = (mem == ODIS_MEM_DEVICE && ekin) ? ekin : (mem == ODIS_MEM_DEVICE ? adv_ekin_scratch(c->adv) : io.out(ekin));
+    if (!dv || !dh || !dd) return ODIS_ERR_CUDA;
+    adv_momentum(c->adv, c->rbf, c->op64.cc.edge, dd, dv, dh, dk, c->stream);
+    c->launches += adv_kernels_per_call();
+    int st = io.back(dvdt, dd, c->E);
+    if (st == ODIS_OK && ekin) st = io.back(ekin, dk, c->N);
     return st != ODIS_OK ? st : io.done();
 }
 

@@ -44,6 +44,13 @@ struct Mesh {
     std::vector<int> interp_friends;   // [E][10]
     std::vector<double> interp_w;      // [E][10]
     std::vector<int> interp_n;         // [E]
+    // vertex geometry of the nonlinear terms (src/mesh.cpp:436-506, 826-866, 911-1029, 1117-1148)
+    std::vector<int> vert_nodes;       // [V][3] the creating node and its two friends
+    std::vector<int> face_verts;       // [E][2] the face's two vertices (centroids j-1, j of its first node)
+    std::vector<double> vert_R;        // [V][3] kite fraction of the vertex in the control volume of vert_nodes
+    std::vector<int> vert_faces;       // [V][3] ascending face ids
+    std::vector<int> vert_face_dir;    // [V][3] +1 / -1: circulation sign of the face normal about the vertex
+    std::vector<double> vert_area;     // [V] spherical area of the triangle of the vertex's nodes
     int nfriends(int i) const { return friends[i * 6 + 5] < 0 ? 5 : 6; }
 };
 

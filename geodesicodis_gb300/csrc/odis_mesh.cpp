@@ -194,6 +194,8 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
     m.vertexes.assign((size_t)N * 6, -1);
     m.vert_sph.clear();
     m.vert_sph.reserve((size_t)N * 4);
+    m.vert_nodes.clear();
+    m.vert_nodes.reserve((size_t)N * 6);
     for (int i = 0; i < N; i++) {
         int k = m.nfriends(i);
         for (int j = 0; j < k; j++) {
@@ -204,6 +206,9 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
             m.vert_sph.push_back(v.lat);
             m.vert_sph.push_back(v.lon);
             const int nb[2] = {m.friends[i * 6 + j % k], m.friends[i * 6 + (j + 1) % k]};
+            m.vert_nodes.push_back(i);
+            m.vert_nodes.push_back(nb[0]);
+            m.vert_nodes.push_back(nb[1]);
             for (int f : nb) {
                 int kf = m.nfriends(f);
                 for (int q = 0; q < kf; q++) {
@@ -357,7 +362,85 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
         }
         m.interp_n[e] = slot;
     }
-    return bad ? ODIS_ERR_MESH : ODIS_OK;
+    if (bad) return ODIS_ERR_MESH;
+
+    // --- vertex geometry of the nonlinear terms ---------------------------
+    const int V = m.V;
+    m.face_verts.assign((size_t)E * 2, -1);
+    for (int e = 0; e < E; e++) {
+        const int i = m.face_nodes[e * 2], j = face_slot[e], k = m.nfriends(i);
+        m.face_verts[e * 2] = m.vertexes[i * 6 + (j + k - 1) % k];
+        m.face_verts[e * 2 + 1] = m.vertexes[i * 6 + j % k];
+    }
+    // kite fractions: the reference assigns vertex_R(v, node) once per face about
+    // the node, and the node's highest-numbered face writes last; the same
+    // ranking about that face gives the same sums, bit for bit
+    m.vert_R.assign((size_t)V * 3, 0.0);
+    int badv = 0;
+#pragma omp parallel for schedule(static) reduction(+ : badv)
+    for (int nd = 0; nd < N; nd++) {
+        const int k = m.nfriends(nd);
+        int e = -1;
+        for (int j = 0; j < k; j++) e = std::max(e, m.faces[nd * 6 + j]);
+        LL ie{m.face_int[e * 2], m.face_int[e * 2 + 1]};
+        LL c = node(nd);
+        Ranked fr[6], vr[6];
+        for (int j = 0; j < k; j++) {
+            int id = m.faces[nd * 6 + j];
+            double a = angle_about(ie, LL{m.face_int[id * 2], m.face_int[id * 2 + 1]}, c) * 180. / kPi;
+            if (a > 0.0 + 1e-8) a -= 360.0;
+            fr[j] = {id, a};
+            int vid = m.vertexes[nd * 6 + j];
+            double b = angle_about(ie, LL{m.vert_sph[vid * 2], m.vert_sph[vid * 2 + 1]}, c) * 180. / kPi;
+            if (b > 0.0 + 1e-8) b -= 360.0;
+            vr[j] = {vid, b};
+        }
+        auto desc = [](const Ranked& a, const Ranked& b) { return a.deg > b.deg; };
+        std::sort(fr, fr + k, desc);
+        std::sort(vr, vr + k, desc);
+        auto vpos = [&](int vid) { return LL{m.vert_sph[vid * 2], m.vert_sph[vid * 2 + 1]}; };
+        auto ipos = [&](int fid) { return LL{m.face_int[fid * 2], m.face_int[fid * 2 + 1]}; };
+        double area_cv = 0.0;
+        for (int j = 0; j < k; j++) area_cv += sph_tri_area(c, vpos(vr[j].id), vpos(vr[(j + 1) % k].id), radius);
+        for (int j = 0; j < k; j++) {
+            LL v = vpos(vr[j].id);
+            const double a1 = sph_tri_area(c, v, ipos(fr[j].id), radius);
+            const double a2 = sph_tri_area(c, v, ipos(fr[(j + 1) % k].id), radius);
+            int slot = -1;
+            for (int q = 0; q < 3; q++)
+                if (m.vert_nodes[vr[j].id * 3 + q] == nd) { slot = q; break; }
+            if (slot < 0) { badv++; continue; }
+            m.vert_R[vr[j].id * 3 + slot] = (a1 + a2) / area_cv;
+        }
+    }
+    if (badv) return ODIS_ERR_MESH;
+    // faces about each vertex, in face order, and their circulation signs
+    m.vert_faces.assign((size_t)V * 3, -1);
+    m.vert_face_dir.assign((size_t)V * 3, 0);
+    for (int e = 0; e < E; e++)
+        for (int q = 0; q < 2; q++) {
+            const int v = m.face_verts[e * 2 + q];
+            for (int j = 0; j < 3; j++) {
+                if (m.vert_faces[v * 3 + j] >= 0) continue;
+                m.vert_faces[v * 3 + j] = e;
+                double mm, xv, yv;
+                stereo(LL{m.face_centre[e * 2], m.face_centre[e * 2 + 1]}, LL{m.vert_sph[v * 2], m.vert_sph[v * 2 + 1]},
+                       radius, mm, xv, yv);
+                const double cross = xv * m.face_normal[e * 2 + 1] - yv * m.face_normal[e * 2];
+                m.vert_face_dir[v * 3 + j] = cross > 0 ? 1 : -1;
+                break;
+            }
+        }
+    m.vert_area.assign(V, 0.0);
+    for (int v = 0; v < V; v++) {
+        if (m.vert_faces[v * 3 + 2] < 0) return ODIS_ERR_MESH;
+        double area = 0.0;
+        for (int j = 0; j < 3; j++)
+            area += std::fabs(sph_tri_area(LL{m.vert_sph[v * 2], m.vert_sph[v * 2 + 1]}, node(m.vert_nodes[v * 3 + j]),
+                                           node(m.vert_nodes[v * 3 + (j + 1) % 3]), radius));
+        m.vert_area[v] = area;
+    }
+    return ODIS_OK;
 }
 
 // Largest gravity-wave frequency of the discrete operator: sqrt of the largest

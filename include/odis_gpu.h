@@ -14,6 +14,8 @@
  *   odis_interpolate_velocity <- interpolateVelocity include/interpolation.h:12, src/interpolation.cpp:26-62
  *   odis_interpolate_cartesian <- interpolateVelocityCartRBF include/interpolation.h:16, src/interpolation.cpp:64-174
  *   odis_update_energy     <- updateEnergy        include/energy.h:10,          src/energy.cpp:13-61
+ *   odis_momentum_advection <- calculateMomentumAdvection src/momAdvection.cpp:11-267 (updateMomentum's
+ *                             advection branch, src/updateMomentum.cpp:35-39)
  *   odis_run_steps         <- the body of ab3Explicit's time loop, src/timeIntegrator.cpp:205-313
  *   odis_get_state / odis_set_state <- writeInitialConditions / loadInitialConditions,
  *                                      src/initialConditions.cpp:19,209
@@ -125,6 +127,15 @@ odis_status odis_mesh_field(const odis_mesh* m, int which, double* out);
  * interp_w [E][10], interp_n [E]; any may be NULL */
 odis_status odis_mesh_topology(const odis_mesh* m, int* face_nodes, int* faces, int* node_face_dir,
                                int* interp_friends, double* interp_w, int* interp_n);
+/* Vertex geometry of the nonlinear terms (src/mesh.cpp:436-506, 826-866,
+ * 911-1029, 1117-1148), per vertex [V]: which = 0 area of the triangle of its
+ * three nodes, 1..3 kite fraction R(v, j) of the vertex in the control volume
+ * of its node j, 4 sin(latitude). */
+odis_status odis_mesh_vertex_field(const odis_mesh* m, int which, double* out);
+/* vert_nodes [V][3], vert_faces [V][3] (ascending), vert_face_dir [V][3],
+ * face_verts [E][2] (the two vertices bounding each face); any may be NULL */
+odis_status odis_mesh_vertex_topology(const odis_mesh* m, int* vert_nodes, int* vert_faces, int* vert_face_dir,
+                                      int* face_verts);
 void odis_mesh_destroy(odis_mesh* m);
 /* Largest gravity-wave frequency (rad/s) of the discrete operator: sqrt of the
  * largest eigenvalue of -g h D G, by `iters` power iterations (host).  The
@@ -173,6 +184,16 @@ odis_status odis_interpolate_velocity(odis_ctx* c, double* uv, const double* v, 
  * radial-basis reconstruction over each node's faces (the "x/y/z velocity"
  * output fields). */
 odis_status odis_interpolate_cartesian(odis_ctx* c, double* uxyz, const double* v, int mem);
+/* calculateMomentumAdvection (include/momAdvection.h, src/momAdvection.cpp:11-267):
+ * dvdt[E] += potential-vorticity flux - G KE for the face velocities v[E] and
+ * the column thickness h_total[N] (h + eta).  The PV is (curl v + f) / h at the
+ * vertices, with h from the nodes by area x kite-fraction weights (Ringler et
+ * al. 2010 eq. 25); the flux is the TRiSK sum with the mean PV (eq. 49); KE is
+ * half the squared RBF Cartesian velocity at the nodes.  ekin[N] (nullable)
+ * receives KE.  `mesh` is the one the context was created from; the first
+ * call builds the vertex operators from it. */
+odis_status odis_momentum_advection(odis_ctx* c, const odis_mesh* mesh, double* dvdt, const double* v,
+                                    const double* h_total, double* ekin, int mem);
 /* e[E] (nullable) per-face dissipation and *avg area-mean (W m^-2) from uv[E][2] */
 odis_status odis_update_energy(odis_ctx* c, double* avg, double* e, const double* uv, int mem);
 

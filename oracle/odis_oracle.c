@@ -260,6 +260,12 @@ typedef struct {
     double *interp_w;     /* [E][10] */
     int *interp_n;        /* [E] number of valid entries (10, 9 or 8) */
     double *trig;         /* [N][10]: cosLat sinLat cosLon sinLon cos2Lat sin2Lat cos2Lon sin2Lon cosSqLat sinSqLat */
+    int *face_verts;      /* [E][2] face_vertexes */
+    double *vert_R;       /* [V][3] kite fraction of vertex v in the control volume of vert_nodes(v, j) */
+    int *vert_faces;      /* [V][3] */
+    int *vert_face_dir;   /* [V][3] */
+    double *vert_area;    /* [V] */
+    orc_csr Curl;         /* V x E, operatorCurl */
     orc_csr G, D, C0;     /* gradient (E x N), divergence (N x E), Coriolis without Omega factor is not kept: C0 = Coriolis with Omega=1 */
 } orc_mesh;
 
@@ -273,7 +279,8 @@ void orc_mesh_free(orc_mesh *M)
     free(M->face_nodes); free(M->face_len); free(M->face_dist); free(M->face_area); free(M->face_centre);
     free(M->face_m); free(M->face_normal); free(M->face_int); free(M->face_nxyz); free(M->interp_friends); free(M->interp_w);
     free(M->interp_n); free(M->trig);
-    csr_free(&M->G); csr_free(&M->D); csr_free(&M->C0);
+    free(M->face_verts); free(M->vert_R); free(M->vert_faces); free(M->vert_face_dir); free(M->vert_area);
+    csr_free(&M->G); csr_free(&M->D); csr_free(&M->C0); csr_free(&M->Curl);
     free(M);
 }
 
@@ -341,6 +348,8 @@ static int assign_faces(orc_mesh *M)
     M->interp_friends = (int *)calloc((size_t)E * 10, sizeof(int));
     M->interp_w = (double *)calloc((size_t)E * 10, sizeof(double));
     M->interp_n = (int *)calloc(E, sizeof(int));
+    M->face_verts = (int *)calloc((size_t)E * 2, sizeof(int));
+    M->vert_R = (double *)calloc((size_t)M->V * 3, sizeof(double));
     for (int i = 0; i < N * 6; i++) M->faces[i] = -1;
 
     int fc = 0;
@@ -437,6 +446,11 @@ static int assign_faces(orc_mesh *M)
                 double a1 = tri_area_sph(sn[0], v1[0], p1[0], sn[1], v1[1], p1[1], r);
                 double a2 = tri_area_sph(sn[0], v1[0], p2[0], sn[1], v1[1], p2[1], r);
                 R[j] = (a1 + a2) / area_cv;
+                /* face_vertexes of the face ranked 1, src/mesh.cpp:826-829 (the last face to rank it wins) */
+                if (j == 1) { M->face_verts[fl[1].id * 2] = vl[1].id; M->face_verts[fl[1].id * 2 + 1] = vl[0].id; }
+                /* vertex_R(v, slot of this node), src/mesh.cpp:857-866 */
+                for (int c = 0; c < 3; c++)
+                    if (M->vert_nodes[vl[j].id * 3 + c] == nd) { M->vert_R[vl[j].id * 3 + c] = R[j]; break; }
             }
             for (int j = 0; j < fn; j++) {
                 if (fl[j].id == i) continue;
@@ -456,6 +470,60 @@ static int assign_faces(orc_mesh *M)
         M->interp_n[i] = jadd;
         M->face_area[i] = M->face_dist[i] * M->face_len[i];                        /* :1093 */
     }
+    return 0;
+}
+
+/* vertex_faces, vertex_face_dir and vertex areas (src/mesh.cpp:911-1029,
+ * 1117-1148); operatorCurl (src/mesh.cpp:3122-3175) */
+static int build_vertex_geometry(orc_mesh *M)
+{
+    int V = M->V, E = M->E;
+    double r = M->r;
+    M->vert_faces = (int *)malloc(sizeof(int) * V * 3);
+    M->vert_face_dir = (int *)calloc((size_t)V * 3, sizeof(int));
+    M->vert_area = (double *)calloc(V, sizeof(double));
+    for (int i = 0; i < V * 3; i++) M->vert_faces[i] = -1;
+    for (int i = 0; i < E; i++) {
+        for (int s = 0; s < 2; s++) {
+            int v = M->face_verts[i * 2 + s];
+            for (int j = 0; j < 3; j++) {
+                if (M->vert_faces[v * 3 + j] >= 0) continue;
+                M->vert_faces[v * 3 + j] = i;
+                double m, xv, yv;
+                map_at_point(&m, &xv, &yv, M->face_centre[i * 2], M->vert_sph[v * 2], M->face_centre[i * 2 + 1],
+                             M->vert_sph[v * 2 + 1], r);
+                double cross = xv * M->face_normal[i * 2 + 1] - yv * M->face_normal[i * 2];
+                M->vert_face_dir[v * 3 + j] = cross > 0 ? 1 : -1;
+                break;
+            }
+        }
+    }
+    for (int i = 0; i < V; i++) {
+        double area = 0.0;
+        const double *sv = &M->vert_sph[i * 2];
+        for (int j = 0; j < 3; j++) {
+            const double *s1 = &M->node_sph[M->vert_nodes[i * 3 + j] * 2];
+            const double *s2 = &M->node_sph[M->vert_nodes[i * 3 + (j + 1) % 3] * 2];
+            area += fabs(tri_area_sph(sv[0], s1[0], s2[0], sv[1], s1[1], s2[1], r));
+        }
+        M->vert_area[i] = area;
+    }
+    orc_csr *C = &M->Curl;
+    C->rows = V; C->cols = E;
+    C->rowptr = (int *)malloc(sizeof(int) * (V + 1));
+    C->col = (int *)malloc(sizeof(int) * 3 * V);
+    C->val = (double *)malloc(sizeof(double) * 3 * V);
+    for (int i = 0; i < V; i++) {
+        C->rowptr[i] = 3 * i;
+        for (int j = 0; j < 3; j++) {
+            int f = M->vert_faces[i * 3 + j];
+            if (f < 0) return -5;
+            C->col[3 * i + j] = f;
+            C->val[3 * i + j] = M->face_dist[f] * M->vert_face_dir[i * 3 + j] / M->vert_area[i];
+        }
+    }
+    C->rowptr[V] = 3 * V;
+    csr_finalise_rows(C);
     return 0;
 }
 
@@ -571,6 +639,7 @@ orc_mesh *orc_mesh_from_arrays(int N, const double *node_sph, const int *friends
     }
     int st = build_vertices(M);
     if (st == 0) st = assign_faces(M);
+    if (st == 0) st = build_vertex_geometry(M);
     if (st != 0) { if (status) *status = st; orc_mesh_free(M); return NULL; }
     build_operators(M);
     build_coriolis(M, 1.0, &M->C0);
@@ -897,6 +966,73 @@ void orc_interpolate_cartesian(const orc_mesh *M, double *uxyz, const double *vn
             uxyz[i * 3 + c] = u;
         }
     }
+}
+
+/* calculateMomentumAdvection, src/momAdvection.cpp:11-267: dvdt += PV flux - G KE.
+ * PV at vertices from the curl and the thickness interpolated with the kite
+ * fractions (Ringler et al. 2010 eq. 25), averaged to faces, TRiSK flux of the
+ * thickness flux h_e v_e with the mean PV (eq. 49); the kinetic energy from
+ * the RBF Cartesian velocity at the nodes.  ekin [N] receives the kinetic energy. */
+void orc_momentum_advection(const orc_mesh *M, double omega, double *dvdt, const double *vel, const double *h_total,
+                            double *ekin)
+{
+    int V = M->V, E = M->E, N = M->N;
+    double *qv = (double *)malloc(sizeof(double) * V);
+    double *qe = (double *)malloc(sizeof(double) * E);
+    double *he = (double *)malloc(sizeof(double) * E);
+    double *uxyz = (double *)malloc(sizeof(double) * N * 3);
+    double *gk = (double *)malloc(sizeof(double) * E);
+    csr_spmv(&M->Curl, vel, 1.0, qv);                                         /* step 1 */
+    for (int i = 0; i < V; i++) {                                              /* steps 2-3 */
+        double f = -2 * omega * sin(M->vert_sph[i * 2]);
+        double thickness = 0.0;
+        for (int j = 0; j < 3; j++) {
+            int n = M->vert_nodes[i * 3 + j];
+            thickness += h_total[n] * M->cv_area[n] * M->vert_R[i * 3 + j];
+        }
+        thickness *= 1.0 / M->vert_area[i];
+        qv[i] = (qv[i] + f) / thickness;
+    }
+    for (int i = 0; i < E; i++) {                                              /* steps 4-5 */
+        qe[i] = 0.5 * (qv[M->face_verts[i * 2]] + qv[M->face_verts[i * 2 + 1]]);
+        he[i] = 0.5 * (h_total[M->face_nodes[i * 2]] + h_total[M->face_nodes[i * 2 + 1]]);
+    }
+    for (int i = 0; i < E; i++) {                                              /* step 6 */
+        double F = 0.0, dr = 1.0 / M->face_dist[i];
+        for (int j = 0; j < M->interp_n[i]; j++) {
+            int f = M->interp_friends[i * 10 + j];
+            double coeff = M->interp_w[i * 10 + j] * M->face_len[f] * dr;
+            F += coeff * (he[f] * vel[f]) * (qe[i] + qe[f]) * 0.5;
+        }
+        dvdt[i] -= -F;
+    }
+    orc_interpolate_cartesian(M, uxyz, vel);                                   /* step 7 */
+    for (int i = 0; i < N; i++)
+        ekin[i] = 0.5 * (uxyz[i * 3] * uxyz[i * 3] + uxyz[i * 3 + 1] * uxyz[i * 3 + 1] + uxyz[i * 3 + 2] * uxyz[i * 3 + 2]);
+    csr_spmv(&M->G, ekin, 1.0, gk);                                            /* step 8 */
+    for (int i = 0; i < E; i++) dvdt[i] += -gk[i];
+    free(qv); free(qe); free(he); free(uxyz); free(gk);
+}
+
+/* vertex fields for checks: which = 0 area, 1..3 kite fractions R(v, j), 4 sin(lat) */
+int orc_mesh_vertex_field(const orc_mesh *M, int which, double *out)
+{
+    for (int i = 0; i < M->V; i++) {
+        if (which == 0) out[i] = M->vert_area[i];
+        else if (which >= 1 && which <= 3) out[i] = M->vert_R[i * 3 + which - 1];
+        else if (which == 4) out[i] = sin(M->vert_sph[i * 2]);
+        else return -1;
+    }
+    return M->V;
+}
+
+/* vertex topology: nodes [V][3], faces [V][3], face directions [V][3], face vertices [E][2] */
+void orc_mesh_vertex_topology(const orc_mesh *M, int *vert_nodes, int *vert_faces, int *vert_face_dir, int *face_verts)
+{
+    memcpy(vert_nodes, M->vert_nodes, sizeof(int) * M->V * 3);
+    memcpy(vert_faces, M->vert_faces, sizeof(int) * M->V * 3);
+    memcpy(vert_face_dir, M->vert_face_dir, sizeof(int) * M->V * 3);
+    memcpy(face_verts, M->face_verts, sizeof(int) * M->E * 2);
 }
 
 /* updateEnergy, LINEAR branch, src/energy.cpp:13-61 */

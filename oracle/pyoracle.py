@@ -60,6 +60,9 @@ def lib() -> C.CDLL:
             "orc_ab3": ([C.c_double, _D, _D, C.c_int, C.c_int, C.c_int], None),
             "orc_interpolate_velocity": ([_V, _D, _D], None),
             "orc_interpolate_cartesian": ([_V, _D, _D], None),
+            "orc_momentum_advection": ([_V, C.c_double, _D, _D, _D, _D], None),
+            "orc_mesh_vertex_field": ([_V, C.c_int, _D], C.c_int),
+            "orc_mesh_vertex_topology": ([_V, _I, _I, _I, _I], None),
             "orc_update_energy": ([_V, C.c_double, C.c_double, _D, _D], C.c_double),
             "orc_plmbar": ([C.c_int, C.c_double, _D], None),
             "orc_sh_basis": ([_V, C.c_int, _D], None),
@@ -119,6 +122,21 @@ class OracleMesh:
         inn = np.zeros(E, np.int32)
         lib().orc_mesh_get_topology(self._h, _ip(fn), _ip(faces), _ip(nfd), _ip(ifr), _dp(iw), _ip(inn))
         return dict(face_nodes=fn, faces=faces, node_face_dir=nfd, interp_friends=ifr, interp_w=iw, interp_n=inn)
+
+    def vertex_field(self, which: int) -> np.ndarray:
+        """0 vertex area, 1-3 kite fractions R(v, j) of the vertex's nodes, 4 sin(lat)."""
+        out = np.zeros(self.n_vertices)
+        lib().orc_mesh_vertex_field(self._h, which, _dp(out))
+        return out
+
+    def vertex_topology(self):
+        V, E = self.n_vertices, self.n_edges
+        vn = np.zeros((V, 3), np.int32)
+        vf = np.zeros((V, 3), np.int32)
+        vd = np.zeros((V, 3), np.int32)
+        fv = np.zeros((E, 2), np.int32)
+        lib().orc_mesh_vertex_topology(self._h, _ip(vn), _ip(vf), _ip(vd), _ip(fv))
+        return dict(vert_nodes=vn, vert_faces=vf, vert_face_dir=vd, face_verts=fv)
 
     def csr(self, op: int):
         """op 0 gradient (E x N), 1 divergence (N x E), 2 Coriolis with Omega = 1 (E x E)."""
@@ -180,6 +198,14 @@ class OracleSolver:
         out = np.zeros((self.N, 3))
         lib().orc_interpolate_cartesian(self.mesh._h, _dp(out), _dp(np.ascontiguousarray(v, np.float64)))
         return out
+
+    def calculateMomentumAdvection(self, dvdt, v, h_total):
+        """dvdt + PV flux - grad KE (src/momAdvection.cpp:11-267); returns (dvdt, ekin)."""
+        out = np.array(dvdt, np.float64, copy=True)
+        ekin = np.zeros(self.N)
+        lib().orc_momentum_advection(self.mesh._h, self.p.angvel, _dp(out), _dp(np.ascontiguousarray(v, np.float64)),
+                                     _dp(np.ascontiguousarray(h_total, np.float64)), _dp(ekin))
+        return out, ekin
 
     def updateEnergy(self, uv):
         e = np.zeros(self.E)

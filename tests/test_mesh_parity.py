@@ -17,6 +17,15 @@ def _compare(path):
     ta, tb = om.topology(), pm.topology()
     for k in ta:
         np.testing.assert_array_equal(ta[k], tb[k], err_msg=k)
+    # vertex geometry of the nonlinear terms; a face's two vertices are an
+    # unordered pair (the reference's order there depends on its face loop and
+    # enters no result)
+    for w in range(5):
+        np.testing.assert_array_equal(om.vertex_field(w), pm.vertex_field(w), err_msg=f"vertex field {w}")
+    va, vb = om.vertex_topology(), pm.vertex_topology()
+    for k in ("vert_nodes", "vert_faces", "vert_face_dir"):
+        np.testing.assert_array_equal(va[k], vb[k], err_msg=k)
+    np.testing.assert_array_equal(np.sort(va["face_verts"], axis=1), np.sort(vb["face_verts"], axis=1))
     return om, pm
 
 

@@ -176,3 +176,51 @@ def test_rbf_cartesian_reconstruction_converges(grid_dir):
         errs.append(np.max(np.abs(u - exact)) / np.max(np.abs(exact)))
     assert errs[0] < 0.04 and errs[1] < 0.012 and errs[2] < 0.004
     assert errs[0] > errs[1] > errs[2]
+
+
+def _zonal_face_velocity(om, u0):
+    """Normal components of the zonal solid-body flow u0 cos(lat) east at the face centres."""
+    def xyz(lat, lon):
+        return np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], -1)
+    fl, fo = om.field(4), om.field(5)
+    nx, ny = om.field(8), om.field(9)
+    east = np.stack([-np.sin(fo), np.cos(fo), 0 * fo], -1)
+    north = np.stack([-np.sin(fl) * np.cos(fo), -np.sin(fl) * np.sin(fo), np.cos(fl)], -1)
+    n = nx[:, None] * east + ny[:, None] * north
+    return u0 * np.sum(n * np.cross([0.0, 0.0, 1.0], xyz(fl, fo)), axis=1)
+
+
+@pytest.mark.parametrize("level", [2, 3])
+def test_pv_flux_does_no_work(grid_dir, level):
+    """The TRiSK potential-vorticity flux of calculateMomentumAdvection is energetically neutral:
+    sum_e l_e d_e h_e v_e (PV flux)_e vanishes to rounding for any v and thickness (antisymmetric weights)."""
+    from oracle import pyoracle as O
+    om = O.OracleMesh(grid_dir / f"grid_{level}.txt", RADIUS)
+    orc = O.OracleSolver(om, radius=RADIUS, g=0.113, angvel=5.307e-5, h=1e4, alpha=1e-5, dt=10.0)
+    rng = np.random.default_rng(level)
+    v = rng.standard_normal(om.n_edges)
+    ht = 1e4 + 10 * rng.standard_normal(om.n_cells)
+    dv, ek = orc.calculateMomentumAdvection(np.zeros(om.n_edges), v, ht)
+    pv = dv + spmv(om.csr(0), ek)                       # remove -G KE
+    fn = om.topology()["face_nodes"]
+    he = 0.5 * (ht[fn[:, 0]] + ht[fn[:, 1]])
+    terms = om.field(0) * om.field(1) * he * v * pv
+    assert abs(terms.sum()) < 1e-10 * np.abs(terms).sum()
+    assert np.all(ek >= 0) and np.abs(pv).max() > 0
+
+
+def test_pv_flux_reduces_to_coriolis(grid_dir):
+    """At rest thickness and vanishing relative vorticity, q = f / h and the PV flux is the Coriolis term:
+    it converges to the linear operator (src/mesh.cpp:2808-2901) at second order with level."""
+    from oracle import pyoracle as O
+    errs = []
+    for lv in (2, 3, 4):
+        om = O.OracleMesh(grid_dir / f"grid_{lv}.txt", RADIUS)
+        orc = O.OracleSolver(om, radius=RADIUS, g=0.113, angvel=5.307e-5, h=1e4, alpha=1e-5, dt=10.0)
+        v = _zonal_face_velocity(om, 1e-6)
+        dv, ek = orc.calculateMomentumAdvection(np.zeros(om.n_edges), v, np.full(om.n_cells, 1e4))
+        pv = dv + spmv(om.csr(0), ek)
+        cv = 5.307e-5 * spmv(om.csr(2), v)
+        errs.append(np.abs(pv - cv).max() / np.abs(cv).max())
+    assert errs[0] < 0.04 and errs[2] < 0.005
+    assert errs[0] / errs[1] > 3 and errs[1] / errs[2] > 1.8
