@@ -95,6 +95,7 @@ _SIGS = {
     "odis_interpolate_velocity": ([_V, _V, _V, C.c_int], C.c_int),
     "odis_interpolate_cartesian": ([_V, _V, _V, C.c_int], C.c_int),
     "odis_momentum_advection": ([_V, _V, _V, _V, _V, _V, C.c_int], C.c_int),
+    "odis_lsq_flux": ([_V, _V, _V, _V, _V, C.c_int], C.c_int),
     "odis_update_energy": ([_V, _V, _V, _V, C.c_int], C.c_int),
     "odis_run_steps": ([_V, C.c_int, _V, C.c_int], C.c_int),
     "odis_get_state": ([_V, _I, _D, _D, _D, _D], C.c_int),
@@ -330,6 +331,14 @@ class Solver:
         _ck(lib().odis_momentum_advection(self._h, self.mesh._h, _vp(out), _vp(v), _vp(h), _vp(ekin), MEM_HOST),
             "odis_momentum_advection")
         return out, ekin
+
+    def interpolateLSQFlux(self, v: np.ndarray, h_total: np.ndarray) -> np.ndarray:
+        """Third-order thickness flux across the faces: the reference's interpolateLSQFlux."""
+        out = np.zeros(self.E)
+        v = np.ascontiguousarray(v, np.float64)
+        h = np.ascontiguousarray(h_total, np.float64)
+        _ck(lib().odis_lsq_flux(self._h, self.mesh._h, _vp(out), _vp(v), _vp(h), MEM_HOST), "odis_lsq_flux")
+        return out
 
     def updateEnergy(self, uv: np.ndarray):
         """(area-mean dissipation W/m^2, per-face dissipation)."""

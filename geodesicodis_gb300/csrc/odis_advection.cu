@@ -88,6 +88,32 @@ __global__ void k_adv_flux(const int* __restrict__ fr, const double* __restrict_
     dvdt[e] = d;
 }
 
+// interpolateLSQFlux (src/interpolation.cpp:311-356), beta = 1: the directional
+// second derivatives at the face's two nodes (7-term rows, ascending node
+// order), then the third-order upwind-biased thickness flux.  Products and sums
+// are rounded separately, as in the unfused FP64 restatement.
+__global__ void k_lsq_flux(const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ dist,
+                           const int* __restrict__ fnode, int E, int Ep, const double* __restrict__ v,
+                           const double* __restrict__ h, double* __restrict__ flux)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const size_t R = (size_t)2 * Ep;
+    double d2i = 0.0, d2o = 0.0;
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+        d2i = __dadd_rn(d2i, __dmul_rn(val[j * R + 2 * e], h[col[j * R + 2 * e]]));
+        d2o = __dadd_rn(d2o, __dmul_rn(val[j * R + 2 * e + 1], h[col[j * R + 2 * e + 1]]));
+    }
+    const double dx = dist[e];
+    const double dx2 = __dmul_rn(__dmul_rn(dx, dx), 1. / 12.0);
+    const double vel = v[e];
+    const double a = __dmul_rn(__dmul_rn(vel, 0.5), __dadd_rn(h[fnode[e]], h[fnode[Ep + e]]));
+    const double b = __dmul_rn(__dmul_rn(dx2, __dadd_rn(d2o, d2i)), vel);
+    const double c = __dmul_rn(__dmul_rn(__dmul_rn(dx2, 1.0), fabs(vel)), __dsub_rn(d2o, d2i));
+    flux[e] = __dadd_rn(__dsub_rn(a, b), c);
+}
+
 template <class T>
 T* upload(const std::vector<T>& h)
 {
@@ -109,6 +135,8 @@ struct AdvDev {
     double *vcoef = nullptr, *vR = nullptr, *vinv = nullptr, *vf = nullptr, *cvA = nullptr, *cw = nullptr,
            *gval = nullptr;
     double *q = nullptr, *qe = nullptr, *he = nullptr, *uxyz = nullptr, *ek = nullptr;
+    int* lcol = nullptr;         // [7][2 Ep] operatorDirectionalSecondDeriv rows
+    double *lval = nullptr, *dist = nullptr;
 };
 
 void adv_destroy(AdvDev* a)
@@ -117,7 +145,7 @@ void adv_destroy(AdvDev* a)
     for (void* p : {(void*)a->vface, (void*)a->vnode, (void*)a->fvert, (void*)a->fnode, (void*)a->fr, (void*)a->nfr,
                     (void*)a->gcol, (void*)a->vcoef, (void*)a->vR, (void*)a->vinv, (void*)a->vf, (void*)a->cvA,
                     (void*)a->cw, (void*)a->gval, (void*)a->q, (void*)a->qe, (void*)a->he, (void*)a->uxyz,
-                    (void*)a->ek})
+                    (void*)a->ek, (void*)a->lcol, (void*)a->lval, (void*)a->dist})
         cudaFree(p);
     delete a;
 }
@@ -172,6 +200,24 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
         gcol[(size_t)Ep + e] = sw ? n0 : n1;
         gval[(size_t)Ep + e] = sw ? g0 : g1;
     }
+    {
+        std::vector<int> rc;
+        std::vector<double> rv;
+        const int st = build_lsq_rows(m, kRbfEps, rc, rv);
+        if (st != ODIS_OK) { adv_destroy(a); return st; }
+        std::vector<int> lc((size_t)7 * 2 * Ep, 0);
+        std::vector<double> lv((size_t)7 * 2 * Ep, 0.0), dist(Ep, 1.0);
+        for (int row = 0; row < 2 * E; row++)
+            for (int j = 0; j < 7; j++) {
+                lc[(size_t)j * 2 * Ep + row] = rc[(size_t)row * 7 + j];
+                lv[(size_t)j * 2 * Ep + row] = rv[(size_t)row * 7 + j];
+            }
+        for (int e = 0; e < E; e++) dist[e] = m.face_dist[e];
+        a->lcol = upload(lc);
+        a->lval = upload(lv);
+        a->dist = upload(dist);
+        if (!a->lcol || !a->lval || !a->dist) { adv_destroy(a); return ODIS_ERR_NOMEM; }
+    }
     a->vface = upload(vface); a->vnode = upload(vnode); a->vcoef = upload(vcoef); a->vR = upload(vR);
     a->vinv = upload(vinv); a->vf = upload(vf); a->cvA = upload(cvA);
     a->fvert = upload(fvert); a->fnode = upload(fnode); a->fr = upload(fr); a->nfr = upload(nfr);
@@ -203,5 +249,11 @@ void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dv
 }
 
 int adv_kernels_per_call() { return 5; }
+
+void adv_lsq_flux(AdvDev* a, double* flux, const double* v, const double* h_total, cudaStream_t s)
+{
+    k_lsq_flux<<<(a->E + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->lcol, a->lval, a->dist, a->fnode, a->E,
+                                                                             a->Ep, v, h_total, flux);
+}
 
 }  // namespace odis

@@ -17,6 +17,8 @@ void adv_destroy(AdvDev* a);
 void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dvdt, const double* v,
                   const double* h_total, double* ekin, cudaStream_t s);
 double* adv_ekin_scratch(AdvDev* a);
+// flux[E]: the reference's interpolateLSQFlux of the column thickness h_total[N] with velocities v[E]
+void adv_lsq_flux(AdvDev* a, double* flux, const double* v, const double* h_total, cudaStream_t s);
 int adv_kernels_per_call();
 
 }  // namespace odis

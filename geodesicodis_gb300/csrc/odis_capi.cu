@@ -767,6 +767,26 @@ extern "C" odis_status odis_momentum_advection(odis_ctx* c, const odis_mesh* mes
     return st != ODIS_OK ? st : io.done();
 }
 
+extern "C" odis_status odis_lsq_flux(odis_ctx* c, const odis_mesh* mesh, double* flux, const double* v,
+                                     const double* h_total, int mem)
+{
+    if (!c || !flux || !v || !h_total || !mem_ok(mem)) return ODIS_ERR_ARG;
+    if (!c->adv) {
+        if (!mesh || mesh->m.N != c->N || mesh->m.E != c->E) return ODIS_ERR_ARG;
+        const int st = adv_create(&c->adv, mesh->m, c->p.angvel, c->Ep, c->Np);
+        if (st != ODIS_OK) return st;
+    }
+    Io io{c, mem};
+    const double* dv = io.in(v, c->E);
+    const double* dh = io.in(h_total, c->N);
+    double* dout = io.out(flux);
+    if (!dv || !dh) return ODIS_ERR_CUDA;
+    adv_lsq_flux(c->adv, dout, dv, dh, c->stream);
+    c->launches += 1;
+    int st = io.back(flux, dout, c->E);
+    return st != ODIS_OK ? st : io.done();
+}
+
 extern "C" odis_status odis_update_eta(odis_ctx* c, double* detadt, const double* v, int mem)
 {
     if (!c || !detadt || !v || !mem_ok(mem)) return ODIS_ERR_ARG;

@@ -65,6 +65,13 @@ int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, 
 // velocities: rbf[(i * 3 + c) * 6 + j] multiplies v at faces(i, j).
 void build_rbf(const Mesh& m, std::vector<double>& rbf);
 
+// operatorDirectionalSecondDeriv (src/mesh.cpp:2364-2716) as rows of 7 (node,
+// coefficient) pairs, ascending node order, padded with zero coefficients:
+// row 2e is the inner node's second derivative normal to face e, 2e+1 the
+// outer node's.  eps is the Gaussian RBF shape parameter ("rbf epsilon").
+int build_lsq_rows(const Mesh& m, double eps, std::vector<int>& col, std::vector<double>& val);
+constexpr double kRbfEps = 0.25;     // the reference's default "rbf epsilon" (src/globals.cpp:570)
+
 // sqrt(largest eigenvalue of -g h D G), power iteration
 double gravity_wave_omega(const Mesh& m, double g, double h, int iters);
 

@@ -586,4 +586,152 @@ int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, 
     return ODIS_OK;
 }
 
+// Gaussian RBF of include/mathRoutines.h:432-439
+static double rbf_gauss(double dist, double eps)
+{
+    double phi = std::exp(-std::pow(eps * dist, 2.0));
+    if (dist < 1e-8) phi = 1;
+    return phi;
+}
+
+// In-place inverse of an n x n row-major matrix (n <= 7): Gauss-Jordan
+// elimination with partial pivoting.  The oracle inverts with the same steps,
+// so the two agree bit for bit.
+static bool gj_inverse(int n, double* a)
+{
+    double b[7 * 7];
+    for (int i = 0; i < n * n; i++) b[i] = 0.0;
+    for (int i = 0; i < n; i++) b[i * n + i] = 1.0;
+    for (int c = 0; c < n; c++) {
+        int piv = c;
+        for (int r = c + 1; r < n; r++)
+            if (std::fabs(a[r * n + c]) > std::fabs(a[piv * n + c])) piv = r;
+        if (a[piv * n + c] == 0.0) return false;
+        if (piv != c)
+            for (int q = 0; q < n; q++) {
+                std::swap(a[c * n + q], a[piv * n + q]);
+                std::swap(b[c * n + q], b[piv * n + q]);
+            }
+        const double d = a[c * n + c];
+        for (int q = 0; q < n; q++) { a[c * n + q] /= d; b[c * n + q] /= d; }
+        for (int r = 0; r < n; r++) {
+            if (r == c) continue;
+            const double f = a[r * n + c];
+            if (f == 0.0) continue;
+            for (int q = 0; q < n; q++) { a[r * n + q] -= f * a[c * n + q]; b[r * n + q] -= f * b[c * n + q]; }
+        }
+    }
+    for (int i = 0; i < n * n; i++) a[i] = b[i];
+    return true;
+}
+
+int build_lsq_rows(const Mesh& m, double eps, std::vector<int>& col, std::vector<double>& val)
+{
+    const int N = m.N, E = m.E;
+    const double r = m.r, r_recip = 1.0 / m.r;
+    std::vector<double> S((size_t)N * 3 * 7, 0.0);
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+    for (int i = 0; i < N; i++) {
+        const int k = m.nfriends(i), K = k + 1;
+        const LL c0{m.node_sph[i * 2], m.node_sph[i * 2 + 1]};
+        double px[7], py[7];
+        for (int j = 0; j < K; j++) {              // node-centred map coordinates (src/mesh.cpp:1384-1450)
+            const int f = j == 0 ? i : m.friends[i * 6 + j - 1];
+            double mm;
+            stereo(c0, LL{m.node_sph[f * 2], m.node_sph[f * 2 + 1]}, r, mm, px[j], py[j]);
+        }
+        double A[7 * 7], nnr[7] = {0, 0, 0, 0, 0, 0, 0};
+        A[0] = 1.0;
+        for (int j1 = 0; j1 < k; j1++) {           // src/mesh.cpp:286-345
+            const double x1 = px[j1 + 1] / r, y1 = py[j1 + 1] / r;
+            const double arc = std::sqrt(x1 * x1 + y1 * y1);
+            A[0 * K + j1 + 1] = rbf_gauss(arc, eps);
+        }
+        for (int j1 = 0; j1 < k; j1++) {
+            const double x1 = px[j1 + 1] / r, y1 = py[j1 + 1] / r;
+            double arc = std::sqrt(x1 * x1 + y1 * y1);
+            A[(j1 + 1) * K + 0] = rbf_gauss(arc, eps);
+            nnr[j1 + 1] = rbf_gauss(arc, eps);
+            for (int j2 = 0; j2 < k; j2++) {
+                const double x2 = px[j2 + 1] / r, y2 = py[j2 + 1] / r;
+                arc = std::sqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));
+                A[(j1 + 1) * K + j2 + 1] = rbf_gauss(arc, eps);
+            }
+        }
+        if (!gj_inverse(K, A)) { bad++; continue; }
+        double D[3][7];                            // rbfDeriv2, src/mesh.cpp:2472-2548
+        for (int c = 0; c < 3; c++)
+            for (int j = 0; j < K; j++) D[c][j] = 0.0;
+        D[0][0] = -2.0 * eps * eps;
+        D[2][0] = -2.0 * eps * eps;
+        for (int j = 0; j < k; j++) {
+            const double x1 = px[j + 1] * r_recip, y1 = py[j + 1] * r_recip;
+            const double arc = std::sqrt(x1 * x1 + y1 * y1);
+            const double xx = x1 * x1, yy = y1 * y1, xy = x1 * y1;
+            const double arc2 = 1.0 / (arc * arc), arc3 = 1.0 / (arc * arc * arc);
+            const double rbf = nnr[j + 1];
+            const double d2phidr2 = 2 * eps * eps * rbf * (2 * arc * arc * eps * eps - 1);
+            const double dphidr = -2 * arc * eps * eps * rbf;
+            D[0][j + 1] = (yy * arc3 * dphidr + xx * arc2 * d2phidr2);
+            D[1][j + 1] = (-xy * arc3 * dphidr + xy * arc2 * d2phidr2);
+            D[2][j + 1] = (xx * arc3 * dphidr + yy * arc2 * d2phidr2);
+        }
+        const double sc = r_recip * r_recip;
+        for (int c = 0; c < 3; c++)
+            for (int j = 0; j < K; j++) {
+                double t = 0.0;
+                for (int q = (c == 1 ? 1 : 0); q < K; q++) t += (sc * D[c][q]) * A[q * K + j];
+                S[((size_t)i * 3 + c) * 7 + j] = t;
+            }
+    }
+    if (bad) return ODIS_ERR_MESH;
+    col.assign((size_t)2 * E * 7, 0);
+    val.assign((size_t)2 * E * 7, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < E; e++)
+        for (int side = 0; side < 2; side++) {
+            const int n = m.face_nodes[e * 2 + side];
+            const int k = m.nfriends(n), K = k + 1;
+            double ca, sa;                         // velTransform, include/mathRoutines.h:79-87
+            {
+                const double lat1 = m.face_int[e * 2], lon1 = m.face_int[e * 2 + 1];
+                const double lat2 = m.node_sph[n * 2], lon2 = m.node_sph[n * 2 + 1];
+                ca = std::cos(lat1) * std::cos(lat2);
+                ca += (1.0 + std::sin(lat1) * std::sin(lat2)) * std::cos(lon2 - lon1);
+                ca /= (1.0 + std::sin(lat1) * std::sin(lat2) + std::cos(lat1) * std::cos(lat2) * std::cos(lon2 - lon1));
+                sa = -(std::sin(lat1) + std::sin(lat2)) * std::sin(lon2 - lon1);
+                sa /= (1.0 + std::sin(lat1) * std::sin(lat2) + std::cos(lat1) * std::cos(lat2) * std::cos(lon2 - lon1));
+            }
+            const double R[3][3] = {{ca * ca, -2 * ca * sa, sa * sa},
+                                    {ca * sa, ca * ca - sa * sa, -sa * ca},
+                                    {sa * sa, 2 * ca * sa, ca * ca}};
+            const double nx = m.face_normal[e * 2], ny = m.face_normal[e * 2 + 1];
+            const double Nv[3] = {nx * nx, 2 * nx * ny, ny * ny};
+            double NR[3];
+            for (int c = 0; c < 3; c++) {
+                double t = 0.0;
+                for (int q = 0; q < 3; q++) t += Nv[q] * R[q][c];
+                NR[c] = t;
+            }
+            int cc[7];
+            double vv[7];
+            for (int j = 0; j < K; j++) {
+                double t = 0.0;
+                for (int c = 0; c < 3; c++) t += NR[c] * S[((size_t)n * 3 + c) * 7 + j];
+                cc[j] = j == 0 ? n : m.friends[n * 6 + j - 1];
+                vv[j] = t;
+            }
+            int idx[7] = {0, 1, 2, 3, 4, 5, 6};
+            std::sort(idx, idx + K, [&](int a, int b) { return cc[a] < cc[b]; });
+            const size_t row = (size_t)(2 * e + side) * 7;
+            for (int j = 0; j < 7; j++) {
+                col[row + j] = j < K ? cc[idx[j]] : cc[idx[K - 1]];
+                val[row + j] = j < K ? vv[idx[j]] : 0.0;
+            }
+        }
+    return ODIS_OK;
+}
+
 }  // namespace odis
+

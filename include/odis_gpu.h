@@ -16,6 +16,8 @@
  *   odis_update_energy     <- updateEnergy        include/energy.h:10,          src/energy.cpp:13-61
  *   odis_momentum_advection <- calculateMomentumAdvection src/momAdvection.cpp:11-267 (updateMomentum's
  *                             advection branch, src/updateMomentum.cpp:35-39)
+ *   odis_lsq_flux          <- interpolateLSQFlux  src/interpolation.cpp:311-356 (updateEta's advection
+ *                             branch, src/updateEta.cpp:22-32)
  *   odis_run_steps         <- the body of ab3Explicit's time loop, src/timeIntegrator.cpp:205-313
  *   odis_get_state / odis_set_state <- writeInitialConditions / loadInitialConditions,
  *                                      src/initialConditions.cpp:19,209
@@ -194,6 +196,15 @@ odis_status odis_interpolate_cartesian(odis_ctx* c, double* uxyz, const double* 
  * call builds the vertex operators from it. */
 odis_status odis_momentum_advection(odis_ctx* c, const odis_mesh* mesh, double* dvdt, const double* v,
                                     const double* h_total, double* ekin, int mem);
+/* interpolateLSQFlux (include/interpolation.h:18, src/interpolation.cpp:311-356),
+ * third order (beta = 1): flux[E] of the node scalar h_total[N] across each
+ * face with velocity v[E], from the Gaussian-RBF directional second
+ * derivatives at the face's two nodes (operatorDirectionalSecondDeriv,
+ * src/mesh.cpp:2364-2716, shape parameter 0.25).  The advective continuity
+ * equation takes the divergence of this flux.  `mesh` as for
+ * odis_momentum_advection. */
+odis_status odis_lsq_flux(odis_ctx* c, const odis_mesh* mesh, double* flux, const double* v, const double* h_total,
+                          int mem);
 /* e[E] (nullable) per-face dissipation and *avg area-mean (W m^-2) from uv[E][2] */
 odis_status odis_update_energy(odis_ctx* c, double* avg, double* e, const double* uv, int mem);
 

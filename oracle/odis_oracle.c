@@ -266,6 +266,7 @@ typedef struct {
     int *vert_face_dir;   /* [V][3] */
     double *vert_area;    /* [V] */
     orc_csr Curl;         /* V x E, operatorCurl */
+    orc_csr D2;           /* 2E x N, operatorDirectionalSecondDeriv (built on first use) */
     orc_csr G, D, C0;     /* gradient (E x N), divergence (N x E), Coriolis without Omega factor is not kept: C0 = Coriolis with Omega=1 */
 } orc_mesh;
 
@@ -280,7 +281,7 @@ void orc_mesh_free(orc_mesh *M)
     free(M->face_m); free(M->face_normal); free(M->face_int); free(M->face_nxyz); free(M->interp_friends); free(M->interp_w);
     free(M->interp_n); free(M->trig);
     free(M->face_verts); free(M->vert_R); free(M->vert_faces); free(M->vert_face_dir); free(M->vert_area);
-    csr_free(&M->G); csr_free(&M->D); csr_free(&M->C0); csr_free(&M->Curl);
+    csr_free(&M->G); csr_free(&M->D); csr_free(&M->C0); csr_free(&M->Curl); csr_free(&M->D2);
     free(M);
 }
 
@@ -1012,6 +1013,175 @@ void orc_momentum_advection(const orc_mesh *M, double omega, double *dvdt, const
     csr_spmv(&M->G, ekin, 1.0, gk);                                            /* step 8 */
     for (int i = 0; i < E; i++) dvdt[i] += -gk[i];
     free(qv); free(qe); free(he); free(uxyz); free(gk);
+}
+
+/* RBF(dist, eps), include/mathRoutines.h:432-439 */
+static double rbf_gauss(double dist, double eps)
+{
+    double phi = exp(-pow(eps * dist, 2.0));
+    if (dist < 1e-8) phi = 1;
+    return phi;
+}
+
+/* In-place inverse of the n x n row-major matrix a (n <= 7) by Gauss-Jordan
+ * elimination with partial pivoting; 0 on success. */
+static int gj_inverse(int n, double *a)
+{
+    double b[7 * 7];
+    for (int i = 0; i < n * n; i++) b[i] = 0.0;
+    for (int i = 0; i < n; i++) b[i * n + i] = 1.0;
+    for (int c = 0; c < n; c++) {
+        int piv = c;
+        for (int r = c + 1; r < n; r++) if (fabs(a[r * n + c]) > fabs(a[piv * n + c])) piv = r;
+        if (a[piv * n + c] == 0.0) return -1;
+        if (piv != c)
+            for (int q = 0; q < n; q++) {
+                double t = a[c * n + q]; a[c * n + q] = a[piv * n + q]; a[piv * n + q] = t;
+                t = b[c * n + q]; b[c * n + q] = b[piv * n + q]; b[piv * n + q] = t;
+            }
+        double d = a[c * n + c];
+        for (int q = 0; q < n; q++) { a[c * n + q] /= d; b[c * n + q] /= d; }
+        for (int r = 0; r < n; r++) {
+            if (r == c) continue;
+            double f = a[r * n + c];
+            if (f == 0.0) continue;
+            for (int q = 0; q < n; q++) { a[r * n + q] -= f * a[c * n + q]; b[r * n + q] -= f * b[c * n + q]; }
+        }
+    }
+    for (int i = 0; i < n * n; i++) a[i] = b[i];
+    return 0;
+}
+
+/* operatorDirectionalSecondDeriv = N R operatorSecondDeriv (src/mesh.cpp:2364-2716):
+ * per node, the second derivatives (xx, xy, yy) of the Gaussian-RBF interpolant
+ * over the node and its friends in node-centred map coordinates
+ * (CalcControlVolumeInterpMatrix, :199-360, inverted as in :2413-2440), rotated
+ * into each face's frame (face_node_vel_trans, :1222-1383) and projected on the
+ * face normal.  Rows 2e (inner node) and 2e+1 (outer node). */
+static int build_lsq(orc_mesh *M, double eps)
+{
+    int N = M->N, E = M->E;
+    double r = M->r, r_recip = 1.0 / M->r;
+    double *S = (double *)calloc((size_t)N * 3 * 7, sizeof(double));       /* [N][3][7] */
+    for (int i = 0; i < N; i++) {
+        int k = nfriends(M, i), K = k + 1;
+        double lat1 = M->node_sph[i * 2], lon1 = M->node_sph[i * 2 + 1];
+        double px[7], py[7];
+        for (int j = 0; j < K; j++) {                /* node_pos_map(i, j), CalcMappingCoords :1384-1450 */
+            double m, x, y;
+            int f = j == 0 ? i : M->friends[i * 6 + j - 1];
+            map_at_point(&m, &x, &y, lat1, M->node_sph[f * 2], lon1, M->node_sph[f * 2 + 1], r);
+            px[j] = x; py[j] = y;
+        }
+        double A[7 * 7], nnr[7];
+        A[0] = 1.0;
+        for (int j1 = 0; j1 < k; j1++) {
+            double x1 = px[j1 + 1] / r, y1 = py[j1 + 1] / r;
+            double arc = sqrt(x1 * x1 + y1 * y1);
+            A[0 * K + j1 + 1] = rbf_gauss(arc, eps);
+        }
+        for (int j1 = 0; j1 < k; j1++) {
+            double x1 = px[j1 + 1] / r, y1 = py[j1 + 1] / r;
+            double arc = sqrt(x1 * x1 + y1 * y1);
+            A[(j1 + 1) * K + 0] = rbf_gauss(arc, eps);
+            nnr[j1 + 1] = rbf_gauss(arc, eps);
+            for (int j2 = 0; j2 < k; j2++) {
+                double x2 = px[j2 + 1] / r, y2 = py[j2 + 1] / r;
+                arc = sqrt((x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2));
+                A[(j1 + 1) * K + j2 + 1] = rbf_gauss(arc, eps);
+            }
+        }
+        if (gj_inverse(K, A) != 0) { free(S); return -6; }
+        /* rbfDeriv2 rows (:2472-2548), scaled by r_recip^2 */
+        double D[3][7];
+        for (int c = 0; c < 3; c++) for (int j = 0; j < K; j++) D[c][j] = 0.0;
+        D[0][0] = -2.0 * eps * eps;
+        D[2][0] = -2.0 * eps * eps;
+        for (int j = 0; j < k; j++) {
+            double x1 = px[j + 1] * r_recip, y1 = py[j + 1] * r_recip;
+            double arc = sqrt(x1 * x1 + y1 * y1);
+            double xx = x1 * x1, yy = y1 * y1, xy = x1 * y1;
+            double arc2 = 1.0 / (arc * arc), arc3 = 1.0 / (arc * arc * arc);
+            double rbf = nnr[j + 1];
+            double d2phidr2 = 2 * eps * eps * rbf * (2 * arc * arc * eps * eps - 1);
+            double dphidr = -2 * arc * eps * eps * rbf;
+            D[0][j + 1] = (yy * arc3 * dphidr + xx * arc2 * d2phidr2);
+            D[1][j + 1] = (-xy * arc3 * dphidr + xy * arc2 * d2phidr2);
+            D[2][j + 1] = (xx * arc3 * dphidr + yy * arc2 * d2phidr2);
+        }
+        double sc = r_recip * r_recip;
+        for (int c = 0; c < 3; c++)
+            for (int j = 0; j < K; j++) {
+                double t = 0.0;
+                for (int q = (c == 1 ? 1 : 0); q < K; q++) t += (sc * D[c][q]) * A[q * K + j];
+                S[((size_t)i * 3 + c) * 7 + j] = t;
+            }
+    }
+    orc_csr *C = &M->D2;
+    C->rows = 2 * E; C->cols = N;
+    C->rowptr = (int *)malloc(sizeof(int) * (2 * E + 1));
+    C->col = (int *)malloc(sizeof(int) * 14 * E);
+    C->val = (double *)malloc(sizeof(double) * 14 * E);
+    int nz = 0;
+    for (int e = 0; e < E; e++)
+        for (int side = 0; side < 2; side++) {
+            int n = M->face_nodes[e * 2 + side];
+            int k = nfriends(M, n), K = k + 1;
+            double ca, sa;                            /* velTransform, include/mathRoutines.h:79-87 */
+            {
+                double lat1 = M->face_int[e * 2], lon1 = M->face_int[e * 2 + 1];
+                double lat2 = M->node_sph[n * 2], lon2 = M->node_sph[n * 2 + 1];
+                ca = cos(lat1) * cos(lat2);
+                ca += (1.0 + sin(lat1) * sin(lat2)) * cos(lon2 - lon1);
+                ca /= (1.0 + sin(lat1) * sin(lat2) + cos(lat1) * cos(lat2) * cos(lon2 - lon1));
+                sa = -(sin(lat1) + sin(lat2)) * sin(lon2 - lon1);
+                sa /= (1.0 + sin(lat1) * sin(lat2) + cos(lat1) * cos(lat2) * cos(lon2 - lon1));
+            }
+            double R[3][3] = {{ca * ca, -2 * ca * sa, sa * sa},
+                              {ca * sa, ca * ca - sa * sa, -sa * ca},
+                              {sa * sa, 2 * ca * sa, ca * ca}};
+            double nx = M->face_normal[e * 2], ny = M->face_normal[e * 2 + 1];
+            double Nv[3] = {nx * nx, 2 * nx * ny, ny * ny};
+            double NR[3];
+            for (int c = 0; c < 3; c++) {
+                double t = 0.0;
+                for (int q = 0; q < 3; q++) t += Nv[q] * R[q][c];
+                NR[c] = t;
+            }
+            C->rowptr[2 * e + side] = nz;
+            for (int j = 0; j < K; j++) {
+                double t = 0.0;
+                for (int c = 0; c < 3; c++) t += NR[c] * S[((size_t)n * 3 + c) * 7 + j];
+                C->col[nz] = j == 0 ? n : M->friends[n * 6 + j - 1];
+                C->val[nz] = t;
+                nz++;
+            }
+        }
+    C->rowptr[2 * E] = nz;
+    csr_finalise_rows(C);
+    free(S);
+    return 0;
+}
+
+/* interpolateLSQFlux, src/interpolation.cpp:311-356 (beta = 1, third order):
+ * flux_e = v (h_in + h_out) / 2 - dx^2/12 (d2_out + d2_in) v + dx^2/12 |v| (d2_out - d2_in) */
+int orc_lsq_flux(orc_mesh *M, double eps, double *flux, const double *vel, const double *h)
+{
+    if (!M->D2.rowptr) { int st = build_lsq(M, eps); if (st) return st; }
+    int E = M->E;
+    double *d2 = (double *)malloc(sizeof(double) * 2 * E);
+    csr_spmv(&M->D2, h, 1.0, d2);
+    double fact = 1. / 12.0, beta = 1.0;
+    for (int i = 0; i < E; i++) {
+        double dx = M->face_dist[i];
+        double dx2 = dx * dx * fact;
+        double v = vel[i];
+        int in = M->face_nodes[i * 2], out = M->face_nodes[i * 2 + 1];
+        double d2o = d2[2 * i + 1], d2i = d2[2 * i];
+        flux[i] = v * 0.5 * (h[in] + h[out]) - dx2 * (d2o + d2i) * v + dx2 * beta * fabs(v) * (d2o - d2i);
+    }
+    free(d2);
+    return 0;
 }
 
 /* vertex fields for checks: which = 0 area, 1..3 kite fractions R(v, j), 4 sin(lat) */

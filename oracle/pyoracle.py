@@ -61,6 +61,7 @@ def lib() -> C.CDLL:
             "orc_interpolate_velocity": ([_V, _D, _D], None),
             "orc_interpolate_cartesian": ([_V, _D, _D], None),
             "orc_momentum_advection": ([_V, C.c_double, _D, _D, _D, _D], None),
+            "orc_lsq_flux": ([_V, C.c_double, _D, _D, _D], C.c_int),
             "orc_mesh_vertex_field": ([_V, C.c_int, _D], C.c_int),
             "orc_mesh_vertex_topology": ([_V, _I, _I, _I, _I], None),
             "orc_update_energy": ([_V, C.c_double, C.c_double, _D, _D], C.c_double),
@@ -206,6 +207,15 @@ class OracleSolver:
         lib().orc_momentum_advection(self.mesh._h, self.p.angvel, _dp(out), _dp(np.ascontiguousarray(v, np.float64)),
                                      _dp(np.ascontiguousarray(h_total, np.float64)), _dp(ekin))
         return out, ekin
+
+    def interpolateLSQFlux(self, v, h_total, eps=0.25):
+        """Third-order thickness flux across the faces (src/interpolation.cpp:311-356)."""
+        out = np.zeros(self.E)
+        st = lib().orc_lsq_flux(self.mesh._h, eps, _dp(out), _dp(np.ascontiguousarray(v, np.float64)),
+                                _dp(np.ascontiguousarray(h_total, np.float64)))
+        if st != 0:
+            raise RuntimeError(f"oracle LSQ operator failed: {st}")
+        return out
 
     def updateEnergy(self, uv):
         e = np.zeros(self.E)

@@ -89,6 +89,18 @@ def test_momentum_advection(grid_dir, level):
     assert rel_err(dg + spmv(G, kg) - d0, do + spmv(G, ko) - d0) < 1e-12
 
 
+@pytest.mark.parametrize("level", [2, 3, 4])
+def test_lsq_flux(grid_dir, level):
+    """interpolateLSQFlux (src/interpolation.cpp:311-356): the device flux against the oracle.  Both build
+    the second-derivative rows with the same host arithmetic, and the kernel rounds every product and sum
+    separately, so the two agree to the last bits."""
+    orc, gpu = _pair(grid_dir / f"grid_{level}.txt")
+    rng = np.random.default_rng(20 + level)
+    v = rng.standard_normal(orc.E)
+    ht = 1e4 + 10 * rng.standard_normal(orc.N)
+    assert rel_err(gpu.interpolateLSQFlux(v, ht), orc.interpolateLSQFlux(v, ht)) < 1e-13
+
+
 def test_interpolate_and_energy(level3):
     orc, gpu = level3
     v = np.random.default_rng(4).standard_normal(orc.E)

@@ -224,3 +224,25 @@ def test_pv_flux_reduces_to_coriolis(grid_dir):
         errs.append(np.abs(pv - cv).max() / np.abs(cv).max())
     assert errs[0] < 0.04 and errs[2] < 0.005
     assert errs[0] / errs[1] > 3 and errs[1] / errs[2] > 1.8
+
+
+def test_lsq_flux_constant_and_smooth_fields(grid_dir):
+    """interpolateLSQFlux (third order, Gaussian-RBF second derivatives): a constant thickness is
+    carried exactly up to the conditioning of the near-flat RBF systems, and the flux of a smooth
+    thickness converges to v h at the face intercept as the grid is refined."""
+    import geodesicodis_gb300 as g
+    from oracle import pyoracle as O
+    const_err, smooth_err = [], []
+    for lv in (2, 3, 4):
+        path = grid_dir / f"grid_{lv}.txt"
+        om = O.OracleMesh(path, RADIUS)
+        orc = O.OracleSolver(om, radius=RADIUS, g=0.113, angvel=5.307e-5, h=1e4, alpha=1e-5, dt=10.0)
+        v = np.random.default_rng(lv).standard_normal(om.n_edges)
+        f0 = orc.interpolateLSQFlux(v, np.full(om.n_cells, 1e4))
+        const_err.append(np.abs(f0 - 1e4 * v).max() / (1e4 * np.abs(v).max()))
+        m = g.Mesh.from_file(path, RADIUS)
+        h = lambda la, lo: 1e4 + 100.0 * np.cos(la) ** 2 * np.cos(2 * lo)   # noqa: E731
+        f1 = orc.interpolateLSQFlux(v, h(m.field(12), m.field(13)))
+        smooth_err.append(np.abs(f1 - v * h(om.field(10), om.field(11))).max() / (100.0 * np.abs(v).max()))
+    assert max(const_err) < 1e-5 and const_err[2] < const_err[0]
+    assert smooth_err[0] > 3 * smooth_err[1] > 9 * smooth_err[2] and smooth_err[2] < 1e-3
