@@ -87,9 +87,12 @@ int main(int argc, char** argv)
     odis_input in;
     odis_status st = odis_params_from_input((dir + "/input.in").c_str(), &in);
     if (st != ODIS_OK) return fail("reading input.in", st);
-    if (in.advection) std::fprintf(stderr, "odis_run: advection is not supported; running the linear equations\n");
     odis_params p = in.params;
     p.precision = prec == "fp32" ? ODIS_FP32 : prec == "df64" ? ODIS_DF64 : ODIS_FP64;
+    if (p.advection && p.precision != ODIS_FP64) {
+        std::fprintf(stderr, "odis_run: advection true runs the nonlinear equations in FP64\n");
+        p.precision = ODIS_FP64;
+    }
     odis_mesh* mesh = nullptr;
     if (!grid.empty()) st = odis_mesh_from_file(grid.c_str(), p.radius, &mesh);
     else st = odis_mesh_generate(level >= 0 ? level : in.grid_level - 1, p.radius, &mesh);

@@ -114,6 +114,81 @@ __global__ void k_lsq_flux(const int* __restrict__ col, const double* __restrict
     flux[e] = __dadd_rn(__dsub_rn(a, b), c);
 }
 
+// ---- the advective time step (src/timeIntegrator.cpp:205-269, advection true) ----
+
+// dvdt = alpha (G eta), the gradient row summed in ascending node order
+__global__ void k_adv_grad(const int* __restrict__ gcol, const double* __restrict__ gval, int E, int Ep, double alpha,
+                           const double* __restrict__ x, double* __restrict__ y)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double t = 0.0;
+    t = __dadd_rn(t, __dmul_rn(gval[e], x[gcol[e]]));
+    t = __dadd_rn(t, __dmul_rn(gval[Ep + e], x[gcol[Ep + e]]));
+    y[e] = __dmul_rn(alpha, t);
+}
+
+// integrateAB3scalar (src/temporalOperators.cpp:17-68) for one unknown; h = its [3] history
+__device__ __forceinline__ void ab3_ref(double& s, double* h, int iter, double dt, int init_load)
+{
+    const double a = 23. / 12., b = -16. / 12., c = 5. / 12.;
+    if (iter > 1 || init_load) {
+        s = __dadd_rn(s, __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(a, h[0]), __dmul_rn(b, h[1])), __dmul_rn(c, h[2])), dt));
+        h[2] = h[1];
+        h[1] = h[0];
+    } else if (iter == 0) {
+        s = __dadd_rn(s, __dmul_rn(h[0], dt));
+        h[2] = h[0];
+    } else {
+        s = __dadd_rn(s, __dmul_rn(h[0], dt));
+        h[1] = h[0];
+    }
+}
+
+// momentum update: drag_e = -alpha v_e + (G U)_e from the velocity before the
+// step, history slot 0 = dvdt, AB3, then v += dt drag (src/timeIntegrator.cpp:213-242)
+__global__ void k_adv_vstep(const int* __restrict__ gcol, const double* __restrict__ gval, int E, int Ep, double alpha,
+                            double dt, int iter, int init_load, const double* __restrict__ dv0,
+                            const double* __restrict__ U, double* __restrict__ v, double* __restrict__ hist)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double gu = 0.0;
+    gu = __dadd_rn(gu, __dmul_rn(gval[e], U[gcol[e]]));
+    gu = __dadd_rn(gu, __dmul_rn(gval[Ep + e], U[gcol[Ep + e]]));
+    gu = __dadd_rn(0.0, __dmul_rn(1.0, gu));
+    double ve = v[e];
+    const double drag = __dadd_rn(__dadd_rn(0.0, __dmul_rn(1.0, __dmul_rn(-alpha, ve))), gu);
+    double* h = hist + (size_t)e * 3;
+    h[0] = dv0[e];
+    ab3_ref(ve, h, iter, dt, init_load);
+    v[e] = __dadd_rn(ve, __dmul_rn(dt, drag));
+}
+
+// continuity update: detadt = D flux (cell's faces in ascending face order),
+// history slot 0, AB3 (src/timeIntegrator.cpp:249-253)
+__global__ void k_adv_estep(const int* __restrict__ dcol, const double* __restrict__ dval, int N, int Np, double dt,
+                            int iter, int init_load, const double* __restrict__ flux, double* __restrict__ eta,
+                            double* __restrict__ hist)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double t = 0.0;
+#pragma unroll
+    for (int j = 0; j < 6; j++) t = __dadd_rn(t, __dmul_rn(dval[j * Np + i], flux[dcol[j * Np + i]]));
+    double* h = hist + (size_t)i * 3;
+    h[0] = __dadd_rn(0.0, __dmul_rn(1.0, t));
+    double s = eta[i];
+    ab3_ref(s, h, iter, dt, init_load);
+    eta[i] = s;
+}
+
+__global__ void k_adv_thickness(int N, double h0, const double* __restrict__ eta, double* __restrict__ ht)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) ht[i] = __dadd_rn(h0, eta[i]);
+}
+
 template <class T>
 T* upload(const std::vector<T>& h)
 {
@@ -137,6 +212,11 @@ struct AdvDev {
     double *q = nullptr, *qe = nullptr, *he = nullptr, *uxyz = nullptr, *ek = nullptr;
     int* lcol = nullptr;         // [7][2 Ep] operatorDirectionalSecondDeriv rows
     double *lval = nullptr, *dist = nullptr;
+    int* dcol = nullptr;         // [6][Np] divergence rows, ascending face order (padded with zero weights)
+    double* dval = nullptr;
+    // state of an advective run, in the reference's layout
+    double *v = nullptr, *eta = nullptr, *hv = nullptr, *hp = nullptr, *ht = nullptr;
+    double *U = nullptr, *dv0 = nullptr, *flux = nullptr, *uv = nullptr;
 };
 
 void adv_destroy(AdvDev* a)
@@ -145,7 +225,9 @@ void adv_destroy(AdvDev* a)
     for (void* p : {(void*)a->vface, (void*)a->vnode, (void*)a->fvert, (void*)a->fnode, (void*)a->fr, (void*)a->nfr,
                     (void*)a->gcol, (void*)a->vcoef, (void*)a->vR, (void*)a->vinv, (void*)a->vf, (void*)a->cvA,
                     (void*)a->cw, (void*)a->gval, (void*)a->q, (void*)a->qe, (void*)a->he, (void*)a->uxyz,
-                    (void*)a->ek, (void*)a->lcol, (void*)a->lval, (void*)a->dist})
+                    (void*)a->ek, (void*)a->lcol, (void*)a->lval, (void*)a->dist, (void*)a->dcol, (void*)a->dval,
+                    (void*)a->v, (void*)a->eta, (void*)a->hv, (void*)a->hp, (void*)a->ht, (void*)a->U, (void*)a->dv0,
+                    (void*)a->flux, (void*)a->uv})
         cudaFree(p);
     delete a;
 }
@@ -218,6 +300,24 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
         a->dist = upload(dist);
         if (!a->lcol || !a->lval || !a->dist) { adv_destroy(a); return ODIS_ERR_NOMEM; }
     }
+    {   // operatorDivergence rows (src/mesh.cpp:3177-3288), ascending face order
+        std::vector<int> dc((size_t)6 * Np, 0);
+        std::vector<double> dvv((size_t)6 * Np, 0.0);
+        for (int i = 0; i < m.N; i++) {
+            const int k = m.nfriends(i);
+            int idx[6] = {0, 1, 2, 3, 4, 5};
+            std::sort(idx, idx + k, [&](int x, int y) { return m.faces[i * 6 + x] < m.faces[i * 6 + y]; });
+            for (int j = 0; j < 6; j++) {
+                const int s = idx[j < k ? j : k - 1];
+                const int f = m.faces[i * 6 + s];
+                dc[(size_t)j * Np + i] = f;
+                dvv[(size_t)j * Np + i] = j < k ? -m.node_face_dir[i * 6 + s] * m.face_len[f] / m.cv_area[i] : 0.0;
+            }
+        }
+        a->dcol = upload(dc);
+        a->dval = upload(dvv);
+        if (!a->dcol || !a->dval) { adv_destroy(a); return ODIS_ERR_NOMEM; }
+    }
     a->vface = upload(vface); a->vnode = upload(vnode); a->vcoef = upload(vcoef); a->vR = upload(vR);
     a->vinv = upload(vinv); a->vf = upload(vf); a->cvA = upload(cvA);
     a->fvert = upload(fvert); a->fnode = upload(fnode); a->fr = upload(fr); a->nfr = upload(nfr);
@@ -249,6 +349,48 @@ void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dv
 }
 
 int adv_kernels_per_call() { return 5; }
+
+int adv_state_alloc(AdvDev* a, double h0)
+{
+    if (a->v) return ODIS_OK;
+    const size_t E = a->Ep, N = a->Np;
+    if (cudaMalloc(&a->v, sizeof(double) * E) != cudaSuccess || cudaMalloc(&a->eta, sizeof(double) * N) != cudaSuccess ||
+        cudaMalloc(&a->hv, sizeof(double) * 3 * E) != cudaSuccess || cudaMalloc(&a->hp, sizeof(double) * 3 * N) != cudaSuccess ||
+        cudaMalloc(&a->ht, sizeof(double) * N) != cudaSuccess || cudaMalloc(&a->U, sizeof(double) * N) != cudaSuccess ||
+        cudaMalloc(&a->dv0, sizeof(double) * E) != cudaSuccess || cudaMalloc(&a->flux, sizeof(double) * E) != cudaSuccess ||
+        cudaMalloc(&a->uv, sizeof(double) * 2 * E) != cudaSuccess)
+        return ODIS_ERR_NOMEM;
+    cudaMemset(a->v, 0, sizeof(double) * E);
+    cudaMemset(a->eta, 0, sizeof(double) * N);
+    cudaMemset(a->hv, 0, sizeof(double) * 3 * E);
+    cudaMemset(a->hp, 0, sizeof(double) * 3 * N);
+    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads>>>(a->N, h0, a->eta, a->ht);
+    return cudaDeviceSynchronize() == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
+}
+
+AdvState adv_state(AdvDev* a) { return AdvState{a->v, a->eta, a->hv, a->hp, a->ht, a->U, a->uv}; }
+
+void adv_step(AdvDev* a, const double* rbf, const int* cell_face, double g, double alpha, double h0, double dt,
+              int iter, int init_load, cudaStream_t s)
+{
+    const int eb = (a->E + kAdvThreads - 1) / kAdvThreads, nb = (a->N + kAdvThreads - 1) / kAdvThreads;
+    // updateMomentum, advection branch: -g G eta + PV flux - G KE
+    k_adv_grad<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, -g * (1 - 0.5 * 0.0), a->eta, a->dv0);
+    adv_momentum(a, rbf, cell_face, a->dv0, a->v, a->ht, a->ek, s);
+    // the caller has put the forcing at t + dt in a->U
+    k_adv_vstep<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, alpha, dt, iter, init_load, a->dv0, a->U, a->v,
+                                          a->hv);
+    // updateEta, advection branch: D (LSQ flux of h + eta)
+    adv_lsq_flux(a, a->flux, a->v, a->ht, s);
+    k_adv_estep<<<nb, kAdvThreads, 0, s>>>(a->dcol, a->dval, a->N, a->Np, dt, iter, init_load, a->flux, a->eta, a->hp);
+}
+
+void adv_thickness(AdvDev* a, double h0, cudaStream_t s)
+{
+    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->N, h0, a->eta, a->ht);
+}
+
+int adv_kernels_per_step() { return 4 + adv_kernels_per_call() + 1; }
 
 void adv_lsq_flux(AdvDev* a, double* flux, const double* v, const double* h_total, cudaStream_t s)
 {

@@ -17,6 +17,20 @@ void adv_destroy(AdvDev* a);
 void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dvdt, const double* v,
                   const double* h_total, double* ekin, cudaStream_t s);
 double* adv_ekin_scratch(AdvDev* a);
+// state of an advective run, reference layout: v[E], eta[N], dvdt history [E][3],
+// detadt history [N][3], column thickness h + eta [N], forcing [N], uv [E][2]
+struct AdvState {
+    double *v, *eta, *hv, *hp, *ht, *U, *uv;
+};
+int adv_state_alloc(AdvDev* a, double h0);
+AdvState adv_state(AdvDev* a);
+// one step of the advective loop up to the continuity update; the caller puts
+// the forcing at t + dt in AdvState.U first, and afterwards computes the power
+// from v and calls adv_thickness
+void adv_step(AdvDev* a, const double* rbf, const int* cell_face, double g, double alpha, double h0, double dt,
+              int iter, int init_load, cudaStream_t s);
+void adv_thickness(AdvDev* a, double h0, cudaStream_t s);
+int adv_kernels_per_step();
 // flux[E]: the reference's interpolateLSQFlux of the column thickness h_total[N] with velocities v[E]
 void adv_lsq_flux(AdvDev* a, double* flux, const double* v, const double* h_total, cudaStream_t s);
 int adv_kernels_per_call();

@@ -531,6 +531,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     if (p->potential < ODIS_POT_NONE || p->potential > ODIS_POT_FULL) return ODIS_ERR_ARG;
     if (!(p->dt > 0.0) || !(p->g > 0.0) || !(p->h > 0.0) || !(p->radius > 0.0) || p->alpha < 0.0) return ODIS_ERR_ARG;
     if (p->sh_lmax < 0 || p->sh_lmax > 64 || (p->sh_lmax > 0 && !p->sh_factors)) return ODIS_ERR_ARG;
+    if (p->advection && (p->precision != ODIS_FP64 || p->sh_lmax > 0)) return ODIS_ERR_ARG;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return ODIS_ERR_CUDA;
     std::unique_ptr<odis_ctx> c(new (std::nothrow) odis_ctx);
@@ -646,8 +647,15 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     }
     c->slot0_saved.assign((size_t)(m.E + m.N), 0.0);
     if (cudaDeviceSynchronize() != cudaSuccess) return ODIS_ERR_CUDA;
-    st = choose_exec_path(c.get());
-    if (st != ODIS_OK) return st;
+    if (p->advection) {            // the nonlinear loop has its own operators and reference-layout state
+        c->persist_ok = false;
+        st = adv_create(&c->adv, m, p->angvel, c->Ep, c->Np);
+        if (st == ODIS_OK) st = adv_state_alloc(c->adv, p->h);
+        if (st != ODIS_OK) return st;
+    } else {
+        st = choose_exec_path(c.get());
+        if (st != ODIS_OK) return st;
+    }
     *out = c.release();
     return ODIS_OK;
 }
@@ -977,10 +985,57 @@ static int run_chunk(odis_ctx* c, int n, double* dpow)
     return ODIS_OK;
 }
 
+// ab3Explicit with advection true (src/timeIntegrator.cpp:205-269): per step the
+// momentum tendency with the advection term, forcing at t + dt, AB3 with drag
+// and forcing outside it, the continuity equation with the LSQ thickness flux,
+// the dissipated power from the new velocity, then the column thickness.
+static odis_status run_advective(odis_ctx* c, int n, double* dpow)
+{
+    const AdvState a = adv_state(c->adv);
+    const odis_params& p = c->p;
+    for (int s = 0; s < n; s++) {
+        const int it = (int)c->iter;
+        const double t = p.dt * it + p.dt;
+        launch_forcing(c->trig, c->N, c->Np, a.U, p.potential, t, p.angvel, p.radius, p.love_reduct, p.ecc, p.obliq,
+                       c->stream);
+        adv_step(c->adv, c->rbf, c->op64.cc.edge, p.g, p.alpha, p.h, p.dt, it, p.init_load, c->stream);
+        launch_interp(c->op64.fc, c->nrm, c->E, c->Ep, a.uv, a.v, c->stream);
+        launch_energy(c->area, c->E, p.alpha * 1000.0 * p.h, 4 * kPi * std::pow(c->r, 2.0), a.uv, nullptr,
+                      c->d_partial, dpow ? dpow + s : c->d_partial + (size_t)c->fold_rows * c->eb, c->stream);
+        adv_thickness(c->adv, p.h, c->stream);
+        c->iter++;
+        c->launches += 1 + adv_kernels_per_step() + 3;
+    }
+    ODIS_CK(cudaGetLastError());
+    return ODIS_OK;
+}
+
 extern "C" odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem)
 {
     if (!c || n < 0 || !mem_ok(mem)) return ODIS_ERR_ARG;
     if (n == 0) return ODIS_OK;
+    if (c->p.advection) {
+        double* dpow = nullptr;
+        if (power && mem == ODIS_MEM_DEVICE) dpow = power;
+        else {
+            if (n > c->power_cap) {
+                if (c->d_power) cudaFree(c->d_power);
+                c->d_power = nullptr;
+                c->power_cap = 0;
+                ODIS_CK(cudaMalloc(&c->d_power, sizeof(double) * n));
+                c->power_cap = n;
+            }
+            dpow = c->d_power;
+        }
+        const int st = run_advective(c, n, dpow);
+        if (st != ODIS_OK) return st;
+        double last = 0.0;
+        ODIS_CK(cudaMemcpyAsync(&last, dpow + n - 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        if (power && mem == ODIS_MEM_HOST)
+            ODIS_CK(cudaMemcpyAsync(power, dpow, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        ODIS_CK(cudaStreamSynchronize(c->stream));
+        return std::isfinite(last) ? ODIS_OK : ODIS_ERR_NONFINITE;
+    }
     double* dpow = nullptr;
     if (power) {
         if (mem == ODIS_MEM_DEVICE) dpow = power;
@@ -1116,6 +1171,14 @@ extern "C" odis_status odis_get_state(odis_ctx* c, int* iter, double* v, double*
     if (!c) return ODIS_ERR_ARG;
     ODIS_CK(cudaStreamSynchronize(c->stream));
     if (iter) *iter = (int)c->iter;
+    if (c->p.advection) {
+        const AdvState a = adv_state(c->adv);
+        if (v) ODIS_CK(cudaMemcpy(v, a.v, sizeof(double) * c->E, cudaMemcpyDeviceToHost));
+        if (eta) ODIS_CK(cudaMemcpy(eta, a.eta, sizeof(double) * c->N, cudaMemcpyDeviceToHost));
+        if (dvdt) ODIS_CK(cudaMemcpy(dvdt, a.hv, sizeof(double) * 3 * c->E, cudaMemcpyDeviceToHost));
+        if (detadt) ODIS_CK(cudaMemcpy(detadt, a.hp, sizeof(double) * 3 * c->N, cudaMemcpyDeviceToHost));
+        return ODIS_OK;
+    }
     if (c->p.precision == ODIS_DF64) return get_state_t<float2>(c, c->sdf, v, eta, dvdt, detadt);
     return c->p.precision == ODIS_FP64 ? get_state_t<double>(c, c->s64, v, eta, dvdt, detadt)
                                        : get_state_t<float>(c, c->s32, v, eta, dvdt, detadt);
@@ -1127,6 +1190,16 @@ extern "C" odis_status odis_set_state(odis_ctx* c, int iter, const double* v, co
     if (!c || iter < 0) return ODIS_ERR_ARG;
     ODIS_CK(cudaStreamSynchronize(c->stream));
     c->iter = iter;
+    if (c->p.advection) {
+        const AdvState a = adv_state(c->adv);
+        if (v) ODIS_CK(cudaMemcpy(a.v, v, sizeof(double) * c->E, cudaMemcpyHostToDevice));
+        if (eta) ODIS_CK(cudaMemcpy(a.eta, eta, sizeof(double) * c->N, cudaMemcpyHostToDevice));
+        if (dvdt) ODIS_CK(cudaMemcpy(a.hv, dvdt, sizeof(double) * 3 * c->E, cudaMemcpyHostToDevice));
+        if (detadt) ODIS_CK(cudaMemcpy(a.hp, detadt, sizeof(double) * 3 * c->N, cudaMemcpyHostToDevice));
+        adv_thickness(c->adv, c->p.h, c->stream);       // src/timeIntegrator.cpp:203
+        ODIS_CK(cudaStreamSynchronize(c->stream));
+        return ODIS_OK;
+    }
     if (c->p.precision == ODIS_DF64) return set_state_t<float2>(c, c->sdf, iter, v, eta, dvdt, detadt);
     return c->p.precision == ODIS_FP64 ? set_state_t<double>(c, c->s64, iter, v, eta, dvdt, detadt)
                                        : set_state_t<float>(c, c->s32, iter, v, eta, dvdt, detadt);

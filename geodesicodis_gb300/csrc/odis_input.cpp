@@ -118,6 +118,7 @@ int parse_input(const char* path, odis_input& out)
     out.output_time = output_time;
     out.sh_degree = lmax;
     out.advection = advection ? 1 : 0;
+    p.advection = out.advection;
     out.fric_linear = friction == "LINEAR" ? 1 : 0;
     out.surface_free = surface == "FREE" ? 1 : 0;
     out.init_kind = init == "NONE" ? 0 : init == "LOAD" ? 1 : init == "ANALYTICAL" ? 2 : -1;

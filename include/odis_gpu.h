@@ -84,6 +84,9 @@ typedef struct odis_params {
     int precision;          /* ODIS_FP64 or ODIS_FP32 */
     int sh_lmax;            /* 0: no self-gravity/loading; else maximum degree (<= 64) */
     const double* sh_factors; /* [sh_lmax+1] per-degree factors (0 and 1 unused); may be NULL if sh_lmax == 0 */
+    int advection;          /* 1: the nonlinear equations ("advection true"): momentum advection
+                               (src/momAdvection.cpp) and the LSQ thickness flux in the continuity
+                               equation (src/updateEta.cpp:22-32); ODIS_FP64 only, no self-gravity */
 } odis_params;
 
 /* Parsed input.in (src/globals.cpp:58-203 keys).  Strings are fixed-size. */
@@ -95,7 +98,7 @@ typedef struct odis_input {
     int grid_level;          /* "geodesic grid level" as written in the file */
     int output_time;         /* dumps per orbit */
     int sh_degree;           /* "sh degree" */
-    int advection;           /* 1 if advection true (unsupported by this library) */
+    int advection;           /* 1 if advection true (also set in params.advection) */
     int fric_linear;         /* 1 LINEAR, 0 QUADRATIC */
     int surface_free;        /* 1 FREE */
     int init_kind;           /* 0 NONE, 1 LOAD, 2 ANALYTICAL */

@@ -771,6 +771,7 @@ typedef struct {
     double radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt;
     int potential;
     int init_load;
+    int advection;        /* 1: the nonlinear branch (momentum advection, LSQ thickness flux) */
 } orc_params;
 
 /* ------------------------------------------------------------------------ */
@@ -1375,6 +1376,7 @@ typedef struct {
     double time;
     double *v, *eta, *dvdt, *detadt;   /* v[E], eta[N], dvdt[E][3], detadt[N][3] */
     double *U, *drag, *dv0, *dp0, *uv, *ediss, *tmp;
+    double *h_total, *ekin, *flux;      /* advection: column thickness h + eta [N], KE [N], thickness flux [E] */
     double power;                       /* last dissipated power, W/m^2 */
 } orc_sim;
 
@@ -1394,6 +1396,10 @@ orc_sim *orc_sim_create(orc_solver *S)
     X->uv = (double *)calloc((size_t)E * 2, sizeof(double));
     X->ediss = (double *)calloc(E, sizeof(double));
     X->tmp = (double *)calloc(E, sizeof(double));
+    X->h_total = (double *)calloc(N, sizeof(double));
+    X->ekin = (double *)calloc(N, sizeof(double));
+    X->flux = (double *)calloc(E, sizeof(double));
+    for (int i = 0; i < N; i++) X->h_total[i] = S->p.h + X->eta[i];      /* :203 */
     return X;
 }
 
@@ -1402,6 +1408,7 @@ void orc_sim_free(orc_sim *X)
     if (!X) return;
     free(X->v); free(X->eta); free(X->dvdt); free(X->detadt); free(X->U); free(X->drag);
     free(X->dv0); free(X->dp0); free(X->uv); free(X->ediss); free(X->tmp);
+    free(X->h_total); free(X->ekin); free(X->flux);
     free(X);
 }
 
@@ -1415,6 +1422,7 @@ void orc_sim_set_state(orc_sim *X, int iter, const double *v, const double *eta,
     if (eta) memcpy(X->eta, eta, sizeof(double) * N);
     if (dvdt) memcpy(X->dvdt, dvdt, sizeof(double) * E * 3);
     if (detadt) memcpy(X->detadt, detadt, sizeof(double) * N * 3);
+    for (int i = 0; i < N; i++) X->h_total[i] = X->S->p.h + X->eta[i];   /* src/timeIntegrator.cpp:203 */
 }
 
 void orc_sim_get_state(const orc_sim *X, int *iter, double *v, double *eta, double *dvdt, double *detadt)
@@ -1434,7 +1442,12 @@ double orc_sim_step(orc_sim *X)
     const orc_mesh *M = S->M;
     int N = M->N, E = M->E;
     double dt = S->p.dt;
-    orc_update_momentum(S, X->dv0, X->v, X->eta);                      /* :213 */
+    if (S->p.advection) {                /* updateMomentum's advection branch, src/updateMomentum.cpp:35-39 */
+        csr_spmv(&M->G, X->eta, -S->p.g * (1 - 0.5 * 0.0), X->dv0);
+        orc_momentum_advection(M, S->p.angvel, X->dv0, X->v, X->h_total, X->ekin);
+    } else {
+        orc_update_momentum(S, X->dv0, X->v, X->eta);                  /* :213 */
+    }
     for (int i = 0; i < E; ++i) X->dvdt[i * 3] = X->dv0[i];              /* :215 */
     orc_forcing(S, X->U, S->p.potential, X->time + dt);                  /* :218 */
     if (S->sh_lmax > 0) orc_sh_add_loading(S, X->eta, X->U);
@@ -1443,11 +1456,19 @@ double orc_sim_step(orc_sim *X)
     for (int i = 0; i < E; i++) X->drag[i] = (0.0 + 1.0 * ((-S->p.alpha) * X->v[i])) + X->tmp[i];
     orc_ab3(dt, X->v, X->dvdt, X->iter, E, S->p.init_load);              /* :239 */
     for (int i = 0; i < E; i++) X->v[i] += dt * X->drag[i];              /* :242 */
-    orc_update_eta(S, X->dp0, X->v);                                     /* :249 */
+    if (S->p.advection) {                /* updateEta's advection branch, src/updateEta.cpp:22-32 */
+        int st = orc_lsq_flux((orc_mesh *)M, 0.25, X->flux, X->v, X->h_total);
+        if (st) return NAN;
+        csr_spmv(&M->D, X->flux, 1.0, X->dp0);
+    } else {
+        orc_update_eta(S, X->dp0, X->v);                                 /* :249 */
+    }
     for (int i = 0; i < N; ++i) X->detadt[i * 3] = X->dp0[i];
     orc_ab3(dt, X->eta, X->detadt, X->iter, N, S->p.init_load);          /* :253 */
     orc_interpolate_velocity(M, X->uv, X->v);                            /* :261 */
     X->power = orc_update_energy(M, S->p.alpha, S->p.h, X->ediss, X->uv);
+    if (S->p.advection)                  /* column thickness for the next step, :266-269 */
+        for (int i = 0; i < N; i++) X->h_total[i] = S->p.h + X->eta[i];
     X->iter++;
     X->time = dt * X->iter;
     return X->power;

@@ -25,7 +25,7 @@ ECC, OBLIQ, OBLIQ_WEST, FULL, FULL2, NONE = 1, 2, 3, 4, 5, 0
 class OrcParams(C.Structure):
     _fields_ = [("radius", C.c_double), ("g", C.c_double), ("angvel", C.c_double), ("h", C.c_double),
                 ("alpha", C.c_double), ("ecc", C.c_double), ("obliq", C.c_double), ("love_reduct", C.c_double),
-                ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int)]
+                ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int), ("advection", C.c_int)]
 
 
 _lib = None
@@ -159,9 +159,9 @@ class OracleSolver:
     """FP64 restatement of the reference step (see odis_oracle.c)."""
 
     def __init__(self, mesh: OracleMesh, *, radius, g, angvel, h, alpha, ecc=0.0, obliq=0.0, love_reduct=1.0,
-                 dt, potential=ECC, init_load=0, sh_lmax=0, sh_factors=None):
+                 dt, potential=ECC, init_load=0, sh_lmax=0, sh_factors=None, advection=0):
         self.mesh = mesh
-        self.p = OrcParams(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load)
+        self.p = OrcParams(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load, advection)
         self._s = C.c_void_p(lib().orc_solver_create(mesh._h, C.byref(self.p)))
         if sh_lmax:
             f = np.ascontiguousarray(sh_factors, np.float64)

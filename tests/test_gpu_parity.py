@@ -101,6 +101,30 @@ def test_lsq_flux(grid_dir, level):
     assert rel_err(gpu.interpolateLSQFlux(v, ht), orc.interpolateLSQFlux(v, ht)) < 1e-13
 
 
+@pytest.mark.parametrize("level,steps", [(2, 700), (3, 400)])
+def test_advective_loop_parity(grid_dir, level, steps):
+    """ab3Explicit with advection true (src/timeIntegrator.cpp:205-269): momentum advection, the LSQ
+    thickness flux in the continuity equation and the column thickness update, against the oracle."""
+    orc, gpu = _pair(grid_dir / f"grid_{level}.txt", advection=1)
+    po, pg = orc.run(steps), gpu.run(steps)
+    _, vo, eo, dvo, deo = orc.get_state()
+    it, vg, eg, dvg, deg = gpu.get_state()
+    assert it == steps
+    assert rel_err(eg, eo) < 1e-10 and rel_err(vg, vo) < 1e-10 and rel_err(pg, po) < 1e-10
+    assert rel_err(dvg, dvo) < 1e-10 and rel_err(deg, deo) < 1e-10
+
+
+def test_advection_options_are_checked(grid_dir):
+    """The nonlinear loop is FP64 only and excludes self-gravity."""
+    import geodesicodis_gb300 as g
+    m = g.Mesh.from_file(grid_dir / "grid_2.txt", RADIUS)
+    for over in (dict(precision=g.FP32), dict(precision=g.DF64),
+                 dict(sh_lmax=4, sh_factors=np.ones(5))):
+        with pytest.raises(g.OdisError) as ei:
+            g.Solver(g.make_params(**config0_params(), advection=1, **over), m)
+        assert ei.value.code == g.ERR_ARG
+
+
 def test_interpolate_and_energy(level3):
     orc, gpu = level3
     v = np.random.default_rng(4).standard_normal(orc.E)

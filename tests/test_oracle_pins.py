@@ -246,3 +246,23 @@ def test_lsq_flux_constant_and_smooth_fields(grid_dir):
         smooth_err.append(np.abs(f1 - v * h(om.field(10), om.field(11))).max() / (100.0 * np.abs(v).max()))
     assert max(const_err) < 1e-5 and const_err[2] < const_err[0]
     assert smooth_err[0] > 3 * smooth_err[1] > 9 * smooth_err[2] and smooth_err[2] < 1e-3
+
+
+def test_advective_loop_stays_near_linear_at_small_amplitude(grid_dir):
+    """ab3Explicit with advection true (momentum advection + LSQ thickness flux): at the config-0
+    tide (eta / h ~ 2e-3) the nonlinear run stays within a fraction of a percent of the linear one,
+    and the gap (discretisation differences of the PV-flux Coriolis term) shrinks with level."""
+    from conftest import config0_params
+    from oracle import pyoracle as O
+    gaps = []
+    for lv in (2, 3):
+        om = O.OracleMesh(grid_dir / f"grid_{lv}.txt", RADIUS)
+        lin = O.OracleSolver(om, **config0_params())
+        adv = O.OracleSolver(om, **config0_params(), advection=1)
+        pl, pa = lin.run(1500), adv.run(1500)
+        _, vl, el, _, _ = lin.get_state()
+        _, va, ea, _, _ = adv.get_state()
+        assert np.all(np.isfinite(pa)) and np.all(np.isfinite(ea))
+        gaps.append(np.abs(ea - el).max() / np.abs(el).max())
+        assert abs(pa[-1] - pl[-1]) / pl[-1] < 0.05
+    assert gaps[1] < gaps[0] < 0.01
