@@ -26,6 +26,7 @@ namespace odis {
 namespace {
 
 constexpr int kAdvThreads = 256;
+constexpr int kAdvGraphSteps = 64;      // steps per captured graph of the advective loop
 
 __global__ void k_adv_pv(const int* __restrict__ vface, const double* __restrict__ vcoef, const int* __restrict__ vnode,
                          const double* __restrict__ vR, const double* __restrict__ vinv, const double* __restrict__ vf,
@@ -146,16 +147,29 @@ __device__ __forceinline__ void ab3_ref(double& s, double* h, int iter, double d
 }
 
 // momentum update: drag_e = -alpha v_e + (G U)_e from the velocity before the
-// step, history slot 0 = dvdt, AB3, then v += dt drag (src/timeIntegrator.cpp:213-242)
+// step, history slot 0 = dvdt, AB3, then v += dt drag (src/timeIntegrator.cpp:213-242).
+// The forcing at t + dt is cos(M) Ua + sin(M) Ub with M = Omega t, t = dt step + dt
+// and the step read from the device counter (one sincos per block).
 __global__ void k_adv_vstep(const int* __restrict__ gcol, const double* __restrict__ gval, int E, int Ep, double alpha,
                             double dt, int iter, int init_load, const double* __restrict__ dv0,
-                            const double* __restrict__ U, double* __restrict__ v, double* __restrict__ hist)
+                            const double* __restrict__ Ua, const double* __restrict__ Ub, double angvel,
+                            const long long* __restrict__ step, double* __restrict__ v, double* __restrict__ hist)
 {
+    __shared__ double cs[2];
+    if (threadIdx.x == 0) {
+        const double t = dt * (double)(*step) + dt;
+        sincos(angvel * t, &cs[1], &cs[0]);
+    }
+    __syncthreads();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
+    const double c = cs[0], sn = cs[1];
+    const int n0 = gcol[e], n1 = gcol[Ep + e];
+    const double u0 = __dadd_rn(__dmul_rn(c, Ua[n0]), __dmul_rn(sn, Ub[n0]));
+    const double u1 = __dadd_rn(__dmul_rn(c, Ua[n1]), __dmul_rn(sn, Ub[n1]));
     double gu = 0.0;
-    gu = __dadd_rn(gu, __dmul_rn(gval[e], U[gcol[e]]));
-    gu = __dadd_rn(gu, __dmul_rn(gval[Ep + e], U[gcol[Ep + e]]));
+    gu = __dadd_rn(gu, __dmul_rn(gval[e], u0));
+    gu = __dadd_rn(gu, __dmul_rn(gval[Ep + e], u1));
     gu = __dadd_rn(0.0, __dmul_rn(1.0, gu));
     double ve = v[e];
     const double drag = __dadd_rn(__dadd_rn(0.0, __dmul_rn(1.0, __dmul_rn(-alpha, ve))), gu);
@@ -183,11 +197,16 @@ __global__ void k_adv_estep(const int* __restrict__ dcol, const double* __restri
     eta[i] = s;
 }
 
-__global__ void k_adv_thickness(int N, double h0, const double* __restrict__ eta, double* __restrict__ ht)
+// column thickness for the next step; the first thread also advances the step counter
+__global__ void k_adv_thickness(int N, double h0, const double* __restrict__ eta, double* __restrict__ ht,
+                                long long* __restrict__ step)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < N) ht[i] = __dadd_rn(h0, eta[i]);
+    if (i == 0 && step) *step += 1;
 }
+
+__global__ void k_adv_set_step(long long* step, long long v) { *step = v; }
 
 template <class T>
 T* upload(const std::vector<T>& h)
@@ -217,6 +236,11 @@ struct AdvDev {
     // state of an advective run, in the reference's layout
     double *v = nullptr, *eta = nullptr, *hv = nullptr, *hp = nullptr, *ht = nullptr;
     double *U = nullptr, *dv0 = nullptr, *flux = nullptr, *uv = nullptr;
+    double *Ua = nullptr, *Ub = nullptr;    // forcing U = cos(M) Ua + sin(M) Ub at the nodes
+    double angvel = 0.0;
+    long long* step = nullptr;              // device step counter (forcing phase)
+    double* pbuf = nullptr;                 // [kAdvGraphSteps] power of a graph chunk
+    cudaGraphExec_t graph = nullptr;
 };
 
 void adv_destroy(AdvDev* a)
@@ -227,8 +251,9 @@ void adv_destroy(AdvDev* a)
                     (void*)a->cw, (void*)a->gval, (void*)a->q, (void*)a->qe, (void*)a->he, (void*)a->uxyz,
                     (void*)a->ek, (void*)a->lcol, (void*)a->lval, (void*)a->dist, (void*)a->dcol, (void*)a->dval,
                     (void*)a->v, (void*)a->eta, (void*)a->hv, (void*)a->hp, (void*)a->ht, (void*)a->U, (void*)a->dv0,
-                    (void*)a->flux, (void*)a->uv})
+                    (void*)a->flux, (void*)a->uv, (void*)a->Ua, (void*)a->Ub, (void*)a->step, (void*)a->pbuf})
         cudaFree(p);
+    if (a->graph) cudaGraphExecDestroy(a->graph);
     delete a;
 }
 
@@ -350,9 +375,20 @@ void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dv
 
 int adv_kernels_per_call() { return 5; }
 
-int adv_state_alloc(AdvDev* a, double h0)
+int adv_state_alloc(AdvDev* a, double h0, const std::vector<double>& Ua, const std::vector<double>& Ub, double angvel)
 {
     if (a->v) return ODIS_OK;
+    {
+        std::vector<double> ua(a->Np, 0.0), ub(a->Np, 0.0);
+        for (int i = 0; i < a->N; i++) { ua[i] = Ua[i]; ub[i] = Ub[i]; }
+        a->Ua = upload(ua);
+        a->Ub = upload(ub);
+        a->angvel = angvel;
+        if (!a->Ua || !a->Ub || cudaMalloc(&a->step, sizeof(long long)) != cudaSuccess ||
+            cudaMalloc(&a->pbuf, sizeof(double) * kAdvGraphSteps) != cudaSuccess)
+            return ODIS_ERR_NOMEM;
+        cudaMemset(a->step, 0, sizeof(long long));
+    }
     const size_t E = a->Ep, N = a->Np;
     if (cudaMalloc(&a->v, sizeof(double) * E) != cudaSuccess || cudaMalloc(&a->eta, sizeof(double) * N) != cudaSuccess ||
         cudaMalloc(&a->hv, sizeof(double) * 3 * E) != cudaSuccess || cudaMalloc(&a->hp, sizeof(double) * 3 * N) != cudaSuccess ||
@@ -364,11 +400,13 @@ int adv_state_alloc(AdvDev* a, double h0)
     cudaMemset(a->eta, 0, sizeof(double) * N);
     cudaMemset(a->hv, 0, sizeof(double) * 3 * E);
     cudaMemset(a->hp, 0, sizeof(double) * 3 * N);
-    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads>>>(a->N, h0, a->eta, a->ht);
+    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads>>>(a->N, h0, a->eta, a->ht, nullptr);
     return cudaDeviceSynchronize() == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
 }
 
 AdvState adv_state(AdvDev* a) { return AdvState{a->v, a->eta, a->hv, a->hp, a->ht, a->U, a->uv}; }
+
+void adv_set_step(AdvDev* a, long long step, cudaStream_t s) { k_adv_set_step<<<1, 1, 0, s>>>(a->step, step); }
 
 void adv_step(AdvDev* a, const double* rbf, const int* cell_face, double g, double alpha, double h0, double dt,
               int iter, int init_load, cudaStream_t s)
@@ -377,20 +415,24 @@ void adv_step(AdvDev* a, const double* rbf, const int* cell_face, double g, doub
     // updateMomentum, advection branch: -g G eta + PV flux - G KE
     k_adv_grad<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, -g * (1 - 0.5 * 0.0), a->eta, a->dv0);
     adv_momentum(a, rbf, cell_face, a->dv0, a->v, a->ht, a->ek, s);
-    // the caller has put the forcing at t + dt in a->U
-    k_adv_vstep<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, alpha, dt, iter, init_load, a->dv0, a->U, a->v,
-                                          a->hv);
+    k_adv_vstep<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, alpha, dt, iter, init_load, a->dv0, a->Ua,
+                                          a->Ub, a->angvel, a->step, a->v, a->hv);
     // updateEta, advection branch: D (LSQ flux of h + eta)
     adv_lsq_flux(a, a->flux, a->v, a->ht, s);
     k_adv_estep<<<nb, kAdvThreads, 0, s>>>(a->dcol, a->dval, a->N, a->Np, dt, iter, init_load, a->flux, a->eta, a->hp);
 }
 
-void adv_thickness(AdvDev* a, double h0, cudaStream_t s)
+void adv_thickness(AdvDev* a, double h0, cudaStream_t s, bool advance)
 {
-    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->N, h0, a->eta, a->ht);
+    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->N, h0, a->eta, a->ht,
+                                                                                  advance ? a->step : nullptr);
 }
 
-int adv_kernels_per_step() { return 4 + adv_kernels_per_call() + 1; }
+double* adv_graph_power(AdvDev* a) { return a->pbuf; }
+cudaGraphExec_t* adv_graph(AdvDev* a) { return &a->graph; }
+
+int adv_kernels_per_step() { return 4 + adv_kernels_per_call(); }
+int adv_graph_steps() { return kAdvGraphSteps; }
 
 void adv_lsq_flux(AdvDev* a, double* flux, const double* v, const double* h_total, cudaStream_t s)
 {

@@ -22,15 +22,21 @@ double* adv_ekin_scratch(AdvDev* a);
 struct AdvState {
     double *v, *eta, *hv, *hp, *ht, *U, *uv;
 };
-int adv_state_alloc(AdvDev* a, double h0);
+// Ua/Ub: the forcing basis at the nodes, U(t) = cos(Omega t) Ua + sin(Omega t) Ub
+int adv_state_alloc(AdvDev* a, double h0, const std::vector<double>& Ua, const std::vector<double>& Ub, double angvel);
 AdvState adv_state(AdvDev* a);
-// one step of the advective loop up to the continuity update; the caller puts
-// the forcing at t + dt in AdvState.U first, and afterwards computes the power
-// from v and calls adv_thickness
+// one step of the advective loop up to the continuity update (forcing phase
+// from the device step counter, AB3 mode from iter); the caller then computes the
+// power from v and calls adv_thickness, which advances the counter
 void adv_step(AdvDev* a, const double* rbf, const int* cell_face, double g, double alpha, double h0, double dt,
               int iter, int init_load, cudaStream_t s);
-void adv_thickness(AdvDev* a, double h0, cudaStream_t s);
+void adv_thickness(AdvDev* a, double h0, cudaStream_t s, bool advance = true);
+void adv_set_step(AdvDev* a, long long step, cudaStream_t s);
 int adv_kernels_per_step();
+// captured graph of adv_graph_steps() steps (owned by AdvDev) and its power buffer
+int adv_graph_steps();
+double* adv_graph_power(AdvDev* a);
+cudaGraphExec_t* adv_graph(AdvDev* a);
 // flux[E]: the reference's interpolateLSQFlux of the column thickness h_total[N] with velocities v[E]
 void adv_lsq_flux(AdvDev* a, double* flux, const double* v, const double* h_total, cudaStream_t s);
 int adv_kernels_per_call();

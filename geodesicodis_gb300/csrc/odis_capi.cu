@@ -650,7 +650,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     if (p->advection) {            // the nonlinear loop has its own operators and reference-layout state
         c->persist_ok = false;
         st = adv_create(&c->adv, m, p->angvel, c->Ep, c->Np);
-        if (st == ODIS_OK) st = adv_state_alloc(c->adv, p->h);
+        if (st == ODIS_OK) st = adv_state_alloc(c->adv, p->h, Ua, Ub, p->angvel);
         if (st != ODIS_OK) return st;
     } else {
         st = choose_exec_path(c.get());
@@ -993,18 +993,46 @@ static odis_status run_advective(odis_ctx* c, int n, double* dpow)
 {
     const AdvState a = adv_state(c->adv);
     const odis_params& p = c->p;
-    for (int s = 0; s < n; s++) {
-        const int it = (int)c->iter;
-        const double t = p.dt * it + p.dt;
-        launch_forcing(c->trig, c->N, c->Np, a.U, p.potential, t, p.angvel, p.radius, p.love_reduct, p.ecc, p.obliq,
-                       c->stream);
+    const int G = adv_graph_steps();
+    const int per_step = adv_kernels_per_step() + 4;
+    double* scratch = c->d_partial + (size_t)c->fold_rows * c->eb;
+    auto step = [&](int it, double* out) {
         adv_step(c->adv, c->rbf, c->op64.cc.edge, p.g, p.alpha, p.h, p.dt, it, p.init_load, c->stream);
         launch_interp(c->op64.fc, c->nrm, c->E, c->Ep, a.uv, a.v, c->stream);
         launch_energy(c->area, c->E, p.alpha * 1000.0 * p.h, 4 * kPi * std::pow(c->r, 2.0), a.uv, nullptr,
-                      c->d_partial, dpow ? dpow + s : c->d_partial + (size_t)c->fold_rows * c->eb, c->stream);
+                      c->d_partial, out, c->stream);
         adv_thickness(c->adv, p.h, c->stream);
-        c->iter++;
-        c->launches += 1 + adv_kernels_per_step() + 3;
+    };
+    adv_set_step(c->adv, c->iter, c->stream);
+    c->launches += 1;
+    for (int done = 0; done < n;) {
+        const int it = (int)c->iter;
+        if ((it > 1 || p.init_load) && n - done >= G) {
+            // AB3 steps in whole chunks: one graph of G steps, captured once (AB3 mode
+            // fixed, forcing phase from the device step counter, power into the chunk buffer)
+            cudaGraphExec_t* ge = adv_graph(c->adv);
+            if (!*ge) {
+                cudaGraph_t gr = nullptr;
+                ODIS_CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+                for (int k = 0; k < G; k++) step(2, adv_graph_power(c->adv) + k);
+                ODIS_CK(cudaStreamEndCapture(c->stream, &gr));
+                const cudaError_t e = cudaGraphInstantiate(ge, gr, 0);
+                cudaGraphDestroy(gr);
+                if (e != cudaSuccess) { *ge = nullptr; return ODIS_ERR_CUDA; }
+            }
+            ODIS_CK(cudaGraphLaunch(*ge, c->stream));
+            if (dpow)
+                ODIS_CK(cudaMemcpyAsync(dpow + done, adv_graph_power(c->adv), sizeof(double) * G,
+                                        cudaMemcpyDeviceToDevice, c->stream));
+            c->iter += G;
+            done += G;
+            c->launches += (long long)G * per_step;
+        } else {
+            step(it, dpow ? dpow + done : scratch);
+            c->iter++;
+            done++;
+            c->launches += per_step;
+        }
     }
     ODIS_CK(cudaGetLastError());
     return ODIS_OK;
@@ -1196,7 +1224,7 @@ extern "C" odis_status odis_set_state(odis_ctx* c, int iter, const double* v, co
         if (eta) ODIS_CK(cudaMemcpy(a.eta, eta, sizeof(double) * c->N, cudaMemcpyHostToDevice));
         if (dvdt) ODIS_CK(cudaMemcpy(a.hv, dvdt, sizeof(double) * 3 * c->E, cudaMemcpyHostToDevice));
         if (detadt) ODIS_CK(cudaMemcpy(a.hp, detadt, sizeof(double) * 3 * c->N, cudaMemcpyHostToDevice));
-        adv_thickness(c->adv, c->p.h, c->stream);       // src/timeIntegrator.cpp:203
+        adv_thickness(c->adv, c->p.h, c->stream, false);   // src/timeIntegrator.cpp:203
         ODIS_CK(cudaStreamSynchronize(c->stream));
         return ODIS_OK;
     }
