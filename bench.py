@@ -133,6 +133,12 @@ def cpu_sample(n_steps: int, threads: int | None, with_sh: bool = True):
     from oracle import pyoracle as O
     env_threads = str(threads or os.cpu_count())
     os.environ["OMP_NUM_THREADS"] = env_threads
+    O.lib()
+    try:                        # the OpenMP runtime may already be up: set its team size directly
+        import ctypes
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(env_threads))
+    except OSError:
+        pass
     angvel, P, dt, n = O.derive_time(ANGVEL_IN, DT_TARGET)
     with tempfile.TemporaryDirectory() as d:
         grid = os.path.join(d, f"grid_{LEVEL}.txt")
@@ -379,6 +385,11 @@ def run_ours(args) -> dict:
         out["cpu_baseline"] = {"value": v, "unit": "cell-steps/s", "cores": os.cpu_count(), "kind": "port",
                                "sample": f"{args.cpu_sample_steps} LTE steps of the same level-6 FP64 + l_max=16 "
                                          f"workload, oracle C restatement with OpenMP over rows/cells"}
+        # the reference's own build is single-threaded: the same sample on one core
+        v1, _ = cpu_sample(max(20, args.cpu_sample_steps // 4), 1)
+        out["cpu_baseline_1thread"] = {"value": v1, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+                                       "sample": f"{max(20, args.cpu_sample_steps // 4)} steps of the same workload, "
+                                                 "one OpenMP thread (the reference's build is single-threaded)"}
     if D:
         barrier()              # the other replicas wait here while rank 0 measures the extras
     return out
@@ -549,6 +560,7 @@ def main():
                     help="run a short level-6 case for an ncu capture (no timing, no JSON)")
     ap.add_argument("--case-sh", type=int, default=0, help="self-gravity degree of --profile-case")
     ap.add_argument("--case-level", type=int, default=LEVEL, help="mesh level of --profile-case (stable dt off level 6)")
+    ap.add_argument("--case-advection", action="store_true", help="--profile-case fp64: the nonlinear (advection) loop")
     ap.add_argument("--sur-train", type=int, default=4096)
     ap.add_argument("--sur-test", type=int, default=512)
     ap.add_argument("--sur-level", type=int, default=5)
@@ -587,9 +599,10 @@ def main():
             dt = P / g.stable_steps_per_orbit(P, mesh.gravity_wave_omega(GRAV, H), 0.95)
         prec = {"fp64": g.FP64, "df64": g.DF64, "fp32": g.FP32}[args.profile_case]
         p = g.make_params(radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt, potential=g.POT_ECC,
-                          precision=prec, sh_lmax=args.case_sh, sh_factors=sh_factors(args.case_sh) if args.case_sh else None)
+                          precision=prec, sh_lmax=args.case_sh, sh_factors=sh_factors(args.case_sh) if args.case_sh else None,
+                          advection=1 if args.case_advection else 0)
         sol = g.Solver(p, mesh)
-        if args.case_graph:
+        if args.case_graph and not args.case_advection:
             sol.set_persistent(False)
         for _ in range(3):
             sol.run(max(1, args.case_steps // 3))
