@@ -70,7 +70,7 @@ def test_input_in_semantics(built, tmp_path):
     assert p.obliq == 0.2 * np.pi / 180.0                          # degrees -> radians
     assert p.love_reduct == 1.0 and p.potential == g.POT_ECC
     assert inp.grid_level == 5                                     # keys are case-insensitive
-    assert inp.advection == 0 and inp.fric_linear == 1 and inp.init_kind == 0
+    assert inp.advection == 0 and inp.params.advection == 0 and inp.fric_linear == 1 and inp.init_kind == 0
     assert p.radius == 252.1e3 and p.h == 1e4 and p.alpha == 1e-5 and p.g == 0.113
     assert inp.end_time == 10 and inp.output_time == 10
 
@@ -95,7 +95,7 @@ def test_reference_input_in_parses(built):
         pytest.skip("reference not mounted")
     inp = g.read_input(src)
     assert inp.params.potential == g.POT_OBLIQ_WEST
-    assert inp.advection == 1 and inp.grid_level == 6
+    assert inp.advection == 1 and inp.params.advection == 1 and inp.grid_level == 6
     assert inp.params.obliq == -2.0 * np.pi / 180.0
     assert inp.period == 2 * round(2 * np.pi / 7.292e-5 / 2)
 
