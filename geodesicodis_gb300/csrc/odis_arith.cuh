@@ -13,6 +13,8 @@ template <> struct Ar<double> {
     using V = double;
     __device__ static V zero() { return 0.0; }
     __device__ static V fma(V a, V b, V c) { return ::fma(a, b, c); }
+    __device__ static V fma_acc(V a, V b, V c) { return ::fma(a, b, c); }   // running sums (see Ar<df64>)
+    __device__ static V norm(V a) { return a; }
     __device__ static V mul(V a, V b) { return a * b; }
     __device__ static V add(V a, V b) { return a + b; }
     __device__ static V sub(V a, V b) { return a - b; }
@@ -30,6 +32,8 @@ template <> struct Ar<float> {
     using V = float;
     __device__ static V zero() { return 0.f; }
     __device__ static V fma(V a, V b, V c) { return fmaf(a, b, c); }
+    __device__ static V fma_acc(V a, V b, V c) { return fmaf(a, b, c); }
+    __device__ static V norm(V a) { return a; }
     __device__ static V mul(V a, V b) { return a * b; }
     __device__ static V add(V a, V b) { return a + b; }
     __device__ static V sub(V a, V b) { return a - b; }
@@ -46,6 +50,9 @@ template <> struct Ar<df64> {
     using V = df64;
     __device__ static V zero() { return df_make(0.f, 0.f); }
     __device__ static V fma(V a, V b, V c) { return df_fma(a, b, c); }
+    // running sums: no renormalisation per term; norm() before the sum is used
+    __device__ static V fma_acc(V a, V b, V c) { return df_fma_acc(a, b, c); }
+    __device__ static V norm(V a) { return df_norm(a); }
     __device__ static V mul(V a, V b) { return df_mul(a, b); }
     __device__ static V add(V a, V b) { return df_add(a, b); }
     __device__ static V sub(V a, V b) { return df_sub(a, b); }

@@ -104,10 +104,10 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
                 if (j < nl) {
                     T p, p2;
                     A::ld2(prow + (size_t)j * Np + i, p, p2);
-                    ac[j] = A::fma(p, ec, ac[j]);
-                    as[j] = A::fma(p, es, as[j]);
-                    bc[j] = A::fma(p2, ec2, bc[j]);
-                    bs[j] = A::fma(p2, es2, bs[j]);
+                    ac[j] = A::fma_acc(p, ec, ac[j]);
+                    as[j] = A::fma_acc(p, es, as[j]);
+                    bc[j] = A::fma_acc(p2, ec2, bc[j]);
+                    bs[j] = A::fma_acc(p2, es2, bs[j]);
                 }
             }
         }
@@ -120,14 +120,17 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
             for (int j = 0; j < kTileL; j++) {
                 if (j < nl) {
                     const T p = prow[(size_t)j * Np + i];
-                    ac[j] = A::fma(p, ec, ac[j]);
-                    as[j] = A::fma(p, es, as[j]);
+                    ac[j] = A::fma_acc(p, ec, ac[j]);
+                    as[j] = A::fma_acc(p, es, as[j]);
                 }
             }
         }
     }
 #pragma unroll
-    for (int j = 0; j < kTileL; j++) { ac[j] = A::add(ac[j], bc[j]); as[j] = A::add(as[j], bs[j]); }
+    for (int j = 0; j < kTileL; j++) {
+        ac[j] = A::add(A::norm(ac[j]), A::norm(bc[j]));
+        as[j] = A::add(A::norm(as[j]), A::norm(bs[j]));
+    }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j < kTileL; j++) {
@@ -211,12 +214,12 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
             else { c0 = cr[i]; c1 = cr[i2]; s0 = sr[i]; s1 = sr[i2]; }
             auto step = [&](int l, T p0, T p1) {
                 const T cc = c[sh_col(l, m, 0)];
-                a0 = A::fma(p0, cc, a0);
-                if (kCells == 2) a1 = A::fma(p1, cc, a1);
+                a0 = A::fma_acc(p0, cc, a0);
+                if (kCells == 2) a1 = A::fma_acc(p1, cc, a1);
                 if (m > 0) {
                     const T cs = c[sh_col(l, m, 1)];
-                    b0 = A::fma(p0, cs, b0);
-                    if (kCells == 2) b1 = A::fma(p1, cs, b1);
+                    b0 = A::fma_acc(p0, cs, b0);
+                    if (kCells == 2) b1 = A::fma_acc(p1, cs, b1);
                 }
             };
             int l = lstart;
@@ -239,8 +242,8 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
                 else { p0 = pr[i]; p1 = kCells == 2 ? pr[i2] : p0; }
                 step(l, p0, p1);
             }
-            u = A::fma(c0, a0, A::fma(s0, b0, u));
-            if (kCells == 2) u2 = A::fma(c1, a1, A::fma(s1, b1, u2));
+            u = A::fma(c0, A::norm(a0), A::fma(s0, A::norm(b0), u));
+            if (kCells == 2) u2 = A::fma(c1, A::norm(a1), A::fma(s1, A::norm(b1), u2));
         }
     }
 #pragma unroll
