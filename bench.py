@@ -359,7 +359,7 @@ def run_ours(args) -> dict:
            "variants_cell_steps_per_s": results,
            "nonlinear": {"cell_steps_per_s": results["fp64_advection"],
                          "method": "ODIS_FP64, advection true: momentum advection + LSQ thickness flux, "
-                                   "13 kernels per step, AB3 steps replayed from a 64-step CUDA graph",
+                                   "7 kernels per step, AB3 steps replayed from a 64-step CUDA graph",
                          "eta_gap_vs_linear": _rel(finals["fp64_advection"][1], finals["fp64_plain"][1]),
                          "power_gap_vs_linear": abs(finals["fp64_advection"][2] - finals["fp64_plain"][2])
                          / abs(finals["fp64_plain"][2])},

@@ -1,19 +1,32 @@
 // Nonlinear momentum advection (calculateMomentumAdvection, src/momAdvection.cpp:11-267)
-// on the device, FP64.
+// and the advective time step on the device, FP64.
 //
-// Per call:
+// Per momentum-advection call (odis_momentum_advection):
 //   k_adv_pv     per vertex: relative vorticity from the curl of v (three faces,
 //                ascending face order), thickness at the vertex from the three
 //                nodes' thicknesses weighted by control-volume area x kite
 //                fraction over the vertex area (Ringler et al. 2010 eq. 25),
 //                potential vorticity q = (zeta + f) / h
-//   k_adv_edge   per face: q and h averaged from the face's two vertices / nodes
-//   k_rbf + k_adv_ke  kinetic energy at the nodes from the RBF Cartesian velocity
+//   k_adv_edge   per face: q averaged from the face's two vertices, and the
+//                thickness flux h_e v_e with h_e averaged from its two nodes
+//   k_adv_node   per node: kinetic energy from the RBF Cartesian velocity
 //   k_adv_flux   per face: dvdt -= -sum_j w_j l_j / d_e (h_j v_j) (q_e + q_j) / 2
 //                (eq. 49), then dvdt += -(G KE)_e with the gradient's two terms in
 //                ascending node order
-// Every sum and product is evaluated in the reference's order, so the results
-// match the FP64 restatement to rounding.
+// Every sum and product is evaluated in the reference's order (the factor 1/2 of
+// eq. 49 is folded into the weights: a power-of-two scaling, so no rounding
+// changes), and the results match the FP64 restatement to rounding.
+//
+// One step of the advective loop (src/timeIntegrator.cpp:205-269) is seven kernels:
+//   k_adv_pv, k_adv_edge
+//   k_adv_node         also the forcing U at the nodes for this step's phase
+//   k_adv_flux<true>   dvdt starts from -g (G eta)_e
+//   k_adv_vstep        drag, G U, AB3 of v
+//   k_adv_lsq_power    interpolateLSQFlux of h + eta, then updateEnergy of the new
+//                      v (tangential velocity, e_i A_i block partials); the last
+//                      block to finish folds the partials in a fixed order
+//   k_adv_estep        D flux, AB3 of eta, h + eta for the next step; one extra
+//                      block advances the step counter and the next forcing phase
 #include "odis_advection.cuh"
 #include "odis_kernels.cuh"
 
@@ -27,6 +40,13 @@ namespace {
 
 constexpr int kAdvThreads = 256;
 constexpr int kAdvGraphSteps = 64;      // steps per captured graph of the advective loop
+
+__device__ __forceinline__ double adv_warp_sum(double x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    return x;
+}
 
 __global__ void k_adv_pv(const int* __restrict__ vface, const double* __restrict__ vcoef, const int* __restrict__ vnode,
                          const double* __restrict__ vR, const double* __restrict__ vinv, const double* __restrict__ vf,
@@ -49,56 +69,84 @@ __global__ void k_adv_pv(const int* __restrict__ vface, const double* __restrict
 }
 
 __global__ void k_adv_edge(const int* __restrict__ fvert, const int* __restrict__ fnode, int E, int Ep,
-                           const double* __restrict__ q, const double* __restrict__ h, double* __restrict__ qe,
-                           double* __restrict__ he)
+                           const double* __restrict__ q, const double* __restrict__ h, const double* __restrict__ v,
+                           double* __restrict__ qe, double* __restrict__ hve)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     qe[e] = 0.5 * (q[fvert[e]] + q[fvert[Ep + e]]);
-    he[e] = 0.5 * (h[fnode[e]] + h[fnode[Ep + e]]);
+    const double he = 0.5 * (h[fnode[e]] + h[fnode[Ep + e]]);
+    hve[e] = he * v[e];
 }
 
-__global__ void k_adv_ke(const double* __restrict__ uxyz, int N, double* __restrict__ ek)
+// kinetic energy 0.5 |u|^2 at the nodes, u from the RBF Cartesian reconstruction
+// (3 x 6 block per node, missing pentagon entries zero; same sums as k_rbf); with
+// U given, also the forcing U_i = cos(M) Ua_i + sin(M) Ub_i of the step's phase
+__global__ void k_adv_node(const double* __restrict__ rbf, const int* __restrict__ edge, int N, int Np,
+                           const double* __restrict__ v, double* __restrict__ ek, const double* __restrict__ phase,
+                           const double* __restrict__ Ua, const double* __restrict__ Ub, double* __restrict__ U)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    const double x = uxyz[3 * i], y = uxyz[3 * i + 1], z = uxyz[3 * i + 2];
-    ek[i] = 0.5 * (x * x + y * y + z * z);
+    double vf[kCellFaces];
+#pragma unroll
+    for (int j = 0; j < kCellFaces; j++) vf[j] = v[__ldg(&edge[j * Np + i])];
+    double u[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        double t = 0.0;
+#pragma unroll
+        for (int j = 0; j < kCellFaces; j++) t = fma(__ldg(&rbf[(c * kCellFaces + j) * Np + i]), vf[j], t);
+        u[c] = t;
+    }
+    ek[i] = 0.5 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    if (U) U[i] = __dadd_rn(__dmul_rn(phase[0], Ua[i]), __dmul_rn(phase[1], Ub[i]));
 }
 
-__global__ void k_adv_flux(const int* __restrict__ fr, const double* __restrict__ cw, const int* __restrict__ nfr,
+// kGrad: dvdt_e = alpha (G eta)_e (gradient row in ascending node order), else
+// dvdt_e as given; then the PV flux and -(G KE)_e
+template <bool kGrad>
+__global__ void k_adv_flux(const int* __restrict__ fr, const double* __restrict__ cwh, const int* __restrict__ nfr,
                            const int* __restrict__ gcol, const double* __restrict__ gval, int E, int Ep,
-                           const double* __restrict__ v, const double* __restrict__ qe, const double* __restrict__ he,
-                           const double* __restrict__ ek, double* __restrict__ dvdt)
+                           const double* __restrict__ qe, const double* __restrict__ hve, const double* __restrict__ ek,
+                           double alpha, const double* __restrict__ eta, double* __restrict__ dvdt)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
+    const int g0 = gcol[e], g1 = gcol[Ep + e];
+    const double w0 = gval[e], w1 = gval[Ep + e];
+    double d;
+    if constexpr (kGrad) {
+        double t = 0.0;
+        t = __dadd_rn(t, __dmul_rn(w0, eta[g0]));
+        t = __dadd_rn(t, __dmul_rn(w1, eta[g1]));
+        d = __dmul_rn(alpha, t);
+    } else {
+        d = dvdt[e];
+    }
     const double q0 = qe[e];
     double F = 0.0;
     const int n = nfr[e];
     for (int j = 0; j < n; j++) {
         const int f = fr[j * Ep + e];
-        F += cw[j * Ep + e] * (he[f] * v[f]) * (q0 + qe[f]) * 0.5;
+        F += cwh[j * Ep + e] * hve[f] * (q0 + qe[f]);
     }
-    double d = dvdt[e];
     d -= -F;
     double gk = 0.0;
-    gk += gval[e] * ek[gcol[e]];
-    gk += gval[Ep + e] * ek[gcol[Ep + e]];
+    gk += w0 * ek[g0];
+    gk += w1 * ek[g1];
     d += -gk;
     dvdt[e] = d;
 }
 
-// interpolateLSQFlux (src/interpolation.cpp:311-356), beta = 1: the directional
-// second derivatives at the face's two nodes (7-term rows, ascending node
-// order), then the third-order upwind-biased thickness flux.  Products and sums
-// are rounded separately, as in the unfused FP64 restatement.
-__global__ void k_lsq_flux(const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ dist,
-                           const int* __restrict__ fnode, int E, int Ep, const double* __restrict__ v,
-                           const double* __restrict__ h, double* __restrict__ flux)
+// interpolateLSQFlux (src/interpolation.cpp:311-356), beta = 1, at face e: the
+// directional second derivatives at the face's two nodes (7-term rows, ascending
+// node order), then the third-order upwind-biased thickness flux.  Products and
+// sums are rounded separately, as in the unfused FP64 restatement.
+__device__ __forceinline__ double lsq_flux_at(int e, int Ep, const int* __restrict__ col,
+                                              const double* __restrict__ val, const double* __restrict__ dist,
+                                              const int* __restrict__ fnode, double vel, const double* __restrict__ h)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
     const size_t R = (size_t)2 * Ep;
     double d2i = 0.0, d2o = 0.0;
 #pragma unroll
@@ -108,26 +156,22 @@ __global__ void k_lsq_flux(const int* __restrict__ col, const double* __restrict
     }
     const double dx = dist[e];
     const double dx2 = __dmul_rn(__dmul_rn(dx, dx), 1. / 12.0);
-    const double vel = v[e];
     const double a = __dmul_rn(__dmul_rn(vel, 0.5), __dadd_rn(h[fnode[e]], h[fnode[Ep + e]]));
     const double b = __dmul_rn(__dmul_rn(dx2, __dadd_rn(d2o, d2i)), vel);
     const double c = __dmul_rn(__dmul_rn(__dmul_rn(dx2, 1.0), fabs(vel)), __dsub_rn(d2o, d2i));
-    flux[e] = __dadd_rn(__dsub_rn(a, b), c);
+    return __dadd_rn(__dsub_rn(a, b), c);
 }
 
-// ---- the advective time step (src/timeIntegrator.cpp:205-269, advection true) ----
-
-// dvdt = alpha (G eta), the gradient row summed in ascending node order
-__global__ void k_adv_grad(const int* __restrict__ gcol, const double* __restrict__ gval, int E, int Ep, double alpha,
-                           const double* __restrict__ x, double* __restrict__ y)
+__global__ void k_lsq_flux(const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ dist,
+                           const int* __restrict__ fnode, int E, int Ep, const double* __restrict__ v,
+                           const double* __restrict__ h, double* __restrict__ flux)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    double t = 0.0;
-    t = __dadd_rn(t, __dmul_rn(gval[e], x[gcol[e]]));
-    t = __dadd_rn(t, __dmul_rn(gval[Ep + e], x[gcol[Ep + e]]));
-    y[e] = __dmul_rn(alpha, t);
+    flux[e] = lsq_flux_at(e, Ep, col, val, dist, fnode, v[e], h);
 }
+
+// ---- the advective time step (src/timeIntegrator.cpp:205-269, advection true) ----
 
 // integrateAB3scalar (src/temporalOperators.cpp:17-68) for one unknown; h = its [3] history
 __device__ __forceinline__ void ab3_ref(double& s, double* h, int iter, double dt, int init_load)
@@ -148,28 +192,16 @@ __device__ __forceinline__ void ab3_ref(double& s, double* h, int iter, double d
 
 // momentum update: drag_e = -alpha v_e + (G U)_e from the velocity before the
 // step, history slot 0 = dvdt, AB3, then v += dt drag (src/timeIntegrator.cpp:213-242).
-// The forcing at t + dt is cos(M) Ua + sin(M) Ub with M = Omega t, t = dt step + dt
-// and the step read from the device counter (one sincos per block).
+// U: the forcing at the nodes at t + dt (k_adv_node).
 __global__ void k_adv_vstep(const int* __restrict__ gcol, const double* __restrict__ gval, int E, int Ep, double alpha,
                             double dt, int iter, int init_load, const double* __restrict__ dv0,
-                            const double* __restrict__ Ua, const double* __restrict__ Ub, double angvel,
-                            const long long* __restrict__ step, double* __restrict__ v, double* __restrict__ hist)
+                            const double* __restrict__ U, double* __restrict__ v, double* __restrict__ hist)
 {
-    __shared__ double cs[2];
-    if (threadIdx.x == 0) {
-        const double t = dt * (double)(*step) + dt;
-        sincos(angvel * t, &cs[1], &cs[0]);
-    }
-    __syncthreads();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    const double c = cs[0], sn = cs[1];
-    const int n0 = gcol[e], n1 = gcol[Ep + e];
-    const double u0 = __dadd_rn(__dmul_rn(c, Ua[n0]), __dmul_rn(sn, Ub[n0]));
-    const double u1 = __dadd_rn(__dmul_rn(c, Ua[n1]), __dmul_rn(sn, Ub[n1]));
     double gu = 0.0;
-    gu = __dadd_rn(gu, __dmul_rn(gval[e], u0));
-    gu = __dadd_rn(gu, __dmul_rn(gval[Ep + e], u1));
+    gu = __dadd_rn(gu, __dmul_rn(gval[e], U[gcol[e]]));
+    gu = __dadd_rn(gu, __dmul_rn(gval[Ep + e], U[gcol[Ep + e]]));
     gu = __dadd_rn(0.0, __dmul_rn(1.0, gu));
     double ve = v[e];
     const double drag = __dadd_rn(__dadd_rn(0.0, __dmul_rn(1.0, __dmul_rn(-alpha, ve))), gu);
@@ -179,12 +211,98 @@ __global__ void k_adv_vstep(const int* __restrict__ gcol, const double* __restri
     v[e] = __dadd_rn(ve, __dmul_rn(dt, drag));
 }
 
-// continuity update: detadt = D flux (cell's faces in ascending face order),
-// history slot 0, AB3 (src/timeIntegrator.cpp:249-253)
-__global__ void k_adv_estep(const int* __restrict__ dcol, const double* __restrict__ dval, int N, int Np, double dt,
-                            int iter, int init_load, const double* __restrict__ flux, double* __restrict__ eta,
-                            double* __restrict__ hist)
+struct PowerArgs {
+    const int* nbr;       // [10][Ep] TRiSK neighbour faces (zero weight in unused slots)
+    const double* w;      // [10][Ep] TRiSK weights
+    const double* nrm;    // [2][Ep] face normal (east, north)
+    const double* area;   // [Ep] face area
+    double coef;          // alpha 1000 h
+    double divisor;       // 4 pi r^2
+    double* part;         // [blocks] partial sums
+    unsigned* count;      // finished blocks of the launch (0 between launches)
+    double* out;          // the step's power
+};
+
+// LSQ thickness flux of the step, then updateEnergy (LINEAR) of the updated v:
+// tangential velocity t_e = sum_k w_k v_k, (u, w) = (nx v + ny t, ny v - nx t),
+// e_i = alpha 1000 h |(u, w)|^2, and the block sum of e_i A_i.  The last block to
+// finish sums the block partials in a fixed order (lane-strided, then the warp
+// tree), so the power does not depend on which block finishes last.
+__global__ void __launch_bounds__(kAdvThreads)
+k_adv_lsq_power(const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ dist,
+                const int* __restrict__ fnode, int E, int Ep, const double* __restrict__ v, const double* __restrict__ h,
+                double* __restrict__ flux, PowerArgs pa)
 {
+    __shared__ double s_red[kAdvThreads / 32];
+    __shared__ bool s_last;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    double x = 0.0;
+    if (e < E) {
+        const double ve = v[e];
+        flux[e] = lsq_flux_at(e, Ep, col, val, dist, fnode, ve, h);
+        double t = 0.0;
+#pragma unroll
+        for (int k = 0; k < kTrisk; k++) t = fma(pa.w[k * Ep + e], v[pa.nbr[k * Ep + e]], t);
+        const double nx = pa.nrm[e], ny = pa.nrm[Ep + e];
+        const double u = nx * ve + ny * t;
+        const double w = ny * ve + (-nx) * t;
+        const double ei = pa.coef * (u * u + w * w);
+        x = ei * pa.area[e];
+    }
+    x = adv_warp_sum(x);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) s_red[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        double s = lane < kAdvThreads / 32 ? s_red[lane] : 0.0;
+        s = adv_warp_sum(s);
+        if (lane == 0) {
+            pa.part[blockIdx.x] = s;
+            __threadfence();
+            s_last = atomicAdd(pa.count, 1u) == gridDim.x - 1;
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    if (!s_last || wid != 0) return;
+    __threadfence();
+    double s = 0.0;
+    for (int k = lane; k < (int)gridDim.x; k += 32) s += __ldcg(pa.part + k);
+    s = adv_warp_sum(s);
+    if (lane == 0) {
+        *pa.out = s / pa.divisor;
+        *pa.count = 0u;
+    }
+}
+
+// forcing phase (cos, sin) of M = Omega t, t = dt step + dt (src/timeIntegrator.cpp:218)
+__device__ __forceinline__ void adv_phase(long long step, double dt, double angvel, double* phase)
+{
+    const double t = dt * (double)step + dt;
+    double sn, c;
+    sincos(angvel * t, &sn, &c);
+    phase[0] = c;
+    phase[1] = sn;
+}
+
+// continuity update: detadt = D flux (cell's faces in ascending face order),
+// history slot 0, AB3 (src/timeIntegrator.cpp:249-253), and the column thickness
+// h + eta of the next step.  The launch has one block more than the cells need:
+// its first thread advances the step counter and computes the next step's phase,
+// alongside the cell blocks.
+__global__ void k_adv_estep(const int* __restrict__ dcol, const double* __restrict__ dval, int N, int Np, double dt,
+                            int iter, int init_load, double h0, const double* __restrict__ flux,
+                            double* __restrict__ eta, double* __restrict__ hist, double* __restrict__ ht,
+                            long long* __restrict__ step, double angvel, double* __restrict__ phase)
+{
+    if (blockIdx.x == gridDim.x - 1) {
+        if (threadIdx.x == 0) {
+            const long long s = *step + 1;
+            *step = s;
+            adv_phase(s, dt, angvel, phase);
+        }
+        return;
+    }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     double t = 0.0;
@@ -195,18 +313,21 @@ __global__ void k_adv_estep(const int* __restrict__ dcol, const double* __restri
     double s = eta[i];
     ab3_ref(s, h, iter, dt, init_load);
     eta[i] = s;
+    ht[i] = __dadd_rn(h0, s);
 }
 
-// column thickness for the next step; the first thread also advances the step counter
-__global__ void k_adv_thickness(int N, double h0, const double* __restrict__ eta, double* __restrict__ ht,
-                                long long* __restrict__ step)
+// column thickness h + eta (after a state is loaded)
+__global__ void k_adv_thickness(int N, double h0, const double* __restrict__ eta, double* __restrict__ ht)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < N) ht[i] = __dadd_rn(h0, eta[i]);
-    if (i == 0 && step) *step += 1;
 }
 
-__global__ void k_adv_set_step(long long* step, long long v) { *step = v; }
+__global__ void k_adv_set_step(long long* step, long long v, double dt, double angvel, double* phase)
+{
+    *step = v;
+    adv_phase(v, dt, angvel, phase);
+}
 
 template <class T>
 T* upload(const std::vector<T>& h)
@@ -226,19 +347,22 @@ struct AdvDev {
     int V = 0, Vp = 0, E = 0, Ep = 0, N = 0, Np = 0;
     int *vface = nullptr, *vnode = nullptr, *fvert = nullptr, *fnode = nullptr, *fr = nullptr, *nfr = nullptr,
         *gcol = nullptr;
-    double *vcoef = nullptr, *vR = nullptr, *vinv = nullptr, *vf = nullptr, *cvA = nullptr, *cw = nullptr,
+    double *vcoef = nullptr, *vR = nullptr, *vinv = nullptr, *vf = nullptr, *cvA = nullptr, *cwh = nullptr,
            *gval = nullptr;
-    double *q = nullptr, *qe = nullptr, *he = nullptr, *uxyz = nullptr, *ek = nullptr;
+    double *q = nullptr, *qe = nullptr, *hve = nullptr, *ek = nullptr;
     int* lcol = nullptr;         // [7][2 Ep] operatorDirectionalSecondDeriv rows
     double *lval = nullptr, *dist = nullptr;
     int* dcol = nullptr;         // [6][Np] divergence rows, ascending face order (padded with zero weights)
     double* dval = nullptr;
     // state of an advective run, in the reference's layout
     double *v = nullptr, *eta = nullptr, *hv = nullptr, *hp = nullptr, *ht = nullptr;
-    double *U = nullptr, *dv0 = nullptr, *flux = nullptr, *uv = nullptr;
+    double *U = nullptr, *dv0 = nullptr, *flux = nullptr;
     double *Ua = nullptr, *Ub = nullptr;    // forcing U = cos(M) Ua + sin(M) Ub at the nodes
     double angvel = 0.0;
     long long* step = nullptr;              // device step counter (forcing phase)
+    double* phase = nullptr;                // [2] cos, sin of the counter's forcing phase
+    double* part = nullptr;                 // [face blocks] power partial sums
+    unsigned* count = nullptr;              // finished blocks of k_adv_lsq_power
     double* pbuf = nullptr;                 // [kAdvGraphSteps] power of a graph chunk
     cudaGraphExec_t graph = nullptr;
 };
@@ -248,10 +372,11 @@ void adv_destroy(AdvDev* a)
     if (!a) return;
     for (void* p : {(void*)a->vface, (void*)a->vnode, (void*)a->fvert, (void*)a->fnode, (void*)a->fr, (void*)a->nfr,
                     (void*)a->gcol, (void*)a->vcoef, (void*)a->vR, (void*)a->vinv, (void*)a->vf, (void*)a->cvA,
-                    (void*)a->cw, (void*)a->gval, (void*)a->q, (void*)a->qe, (void*)a->he, (void*)a->uxyz,
-                    (void*)a->ek, (void*)a->lcol, (void*)a->lval, (void*)a->dist, (void*)a->dcol, (void*)a->dval,
-                    (void*)a->v, (void*)a->eta, (void*)a->hv, (void*)a->hp, (void*)a->ht, (void*)a->U, (void*)a->dv0,
-                    (void*)a->flux, (void*)a->uv, (void*)a->Ua, (void*)a->Ub, (void*)a->step, (void*)a->pbuf})
+                    (void*)a->cwh, (void*)a->gval, (void*)a->q, (void*)a->qe, (void*)a->hve, (void*)a->ek,
+                    (void*)a->lcol, (void*)a->lval, (void*)a->dist, (void*)a->dcol, (void*)a->dval, (void*)a->v,
+                    (void*)a->eta, (void*)a->hv, (void*)a->hp, (void*)a->ht, (void*)a->U, (void*)a->dv0,
+                    (void*)a->flux, (void*)a->Ua, (void*)a->Ub, (void*)a->step, (void*)a->phase, (void*)a->part,
+                    (void*)a->count, (void*)a->pbuf})
         cudaFree(p);
     if (a->graph) cudaGraphExecDestroy(a->graph);
     delete a;
@@ -284,7 +409,7 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
     for (int i = 0; i < m.N; i++) cvA[i] = m.cv_area[i];
     std::vector<int> fvert((size_t)2 * Ep, 0), fnode((size_t)2 * Ep, 0), fr((size_t)10 * Ep, 0), nfr(Ep, 0),
         gcol((size_t)2 * Ep, 0);
-    std::vector<double> cw((size_t)10 * Ep, 0.0), gval((size_t)2 * Ep, 0.0);
+    std::vector<double> cwh((size_t)10 * Ep, 0.0), gval((size_t)2 * Ep, 0.0);
     for (int e = 0; e < E; e++) {
         fvert[e] = m.face_verts[e * 2];
         fvert[(size_t)Ep + e] = m.face_verts[e * 2 + 1];
@@ -295,7 +420,7 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
         for (int j = 0; j < m.interp_n[e]; j++) {
             const int f = m.interp_friends[e * 10 + j];
             fr[(size_t)j * Ep + e] = f;
-            cw[(size_t)j * Ep + e] = m.interp_w[e * 10 + j] * m.face_len[f] * dr;
+            cwh[(size_t)j * Ep + e] = m.interp_w[e * 10 + j] * m.face_len[f] * dr * 0.5;
         }
         // operatorGradient row (src/mesh.cpp:3005-3120), ascending node order
         const int n0 = m.face_nodes[e * 2], n1 = m.face_nodes[e * 2 + 1];
@@ -346,12 +471,11 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
     a->vface = upload(vface); a->vnode = upload(vnode); a->vcoef = upload(vcoef); a->vR = upload(vR);
     a->vinv = upload(vinv); a->vf = upload(vf); a->cvA = upload(cvA);
     a->fvert = upload(fvert); a->fnode = upload(fnode); a->fr = upload(fr); a->nfr = upload(nfr);
-    a->cw = upload(cw); a->gcol = upload(gcol); a->gval = upload(gval);
+    a->cwh = upload(cwh); a->gcol = upload(gcol); a->gval = upload(gval);
     bool ok = a->vface && a->vnode && a->vcoef && a->vR && a->vinv && a->vf && a->cvA && a->fvert && a->fnode &&
-              a->fr && a->nfr && a->cw && a->gcol && a->gval;
+              a->fr && a->nfr && a->cwh && a->gcol && a->gval;
     ok = ok && cudaMalloc(&a->q, sizeof(double) * Vp) == cudaSuccess &&
-         cudaMalloc(&a->qe, sizeof(double) * Ep) == cudaSuccess && cudaMalloc(&a->he, sizeof(double) * Ep) == cudaSuccess &&
-         cudaMalloc(&a->uxyz, sizeof(double) * 3 * (size_t)Np) == cudaSuccess &&
+         cudaMalloc(&a->qe, sizeof(double) * Ep) == cudaSuccess && cudaMalloc(&a->hve, sizeof(double) * Ep) == cudaSuccess &&
          cudaMalloc(&a->ek, sizeof(double) * Np) == cudaSuccess;
     if (!ok) { adv_destroy(a); return ODIS_ERR_NOMEM; }
     *out = a;
@@ -360,20 +484,26 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
 
 double* adv_ekin_scratch(AdvDev* a) { return a->ek; }
 
-void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dvdt, const double* v,
-                  const double* h_total, double* ekin, cudaStream_t s)
+static void momentum_head(AdvDev* a, const double* rbf, const int* cell_face, const double* v, const double* h_total,
+                          double* ekin, double* U, cudaStream_t s)
 {
     k_adv_pv<<<(a->V + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->vface, a->vcoef, a->vnode, a->vR, a->vinv,
                                                                            a->vf, a->cvA, a->V, a->Vp, v, h_total, a->q);
     k_adv_edge<<<(a->E + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->fvert, a->fnode, a->E, a->Ep, a->q,
-                                                                             h_total, a->qe, a->he);
-    launch_rbf(rbf, cell_face, a->N, a->Np, v, a->uxyz, s);
-    k_adv_ke<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->uxyz, a->N, ekin);
-    k_adv_flux<<<(a->E + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->fr, a->cw, a->nfr, a->gcol, a->gval,
-                                                                             a->E, a->Ep, v, a->qe, a->he, ekin, dvdt);
+                                                                             h_total, v, a->qe, a->hve);
+    k_adv_node<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(rbf, cell_face, a->N, a->Np, v, ekin,
+                                                                             a->phase, a->Ua, a->Ub, U);
 }
 
-int adv_kernels_per_call() { return 5; }
+void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dvdt, const double* v,
+                  const double* h_total, double* ekin, cudaStream_t s)
+{
+    momentum_head(a, rbf, cell_face, v, h_total, ekin, nullptr, s);
+    k_adv_flux<false><<<(a->E + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(
+        a->fr, a->cwh, a->nfr, a->gcol, a->gval, a->E, a->Ep, a->qe, a->hve, ekin, 0.0, nullptr, dvdt);
+}
+
+int adv_kernels_per_call() { return 4; }
 
 int adv_state_alloc(AdvDev* a, double h0, const std::vector<double>& Ua, const std::vector<double>& Ub, double angvel)
 {
@@ -384,54 +514,65 @@ int adv_state_alloc(AdvDev* a, double h0, const std::vector<double>& Ua, const s
         a->Ua = upload(ua);
         a->Ub = upload(ub);
         a->angvel = angvel;
+        const int eb = (a->E + kAdvThreads - 1) / kAdvThreads;
         if (!a->Ua || !a->Ub || cudaMalloc(&a->step, sizeof(long long)) != cudaSuccess ||
+            cudaMalloc(&a->phase, sizeof(double) * 2) != cudaSuccess ||
+            cudaMalloc(&a->part, sizeof(double) * eb) != cudaSuccess ||
+            cudaMalloc(&a->count, sizeof(unsigned)) != cudaSuccess ||
             cudaMalloc(&a->pbuf, sizeof(double) * kAdvGraphSteps) != cudaSuccess)
             return ODIS_ERR_NOMEM;
         cudaMemset(a->step, 0, sizeof(long long));
+        cudaMemset(a->phase, 0, sizeof(double) * 2);
+        cudaMemset(a->count, 0, sizeof(unsigned));
     }
     const size_t E = a->Ep, N = a->Np;
     if (cudaMalloc(&a->v, sizeof(double) * E) != cudaSuccess || cudaMalloc(&a->eta, sizeof(double) * N) != cudaSuccess ||
         cudaMalloc(&a->hv, sizeof(double) * 3 * E) != cudaSuccess || cudaMalloc(&a->hp, sizeof(double) * 3 * N) != cudaSuccess ||
         cudaMalloc(&a->ht, sizeof(double) * N) != cudaSuccess || cudaMalloc(&a->U, sizeof(double) * N) != cudaSuccess ||
-        cudaMalloc(&a->dv0, sizeof(double) * E) != cudaSuccess || cudaMalloc(&a->flux, sizeof(double) * E) != cudaSuccess ||
-        cudaMalloc(&a->uv, sizeof(double) * 2 * E) != cudaSuccess)
+        cudaMalloc(&a->dv0, sizeof(double) * E) != cudaSuccess || cudaMalloc(&a->flux, sizeof(double) * E) != cudaSuccess)
         return ODIS_ERR_NOMEM;
     cudaMemset(a->v, 0, sizeof(double) * E);
     cudaMemset(a->eta, 0, sizeof(double) * N);
     cudaMemset(a->hv, 0, sizeof(double) * 3 * E);
     cudaMemset(a->hp, 0, sizeof(double) * 3 * N);
-    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads>>>(a->N, h0, a->eta, a->ht, nullptr);
+    cudaMemset(a->U, 0, sizeof(double) * N);
+    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads>>>(a->N, h0, a->eta, a->ht);
     return cudaDeviceSynchronize() == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
 }
 
-AdvState adv_state(AdvDev* a) { return AdvState{a->v, a->eta, a->hv, a->hp, a->ht, a->U, a->uv}; }
+AdvState adv_state(AdvDev* a) { return AdvState{a->v, a->eta, a->hv, a->hp, a->ht, a->U}; }
 
-void adv_set_step(AdvDev* a, long long step, cudaStream_t s) { k_adv_set_step<<<1, 1, 0, s>>>(a->step, step); }
+void adv_set_step(AdvDev* a, long long step, double dt, cudaStream_t s)
+{
+    k_adv_set_step<<<1, 1, 0, s>>>(a->step, step, dt, a->angvel, a->phase);
+}
 
-void adv_step(AdvDev* a, const double* rbf, const int* cell_face, double g, double alpha, double h0, double dt,
-              int iter, int init_load, cudaStream_t s)
+void adv_step(AdvDev* a, const AdvStepArgs& x, int iter, double* power, cudaStream_t s)
 {
     const int eb = (a->E + kAdvThreads - 1) / kAdvThreads, nb = (a->N + kAdvThreads - 1) / kAdvThreads;
     // updateMomentum, advection branch: -g G eta + PV flux - G KE
-    k_adv_grad<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, -g * (1 - 0.5 * 0.0), a->eta, a->dv0);
-    adv_momentum(a, rbf, cell_face, a->dv0, a->v, a->ht, a->ek, s);
-    k_adv_vstep<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, alpha, dt, iter, init_load, a->dv0, a->Ua,
-                                          a->Ub, a->angvel, a->step, a->v, a->hv);
-    // updateEta, advection branch: D (LSQ flux of h + eta)
-    adv_lsq_flux(a, a->flux, a->v, a->ht, s);
-    k_adv_estep<<<nb, kAdvThreads, 0, s>>>(a->dcol, a->dval, a->N, a->Np, dt, iter, init_load, a->flux, a->eta, a->hp);
+    momentum_head(a, x.rbf, x.cell_face, a->v, a->ht, a->ek, a->U, s);
+    k_adv_flux<true><<<eb, kAdvThreads, 0, s>>>(a->fr, a->cwh, a->nfr, a->gcol, a->gval, a->E, a->Ep, a->qe, a->hve,
+                                                a->ek, -x.g * (1 - 0.5 * 0.0), a->eta, a->dv0);
+    k_adv_vstep<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, x.alpha, x.dt, iter, x.init_load, a->dv0,
+                                          a->U, a->v, a->hv);
+    // updateEta, advection branch: D (LSQ flux of h + eta); updateEnergy of the new v
+    const PowerArgs pa{x.nbr, x.w, x.nrm, x.area, x.alpha * 1000.0 * x.h0, x.divisor, a->part, a->count, power};
+    k_adv_lsq_power<<<eb, kAdvThreads, 0, s>>>(a->lcol, a->lval, a->dist, a->fnode, a->E, a->Ep, a->v, a->ht, a->flux,
+                                              pa);
+    k_adv_estep<<<nb + 1, kAdvThreads, 0, s>>>(a->dcol, a->dval, a->N, a->Np, x.dt, iter, x.init_load, x.h0, a->flux,
+                                              a->eta, a->hp, a->ht, a->step, a->angvel, a->phase);
 }
 
-void adv_thickness(AdvDev* a, double h0, cudaStream_t s, bool advance)
+void adv_thickness(AdvDev* a, double h0, cudaStream_t s)
 {
-    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->N, h0, a->eta, a->ht,
-                                                                                  advance ? a->step : nullptr);
+    k_adv_thickness<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->N, h0, a->eta, a->ht);
 }
 
 double* adv_graph_power(AdvDev* a) { return a->pbuf; }
 cudaGraphExec_t* adv_graph(AdvDev* a) { return &a->graph; }
 
-int adv_kernels_per_step() { return 4 + adv_kernels_per_call(); }
+int adv_kernels_per_step() { return 7; }
 int adv_graph_steps() { return kAdvGraphSteps; }
 
 void adv_lsq_flux(AdvDev* a, double* flux, const double* v, const double* h_total, cudaStream_t s)

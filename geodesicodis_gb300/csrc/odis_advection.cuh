@@ -18,20 +18,33 @@ void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dv
                   const double* h_total, double* ekin, cudaStream_t s);
 double* adv_ekin_scratch(AdvDev* a);
 // state of an advective run, reference layout: v[E], eta[N], dvdt history [E][3],
-// detadt history [N][3], column thickness h + eta [N], forcing [N], uv [E][2]
+// detadt history [N][3], column thickness h + eta [N], forcing [N]
 struct AdvState {
-    double *v, *eta, *hv, *hp, *ht, *U, *uv;
+    double *v, *eta, *hv, *hp, *ht, *U;
 };
 // Ua/Ub: the forcing basis at the nodes, U(t) = cos(Omega t) Ua + sin(Omega t) Ub
 int adv_state_alloc(AdvDev* a, double h0, const std::vector<double>& Ua, const std::vector<double>& Ub, double angvel);
 AdvState adv_state(AdvDev* a);
-// one step of the advective loop up to the continuity update (forcing phase
-// from the device step counter, AB3 mode from iter); the caller then computes the
-// power from v and calls adv_thickness, which advances the counter
-void adv_step(AdvDev* a, const double* rbf, const int* cell_face, double g, double alpha, double h0, double dt,
-              int iter, int init_load, cudaStream_t s);
-void adv_thickness(AdvDev* a, double h0, cudaStream_t s, bool advance = true);
-void adv_set_step(AdvDev* a, long long step, cudaStream_t s);
+// what one advective step needs from the context
+struct AdvStepArgs {
+    const double* rbf;        // [3][6][Np] Cartesian reconstruction blocks
+    const int* cell_face;     // [6][Np] cell-face table
+    const int* nbr;           // [10][Ep] TRiSK neighbour faces
+    const double* w;          // [10][Ep] TRiSK weights (tangential velocity)
+    const double* nrm;        // [2][Ep] face normals
+    const double* area;       // [Ep] face areas
+    double g, alpha, h0, dt;
+    double divisor;           // 4 pi r^2
+    int init_load;
+};
+// one whole step of the advective loop (7 kernels): momentum with advection, the
+// continuity update, the power of the updated velocity into *power (device), and
+// h + eta, step counter and forcing phase for the next step.  AB3 mode from iter.
+void adv_step(AdvDev* a, const AdvStepArgs& x, int iter, double* power, cudaStream_t s);
+// h + eta from the current eta (after a state is loaded)
+void adv_thickness(AdvDev* a, double h0, cudaStream_t s);
+// step counter and the forcing phase of that step
+void adv_set_step(AdvDev* a, long long step, double dt, cudaStream_t s);
 int adv_kernels_per_step();
 // captured graph of adv_graph_steps() steps (owned by AdvDev) and its power buffer
 int adv_graph_steps();

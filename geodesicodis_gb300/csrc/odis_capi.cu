@@ -991,19 +991,13 @@ static int run_chunk(odis_ctx* c, int n, double* dpow)
 // the dissipated power from the new velocity, then the column thickness.
 static odis_status run_advective(odis_ctx* c, int n, double* dpow)
 {
-    const AdvState a = adv_state(c->adv);
     const odis_params& p = c->p;
     const int G = adv_graph_steps();
-    const int per_step = adv_kernels_per_step() + 4;
-    double* scratch = c->d_partial + (size_t)c->fold_rows * c->eb;
-    auto step = [&](int it, double* out) {
-        adv_step(c->adv, c->rbf, c->op64.cc.edge, p.g, p.alpha, p.h, p.dt, it, p.init_load, c->stream);
-        launch_interp(c->op64.fc, c->nrm, c->E, c->Ep, a.uv, a.v, c->stream);
-        launch_energy(c->area, c->E, p.alpha * 1000.0 * p.h, 4 * kPi * std::pow(c->r, 2.0), a.uv, nullptr,
-                      c->d_partial, out, c->stream);
-        adv_thickness(c->adv, p.h, c->stream);
-    };
-    adv_set_step(c->adv, c->iter, c->stream);
+    const int per_step = adv_kernels_per_step();
+    const AdvStepArgs x{c->rbf, c->op64.cc.edge, c->op64.fc.nbr, c->op64.fc.w, c->nrm, c->area, p.g, p.alpha, p.h,
+                        p.dt, 4 * kPi * std::pow(c->r, 2.0), p.init_load};
+    auto step = [&](int it, double* out) { adv_step(c->adv, x, it, out, c->stream); };
+    adv_set_step(c->adv, c->iter, p.dt, c->stream);
     c->launches += 1;
     for (int done = 0; done < n;) {
         const int it = (int)c->iter;
@@ -1028,7 +1022,7 @@ static odis_status run_advective(odis_ctx* c, int n, double* dpow)
             done += G;
             c->launches += (long long)G * per_step;
         } else {
-            step(it, dpow ? dpow + done : scratch);
+            step(it, dpow + done);
             c->iter++;
             done++;
             c->launches += per_step;
@@ -1224,7 +1218,7 @@ extern "C" odis_status odis_set_state(odis_ctx* c, int iter, const double* v, co
         if (eta) ODIS_CK(cudaMemcpy(a.eta, eta, sizeof(double) * c->N, cudaMemcpyHostToDevice));
         if (dvdt) ODIS_CK(cudaMemcpy(a.hv, dvdt, sizeof(double) * 3 * c->E, cudaMemcpyHostToDevice));
         if (detadt) ODIS_CK(cudaMemcpy(a.hp, detadt, sizeof(double) * 3 * c->N, cudaMemcpyHostToDevice));
-        adv_thickness(c->adv, c->p.h, c->stream, false);   // src/timeIntegrator.cpp:203
+        adv_thickness(c->adv, c->p.h, c->stream);   // src/timeIntegrator.cpp:203
         ODIS_CK(cudaStreamSynchronize(c->stream));
         return ODIS_OK;
     }
