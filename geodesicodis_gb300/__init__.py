@@ -113,6 +113,9 @@ _SIGS = {
     "odis_batch_get_mesh_members": ([_V, C.c_int, _D, _D], C.c_int),
     "odis_batch_set_mesh_members": ([_V, C.c_int, _D, _D], C.c_int),
     "odis_batch_project": ([_V, C.c_int, _V, C.c_int, _V, C.c_int, _D, C.c_int], C.c_int),
+    "odis_h5_create": ([C.c_char_p, C.c_int, C.POINTER(C.c_char_p), _I, C.POINTER(C.c_longlong), C.POINTER(_V)], C.c_int),
+    "odis_h5_write_rows": ([_V, C.c_int, C.c_longlong, C.c_longlong, _V], C.c_int),
+    "odis_h5_close": ([_V], C.c_int),
     "odis_mlp_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(_V)], C.c_int),
     "odis_mlp_destroy": ([_V], None),
     "odis_mlp_num_params": ([_V, C.POINTER(C.c_longlong)], C.c_int),
@@ -155,6 +158,50 @@ def _vp(a: np.ndarray):
 def generate_grid_file(level: int, path: str | os.PathLike) -> None:
     """Icosahedral grid at `level` (10*4^level+2 cells) in the reference grid-file format."""
     _ck(lib().odis_grid_generate_file(int(level), os.fsencode(str(path))), "odis_grid_generate_file")
+
+
+class H5Writer:
+    """DATA/data.h5-style output (src/outFiles.cpp:138-823): float32 datasets of
+    rank 1 or 2 in the root group of an HDF5 file, written by the library's own
+    writer (odis_h5_*).  `datasets` is a list of (name, shape); storage is
+    zero-filled at creation and rows are written in place."""
+
+    def __init__(self, path: str | os.PathLike, datasets):
+        names = [str(n).encode() for n, _ in datasets]
+        shapes = [tuple(int(x) for x in sh) for _, sh in datasets]
+        arr = (C.c_char_p * len(names))(*names)
+        ranks = np.array([len(sh) for sh in shapes], np.int32)
+        dims = np.array([[sh[0], sh[1] if len(sh) > 1 else 0] for sh in shapes], np.int64).ravel()
+        self.shapes = shapes
+        self.index = {n: k for k, (n, _) in enumerate(datasets)}
+        h = _V()
+        _ck(lib().odis_h5_create(os.fsencode(str(path)), len(names), arr, ranks.ctypes.data_as(_I),
+                                 dims.ctypes.data_as(C.POINTER(C.c_longlong)), C.byref(h)), "odis_h5_create")
+        self._h = h
+
+    def write_rows(self, name: str, row0: int, rows) -> None:
+        k = self.index[name]
+        a = np.ascontiguousarray(rows, dtype=np.float32)
+        per_row = self.shapes[k][1] if len(self.shapes[k]) == 2 else 1
+        n = a.size // per_row
+        if a.size != n * per_row:
+            raise OdisError(ERR_ARG, f"{name}: {a.size} values are not whole rows of {per_row}")
+        _ck(lib().odis_h5_write_rows(self._h, k, int(row0), int(n), _vp(a)), "odis_h5_write_rows")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            h, self._h = self._h, None
+            _ck(lib().odis_h5_close(h), "odis_h5_close")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _lib is not None:
+            _lib.odis_h5_close(self._h)
 
 
 def derive_time(angvel_in: float, dt_target: float):

@@ -9,8 +9,10 @@
 // to stdout and OUTPUT.txt, and writes the final state back in the
 // InitialConditions format.  DATA/power.txt gets one "orbit  W/m^2  GW" line
 // per output interval, DATA/final_nodes.txt the final displacement and Cartesian
-// velocity (RBF reconstruction) per node; the HDF5 field dumps (src/outFiles.cpp)
-// are not written.
+// velocity (RBF reconstruction) per node.  DATA/data.h5 holds the reference's
+// field dumps (OutFiles::CreateHDF5Framework, DumpGridData, DumpData,
+// src/outFiles.cpp:138-823): float32 datasets [dumps][faces or nodes], one row
+// per dump, for the outputs input.in switches on.
 //
 //   odis_run [--dir D] [--grid FILE | --level N] [--precision fp64|df64|fp32] [--orbits X]
 //
@@ -62,6 +64,96 @@ int fail(const char* what, odis_status st)
     std::fprintf(stderr, "odis_run: %s failed (status %d)\n", what, st);
     return 2;
 }
+
+// DATA/data.h5 in the reference's layout.  Datasets, in CreateHDF5Framework's
+// order (src/outFiles.cpp:222-333) and DumpGridData's (:463-521); the dump at
+// time level t writes row t-1 (DumpData, :523-823).
+struct DataFile {
+    enum { kEast, kNorth, kX, kY, kZ, kDisp, kDiss, kDissAvg, kTime, kDummy1, kCount };
+    odis_h5* h = nullptr;
+    int index[kCount];
+    int N = 0, E = 0;
+
+    odis_status open(const std::string& path, int flags, long long T, int n_cells, int n_faces, const odis_mesh* mesh)
+    {
+        N = n_cells;
+        E = n_faces;
+        std::vector<const char*> names;
+        std::vector<int> ranks;
+        std::vector<long long> dims;
+        for (int& i : index) i = -1;
+        auto add = [&](int id, const char* name, long long rows, long long cols) {
+            if (id >= 0) index[id] = (int)names.size();
+            names.push_back(name);
+            ranks.push_back(cols ? 2 : 1);
+            dims.push_back(rows);
+            dims.push_back(cols);
+        };
+        if (flags & 1) { add(kEast, "east velocity", T, E); add(kNorth, "north velocity", T, E); }
+        if (flags & 2) { add(kX, "x velocity", T, N); add(kY, "y velocity", T, N); add(kZ, "z velocity", T, N); }
+        if (flags & 4) add(kDisp, "displacement", T, N);
+        if (flags & 8) add(kDiss, "dissipated energy", T, E);
+        if (flags & 16) add(kDissAvg, "dissipation avg output", T, 0);
+        if (flags & 32) add(kTime, "kinetic avg output", T, 0);
+        if (flags & 64) add(kDummy1, "dummy1 output", T, N);
+        add(-1, "face longitude", E, 0);
+        add(-1, "face latitude", E, 0);
+        odis_status st = odis_h5_create(path.c_str(), (int)names.size(), names.data(), ranks.data(), dims.data(), &h);
+        if (st != ODIS_OK) return st;
+        // face centres in degrees: (float) of the angle, times 180/pi, to float (src/outFiles.cpp:491-492)
+        std::vector<double> lat(E), lon(E);
+        std::vector<float> out(E);
+        if ((st = odis_mesh_field(mesh, 4, lat.data())) != ODIS_OK || (st = odis_mesh_field(mesh, 5, lon.data())) != ODIS_OK)
+            return st;
+        for (int i = 0; i < E; i++) out[i] = (float)((double)(float)lon[i] * 180. / kPi);
+        if ((st = odis_h5_write_rows(h, (int)names.size() - 2, 0, E, out.data())) != ODIS_OK) return st;
+        for (int i = 0; i < E; i++) out[i] = (float)((double)(float)lat[i] * 180. / kPi);
+        return odis_h5_write_rows(h, (int)names.size() - 1, 0, E, out.data());
+    }
+
+    bool wants(int id) const { return h && index[id] >= 0; }
+
+    odis_status row(int id, long long t, const double* x, int n, int stride)
+    {
+        if (!wants(id)) return ODIS_OK;
+        std::vector<float> r(n);
+        for (int i = 0; i < n; i++) r[i] = (float)x[(size_t)i * stride];
+        return odis_h5_write_rows(h, index[id], t, 1, r.data());
+    }
+
+    // one dump: the state's face velocities (east, north), Cartesian node velocity,
+    // displacement, per-face dissipation, mean dissipation, time, and cv_mass
+    // (computed by the reference before the initial conditions load, so zero)
+    odis_status dump(odis_ctx* ctx, long long t, double time)
+    {
+        if (!h) return ODIS_OK;
+        std::vector<double> v(E), eta(N), uv((size_t)2 * E), e(E), uxyz((size_t)3 * N, 0.0), zero(N, 0.0);
+        int iter = 0;
+        odis_status st = odis_get_state(ctx, &iter, v.data(), eta.data(), nullptr, nullptr);
+        if (st == ODIS_OK) st = odis_interpolate_velocity(ctx, uv.data(), v.data(), ODIS_MEM_HOST);
+        double avg = 0.0;
+        if (st == ODIS_OK) st = odis_update_energy(ctx, &avg, e.data(), uv.data(), ODIS_MEM_HOST);
+        if (st == ODIS_OK && wants(kX)) st = odis_interpolate_cartesian(ctx, uxyz.data(), v.data(), ODIS_MEM_HOST);
+        if (st == ODIS_OK) st = row(kEast, t, uv.data(), E, 2);
+        if (st == ODIS_OK) st = row(kNorth, t, uv.data() + 1, E, 2);
+        if (st == ODIS_OK) st = row(kX, t, uxyz.data(), N, 3);
+        if (st == ODIS_OK) st = row(kY, t, uxyz.data() + 1, N, 3);
+        if (st == ODIS_OK) st = row(kZ, t, uxyz.data() + 2, N, 3);
+        if (st == ODIS_OK) st = row(kDisp, t, eta.data(), N, 1);
+        if (st == ODIS_OK) st = row(kDiss, t, e.data(), E, 1);
+        if (st == ODIS_OK) st = row(kDissAvg, t, &avg, 1, 1);
+        if (st == ODIS_OK) st = row(kTime, t, &time, 1, 1);
+        if (st == ODIS_OK) st = row(kDummy1, t, zero.data(), N, 1);
+        return st;
+    }
+
+    odis_status close()
+    {
+        odis_status st = h ? odis_h5_close(h) : ODIS_OK;
+        h = nullptr;
+        return st;
+    }
+};
 
 }  // namespace
 
@@ -126,7 +218,25 @@ int main(int argc, char** argv)
     FILE* pw = std::fopen((dir + "/DATA/power.txt").c_str(), "w");
     std::vector<double> power(out_every);
     const double area = 4.0 * kPi * p.radius * p.radius;
-    int rc = 0, count = 1;
+    // DATA/data.h5: the initial dump and one per output interval
+    DataFile data;
+    const long long dumps = 1 + (total_steps + out_every - 1) / out_every;
+    st = data.open(dir + "/DATA/data.h5", in.out_flags, dumps, N, E, mesh);
+    if (st != ODIS_OK) return fail("creating DATA/data.h5", st);
+    {   // the dump before the loop (src/timeIntegrator.cpp:186-196)
+        std::vector<double> v0(E), uv0((size_t)2 * E);
+        double avg0 = 0.0;
+        st = odis_get_state(ctx, nullptr, v0.data(), nullptr, nullptr, nullptr);
+        if (st == ODIS_OK) st = odis_interpolate_velocity(ctx, uv0.data(), v0.data(), ODIS_MEM_HOST);
+        if (st == ODIS_OK) st = odis_update_energy(ctx, &avg0, nullptr, uv0.data(), ODIS_MEM_HOST);
+        if (st == ODIS_OK) st = data.dump(ctx, 0, 0.0);
+        if (st != ODIS_OK) return fail("the initial dump", st);
+        char line[256];
+        std::snprintf(line, sizeof line, "DUMPING DATA AT %f AVG DISS: %e GW%d", 0.0, avg0 * area / 1e9, 1);
+        std::printf("%s\n", line);
+        if (out) std::fprintf(out, "%s\n", line);
+    }
+    int rc = 0, count = 2;
     for (long long done = 0; done < total_steps; done += out_every, count++) {
         const int n = (int)std::min<long long>(out_every, total_steps - done);
         st = odis_run_steps(ctx, n, power.data(), ODIS_MEM_HOST);
@@ -145,7 +255,10 @@ int main(int argc, char** argv)
             break;
         }
         if (st != ODIS_OK) { rc = fail("odis_run_steps", st); break; }
+        st = data.dump(ctx, count - 1, p.dt * (double)(done + n));
+        if (st != ODIS_OK) { rc = fail("writing DATA/data.h5", st); break; }
     }
+    if (data.close() != ODIS_OK && rc == 0) rc = fail("closing DATA/data.h5", ODIS_ERR_IO);
     if (out) std::fclose(out);
     if (pw) std::fclose(pw);
     int iter = 0;

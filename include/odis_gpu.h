@@ -25,6 +25,9 @@
  *                             src/mesh.cpp:32-197, :508-1154, :2808-3288, :4016-4089
  *   odis_params_from_input <- Globals::Globals + ReadGlobals + CalcMaxTimeStep,
  *                             src/globals.cpp:35-323,325-477; src/mesh.cpp:1566-1621
+ *   odis_h5_*              <- the HDF5 calls of OutFiles::CreateHDF5Framework, DumpGridData
+ *                             and DumpData (H5Fcreate, H5Dcreate, H5Dwrite of one row),
+ *                             include/outFiles.h:9, src/outFiles.cpp:138-823
  */
 #ifndef ODIS_GPU_H
 #define ODIS_GPU_H
@@ -110,6 +113,22 @@ typedef struct odis_input {
     char solver_name[32];
     char init_name[32];
 } odis_input;
+
+/* ---- output file (DATA/data.h5) ---------------------------------------- */
+/* An HDF5 file of float32 datasets in the root group, with the structure the
+ * HDF5 library gives H5Fcreate/H5Dcreate under default property lists
+ * (superblock 0, symbol-table root group, contiguous storage), written without
+ * the library.  Dataset k has rank ranks[k] (1 or 2) and extents dims[2k],
+ * dims[2k+1] (the second unused for rank 1); names are unique, non-empty and
+ * at most 2 x 4 x 2 x 16 = 256 of them.  Storage is allocated and zero-filled at
+ * creation (unwritten rows read as the fill value 0).  Host-only: no GPU needed. */
+typedef struct odis_h5 odis_h5;
+odis_status odis_h5_create(const char* path, int n, const char* const* names, const int* ranks,
+                           const long long* dims, odis_h5** out);
+/* rows [row0, row0 + nrows) of dataset k; a row is dims[2k+1] values (rank 2)
+ * or one value (rank 1).  ODIS_ERR_ARG past the extent. */
+odis_status odis_h5_write_rows(odis_h5* h, int k, long long row0, long long nrows, const float* data);
+odis_status odis_h5_close(odis_h5* h);
 
 /* ---- grid -------------------------------------------------------------- */
 /* Icosahedral grid at level n (10*4^n+2 cells), written in the reference's

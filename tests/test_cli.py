@@ -65,3 +65,60 @@ def test_cli_run_and_restart_match_the_library(built, tmp_path):
     _, v2, eta2, _, _ = sol2.get_state()
     vf2, _ = _read(d2 / "InitialConditions" / "vel_init.txt")
     assert np.max(np.abs(vf2 - v2)) <= 1e-6 * np.max(np.abs(v2))
+
+
+OUTPUT_KEYS = """dissipation output; 	      true; 	 	 	 data out opt;
+dissipation avg output;       true; 	 	 	 data out opt;
+kinetic avg output; 	      true; 	 	 	 data out opt;
+displacement output; 	 	  true; 	 	 	 data out opt;
+velocity output; 	 	 	  true; 	 	 	 data out opt;
+velocity cartesian output; 	 	  true; 	 	 	 data out opt;
+dummy1 output;                true;                  div;
+"""
+
+
+@pytest.mark.gpu
+def test_cli_writes_data_h5(built, tmp_path):
+    """DATA/data.h5 in the reference's layout (src/outFiles.cpp:138-823), read back with the
+    specification reader: one row per dump (the initial state, then every output interval), each
+    row the float32 of the library's own operators on the state at that dump."""
+    import geodesicodis_gb300 as g
+    import h5read
+    d = _rundir(tmp_path)
+    (d / "input.in").write_text((d / "input.in").read_text() + OUTPUT_KEYS)
+    r = subprocess.run([str(CLI), "--dir", str(d), "--orbits", "0.2"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = (d / "OUTPUT.txt").read_text().splitlines()
+    assert lines[0].startswith("DUMPING DATA AT 0.000000 AVG DISS:") and lines[0].endswith("GW1")
+    assert lines[-1].endswith("GW3")
+    inp = g.read_input(d / "input.in")
+    mesh = g.Mesh.generate(inp.grid_level - 1, inp.params.radius)
+    N, E = mesh.n_cells, mesh.n_edges
+    ds = h5read.H5File(d / "DATA" / "data.h5").datasets()
+    T = 3                                      # 0.2 orbits at 10 dumps per orbit, plus the initial dump
+    shapes = {"east velocity": (T, E), "north velocity": (T, E), "x velocity": (T, N), "y velocity": (T, N),
+              "z velocity": (T, N), "displacement": (T, N), "dissipated energy": (T, E),
+              "dissipation avg output": (T,), "kinetic avg output": (T,), "dummy1 output": (T, N),
+              "face longitude": (E,), "face latitude": (E,)}
+    assert {k: v.shape for k, v in ds.items()} == shapes
+    a = {k: v.read() for k, v in ds.items()}
+    sol = g.Solver(inp.params, mesh)
+    for t in range(T):
+        if t:
+            sol.run(200)
+        _, v, eta, _, _ = sol.get_state()
+        uv = sol.interpolateVelocity(v)
+        avg, e = sol.updateEnergy(uv)
+        ux = sol.interpolateVelocityCart(v)
+        for name, ref in (("east velocity", uv[:, 0]), ("north velocity", uv[:, 1]), ("displacement", eta),
+                          ("x velocity", ux[:, 0]), ("y velocity", ux[:, 1]), ("z velocity", ux[:, 2]),
+                          ("dissipated energy", e)):
+            scale = max(np.max(np.abs(ref)), 1e-30)
+            assert np.max(np.abs(a[name][t] - ref.astype(np.float32))) <= 1e-6 * scale, (name, t)
+        assert a["dissipation avg output"][t] == pytest.approx(avg, rel=1e-6, abs=1e-30)
+        assert a["kinetic avg output"][t] == np.float32(t * 200 * inp.params.dt)
+    assert not a["dummy1 output"].any()
+    np.testing.assert_array_equal(a["face latitude"], (mesh.field(4).astype(np.float32).astype(np.float64) * 180.0
+                                                        / np.pi).astype(np.float32))
+    np.testing.assert_array_equal(a["face longitude"], (mesh.field(5).astype(np.float32).astype(np.float64) * 180.0
+                                                         / np.pi).astype(np.float32))
