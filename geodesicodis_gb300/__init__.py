@@ -113,6 +113,7 @@ _SIGS = {
     "odis_batch_get_mesh_members": ([_V, C.c_int, _D, _D], C.c_int),
     "odis_batch_set_mesh_members": ([_V, C.c_int, _D, _D], C.c_int),
     "odis_batch_project": ([_V, C.c_int, _V, C.c_int, _V, C.c_int, _D, C.c_int], C.c_int),
+    "odis_analytical_state": ([C.POINTER(Params), _V, C.c_double, _D, _D, _D, _D], C.c_int),
     "odis_h5_create": ([C.c_char_p, C.c_int, C.POINTER(C.c_char_p), _I, C.POINTER(C.c_longlong), C.POINTER(_V)], C.c_int),
     "odis_h5_write_rows": ([_V, C.c_int, C.c_longlong, C.c_longlong, _V], C.c_int),
     "odis_h5_close": ([_V], C.c_int),
@@ -158,6 +159,16 @@ def _vp(a: np.ndarray):
 def generate_grid_file(level: int, path: str | os.PathLike) -> None:
     """Icosahedral grid at `level` (10*4^level+2 cells) in the reference grid-file format."""
     _ck(lib().odis_grid_generate_file(int(level), os.fsencode(str(path))), "odis_grid_generate_file")
+
+
+def analytical_state(params: Params, mesh: "Mesh", t: float = 0.0):
+    """(v[E], eta[N], dvdt[E,3], detadt[N,3]) of "initial conditions ANALYTICAL": the reference's
+    closed-form westward obliquity-tide solution at time t (potential POT_OBLIQ_WEST)."""
+    E, N = mesh.n_edges, mesh.n_cells
+    v, eta, dv, de = np.zeros(E), np.zeros(N), np.zeros((E, 3)), np.zeros((N, 3))
+    _ck(lib().odis_analytical_state(C.byref(params), mesh._h, float(t), _dp(v), _dp(eta), _dp(dv), _dp(de)),
+        "odis_analytical_state")
+    return v, eta, dv, de
 
 
 class H5Writer:

@@ -3,7 +3,8 @@
 // Reads a run directory the way the reference's main (src/main.cpp) and
 // ab3Explicit (src/timeIntegrator.cpp:57-322) do: input.in keys
 // (src/globals.cpp:58-203), optional InitialConditions/{vel,pres}_init.txt
-// (src/initialConditions.cpp:209-276) when "initial conditions" is LOAD.  It runs
+// (src/initialConditions.cpp:209-276) when "initial conditions" is LOAD, or the
+// closed-form OBLIQ_WEST state when it is ANALYTICAL.  It runs
 // the time loop on the GPU, prints the reference's "DUMPING DATA AT ... AVG
 // DISS: ... GW" line at every output interval (src/timeIntegrator.cpp:190-193)
 // to stdout and OUTPUT.txt, and writes the final state back in the
@@ -207,6 +208,14 @@ int main(int argc, char** argv)
         if (!read_state(dir + "/InitialConditions/vel_init.txt", E, v, dv) ||
             !read_state(dir + "/InitialConditions/pres_init.txt", N, eta, de))
             return fail("reading InitialConditions", ODIS_ERR_IO);
+        st = odis_set_state(ctx, 0, v.data(), eta.data(), dv.data(), de.data());
+        if (st != ODIS_OK) return fail("odis_set_state", st);
+    } else if (in.init_kind == 2) {
+        // analyticalInitialConditions at t = 0 (src/initialConditions.cpp:150-211); the AB3
+        // loop still starts with its two Euler steps, as for NONE
+        v.assign(E, 0.0); eta.assign(N, 0.0); dv.assign((size_t)3 * E, 0.0); de.assign((size_t)3 * N, 0.0);
+        st = odis_analytical_state(&p, mesh, 0.0, v.data(), eta.data(), dv.data(), de.data());
+        if (st != ODIS_OK) return fail("initial conditions ANALYTICAL (potential OBLIQ_WEST only)", st);
         st = odis_set_state(ctx, 0, v.data(), eta.data(), dv.data(), de.data());
         if (st != ODIS_OK) return fail("odis_set_state", st);
     }

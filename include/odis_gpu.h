@@ -21,6 +21,8 @@
  *   odis_run_steps         <- the body of ab3Explicit's time loop, src/timeIntegrator.cpp:205-313
  *   odis_get_state / odis_set_state <- writeInitialConditions / loadInitialConditions,
  *                                      src/initialConditions.cpp:19,209
+ *   odis_analytical_state  <- analyticalInitialConditions + analyticalLTE (OBLIQ_WEST),
+ *                             src/initialConditions.cpp:150-211, src/analyticalLTE.cpp:22-181
  *   odis_mesh_*            <- Mesh::Mesh + ReadMeshFile + AssignFaces + Calc*OperatorCoeffs,
  *                             src/mesh.cpp:32-197, :508-1154, :2808-3288, :4016-4089
  *   odis_params_from_input <- Globals::Globals + ReadGlobals + CalcMaxTimeStep,
@@ -239,6 +241,15 @@ odis_status odis_run_steps(odis_ctx* c, int n, double* power, int mem);
 odis_status odis_get_state(odis_ctx* c, int* iter, double* v, double* eta, double* dvdt, double* detadt);
 odis_status odis_set_state(odis_ctx* c, int iter, const double* v, const double* eta,
                            const double* dvdt, const double* detadt);
+/* "initial conditions ANALYTICAL": the closed-form westward obliquity-tide
+ * solution at time t in the same layout (v at the face centres along the face
+ * normals, eta at the nodes, tendencies at t, t - dt, t - 2 dt), for
+ * odis_set_state at iter 0.  p->potential must be ODIS_POT_OBLIQ_WEST (the one
+ * case the reference's solution has), else ODIS_ERR_ARG.  Outputs are host
+ * arrays, each nullable.  Host-only.  Exact for the undamped equations; with
+ * drag it is the reference's truncated form. */
+odis_status odis_analytical_state(const odis_params* p, const odis_mesh* mesh, double t, double* v, double* eta,
+                                  double* dvdt, double* detadt);
 
 /* ---- allocation-free dissipation --------------------------------------- */
 /* Same result as odis_update_energy, for callers that cannot allocate device

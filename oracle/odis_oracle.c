@@ -707,6 +707,9 @@ int orc_mesh_get_field(const orc_mesh *M, int which, double *out)
     case 1: memcpy(out, M->face_dist, sizeof(double) * E); return E;
     case 2: memcpy(out, M->face_area, sizeof(double) * E); return E;
     case 3: memcpy(out, M->cv_area, sizeof(double) * M->N); return M->N;
+    case 12: case 13:
+        for (int i = 0; i < M->N; i++) out[i] = M->node_sph[i * 2 + (which - 12)];
+        return M->N;
     default: break;
     }
     const double *src = NULL; int off = 0;

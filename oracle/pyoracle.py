@@ -109,7 +109,7 @@ class OracleMesh:
         self.n_cells, self.n_edges, self.n_vertices = n.value, e.value, v.value
 
     def field(self, which: int) -> np.ndarray:
-        out = np.zeros(self.n_cells if which == 3 else self.n_edges)
+        out = np.zeros(self.n_cells if which in (3, 12, 13) else self.n_edges)
         lib().orc_mesh_get_field(self._h, which, _dp(out))
         return out
 
