@@ -5,17 +5,17 @@
 //   k_adv_pv     per vertex: relative vorticity from the curl of v (three faces,
 //                ascending face order), thickness at the vertex from the three
 //                nodes' thicknesses weighted by control-volume area x kite
-//                fraction over the vertex area (Ringler et al. 2010 eq. 25),
-//                potential vorticity q = (zeta + f) / h
-//   k_adv_edge   per face: q averaged from the face's two vertices, and the
-//                thickness flux h_e v_e with h_e averaged from its two nodes
+//                fraction over the vertex area (Ringler et al. 2010 eq. 25, the
+//                weights premultiplied per vertex), potential vorticity q = (zeta + f) / h
+//   k_adv_edge   per face: q averaged from the face's two vertices, the thickness
+//                flux h_e v_e with h_e averaged from its two nodes, and h_e v_e q_e
 //   k_adv_node   per node: kinetic energy from the RBF Cartesian velocity
 //   k_adv_flux   per face: dvdt -= -sum_j w_j l_j / d_e (h_j v_j) (q_e + q_j) / 2
-//                (eq. 49), then dvdt += -(G KE)_e with the gradient's two terms in
-//                ascending node order
-// Every sum and product is evaluated in the reference's order (the factor 1/2 of
-// eq. 49 is folded into the weights: a power-of-two scaling, so no rounding
-// changes), and the results match the FP64 restatement to rounding.
+//                (eq. 49), as q_e sum_j c_j (h v)_j + sum_j c_j (h v q)_j with
+//                c_j = w_j l_j / (2 d_e), then dvdt += -(G KE)_e
+// Products are fused into the sums (the nonlinear loop is bound by GB300's FP64
+// issue rate), so the results match the FP64 restatement to rounding, not bit
+// for bit.
 //
 // One step of the advective loop (src/timeIntegrator.cpp:205-269) is seven kernels:
 //   k_adv_pv, k_adv_edge
@@ -32,13 +32,15 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 namespace odis {
 
 namespace {
 
-constexpr int kAdvThreads = 256;
+constexpr int kAdvThreads = 256;       // largest block; k_adv_lsq_power's reduction is sized for it
 constexpr int kAdvGraphSteps = 64;      // steps per captured graph of the advective loop
 
 __device__ __forceinline__ double adv_warp_sum(double x)
@@ -48,35 +50,35 @@ __device__ __forceinline__ double adv_warp_sum(double x)
     return x;
 }
 
+// vwt[j][i] = A_n R_j / A_v: the node's control-volume area times the kite
+// fraction over the vertex area, so that h_v = sum_j vwt_j h_n
 __global__ void k_adv_pv(const int* __restrict__ vface, const double* __restrict__ vcoef, const int* __restrict__ vnode,
-                         const double* __restrict__ vR, const double* __restrict__ vinv, const double* __restrict__ vf,
-                         const double* __restrict__ cvA, int V, int Vp, const double* __restrict__ v,
-                         const double* __restrict__ h, double* __restrict__ q)
+                         const double* __restrict__ vwt, const double* __restrict__ vf, int V, int Vp,
+                         const double* __restrict__ v, const double* __restrict__ h, double* __restrict__ q)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
-    double zeta = 0.0;
-#pragma unroll
-    for (int j = 0; j < 3; j++) zeta += vcoef[j * Vp + i] * v[vface[j * Vp + i]];
-    double th = 0.0;
+    double zeta = 0.0, th = 0.0;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-        const int n = vnode[j * Vp + i];
-        th += h[n] * cvA[n] * vR[j * Vp + i];
+        zeta = fma(vcoef[j * Vp + i], v[vface[j * Vp + i]], zeta);
+        th = fma(h[vnode[j * Vp + i]], vwt[j * Vp + i], th);
     }
-    th *= vinv[i];
     q[i] = (zeta + vf[i]) / th;
 }
 
+// per face: q_e, the thickness flux h_e v_e and its product with q_e
 __global__ void k_adv_edge(const int* __restrict__ fvert, const int* __restrict__ fnode, int E, int Ep,
                            const double* __restrict__ q, const double* __restrict__ h, const double* __restrict__ v,
-                           double* __restrict__ qe, double* __restrict__ hve)
+                           double* __restrict__ qe, double* __restrict__ hve, double* __restrict__ hvq)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    qe[e] = 0.5 * (q[fvert[e]] + q[fvert[Ep + e]]);
-    const double he = 0.5 * (h[fnode[e]] + h[fnode[Ep + e]]);
-    hve[e] = he * v[e];
+    const double qv = 0.5 * (q[fvert[e]] + q[fvert[Ep + e]]);
+    const double hv = (0.5 * (h[fnode[e]] + h[fnode[Ep + e]])) * v[e];
+    qe[e] = qv;
+    hve[e] = hv;
+    hvq[e] = hv * qv;
 }
 
 // kinetic energy 0.5 |u|^2 at the nodes, u from the RBF Cartesian reconstruction
@@ -100,16 +102,18 @@ __global__ void k_adv_node(const double* __restrict__ rbf, const int* __restrict
         u[c] = t;
     }
     ek[i] = 0.5 * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
-    if (U) U[i] = __dadd_rn(__dmul_rn(phase[0], Ua[i]), __dmul_rn(phase[1], Ub[i]));
+    if (U) U[i] = fma(phase[1], Ub[i], phase[0] * Ua[i]);
 }
 
 // kGrad: dvdt_e = alpha (G eta)_e (gradient row in ascending node order), else
-// dvdt_e as given; then the PV flux and -(G KE)_e
+// dvdt_e as given; then the PV flux and -(G KE)_e.  The flux
+// sum_j c_j (h v)_j (q_e + q_j) is formed as q_e sum_j c_j (h v)_j + sum_j c_j (h v q)_j.
 template <bool kGrad>
 __global__ void k_adv_flux(const int* __restrict__ fr, const double* __restrict__ cwh, const int* __restrict__ nfr,
                            const int* __restrict__ gcol, const double* __restrict__ gval, int E, int Ep,
-                           const double* __restrict__ qe, const double* __restrict__ hve, const double* __restrict__ ek,
-                           double alpha, const double* __restrict__ eta, double* __restrict__ dvdt)
+                           const double* __restrict__ qe, const double* __restrict__ hve, const double* __restrict__ hvq,
+                           const double* __restrict__ ek, double alpha, const double* __restrict__ eta,
+                           double* __restrict__ dvdt)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
@@ -117,21 +121,19 @@ __global__ void k_adv_flux(const int* __restrict__ fr, const double* __restrict_
     const double w0 = gval[e], w1 = gval[Ep + e];
     double d;
     if constexpr (kGrad) {
-        double t = 0.0;
-        t = __dadd_rn(t, __dmul_rn(w0, eta[g0]));
-        t = __dadd_rn(t, __dmul_rn(w1, eta[g1]));
-        d = __dmul_rn(alpha, t);
+        d = alpha * fma(w1, eta[g1], w0 * eta[g0]);
     } else {
         d = dvdt[e];
     }
-    const double q0 = qe[e];
-    double F = 0.0;
+    double s1 = 0.0, s2 = 0.0;
     const int n = nfr[e];
     for (int j = 0; j < n; j++) {
         const int f = fr[j * Ep + e];
-        F += cwh[j * Ep + e] * hve[f] * (q0 + qe[f]);
+        const double c = cwh[j * Ep + e];
+        s1 = fma(c, hve[f], s1);
+        s2 = fma(c, hvq[f], s2);
     }
-    d -= -F;
+    d += fma(qe[e], s1, s2);
     double gk = 0.0;
     gk += w0 * ek[g0];
     gk += w1 * ek[g1];
@@ -141,51 +143,50 @@ __global__ void k_adv_flux(const int* __restrict__ fr, const double* __restrict_
 
 // interpolateLSQFlux (src/interpolation.cpp:311-356), beta = 1, at face e: the
 // directional second derivatives at the face's two nodes (7-term rows, ascending
-// node order), then the third-order upwind-biased thickness flux.  Products and
-// sums are rounded separately, as in the unfused FP64 restatement.
+// node order, fused multiply-adds), then the third-order upwind-biased thickness
+// flux (u/2 (h_i + h_o) - dx^2/12 (d2_o + d2_i) u + dx^2/12 |u| (d2_o - d2_i)).
+// dx2: d_e^2 / 12 per face, rounded on the host as the reference rounds it.
 __device__ __forceinline__ double lsq_flux_at(int e, int Ep, const int* __restrict__ col,
-                                              const double* __restrict__ val, const double* __restrict__ dist,
+                                              const double* __restrict__ val, const double* __restrict__ dx2v,
                                               const int* __restrict__ fnode, double vel, const double* __restrict__ h)
 {
     const size_t R = (size_t)2 * Ep;
     double d2i = 0.0, d2o = 0.0;
 #pragma unroll
     for (int j = 0; j < 7; j++) {
-        d2i = __dadd_rn(d2i, __dmul_rn(val[j * R + 2 * e], h[col[j * R + 2 * e]]));
-        d2o = __dadd_rn(d2o, __dmul_rn(val[j * R + 2 * e + 1], h[col[j * R + 2 * e + 1]]));
+        d2i = fma(val[j * R + 2 * e], h[col[j * R + 2 * e]], d2i);
+        d2o = fma(val[j * R + 2 * e + 1], h[col[j * R + 2 * e + 1]], d2o);
     }
-    const double dx = dist[e];
-    const double dx2 = __dmul_rn(__dmul_rn(dx, dx), 1. / 12.0);
-    const double a = __dmul_rn(__dmul_rn(vel, 0.5), __dadd_rn(h[fnode[e]], h[fnode[Ep + e]]));
-    const double b = __dmul_rn(__dmul_rn(dx2, __dadd_rn(d2o, d2i)), vel);
-    const double c = __dmul_rn(__dmul_rn(__dmul_rn(dx2, 1.0), fabs(vel)), __dsub_rn(d2o, d2i));
-    return __dadd_rn(__dsub_rn(a, b), c);
+    const double dx2 = dx2v[e];
+    const double a = (vel * 0.5) * (h[fnode[e]] + h[fnode[Ep + e]]);
+    const double b = (dx2 * (d2o + d2i)) * vel;
+    return fma(dx2 * fabs(vel), d2o - d2i, a - b);
 }
 
-__global__ void k_lsq_flux(const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ dist,
+__global__ void k_lsq_flux(const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ dx2,
                            const int* __restrict__ fnode, int E, int Ep, const double* __restrict__ v,
                            const double* __restrict__ h, double* __restrict__ flux)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    flux[e] = lsq_flux_at(e, Ep, col, val, dist, fnode, v[e], h);
+    flux[e] = lsq_flux_at(e, Ep, col, val, dx2, fnode, v[e], h);
 }
 
 // ---- the advective time step (src/timeIntegrator.cpp:205-269, advection true) ----
 
 // integrateAB3scalar (src/temporalOperators.cpp:17-68) for one unknown; h = its [3] history
-__device__ __forceinline__ void ab3_ref(double& s, double* h, int iter, double dt, int init_load)
+__device__ __forceinline__ void ab3_step(double& s, double* h, int iter, double dt, int init_load)
 {
     const double a = 23. / 12., b = -16. / 12., c = 5. / 12.;
     if (iter > 1 || init_load) {
-        s = __dadd_rn(s, __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(a, h[0]), __dmul_rn(b, h[1])), __dmul_rn(c, h[2])), dt));
+        s = fma(fma(c, h[2], fma(b, h[1], a * h[0])), dt, s);
         h[2] = h[1];
         h[1] = h[0];
     } else if (iter == 0) {
-        s = __dadd_rn(s, __dmul_rn(h[0], dt));
+        s = fma(h[0], dt, s);
         h[2] = h[0];
     } else {
-        s = __dadd_rn(s, __dmul_rn(h[0], dt));
+        s = fma(h[0], dt, s);
         h[1] = h[0];
     }
 }
@@ -199,16 +200,13 @@ __global__ void k_adv_vstep(const int* __restrict__ gcol, const double* __restri
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    double gu = 0.0;
-    gu = __dadd_rn(gu, __dmul_rn(gval[e], U[gcol[e]]));
-    gu = __dadd_rn(gu, __dmul_rn(gval[Ep + e], U[gcol[Ep + e]]));
-    gu = __dadd_rn(0.0, __dmul_rn(1.0, gu));
+    const double gu = fma(gval[Ep + e], U[gcol[Ep + e]], gval[e] * U[gcol[e]]);
     double ve = v[e];
-    const double drag = __dadd_rn(__dadd_rn(0.0, __dmul_rn(1.0, __dmul_rn(-alpha, ve))), gu);
+    const double drag = fma(-alpha, ve, gu);
     double* h = hist + (size_t)e * 3;
     h[0] = dv0[e];
-    ab3_ref(ve, h, iter, dt, init_load);
-    v[e] = __dadd_rn(ve, __dmul_rn(dt, drag));
+    ab3_step(ve, h, iter, dt, init_load);
+    v[e] = fma(dt, drag, ve);
 }
 
 struct PowerArgs {
@@ -229,7 +227,7 @@ struct PowerArgs {
 // finish sums the block partials in a fixed order (lane-strided, then the warp
 // tree), so the power does not depend on which block finishes last.
 __global__ void __launch_bounds__(kAdvThreads)
-k_adv_lsq_power(const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ dist,
+k_adv_lsq_power(const int* __restrict__ col, const double* __restrict__ val, const double* __restrict__ dx2,
                 const int* __restrict__ fnode, int E, int Ep, const double* __restrict__ v, const double* __restrict__ h,
                 double* __restrict__ flux, PowerArgs pa)
 {
@@ -239,7 +237,7 @@ k_adv_lsq_power(const int* __restrict__ col, const double* __restrict__ val, con
     double x = 0.0;
     if (e < E) {
         const double ve = v[e];
-        flux[e] = lsq_flux_at(e, Ep, col, val, dist, fnode, ve, h);
+        flux[e] = lsq_flux_at(e, Ep, col, val, dx2, fnode, ve, h);
         double t = 0.0;
 #pragma unroll
         for (int k = 0; k < kTrisk; k++) t = fma(pa.w[k * Ep + e], v[pa.nbr[k * Ep + e]], t);
@@ -254,7 +252,7 @@ k_adv_lsq_power(const int* __restrict__ col, const double* __restrict__ val, con
     if (lane == 0) s_red[wid] = x;
     __syncthreads();
     if (wid == 0) {
-        double s = lane < kAdvThreads / 32 ? s_red[lane] : 0.0;
+        double s = lane < (int)(blockDim.x >> 5) ? s_red[lane] : 0.0;
         s = adv_warp_sum(s);
         if (lane == 0) {
             pa.part[blockIdx.x] = s;
@@ -307,20 +305,20 @@ __global__ void k_adv_estep(const int* __restrict__ dcol, const double* __restri
     if (i >= N) return;
     double t = 0.0;
 #pragma unroll
-    for (int j = 0; j < 6; j++) t = __dadd_rn(t, __dmul_rn(dval[j * Np + i], flux[dcol[j * Np + i]]));
+    for (int j = 0; j < 6; j++) t = fma(dval[j * Np + i], flux[dcol[j * Np + i]], t);
     double* h = hist + (size_t)i * 3;
-    h[0] = __dadd_rn(0.0, __dmul_rn(1.0, t));
+    h[0] = t;
     double s = eta[i];
-    ab3_ref(s, h, iter, dt, init_load);
+    ab3_step(s, h, iter, dt, init_load);
     eta[i] = s;
-    ht[i] = __dadd_rn(h0, s);
+    ht[i] = h0 + s;
 }
 
 // column thickness h + eta (after a state is loaded)
 __global__ void k_adv_thickness(int N, double h0, const double* __restrict__ eta, double* __restrict__ ht)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < N) ht[i] = __dadd_rn(h0, eta[i]);
+    if (i < N) ht[i] = h0 + eta[i];
 }
 
 __global__ void k_adv_set_step(long long* step, long long v, double dt, double angvel, double* phase)
@@ -347,11 +345,11 @@ struct AdvDev {
     int V = 0, Vp = 0, E = 0, Ep = 0, N = 0, Np = 0;
     int *vface = nullptr, *vnode = nullptr, *fvert = nullptr, *fnode = nullptr, *fr = nullptr, *nfr = nullptr,
         *gcol = nullptr;
-    double *vcoef = nullptr, *vR = nullptr, *vinv = nullptr, *vf = nullptr, *cvA = nullptr, *cwh = nullptr,
+    double *vcoef = nullptr, *vwt = nullptr, *vf = nullptr, *cwh = nullptr,
            *gval = nullptr;
-    double *q = nullptr, *qe = nullptr, *hve = nullptr, *ek = nullptr;
+    double *q = nullptr, *qe = nullptr, *hve = nullptr, *hvq = nullptr, *ek = nullptr;
     int* lcol = nullptr;         // [7][2 Ep] operatorDirectionalSecondDeriv rows
-    double *lval = nullptr, *dist = nullptr;
+    double *lval = nullptr, *dx2 = nullptr;     // rows' weights; d_e^2 / 12 per face
     int* dcol = nullptr;         // [6][Np] divergence rows, ascending face order (padded with zero weights)
     double* dval = nullptr;
     // state of an advective run, in the reference's layout
@@ -364,6 +362,10 @@ struct AdvDev {
     double* part = nullptr;                 // [face blocks] power partial sums
     unsigned* count = nullptr;              // finished blocks of k_adv_lsq_power
     double* pbuf = nullptr;                 // [kAdvGraphSteps] power of a graph chunk
+    // threads per block for the node/vertex, face, and LSQ + power kernels: small blocks
+    // spread these one-wave grids evenly over the SMs (level 6: 46 us/step against 49 us
+    // with 256 threads everywhere); ODIS_ADV_BLOCKS="n,f,p" overrides them
+    int bn = 64, bf = 64, bp = 128;
     cudaGraphExec_t graph = nullptr;
 };
 
@@ -371,9 +373,9 @@ void adv_destroy(AdvDev* a)
 {
     if (!a) return;
     for (void* p : {(void*)a->vface, (void*)a->vnode, (void*)a->fvert, (void*)a->fnode, (void*)a->fr, (void*)a->nfr,
-                    (void*)a->gcol, (void*)a->vcoef, (void*)a->vR, (void*)a->vinv, (void*)a->vf, (void*)a->cvA,
-                    (void*)a->cwh, (void*)a->gval, (void*)a->q, (void*)a->qe, (void*)a->hve, (void*)a->ek,
-                    (void*)a->lcol, (void*)a->lval, (void*)a->dist, (void*)a->dcol, (void*)a->dval, (void*)a->v,
+                    (void*)a->gcol, (void*)a->vcoef, (void*)a->vwt, (void*)a->vf,
+                    (void*)a->cwh, (void*)a->gval, (void*)a->q, (void*)a->qe, (void*)a->hve, (void*)a->hvq, (void*)a->ek,
+                    (void*)a->lcol, (void*)a->lval, (void*)a->dx2, (void*)a->dcol, (void*)a->dval, (void*)a->v,
                     (void*)a->eta, (void*)a->hv, (void*)a->hp, (void*)a->ht, (void*)a->U, (void*)a->dv0,
                     (void*)a->flux, (void*)a->Ua, (void*)a->Ub, (void*)a->step, (void*)a->phase, (void*)a->part,
                     (void*)a->count, (void*)a->pbuf})
@@ -387,10 +389,17 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
     *out = nullptr;
     if (m.vert_area.empty()) return ODIS_ERR_MESH;
     AdvDev* a = new AdvDev;
+    if (const char* env = std::getenv("ODIS_ADV_BLOCKS")) {
+        int x = 0, y = 0, z = 0;
+        if (std::sscanf(env, "%d,%d,%d", &x, &y, &z) == 3 && x >= 32 && y >= 32 && z >= 32 && x <= 256 && y <= 256 &&
+            z <= 256 && x % 32 == 0 && y % 32 == 0 && z % 32 == 0) {
+            a->bn = x; a->bf = y; a->bp = z;
+        }
+    }
     a->V = m.V; a->Vp = (m.V + 127) / 128 * 128; a->E = m.E; a->Ep = Ep; a->N = m.N; a->Np = Np;
     const int V = m.V, Vp = a->Vp, E = m.E;
     std::vector<int> vface((size_t)3 * Vp, 0), vnode((size_t)3 * Vp, 0);
-    std::vector<double> vcoef((size_t)3 * Vp, 0.0), vR((size_t)3 * Vp, 0.0), vinv(Vp, 1.0), vf(Vp, 0.0);
+    std::vector<double> vcoef((size_t)3 * Vp, 0.0), vwt((size_t)3 * Vp, 0.0), vf(Vp, 0.0);
     for (int v = 0; v < V; v++) {
         // operatorCurl row (src/mesh.cpp:3122-3175): ascending face order
         int idx[3] = {0, 1, 2};
@@ -399,14 +408,13 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
             const int s = idx[j], f = m.vert_faces[v * 3 + s];
             vface[(size_t)j * Vp + v] = f;
             vcoef[(size_t)j * Vp + v] = m.face_dist[f] * m.vert_face_dir[v * 3 + s] / m.vert_area[v];
-            vnode[(size_t)j * Vp + v] = m.vert_nodes[v * 3 + j];
-            vR[(size_t)j * Vp + v] = m.vert_R[v * 3 + j];
+            const int n = m.vert_nodes[v * 3 + j];
+            vnode[(size_t)j * Vp + v] = n;
+            // thickness at the vertex (Ringler et al. 2010 eq. 25): kite-weighted node thicknesses
+            vwt[(size_t)j * Vp + v] = m.cv_area[n] * m.vert_R[v * 3 + j] / m.vert_area[v];
         }
-        vinv[v] = 1.0 / m.vert_area[v];
         vf[v] = -2 * angvel * std::sin(m.vert_sph[v * 2]);
     }
-    std::vector<double> cvA(Np, 0.0);
-    for (int i = 0; i < m.N; i++) cvA[i] = m.cv_area[i];
     std::vector<int> fvert((size_t)2 * Ep, 0), fnode((size_t)2 * Ep, 0), fr((size_t)10 * Ep, 0), nfr(Ep, 0),
         gcol((size_t)2 * Ep, 0);
     std::vector<double> cwh((size_t)10 * Ep, 0.0), gval((size_t)2 * Ep, 0.0);
@@ -438,17 +446,17 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
         const int st = build_lsq_rows(m, kRbfEps, rc, rv);
         if (st != ODIS_OK) { adv_destroy(a); return st; }
         std::vector<int> lc((size_t)7 * 2 * Ep, 0);
-        std::vector<double> lv((size_t)7 * 2 * Ep, 0.0), dist(Ep, 1.0);
+        std::vector<double> lv((size_t)7 * 2 * Ep, 0.0), dx2(Ep, 1.0);
         for (int row = 0; row < 2 * E; row++)
             for (int j = 0; j < 7; j++) {
                 lc[(size_t)j * 2 * Ep + row] = rc[(size_t)row * 7 + j];
                 lv[(size_t)j * 2 * Ep + row] = rv[(size_t)row * 7 + j];
             }
-        for (int e = 0; e < E; e++) dist[e] = m.face_dist[e];
+        for (int e = 0; e < E; e++) dx2[e] = (m.face_dist[e] * m.face_dist[e]) * (1. / 12.0);
         a->lcol = upload(lc);
         a->lval = upload(lv);
-        a->dist = upload(dist);
-        if (!a->lcol || !a->lval || !a->dist) { adv_destroy(a); return ODIS_ERR_NOMEM; }
+        a->dx2 = upload(dx2);
+        if (!a->lcol || !a->lval || !a->dx2) { adv_destroy(a); return ODIS_ERR_NOMEM; }
     }
     {   // operatorDivergence rows (src/mesh.cpp:3177-3288), ascending face order
         std::vector<int> dc((size_t)6 * Np, 0);
@@ -468,14 +476,15 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
         a->dval = upload(dvv);
         if (!a->dcol || !a->dval) { adv_destroy(a); return ODIS_ERR_NOMEM; }
     }
-    a->vface = upload(vface); a->vnode = upload(vnode); a->vcoef = upload(vcoef); a->vR = upload(vR);
-    a->vinv = upload(vinv); a->vf = upload(vf); a->cvA = upload(cvA);
+    a->vface = upload(vface); a->vnode = upload(vnode); a->vcoef = upload(vcoef); a->vwt = upload(vwt);
+    a->vf = upload(vf);
     a->fvert = upload(fvert); a->fnode = upload(fnode); a->fr = upload(fr); a->nfr = upload(nfr);
     a->cwh = upload(cwh); a->gcol = upload(gcol); a->gval = upload(gval);
-    bool ok = a->vface && a->vnode && a->vcoef && a->vR && a->vinv && a->vf && a->cvA && a->fvert && a->fnode &&
+    bool ok = a->vface && a->vnode && a->vcoef && a->vwt && a->vf && a->fvert && a->fnode &&
               a->fr && a->nfr && a->cwh && a->gcol && a->gval;
     ok = ok && cudaMalloc(&a->q, sizeof(double) * Vp) == cudaSuccess &&
          cudaMalloc(&a->qe, sizeof(double) * Ep) == cudaSuccess && cudaMalloc(&a->hve, sizeof(double) * Ep) == cudaSuccess &&
+         cudaMalloc(&a->hvq, sizeof(double) * Ep) == cudaSuccess &&
          cudaMalloc(&a->ek, sizeof(double) * Np) == cudaSuccess;
     if (!ok) { adv_destroy(a); return ODIS_ERR_NOMEM; }
     *out = a;
@@ -487,11 +496,11 @@ double* adv_ekin_scratch(AdvDev* a) { return a->ek; }
 static void momentum_head(AdvDev* a, const double* rbf, const int* cell_face, const double* v, const double* h_total,
                           double* ekin, double* U, cudaStream_t s)
 {
-    k_adv_pv<<<(a->V + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->vface, a->vcoef, a->vnode, a->vR, a->vinv,
-                                                                           a->vf, a->cvA, a->V, a->Vp, v, h_total, a->q);
-    k_adv_edge<<<(a->E + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->fvert, a->fnode, a->E, a->Ep, a->q,
-                                                                             h_total, v, a->qe, a->hve);
-    k_adv_node<<<(a->N + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(rbf, cell_face, a->N, a->Np, v, ekin,
+    k_adv_pv<<<(a->V + a->bn - 1) / a->bn, a->bn, 0, s>>>(a->vface, a->vcoef, a->vnode, a->vwt, a->vf, a->V, a->Vp, v,
+                                                         h_total, a->q);
+    k_adv_edge<<<(a->E + a->bf - 1) / a->bf, a->bf, 0, s>>>(a->fvert, a->fnode, a->E, a->Ep, a->q,
+                                                                             h_total, v, a->qe, a->hve, a->hvq);
+    k_adv_node<<<(a->N + a->bn - 1) / a->bn, a->bn, 0, s>>>(rbf, cell_face, a->N, a->Np, v, ekin,
                                                                              a->phase, a->Ua, a->Ub, U);
 }
 
@@ -499,8 +508,8 @@ void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dv
                   const double* h_total, double* ekin, cudaStream_t s)
 {
     momentum_head(a, rbf, cell_face, v, h_total, ekin, nullptr, s);
-    k_adv_flux<false><<<(a->E + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(
-        a->fr, a->cwh, a->nfr, a->gcol, a->gval, a->E, a->Ep, a->qe, a->hve, ekin, 0.0, nullptr, dvdt);
+    k_adv_flux<false><<<(a->E + a->bf - 1) / a->bf, a->bf, 0, s>>>(
+        a->fr, a->cwh, a->nfr, a->gcol, a->gval, a->E, a->Ep, a->qe, a->hve, a->hvq, ekin, 0.0, nullptr, dvdt);
 }
 
 int adv_kernels_per_call() { return 4; }
@@ -514,7 +523,7 @@ int adv_state_alloc(AdvDev* a, double h0, const std::vector<double>& Ua, const s
         a->Ua = upload(ua);
         a->Ub = upload(ub);
         a->angvel = angvel;
-        const int eb = (a->E + kAdvThreads - 1) / kAdvThreads;
+        const int eb = (a->E + 31) / 32;      // enough partials for any block size
         if (!a->Ua || !a->Ub || cudaMalloc(&a->step, sizeof(long long)) != cudaSuccess ||
             cudaMalloc(&a->phase, sizeof(double) * 2) != cudaSuccess ||
             cudaMalloc(&a->part, sizeof(double) * eb) != cudaSuccess ||
@@ -549,18 +558,18 @@ void adv_set_step(AdvDev* a, long long step, double dt, cudaStream_t s)
 
 void adv_step(AdvDev* a, const AdvStepArgs& x, int iter, double* power, cudaStream_t s)
 {
-    const int eb = (a->E + kAdvThreads - 1) / kAdvThreads, nb = (a->N + kAdvThreads - 1) / kAdvThreads;
+    const int fb = (a->E + a->bf - 1) / a->bf, pb = (a->E + a->bp - 1) / a->bp, nb = (a->N + a->bn - 1) / a->bn;
     // updateMomentum, advection branch: -g G eta + PV flux - G KE
     momentum_head(a, x.rbf, x.cell_face, a->v, a->ht, a->ek, a->U, s);
-    k_adv_flux<true><<<eb, kAdvThreads, 0, s>>>(a->fr, a->cwh, a->nfr, a->gcol, a->gval, a->E, a->Ep, a->qe, a->hve,
-                                                a->ek, -x.g * (1 - 0.5 * 0.0), a->eta, a->dv0);
-    k_adv_vstep<<<eb, kAdvThreads, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, x.alpha, x.dt, iter, x.init_load, a->dv0,
+    k_adv_flux<true><<<fb, a->bf, 0, s>>>(a->fr, a->cwh, a->nfr, a->gcol, a->gval, a->E, a->Ep, a->qe, a->hve,
+                                                a->hvq, a->ek, -x.g * (1 - 0.5 * 0.0), a->eta, a->dv0);
+    k_adv_vstep<<<fb, a->bf, 0, s>>>(a->gcol, a->gval, a->E, a->Ep, x.alpha, x.dt, iter, x.init_load, a->dv0,
                                           a->U, a->v, a->hv);
     // updateEta, advection branch: D (LSQ flux of h + eta); updateEnergy of the new v
     const PowerArgs pa{x.nbr, x.w, x.nrm, x.area, x.alpha * 1000.0 * x.h0, x.divisor, a->part, a->count, power};
-    k_adv_lsq_power<<<eb, kAdvThreads, 0, s>>>(a->lcol, a->lval, a->dist, a->fnode, a->E, a->Ep, a->v, a->ht, a->flux,
+    k_adv_lsq_power<<<pb, a->bp, 0, s>>>(a->lcol, a->lval, a->dx2, a->fnode, a->E, a->Ep, a->v, a->ht, a->flux,
                                               pa);
-    k_adv_estep<<<nb + 1, kAdvThreads, 0, s>>>(a->dcol, a->dval, a->N, a->Np, x.dt, iter, x.init_load, x.h0, a->flux,
+    k_adv_estep<<<nb + 1, a->bn, 0, s>>>(a->dcol, a->dval, a->N, a->Np, x.dt, iter, x.init_load, x.h0, a->flux,
                                               a->eta, a->hp, a->ht, a->step, a->angvel, a->phase);
 }
 
@@ -577,7 +586,7 @@ int adv_graph_steps() { return kAdvGraphSteps; }
 
 void adv_lsq_flux(AdvDev* a, double* flux, const double* v, const double* h_total, cudaStream_t s)
 {
-    k_lsq_flux<<<(a->E + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->lcol, a->lval, a->dist, a->fnode, a->E,
+    k_lsq_flux<<<(a->E + kAdvThreads - 1) / kAdvThreads, kAdvThreads, 0, s>>>(a->lcol, a->lval, a->dx2, a->fnode, a->E,
                                                                              a->Ep, v, h_total, flux);
 }
 

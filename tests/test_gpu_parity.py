@@ -92,8 +92,8 @@ def test_momentum_advection(grid_dir, level):
 @pytest.mark.parametrize("level", [2, 3, 4])
 def test_lsq_flux(grid_dir, level):
     """interpolateLSQFlux (src/interpolation.cpp:311-356): the device flux against the oracle.  Both build
-    the second-derivative rows with the same host arithmetic, and the kernel rounds every product and sum
-    separately, so the two agree to the last bits."""
+    the second-derivative rows with the same host arithmetic; the kernel sums the rows with fused
+    multiply-adds, so the two agree to a few units in the last place of the flux."""
     orc, gpu = _pair(grid_dir / f"grid_{level}.txt")
     rng = np.random.default_rng(20 + level)
     v = rng.standard_normal(orc.E)
