@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -545,7 +547,18 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     c->Ep = pad128(m.E);
     c->Np = pad128(m.N);
     c->r = m.r;
-    c->eb = (m.E + kStepThreads - 1) / kStepThreads;
+    // threads per block of the graph path's face and cell kernels; ODIS_STEP_BLOCKS="face,cell" overrides
+    c->sc.face_threads = kFaceThreads;
+    c->sc.cell_threads = kCellThreads;
+    if (const char* env = std::getenv("ODIS_STEP_BLOCKS")) {
+        int f = 0, cl = 0;
+        if (std::sscanf(env, "%d,%d", &f, &cl) == 2 && f >= 64 && f <= kStepThreads && f % 64 == 0 && cl >= 32 &&
+            cl <= kStepThreads && cl % 32 == 0) {
+            c->sc.face_threads = f;
+            c->sc.cell_threads = cl;
+        }
+    }
+    c->eb = (m.E + c->sc.face_threads - 1) / c->sc.face_threads;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return ODIS_ERR_CUDA;
     c->own_stream = true;
     DevArena& A = c->mem;
