@@ -306,7 +306,8 @@ def run_ours(args) -> dict:
     for key, prec, lmax, tc, adv in (("df64_sh16", g.DF64, LMAX, None, 0), ("fp64_sh16", g.FP64, LMAX, None, 0),
                                      ("fp32_sh16", g.FP32, LMAX, None, 0), ("fp32_sh16_tc", g.FP32, LMAX, "1", 0),
                                      ("df64_plain", g.DF64, 0, None, 0), ("fp64_plain", g.FP64, 0, None, 0),
-                                     ("fp32_plain", g.FP32, 0, None, 0), ("fp64_advection", g.FP64, 0, None, 1)):
+                                     ("fp32_plain", g.FP32, 0, None, 0), ("fp64_advection", g.FP64, 0, None, 1),
+                                     ("df64_advection", g.DF64, 0, None, 1)):
         s = solver(prec, lmax, tc, adv)
         t, _ = timed_orbits(s, kv, 1, collective=False)     # rank 0 only
         if key != "df64_sh16":
@@ -318,7 +319,8 @@ def run_ours(args) -> dict:
         s.close()
     errors = {}
     for key, ref in (("fp32_sh16", "fp64_sh16"), ("fp32_sh16_tc", "fp64_sh16"), ("df64_sh16", "fp64_sh16"),
-                     ("fp32_plain", "fp64_plain"), ("df64_plain", "fp64_plain")):
+                     ("fp32_plain", "fp64_plain"), ("df64_plain", "fp64_plain"),
+                     ("df64_advection", "fp64_advection")):
         (va, ea, pa), (vb, eb_, pb) = finals[key], finals[ref]
         errors[f"{key}_vs_{ref}"] = {"eta": _rel(ea, eb_), "velocity": _rel(va, vb), "power": abs(pa - pb) / abs(pb),
                                      "orbits": 1 + kv}
@@ -357,9 +359,10 @@ def run_ours(args) -> dict:
                                                  "method": "ODIS_DF64: FP64-parity (1e-10) double-float arithmetic",
                                                  "sh_tiles_autotuned": tiles},
            "variants_cell_steps_per_s": results,
-           "nonlinear": {"cell_steps_per_s": results["fp64_advection"],
-                         "method": "ODIS_FP64, advection true: momentum advection + LSQ thickness flux, "
-                                   "7 kernels per step, AB3 steps replayed from a 64-step CUDA graph",
+           "nonlinear": {"cell_steps_per_s": results["df64_advection"],
+                         "fp64_cell_steps_per_s": results["fp64_advection"],
+                         "method": "ODIS_DF64 (FP64 parity), advection true: momentum advection + LSQ thickness "
+                                   "flux, 7 kernels per step, AB3 steps replayed from a 64-step CUDA graph",
                          "eta_gap_vs_linear": _rel(finals["fp64_advection"][1], finals["fp64_plain"][1]),
                          "power_gap_vs_linear": abs(finals["fp64_advection"][2] - finals["fp64_plain"][2])
                          / abs(finals["fp64_plain"][2])},
@@ -560,7 +563,8 @@ def main():
                     help="run a short level-6 case for an ncu capture (no timing, no JSON)")
     ap.add_argument("--case-sh", type=int, default=0, help="self-gravity degree of --profile-case")
     ap.add_argument("--case-level", type=int, default=LEVEL, help="mesh level of --profile-case (stable dt off level 6)")
-    ap.add_argument("--case-advection", action="store_true", help="--profile-case fp64: the nonlinear (advection) loop")
+    ap.add_argument("--case-advection", action="store_true",
+                    help="--profile-case fp64|df64: the nonlinear (advection) loop")
     ap.add_argument("--sur-train", type=int, default=4096)
     ap.add_argument("--sur-test", type=int, default=512)
     ap.add_argument("--sur-level", type=int, default=5)

@@ -188,8 +188,8 @@ int main(int argc, char** argv)
         return 2;
     }
     p.precision = prec == "fp32" ? ODIS_FP32 : prec == "df64" ? ODIS_DF64 : ODIS_FP64;
-    if (p.advection && p.precision != ODIS_FP64) {
-        std::fprintf(stderr, "odis_run: advection true runs the nonlinear equations in FP64\n");
+    if (p.advection && p.precision == ODIS_FP32) {
+        std::fprintf(stderr, "odis_run: advection true runs the nonlinear equations in FP64 or df64; using fp64\n");
         p.precision = ODIS_FP64;
     }
     odis_mesh* mesh = nullptr;

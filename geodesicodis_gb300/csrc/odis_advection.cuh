@@ -17,22 +17,22 @@ void adv_destroy(AdvDev* a);
 void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dvdt, const double* v,
                   const double* h_total, double* ekin, cudaStream_t s);
 double* adv_ekin_scratch(AdvDev* a);
-// state of an advective run, reference layout: v[E], eta[N], dvdt history [E][3],
-// detadt history [N][3], column thickness h + eta [N], forcing [N]
-struct AdvState {
-    double *v, *eta, *hv, *hp, *ht, *U;
-};
-// Ua/Ub: the forcing basis at the nodes, U(t) = cos(Omega t) Ua + sin(Omega t) Ub
-int adv_state_alloc(AdvDev* a, double h0, const std::vector<double>& Ua, const std::vector<double>& Ub, double angvel);
-AdvState adv_state(AdvDev* a);
-// what one advective step needs from the context
+// Run state in the method's number type (ODIS_FP64: double; ODIS_DF64: double-float
+// pairs), allocated once: v, eta, the AB3 histories, h + eta, the forcing at the
+// nodes.  Ua/Ub: the forcing basis at the nodes, U(t) = cos(Omega t) Ua + sin(Omega t) Ub.
+int adv_state_alloc(AdvDev* a, int precision, double h0, const std::vector<double>& Ua, const std::vector<double>& Ub);
+// reference layout on the host: v[E], eta[N], dvdt history [E][3], detadt history [N][3] (each nullable)
+int adv_get_state(AdvDev* a, double* v, double* eta, double* dvdt, double* detadt);
+int adv_set_state(AdvDev* a, const double* v, const double* eta, const double* dvdt, const double* detadt);
+// what one advective step needs from the context; the typed tables are in the
+// run's number type (double, or df64 for an ODIS_DF64 run)
 struct AdvStepArgs {
-    const double* rbf;        // [3][6][Np] Cartesian reconstruction blocks
+    const void* rbf;          // [3][6][Np] Cartesian reconstruction blocks
     const int* cell_face;     // [6][Np] cell-face table
     const int* nbr;           // [10][Ep] TRiSK neighbour faces
-    const double* w;          // [10][Ep] TRiSK weights (tangential velocity)
-    const double* nrm;        // [2][Ep] face normals
-    const double* area;       // [Ep] face areas
+    const void* w;            // [10][Ep] TRiSK weights (tangential velocity)
+    const void* nrm;          // [2][Ep] face normals
+    const void* area;         // [Ep] face areas
     double g, alpha, h0, dt;
     double divisor;           // 4 pi r^2
     int init_load;

@@ -19,6 +19,9 @@ template <> struct Ar<double> {
     __device__ static V add(V a, V b) { return a + b; }
     __device__ static V sub(V a, V b) { return a - b; }
     __device__ static V neg(V a) { return -a; }
+    __device__ static V div(V a, V b) { return a / b; }
+    __device__ static V abs(V a) { return ::fabs(a); }
+    __device__ static V half(V a) { return a * 0.5; }
     __device__ static V from(double x) { return x; }
     __device__ static double to(V a) { return a; }
     __device__ static V shfl(V a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
@@ -38,6 +41,9 @@ template <> struct Ar<float> {
     __device__ static V add(V a, V b) { return a + b; }
     __device__ static V sub(V a, V b) { return a - b; }
     __device__ static V neg(V a) { return -a; }
+    __device__ static V div(V a, V b) { return a / b; }
+    __device__ static V abs(V a) { return fabsf(a); }
+    __device__ static V half(V a) { return a * 0.5f; }
     __device__ static V from(double x) { return (float)x; }
     __device__ static double to(V a) { return (double)a; }
     __device__ static V shfl(V a, int o) { return __shfl_down_sync(0xffffffffu, a, o); }
@@ -57,6 +63,9 @@ template <> struct Ar<df64> {
     __device__ static V add(V a, V b) { return df_add(a, b); }
     __device__ static V sub(V a, V b) { return df_sub(a, b); }
     __device__ static V neg(V a) { return df_neg(a); }
+    __device__ static V div(V a, V b) { return df_div(a, b); }
+    __device__ static V abs(V a) { return df_abs(a); }
+    __device__ static V half(V a) { return df_scale2(a, 0.5f); }
     __device__ static V from(double x) { return df_from_double(x); }
     __device__ static double to(V a) { return df_to_double(a); }
     __device__ static V shfl(V a, int o) { return df_shfl_down(a, o); }

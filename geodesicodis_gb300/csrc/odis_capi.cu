@@ -90,6 +90,8 @@ struct odis_ctx {
     double* area = nullptr;      // [Ep]
     double* trig = nullptr;      // [10][Np]
     double* rbf = nullptr;       // [3][6][Np] Cartesian reconstruction blocks
+    // double-float copies of rbf, nrm and area for an ODIS_DF64 nonlinear run
+    float2 *rbf_df = nullptr, *nrm_df = nullptr, *area_df = nullptr;
     State<double> s64{};
     State<float> s32{};
     State<float2> sdf{};
@@ -533,7 +535,8 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     if (p->potential < ODIS_POT_NONE || p->potential > ODIS_POT_FULL) return ODIS_ERR_ARG;
     if (!(p->dt > 0.0) || !(p->g > 0.0) || !(p->h > 0.0) || !(p->radius > 0.0) || p->alpha < 0.0) return ODIS_ERR_ARG;
     if (p->sh_lmax < 0 || p->sh_lmax > 64 || (p->sh_lmax > 0 && !p->sh_factors)) return ODIS_ERR_ARG;
-    if (p->advection && (p->precision != ODIS_FP64 || p->sh_lmax > 0)) return ODIS_ERR_ARG;
+    if (p->advection && ((p->precision != ODIS_FP64 && p->precision != ODIS_DF64) || p->sh_lmax > 0))
+        return ODIS_ERR_ARG;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return ODIS_ERR_CUDA;
     std::unique_ptr<odis_ctx> c(new (std::nothrow) odis_ctx);
@@ -606,6 +609,17 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
         for (int i = 0; i < m.N; i++)
             for (int q = 0; q < 18; q++) soa[(size_t)q * c->Np + i] = blk[(size_t)i * 18 + q];
         c->rbf = A.upload(soa);
+        if (p->advection && p->precision == ODIS_DF64) {
+            auto df = [](const std::vector<double>& x) {
+                std::vector<float2> y(x.size());
+                for (size_t i = 0; i < x.size(); i++) y[i] = df_from_double(x[i]);
+                return y;
+            };
+            c->rbf_df = A.upload(df(soa));
+            c->nrm_df = A.upload(df(nrm));
+            c->area_df = A.upload(df(area));
+            if (!c->rbf_df || !c->nrm_df || !c->area_df) return ODIS_ERR_NOMEM;
+        }
     }
     if (!c->nrm || !c->area || !c->trig || !c->rbf) return ODIS_ERR_NOMEM;
 
@@ -663,7 +677,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     if (p->advection) {            // the nonlinear loop has its own operators and reference-layout state
         c->persist_ok = false;
         st = adv_create(&c->adv, m, p->angvel, c->Ep, c->Np);
-        if (st == ODIS_OK) st = adv_state_alloc(c->adv, p->h, Ua, Ub, p->angvel);
+        if (st == ODIS_OK) st = adv_state_alloc(c->adv, p->precision, p->h, Ua, Ub);
         if (st != ODIS_OK) return st;
     } else {
         st = choose_exec_path(c.get());
@@ -1007,7 +1021,11 @@ static odis_status run_advective(odis_ctx* c, int n, double* dpow)
     const odis_params& p = c->p;
     const int G = adv_graph_steps();
     const int per_step = adv_kernels_per_step();
-    const AdvStepArgs x{c->rbf, c->op64.cc.edge, c->op64.fc.nbr, c->op64.fc.w, c->nrm, c->area, p.g, p.alpha, p.h,
+    const bool df = p.precision == ODIS_DF64;
+    const AdvStepArgs x{df ? (const void*)c->rbf_df : (const void*)c->rbf, c->op64.cc.edge,
+                        df ? c->opdf.fc.nbr : c->op64.fc.nbr, df ? (const void*)c->opdf.fc.w : (const void*)c->op64.fc.w,
+                        df ? (const void*)c->nrm_df : (const void*)c->nrm,
+                        df ? (const void*)c->area_df : (const void*)c->area, p.g, p.alpha, p.h,
                         p.dt, 4 * kPi * std::pow(c->r, 2.0), p.init_load};
     auto step = [&](int it, double* out) { adv_step(c->adv, x, it, out, c->stream); };
     adv_set_step(c->adv, c->iter, p.dt, c->stream);
@@ -1206,14 +1224,7 @@ extern "C" odis_status odis_get_state(odis_ctx* c, int* iter, double* v, double*
     if (!c) return ODIS_ERR_ARG;
     ODIS_CK(cudaStreamSynchronize(c->stream));
     if (iter) *iter = (int)c->iter;
-    if (c->p.advection) {
-        const AdvState a = adv_state(c->adv);
-        if (v) ODIS_CK(cudaMemcpy(v, a.v, sizeof(double) * c->E, cudaMemcpyDeviceToHost));
-        if (eta) ODIS_CK(cudaMemcpy(eta, a.eta, sizeof(double) * c->N, cudaMemcpyDeviceToHost));
-        if (dvdt) ODIS_CK(cudaMemcpy(dvdt, a.hv, sizeof(double) * 3 * c->E, cudaMemcpyDeviceToHost));
-        if (detadt) ODIS_CK(cudaMemcpy(detadt, a.hp, sizeof(double) * 3 * c->N, cudaMemcpyDeviceToHost));
-        return ODIS_OK;
-    }
+    if (c->p.advection) return adv_get_state(c->adv, v, eta, dvdt, detadt);
     if (c->p.precision == ODIS_DF64) return get_state_t<float2>(c, c->sdf, v, eta, dvdt, detadt);
     return c->p.precision == ODIS_FP64 ? get_state_t<double>(c, c->s64, v, eta, dvdt, detadt)
                                        : get_state_t<float>(c, c->s32, v, eta, dvdt, detadt);
@@ -1226,11 +1237,8 @@ extern "C" odis_status odis_set_state(odis_ctx* c, int iter, const double* v, co
     ODIS_CK(cudaStreamSynchronize(c->stream));
     c->iter = iter;
     if (c->p.advection) {
-        const AdvState a = adv_state(c->adv);
-        if (v) ODIS_CK(cudaMemcpy(a.v, v, sizeof(double) * c->E, cudaMemcpyHostToDevice));
-        if (eta) ODIS_CK(cudaMemcpy(a.eta, eta, sizeof(double) * c->N, cudaMemcpyHostToDevice));
-        if (dvdt) ODIS_CK(cudaMemcpy(a.hv, dvdt, sizeof(double) * 3 * c->E, cudaMemcpyHostToDevice));
-        if (detadt) ODIS_CK(cudaMemcpy(a.hp, detadt, sizeof(double) * 3 * c->N, cudaMemcpyHostToDevice));
+        const int st = adv_set_state(c->adv, v, eta, dvdt, detadt);
+        if (st != ODIS_OK) return st;
         adv_thickness(c->adv, c->p.h, c->stream);   // src/timeIntegrator.cpp:203
         ODIS_CK(cudaStreamSynchronize(c->stream));
         return ODIS_OK;

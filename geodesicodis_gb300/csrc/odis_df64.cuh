@@ -92,6 +92,21 @@ __device__ __forceinline__ df64 df_fma_acc(df64 a, df64 b, df64 c)
 
 __device__ __forceinline__ df64 df_norm(df64 a) { return df_quick_two_sum(a.x, a.y); }
 
+// a / b (Dekker's long division in double-float): an FP32 quotient q1, the
+// remainder a - q1 b in double-float, one FP32 correction q2; about 2^-47 relative
+__device__ __forceinline__ df64 df_div(df64 a, df64 b)
+{
+    const float q1 = __fdiv_rn(a.x, b.x);
+    const df64 r = df_sub(a, df_mul(b, make_float2(q1, 0.f)));
+    const float q2 = __fdiv_rn(r.x, b.x);
+    return df_quick_two_sum(q1, q2);
+}
+
+__device__ __forceinline__ df64 df_abs(df64 a) { return a.x < 0.f ? df_neg(a) : a; }
+
+// a * 2^k for a power-of-two factor: exact on both words
+__device__ __forceinline__ df64 df_scale2(df64 a, float s) { return make_float2(a.x * s, a.y * s); }
+
 __device__ __forceinline__ df64 df_shfl_down(df64 a, int o)
 {
     return make_float2(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o));

@@ -91,7 +91,7 @@ typedef struct odis_params {
     const double* sh_factors; /* [sh_lmax+1] per-degree factors (0 and 1 unused); may be NULL if sh_lmax == 0 */
     int advection;          /* 1: the nonlinear equations ("advection true"): momentum advection
                                (src/momAdvection.cpp) and the LSQ thickness flux in the continuity
-                               equation (src/updateEta.cpp:22-32); ODIS_FP64 only, no self-gravity */
+                               equation (src/updateEta.cpp:22-32); ODIS_FP64 or ODIS_DF64, no self-gravity */
 } odis_params;
 
 /* Parsed input.in (src/globals.cpp:58-203 keys).  Strings are fixed-size. */

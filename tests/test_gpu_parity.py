@@ -101,11 +101,12 @@ def test_lsq_flux(grid_dir, level):
     assert rel_err(gpu.interpolateLSQFlux(v, ht), orc.interpolateLSQFlux(v, ht)) < 1e-13
 
 
-@pytest.mark.parametrize("level,steps", [(2, 700), (3, 400)])
-def test_advective_loop_parity(grid_dir, level, steps):
+@pytest.mark.parametrize("level,steps,precision", [(2, 700, 0), (3, 400, 0), (2, 700, 2), (3, 400, 2)])
+def test_advective_loop_parity(grid_dir, level, steps, precision):
     """ab3Explicit with advection true (src/timeIntegrator.cpp:205-269): momentum advection, the LSQ
-    thickness flux in the continuity equation and the column thickness update, against the oracle."""
-    orc, gpu = _pair(grid_dir / f"grid_{level}.txt", advection=1)
+    thickness flux in the continuity equation and the column thickness update, against the oracle,
+    in FP64 and in double-float (ODIS_DF64)."""
+    orc, gpu = _pair(grid_dir / f"grid_{level}.txt", precision=precision, advection=1)
     po, pg = orc.run(steps), gpu.run(steps)
     _, vo, eo, dvo, deo = orc.get_state()
     it, vg, eg, dvg, deg = gpu.get_state()
@@ -114,11 +115,12 @@ def test_advective_loop_parity(grid_dir, level, steps):
     assert rel_err(dvg, dvo) < 1e-10 and rel_err(deg, deo) < 1e-10
 
 
-def test_advective_graph_and_eager_steps_agree(grid_dir):
+@pytest.mark.parametrize("precision", [0, 2])
+def test_advective_graph_and_eager_steps_agree(grid_dir, precision):
     """The advective loop replays 64-step graphs for AB3 chunks and launches the rest eagerly; any
     chunking of the same steps gives the same bits."""
-    _, a = _pair(grid_dir / "grid_2.txt", advection=1)
-    _, b = _pair(grid_dir / "grid_2.txt", advection=1)
+    _, a = _pair(grid_dir / "grid_2.txt", precision=precision, advection=1)
+    _, b = _pair(grid_dir / "grid_2.txt", precision=precision, advection=1)
     pa = a.run(64 * 3 + 5)
     pb = np.concatenate([b.run(10), b.run(63), b.run(64 * 2 - 5), b.run(1)])
     np.testing.assert_array_equal(pa, pb)
@@ -126,11 +128,10 @@ def test_advective_graph_and_eager_steps_agree(grid_dir):
 
 
 def test_advection_options_are_checked(grid_dir):
-    """The nonlinear loop is FP64 only and excludes self-gravity."""
+    """The nonlinear loop runs in FP64 or double-float, and excludes self-gravity."""
     import geodesicodis_gb300 as g
     m = g.Mesh.from_file(grid_dir / "grid_2.txt", RADIUS)
-    for over in (dict(precision=g.FP32), dict(precision=g.DF64),
-                 dict(sh_lmax=4, sh_factors=np.ones(5))):
+    for over in (dict(precision=g.FP32), dict(sh_lmax=4, sh_factors=np.ones(5))):
         with pytest.raises(g.OdisError) as ei:
             g.Solver(g.make_params(**config0_params(), advection=1, **over), m)
         assert ei.value.code == g.ERR_ARG
