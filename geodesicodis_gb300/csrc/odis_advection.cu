@@ -15,8 +15,8 @@
 //                flux h_e v_e with h_e averaged from its two nodes, and h_e v_e q_e
 //   k_adv_node   per node: kinetic energy from the RBF Cartesian velocity
 //   k_adv_flux   per face: dvdt -= -sum_j w_j l_j / d_e (h_j v_j) (q_e + q_j) / 2
-//                (eq. 49), as q_e sum_j c_j (h v)_j + sum_j c_j (h v q)_j with
-//                c_j = w_j l_j / (2 d_e), then dvdt += -(G KE)_e
+//                (eq. 49), as (q_e sum_j c_j (h v)_j + sum_j c_j (h v q)_j) / 2 with
+//                c_j = w_j l_j / d_e (the TRiSK table), then dvdt += -(G KE)_e
 // Products are fused into the sums (the nonlinear loop is bound by GB300's FP64
 // issue rate), so the results match the FP64 restatement to rounding, not bit
 // for bit.
@@ -120,9 +120,11 @@ __global__ void k_adv_node(const T* __restrict__ rbf, const int* __restrict__ ed
 
 // kGrad: dvdt_e = ga (G eta)_e (gradient row in ascending node order), else
 // dvdt_e as given; then the PV flux and -(G KE)_e.  The flux
-// sum_j c_j (h v)_j (q_e + q_j) is formed as q_e sum_j c_j (h v)_j + sum_j c_j (h v q)_j.
+// sum_j w_j (h v)_j (q_e + q_j) / 2 is formed as (q_e sum_j w_j (h v)_j + sum_j w_j (h v q)_j) / 2
+// over the context's TRiSK table (w_j = w_ee' l_e' / d_e, zero in unused slots), the
+// same table the power kernel reads for the tangential velocity.
 template <class T, bool kGrad>
-__global__ void k_adv_flux(const int* __restrict__ fr, const T* __restrict__ cwh, const int* __restrict__ nfr,
+__global__ void k_adv_flux(const int* __restrict__ nbr, const T* __restrict__ tw,
                            const int* __restrict__ gcol, const T* __restrict__ gval, int E, int Ep,
                            const T* __restrict__ qe, const T* __restrict__ hve, const T* __restrict__ hvq,
                            const T* __restrict__ ek, T ga, const T* __restrict__ eta, T* __restrict__ dvdt)
@@ -136,14 +138,14 @@ __global__ void k_adv_flux(const int* __restrict__ fr, const T* __restrict__ cwh
     if constexpr (kGrad) d = A::mul(ga, A::fma(w1, eta[g1], A::mul(w0, eta[g0])));
     else d = dvdt[e];
     T s1 = A::zero(), s2 = A::zero();
-    const int n = nfr[e];
-    for (int j = 0; j < n; j++) {
-        const int f = fr[j * Ep + e];
-        const T c = cwh[j * Ep + e];
+#pragma unroll
+    for (int j = 0; j < kTrisk; j++) {
+        const int f = nbr[j * Ep + e];
+        const T c = tw[j * Ep + e];
         s1 = A::fma(c, hve[f], s1);
         s2 = A::fma(c, hvq[f], s2);
     }
-    d = A::add(d, A::fma(qe[e], s1, s2));
+    d = A::add(d, A::half(A::fma(qe[e], s1, s2)));
     d = A::sub(d, A::fma(w1, ek[g1], A::mul(w0, ek[g0])));
     dvdt[e] = d;
 }
@@ -398,15 +400,14 @@ T* dalloc(size_t n, bool zero = true)
 template <class T>
 struct AdvTab {
     T *vcoef = nullptr, *vwt = nullptr, *vf = nullptr;   // [3][Vp] curl, vertex-thickness weights; [Vp] f
-    T *cwh = nullptr;                                    // [10][Ep] TRiSK weight x length / (2 d_e)
     T *gval = nullptr;                                   // [2][Ep] gradient row, ascending node order
     T *lval = nullptr, *dx2 = nullptr;                   // [7][2 Ep] second-derivative rows; [Ep] d_e^2 / 12
     T *dval = nullptr;                                   // [6][Np] divergence rows
     void release()
     {
-        for (T* p : {vcoef, vwt, vf, cwh, gval, lval, dx2, dval}) cudaFree(p);
+        for (T* p : {vcoef, vwt, vf, gval, lval, dx2, dval}) cudaFree(p);
     }
-    bool ok() const { return vcoef && vwt && vf && cwh && gval && lval && dx2 && dval; }
+    bool ok() const { return vcoef && vwt && vf && gval && lval && dx2 && dval; }
 };
 
 // work arrays and the state of a run, in the method's number type
@@ -423,15 +424,14 @@ struct AdvWork {
 
 struct AdvDev {
     int V = 0, Vp = 0, E = 0, Ep = 0, N = 0, Np = 0;
-    int *vface = nullptr, *vnode = nullptr, *fvert = nullptr, *fnode = nullptr, *fr = nullptr, *nfr = nullptr,
-        *gcol = nullptr;
+    int *vface = nullptr, *vnode = nullptr, *fvert = nullptr, *fnode = nullptr, *gcol = nullptr;
     int* lcol = nullptr;         // [7][2 Ep] operatorDirectionalSecondDeriv rows
     int* dcol = nullptr;         // [6][Np] divergence rows, ascending face order (padded with zero weights)
     AdvTab<double> t64;          // FP64 tables: per-operator calls and ODIS_FP64 runs
     AdvTab<df64> tdf;            // double-float tables of an ODIS_DF64 run
     AdvWork<double> w64;         // FP64 work arrays (per-operator calls) and the ODIS_FP64 run state
     AdvWork<df64> wdf;           // the ODIS_DF64 run state
-    std::vector<double> host[8]; // FP64 tables kept on the host until the run's precision is known
+    std::vector<double> host[7]; // FP64 tables (vcoef, vwt, vf, gval, lval, dx2, dval) for a DF64 run's copies
     int prec = -1;               // precision of the run state, once allocated
     double angvel = 0.0;
     long long* step = nullptr;   // device step counter (forcing phase)
@@ -450,8 +450,7 @@ struct AdvDev {
 void adv_destroy(AdvDev* a)
 {
     if (!a) return;
-    for (void* p : {(void*)a->vface, (void*)a->vnode, (void*)a->fvert, (void*)a->fnode, (void*)a->fr, (void*)a->nfr,
-                    (void*)a->gcol, (void*)a->lcol, (void*)a->dcol, (void*)a->step, (void*)a->part, (void*)a->count,
+    for (void* p : {(void*)a->vface, (void*)a->vnode, (void*)a->fvert, (void*)a->fnode, (void*)a->gcol, (void*)a->lcol, (void*)a->dcol, (void*)a->step, (void*)a->part, (void*)a->count,
                     (void*)a->pbuf})
         cudaFree(p);
     a->t64.release();
@@ -468,11 +467,10 @@ static bool upload_tables(AdvDev* a, AdvTab<T>& t)
     t.vcoef = upload_as<T>(a->host[0]);
     t.vwt = upload_as<T>(a->host[1]);
     t.vf = upload_as<T>(a->host[2]);
-    t.cwh = upload_as<T>(a->host[3]);
-    t.gval = upload_as<T>(a->host[4]);
-    t.lval = upload_as<T>(a->host[5]);
-    t.dx2 = upload_as<T>(a->host[6]);
-    t.dval = upload_as<T>(a->host[7]);
+    t.gval = upload_as<T>(a->host[3]);
+    t.lval = upload_as<T>(a->host[4]);
+    t.dx2 = upload_as<T>(a->host[5]);
+    t.dval = upload_as<T>(a->host[6]);
     return t.ok();
 }
 
@@ -509,21 +507,13 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
         }
         vf[v] = -2 * angvel * std::sin(m.vert_sph[v * 2]);
     }
-    std::vector<int> fvert((size_t)2 * Ep, 0), fnode((size_t)2 * Ep, 0), fr((size_t)10 * Ep, 0), nfr(Ep, 0),
-        gcol((size_t)2 * Ep, 0);
-    std::vector<double> cwh((size_t)10 * Ep, 0.0), gval((size_t)2 * Ep, 0.0);
+    std::vector<int> fvert((size_t)2 * Ep, 0), fnode((size_t)2 * Ep, 0), gcol((size_t)2 * Ep, 0);
+    std::vector<double> gval((size_t)2 * Ep, 0.0);
     for (int e = 0; e < E; e++) {
         fvert[e] = m.face_verts[e * 2];
         fvert[(size_t)Ep + e] = m.face_verts[e * 2 + 1];
         fnode[e] = m.face_nodes[e * 2];
         fnode[(size_t)Ep + e] = m.face_nodes[e * 2 + 1];
-        nfr[e] = m.interp_n[e];
-        const double dr = 1.0 / m.face_dist[e];
-        for (int j = 0; j < m.interp_n[e]; j++) {
-            const int f = m.interp_friends[e * 10 + j];
-            fr[(size_t)j * Ep + e] = f;
-            cwh[(size_t)j * Ep + e] = m.interp_w[e * 10 + j] * m.face_len[f] * dr * 0.5;
-        }
         // operatorGradient row (src/mesh.cpp:3005-3120), ascending node order
         const int n0 = m.face_nodes[e * 2], n1 = m.face_nodes[e * 2 + 1];
         const double d = m.face_dist[e];
@@ -563,12 +553,12 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
         }
     }
     a->host[0] = std::move(vcoef); a->host[1] = std::move(vwt); a->host[2] = std::move(vf);
-    a->host[3] = std::move(cwh); a->host[4] = std::move(gval); a->host[5] = std::move(lv);
-    a->host[6] = std::move(dx2); a->host[7] = std::move(dvv);
+    a->host[3] = std::move(gval); a->host[4] = std::move(lv);
+    a->host[5] = std::move(dx2); a->host[6] = std::move(dvv);
     a->vface = upload_int(vface); a->vnode = upload_int(vnode); a->fvert = upload_int(fvert);
-    a->fnode = upload_int(fnode); a->fr = upload_int(fr); a->nfr = upload_int(nfr); a->gcol = upload_int(gcol);
+    a->fnode = upload_int(fnode); a->gcol = upload_int(gcol);
     a->lcol = upload_int(lc); a->dcol = upload_int(dc);
-    bool ok = a->vface && a->vnode && a->fvert && a->fnode && a->fr && a->nfr && a->gcol && a->lcol && a->dcol &&
+    bool ok = a->vface && a->vnode && a->fvert && a->fnode && a->gcol && a->lcol && a->dcol &&
               upload_tables<double>(a, a->t64);
     AdvWork<double>& w = a->w64;
     ok = ok && (w.q = dalloc<double>(Vp)) && (w.qe = dalloc<double>(Ep)) && (w.hve = dalloc<double>(Ep)) &&
@@ -592,13 +582,12 @@ static void momentum_head(AdvDev* a, const AdvTab<T>& t, AdvWork<T>& w, const T*
                                                               w.Ub, U);
 }
 
-void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dvdt, const double* v,
-                  const double* h_total, double* ekin, cudaStream_t s)
+void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, const int* nbr, const double* tw, double* dvdt,
+                  const double* v, const double* h_total, double* ekin, cudaStream_t s)
 {
     momentum_head<double>(a, a->t64, a->w64, rbf, cell_face, v, h_total, ekin, nullptr, s);
     k_adv_flux<double, false><<<(a->E + a->bf - 1) / a->bf, a->bf, 0, s>>>(
-        a->fr, a->t64.cwh, a->nfr, a->gcol, a->t64.gval, a->E, a->Ep, a->w64.qe, a->w64.hve, a->w64.hvq, ekin, 0.0,
-        nullptr, dvdt);
+        nbr, tw, a->gcol, a->t64.gval, a->E, a->Ep, a->w64.qe, a->w64.hve, a->w64.hvq, ekin, 0.0, nullptr, dvdt);
 }
 
 int adv_kernels_per_call() { return 4; }
@@ -665,8 +654,8 @@ static void step_t(AdvDev* a, const AdvTab<T>& t, AdvWork<T>& w, const AdvStepAr
     k.coef = host_cvt<T>(x.alpha * 1000.0 * x.h0);
     // updateMomentum, advection branch: -g G eta + PV flux - G KE
     momentum_head<T>(a, t, w, rbf, x.cell_face, w.v, w.ht, w.ek, w.U, s);
-    k_adv_flux<T, true><<<fb, a->bf, 0, s>>>(a->fr, t.cwh, a->nfr, a->gcol, t.gval, a->E, a->Ep, w.qe, w.hve, w.hvq,
-                                             w.ek, k.ga, w.eta, w.dv0);
+    k_adv_flux<T, true><<<fb, a->bf, 0, s>>>(x.nbr, tw, a->gcol, t.gval, a->E, a->Ep, w.qe, w.hve, w.hvq, w.ek, k.ga,
+                                             w.eta, w.dv0);
     k_adv_vstep<T><<<fb, a->bf, 0, s>>>(a->gcol, t.gval, a->E, a->Ep, k, iter, x.init_load, w.dv0, w.U, w.v, w.hv);
     // updateEta, advection branch: D (LSQ flux of h + eta); updateEnergy of the new v
     const PowerArgs<T> pa{x.nbr, tw, nrm, area, x.divisor, a->part, a->count, power};

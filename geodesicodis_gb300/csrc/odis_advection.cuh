@@ -13,9 +13,10 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np);
 void adv_destroy(AdvDev* a);
 // dvdt[E] += PV flux - G KE for velocity v[E] and column thickness h_total[N];
 // ekin[N] receives the kinetic energy (device; adv_ekin_scratch gives a buffer).
-// rbf / cell_face: the context's Cartesian reconstruction blocks and cell-face table.
-void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, double* dvdt, const double* v,
-                  const double* h_total, double* ekin, cudaStream_t s);
+// rbf / cell_face / nbr / tw: the context's Cartesian reconstruction blocks, cell-face
+// table and TRiSK table ([10][Ep] neighbours and weights w_ee' l_e' / d_e, FP64).
+void adv_momentum(AdvDev* a, const double* rbf, const int* cell_face, const int* nbr, const double* tw, double* dvdt,
+                  const double* v, const double* h_total, double* ekin, cudaStream_t s);
 double* adv_ekin_scratch(AdvDev* a);
 // Run state in the method's number type (ODIS_FP64: double; ODIS_DF64: double-float
 // pairs), allocated once: v, eta, the AB3 histories, h + eta, the forcing at the

@@ -795,7 +795,7 @@ extern "C" odis_status odis_momentum_advection(odis_ctx* c, const odis_mesh* mes
     double* dd = io.in(dvdt, c->E);
     double* dk = (mem == ODIS_MEM_DEVICE && ekin) ? ekin : (mem == ODIS_MEM_DEVICE ? adv_ekin_scratch(c->adv) : io.out(ekin));
     if (!dv || !dh || !dd) return ODIS_ERR_CUDA;
-    adv_momentum(c->adv, c->rbf, c->op64.cc.edge, dd, dv, dh, dk, c->stream);
+    adv_momentum(c->adv, c->rbf, c->op64.cc.edge, c->op64.fc.nbr, c->op64.fc.w, dd, dv, dh, dk, c->stream);
     c->launches += adv_kernels_per_call();
     int st = io.back(dvdt, dd, c->E);
     if (st == ODIS_OK && ekin) st = io.back(ekin, dk, c->N);
