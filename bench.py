@@ -361,6 +361,10 @@ def run_ours(args) -> dict:
            "variants_cell_steps_per_s": results,
            "nonlinear": {"cell_steps_per_s": results["df64_advection"],
                          "fp64_cell_steps_per_s": results["fp64_advection"],
+                         "bytes_per_step": nonlinear_bytes(N, E, mesh.n_vertices),
+                         "roofline_frac": {k: nonlinear_bytes(N, E, mesh.n_vertices) * results[k] / N / 1e9
+                                           / peak
+                                           for k in ("df64_advection", "fp64_advection")},
                          "method": "ODIS_DF64 (FP64 parity), advection true: momentum advection + LSQ thickness "
                                    "flux, 7 kernels per step, AB3 steps replayed from a 64-step CUDA graph",
                          "eta_gap_vs_linear": _rel(finals["fp64_advection"][1], finals["fp64_plain"][1]),
@@ -473,6 +477,23 @@ def run_sweep(args, fp64_plain: float, peak: float) -> dict:
             "timing": "host wall clock around the synchronous run call; inputs resident on the device"}
 
 
+def nonlinear_bytes(N: int, E: int, V: int, s: int = 8) -> int:
+    """Algorithmic bytes of one step of the nonlinear loop: every table, input and output of each of its
+    seven kernels once (s = 8 for FP64 and double-float values, 4-byte indices), gathered arrays once per
+    kernel that gathers them:
+      k_adv_pv         V (24 + 8s) + (E + N) s      curl and vertex-thickness rows, f, q; v and h
+      k_adv_edge       E (16 + 4s) + (V + N) s      vertex / node pairs, v, q_e, h v, h v q; q and h
+      k_adv_node       N (24 + 22s) + E s           cell faces, RBF blocks, KE, Ua, Ub, U; v
+      k_adv_flux       E (48 + 14s) + (2E + 2N) s   TRiSK table, gradient row, q_e, dvdt; h v, h v q, KE, eta
+      k_adv_vstep      E (8 + 10s) + N s            gradient row, v, AB3 history, dvdt; U
+      k_adv_lsq_power  E (104 + 30s) + N s          7-term rows, d^2/12, nodes, TRiSK table, normals, area, v,
+                                                    flux; h
+      k_adv_estep      N (24 + 14s) + E s           divergence rows, eta, AB3 history, h + eta; flux"""
+    return (V * (24 + 8 * s) + (E + N) * s + E * (16 + 4 * s) + (V + N) * s + N * (24 + 22 * s) + E * s
+            + E * (48 + 14 * s) + (2 * E + 2 * N) * s + E * (8 + 10 * s) + N * s + E * (104 + 30 * s) + N * s
+            + N * (24 + 14 * s) + E * s)
+
+
 def run_level8(args) -> dict:
     """configs[4]: level 8 (655362 cells), eccentricity + obliquity tide, h = 20 km, drag 1e-6, self-gravity
     l_max = 32; every method with and without self-gravity, `args.case_steps` timed steps each, errors of
@@ -496,10 +517,12 @@ def run_level8(args) -> dict:
     for name, prec, lmax, tc in (("fp32_sh32", g.FP32, 32, None), ("fp32_sh32_tc", g.FP32, 32, "1"),
                                  ("df64_sh32", g.DF64, 32, None), ("fp64_sh32", g.FP64, 32, None),
                                  ("fp32_plain", g.FP32, 0, None), ("df64_plain", g.DF64, 0, None),
-                                 ("fp64_plain", g.FP64, 0, None)):
+                                 ("fp64_plain", g.FP64, 0, None), ("df64_advection", g.DF64, 0, None),
+                                 ("fp64_advection", g.FP64, 0, None)):
+        adv = name.endswith("_advection")
         p = g.make_params(radius=RADIUS, g=GRAV, angvel=angvel, h=h, alpha=alpha, ecc=ECC, obliq=np.deg2rad(0.2),
                           dt=P / n, potential=g.POT_FULL, precision=prec, sh_lmax=lmax,
-                          sh_factors=fac if lmax else None)
+                          sh_factors=fac if lmax else None, advection=1 if adv else 0)
         with sh_path(tc):
             s = g.Solver(p, mesh)
         s.run(50)
@@ -509,6 +532,13 @@ def run_level8(args) -> dict:
         el = time.perf_counter() - t
         _, v, eta, _, _ = s.get_state()
         finals[name] = (v, eta, float(pw[-1]))
+        if adv:     # the nonlinear loop: whole-step time against its algorithmic bytes
+            nb = nonlinear_bytes(N, E, mesh.n_vertices)
+            out["methods"][name] = {"us_per_step": el / args.case_steps * 1e6,
+                                    "cell_steps_per_s": N * args.case_steps / el, "bytes_per_step": nb,
+                                    "hbm_frac": nb / (el / args.case_steps) / 1e9 / peak}
+            s.close()
+            continue
         ms = s.profile_kernels(20)
         sb = 4 if prec == g.FP32 else 8
         fb, cb = E * (19 * sb + 48), N * (13 * sb + 24)
@@ -519,7 +549,7 @@ def run_level8(args) -> dict:
             "sh_tiles": list(s.sh_tiles()) if lmax else None}
         s.close()
     for a, b in (("fp32_sh32", "fp64_sh32"), ("fp32_sh32_tc", "fp64_sh32"), ("df64_sh32", "fp64_sh32"),
-                 ("fp32_plain", "fp64_plain")):
+                 ("fp32_plain", "fp64_plain"), ("df64_advection", "fp64_advection")):
         (va, ea, pa), (vb, eb_, pb) = finals[a], finals[b]
         out[f"{a}_vs_{b}"] = {"v": _rel(va, vb), "eta": _rel(ea, eb_), "power": abs(pa - pb) / abs(pb),
                               "steps": 50 + args.case_steps}
