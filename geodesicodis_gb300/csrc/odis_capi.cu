@@ -20,8 +20,6 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <cstdio>
-#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -550,18 +548,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     c->Ep = pad128(m.E);
     c->Np = pad128(m.N);
     c->r = m.r;
-    // threads per block of the graph path's face and cell kernels; ODIS_STEP_BLOCKS="face,cell" overrides
-    c->sc.face_threads = kFaceThreads;
-    c->sc.cell_threads = kCellThreads;
-    if (const char* env = std::getenv("ODIS_STEP_BLOCKS")) {
-        int f = 0, cl = 0;
-        if (std::sscanf(env, "%d,%d", &f, &cl) == 2 && f >= 64 && f <= kStepThreads && f % 64 == 0 && cl >= 32 &&
-            cl <= kStepThreads && cl % 32 == 0) {
-            c->sc.face_threads = f;
-            c->sc.cell_threads = cl;
-        }
-    }
-    c->eb = (m.E + c->sc.face_threads - 1) / c->sc.face_threads;
+    c->eb = (m.E + kStepThreads - 1) / kStepThreads;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return ODIS_ERR_CUDA;
     c->own_stream = true;
     DevArena& A = c->mem;

@@ -49,8 +49,6 @@ struct StepConst {
     float2 df_dt, df_malpha, df_a, df_b, df_c;
     // and rounded to FP32 for the FP32-state variant (no per-thread conversions)
     float f_dt, f_malpha, f_a, f_b, f_c;
-    // threads per block of the face and cell kernels (host side; at most 256)
-    int face_threads, cell_threads;
 };
 
 // Mutable state of one instance.  The time level of v alternates between

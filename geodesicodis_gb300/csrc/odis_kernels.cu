@@ -52,7 +52,7 @@ __device__ __forceinline__ double block_sum(double x, double* smem)
     __syncthreads();
     double s = 0.0;
     if (wid == 0) {
-        s = lane < (int)(blockDim.x >> 5) ? smem[lane] : 0.0;
+        s = lane < kThreads / 32 ? smem[lane] : 0.0;
         s = warp_sum(s);
     }
     return s;
@@ -100,7 +100,7 @@ __device__ __forceinline__ double block_power(T pw, double* smem)
     __syncthreads();
     double s = 0.0;
     if (wid == 0) {
-        s = lane < (int)(blockDim.x >> 5) ? smem[lane] : 0.0;
+        s = lane < kStepThreads / 32 ? smem[lane] : 0.0;
         s = warp_sum(s);
     }
     return s;
@@ -496,23 +496,23 @@ template <class T, bool kMaster>
 void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
     if constexpr (kMaster) {
-        k_edge_step_f32x2<<<face_blocks(sc, true), sc.face_threads, 0, s>>>(fc, st, sc, offset);
+        k_edge_step_f32x2<<<face_blocks(sc, true), kStepThreads, 0, s>>>(fc, st, sc, offset);
     } else {
-        k_edge_step<T, kMaster><<<face_blocks(sc, false), sc.face_threads, 0, s>>>(fc, st, sc, offset);
+        k_edge_step<T, kMaster><<<face_blocks(sc, false), kStepThreads, 0, s>>>(fc, st, sc, offset);
     }
 }
 
 int face_blocks(const StepConst& sc, bool pairs)
 {
     const int n = pairs ? (sc.E + 1) / 2 : sc.E;
-    return (n + sc.face_threads - 1) / sc.face_threads;
+    return (n + kStepThreads - 1) / kStepThreads;
 }
 
 template <class T, bool kMaster>
 void launch_cell(const CellCoef<T>& cc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
-    const int cb = (sc.N + sc.cell_threads - 1) / sc.cell_threads;
-    k_cell_step<T, kMaster><<<cb, sc.cell_threads, 0, s>>>(cc, st, sc, offset);
+    const int cb = (sc.N + kStepThreads - 1) / kStepThreads;
+    k_cell_step<T, kMaster><<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset);
 }
 
 template <class T, bool kMaster>
@@ -528,8 +528,8 @@ void launch_power_tail(const FaceCoef<T>& fc, const State<T>& st, const StepCons
 {
     constexpr bool pairs = std::is_same<T, float>::value;
     const int eb = face_blocks(sc, pairs);
-    if constexpr (pairs) k_power_partial_f32x2<<<eb, sc.face_threads, 0, s>>>(fc, st, sc);
-    else k_power_partial<T><<<eb, sc.face_threads, 0, s>>>(fc, st, sc);
+    if constexpr (pairs) k_power_partial_f32x2<<<eb, kStepThreads, 0, s>>>(fc, st, sc);
+    else k_power_partial<T><<<eb, kStepThreads, 0, s>>>(fc, st, sc);
     launch_power_fold(st.partial, eb, n, st.power, s);
 }
 

@@ -5,9 +5,7 @@
 
 namespace odis {
 
-constexpr int kStepThreads = 256;    // largest block of the step kernels (shared-memory reduction sizes)
-constexpr int kFaceThreads = 256;    // default blocks of the fused step's face and cell kernels (a sweep
-constexpr int kCellThreads = 256;    // of 64-256 threads moved the level-6 step by at most 3 %)
+constexpr int kStepThreads = 256;
 
 template <class T, bool kMaster>
 void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s);

@@ -24,7 +24,7 @@ __device__ __forceinline__ double block_sum_df(df64 x, df64* smem)
     __syncthreads();
     df64 s = df_make(0.f, 0.f);
     if (wid == 0) {
-        s = lane < (int)(blockDim.x >> 5) ? smem[lane] : df_make(0.f, 0.f);
+        s = lane < kStepThreads / 32 ? smem[lane] : df_make(0.f, 0.f);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
     }
@@ -118,20 +118,20 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64
 
 void launch_edge_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
-    const int eb = (sc.E + sc.face_threads - 1) / sc.face_threads;
-    k_edge_step_df<<<eb, sc.face_threads, 0, s>>>(fc, st, sc, offset);
+    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
+    k_edge_step_df<<<eb, kStepThreads, 0, s>>>(fc, st, sc, offset);
 }
 
 void launch_cell_df(const CellCoef<df64>& cc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
-    const int cb = (sc.N + sc.cell_threads - 1) / sc.cell_threads;
-    k_cell_step_df<<<cb, sc.cell_threads, 0, s>>>(cc, st, sc, offset);
+    const int cb = (sc.N + kStepThreads - 1) / kStepThreads;
+    k_cell_step_df<<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset);
 }
 
 void launch_power_tail_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, int n, cudaStream_t s)
 {
-    const int eb = (sc.E + sc.face_threads - 1) / sc.face_threads;
-    k_power_partial_df<<<eb, sc.face_threads, 0, s>>>(fc, st, sc);
+    const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
+    k_power_partial_df<<<eb, kStepThreads, 0, s>>>(fc, st, sc);
     launch_power_fold(st.partial, eb, n, st.power, s);
 }
 
