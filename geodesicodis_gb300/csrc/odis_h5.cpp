@@ -9,7 +9,8 @@
 //   * the root group as a symbol table: a version-1 object header holding a
 //     symbol-table message, a version-1 B-tree of type 0 (one leaf node), symbol
 //     nodes of at most 2 x 4 entries in name order, and a local heap with the
-//     link names;
+//     link names and one trailing free block (whose next-block offset is 1, the
+//     library's end of list);
 //   * per dataset a version-1 object header with dataspace (version 1, current
 //     and maximum extents equal), IEEE float32 little-endian datatype, fill value
 //     (version 2, default fill), contiguous layout (version 3) and modification
@@ -152,6 +153,11 @@ extern "C" odis_status odis_h5_create(const char* path, int n, const char* const
         heap.u8(0);
         heap.pad_to((heap.b.size() + 7) / 8 * 8);
     }
+    // a trailing free block, as the library leaves one: offset of the next free
+    // block (1 = none) and this block's size
+    const uint64_t free_off = heap.b.size();
+    heap.u64(1);
+    heap.u64(16);
     const int nsnod = (n + 2 * kLeafK - 1) / (2 * kLeafK);
     const uint64_t a_root = kSuperblock, a_btree = a_root + kRootHeader, a_heap = a_btree + kBtreeNode;
     const uint64_t a_heap_data = a_heap + kHeapHeader, a_snod = a_heap_data + heap.b.size();
@@ -187,8 +193,8 @@ extern "C" odis_status odis_h5_create(const char* path, int n, const char* const
         o.u64(ds[order[last]].heap_off);
     }
     o.pad_to(a_heap);
-    // local heap, version 0, no free block
-    o.tag("HEAP"); o.u8(0); o.zeros(3); o.u64(heap.b.size()); o.u64(kUndef); o.u64(a_heap_data);
+    // local heap, version 0: data segment size, head of the free list, data segment address
+    o.tag("HEAP"); o.u8(0); o.zeros(3); o.u64(heap.b.size()); o.u64(free_off); o.u64(a_heap_data);
     o.b.insert(o.b.end(), heap.b.begin(), heap.b.end());
     // symbol nodes, version 1
     for (int s = 0; s < nsnod; s++) {

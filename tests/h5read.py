@@ -122,7 +122,17 @@ class H5File:
         if b[p:p + 4] != b"HEAP":
             raise H5Error("local heap signature")
         size, free, data = struct.unpack_from("<QQQ", b, p + 8)
-        return self._addr(data), size
+        data = self._addr(data)
+        # the free list: offsets inside the data segment, ended by 1 (as the library writes it)
+        seen = 0
+        while free != 1:
+            if free == UNDEF or free + 16 > size or seen > size:
+                raise H5Error("bad local heap free list")
+            free, fsize = struct.unpack_from("<QQ", b, data + free)
+            if fsize < 16:
+                raise H5Error("bad local heap free block")
+            seen += 1
+        return data, size
 
     def _heap_str(self, heap, off):
         data, size = heap
