@@ -461,6 +461,12 @@ void adv_destroy(AdvDev* a)
     delete a;
 }
 
+// the host copies of the FP64 tables are needed only for a double-float run's tables
+static void release_host(AdvDev* a)
+{
+    for (std::vector<double>& h : a->host) std::vector<double>().swap(h);
+}
+
 template <class T>
 static bool upload_tables(AdvDev* a, AdvTab<T>& t)
 {
@@ -474,7 +480,7 @@ static bool upload_tables(AdvDev* a, AdvTab<T>& t)
     return t.ok();
 }
 
-int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
+int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np, bool df64_run)
 {
     *out = nullptr;
     if (m.vert_area.empty()) return ODIS_ERR_MESH;
@@ -564,6 +570,7 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np)
     ok = ok && (w.q = dalloc<double>(Vp)) && (w.qe = dalloc<double>(Ep)) && (w.hve = dalloc<double>(Ep)) &&
          (w.hvq = dalloc<double>(Ep)) && (w.ek = dalloc<double>(Np));
     if (!ok) { adv_destroy(a); return ODIS_ERR_NOMEM; }
+    if (!df64_run) release_host(a);
     *out = a;
     return ODIS_OK;
 }
@@ -622,12 +629,13 @@ int adv_state_alloc(AdvDev* a, int precision, double h0, const std::vector<doubl
     int st = ODIS_OK;
     if (precision == ODIS_DF64) {
         if (!a->blocks_fixed) a->bn = a->bf = a->bp = 256;
-        if (!upload_tables<df64>(a, a->tdf)) return ODIS_ERR_NOMEM;
+        if (a->host[0].empty() || !upload_tables<df64>(a, a->tdf)) return ODIS_ERR_NOMEM;
         st = alloc_run<df64>(a, a->wdf, h0, Ua, Ub);
     } else {
         st = alloc_run<double>(a, a->w64, h0, Ua, Ub);
     }
     if (st != ODIS_OK) return st;
+    release_host(a);
     a->prec = precision;
     return cudaDeviceSynchronize() == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
 }

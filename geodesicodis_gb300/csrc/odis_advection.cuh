@@ -9,7 +9,9 @@ namespace odis {
 
 struct AdvDev;
 
-int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np);
+// df64_run: the context will run the loop in double-float (keeps the host copies of
+// the tables until adv_state_alloc converts them)
+int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np, bool df64_run = false);
 void adv_destroy(AdvDev* a);
 // dvdt[E] += PV flux - G KE for velocity v[E] and column thickness h_total[N];
 // ekin[N] receives the kinetic energy (device; adv_ekin_scratch gives a buffer).

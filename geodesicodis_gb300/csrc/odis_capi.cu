@@ -663,7 +663,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     if (cudaDeviceSynchronize() != cudaSuccess) return ODIS_ERR_CUDA;
     if (p->advection) {            // the nonlinear loop has its own operators and reference-layout state
         c->persist_ok = false;
-        st = adv_create(&c->adv, m, p->angvel, c->Ep, c->Np);
+        st = adv_create(&c->adv, m, p->angvel, c->Ep, c->Np, p->precision == ODIS_DF64);
         if (st == ODIS_OK) st = adv_state_alloc(c->adv, p->precision, p->h, Ua, Ub);
         if (st != ODIS_OK) return st;
     } else {
