@@ -133,3 +133,34 @@ def test_cli_writes_data_h5(built, tmp_path):
                                                         / np.pi).astype(np.float32))
     np.testing.assert_array_equal(a["face longitude"], (mesh.field(5).astype(np.float32).astype(np.float64) * 180.0
                                                          / np.pi).astype(np.float32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_cli_nonlinear_run(built, tmp_path, precision):
+    """The reference's default mode, advection true, through the driver in FP64 and in double-float:
+    the final state equals the library's run of the same steps, and DATA/data.h5 holds the dumps."""
+    import geodesicodis_gb300 as g
+    import h5read
+    d = _rundir(tmp_path)
+    text = (d / "input.in").read_text().replace("advection;                     false;",
+                                                "advection;                     true;")
+    assert "advection;                     true;" in text
+    (d / "input.in").write_text(text + OUTPUT_KEYS)
+    r = subprocess.run([str(CLI), "--dir", str(d), "--orbits", "0.1", "--precision", precision],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    inp = g.read_input(d / "input.in")
+    assert inp.params.advection == 1
+    mesh = g.Mesh.generate(inp.grid_level - 1, inp.params.radius)
+    p = inp.params
+    p.precision = g.DF64 if precision == "df64" else g.FP64
+    sol = g.Solver(p, mesh)
+    sol.run(200, power=False)
+    _, v, eta, _, _ = sol.get_state()
+    vf = np.loadtxt(d / "InitialConditions" / "vel_init.txt", delimiter=",")[:, 0]
+    assert np.max(np.abs(vf - v)) <= 1e-6 * np.max(np.abs(v))
+    ds = h5read.H5File(d / "DATA" / "data.h5").datasets()
+    assert ds["displacement"].shape == (2, mesh.n_cells)
+    last = ds["displacement"].read()[1]
+    assert np.max(np.abs(last - eta.astype(np.float32))) <= 1e-6 * np.max(np.abs(eta))

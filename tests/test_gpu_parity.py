@@ -127,6 +127,22 @@ def test_advective_graph_and_eager_steps_agree(grid_dir, precision):
     np.testing.assert_array_equal(a.get_state()[2], b.get_state()[2])
 
 
+def test_operator_calls_on_a_double_float_nonlinear_context(grid_dir):
+    """The per-operator calls stay FP64 on a context whose nonlinear loop runs in double-float."""
+    orc, gpu = _pair(grid_dir / "grid_3.txt", precision=2, advection=1)
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(orc.E)
+    ht = 1e4 + 10 * rng.standard_normal(orc.N)
+    assert rel_err(gpu.interpolateLSQFlux(v, ht), orc.interpolateLSQFlux(v, ht)) < 1e-13
+    d0 = rng.standard_normal(orc.E)
+    dg, _ = gpu.calculateMomentumAdvection(d0, v, ht)
+    do, _ = orc.calculateMomentumAdvection(d0, v, ht)
+    assert rel_err(dg, do) < 1e-9
+    gpu.run(70)                       # and the loop itself still runs after them
+    orc.run(70)
+    assert rel_err(gpu.get_state()[2], orc.get_state()[2]) < 1e-10
+
+
 def test_advection_options_are_checked(grid_dir):
     """The nonlinear loop runs in FP64 or double-float, and excludes self-gravity."""
     import geodesicodis_gb300 as g
