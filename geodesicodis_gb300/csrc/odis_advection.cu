@@ -211,6 +211,20 @@ __device__ __forceinline__ void ab3_step(T& s, T* h, int iter, const AdvK<T>& k,
     }
 }
 
+// AB3 of unknown i with the new tendency f: the history is slot-outermost
+// ([3][P]: slot 0 the latest tendency, as the reference's [n][3] columns), so the
+// three slot accesses of a warp are each one contiguous run
+template <class T>
+__device__ __forceinline__ void ab3_slots(T& s, T f, T* __restrict__ hist, int i, int P, int iter, const AdvK<T>& k,
+                                          int init_load)
+{
+    T h[3] = {f, hist[P + i], hist[2 * P + i]};
+    ab3_step<T>(s, h, iter, k, init_load);
+    hist[i] = h[0];
+    hist[P + i] = h[1];
+    hist[2 * P + i] = h[2];
+}
+
 // momentum update: drag_e = -alpha v_e + (G U)_e from the velocity before the
 // step, history slot 0 = dvdt, AB3, then v += dt drag (src/timeIntegrator.cpp:213-242).
 // U: the forcing at the nodes at t + dt (k_adv_node).
@@ -225,9 +239,7 @@ __global__ void k_adv_vstep(const int* __restrict__ gcol, const T* __restrict__ 
     const T gu = A::fma(gval[Ep + e], U[gcol[Ep + e]], A::mul(gval[e], U[gcol[e]]));
     T ve = v[e];
     const T drag = A::fma(k.malpha, ve, gu);
-    T* h = hist + (size_t)e * 3;
-    h[0] = dv0[e];
-    ab3_step<T>(ve, h, iter, k, init_load);
+    ab3_slots<T>(ve, dv0[e], hist, e, Ep, iter, k, init_load);
     v[e] = A::fma(k.dt, drag, ve);
 }
 
@@ -332,10 +344,8 @@ __global__ void k_adv_estep(const int* __restrict__ dcol, const T* __restrict__ 
     T t = A::zero();
 #pragma unroll
     for (int j = 0; j < 6; j++) t = A::fma(dval[j * Np + i], flux[dcol[j * Np + i]], t);
-    T* h = hist + (size_t)i * 3;
-    h[0] = t;
     T s = eta[i];
-    ab3_step<T>(s, h, iter, k, init_load);
+    ab3_slots<T>(s, t, hist, i, Np, iter, k, init_load);
     eta[i] = s;
     ht[i] = A::add(k.h0, s);
 }
@@ -441,8 +451,8 @@ struct AdvDev {
     // threads per block for the node/vertex, face, and LSQ + power kernels.  FP64: small
     // blocks spread the FP64-issue-bound one-wave grids evenly over the SMs (level 6:
     // 45.7 us/step against 49.4 us with 256 threads); DF64 is fastest with 256 (42.4
-    // against 44.8 us).  ODIS_ADV_BLOCKS="n,f,p" overrides both.
-    int bn = 64, bf = 64, bp = 128;
+    // against 44.8 us).  ODIS_ADV_BLOCKS="n,f,p[,v,e]" overrides both.
+    int bn = 64, bf = 64, bp = 128, bv = 64, be = 64;   // + AB3 kernels: vstep, estep
     bool blocks_fixed = false;
     cudaGraphExec_t graph = nullptr;
 };
@@ -486,10 +496,14 @@ int adv_create(AdvDev** out, const Mesh& m, double angvel, int Ep, int Np, bool 
     if (m.vert_area.empty()) return ODIS_ERR_MESH;
     AdvDev* a = new AdvDev;
     if (const char* env = std::getenv("ODIS_ADV_BLOCKS")) {
-        int x = 0, y = 0, z = 0;
-        if (std::sscanf(env, "%d,%d,%d", &x, &y, &z) == 3 && x >= 32 && y >= 32 && z >= 32 && x <= 256 && y <= 256 &&
-            z <= 256 && x % 32 == 0 && y % 32 == 0 && z % 32 == 0) {
-            a->bn = x; a->bf = y; a->bp = z;
+        int b[5] = {0, 0, 0, 0, 0};
+        const int got = std::sscanf(env, "%d,%d,%d,%d,%d", &b[0], &b[1], &b[2], &b[3], &b[4]);
+        bool ok = got == 3 || got == 5;
+        for (int k = 0; k < got && ok; k++) ok = b[k] >= 32 && b[k] <= 256 && b[k] % 32 == 0;
+        if (ok) {
+            a->bn = b[0]; a->bf = b[1]; a->bp = b[2];
+            a->bv = got == 5 ? b[3] : b[1];
+            a->be = got == 5 ? b[4] : b[0];
             a->blocks_fixed = true;
         }
     }
@@ -628,7 +642,7 @@ int adv_state_alloc(AdvDev* a, int precision, double h0, const std::vector<doubl
         return ODIS_ERR_NOMEM;
     int st = ODIS_OK;
     if (precision == ODIS_DF64) {
-        if (!a->blocks_fixed) a->bn = a->bf = a->bp = 256;
+        if (!a->blocks_fixed) a->bn = a->bf = a->bp = a->bv = a->be = 256;
         if (a->host[0].empty() || !upload_tables<df64>(a, a->tdf)) return ODIS_ERR_NOMEM;
         st = alloc_run<df64>(a, a->wdf, h0, Ua, Ub);
     } else {
@@ -650,7 +664,8 @@ template <class T>
 static void step_t(AdvDev* a, const AdvTab<T>& t, AdvWork<T>& w, const AdvStepArgs& x, const T* rbf, const T* tw,
                    const T* nrm, const T* area, int iter, double* power, cudaStream_t s)
 {
-    const int fb = (a->E + a->bf - 1) / a->bf, pb = (a->E + a->bp - 1) / a->bp, nb = (a->N + a->bn - 1) / a->bn;
+    const int fb = (a->E + a->bf - 1) / a->bf, pb = (a->E + a->bp - 1) / a->bp;
+    const int vb = (a->E + a->bv - 1) / a->bv, nb = (a->N + a->be - 1) / a->be;
     AdvK<T> k;
     k.a = host_cvt<T>(23. / 12.);
     k.b = host_cvt<T>(-16. / 12.);
@@ -664,12 +679,12 @@ static void step_t(AdvDev* a, const AdvTab<T>& t, AdvWork<T>& w, const AdvStepAr
     momentum_head<T>(a, t, w, rbf, x.cell_face, w.v, w.ht, w.ek, w.U, s);
     k_adv_flux<T, true><<<fb, a->bf, 0, s>>>(x.nbr, tw, a->gcol, t.gval, a->E, a->Ep, w.qe, w.hve, w.hvq, w.ek, k.ga,
                                              w.eta, w.dv0);
-    k_adv_vstep<T><<<fb, a->bf, 0, s>>>(a->gcol, t.gval, a->E, a->Ep, k, iter, x.init_load, w.dv0, w.U, w.v, w.hv);
+    k_adv_vstep<T><<<vb, a->bv, 0, s>>>(a->gcol, t.gval, a->E, a->Ep, k, iter, x.init_load, w.dv0, w.U, w.v, w.hv);
     // updateEta, advection branch: D (LSQ flux of h + eta); updateEnergy of the new v
     const PowerArgs<T> pa{x.nbr, tw, nrm, area, x.divisor, a->part, a->count, power};
     k_adv_lsq_power<T><<<pb, a->bp, 0, s>>>(a->lcol, t.lval, t.dx2, a->fnode, a->E, a->Ep, w.v, w.ht, w.flux, k.coef,
                                             pa);
-    k_adv_estep<T><<<nb + 1, a->bn, 0, s>>>(a->dcol, t.dval, a->N, a->Np, k, iter, x.init_load, w.flux, w.eta, w.hp,
+    k_adv_estep<T><<<nb + 1, a->be, 0, s>>>(a->dcol, t.dval, a->N, a->Np, k, iter, x.init_load, w.flux, w.eta, w.hp,
                                             w.ht, a->step, x.dt, a->angvel, w.phase);
 }
 
@@ -693,65 +708,75 @@ void adv_thickness(AdvDev* a, double h0, cudaStream_t s)
 }
 
 template <class T>
-static int get_t(const T* d, size_t n, double* out)
+static double to_host_double(T x)
+{
+    if constexpr (std::is_same<T, df64>::value) return df_to_double(x);
+    else return x;
+}
+
+// device values -> host doubles; with stride P: the [3][P] history -> the reference's [n][3]
+template <class T>
+static int get_t(const T* d, size_t n, double* out, size_t P = 0)
 {
     if (!out) return ODIS_OK;
-    std::vector<T> h(n);
-    if (cudaMemcpy(h.data(), d, sizeof(T) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return ODIS_ERR_CUDA;
-    for (size_t i = 0; i < n; i++) {
-        if constexpr (std::is_same<T, df64>::value) out[i] = df_to_double(h[i]);
-        else out[i] = h[i];
+    const size_t m = P ? 3 * P : n;
+    std::vector<T> h(m);
+    if (cudaMemcpy(h.data(), d, sizeof(T) * m, cudaMemcpyDeviceToHost) != cudaSuccess) return ODIS_ERR_CUDA;
+    if (!P) {
+        for (size_t i = 0; i < n; i++) out[i] = to_host_double(h[i]);
+    } else {
+        for (size_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) out[3 * i + k] = to_host_double(h[(size_t)k * P + i]);
     }
     return ODIS_OK;
 }
 
 template <class T>
-static int set_t(T* d, size_t n, const double* in)
+static int set_t(T* d, size_t n, const double* in, size_t P = 0)
 {
     if (!in) return ODIS_OK;
-    std::vector<T> h(n);
-    for (size_t i = 0; i < n; i++) h[i] = host_cvt<T>(in[i]);
-    return cudaMemcpy(d, h.data(), sizeof(T) * n, cudaMemcpyHostToDevice) == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
+    const size_t m = P ? 3 * P : n;
+    std::vector<T> h(m, host_cvt<T>(0.0));
+    if (!P) {
+        for (size_t i = 0; i < n; i++) h[i] = host_cvt<T>(in[i]);
+    } else {
+        for (size_t i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) h[(size_t)k * P + i] = host_cvt<T>(in[3 * i + k]);
+    }
+    return cudaMemcpy(d, h.data(), sizeof(T) * m, cudaMemcpyHostToDevice) == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
+}
+
+template <class T>
+static int get_state_t(AdvDev* a, const AdvWork<T>& w, double* v, double* eta, double* dvdt, double* detadt)
+{
+    int st = get_t(w.v, a->E, v);
+    if (st == ODIS_OK) st = get_t(w.eta, a->N, eta);
+    if (st == ODIS_OK) st = get_t(w.hv, a->E, dvdt, a->Ep);
+    if (st == ODIS_OK) st = get_t(w.hp, a->N, detadt, a->Np);
+    return st;
+}
+
+template <class T>
+static int set_state_t(AdvDev* a, AdvWork<T>& w, const double* v, const double* eta, const double* dvdt,
+                       const double* detadt)
+{
+    int st = set_t(w.v, a->E, v);
+    if (st == ODIS_OK) st = set_t(w.eta, a->N, eta);
+    if (st == ODIS_OK) st = set_t(w.hv, a->E, dvdt, a->Ep);
+    if (st == ODIS_OK) st = set_t(w.hp, a->N, detadt, a->Np);
+    return st;
 }
 
 int adv_get_state(AdvDev* a, double* v, double* eta, double* dvdt, double* detadt)
 {
-    const size_t E = a->E, N = a->N;
-    int st = ODIS_OK;
-    if (a->prec == ODIS_DF64) {
-        const AdvWork<df64>& w = a->wdf;
-        if (st == ODIS_OK) st = get_t(w.v, E, v);
-        if (st == ODIS_OK) st = get_t(w.eta, N, eta);
-        if (st == ODIS_OK) st = get_t(w.hv, 3 * E, dvdt);
-        if (st == ODIS_OK) st = get_t(w.hp, 3 * N, detadt);
-    } else {
-        const AdvWork<double>& w = a->w64;
-        if (st == ODIS_OK) st = get_t(w.v, E, v);
-        if (st == ODIS_OK) st = get_t(w.eta, N, eta);
-        if (st == ODIS_OK) st = get_t(w.hv, 3 * E, dvdt);
-        if (st == ODIS_OK) st = get_t(w.hp, 3 * N, detadt);
-    }
-    return st;
+    return a->prec == ODIS_DF64 ? get_state_t(a, a->wdf, v, eta, dvdt, detadt)
+                                : get_state_t(a, a->w64, v, eta, dvdt, detadt);
 }
 
 int adv_set_state(AdvDev* a, const double* v, const double* eta, const double* dvdt, const double* detadt)
 {
-    const size_t E = a->E, N = a->N;
-    int st = ODIS_OK;
-    if (a->prec == ODIS_DF64) {
-        AdvWork<df64>& w = a->wdf;
-        if (st == ODIS_OK) st = set_t(w.v, E, v);
-        if (st == ODIS_OK) st = set_t(w.eta, N, eta);
-        if (st == ODIS_OK) st = set_t(w.hv, 3 * E, dvdt);
-        if (st == ODIS_OK) st = set_t(w.hp, 3 * N, detadt);
-    } else {
-        AdvWork<double>& w = a->w64;
-        if (st == ODIS_OK) st = set_t(w.v, E, v);
-        if (st == ODIS_OK) st = set_t(w.eta, N, eta);
-        if (st == ODIS_OK) st = set_t(w.hv, 3 * E, dvdt);
-        if (st == ODIS_OK) st = set_t(w.hp, 3 * N, detadt);
-    }
-    return st;
+    return a->prec == ODIS_DF64 ? set_state_t(a, a->wdf, v, eta, dvdt, detadt)
+                                : set_state_t(a, a->w64, v, eta, dvdt, detadt);
 }
 
 double* adv_graph_power(AdvDev* a) { return a->pbuf; }
