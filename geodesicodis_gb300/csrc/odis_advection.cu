@@ -165,8 +165,12 @@ __device__ __forceinline__ T lsq_flux_at(int e, int Ep, const int* __restrict__ 
     T d2i = A::zero(), d2o = A::zero();
 #pragma unroll
     for (int j = 0; j < 7; j++) {
-        d2i = A::fma(val[j * R + 2 * e], h[col[j * R + 2 * e]], d2i);
-        d2o = A::fma(val[j * R + 2 * e + 1], h[col[j * R + 2 * e + 1]], d2o);
+        // the inner and outer rows' j-th terms are adjacent: one 16-byte load of each pair
+        T vi, vo;
+        A::ld2(val + j * R + 2 * e, vi, vo);
+        const int2 c = *reinterpret_cast<const int2*>(col + j * R + 2 * e);
+        d2i = A::fma(vi, h[c.x], d2i);
+        d2o = A::fma(vo, h[c.y], d2o);
     }
     const T dx2 = dx2v[e];
     const T a = A::mul(A::half(vel), A::add(h[fnode[e]], h[fnode[Ep + e]]));
