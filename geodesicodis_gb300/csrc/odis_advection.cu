@@ -17,9 +17,10 @@
 //   k_adv_flux   per face: dvdt -= -sum_j w_j l_j / d_e (h_j v_j) (q_e + q_j) / 2
 //                (eq. 49), as (q_e sum_j c_j (h v)_j + sum_j c_j (h v q)_j) / 2 with
 //                c_j = w_j l_j / d_e (the TRiSK table), then dvdt += -(G KE)_e
-// Products are fused into the sums (the nonlinear loop is bound by GB300's FP64
+// Products are fused into the sums (in FP64 the loop is bound by GB300's FP64
 // issue rate), so the results match the FP64 restatement to rounding, not bit
-// for bit.
+// for bit.  The AB3 histories are slot-outermost on the device ([3][n]);
+// adv_get_state / adv_set_state convert to and from the reference's [n][3].
 //
 // One step of the advective loop (src/timeIntegrator.cpp:205-269) is seven kernels:
 //   k_adv_pv, k_adv_edge
@@ -41,7 +42,6 @@
 #include <cstdlib>
 #include <type_traits>
 #include <vector>
-
 
 namespace odis {
 
