@@ -35,6 +35,7 @@
 #include "odis_advection.cuh"
 #include "odis_arith.cuh"
 #include "odis_kernels.cuh"
+#include "odis_pdl.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -57,13 +58,7 @@ __device__ __forceinline__ double adv_warp_sum(double x)
     return x;
 }
 
-// Programmatic dependent launch: the kernels of a step are launched with
-// programmatic stream serialization, and each waits here, before any memory
-// access, until the previous kernel has completed and its writes are visible (a
-// no-op for an ordinary launch).  The CTAs trigger their dependents implicitly when
-// they exit; an explicit trigger on entry was slower (30.0 -> 38.7 us per DF64 step
-// at level 6), because the next kernels' CTAs then occupied the SMs while waiting.
-__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 
 // vwt[j][i] = A_n R_j / A_v: the node's control-volume area times the kite
 // fraction over the vertex area, so that h_v = sum_j vwt_j h_n
@@ -73,7 +68,7 @@ __global__ void k_adv_pv(const int* __restrict__ vface, const T* __restrict__ vc
                          const T* __restrict__ h, T* __restrict__ q)
 {
     using A = Ar<T>;
-    pdl_enter();
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     T zeta = A::zero(), th = A::zero();
@@ -92,7 +87,7 @@ __global__ void k_adv_edge(const int* __restrict__ fvert, const int* __restrict_
                            T* __restrict__ qe, T* __restrict__ hve, T* __restrict__ hvq)
 {
     using A = Ar<T>;
-    pdl_enter();
+    pdl_wait();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     const T qv = A::half(A::add(q[fvert[e]], q[fvert[Ep + e]]));
@@ -111,7 +106,7 @@ __global__ void k_adv_node(const T* __restrict__ rbf, const int* __restrict__ ed
                            const T* __restrict__ Ua, const T* __restrict__ Ub, T* __restrict__ U)
 {
     using A = Ar<T>;
-    pdl_enter();
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     T vf[kCellFaces];
@@ -141,7 +136,7 @@ __global__ void k_adv_flux(const int* __restrict__ nbr, const T* __restrict__ tw
                            const T* __restrict__ ek, T ga, const T* __restrict__ eta, T* __restrict__ dvdt)
 {
     using A = Ar<T>;
-    pdl_enter();
+    pdl_wait();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     const int g0 = gcol[e], g1 = gcol[Ep + e];
@@ -250,7 +245,7 @@ __global__ void k_adv_vstep(const int* __restrict__ gcol, const T* __restrict__ 
                             T* __restrict__ v, T* __restrict__ hist)
 {
     using A = Ar<T>;
-    pdl_enter();
+    pdl_wait();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     const T gu = A::fma(gval[Ep + e], U[gcol[Ep + e]], A::mul(gval[e], U[gcol[e]]));
@@ -284,7 +279,7 @@ k_adv_lsq_power(const int* __restrict__ col, const T* __restrict__ val, const T*
                 T* __restrict__ flux, T coef, PowerArgs<T> pa)
 {
     using A = Ar<T>;
-    pdl_enter();
+    pdl_wait();
     __shared__ double s_red[kAdvThreads / 32];
     __shared__ bool s_last;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -349,7 +344,7 @@ __global__ void k_adv_estep(const int* __restrict__ dcol, const T* __restrict__ 
                             double angvel, T* __restrict__ phase)
 {
     using A = Ar<T>;
-    pdl_enter();
+    pdl_wait();
     if (blockIdx.x == gridDim.x - 1) {
         if (threadIdx.x == 0) {
             const long long s = *step + 1;
@@ -382,33 +377,6 @@ __global__ void k_adv_set_step(long long* step, long long v, double dt, double a
 {
     *step = v;
     adv_phase<T>(v, dt, angvel, phase);
-}
-
-// launch with programmatic stream serialization (the kernels call pdl_enter first);
-// ODIS_PDL=0 launches them in plain stream order
-bool pdl_on()
-{
-    static const bool on = [] {
-        const char* e = std::getenv("ODIS_PDL");
-        return !(e && e[0] == '0');
-    }();
-    return on;
-}
-
-template <typename... KArgs, typename... Args>
-void pdl_launch(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s, Args... args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = pdl_on() ? 1 : 0;
-    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
 // host-side conversion of the FP64 tables to the method's number type
@@ -641,11 +609,11 @@ template <class T>
 static void momentum_head(AdvDev* a, const AdvTab<T>& t, AdvWork<T>& w, const T* rbf, const int* cell_face,
                           const T* v, const T* h_total, T* ekin, T* U, cudaStream_t s)
 {
-    pdl_launch(k_adv_pv<T>, (a->V + a->bn - 1) / a->bn, a->bn, s, a->vface, t.vcoef, a->vnode, t.vwt, t.vf, a->V,
+    pdl_launch(k_adv_pv<T>, (a->V + a->bn - 1) / a->bn, a->bn, 0, s, a->vface, t.vcoef, a->vnode, t.vwt, t.vf, a->V,
                a->Vp, v, h_total, w.q);
-    pdl_launch(k_adv_edge<T>, (a->E + a->bf - 1) / a->bf, a->bf, s, a->fvert, a->fnode, a->E, a->Ep, w.q, h_total, v,
+    pdl_launch(k_adv_edge<T>, (a->E + a->bf - 1) / a->bf, a->bf, 0, s, a->fvert, a->fnode, a->E, a->Ep, w.q, h_total, v,
                w.qe, w.hve, w.hvq);
-    pdl_launch(k_adv_node<T>, (a->N + a->bn - 1) / a->bn, a->bn, s, rbf, cell_face, a->N, a->Np, v, ekin, w.phase,
+    pdl_launch(k_adv_node<T>, (a->N + a->bn - 1) / a->bn, a->bn, 0, s, rbf, cell_face, a->N, a->Np, v, ekin, w.phase,
                w.Ua, w.Ub, U);
 }
 
@@ -723,15 +691,15 @@ static void step_t(AdvDev* a, const AdvTab<T>& t, AdvWork<T>& w, const AdvStepAr
     k.coef = host_cvt<T>(x.alpha * 1000.0 * x.h0);
     // updateMomentum, advection branch: -g G eta + PV flux - G KE
     momentum_head<T>(a, t, w, rbf, x.cell_face, w.v, w.ht, w.ek, w.U, s);
-    pdl_launch(k_adv_flux<T, true>, fb, a->bf, s, x.nbr, tw, a->gcol, t.gval, a->E, a->Ep, w.qe, w.hve, w.hvq, w.ek,
+    pdl_launch(k_adv_flux<T, true>, fb, a->bf, 0, s, x.nbr, tw, a->gcol, t.gval, a->E, a->Ep, w.qe, w.hve, w.hvq, w.ek,
                k.ga, w.eta, w.dv0);
-    pdl_launch(k_adv_vstep<T>, vb, a->bv, s, a->gcol, t.gval, a->E, a->Ep, k, iter, x.init_load, w.dv0, w.U, w.v,
+    pdl_launch(k_adv_vstep<T>, vb, a->bv, 0, s, a->gcol, t.gval, a->E, a->Ep, k, iter, x.init_load, w.dv0, w.U, w.v,
                w.hv);
     // updateEta, advection branch: D (LSQ flux of h + eta); updateEnergy of the new v
     const PowerArgs<T> pa{x.nbr, tw, nrm, area, x.divisor, a->part, a->count, power};
-    pdl_launch(k_adv_lsq_power<T>, pb, a->bp, s, a->lcol, t.lval, t.dx2, a->fnode, a->E, a->Ep, w.v, w.ht, w.flux,
+    pdl_launch(k_adv_lsq_power<T>, pb, a->bp, 0, s, a->lcol, t.lval, t.dx2, a->fnode, a->E, a->Ep, w.v, w.ht, w.flux,
                k.coef, pa);
-    pdl_launch(k_adv_estep<T>, nb + 1, a->be, s, a->dcol, t.dval, a->N, a->Np, k, iter, x.init_load, w.flux, w.eta,
+    pdl_launch(k_adv_estep<T>, nb + 1, a->be, 0, s, a->dcol, t.dval, a->N, a->Np, k, iter, x.init_load, w.flux, w.eta,
                w.hp, w.ht, a->step, x.dt, a->angvel, w.phase);
 }
 

@@ -22,6 +22,7 @@
 #include "odis_device.cuh"
 #include "odis_df64.cuh"
 #include "odis_kernels.cuh"
+#include "odis_pdl.cuh"
 
 #include <type_traits>
 
@@ -114,6 +115,7 @@ __device__ __forceinline__ double block_power(T pw, double* smem)
 template <class T, bool kMaster>
 __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, State<T> st, StepConst sc, int offset)
 {
+    pdl_wait();
     __shared__ double s_red[kStepThreads / 32];
     const long long it = *st.iter + offset;
     // forcing phase at t^{n+1} (precomputed per run by k_phase)
@@ -178,6 +180,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, Stat
 __global__ void __launch_bounds__(kStepThreads) k_edge_step_f32x2(FaceCoef<float> fc, State<float> st, StepConst sc,
                                                                      int offset)
 {
+    pdl_wait();
     __shared__ double s_red[kStepThreads / 32];
     const long long it = *st.iter + offset;
     const long long kstep = it - *st.run_first;
@@ -264,6 +267,7 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial_f32x2(FaceCoef<f
 template <class T, bool kMaster>
 __global__ void __launch_bounds__(kStepThreads) k_cell_step(CellCoef<T> cc, State<T> st, StepConst sc, int offset)
 {
+    pdl_wait();
     const long long it = *st.iter + offset;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int Np = sc.Np;
@@ -496,9 +500,9 @@ template <class T, bool kMaster>
 void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
     if constexpr (kMaster) {
-        k_edge_step_f32x2<<<face_blocks(sc, true), kStepThreads, 0, s>>>(fc, st, sc, offset);
+        pdl_launch(k_edge_step_f32x2, face_blocks(sc, true), kStepThreads, 0, s, fc, st, sc, offset);
     } else {
-        k_edge_step<T, kMaster><<<face_blocks(sc, false), kStepThreads, 0, s>>>(fc, st, sc, offset);
+        pdl_launch(k_edge_step<T, kMaster>, face_blocks(sc, false), kStepThreads, 0, s, fc, st, sc, offset);
     }
 }
 
@@ -512,7 +516,7 @@ template <class T, bool kMaster>
 void launch_cell(const CellCoef<T>& cc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
     const int cb = (sc.N + kStepThreads - 1) / kStepThreads;
-    k_cell_step<T, kMaster><<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset);
+    pdl_launch(k_cell_step<T, kMaster>, cb, kStepThreads, 0, s, cc, st, sc, offset);
 }
 
 template <class T, bool kMaster>

@@ -9,6 +9,7 @@
 #include "odis_device.cuh"
 #include "odis_df64.cuh"
 #include "odis_kernels.cuh"
+#include "odis_pdl.cuh"
 
 namespace odis {
 
@@ -37,6 +38,7 @@ __device__ __forceinline__ df64 ldg2(const df64* p) { return __ldg(p); }
 
 __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc, State<df64> st, StepConst sc, int offset)
 {
+    pdl_wait();
     __shared__ df64 s_red[kStepThreads / 32];
     const long long it = *st.iter + offset;
     const long long kstep = it - *st.run_first;        // forcing phase at t^{n+1}, precomputed per run
@@ -77,6 +79,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc
 
 __global__ void __launch_bounds__(kStepThreads) k_cell_step_df(CellCoef<df64> cc, State<df64> st, StepConst sc, int offset)
 {
+    pdl_wait();
     const long long it = *st.iter + offset;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int Np = sc.Np;
@@ -119,13 +122,13 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64
 void launch_edge_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
     const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
-    k_edge_step_df<<<eb, kStepThreads, 0, s>>>(fc, st, sc, offset);
+    pdl_launch(k_edge_step_df, eb, kStepThreads, 0, s, fc, st, sc, offset);
 }
 
 void launch_cell_df(const CellCoef<df64>& cc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
     const int cb = (sc.N + kStepThreads - 1) / kStepThreads;
-    k_cell_step_df<<<cb, kStepThreads, 0, s>>>(cc, st, sc, offset);
+    pdl_launch(k_cell_step_df, cb, kStepThreads, 0, s, cc, st, sc, offset);
 }
 
 void launch_power_tail_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, int n, cudaStream_t s)

@@ -23,6 +23,7 @@
 #include "odis_sh_tc.cuh"
 #include "odis_df64.cuh"
 #include "odis_arith.cuh"
+#include "odis_pdl.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -74,6 +75,7 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
                                                             const int* __restrict__ tiles, int nchunk,
                                                             T* __restrict__ part)
 {
+    pdl_wait();
     using A = Ar<T>;
     __shared__ T red[kShThreads / 32][2 * kTileL];
     const int m = tiles[3 * blockIdx.x], l0 = tiles[3 * blockIdx.x + 1], nl = tiles[3 * blockIdx.x + 2];
@@ -156,6 +158,7 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
 template <class T>
 __global__ void __launch_bounds__(128) k_sh_fold(const T* __restrict__ part, int K, int nchunk, double* __restrict__ t)
 {
+    pdl_wait();
     using A = Ar<T>;
     const int k = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (k >= K) return;
@@ -171,6 +174,7 @@ template <class T>
 __global__ void __launch_bounds__(32) k_sh_coef(const double* __restrict__ t, int K, const double* __restrict__ FGinv,
                                                 T* __restrict__ coef)
 {
+    pdl_wait();
     const int a = blockIdx.x;
     const double* row = FGinv + (size_t)a * K;
     double s = 0.0;
@@ -189,6 +193,7 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
                                                             const T* __restrict__ coef, int N, int Np, int L, int K,
                                                             T* __restrict__ usg)
 {
+    pdl_wait();
     using A = Ar<T>;
     extern __shared__ unsigned char c_raw[];
     T* c = reinterpret_cast<T*>(c_raw);
@@ -489,9 +494,11 @@ static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int nt
     const dim3 grid(ntiles, nchunk);
     const T* P = (const T*)s->P;
     const T* trig = (const T*)s->trig;
-    if (tl == 2) k_sh_analysis<T, 2><<<grid, kShThreads, 0, st>>>(P, trig, (const T*)eta, s->N, s->Np, s->L, tiles, nchunk, (T*)s->part);
-    else if (tl == 4) k_sh_analysis<T, 4><<<grid, kShThreads, 0, st>>>(P, trig, (const T*)eta, s->N, s->Np, s->L, tiles, nchunk, (T*)s->part);
-    else k_sh_analysis<T, 8><<<grid, kShThreads, 0, st>>>(P, trig, (const T*)eta, s->N, s->Np, s->L, tiles, nchunk, (T*)s->part);
+    const T* e = (const T*)eta;
+    T* part = (T*)s->part;
+    if (tl == 2) pdl_launch(k_sh_analysis<T, 2>, grid, kShThreads, 0, st, P, trig, e, s->N, s->Np, s->L, tiles, nchunk, part);
+    else if (tl == 4) pdl_launch(k_sh_analysis<T, 4>, grid, kShThreads, 0, st, P, trig, e, s->N, s->Np, s->L, tiles, nchunk, part);
+    else pdl_launch(k_sh_analysis<T, 8>, grid, kShThreads, 0, st, P, trig, e, s->N, s->Np, s->L, tiles, nchunk, part);
 }
 
 template <class T>
@@ -503,7 +510,7 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
     const T* trig = (const T*)s->trig;
     const T* c = (const T*)s->coef;
     T* u = (T*)s->usg;
-#define ODIS_SYNTH(LN, CL) k_sh_synth<T, LN, CL><<<sb, kSynthThreads, sm, st>>>(P, trig, c, s->N, s->Np, s->L, s->K, u)
+#define ODIS_SYNTH(LN, CL) pdl_launch(k_sh_synth<T, LN, CL>, sb, kSynthThreads, sm, st, P, trig, c, s->N, s->Np, s->L, s->K, u)
     if (cells == 2) {
         if (lanes == 1) ODIS_SYNTH(1, 2); else if (lanes == 2) ODIS_SYNTH(2, 2); else if (lanes == 4) ODIS_SYNTH(4, 2); else ODIS_SYNTH(8, 2);
     } else {
@@ -657,8 +664,8 @@ static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st)
         }
     }
     launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, eta, st);
-    k_sh_fold<T><<<(s->K + 3) / 4, 128, 0, st>>>((const T*)s->part, s->K, s->nchunk, s->t);
-    k_sh_coef<T><<<s->K, 32, 0, st>>>(s->t, s->K, s->FGinv, (T*)s->coef);
+    pdl_launch(k_sh_fold<T>, (s->K + 3) / 4, 128, 0, st, (const T*)s->part, s->K, s->nchunk, s->t);
+    pdl_launch(k_sh_coef<T>, s->K, 32, 0, st, s->t, s->K, s->FGinv, (T*)s->coef);
     launch_synth<T>(s, s->lanes, s->cells, st);
 }
 
