@@ -40,11 +40,15 @@ class OdisError(RuntimeError):
         self.code = code
 
 
+FRIC_LINEAR, FRIC_QUADRATIC = 0, 1      # odis_params.friction (input.in "friction type")
+
+
 class Params(C.Structure):
     _fields_ = [("radius", C.c_double), ("g", C.c_double), ("angvel", C.c_double), ("h", C.c_double),
                 ("alpha", C.c_double), ("ecc", C.c_double), ("obliq", C.c_double), ("love_reduct", C.c_double),
                 ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int), ("precision", C.c_int),
-                ("sh_lmax", C.c_int), ("sh_factors", C.POINTER(C.c_double)), ("advection", C.c_int)]
+                ("sh_lmax", C.c_int), ("sh_factors", C.POINTER(C.c_double)), ("advection", C.c_int),
+                ("friction", C.c_int)]
 
 
 class BatchMember(C.Structure):
@@ -324,9 +328,9 @@ class Mesh:
 
 
 def make_params(*, radius, g, angvel, h, alpha, ecc=0.0, obliq=0.0, love_reduct=1.0, dt, potential=POT_ECC,
-                init_load=0, precision=FP64, sh_lmax=0, sh_factors=None, advection=0) -> Params:
+                init_load=0, precision=FP64, sh_lmax=0, sh_factors=None, advection=0, friction=FRIC_LINEAR) -> Params:
     p = Params(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load, precision, sh_lmax, None,
-               advection)
+               advection, friction)
     if sh_lmax:
         arr = np.ascontiguousarray(sh_factors, dtype=np.float64)
         p._factors = arr  # keep alive

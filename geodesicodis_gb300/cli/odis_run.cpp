@@ -181,12 +181,6 @@ int main(int argc, char** argv)
     odis_status st = odis_params_from_input((dir + "/input.in").c_str(), &in);
     if (st != ODIS_OK) return fail("reading input.in", st);
     odis_params p = in.params;
-    if (!in.fric_linear) {
-        // QUADRATIC changes only updateEnergy's output in the reference (alpha / h |u|^3; the
-        // momentum equation keeps linear drag); this build computes the LINEAR dissipation only
-        std::fprintf(stderr, "odis_run: friction type QUADRATIC is not supported; use LINEAR\n");
-        return 2;
-    }
     p.precision = prec == "fp32" ? ODIS_FP32 : prec == "df64" ? ODIS_DF64 : ODIS_FP64;
     if (p.advection && p.precision == ODIS_FP32) {
         std::fprintf(stderr, "odis_run: advection true runs the nonlinear equations in FP64 or df64; using fp64\n");

@@ -201,7 +201,8 @@ template <class T>
 struct AdvK {
     T a, b, c;          // AB3: 23/12, -16/12, 5/12
     T dt, malpha, ga;   // dt, -alpha, -g (gradient of eta)
-    T h0, coef;         // mean thickness; alpha 1000 h (dissipation)
+    T h0, coef;         // mean thickness; alpha 1000 h (LINEAR) or alpha / h (QUADRATIC) dissipation
+    int quad;
 };
 
 // integrateAB3scalar (src/temporalOperators.cpp:17-68) for one unknown; h = its [3] history
@@ -265,9 +266,10 @@ struct PowerArgs {
     double* part;         // [blocks] partial sums
     unsigned* count;      // finished blocks of the launch (0 between launches)
     double* out;          // the step's power
+    int quad;             // QUADRATIC friction
 };
 
-// LSQ thickness flux of the step, then updateEnergy (LINEAR) of the updated v:
+// LSQ thickness flux of the step, then updateEnergy (LINEAR or QUADRATIC) of the updated v:
 // tangential velocity t_e = sum_k w_k v_k, (u, w) = (nx v + ny t, ny v - nx t),
 // e_i = alpha 1000 h |(u, w)|^2, and the FP64 block sum of e_i A_i.  The last
 // block to finish sums the block partials in a fixed order (lane-strided, then
@@ -293,7 +295,7 @@ k_adv_lsq_power(const int* __restrict__ col, const T* __restrict__ val, const T*
         const T nx = pa.nrm[e], ny = pa.nrm[Ep + e];
         const T u = A::fma(nx, ve, A::mul(ny, t));
         const T w = A::fma(ny, ve, A::mul(A::neg(nx), t));
-        x = A::to(A::mul(A::mul(coef, A::fma(u, u, A::mul(w, w))), pa.area[e]));
+        x = A::to(A::mul(face_diss(coef, A::fma(u, u, A::mul(w, w)), pa.quad), pa.area[e]));
     }
     x = adv_warp_sum(x);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -688,7 +690,8 @@ static void step_t(AdvDev* a, const AdvTab<T>& t, AdvWork<T>& w, const AdvStepAr
     k.malpha = host_cvt<T>(-x.alpha);
     k.ga = host_cvt<T>(-x.g * (1 - 0.5 * 0.0));
     k.h0 = host_cvt<T>(x.h0);
-    k.coef = host_cvt<T>(x.alpha * 1000.0 * x.h0);
+    k.coef = host_cvt<T>(x.quad ? x.alpha / x.h0 : x.alpha * 1000.0 * x.h0);
+    k.quad = x.quad;
     // updateMomentum, advection branch: -g G eta + PV flux - G KE
     momentum_head<T>(a, t, w, rbf, x.cell_face, w.v, w.ht, w.ek, w.U, s);
     pdl_launch(k_adv_flux<T, true>, fb, a->bf, 0, s, x.nbr, tw, a->gcol, t.gval, a->E, a->Ep, w.qe, w.hve, w.hvq, w.ek,
@@ -696,7 +699,7 @@ static void step_t(AdvDev* a, const AdvTab<T>& t, AdvWork<T>& w, const AdvStepAr
     pdl_launch(k_adv_vstep<T>, vb, a->bv, 0, s, a->gcol, t.gval, a->E, a->Ep, k, iter, x.init_load, w.dv0, w.U, w.v,
                w.hv);
     // updateEta, advection branch: D (LSQ flux of h + eta); updateEnergy of the new v
-    const PowerArgs<T> pa{x.nbr, tw, nrm, area, x.divisor, a->part, a->count, power};
+    const PowerArgs<T> pa{x.nbr, tw, nrm, area, x.divisor, a->part, a->count, power, x.quad};
     pdl_launch(k_adv_lsq_power<T>, pb, a->bp, 0, s, a->lcol, t.lval, t.dx2, a->fnode, a->E, a->Ep, w.v, w.ht, w.flux,
                k.coef, pa);
     pdl_launch(k_adv_estep<T>, nb + 1, a->be, 0, s, a->dcol, t.dval, a->N, a->Np, k, iter, x.init_load, w.flux, w.eta,

@@ -39,6 +39,7 @@ struct AdvStepArgs {
     double g, alpha, h0, dt;
     double divisor;           // 4 pi r^2
     int init_load;
+    int quad;                 // QUADRATIC friction: dissipation alpha / h |u|^3
 };
 // one whole step of the advective loop (7 kernels): momentum with advection, the
 // continuity update, the power of the updated velocity into *power (device), and

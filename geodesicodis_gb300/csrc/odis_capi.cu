@@ -358,7 +358,7 @@ static int build_operators(odis_ctx* c, const Mesh& m, const std::vector<double>
         cor[e] = cvt<T>(-2.0 * p.angvel * std::sin(m.face_centre[(size_t)e * 2]));
         fP[e] = cvt<T>(g0 * Ua[a] + g1 * Ua[b]);
         fQ[e] = cvt<T>(g0 * Ub[a] + g1 * Ub[b]);
-        diss[e] = cvt<T>(p.alpha * 1000.0 * p.h * m.face_area[e] / four_pi_r2);
+        diss[e] = cvt<T>(energy_coef(p) * m.face_area[e] / four_pi_r2);
     }
     for (int i = 0; i < Np; i++) {
         const int ii = i < N ? i : 0;
@@ -533,6 +533,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     if (p->potential < ODIS_POT_NONE || p->potential > ODIS_POT_FULL) return ODIS_ERR_ARG;
     if (!(p->dt > 0.0) || !(p->g > 0.0) || !(p->h > 0.0) || !(p->radius > 0.0) || p->alpha < 0.0) return ODIS_ERR_ARG;
     if (p->sh_lmax < 0 || p->sh_lmax > 64 || (p->sh_lmax > 0 && !p->sh_factors)) return ODIS_ERR_ARG;
+    if (p->friction != ODIS_FRIC_LINEAR && p->friction != ODIS_FRIC_QUADRATIC) return ODIS_ERR_ARG;
     if (p->advection && ((p->precision != ODIS_FP64 && p->precision != ODIS_DF64) || p->sh_lmax > 0))
         return ODIS_ERR_ARG;
     int dev = 0;
@@ -639,6 +640,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     sc.ab3b = -16. / 12.;
     sc.ab3c = 5. / 12.;
     sc.init_load = p->init_load ? 1 : 0;
+    sc.quad = p->friction == ODIS_FRIC_QUADRATIC ? 1 : 0;
     sc.use_sg = p->sh_lmax > 0 ? 1 : 0;
     sc.df_dt = df_from_double(p->dt);
     sc.df_malpha = df_from_double(-p->alpha);
@@ -866,8 +868,8 @@ extern "C" odis_status odis_update_energy(odis_ctx* c, double* avg, double* e, c
     double* de = e ? io.out(e) : nullptr;
     double* davg = mem == ODIS_MEM_DEVICE ? avg : c->stage[3];
     if (!duv) return ODIS_ERR_CUDA;
-    launch_energy(c->area, c->E, c->p.alpha * 1000.0 * c->p.h, 4 * kPi * std::pow(c->r, 2.0), duv, de, c->d_partial,
-                  davg, c->stream);
+    launch_energy(c->area, c->E, energy_coef(c->p), c->p.friction == ODIS_FRIC_QUADRATIC, 4 * kPi * std::pow(c->r, 2.0),
+                  duv, de, c->d_partial, davg, c->stream);
     int st = e ? io.back(e, de, c->E) : ODIS_OK;
     if (st == ODIS_OK) st = io.back(avg, davg, 1);
     return st != ODIS_OK ? st : io.done();
@@ -1013,7 +1015,7 @@ static odis_status run_advective(odis_ctx* c, int n, double* dpow)
                         df ? c->opdf.fc.nbr : c->op64.fc.nbr, df ? (const void*)c->opdf.fc.w : (const void*)c->op64.fc.w,
                         df ? (const void*)c->nrm_df : (const void*)c->nrm,
                         df ? (const void*)c->area_df : (const void*)c->area, p.g, p.alpha, p.h,
-                        p.dt, 4 * kPi * std::pow(c->r, 2.0), p.init_load};
+                        p.dt, 4 * kPi * std::pow(c->r, 2.0), p.init_load, p.friction == ODIS_FRIC_QUADRATIC};
     auto step = [&](int it, double* out) { adv_step(c->adv, x, it, out, c->stream); };
     adv_set_step(c->adv, c->iter, p.dt, c->stream);
     c->launches += 1;

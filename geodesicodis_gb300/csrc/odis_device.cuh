@@ -45,6 +45,7 @@ struct StepConst {
     double ab3a, ab3b, ab3c;  // 23/12, -16/12, 5/12
     int init_load;            // 1: AB3 from the first step
     int use_sg;               // 1: add the self-gravity / loading potential
+    int quad;                 // 1: QUADRATIC friction (dissipation diss_e |u|^3 instead of diss_e |u|^2)
     // the same constants as double-float (hi, lo) pairs for the ODIS_DF64 method
     float2 df_dt, df_malpha, df_a, df_b, df_c;
     // and rounded to FP32 for the FP32-state variant (no per-thread conversions)

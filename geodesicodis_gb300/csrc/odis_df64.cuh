@@ -114,4 +114,36 @@ __device__ __forceinline__ df64 df_shfl_down(df64 a, int o)
 
 __device__ __forceinline__ bool df_finite(df64 a) { return (__float_as_int(a.x) & 0x7f800000) != 0x7f800000; }
 
+// Square root of a non-negative double-float: the FP32 root s of the high part,
+// refined by one Newton step on the residual a - s^2, whose s^2 is formed
+// exactly (Karp and Markstein, "High-precision division and square root", ACM
+// TOMS 23, 1997): relative error about 2^-46.  Zero for a <= 0.
+__device__ __forceinline__ df64 df_sqrt(df64 a)
+{
+    if (!(a.x > 0.f)) return df_make(0.f, 0.f);
+    const float s = sqrtf(a.x);
+    const float p = s * s, pe = fmaf(s, s, -p);      // s^2 = p + pe exactly
+    const float r = ((a.x - p) - pe) + a.y;
+    return df_two_sum(s, r * (0.5f / s));
+}
+
+// Dissipation of one face from q = u^2 + v^2 and the face's coefficient d
+// (updateEnergy, src/energy.cpp:30-53, times A_e / (4 pi r^2)): d q for LINEAR
+// friction and d q sqrt(q) for QUADRATIC.
+__device__ __forceinline__ double face_diss(double d, double q, int quad)
+{
+    const double x = d * q;
+    return quad ? x * sqrt(q) : x;
+}
+__device__ __forceinline__ float face_diss(float d, float q, int quad)
+{
+    const float x = d * q;
+    return quad ? x * sqrtf(q) : x;
+}
+__device__ __forceinline__ df64 face_diss(df64 d, df64 q, int quad)
+{
+    const df64 x = df_mul(d, q);
+    return quad ? df_mul(x, df_sqrt(q)) : x;
+}
+
 }  // namespace odis

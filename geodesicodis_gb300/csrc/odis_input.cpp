@@ -120,6 +120,7 @@ int parse_input(const char* path, odis_input& out)
     out.advection = advection ? 1 : 0;
     p.advection = out.advection;
     out.fric_linear = friction == "LINEAR" ? 1 : 0;
+    p.friction = out.fric_linear ? ODIS_FRIC_LINEAR : ODIS_FRIC_QUADRATIC;
     out.surface_free = surface == "FREE" ? 1 : 0;
     out.init_kind = init == "NONE" ? 0 : init == "LOAD" ? 1 : init == "ANALYTICAL" ? 2 : -1;
     out.out_flags = (out_vel ? 1 : 0) | (out_cart ? 2 : 0) | (out_disp ? 4 : 0) | (out_diss ? 8 : 0) |

@@ -112,7 +112,10 @@ __device__ __forceinline__ double block_power(T pw, double* smem)
 // ---------------------------------------------------------------------------
 // fused step, face part
 // ---------------------------------------------------------------------------
-template <class T, bool kMaster>
+// kQuad: QUADRATIC friction.  A compile-time switch here because the FP64 square
+// root's code, even untaken, raised the FP64 kernel from 32 to 38 registers and
+// cost occupancy (FP64 plain step 3.3 -> 2.7 G cell-steps/s at level 6).
+template <class T, bool kMaster, bool kQuad>
 __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, State<T> st, StepConst sc, int offset)
 {
     pdl_wait();
@@ -131,7 +134,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, Stat
         for (int k = 0; k < kTrisk; k++) tsum = fmaT<T>(__ldg(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
         const T ve = vin[e];
         const int i0 = __ldg(&fc.n0[e]), i1 = __ldg(&fc.n1[e]);
-        pw = __ldg(&fc.diss[e]) * fmaT<T>(ve, ve, tsum * tsum);
+        pw = face_diss(__ldg(&fc.diss[e]), fmaT<T>(ve, ve, tsum * tsum), kQuad);
         // updateMomentum: -g G eta + C v
         const T g0 = __ldg(&fc.gg0[e]), g1 = __ldg(&fc.gg1[e]);
         const T f0 = fmaT<T>(__ldg(&fc.cor[e]), tsum, fmaT<T>(g0, st.eta[i0], g1 * st.eta[i1]));
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_f32x2(FaceCoef<float
         }
         const float2 ve = *reinterpret_cast<const float2*>(&vin[e]);
         const float2 diss = __ldg(reinterpret_cast<const float2*>(&fc.diss[e]));
-        pw = diss.x * fmaf(ve.x, ve.x, tx * tx) + diss.y * fmaf(ve.y, ve.y, ty * ty);
+        pw = face_diss(diss.x, fmaf(ve.x, ve.x, tx * tx), sc.quad) + face_diss(diss.y, fmaf(ve.y, ve.y, ty * ty), sc.quad);
         const int2 n0 = __ldg(reinterpret_cast<const int2*>(&fc.n0[e]));
         const int2 n1 = __ldg(reinterpret_cast<const int2*>(&fc.n1[e]));
         const float2 g0 = __ldg(reinterpret_cast<const float2*>(&fc.gg0[e]));
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial_f32x2(FaceCoef<f
 #pragma unroll
         for (int k = 0; k < kTrisk; k++) tsum = fmaf(__ldg(&fc.w[k * Ep + f]), vin[__ldg(&fc.nbr[k * Ep + f])], tsum);
         const float ve = vin[f];
-        pw += __ldg(&fc.diss[f]) * fmaf(ve, ve, tsum * tsum);
+        pw += face_diss(__ldg(&fc.diss[f]), fmaf(ve, ve, tsum * tsum), sc.quad);
     }
     const double bs = block_power<float>(pw, s_red);
     if (threadIdx.x == 0) st.partial[(it - *st.run_first) * gridDim.x + blockIdx.x] = bs;
@@ -311,7 +314,7 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial(FaceCoef<T> fc, 
 #pragma unroll
         for (int k = 0; k < kTrisk; k++) tsum = fmaT<T>(__ldg(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
         const T ve = vin[e];
-        pw = (double)(__ldg(&fc.diss[e]) * fmaT<T>(ve, ve, tsum * tsum));
+        pw = (double)face_diss(__ldg(&fc.diss[e]), fmaT<T>(ve, ve, tsum * tsum), sc.quad);
     }
     const double bs = block_sum<kStepThreads>(pw, s_red);
     if (threadIdx.x == 0) st.partial[(it - *st.run_first) * gridDim.x + blockIdx.x] = bs;
@@ -447,15 +450,17 @@ __global__ void k_interp(FaceCoef<double> fc, const double* nrm, int E, int Ep, 
 }
 
 // updateEnergy (LINEAR): e_i = alpha 1000 h |uv_i|^2, block partials of e_i * A_i
-__global__ void __launch_bounds__(kStepThreads) k_energy_partial(const double* area, int E, double coef, const double* uv,
-                                                                 double* e_out, double* partial)
+__global__ void __launch_bounds__(kStepThreads) k_energy_partial(const double* area, int E, double coef, int quad,
+                                                                 const double* uv, double* e_out, double* partial)
 {
     __shared__ double s_red[kStepThreads / 32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double x = 0.0;
     if (i < E) {
         const double u = uv[2 * i], w = uv[2 * i + 1];
-        const double ei = coef * (u * u + w * w);
+        const double q = u * u + w * w;
+        // src/energy.cpp:34 (LINEAR) and :48-49 (QUADRATIC, coef sqrt(q) q in the reference's order)
+        const double ei = quad ? coef * sqrt(q) * q : coef * q;
         if (e_out) e_out[i] = ei;
         x = ei * area[i];
     }
@@ -502,7 +507,8 @@ void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc,
     if constexpr (kMaster) {
         pdl_launch(k_edge_step_f32x2, face_blocks(sc, true), kStepThreads, 0, s, fc, st, sc, offset);
     } else {
-        pdl_launch(k_edge_step<T, kMaster>, face_blocks(sc, false), kStepThreads, 0, s, fc, st, sc, offset);
+        if (sc.quad) pdl_launch(k_edge_step<T, kMaster, true>, face_blocks(sc, false), kStepThreads, 0, s, fc, st, sc, offset);
+        else pdl_launch(k_edge_step<T, kMaster, false>, face_blocks(sc, false), kStepThreads, 0, s, fc, st, sc, offset);
     }
 }
 
@@ -576,11 +582,11 @@ void launch_interp(const FaceCoef<double>& fc, const double* nrm, int E, int Ep,
 
 int energy_blocks(int E) { return blocks(E, kStepThreads); }
 
-void launch_energy(const double* area, int E, double coef, double divisor, const double* uv, double* e_out,
+void launch_energy(const double* area, int E, double coef, int quad, double divisor, const double* uv, double* e_out,
                    double* partial, double* out, cudaStream_t s)
 {
     const int nb = energy_blocks(E);
-    k_energy_partial<<<nb, kStepThreads, 0, s>>>(area, E, coef, uv, e_out, partial);
+    k_energy_partial<<<nb, kStepThreads, 0, s>>>(area, E, coef, quad, uv, e_out, partial);
     k_fold<<<1, 32, 0, s>>>(partial, nb, divisor, out);
 }
 

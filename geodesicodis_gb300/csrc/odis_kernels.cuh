@@ -1,6 +1,7 @@
 // Launchers of the LTE kernels (odis_kernels.cu), called by the C ABI.
 #pragma once
 
+#include "../../include/odis_gpu.h"
 #include "odis_device.cuh"
 
 namespace odis {
@@ -40,7 +41,15 @@ void launch_ab3_ref(double* x, double* h, int iter, int num, double dt, int init
 void launch_interp(const FaceCoef<double>& fc, const double* nrm, int E, int Ep, double* uv, const double* v,
                    cudaStream_t s);
 int energy_blocks(int E);
-void launch_energy(const double* area, int E, double coef, double divisor, const double* uv, double* e_out,
+// Dissipation coefficient of updateEnergy (src/energy.cpp:30-53): e_e = coef |u|^2
+// for LINEAR friction (coef = alpha 1000 h) and coef |u|^3 for QUADRATIC
+// (coef = alpha / h).
+inline double energy_coef(const odis_params& p)
+{
+    return p.friction == ODIS_FRIC_QUADRATIC ? p.alpha / p.h : p.alpha * 1000.0 * p.h;
+}
+
+void launch_energy(const double* area, int E, double coef, int quad, double divisor, const double* uv, double* e_out,
                    double* partial, double* out, cudaStream_t s);
 
 }  // namespace odis

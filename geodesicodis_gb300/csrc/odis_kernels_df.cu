@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc
         for (int k = 0; k < kTrisk; k++) tsum = df_fma(ldg2(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
         const df64 ve = vin[e];
         const int i0 = __ldg(&fc.n0[e]), i1 = __ldg(&fc.n1[e]);
-        pw = df_mul(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)));
+        pw = face_diss(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)), sc.quad);
         const df64 g0 = ldg2(&fc.gg0[e]), g1 = ldg2(&fc.gg1[e]);
         const df64 f0 = df_fma(ldg2(&fc.cor[e]), tsum, df_fma(g0, st.eta[i0], df_mul(g1, st.eta[i1])));
         df64 gu = df_fma(cosM, ldg2(&fc.fP[e]), df_mul(sinM, ldg2(&fc.fQ[e])));
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64
 #pragma unroll
         for (int k = 0; k < kTrisk; k++) tsum = df_fma(ldg2(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
         const df64 ve = vin[e];
-        pw = df_mul(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)));
+        pw = face_diss(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)), sc.quad);
     }
     const double bs = block_sum_df(pw, s_red);
     if (threadIdx.x == 0) st.partial[(it - *st.run_first) * gridDim.x + blockIdx.x] = bs;

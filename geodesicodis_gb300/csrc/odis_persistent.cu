@@ -104,6 +104,7 @@ struct FaceCtx {
     const T* eta;
     T cosM, sinM, malpha, ca, cb, cc3, dt;
     int NF, nfi;
+    int quad;           // QUADRATIC friction
     bool ab3;
     int* status;
 };
@@ -120,7 +121,7 @@ __device__ __forceinline__ void face_update(const FaceCtx<T> f, int lf, T& pw)
         tsum = A::fma(f.sw[k * NF + lf], c >= 0 ? f.svi[c] : A::ldcg(&f.vin[-1 - c]), tsum);
     }
     const T ve = f.svi[lf];
-    pw = A::add(pw, A::mul(f.sdiss[lf], A::fma(ve, ve, A::mul(tsum, tsum))));
+    pw = A::add(pw, face_diss(f.sdiss[lf], A::fma(ve, ve, A::mul(tsum, tsum)), f.quad));
     const int c0 = f.sn0[lf], c1 = f.sn1[lf];
     const T e0 = c0 >= 0 ? f.seta[c0] : A::ldcg(&f.eta[-1 - c0]);
     const T e1 = c1 >= 0 ? f.seta[c1] : A::ldcg(&f.eta[-1 - c1]);
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_persistent(FaceCoef<T> fc, 
         fx.svi = svi; fx.seta = seta; fx.snbr = snbr; fx.sn0 = sn0; fx.sn1 = sn1; fx.sface = sface;
         fx.hcur = hcur; fx.svo = svo; fx.hold = hold; fx.vin = vin; fx.vout = vout; fx.eta = st.eta;
         fx.cosM = cosM; fx.sinM = sinM; fx.malpha = malpha; fx.ca = ca; fx.cb = cb; fx.cc3 = cc3; fx.dt = dt;
-        fx.NF = NF; fx.nfi = nfi; fx.ab3 = ab3; fx.status = st.status;
+        fx.NF = NF; fx.nfi = nfi; fx.quad = sc.quad; fx.ab3 = ab3; fx.status = st.status;
         for (int lf = threadIdx.x; lf < nfi; lf += blockDim.x) face_update<T>(fx, lf, pw);
         if (s > 0 && !wait_deps(pl.flag_c, depA, ndA, (unsigned)s, st.status)) { ok = false; break; }
         for (int lf = nfi + threadIdx.x; lf < nf; lf += blockDim.x) face_update<T>(fx, lf, pw);
@@ -291,7 +292,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_persistent(FaceCoef<T> fc, 
                 tsum = A::fma(sw[k * NF + lf], c >= 0 ? svi[c] : A::ldcg(&vin[-1 - c]), tsum);
             }
             const T ve = svi[lf];
-            pw = A::add(pw, A::mul(sdiss[lf], A::fma(ve, ve, A::mul(tsum, tsum))));
+            pw = A::add(pw, face_diss(sdiss[lf], A::fma(ve, ve, A::mul(tsum, tsum)), sc.quad));
         }
         const T bs = block_sum_t<T>(pw, red);
         if (threadIdx.x == 0) part[(size_t)n * P + b] = bs;

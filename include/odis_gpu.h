@@ -63,6 +63,11 @@ typedef int odis_status;
 #define ODIS_DF64 2             /* the FP64 method in double-float (2 x FP32, 48-bit significand) on the
                                    FP32 pipes; meets the FP64 parity bar (1e-10 against the FP64 oracle) */
 
+/* friction type (input.in "friction type"): the dissipation per face is
+ * alpha 1000 h |u|^2 (LINEAR) or alpha / h |u|^3 (QUADRATIC) */
+#define ODIS_FRIC_LINEAR 0
+#define ODIS_FRIC_QUADRATIC 1
+
 /* where the pointers passed to per-operator calls live */
 #define ODIS_MEM_HOST 0
 #define ODIS_MEM_DEVICE 1
@@ -92,6 +97,9 @@ typedef struct odis_params {
     int advection;          /* 1: the nonlinear equations ("advection true"): momentum advection
                                (src/momAdvection.cpp) and the LSQ thickness flux in the continuity
                                equation (src/updateEta.cpp:22-32); ODIS_FP64 or ODIS_DF64, no self-gravity */
+    int friction;           /* ODIS_FRIC_LINEAR (0) or ODIS_FRIC_QUADRATIC (1): which dissipation
+                               updateEnergy reports (src/energy.cpp:30-53); the momentum equation
+                               keeps the linear drag -alpha v in both, as in the reference */
 } odis_params;
 
 /* Parsed input.in (src/globals.cpp:58-203 keys).  Strings are fixed-size. */

@@ -27,7 +27,7 @@
  *   updateEta ............... src/updateEta.cpp:7-44 (linear branch :39)
  *   integrateAB3scalar ...... src/temporalOperators.cpp:17-68
  *   interpolateVelocity ..... src/interpolation.cpp:26-62
- *   updateEnergy ............ src/energy.cpp:13-61 (LINEAR branch)
+ *   updateEnergy ............ src/energy.cpp:13-61 (LINEAR and QUADRATIC branches)
  *   time loop ............... src/timeIntegrator.cpp:205-272 (ab3Explicit)
  *
  * Sparse operators are held as CSR with each row sorted by ascending column,
@@ -775,6 +775,7 @@ typedef struct {
     int potential;
     int init_load;
     int advection;        /* 1: the nonlinear branch (momentum advection, LSQ thickness flux) */
+    int friction;         /* 0 LINEAR, 1 QUADRATIC (src/globals.cpp:232-234) */
 } orc_params;
 
 /* ------------------------------------------------------------------------ */
@@ -1209,17 +1210,25 @@ void orc_mesh_vertex_topology(const orc_mesh *M, int *vert_nodes, int *vert_face
     memcpy(face_verts, M->face_verts, sizeof(int) * M->E * 2);
 }
 
-/* updateEnergy, LINEAR branch, src/energy.cpp:13-61 */
-double orc_update_energy(const orc_mesh *M, double alpha, double h, double *e, const double *uv)
+/* updateEnergy, src/energy.cpp:13-61: LINEAR (:30-43) alpha 1000 h |u|^2,
+ * QUADRATIC (:45-53) alpha / h |u| |u|^2; area-weighted sum over 4 pi r^2 */
+double orc_update_energy_fric(const orc_mesh *M, double alpha, double h, int friction, double *e, const double *uv)
 {
     double avg = 0.0;
     for (int i = 0; i < M->E; i++) {
-        double ei = alpha * 1000.0 * h * (uv[i * 2] * uv[i * 2] + uv[i * 2 + 1] * uv[i * 2 + 1]);
+        double q = uv[i * 2] * uv[i * 2] + uv[i * 2 + 1] * uv[i * 2 + 1];
+        double ei = friction ? alpha / h * sqrt(q) * q : alpha * 1000.0 * h * q;
         if (e) e[i] = ei;
         avg += ei * M->face_area[i];
     }
     avg /= (4 * ORC_PI * pow(M->r, 2.0));
     return avg;
+}
+
+/* updateEnergy, LINEAR branch */
+double orc_update_energy(const orc_mesh *M, double alpha, double h, double *e, const double *uv)
+{
+    return orc_update_energy_fric(M, alpha, h, 0, e, uv);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1469,7 +1478,7 @@ double orc_sim_step(orc_sim *X)
     for (int i = 0; i < N; ++i) X->detadt[i * 3] = X->dp0[i];
     orc_ab3(dt, X->eta, X->detadt, X->iter, N, S->p.init_load);          /* :253 */
     orc_interpolate_velocity(M, X->uv, X->v);                            /* :261 */
-    X->power = orc_update_energy(M, S->p.alpha, S->p.h, X->ediss, X->uv);
+    X->power = orc_update_energy_fric(M, S->p.alpha, S->p.h, S->p.friction, X->ediss, X->uv);
     if (S->p.advection)                  /* column thickness for the next step, :266-269 */
         for (int i = 0; i < N; i++) X->h_total[i] = S->p.h + X->eta[i];
     X->iter++;

@@ -25,7 +25,8 @@ ECC, OBLIQ, OBLIQ_WEST, FULL, FULL2, NONE = 1, 2, 3, 4, 5, 0
 class OrcParams(C.Structure):
     _fields_ = [("radius", C.c_double), ("g", C.c_double), ("angvel", C.c_double), ("h", C.c_double),
                 ("alpha", C.c_double), ("ecc", C.c_double), ("obliq", C.c_double), ("love_reduct", C.c_double),
-                ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int), ("advection", C.c_int)]
+                ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int), ("advection", C.c_int),
+                ("friction", C.c_int)]
 
 
 _lib = None
@@ -65,6 +66,7 @@ def lib() -> C.CDLL:
             "orc_mesh_vertex_field": ([_V, C.c_int, _D], C.c_int),
             "orc_mesh_vertex_topology": ([_V, _I, _I, _I, _I], None),
             "orc_update_energy": ([_V, C.c_double, C.c_double, _D, _D], C.c_double),
+            "orc_update_energy_fric": ([_V, C.c_double, C.c_double, C.c_int, _D, _D], C.c_double),
             "orc_plmbar": ([C.c_int, C.c_double, _D], None),
             "orc_sh_basis": ([_V, C.c_int, _D], None),
             "orc_sh_analysis": ([_V, _D, _D], None),
@@ -159,9 +161,10 @@ class OracleSolver:
     """FP64 restatement of the reference step (see odis_oracle.c)."""
 
     def __init__(self, mesh: OracleMesh, *, radius, g, angvel, h, alpha, ecc=0.0, obliq=0.0, love_reduct=1.0,
-                 dt, potential=ECC, init_load=0, sh_lmax=0, sh_factors=None, advection=0):
+                 dt, potential=ECC, init_load=0, sh_lmax=0, sh_factors=None, advection=0, friction=0):
         self.mesh = mesh
-        self.p = OrcParams(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load, advection)
+        self.p = OrcParams(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load, advection,
+                           friction)
         self._s = C.c_void_p(lib().orc_solver_create(mesh._h, C.byref(self.p)))
         if sh_lmax:
             f = np.ascontiguousarray(sh_factors, np.float64)
@@ -219,8 +222,8 @@ class OracleSolver:
 
     def updateEnergy(self, uv):
         e = np.zeros(self.E)
-        avg = lib().orc_update_energy(self.mesh._h, self.p.alpha, self.p.h, _dp(e),
-                                      _dp(np.ascontiguousarray(uv, np.float64)))
+        avg = lib().orc_update_energy_fric(self.mesh._h, self.p.alpha, self.p.h, self.p.friction, _dp(e),
+                                           _dp(np.ascontiguousarray(uv, np.float64)))
         return avg, e
 
     def sh_analysis(self, eta):

@@ -18,15 +18,17 @@ def test_cli_is_built_and_rejects_bad_arguments(built):
     assert r.returncode == 2 and "usage" in r.stderr
 
 
-def test_cli_refuses_quadratic_friction(built, tmp_path):
-    """friction type QUADRATIC would change the reported dissipation (src/energy.cpp:46-53); the
-    driver refuses it before touching the GPU instead of reporting the linear one."""
-    d = tmp_path / "q"
-    d.mkdir()
-    (d / "input.in").write_text(INPUT_IN.replace("friction type; \t \t     LINEAR;", "friction type; \t \t     QUADRATIC;"))
-    assert "QUADRATIC" in (d / "input.in").read_text()
-    r = subprocess.run([str(CLI), "--dir", str(d)], capture_output=True, text=True)
-    assert r.returncode == 2 and "QUADRATIC" in r.stderr
+def test_quadratic_friction_reaches_params(built, tmp_path):
+    """friction type QUADRATIC (src/globals.cpp:232-234) selects updateEnergy's |u|^3 branch
+    (src/energy.cpp:45-53) through odis_params.friction; LINEAR is the other value."""
+    import geodesicodis_gb300 as g
+    f = tmp_path / "input.in"
+    f.write_text(INPUT_IN.replace("friction type; \t \t     LINEAR;", "friction type; \t \t     QUADRATIC;"))
+    assert "QUADRATIC" in f.read_text()
+    inp = g.read_input(f)
+    assert inp.fric_linear == 0 and inp.params.friction == 1
+    f.write_text(INPUT_IN)
+    assert g.read_input(f).params.friction == 0
 
 
 def _rundir(tmp_path, init="NONE"):

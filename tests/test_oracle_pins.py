@@ -266,3 +266,20 @@ def test_advective_loop_stays_near_linear_at_small_amplitude(grid_dir):
         gaps.append(np.abs(ea - el).max() / np.abs(el).max())
         assert abs(pa[-1] - pl[-1]) / pl[-1] < 0.05
     assert gaps[1] < gaps[0] < 0.01
+
+
+def test_oracle_quadratic_energy_branch(grid_dir):
+    """updateEnergy QUADRATIC (src/energy.cpp:45-53): e_e = alpha / h sqrt(u^2 + v^2) (u^2 + v^2),
+    restated here in numpy; LINEAR stays alpha 1000 h |u|^2.  Both means weight e_e by the same
+    face areas, so their ratio is the area-weighted ratio of the two fields."""
+    from conftest import config0_params
+    from oracle import pyoracle as O
+    om = O.OracleMesh(grid_dir / "grid_3.txt", RADIUS)
+    uv = np.random.default_rng(5).standard_normal((om.n_edges, 2)) * 0.05
+    q = uv[:, 0] * uv[:, 0] + uv[:, 1] * uv[:, 1]
+    out = {}
+    for fric, e_ref in ((1, 1e-5 / 1e4 * np.sqrt(q) * q), (0, 1e-5 * 1000.0 * 1e4 * q)):
+        avg, e = O.OracleSolver(om, **config0_params(friction=fric)).updateEnergy(uv)
+        np.testing.assert_allclose(e, e_ref, rtol=1e-15)
+        out[fric] = avg
+    assert out[0] > 0 and out[1] > 0 and out[1] < 1e-6 * out[0]
