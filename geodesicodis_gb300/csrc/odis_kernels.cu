@@ -180,6 +180,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, Stat
 // latency bound well below the HBM rate once the working set leaves L2.  The
 // pad faces past E (Ep is a multiple of 128) have zero coefficients and point
 // at face 0, so the second face of an odd tail computes and stores zeros.
+template <bool kQuad>   // QUADRATIC friction, a compile-time switch as in k_edge_step
 __global__ void __launch_bounds__(kStepThreads) k_edge_step_f32x2(FaceCoef<float> fc, State<float> st, StepConst sc,
                                                                      int offset)
 {
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_f32x2(FaceCoef<float
         }
         const float2 ve = *reinterpret_cast<const float2*>(&vin[e]);
         const float2 diss = __ldg(reinterpret_cast<const float2*>(&fc.diss[e]));
-        pw = face_diss(diss.x, fmaf(ve.x, ve.x, tx * tx), sc.quad) + face_diss(diss.y, fmaf(ve.y, ve.y, ty * ty), sc.quad);
+        pw = face_diss(diss.x, fmaf(ve.x, ve.x, tx * tx), kQuad) + face_diss(diss.y, fmaf(ve.y, ve.y, ty * ty), kQuad);
         const int2 n0 = __ldg(reinterpret_cast<const int2*>(&fc.n0[e]));
         const int2 n1 = __ldg(reinterpret_cast<const int2*>(&fc.n1[e]));
         const float2 g0 = __ldg(reinterpret_cast<const float2*>(&fc.gg0[e]));
@@ -505,7 +506,8 @@ template <class T, bool kMaster>
 void launch_edge(const FaceCoef<T>& fc, const State<T>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
     if constexpr (kMaster) {
-        pdl_launch(k_edge_step_f32x2, face_blocks(sc, true), kStepThreads, 0, s, fc, st, sc, offset);
+        if (sc.quad) pdl_launch(k_edge_step_f32x2<true>, face_blocks(sc, true), kStepThreads, 0, s, fc, st, sc, offset);
+        else pdl_launch(k_edge_step_f32x2<false>, face_blocks(sc, true), kStepThreads, 0, s, fc, st, sc, offset);
     } else {
         if (sc.quad) pdl_launch(k_edge_step<T, kMaster, true>, face_blocks(sc, false), kStepThreads, 0, s, fc, st, sc, offset);
         else pdl_launch(k_edge_step<T, kMaster, false>, face_blocks(sc, false), kStepThreads, 0, s, fc, st, sc, offset);

@@ -36,6 +36,7 @@ __device__ __forceinline__ df64 ldg2(const df64* p) { return __ldg(p); }
 
 }  // namespace
 
+template <bool kQuad>   // QUADRATIC friction, a compile-time switch as in k_edge_step
 __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc, State<df64> st, StepConst sc, int offset)
 {
     pdl_wait();
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc
         for (int k = 0; k < kTrisk; k++) tsum = df_fma(ldg2(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
         const df64 ve = vin[e];
         const int i0 = __ldg(&fc.n0[e]), i1 = __ldg(&fc.n1[e]);
-        pw = face_diss(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)), sc.quad);
+        pw = face_diss(ldg2(&fc.diss[e]), df_fma(ve, ve, df_mul(tsum, tsum)), kQuad);
         const df64 g0 = ldg2(&fc.gg0[e]), g1 = ldg2(&fc.gg1[e]);
         const df64 f0 = df_fma(ldg2(&fc.cor[e]), tsum, df_fma(g0, st.eta[i0], df_mul(g1, st.eta[i1])));
         df64 gu = df_fma(cosM, ldg2(&fc.fP[e]), df_mul(sinM, ldg2(&fc.fQ[e])));
@@ -122,7 +123,8 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64
 void launch_edge_df(const FaceCoef<df64>& fc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
 {
     const int eb = (sc.E + kStepThreads - 1) / kStepThreads;
-    pdl_launch(k_edge_step_df, eb, kStepThreads, 0, s, fc, st, sc, offset);
+    if (sc.quad) pdl_launch(k_edge_step_df<true>, eb, kStepThreads, 0, s, fc, st, sc, offset);
+    else pdl_launch(k_edge_step_df<false>, eb, kStepThreads, 0, s, fc, st, sc, offset);
 }
 
 void launch_cell_df(const CellCoef<df64>& cc, const State<df64>& st, const StepConst& sc, int offset, cudaStream_t s)
