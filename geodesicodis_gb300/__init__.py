@@ -20,7 +20,8 @@ import numpy as np
 
 __all__ = [
     "OdisError", "lib", "Params", "Input", "Mesh", "Solver", "generate_grid_file", "derive_time",
-    "read_input", "Batch", "BatchMember", "MLP", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL", "FP64", "FP32", "DF64",
+    "read_input", "Batch", "BatchMember", "MLP", "POT_NONE", "POT_ECC", "POT_OBLIQ", "POT_OBLIQ_WEST", "POT_FULL",
+    "POT_FULL2", "POT_PLANET", "POT_GENERAL", "FP64", "FP32", "DF64",
 ]
 
 _PKG = Path(__file__).resolve().parent
@@ -29,7 +30,9 @@ LIB_PATH = _PKG / "lib" / "libodis_gpu.so"
 OK, ERR_ARG, ERR_CUDA, ERR_OOB, ERR_NONFINITE, ERR_TIMEOUT, ERR_IO, ERR_MESH, ERR_NOMEM = range(9)
 _NAMES = {1: "ODIS_ERR_ARG", 2: "ODIS_ERR_CUDA", 3: "ODIS_ERR_OOB", 4: "ODIS_ERR_NONFINITE",
           5: "ODIS_ERR_TIMEOUT", 6: "ODIS_ERR_IO", 7: "ODIS_ERR_MESH", 8: "ODIS_ERR_NOMEM"}
-POT_NONE, POT_ECC, POT_OBLIQ, POT_OBLIQ_WEST, POT_FULL = range(5)
+# forcing types: the values of the reference's enum Potential (include/globals.h:60-76)
+(POT_OBLIQ, POT_OBLIQ_WEST, POT_OBLIQ_EAST, POT_ECC_RAD, POT_ECC_LIB, POT_ECC, POT_ECC_WEST, POT_ECC_EAST, POT_FULL,
+ POT_FULL2, POT_TOTAL, POT_ECC_W3, POT_OBLIQ_W3, POT_PLANET, POT_PLANET_OBL, POT_GENERAL, POT_NONE) = range(17)
 FP64, FP32, DF64 = 0, 1, 2
 MEM_HOST, MEM_DEVICE = 0, 1
 
@@ -48,7 +51,7 @@ class Params(C.Structure):
                 ("alpha", C.c_double), ("ecc", C.c_double), ("obliq", C.c_double), ("love_reduct", C.c_double),
                 ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int), ("precision", C.c_int),
                 ("sh_lmax", C.c_int), ("sh_factors", C.POINTER(C.c_double)), ("advection", C.c_int),
-                ("friction", C.c_int)]
+                ("friction", C.c_int), ("semimajor_axis", C.c_double), ("fourier_freq", C.c_int)]
 
 
 class BatchMember(C.Structure):
@@ -94,7 +97,7 @@ _SIGS = {
     "odis_device_status": ([_V], C.c_int),
     "odis_update_momentum": ([_V, _V, _V, _V, C.c_int], C.c_int),
     "odis_update_eta": ([_V, _V, _V, C.c_int], C.c_int),
-    "odis_forcing": ([_V, _V, C.c_int, C.c_double, C.c_int], C.c_int),
+    "odis_forcing": ([_V, _V, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int], C.c_int),
     "odis_ab3": ([_V, _V, _V, C.c_int, C.c_int, C.c_int], C.c_int),
     "odis_interpolate_velocity": ([_V, _V, _V, C.c_int], C.c_int),
     "odis_interpolate_cartesian": ([_V, _V, _V, C.c_int], C.c_int),
@@ -328,9 +331,10 @@ class Mesh:
 
 
 def make_params(*, radius, g, angvel, h, alpha, ecc=0.0, obliq=0.0, love_reduct=1.0, dt, potential=POT_ECC,
-                init_load=0, precision=FP64, sh_lmax=0, sh_factors=None, advection=0, friction=FRIC_LINEAR) -> Params:
+                init_load=0, precision=FP64, sh_lmax=0, sh_factors=None, advection=0, friction=FRIC_LINEAR,
+                semimajor_axis=1221.87e6, fourier_freq=1) -> Params:
     p = Params(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load, precision, sh_lmax, None,
-               advection, friction)
+               advection, friction, semimajor_axis, fourier_freq)
     if sh_lmax:
         arr = np.ascontiguousarray(sh_factors, dtype=np.float64)
         p._factors = arr  # keep alive
@@ -362,9 +366,14 @@ class Solver:
         _ck(lib().odis_update_eta(self._h, _vp(out), _vp(v), MEM_HOST), "odis_update_eta")
         return out
 
-    def forcing(self, type_: int, t: float) -> np.ndarray:
-        out = np.zeros(self.N)
-        _ck(lib().odis_forcing(self._h, _vp(out), int(type_), float(t), MEM_HOST), "odis_forcing")
+    def forcing(self, type_: int, t: float, ecc: float | None = None, obl: float | None = None,
+                out: np.ndarray | None = None) -> np.ndarray:
+        """forcing(..., type, time, ecc, obl): ecc/obl default to the context's; types without a case in
+        the reference's switch leave `out` (zeros if not given) untouched."""
+        out = np.zeros(self.N) if out is None else np.ascontiguousarray(out, np.float64)
+        _ck(lib().odis_forcing(self._h, _vp(out), int(type_), float(t),
+                               float(self.params.ecc if ecc is None else ecc),
+                               float(self.params.obliq if obl is None else obl), MEM_HOST), "odis_forcing")
         return out
 
     def integrateAB3scalar(self, s: np.ndarray, ds_dt: np.ndarray, it: int) -> None:

@@ -667,6 +667,8 @@ int adv_state_alloc(AdvDev* a, int precision, double h0, const std::vector<doubl
     if (st != ODIS_OK) return st;
     release_host(a);
     a->prec = precision;
+    // the allocations' zero fills and k_adv_thickness ran on the legacy default stream;
+    // this wait orders them before the caller's first use of the context's own stream
     return cudaDeviceSynchronize() == cudaSuccess ? ODIS_OK : ODIS_ERR_CUDA;
 }
 

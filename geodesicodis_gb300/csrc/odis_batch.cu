@@ -27,6 +27,7 @@
 // and returns, so the launch always ends.
 #include "../../include/odis_gpu.h"
 #include "odis_internal.h"
+#include "odis_forcing.cuh"
 
 #include <cuda_runtime.h>
 
@@ -676,7 +677,11 @@ extern "C" odis_status odis_batch_create(const odis_params* common, const odis_m
     if (!common || !meshes || n_meshes <= 0 || !members || count <= 0 || !out) return ODIS_ERR_ARG;
     *out = nullptr;
     if (!(common->g > 0.0) || !(common->radius > 0.0) || !(common->angvel > 0.0)) return ODIS_ERR_ARG;
-    if (common->potential < ODIS_POT_NONE || common->potential > ODIS_POT_FULL) return ODIS_ERR_ARG;
+    // a member's forcing is ecc x (the unit-eccentricity potential) + obliq x (the unit-obliquity one):
+    // the single-frequency potentials (and the unforced types), not FULL2 / PLANET / GENERAL
+    if (!pot_valid(common->potential) || pot_nodal(common->potential)) return ODIS_ERR_ARG;
+    // the batch reports LINEAR dissipation (alpha 1000 h |u|^2) only
+    if (common->friction != ODIS_FRIC_LINEAR) return ODIS_ERR_ARG;
     for (int k = 0; k < n_meshes; k++) if (!meshes[k]) return ODIS_ERR_ARG;
     for (int i = 0; i < count; i++) {
         const odis_batch_member& mb = members[i];

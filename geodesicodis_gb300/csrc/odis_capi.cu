@@ -86,7 +86,12 @@ struct odis_ctx {
     Operators<float2> opdf;      // double-float method
     double* nrm = nullptr;       // [2][Ep]
     double* area = nullptr;      // [Ep]
-    double* trig = nullptr;      // [10][Np]
+    double* trig = nullptr;      // [kNodeTrig][Np] node trig table and Pbar_20, Pbar_22 (forcing)
+    ForcingConst fk{};           // the run's forcing type and constants
+    bool nodal = false;          // forcing evaluated at the nodes every step (FULL2, PLANET, GENERAL)
+    double* d_fterms = nullptr;  // [fterms_cap][kForcingTerms] time terms of the current run (nodal forcing)
+    int fterms_cap = 0;
+    void* ufr = nullptr;         // [Np] nodal forcing / g in the method's type when there is no self-gravity
     double* rbf = nullptr;       // [3][6][Np] Cartesian reconstruction blocks
     // double-float copies of rbf, nrm and area for an ODIS_DF64 nonlinear run
     float2 *rbf_df = nullptr, *nrm_df = nullptr, *area_df = nullptr;
@@ -126,6 +131,7 @@ struct odis_ctx {
         if (adv) adv_destroy(adv);
         if (d_power) cudaFree(d_power);
         if (d_phase) cudaFree(d_phase);
+        if (d_fterms) cudaFree(d_fterms);
         if (plan.part) cudaFree(plan.part);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
@@ -530,7 +536,8 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     if (!p || !mp || !out) return ODIS_ERR_ARG;
     *out = nullptr;
     if (p->precision != ODIS_FP64 && p->precision != ODIS_FP32 && p->precision != ODIS_DF64) return ODIS_ERR_ARG;
-    if (p->potential < ODIS_POT_NONE || p->potential > ODIS_POT_FULL) return ODIS_ERR_ARG;
+    if (!pot_valid(p->potential)) return ODIS_ERR_ARG;
+    if (p->advection && pot_nodal(p->potential)) return ODIS_ERR_ARG;
     if (!(p->dt > 0.0) || !(p->g > 0.0) || !(p->h > 0.0) || !(p->radius > 0.0) || p->alpha < 0.0) return ODIS_ERR_ARG;
     if (p->sh_lmax < 0 || p->sh_lmax > 64 || (p->sh_lmax > 0 && !p->sh_factors)) return ODIS_ERR_ARG;
     if (p->friction != ODIS_FRIC_LINEAR && p->friction != ODIS_FRIC_QUADRATIC) return ODIS_ERR_ARG;
@@ -575,7 +582,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
         if (st != ODIS_OK) return st;
     }
     // geometry needed by the per-operator calls
-    std::vector<double> nrm((size_t)2 * c->Ep, 0.0), area(c->Ep, 0.0), trig((size_t)10 * c->Np, 0.0);
+    std::vector<double> nrm((size_t)2 * c->Ep, 0.0), area(c->Ep, 0.0), trig((size_t)kNodeTrig * c->Np, 0.0);
     for (int e = 0; e < m.E; e++) {
         nrm[e] = m.face_normal[(size_t)e * 2];
         nrm[(size_t)c->Ep + e] = m.face_normal[(size_t)e * 2 + 1];
@@ -583,10 +590,16 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     }
     for (int i = 0; i < m.N; i++) {
         const double lat = m.node_sph[(size_t)i * 2], lon = m.node_sph[(size_t)i * 2 + 1];
-        const double t[10] = {std::cos(lat), std::sin(lat), std::cos(lon), std::sin(lon), std::cos(2.0 * lat),
-                              std::sin(2.0 * lat), std::cos(2.0 * lon), std::sin(2.0 * lon),
-                              std::pow(std::cos(lat), 2.0), std::pow(std::sin(lat), 2.0)};
-        for (int k = 0; k < 10; k++) trig[(size_t)k * c->Np + i] = t[k];
+        // Pbar_20, Pbar_22 (4pi-normalised, Condon-Shortley phase) of z = sin(lat) by the
+        // recurrences of the fully normalised functions, as the self-gravity basis
+        const double z = std::cos(kPi * 0.5 - lat), sz = std::sqrt(std::fmax(0.0, 1.0 - z * z));
+        const double p10 = std::sqrt(3.0) * z, p11 = -std::sqrt(3.0) * sz;
+        const double p20 = std::sqrt(15.0 / 4.0) * z * p10 - std::sqrt(5.0 / 4.0) * 1.0;
+        const double p22 = -std::sqrt(5.0 / 4.0) * sz * p11;
+        const double t[kNodeTrig] = {std::cos(lat), std::sin(lat), std::cos(lon), std::sin(lon), std::cos(2.0 * lat),
+                                     std::sin(2.0 * lat), std::cos(2.0 * lon), std::sin(2.0 * lon),
+                                     std::pow(std::cos(lat), 2.0), std::pow(std::sin(lat), 2.0), p20, p22};
+        for (int k = 0; k < kNodeTrig; k++) trig[(size_t)k * c->Np + i] = t[k];
     }
     c->nrm = A.upload(nrm);
     c->area = A.upload(area);
@@ -628,6 +641,17 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
         c->s32.usg = sh_usg32(c->sh);
         c->sdf.usg = sh_usgdf(c->sh);
     }
+    c->fk = ForcingConst{p->potential, p->angvel, p->radius, p->love_reduct, p->ecc, p->obliq, p->semimajor_axis,
+                         (double)p->fourier_freq};
+    c->nodal = pot_nodal(p->potential);
+    if (c->nodal && !c->sh) {      // a node buffer of its own; with self-gravity the synthesis buffer takes the sum
+        const size_t esz = p->precision == ODIS_FP32 ? sizeof(float) : sizeof(double);
+        c->ufr = A.alloc<double>(((size_t)c->Np * esz + 7) / 8);
+        if (!c->ufr) return ODIS_ERR_NOMEM;
+        c->s64.usg = p->precision == ODIS_FP64 ? (const double*)c->ufr : nullptr;
+        c->s32.usg = p->precision == ODIS_FP32 ? (const float*)c->ufr : nullptr;
+        c->sdf.usg = p->precision == ODIS_DF64 ? (const float2*)c->ufr : nullptr;
+    }
     StepConst& sc = c->sc;
     sc.E = m.E;
     sc.N = m.N;
@@ -641,7 +665,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     sc.ab3c = 5. / 12.;
     sc.init_load = p->init_load ? 1 : 0;
     sc.quad = p->friction == ODIS_FRIC_QUADRATIC ? 1 : 0;
-    sc.use_sg = p->sh_lmax > 0 ? 1 : 0;
+    sc.use_sg = (p->sh_lmax > 0 || c->nodal) ? 1 : 0;
     sc.df_dt = df_from_double(p->dt);
     sc.df_malpha = df_from_double(-p->alpha);
     sc.df_a = df_from_double(sc.ab3a);
@@ -652,7 +676,7 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
     sc.f_a = (float)sc.ab3a;
     sc.f_b = (float)sc.ab3b;
     sc.f_c = (float)sc.ab3c;
-    if ((p->precision == ODIS_FP64 || p->precision == ODIS_DF64) && p->sh_lmax == 0) {
+    if ((p->precision == ODIS_FP64 || p->precision == ODIS_DF64) && p->sh_lmax == 0 && !c->nodal) {
         st = build_persist_plan(c.get(), m);
         if (st != ODIS_OK) return st;
     }
@@ -823,13 +847,15 @@ extern "C" odis_status odis_update_eta(odis_ctx* c, double* detadt, const double
     return st != ODIS_OK ? st : io.done();
 }
 
-extern "C" odis_status odis_forcing(odis_ctx* c, double* U, int type, double t, int mem)
+extern "C" odis_status odis_forcing(odis_ctx* c, double* U, int type, double t, double ecc, double obl, int mem)
 {
-    if (!c || !U || !mem_ok(mem) || type < ODIS_POT_NONE || type > ODIS_POT_FULL) return ODIS_ERR_ARG;
+    if (!c || !U || !mem_ok(mem) || !pot_valid(type)) return ODIS_ERR_ARG;
+    if (!pot_has_case(type)) return ODIS_OK;       // the reference's switch leaves U as it is
     Io io{c, mem};
     double* dout = io.out(U);
-    launch_forcing(c->trig, c->N, c->Np, dout, type, t, c->p.angvel, c->p.radius, c->p.love_reduct, c->p.ecc,
-                   c->p.obliq, c->stream);
+    const ForcingConst k{type, c->p.angvel, c->p.radius, c->p.love_reduct, ecc, obl, c->p.semimajor_axis,
+                         (double)c->p.fourier_freq};
+    launch_forcing(c->trig, c->N, c->Np, dout, k, forcing_terms(k, t), c->stream);
     int st = io.back(U, dout, c->N);
     return st != ODIS_OK ? st : io.done();
 }
@@ -884,13 +910,25 @@ static const void* state_eta(const odis_ctx* c)
          : c->p.precision == ODIS_DF64 ? (const void*)c->sdf.eta : (const void*)c->s64.eta;
 }
 
-static int kernels_per_step(const odis_ctx* c) { return 2 + (c->sh ? sh_kernels_per_step(c->sh) : 0); }
+static int kernels_per_step(const odis_ctx* c)
+{
+    return 2 + (c->sh ? sh_kernels_per_step(c->sh) : 0) + (c->nodal ? 1 : 0);
+}
+
+static void* usg_buffer(odis_ctx* c)
+{
+    return c->p.precision == ODIS_FP32 ? (void*)c->s32.usg : c->p.precision == ODIS_DF64 ? (void*)c->sdf.usg
+                                                                                         : (void*)c->s64.usg;
+}
 
 static void enqueue_steps(odis_ctx* c, int n)
 {
     c->launches += (long long)n * kernels_per_step(c) + 1;
     for (int k = 0; k < n; k++) {
         if (c->sh) sh_enqueue(c->sh, state_eta(c), c->stream);
+        if (c->nodal)
+            launch_node_forcing(c->p.precision, c->trig, c->N, c->Np, usg_buffer(c), c->sh ? 1 : 0, 1.0 / c->p.g, c->fk,
+                                c->d_fterms, c->d_iter, c->d_run_first, k, c->stream);
         if (c->p.precision == ODIS_FP64) launch_step<double, false>(c->op64.fc, c->op64.cc, c->s64, c->sc, k, c->stream);
         else if (c->p.precision == ODIS_FP32) launch_step<float, true>(c->op32.fc, c->op32.cc, c->s32, c->sc, k, c->stream);
         else {
@@ -934,6 +972,19 @@ static int prepare_phase(odis_ctx* c, long long first, int n)
         c->s32.phase = (const float*)c->d_phase;
         c->sdf.phase = (const float2*)c->d_phase;
         if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    }
+    if (c->nodal) {
+        if (n > c->fterms_cap) {
+            if (c->d_fterms) cudaFree(c->d_fterms);
+            c->d_fterms = nullptr;
+            c->fterms_cap = 0;
+            const int cap = std::max(n, 4096);
+            ODIS_CK(cudaMalloc(&c->d_fterms, sizeof(double) * kForcingTerms * (size_t)cap));
+            c->fterms_cap = cap;
+            if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+        }
+        launch_forcing_terms(c->d_fterms, c->fk, first, n, c->p.dt, c->stream);
+        c->launches += 1;
     }
     launch_phase(c->d_phase, c->p.precision, first, n, c->p.dt, c->p.angvel, c->stream);
     c->launches += 1;

@@ -40,8 +40,8 @@ int parse_input(const char* path, odis_input& out)
     // defaults, src/globals.cpp:479-571
     double radius = 2574.73e3, k2 = .120, h2 = .2, love = 0.920012, h = 400, g = 1.35;
     double e = 0.0288, theta_default = 0.32 * kPi / 180., alpha = 2.28e-7;
-    double dt_target = 40., angvel = 4.56e-6, end_time = 80.;
-    int lmax = 10, level = 1, output_time = 1;
+    double dt_target = 40., angvel = 4.56e-6, end_time = 80., semimajor = 1221.87e6;
+    int lmax = 10, level = 1, output_time = 1, fourier_freq = 0;
     bool advection = false, diss_avg = true, kinetic_avg = false;
     bool out_disp = false, out_vel = false, out_cart = false, out_diss = false, out_dummy1 = false;
     std::string potential = "ECC", friction = "QUADRATIC", surface = "FREE", solver = "AB3", init = "NONE";
@@ -65,6 +65,8 @@ int parse_input(const char* path, odis_input& out)
         else if (key == "ocean thickness") rd(h);
         else if (key == "surface gravity") rd(g);
         else if (key == "eccentricity") rd(e);
+        else if (key == "semimajor axis") rd(semimajor);
+        else if (key == "fourier freq") ri(fourier_freq);
         else if (key == "obliquity") { rd(theta_read); theta_given = true; }
         else if (key == "time step") rd(dt_target);
         else if (key == "friction coefficient") rd(alpha);
@@ -104,9 +106,15 @@ int parse_input(const char* path, odis_input& out)
     p.obliq = theta;
     p.love_reduct = (surface == "FREE") ? 1.0 + k2 - h2 : love;
     p.dt = dt;
-    p.potential = potential == "ECC" ? ODIS_POT_ECC : potential == "OBLIQ" ? ODIS_POT_OBLIQ
-                : potential == "OBLIQ_WEST" ? ODIS_POT_OBLIQ_WEST : potential == "FULL" ? ODIS_POT_FULL
-                : potential == "NONE" ? ODIS_POT_NONE : -1;
+    // the reference's name -> tide_type mapping (src/globals.cpp:250-266)
+    static const char* const kPotNames[] = {"OBLIQ", "OBLIQ_WEST", "OBLIQ_EAST", "ECC_RAD", "ECC_LIB", "ECC",
+                                            "ECC_WEST", "ECC_EAST", "FULL", "FULL2", "TOTAL", "ECC_W3",
+                                            "OBLIQ_W3", "PLANET", "PLANET_OBL", "GENERAL", "NONE"};
+    p.potential = -1;
+    for (int k = 0; k <= ODIS_POT_NONE; k++)
+        if (potential == kPotNames[k]) p.potential = k;
+    p.semimajor_axis = semimajor;
+    p.fourier_freq = fourier_freq;
     p.init_load = init == "LOAD" ? 1 : 0;
     p.precision = ODIS_FP64;
     p.sh_lmax = 0;

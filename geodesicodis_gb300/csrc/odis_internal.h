@@ -58,7 +58,8 @@ int build_mesh(int N, const double* node_sph, const int* friends, const double* 
                double radius, Mesh& m);
 
 // Forcing as a single-frequency pair: U_i(t) = cos(M) Ua_i + sin(M) Ub_i with
-// M = angvel * t, for the ECC / OBLIQ / OBLIQ_WEST / FULL potentials.
+// M = angvel * t, for the ECC / OBLIQ / OBLIQ_WEST / FULL potentials; zero for
+// the other valid types (unforced, or evaluated at the nodes every step).
 int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, std::vector<double>& Ub);
 
 // RBF reconstruction of Cartesian velocity at the nodes from the face-normal

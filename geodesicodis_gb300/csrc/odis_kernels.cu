@@ -23,6 +23,7 @@
 #include "odis_df64.cuh"
 #include "odis_kernels.cuh"
 #include "odis_pdl.cuh"
+#include "odis_forcing.cuh"
 
 #include <type_traits>
 
@@ -338,6 +339,9 @@ __global__ void k_bump_iter(long long* iter, int n)
 
 template <class T> __device__ __forceinline__ T from_double_dev(double x) { return (T)x; }
 template <> __device__ __forceinline__ float2 from_double_dev<float2>(double x) { return df_from_double(x); }
+__device__ __forceinline__ double to_double_dev(double x) { return x; }
+__device__ __forceinline__ double to_double_dev(float x) { return (double)x; }
+__device__ __forceinline__ double to_double_dev(float2 x) { return df_to_double(x); }
 
 // cos, sin of the forcing phase Omega * t^{n+1}, t^{n+1} = dt*n + dt
 // (src/timeIntegrator.cpp:218), for the steps first .. first+n-1, stored in
@@ -388,33 +392,53 @@ __global__ void k_divergence(CellCoef<double> cc, int N, int Np, double* q, cons
     q[i] = s;
 }
 
-// forcing (src/tidalPotentials.cpp:29-174), from the node trig tables
-// trig[10][Np]: cosLat sinLat cosLon sinLon cos2Lat sin2Lat cos2Lon sin2Lon cos^2Lat sin^2Lat
-__global__ void k_forcing(const double* trig, int N, int Np, double* U, int type, double t,
-                          double omega, double radius, double love, double ecc, double obl)
+// forcing (src/tidalPotentials.cpp:29-334) at one time, from the node table
+// trig[kNodeTrig][Np] and the time terms computed on the host
+__global__ void k_forcing(const double* __restrict__ trig, int N, int Np, double* __restrict__ U, ForcingConst k,
+                          ForcingTerms f)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    double sinM, cosM;
-    sincos(omega * t, &sinM, &cosM);
-    const double cosLat = trig[0 * Np + i], sinLat = trig[1 * Np + i], cosLon = trig[2 * Np + i];
-    const double sinLon = trig[3 * Np + i], sin2Lat = trig[5 * Np + i];
-    const double cos2Lon = trig[6 * Np + i], sin2Lon = trig[7 * Np + i], cosSq = trig[8 * Np + i], sinSq = trig[9 * Np + i];
-    const double w2r2 = omega * omega * (radius * radius);
-    double u = 0.0;
-    if (type == ODIS_POT_ECC || type == ODIS_POT_FULL) {
-        const double f = 0.75 * love * w2r2 * ecc;
-        u = f * ((1. - 3. * sinSq) * cosM + cosSq * (3. * cosM * cos2Lon + 4. * sinM * sin2Lon));
-    }
-    if (type == ODIS_POT_OBLIQ || type == ODIS_POT_FULL) {
-        const double f = -3. / 2. * love * w2r2 * obl;
-        u += f * cosM * sin2Lat * cosLon;
-    }
-    if (type == ODIS_POT_OBLIQ_WEST) {
-        const double f = 0.5 * love * w2r2 * obl;
-        u = 3 * f * sinLat * cosLat * (cosLon * cosM - sinLon * sinM);
-    }
-    U[i] = u;
+    double tr[kNodeTrig];
+#pragma unroll
+    for (int q = 0; q < kNodeTrig; q++) tr[q] = trig[(size_t)q * Np + i];
+    U[i] = forcing_node(k, f, tr);
+}
+
+// time terms of every step of a run: row k at t = dt (first + k) + dt
+__global__ void k_forcing_terms(double* __restrict__ terms, ForcingConst k, long long first, int n, double dt)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const ForcingTerms f = forcing_terms(k, dt * (double)(first + q) + dt);
+    const double* src = reinterpret_cast<const double*>(&f);
+#pragma unroll
+    for (int j = 0; j < kForcingTerms; j++) terms[(size_t)q * kForcingTerms + j] = src[j];
+}
+
+// the fused loop's nodal forcing (FULL2, PLANET, GENERAL): the potential at
+// t^{n+1} over g, written (or added, after the self-gravity synthesis) into the
+// node buffer whose gradient the face kernel adds to the momentum forcing
+template <class T>
+__global__ void __launch_bounds__(256) k_node_forcing(const double* __restrict__ trig, int N, int Np, T* __restrict__ usg,
+                                                      int add, double inv_g, ForcingConst k,
+                                                      const double* __restrict__ terms, const long long* iter,
+                                                      const long long* run_first, int offset)
+{
+    pdl_wait();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const long long kstep = *iter + offset - *run_first;
+    ForcingTerms f;
+    double* dst = reinterpret_cast<double*>(&f);
+#pragma unroll
+    for (int j = 0; j < kForcingTerms; j++) dst[j] = __ldg(&terms[(size_t)kstep * kForcingTerms + j]);
+    double tr[kNodeTrig];
+#pragma unroll
+    for (int q = 0; q < kNodeTrig; q++) tr[q] = __ldg(&trig[(size_t)q * Np + i]);
+    double u = forcing_node(k, f, tr) * inv_g;
+    if (add) u += to_double_dev(usg[i]);
+    usg[i] = from_double_dev<T>(u);
 }
 
 // integrateAB3scalar with the reference's [num][3] history layout
@@ -572,9 +596,25 @@ void launch_momentum(const FaceCoef<double>& fc, int E, int Ep, double* dvdt, co
 void launch_divergence(const CellCoef<double>& cc, int N, int Np, double* q, const double* v, cudaStream_t s)
 { k_divergence<<<blocks(N, 256), 256, 0, s>>>(cc, N, Np, q, v); }
 
-void launch_forcing(const double* trig, int N, int Np, double* U, int type, double t, double omega, double radius,
-                    double love, double ecc, double obl, cudaStream_t s)
-{ k_forcing<<<blocks(N, 256), 256, 0, s>>>(trig, N, Np, U, type, t, omega, radius, love, ecc, obl); }
+void launch_forcing(const double* trig, int N, int Np, double* U, const ForcingConst& k, const ForcingTerms& f,
+                    cudaStream_t s)
+{ k_forcing<<<blocks(N, 256), 256, 0, s>>>(trig, N, Np, U, k, f); }
+
+void launch_forcing_terms(double* terms, const ForcingConst& k, long long first, int n, double dt, cudaStream_t s)
+{ k_forcing_terms<<<blocks(n, 128), 128, 0, s>>>(terms, k, first, n, dt); }
+
+void launch_node_forcing(int precision, const double* trig, int N, int Np, void* usg, int add, double inv_g,
+                         const ForcingConst& k, const double* terms, const long long* iter, const long long* run_first,
+                         int offset, cudaStream_t s)
+{
+    const int nb = blocks(N, 256);
+    if (precision == ODIS_FP64)
+        pdl_launch(k_node_forcing<double>, nb, 256, 0, s, trig, N, Np, (double*)usg, add, inv_g, k, terms, iter, run_first, offset);
+    else if (precision == ODIS_FP32)
+        pdl_launch(k_node_forcing<float>, nb, 256, 0, s, trig, N, Np, (float*)usg, add, inv_g, k, terms, iter, run_first, offset);
+    else
+        pdl_launch(k_node_forcing<float2>, nb, 256, 0, s, trig, N, Np, (float2*)usg, add, inv_g, k, terms, iter, run_first, offset);
+}
 
 void launch_ab3_ref(double* x, double* h, int iter, int num, double dt, int init_load, cudaStream_t s)
 { k_ab3_ref<<<blocks(num, 256), 256, 0, s>>>(x, h, iter, num, dt, init_load); }

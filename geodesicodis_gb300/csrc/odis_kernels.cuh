@@ -3,6 +3,7 @@
 
 #include "../../include/odis_gpu.h"
 #include "odis_device.cuh"
+#include "odis_forcing.cuh"
 
 namespace odis {
 
@@ -35,8 +36,6 @@ void launch_power_tail_df(const FaceCoef<float2>& fc, const State<float2>& st, c
 void launch_momentum(const FaceCoef<double>& fc, int E, int Ep, double* dvdt, const double* v, const double* eta,
                      cudaStream_t s);
 void launch_divergence(const CellCoef<double>& cc, int N, int Np, double* q, const double* v, cudaStream_t s);
-void launch_forcing(const double* trig, int N, int Np, double* U, int type, double t, double omega, double radius,
-                    double love, double ecc, double obl, cudaStream_t s);
 void launch_ab3_ref(double* x, double* h, int iter, int num, double dt, int init_load, cudaStream_t s);
 void launch_interp(const FaceCoef<double>& fc, const double* nrm, int E, int Ep, double* uv, const double* v,
                    cudaStream_t s);

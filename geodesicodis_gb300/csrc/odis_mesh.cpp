@@ -19,6 +19,7 @@
 //   TRiSK weights ..................... src/mesh.cpp:680-907
 //   face area (no 1/2) ................ src/mesh.cpp:1093
 #include "odis_internal.h"
+#include "odis_forcing.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -562,7 +563,6 @@ int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, 
         double fe = 0.75 * p.love_reduct * w2r2 * p.ecc;
         double fo = -3. / 2. * p.love_reduct * w2r2 * p.obliq;
         switch (p.potential) {
-        case ODIS_POT_NONE: break;
         case ODIS_POT_ECC:
             Ua[i] = fe * ((1. - 3. * sinSqLat) + cosSqLat * 3. * cos2Lon);
             Ub[i] = fe * (cosSqLat * 4. * sin2Lon);
@@ -579,8 +579,9 @@ int forcing_basis(const Mesh& m, const odis_params& p, std::vector<double>& Ua, 
             Ua[i] = fe * ((1 - 3 * sinSqLat) + cosSqLat * 3 * cos2Lon) + fo * sin2Lat * cosLon;
             Ub[i] = fe * (cosSqLat * 4 * sin2Lon);
             break;
-        default:
-            return ODIS_ERR_ARG;
+        default:            // unforced types, and the nodal ones (evaluated per step at the nodes)
+            if (!pot_valid(p.potential)) return ODIS_ERR_ARG;
+            break;
         }
     }
     return ODIS_OK;

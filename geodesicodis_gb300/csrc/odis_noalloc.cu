@@ -17,7 +17,10 @@
 // capture).  All calls share the array: two calls that overlap on the GPU
 // (different streams, or threads racing) race on it and may return wrong sums;
 // serialise them.  Nothing in the array has to start at zero: each call writes
-// every partial it later reads.
+// every partial it later reads.  The cached address belongs to the device's
+// primary context: after a cudaDeviceReset in this process it is stale, and
+// this entry point must not be called again.  QUADRATIC friction is not
+// computed here; odis_update_energy covers it.
 #include "../../include/odis_gpu.h"
 
 #include <cuda_runtime.h>

@@ -26,8 +26,12 @@ inline bool pdl_on()
     return on;
 }
 
+// Returns the launch status.  If the driver refuses the attributed launch (for
+// instance under a capture mode that does not take it), the kernel is launched
+// again in plain stream order and that launch's status is returned.
 template <typename... KArgs, typename... Args>
-inline void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args)
+inline cudaError_t pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
@@ -39,7 +43,13 @@ inline void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = pdl_on() ? 1 : 0;
-    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    if (e != cudaSuccess && cfg.numAttrs) {
+        (void)cudaGetLastError();          // the refused launch's error, replaced by the retry's
+        cfg.numAttrs = 0;
+        e = cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    }
+    return e;
 }
 
 }  // namespace odis

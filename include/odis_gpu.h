@@ -49,12 +49,28 @@ typedef int odis_status;
 #define ODIS_ERR_MESH 7         /* inconsistent grid */
 #define ODIS_ERR_NOMEM 8        /* allocation failed */
 
-/* forcing types (the reference's `potential` keys) */
-#define ODIS_POT_NONE 0
-#define ODIS_POT_ECC 1
-#define ODIS_POT_OBLIQ 2
-#define ODIS_POT_OBLIQ_WEST 3
-#define ODIS_POT_FULL 4
+/* forcing types: the values of the reference's enum Potential
+ * (include/globals.h:60-76), so that globals->tide_type passes through
+ * unchanged.  forcing() (src/tidalPotentials.cpp:29-334) has cases for ECC,
+ * OBLIQ, OBLIQ_WEST, FULL, FULL2, PLANET and GENERAL; the other types leave
+ * the potential array untouched (a run with one of them is unforced). */
+#define ODIS_POT_OBLIQ 0
+#define ODIS_POT_OBLIQ_WEST 1
+#define ODIS_POT_OBLIQ_EAST 2
+#define ODIS_POT_ECC_RAD 3
+#define ODIS_POT_ECC_LIB 4
+#define ODIS_POT_ECC 5
+#define ODIS_POT_ECC_WEST 6
+#define ODIS_POT_ECC_EAST 7
+#define ODIS_POT_FULL 8
+#define ODIS_POT_FULL2 9
+#define ODIS_POT_TOTAL 10
+#define ODIS_POT_ECC_W3 11
+#define ODIS_POT_OBLIQ_W3 12
+#define ODIS_POT_PLANET 13
+#define ODIS_POT_PLANET_OBL 14
+#define ODIS_POT_GENERAL 15
+#define ODIS_POT_NONE 16
 
 /* arithmetic of the state and stencils */
 #define ODIS_FP64 0             /* everything in FP64 (the reference's method) */
@@ -100,6 +116,10 @@ typedef struct odis_params {
     int friction;           /* ODIS_FRIC_LINEAR (0) or ODIS_FRIC_QUADRATIC (1): which dissipation
                                updateEnergy reports (src/energy.cpp:30-53); the momentum equation
                                keeps the linear drag -alpha v in both, as in the reference */
+    double semimajor_axis;  /* m, input.in "semimajor axis" (src/globals.cpp:82): the orbit radius a2
+                               of the PLANET forcing (src/tidalPotentials.cpp:176-225) */
+    int fourier_freq;       /* input.in "fourier freq" (src/globals.cpp:130): the harmonic q_max of
+                               the GENERAL forcing (src/tidalPotentials.cpp:227-281) */
 } odis_params;
 
 /* Parsed input.in (src/globals.cpp:58-203 keys).  Strings are fixed-size. */
@@ -206,8 +226,14 @@ odis_status odis_device_status(odis_ctx* c);
 odis_status odis_update_momentum(odis_ctx* c, double* dvdt, const double* v, const double* eta, int mem);
 /* detadt[N] = h*D*v */
 odis_status odis_update_eta(odis_ctx* c, double* detadt, const double* v, int mem);
-/* U[N] = tidal potential of type `type` at time t (s) */
-odis_status odis_forcing(odis_ctx* c, double* U, int type, double t, int mem);
+/* forcing(globals, grid, U, type, t, ecc, obl): U[N] = tidal potential of type
+ * `type` (ODIS_POT_*, the reference's Potential values) at time t (s) with
+ * eccentricity ecc and obliquity obl (rad).  Types without a case in the
+ * reference's switch, and NONE, leave U untouched (ODIS_OK).  GENERAL uses the
+ * 4pi-normalised Pbar_20 and Pbar_22 at the nodes; the reference's v1.11 never
+ * fills those arrays (CalcLegendreFuncs is commented out), so there its GENERAL
+ * potential is zero.  ODIS_ERR_ARG for a type outside 0..16. */
+odis_status odis_forcing(odis_ctx* c, double* U, int type, double t, double ecc, double obl, int mem);
 /* integrateAB3scalar on s[num] with history hist[num][3] at iteration iter */
 odis_status odis_ab3(odis_ctx* c, double* s, double* hist, int iter, int num, int mem);
 /* uv[E][2] = (east, north) velocity at faces from normal velocity v[E] */
@@ -260,7 +286,8 @@ odis_status odis_analytical_state(const odis_params* p, const odis_mesh* mesh, d
                                   double* dvdt, double* detadt);
 
 /* ---- allocation-free dissipation --------------------------------------- */
-/* Same result as odis_update_energy, for callers that cannot allocate device
+/* Same result as odis_update_energy for LINEAR friction (the only dissipation it
+ * computes), for callers that cannot allocate device
  * memory (host callbacks or graph host nodes, fixed-budget real-time loops,
  * plugins handed only device buffers): no context, no cudaMalloc/cudaFree.
  * No counterpart in the reference (its updateEnergy, src/energy.cpp:13-61, is
@@ -272,7 +299,9 @@ odis_status odis_analytical_state(const odis_params* p, const odis_mesh* mesh, d
  * that loads the library until exit: n_faces above 2,097,152 returns
  * ODIS_ERR_ARG.  The first call on a device sets up that device's scratch
  * address (make it before any stream capture).  Calls share the scratch, so
- * calls that overlap on the GPU race: serialise them. */
+ * calls that overlap on the GPU race: serialise them.  The cached per-device
+ * address goes stale if the process resets the device (cudaDeviceReset): do
+ * not call this entry point after a reset. */
 odis_status odis_update_energy_noalloc(const double* uv, const double* area, int n_faces, double alpha, double h,
                                        double radius, double* e_out, double* avg_out, void* stream);
 

@@ -22,7 +22,7 @@
  *   Coriolis operator ....... src/mesh.cpp:2808-2901 (CalcCoriolisOperatorCoeffs)
  *   linear drag ............. src/mesh.cpp:2903-3003 (CalcLinearDragOperatorCoeffs)
  *   geometry helpers ........ include/mathRoutines.h:29-439
- *   forcing ................. src/tidalPotentials.cpp:29-174
+ *   forcing ................. src/tidalPotentials.cpp:29-334 (every live case)
  *   updateMomentum .......... src/updateMomentum.cpp:16-46 (linear branch :42)
  *   updateEta ............... src/updateEta.cpp:7-44 (linear branch :39)
  *   integrateAB3scalar ...... src/temporalOperators.cpp:17-68
@@ -59,9 +59,17 @@
 #define ORC_PI 3.1415926535897932384626433832795028841971693993751058
 #define ORC_RADCONV (ORC_PI / 180.0)
 
-/* forcing types, numbered as in include/globals.h of the reference */
-enum { ORC_NONE = 0, ORC_ECC = 1, ORC_OBLIQ = 2, ORC_OBLIQ_WEST = 3,
-       ORC_FULL = 4, ORC_FULL2 = 5 };
+void orc_plmbar(int L, double z, double *P);
+
+/* forcing types: the values of the reference's enum Potential
+ * (include/globals.h:60-76), which ab3Explicit passes to forcing() as
+ * globals->tide_type.  Types without a case in forcing()'s switch
+ * (OBLIQ_EAST, ECC_RAD, ECC_LIB, ECC_WEST, ECC_EAST, TOTAL, ECC_W3, OBLIQ_W3,
+ * PLANET_OBL) leave the potential array as it was, like NONE. */
+enum { ORC_OBLIQ = 0, ORC_OBLIQ_WEST = 1, ORC_OBLIQ_EAST = 2, ORC_ECC_RAD = 3, ORC_ECC_LIB = 4,
+       ORC_ECC = 5, ORC_ECC_WEST = 6, ORC_ECC_EAST = 7, ORC_FULL = 8, ORC_FULL2 = 9, ORC_TOTAL = 10,
+       ORC_ECC_W3 = 11, ORC_OBLIQ_W3 = 12, ORC_PLANET = 13, ORC_PLANET_OBL = 14, ORC_GENERAL = 15,
+       ORC_NONE = 16 };
 
 /* ------------------------------------------------------------------------ */
 /* mathRoutines.h restatements (include/mathRoutines.h:29-439)               */
@@ -260,6 +268,7 @@ typedef struct {
     double *interp_w;     /* [E][10] */
     int *interp_n;        /* [E] number of valid entries (10, 9 or 8) */
     double *trig;         /* [N][10]: cosLat sinLat cosLon sinLon cos2Lat sin2Lat cos2Lon sin2Lon cosSqLat sinSqLat */
+    double *pbar2;        /* [N][2]: 4pi-normalised Pbar_20, Pbar_22 (GENERAL forcing) */
     int *face_verts;      /* [E][2] face_vertexes */
     double *vert_R;       /* [V][3] kite fraction of vertex v in the control volume of vert_nodes(v, j) */
     int *vert_faces;      /* [V][3] */
@@ -279,7 +288,7 @@ void orc_mesh_free(orc_mesh *M)
     free(M->vertexes); free(M->vert_sph); free(M->vert_nodes); free(M->faces); free(M->node_face_dir);
     free(M->face_nodes); free(M->face_len); free(M->face_dist); free(M->face_area); free(M->face_centre);
     free(M->face_m); free(M->face_normal); free(M->face_int); free(M->face_nxyz); free(M->interp_friends); free(M->interp_w);
-    free(M->interp_n); free(M->trig);
+    free(M->interp_n); free(M->trig); free(M->pbar2);
     free(M->face_verts); free(M->vert_R); free(M->vert_faces); free(M->vert_face_dir); free(M->vert_area);
     csr_free(&M->G); csr_free(&M->D); csr_free(&M->C0); csr_free(&M->Curl); csr_free(&M->D2);
     free(M);
@@ -611,6 +620,7 @@ orc_mesh *orc_mesh_from_arrays(int N, const double *node_sph, const int *friends
     M->cent_map = (double *)calloc((size_t)N * 12, sizeof(double));
     M->cv_area = (double *)calloc(N, sizeof(double));
     M->trig = (double *)calloc((size_t)N * 10, sizeof(double));
+    M->pbar2 = (double *)calloc((size_t)N * 2, sizeof(double));
     for (int i = 0; i < N; i++) {
         double lat1 = M->node_sph[i * 2], lon1 = M->node_sph[i * 2 + 1];
         for (int j = 0; j < 6; j++) {
@@ -637,6 +647,12 @@ orc_mesh *orc_mesh_from_arrays(int N, const double *node_sph, const int *friends
         t[0] = cos(lat1); t[1] = sin(lat1); t[2] = cos(lon1); t[3] = sin(lon1);
         t[4] = cos(2.0 * lat1); t[5] = sin(2.0 * lat1); t[6] = cos(2.0 * lon1); t[7] = sin(2.0 * lon1);
         t[8] = pow(cos(lat1), 2.0); t[9] = pow(sin(lat1), 2.0);
+        {   /* Pbar_20, Pbar_22 at the node (src/mesh.cpp:2193-2194, dead in v1.11) */
+            double P[6];
+            orc_plmbar(2, cos(ORC_PI * 0.5 - lat1), P);
+            M->pbar2[i * 2] = P[3];
+            M->pbar2[i * 2 + 1] = P[5];
+        }
     }
     int st = build_vertices(M);
     if (st == 0) st = assign_faces(M);
@@ -772,10 +788,12 @@ void orc_derive_time(double angvel_in, double dt_target, double *angvel, double 
 
 typedef struct {
     double radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt;
-    int potential;
+    int potential;        /* ORC_* (the reference's Potential values) */
     int init_load;
     int advection;        /* 1: the nonlinear branch (momentum advection, LSQ thickness flux) */
     int friction;         /* 0 LINEAR, 1 QUADRATIC (src/globals.cpp:232-234) */
+    double semimajor_axis;   /* "semimajor axis" (src/globals.cpp:82), m: PLANET's a2 */
+    int fourier_freq;        /* "fourier freq" (src/globals.cpp:130): GENERAL's q_max */
 } orc_params;
 
 /* ------------------------------------------------------------------------ */
@@ -787,8 +805,8 @@ typedef struct {
     orc_csr C;            /* Coriolis operator at the run's rotation rate */
     /* optional self-gravity / loading */
     int sh_lmax;          /* 0: off */
-    double *sh_B;         /* [K][N] analysis rows (LSQ pseudo-inverse rows), K=(L+1)^2 */
-    double *sh_Y;         /* [N][K] synthesis basis */
+    double *sh_R;         /* [K][K] Cholesky factor (lower) of the Gram matrix Y^T Y, K=(L+1)^2 */
+    double *sh_Y;         /* [K][N] basis rows Y_k(node) */
     double *sh_f;         /* [L+1] per-degree factor */
 } orc_solver;
 
@@ -804,7 +822,7 @@ void orc_solver_free(orc_solver *S)
 {
     if (!S) return;
     csr_free(&S->C);
-    free(S->sh_B); free(S->sh_Y); free(S->sh_f);
+    free(S->sh_R); free(S->sh_Y); free(S->sh_f);
     free(S);
 }
 
@@ -826,16 +844,45 @@ void orc_update_eta(const orc_solver *S, double *detadt, const double *v)
     csr_spmv(&S->M->D, v, S->p.h, detadt);
 }
 
-/* forcing, src/tidalPotentials.cpp:29-174 */
-void orc_forcing(const orc_solver *S, double *U, int type, double t)
+/* forcing, src/tidalPotentials.cpp:29-334: the potential of type `type` at time
+ * t with the caller's eccentricity and obliquity, as forcing(consts, grid,
+ * potential, type, time, ecc, obl).  Types without a case leave U untouched.
+ * GENERAL reads Pbar_20 and Pbar_22 at the nodes (src/tidalPotentials.cpp:238-
+ * 239); v1.11 never fills those arrays (their filler, CalcLegendreFuncs, is
+ * commented out at src/mesh.cpp:2154-2258, so they stay zero and the live
+ * reference's GENERAL potential is zero).  Here they hold the 4pi-normalised
+ * P20 and P22 that the dead code would assign (src/mesh.cpp:2193-2194). */
+void orc_forcing(const orc_solver *S, double *U, int type, double t, double ecc, double obl)
 {
     const orc_mesh *M = S->M;
-    double radius = S->p.radius, omega = S->p.angvel, ecc = S->p.ecc, obl = S->p.obliq;
+    double radius = S->p.radius, omega = S->p.angvel;
     double lr = S->p.love_reduct;
+    if (type != ORC_ECC && type != ORC_OBLIQ && type != ORC_OBLIQ_WEST && type != ORC_FULL2 &&
+        type != ORC_FULL && type != ORC_PLANET && type != ORC_GENERAL)
+        return;                                                   /* no case, or NONE */
     double cosM = cos(omega * t), sinM = sin(omega * t);
     double cos2M = cos(2 * omega * t);
     double cos3M = cos(3 * omega * t), cos4M = cos(4 * omega * t);
-    (void)cos2M;
+    /* PLANET (:176-225): Io-like perturber m2 at a1, this body at a2 = semimajor axis */
+    double pl_factor = 0.0, pl_p = 0.0, pl_cosphi = 0.0, pl_sinphi = 0.0;
+    if (type == ORC_PLANET) {
+        double m2 = 8.931938e+22, a1 = 421800000.0, a2 = S->p.semimajor_axis;
+        double n2 = omega, n1 = n2 * 2.0, nij = n1 - n2;
+        double cosnt = cos(nij * t), sinnt = sin(nij * t);
+        pl_p = pow(a1, 2.0) + pow(a2, 2.0) - 2. * a1 * a2 * cosnt;
+        pl_cosphi = (a1 - a2 * cosnt);
+        pl_sinphi = a2 * sinnt;
+        pl_factor = 0.5 * 6.67408e-11 * m2 * pow(radius / pl_p, 2.0) / sqrt(pl_p);
+    }
+    /* GENERAL (:227-281) */
+    double ge_cos = 0.0, ge_sin = 0.0;
+    const double a20 = -9.991062592506567e-05 * 2.0, a22 = 0.0012049514054640862 * 2.0,
+                 b22 = -0.0012017622891820471 * 2.0;
+    if (type == ORC_GENERAL) {
+        double n2 = omega, n1 = n2 * 2.0, nij = n1 - n2;
+        ge_cos = cos((double)S->p.fourier_freq * nij * t);
+        ge_sin = sin((double)S->p.fourier_freq * nij * t);
+    }
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < M->N; i++) {
         const double *tr = &M->trig[i * 10];
@@ -844,41 +891,52 @@ void orc_forcing(const orc_solver *S, double *U, int type, double t)
         double cosSqLat = tr[8], sinSqLat = tr[9];
         double factor, factor2;
         switch (type) {
-        case ORC_ECC:
+        case ORC_ECC:                                                 /* :82-101 */
             factor = 0.75 * lr * pow(omega, 2.0) * pow(radius, 2.0) * ecc;
             U[i] = factor * ((1. - 3. * sinSqLat) * cosM + cosSqLat * (3. * cosM * cos2Lon + 4. * sinM * sin2Lon));
             break;
-        case ORC_OBLIQ:
+        case ORC_OBLIQ:                                               /* :104-116 */
             factor = -3. / 2. * lr * pow(omega, 2.0) * pow(radius, 2.0) * obl;
             U[i] = factor * cosM * sin2Lat * cosLon;
             break;
-        case ORC_OBLIQ_WEST:
+        case ORC_OBLIQ_WEST:                                          /* :118-131 */
             factor = 0.5 * lr * pow(omega, 2.0) * pow(radius, 2.0) * obl;
             U[i] = 3 * factor * sinLat * cosLat * (cosLon * cosM - sinLon * sinM);
             break;
-        case ORC_FULL:
+        case ORC_FULL:                                                /* :158-174 */
             factor = 0.75 * lr * pow(omega, 2.0) * pow(radius, 2.0) * ecc;
             factor2 = -3. / 2. * lr * pow(omega, 2.0) * pow(radius, 2.0) * obl;
             U[i] = factor * ((1 - 3 * sinSqLat) * cosM + cosSqLat * (3 * cosM * cos2Lon + 4 * sinM * sin2Lon))
                    + factor2 * cosM * sin2Lat * cosLon;
             break;
-        case ORC_FULL2: {
-            double c2M = cos(2 * omega * t);
+        case ORC_FULL2: {                                             /* :133-156 */
             factor = 1 / 32. * lr * pow(omega, 2.0) * pow(radius, 2.0);
             double T1, T2, T3;
-            T1 = 3. * ecc * (4. - 7. * obl * obl) * cosM + 6 * (obl * obl + ecc * ecc * (3 - 7 * obl * obl)) * c2M;
+            T1 = 3. * ecc * (4. - 7. * obl * obl) * cosM + 6 * (obl * obl + ecc * ecc * (3 - 7 * obl * obl)) * cos2M;
             T1 += 3 * ecc * obl * obl * (7 * cos3M + 17 * ecc * cos4M);
             T1 *= -(1 - 3 * cos2Lat);
-            T2 = (4 + 15 * ecc * ecc + 20 * ecc * cosM + 43 * ecc * ecc * c2M) * cosLon;
+            T2 = (4 + 15 * ecc * ecc + 20 * ecc * cosM + 43 * ecc * ecc * cos2M) * cosLon;
             T2 += 2 * ecc * (4 + 25 * ecc * cosM) * sinM * sinLon;
             T2 *= 24 * obl * cosLat * sinLat * sinM;
-            T3 = obl * obl * (2 + 3 * ecc * ecc + 6 * ecc * cosM + 9 * ecc * ecc * c2M) * (cosM * cosLon + sinM * sinLon);
-            T3 += -(obl * obl - 2) * ((6 * ecc * cosM + 17 * ecc * ecc * c2M) * cos2Lon + 2 * ecc * (4 + 17 * ecc * cosM) * sinM * sin2Lon);
+            T3 = obl * obl * (2 + 3 * ecc * ecc + 6 * ecc * cosM + 9 * ecc * ecc * cos2M) * (cosM * cosLon + sinM * sinLon);
+            T3 += -(obl * obl - 2) * ((6 * ecc * cosM + 17 * ecc * ecc * cos2M) * cos2Lon + 2 * ecc * (4 + 17 * ecc * cosM) * sinM * sin2Lon);
             T3 *= 6 * cosSqLat;
             U[i] = factor * (T1 + T2 + T3);
             break; }
-        default:
-            U[i] = 0.0;
+        case ORC_PLANET: {                                            /* :176-225 */
+            double cosgam = cosLat * (cosLon * pl_cosphi + sinLon * pl_sinphi);
+            U[i] = pl_factor * (3. * pow(cosgam, 2.0) - pl_p);
+            break; }
+        case ORC_GENERAL: {                                           /* :227-281 */
+            double U20 = 0.0, U22a = 0.0, U22b = 0.0;
+            U20 += (a20 * ge_cos);
+            U22a += (a22 * ge_cos);
+            U22b += (b22 * ge_sin);
+            U20 = (U20) * M->pbar2[i * 2];
+            U22a = (U22a) * M->pbar2[i * 2 + 1] * cos2Lon;
+            U22b = (U22b) * M->pbar2[i * 2 + 1] * sin2Lon;
+            U[i] = (U20 + U22a + U22b);
+            break; }
         }
     }
 }
@@ -1266,52 +1324,59 @@ void orc_plmbar(int L, double z, double *P)
  * k = l*l + 2m - (m>0) for cos, l*l + 2m for sin (m>0) */
 static int sh_col(int l, int m, int is_sin) { return l * l + (m == 0 ? 0 : 2 * m - 1 + is_sin); }
 
-static int cholesky_solve_inplace(double *A, int n, double *B, int nrhs)
-{   /* A (n x n, SPD) overwritten by its Cholesky factor; B (n x nrhs) solved in place */
+static int cholesky_factor(double *A, int n)
+{   /* A (n x n, SPD) overwritten by its lower Cholesky factor R, A = R R^T */
     for (int j = 0; j < n; j++) {
-        double d = A[j * n + j];
-        for (int k = 0; k < j; k++) d -= A[j * n + k] * A[j * n + k];
+        double d = A[(size_t)j * n + j];
+        for (int k = 0; k < j; k++) d -= A[(size_t)j * n + k] * A[(size_t)j * n + k];
         if (d <= 0.0) return -1;
         d = sqrt(d);
-        A[j * n + j] = d;
+        A[(size_t)j * n + j] = d;
+#pragma omp parallel for schedule(static)
         for (int i = j + 1; i < n; i++) {
-            double s = A[i * n + j];
-            for (int k = 0; k < j; k++) s -= A[i * n + k] * A[j * n + k];
-            A[i * n + j] = s / d;
-        }
-    }
-    for (int c = 0; c < nrhs; c++) {
-        for (int i = 0; i < n; i++) {           /* forward */
-            double s = B[i * nrhs + c];
-            for (int k = 0; k < i; k++) s -= A[i * n + k] * B[k * nrhs + c];
-            B[i * nrhs + c] = s / A[i * n + i];
-        }
-        for (int i = n - 1; i >= 0; i--) {      /* backward */
-            double s = B[i * nrhs + c];
-            for (int k = i + 1; k < n; k++) s -= A[k * n + i] * B[k * nrhs + c];
-            B[i * nrhs + c] = s / A[i * n + i];
+            double s = A[(size_t)i * n + j];
+            for (int k = 0; k < j; k++) s -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
+            A[(size_t)i * n + j] = s / d;
         }
     }
     return 0;
 }
 
-/* Real SH basis at the nodes, Y[i][k] = Pbar_lm(sin lat) * (cos m lon | sin m lon),
- * as the rows of sh_matrix in src/mesh.cpp:2219-2252 (with l = 0, 1 kept). */
+static void cholesky_solve(const double *R, int n, double *x)
+{   /* x <- (R R^T)^-1 x: forward then backward substitution */
+    for (int i = 0; i < n; i++) {
+        double s = x[i];
+        for (int k = 0; k < i; k++) s -= R[(size_t)i * n + k] * x[k];
+        x[i] = s / R[(size_t)i * n + i];
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        double s = x[i];
+        for (int k = i + 1; k < n; k++) s -= R[(size_t)k * n + i] * x[k];
+        x[i] = s / R[(size_t)i * n + i];
+    }
+}
+
+/* Real SH basis rows at the nodes, Y[k][i] = Pbar_lm(sin lat_i) * (cos m lon_i | sin m lon_i),
+ * the columns of sh_matrix in src/mesh.cpp:2219-2252 (with l = 0, 1 kept). */
 void orc_sh_basis(const orc_mesh *M, int L, double *Y)
 {
-    int K = (L + 1) * (L + 1);
-    double *P = (double *)malloc(sizeof(double) * (L + 1) * (L + 2) / 2);
-    for (int i = 0; i < M->N; i++) {
-        double lat = M->node_sph[i * 2], lon = M->node_sph[i * 2 + 1];
-        orc_plmbar(L, cos(ORC_PI * 0.5 - lat), P);
-        for (int l = 0; l <= L; l++)
-            for (int m = 0; m <= l; m++) {
-                double p = P[l * (l + 1) / 2 + m];
-                Y[(size_t)i * K + sh_col(l, m, 0)] = p * cos((double)m * lon);
-                if (m > 0) Y[(size_t)i * K + sh_col(l, m, 1)] = p * sin((double)m * lon);
-            }
+    int N = M->N;
+#pragma omp parallel
+    {
+        double *P = (double *)malloc(sizeof(double) * (L + 1) * (L + 2) / 2);
+#pragma omp for schedule(static)
+        for (int i = 0; i < N; i++) {
+            double lat = M->node_sph[i * 2], lon = M->node_sph[i * 2 + 1];
+            orc_plmbar(L, cos(ORC_PI * 0.5 - lat), P);
+            for (int l = 0; l <= L; l++)
+                for (int m = 0; m <= l; m++) {
+                    double p = P[l * (l + 1) / 2 + m];
+                    Y[(size_t)sh_col(l, m, 0) * N + i] = p * cos((double)m * lon);
+                    if (m > 0) Y[(size_t)sh_col(l, m, 1) * N + i] = p * sin((double)m * lon);
+                }
+        }
+        free(P);
     }
-    free(P);
 }
 
 /* Enable self-gravity/loading: U_eff = U + g * sum_{l=2..L} f_l * sum_m c_lm Y_lm,
@@ -1321,47 +1386,54 @@ int orc_solver_set_loading(orc_solver *S, int L, const double *factors)
 {
     const orc_mesh *M = S->M;
     int N = M->N, K = (L + 1) * (L + 1);
-    free(S->sh_B); free(S->sh_Y); free(S->sh_f);
+    free(S->sh_R); free(S->sh_Y); free(S->sh_f);
+    S->sh_R = S->sh_Y = S->sh_f = NULL;
     S->sh_lmax = 0;
     if (L <= 0) return 0;
     if (N < K) return -1;
     double *Y = (double *)malloc(sizeof(double) * (size_t)N * K);
+    if (!Y) return -3;
     orc_sh_basis(M, L, Y);
+    /* Gram matrix of the basis rows: each entry a dot product over the nodes in
+     * four interleaved partial sums (the setup's own order; setup only) */
     double *A = (double *)calloc((size_t)K * K, sizeof(double));
 #pragma omp parallel for schedule(dynamic)
     for (int a = 0; a < K; a++)
         for (int b = 0; b <= a; b++) {
-            double s = 0.0;
-            for (int i = 0; i < N; i++) s += Y[(size_t)i * K + a] * Y[(size_t)i * K + b];
-            A[a * K + b] = s;
+            const double *ya = &Y[(size_t)a * N], *yb = &Y[(size_t)b * N];
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            int i = 0;
+            for (; i + 3 < N; i += 4) {
+                s0 += ya[i] * yb[i]; s1 += ya[i + 1] * yb[i + 1];
+                s2 += ya[i + 2] * yb[i + 2]; s3 += ya[i + 3] * yb[i + 3];
+            }
+            for (; i < N; i++) s0 += ya[i] * yb[i];
+            A[(size_t)a * K + b] = (s0 + s1) + (s2 + s3);
         }
-    for (int a = 0; a < K; a++) for (int b = a + 1; b < K; b++) A[a * K + b] = A[b * K + a];
-    /* B = (Y^T Y)^-1 Y^T  stored [K][N] */
-    double *B = (double *)malloc(sizeof(double) * (size_t)K * N);
-    for (int a = 0; a < K; a++) for (int i = 0; i < N; i++) B[(size_t)a * N + i] = Y[(size_t)i * K + a];
-    if (cholesky_solve_inplace(A, K, B, N) != 0) { free(A); free(B); free(Y); return -2; }
-    free(A);
-    S->sh_B = B; S->sh_Y = Y;
+    for (int a = 0; a < K; a++) for (int b = a + 1; b < K; b++) A[(size_t)a * K + b] = A[(size_t)b * K + a];
+    if (cholesky_factor(A, K) != 0) { free(A); free(Y); return -2; }
+    S->sh_R = A; S->sh_Y = Y;
     S->sh_f = (double *)malloc(sizeof(double) * (L + 1));
     memcpy(S->sh_f, factors, sizeof(double) * (L + 1));
     S->sh_lmax = L;
     return 0;
 }
 
-/* coefficients c[K] of eta (LSQ), c = B eta */
+/* coefficients c[K] of eta (LSQ): t = Y^T eta, then c = (Y^T Y)^-1 t */
 void orc_sh_analysis(const orc_solver *S, const double *eta, double *c)
 {
     int N = S->M->N, K = (S->sh_lmax + 1) * (S->sh_lmax + 1);
 #pragma omp parallel for schedule(static)
     for (int a = 0; a < K; a++) {
         double s = 0.0;
-        const double *b = &S->sh_B[(size_t)a * N];
-        for (int i = 0; i < N; i++) s += b[i] * eta[i];
+        const double *y = &S->sh_Y[(size_t)a * N];
+        for (int i = 0; i < N; i++) s += y[i] * eta[i];
         c[a] = s;
     }
+    cholesky_solve(S->sh_R, K, c);
 }
 
-/* U[i] += g * sum_{l>=2} f_l c_lm Y_lm(i) */
+/* U[i] += g * sum_{l>=2} f_l c_lm Y_lm(i), each node's sum in ascending harmonic order */
 void orc_sh_add_loading(const orc_solver *S, const double *eta, double *U)
 {
     int L = S->sh_lmax, N = S->M->N, K = (L + 1) * (L + 1);
@@ -1369,12 +1441,18 @@ void orc_sh_add_loading(const orc_solver *S, const double *eta, double *U)
     orc_sh_analysis(S, eta, c);
     for (int l = 0; l <= L; l++)
         for (int k = l * l; k < (l + 1) * (l + 1); k++) c[k] = (l >= 2) ? c[k] * S->sh_f[l] : 0.0;
+    const int B = 256;
 #pragma omp parallel for schedule(static)
-    for (int i = 0; i < N; i++) {
-        double s = 0.0;
-        const double *y = &S->sh_Y[(size_t)i * K];
-        for (int k = 4; k < K; k++) s += y[k] * c[k];
-        U[i] += S->p.g * s;
+    for (int i0 = 0; i0 < N; i0 += B) {
+        double s[256];
+        int n = N - i0 < B ? N - i0 : B;
+        for (int q = 0; q < n; q++) s[q] = 0.0;
+        for (int k = 4; k < K; k++) {
+            const double *y = &S->sh_Y[(size_t)k * N + i0];
+            double ck = c[k];
+            for (int q = 0; q < n; q++) s[q] += y[q] * ck;
+        }
+        for (int q = 0; q < n; q++) U[i0 + q] += S->p.g * s[q];
     }
     free(c);
 }
@@ -1461,7 +1539,7 @@ double orc_sim_step(orc_sim *X)
         orc_update_momentum(S, X->dv0, X->v, X->eta);                  /* :213 */
     }
     for (int i = 0; i < E; ++i) X->dvdt[i * 3] = X->dv0[i];              /* :215 */
-    orc_forcing(S, X->U, S->p.potential, X->time + dt);                  /* :218 */
+    orc_forcing(S, X->U, S->p.potential, X->time + dt, S->p.ecc, S->p.obliq);   /* :218 */
     if (S->sh_lmax > 0) orc_sh_add_loading(S, X->eta, X->U);
     /* drag_term = Ldrag*v + G*U (:219); Ldrag is the diagonal -alpha */
     csr_spmv(&M->G, X->U, 1.0, X->tmp);
@@ -1497,3 +1575,199 @@ int orc_sim_run(orc_sim *X, int nsteps, double *power)
 
 double orc_sim_power(const orc_sim *X) { return X->power; }
 void orc_sim_energy_field(const orc_sim *X, double *e) { memcpy(e, X->ediss, sizeof(double) * X->S->M->E); }
+
+/* ------------------------------------------------------------------------ */
+/* Icosahedral grid in the reference's grid-file format (test infrastructure: */
+/* the CPU baseline's own copy of the benchmark grids)                        */
+/* ------------------------------------------------------------------------ */
+/* The grid is defined by: a regular icosahedron with vertices at the poles
+ * and at latitude +-atan(1/2) (longitudes 72 k and 72 k + 36 degrees), each
+ * triangle split into four through its edge midpoints, level times, every
+ * new vertex the normalised sum of its edge's end points.  Its Voronoi cells
+ * are what the reference reads (src/mesh.cpp:4016-4089): per node its
+ * friends in clockwise order as seen from outside the sphere, and per friend
+ * j the spherical circumcentre of the triangle (node, friend j, friend j+1).
+ * The node numbering here is the order of creation (12 icosahedron vertices,
+ * then each level's midpoints); any numbering describes the same mesh. */
+typedef struct { double x, y, z; } orc_v3;
+
+static orc_v3 v3_unit(orc_v3 a)
+{
+    double n = sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    orc_v3 r = {a.x / n, a.y / n, a.z / n};
+    return r;
+}
+
+typedef struct { long long *key; int *val; size_t cap; } orc_edge_map;
+
+static int edge_midpoint(orc_edge_map *h, orc_v3 *pos, int *npos, int a, int b)
+{
+    long long lo = a < b ? a : b, hi = a < b ? b : a;
+    long long key = (lo << 32) | hi;
+    size_t slot = (size_t)((unsigned long long)key * 0x9E3779B97F4A7C15ull >> 17) & (h->cap - 1);
+    while (h->key[slot] != -1) {
+        if (h->key[slot] == key) return h->val[slot];
+        slot = (slot + 1) & (h->cap - 1);
+    }
+    orc_v3 s = {pos[a].x + pos[b].x, pos[a].y + pos[b].y, pos[a].z + pos[b].z};
+    int id = (*npos)++;
+    pos[id] = v3_unit(s);
+    h->key[slot] = key;
+    h->val[slot] = id;
+    return id;
+}
+
+static void deg_latlon(orc_v3 p, double *lat, double *lon)
+{
+    *lat = atan2(p.z, sqrt(p.x * p.x + p.y * p.y)) * 180.0 / ORC_PI;
+    *lon = atan2(p.y, p.x) * 180.0 / ORC_PI;
+    if (*lon < 0.0) *lon += 360.0;
+    if (*lon >= 360.0) *lon -= 360.0;
+}
+
+typedef struct { double ang; int node; } orc_nbr_ang;
+
+static int ang_desc(const void *a, const void *b)
+{
+    double x = ((const orc_nbr_ang *)a)->ang, y = ((const orc_nbr_ang *)b)->ang;
+    return x < y ? 1 : (x > y ? -1 : 0);
+}
+
+int orc_generate_grid_file(int level, const char *path)
+{
+    if (level < 0 || level > 10) return -1;
+    long long N = 10ll * (1ll << (2 * level)) + 2, T = 20ll * (1ll << (2 * level));
+    orc_v3 *pos = (orc_v3 *)malloc(sizeof(orc_v3) * N);
+    int *tri = (int *)malloc(sizeof(int) * 3 * T), *tri2 = (int *)malloc(sizeof(int) * 3 * T);
+    orc_edge_map h;
+    h.cap = 1;
+    while (h.cap < (size_t)(4 * N)) h.cap <<= 1;
+    h.key = (long long *)malloc(sizeof(long long) * h.cap);
+    h.val = (int *)malloc(sizeof(int) * h.cap);
+    if (!pos || !tri || !tri2 || !h.key || !h.val) { free(pos); free(tri); free(tri2); free(h.key); free(h.val); return -2; }
+    memset(h.key, 0xff, sizeof(long long) * h.cap);
+    const double pi = 3.14159265358979323846, lat0 = atan(0.5);
+    int npos = 0;
+    pos[npos++] = (orc_v3){0.0, 0.0, 1.0};
+    for (int k = 0; k < 5; k++) {
+        double lon = 2.0 * pi * k / 5.0;
+        pos[npos++] = (orc_v3){cos(lat0) * cos(lon), cos(lat0) * sin(lon), sin(lat0)};
+    }
+    for (int k = 0; k < 5; k++) {
+        double lon = 2.0 * pi * k / 5.0 + pi / 5.0;
+        pos[npos++] = (orc_v3){cos(lat0) * cos(lon), cos(lat0) * sin(lon), -sin(lat0)};
+    }
+    pos[npos++] = (orc_v3){0.0, 0.0, -1.0};
+    long long nt = 0;
+    for (int k = 0; k < 5; k++) {
+        int u0 = 1 + k, u1 = 1 + (k + 1) % 5, l0 = 6 + k, l1 = 6 + (k + 1) % 5;
+        int base[4][3] = {{0, u0, u1}, {u0, l0, u1}, {u1, l0, l1}, {11, l1, l0}};
+        for (int q = 0; q < 4; q++, nt++)
+            for (int c = 0; c < 3; c++) tri[3 * nt + c] = base[q][c];
+    }
+    for (int lv = 0; lv < level; lv++) {           /* one level of 4-way splits */
+        long long nn = 0;
+        for (long long t = 0; t < nt; t++) {
+            int a = tri[3 * t], b = tri[3 * t + 1], c = tri[3 * t + 2];
+            int ab = edge_midpoint(&h, pos, &npos, a, b);
+            int bc = edge_midpoint(&h, pos, &npos, b, c);
+            int ca = edge_midpoint(&h, pos, &npos, c, a);
+            int kids[4][3] = {{a, ab, ca}, {ab, bc, ca}, {ab, b, bc}, {ca, bc, c}};
+            for (int q = 0; q < 4; q++, nn++)
+                for (int e = 0; e < 3; e++) tri2[3 * nn + e] = kids[q][e];
+        }
+        int *sw = tri; tri = tri2; tri2 = sw;
+        nt = nn;
+    }
+    free(h.key); free(h.val); free(tri2);
+    int st = 0;
+    if (npos != N || nt != T) st = -3;
+    /* node -> incident triangles */
+    int *start = (int *)calloc((size_t)N + 1, sizeof(int)), *inc = (int *)malloc(sizeof(int) * 3 * T);
+    int *fill = (int *)calloc((size_t)N, sizeof(int));
+    orc_v3 *cc = (orc_v3 *)malloc(sizeof(orc_v3) * T);
+    if (!start || !inc || !fill || !cc) st = -2;
+    FILE *fp = st == 0 ? fopen(path, "w") : NULL;
+    if (st == 0 && !fp) st = -4;
+    if (st == 0) {
+        for (long long t = 0; t < 3 * T; t++) start[tri[t] + 1]++;
+        for (long long i = 0; i < N; i++) start[i + 1] += start[i];
+        for (long long t = 0; t < T; t++)
+            for (int q = 0; q < 3; q++) { int v = tri[3 * t + q]; inc[start[v] + fill[v]++] = (int)t; }
+        /* circumcentre direction of each triangle: (b - a) x (c - a), outward */
+        for (long long t = 0; t < T; t++) {
+            orc_v3 a = pos[tri[3 * t]], b = pos[tri[3 * t + 1]], c = pos[tri[3 * t + 2]];
+            orc_v3 u = {b.x - a.x, b.y - a.y, b.z - a.z}, w = {c.x - a.x, c.y - a.y, c.z - a.z};
+            orc_v3 n = {u.y * w.z - u.z * w.y, u.z * w.x - u.x * w.z, u.x * w.y - u.y * w.x};
+            if (n.x * (a.x + b.x + c.x) + n.y * (a.y + b.y + c.y) + n.z * (a.z + b.z + c.z) < 0) {
+                n.x = -n.x; n.y = -n.y; n.z = -n.z;
+            }
+            cc[t] = v3_unit(n);
+        }
+        fprintf(fp, "ID    NODE LAT     NODE LON     FRIENDS LIST                           CENTROID COORD LIST \n");
+        for (long long i = 0; i < N && st == 0; i++) {
+            orc_v3 p = pos[i];
+            int nb[6], k = 0;
+            for (int q = start[i]; q < start[i + 1]; q++) {
+                const int *tv = &tri[3 * (size_t)inc[q]];
+                for (int c = 0; c < 3; c++) {
+                    int v = tv[c], seen = (v == (int)i);
+                    for (int j = 0; j < k && !seen; j++) seen = nb[j] == v;
+                    if (!seen) { if (k == 6) { st = -5; break; } nb[k++] = v; }
+                }
+            }
+            if (st != 0 || (k != 5 && k != 6)) { st = -5; break; }
+            /* clockwise seen from outside: descending angle in the local east/north plane */
+            double lr = atan2(p.y, p.x);
+            orc_v3 east = {-sin(lr), cos(lr), 0.0};
+            orc_v3 north = {p.y * east.z - p.z * east.y, p.z * east.x - p.x * east.z, p.x * east.y - p.y * east.x};
+            orc_nbr_ang ang[6];
+            for (int j = 0; j < k; j++) {
+                orc_v3 d = {pos[nb[j]].x - p.x, pos[nb[j]].y - p.y, pos[nb[j]].z - p.z};
+                ang[j].ang = atan2(d.x * north.x + d.y * north.y + d.z * north.z, d.x * east.x + d.y * east.y + d.z * east.z);
+                ang[j].node = nb[j];
+            }
+            qsort(ang, k, sizeof(orc_nbr_ang), ang_desc);
+            double lat, lon;
+            deg_latlon(p, &lat, &lon);
+            fprintf(fp, "%-5lld %.16f %.16f {", i, lat, lon);
+            for (int j = 0; j < 6; j++) fprintf(fp, "%5d%s", j < k ? ang[j].node : -1, j < 5 ? ", " : "}, {");
+            for (int j = 0; j < 6; j++) {
+                double clat = -1.0, clon = -1.0;
+                if (j < k) {
+                    int fa = ang[j].node, fb = ang[(j + 1) % k].node, found = -1;
+                    for (int q = start[i]; q < start[i + 1] && found < 0; q++) {
+                        const int *tv = &tri[3 * (size_t)inc[q]];
+                        int ha = tv[0] == fa || tv[1] == fa || tv[2] == fa;
+                        int hb = tv[0] == fb || tv[1] == fb || tv[2] == fb;
+                        if (ha && hb) found = inc[q];
+                    }
+                    if (found < 0) { st = -6; break; }
+                    deg_latlon(cc[found], &clat, &clon);
+                }
+                fprintf(fp, "(%.16f, %.16f)%s", clat, clon, j < 5 ? ", " : "} \n");
+            }
+        }
+        if (fclose(fp) != 0 && st == 0) st = -4;
+    }
+    free(pos); free(tri); free(start); free(inc); free(fill); free(cc);
+    return st;
+}
+
+/* FREE_LOADING degree factors, src/boundaryConditions.cpp:29-76: loading Love
+ * numbers of a uniform elastic body (rigidity 40 GPa, bulk density
+ * 1609.22 kg/m^3, ocean 1000 kg/m^3), gamma_l = (1 + k_l - h_l) 3 rho_o /
+ * ((2l+1) rho_b), for l = 0..lmax in the reference's loop order and form. */
+void orc_loading_factors(double g, double r, int lmax, double *out)
+{
+    double ocean_den = 1000.0, bulk_den = 1609.22, rig = 40e9;
+    for (int l = 0; l < lmax + 1; l++) {
+        double eff_rig = (double)(2 * l * l + 4 * l + 3);
+        eff_rig /= (double)l;
+        eff_rig *= rig / (bulk_den * g * r);
+        double k_l = -(1.0 / (1.0 + eff_rig));
+        double h_l = -(1.0 / (1.0 + eff_rig)) * (2.0 * (double)l + 1.0) / 3.0;
+        out[l] = (1.0 + k_l - h_l);
+        out[l] *= 3. * ocean_den / ((2. * (double)l + 1.0) * bulk_den);
+    }
+}

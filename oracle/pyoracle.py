@@ -19,14 +19,16 @@ _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
 _V = C.c_void_p
 
-ECC, OBLIQ, OBLIQ_WEST, FULL, FULL2, NONE = 1, 2, 3, 4, 5, 0
+# forcing types: the values of the reference's enum Potential (include/globals.h:60-76)
+(OBLIQ, OBLIQ_WEST, OBLIQ_EAST, ECC_RAD, ECC_LIB, ECC, ECC_WEST, ECC_EAST, FULL, FULL2, TOTAL, ECC_W3, OBLIQ_W3,
+ PLANET, PLANET_OBL, GENERAL, NONE) = range(17)
 
 
 class OrcParams(C.Structure):
     _fields_ = [("radius", C.c_double), ("g", C.c_double), ("angvel", C.c_double), ("h", C.c_double),
                 ("alpha", C.c_double), ("ecc", C.c_double), ("obliq", C.c_double), ("love_reduct", C.c_double),
                 ("dt", C.c_double), ("potential", C.c_int), ("init_load", C.c_int), ("advection", C.c_int),
-                ("friction", C.c_int)]
+                ("friction", C.c_int), ("semimajor_axis", C.c_double), ("fourier_freq", C.c_int)]
 
 
 _lib = None
@@ -57,7 +59,9 @@ def lib() -> C.CDLL:
             "orc_solver_set_loading": ([_V, C.c_int, _D], C.c_int),
             "orc_update_momentum": ([_V, _D, _D, _D], None),
             "orc_update_eta": ([_V, _D, _D], None),
-            "orc_forcing": ([_V, _D, C.c_int, C.c_double], None),
+            "orc_forcing": ([_V, _D, C.c_int, C.c_double, C.c_double, C.c_double], None),
+            "orc_generate_grid_file": ([C.c_int, C.c_char_p], C.c_int),
+            "orc_loading_factors": ([C.c_double, C.c_double, C.c_int, _D], None),
             "orc_ab3": ([C.c_double, _D, _D, C.c_int, C.c_int, C.c_int], None),
             "orc_interpolate_velocity": ([_V, _D, _D], None),
             "orc_interpolate_cartesian": ([_V, _D, _D], None),
@@ -161,10 +165,11 @@ class OracleSolver:
     """FP64 restatement of the reference step (see odis_oracle.c)."""
 
     def __init__(self, mesh: OracleMesh, *, radius, g, angvel, h, alpha, ecc=0.0, obliq=0.0, love_reduct=1.0,
-                 dt, potential=ECC, init_load=0, sh_lmax=0, sh_factors=None, advection=0, friction=0):
+                 dt, potential=ECC, init_load=0, sh_lmax=0, sh_factors=None, advection=0, friction=0,
+                 semimajor_axis=1221.87e6, fourier_freq=1):
         self.mesh = mesh
         self.p = OrcParams(radius, g, angvel, h, alpha, ecc, obliq, love_reduct, dt, potential, init_load, advection,
-                           friction)
+                           friction, semimajor_axis, fourier_freq)
         self._s = C.c_void_p(lib().orc_solver_create(mesh._h, C.byref(self.p)))
         if sh_lmax:
             f = np.ascontiguousarray(sh_factors, np.float64)
@@ -173,6 +178,7 @@ class OracleSolver:
                 raise RuntimeError(f"oracle SH setup failed: {st}")
         self._x = C.c_void_p(lib().orc_sim_create(self._s))
         self.E, self.N = mesh.n_edges, mesh.n_cells
+        self.sh_lmax = int(sh_lmax)
 
     def updateMomentum(self, v, eta):
         out = np.zeros(self.E)
@@ -185,9 +191,12 @@ class OracleSolver:
         lib().orc_update_eta(self._s, _dp(out), _dp(np.ascontiguousarray(v, np.float64)))
         return out
 
-    def forcing(self, type_, t):
-        out = np.zeros(self.N)
-        lib().orc_forcing(self._s, _dp(out), int(type_), float(t))
+    def forcing(self, type_, t, ecc=None, obl=None, out=None):
+        """forcing(..., type, time, ecc, obl) (src/tidalPotentials.cpp:29-334); ecc/obl default to the
+        solver's.  Types without a case leave `out` (zeros if not given) untouched."""
+        out = np.zeros(self.N) if out is None else np.ascontiguousarray(out, np.float64)
+        lib().orc_forcing(self._s, _dp(out), int(type_), float(t), float(self.p.ecc if ecc is None else ecc),
+                          float(self.p.obliq if obl is None else obl))
         return out
 
     def integrateAB3scalar(self, s, ds_dt, it):
@@ -227,7 +236,11 @@ class OracleSolver:
         return avg, e
 
     def sh_analysis(self, eta):
-        raise NotImplementedError
+        """Least-squares SH coefficients c[(L+1)^2] of a node field (needs sh_lmax)."""
+        K = (self.sh_lmax + 1) ** 2
+        out = np.zeros(K)
+        lib().orc_sh_analysis(self._s, _dp(np.ascontiguousarray(eta, np.float64)), _dp(out))
+        return out
 
     def run(self, nsteps):
         out = np.zeros(nsteps)
@@ -254,6 +267,28 @@ class OracleSolver:
         if getattr(self, "_s", None) and self._s.value:
             _lib.orc_solver_free(self._s)
             self._s = C.c_void_p()
+
+
+def generate_grid_file(level: int, path: str | os.PathLike) -> None:
+    """Icosahedral grid of 10*4^level+2 cells in the reference's grid-file format, generated by the oracle
+    (its own numbering; the same mesh as the product's generator)."""
+    st = lib().orc_generate_grid_file(int(level), os.fsencode(str(path)))
+    if st != 0:
+        raise RuntimeError(f"oracle grid generation failed: {st}")
+
+
+def loading_factors(g: float, radius: float, lmax: int) -> np.ndarray:
+    """FREE_LOADING gamma_l, l = 0..lmax (src/boundaryConditions.cpp:29-76)."""
+    out = np.zeros(lmax + 1)
+    lib().orc_loading_factors(float(g), float(radius), int(lmax), _dp(out))
+    return out
+
+
+def benchmark_sh_factors(g: float, radius: float, lmax: int, seed: int = 1) -> np.ndarray:
+    """f_l * gamma_l with f_l ~ U[0.5, 1.5] (numpy default_rng(seed), degrees 2..lmax in order); entries 0, 1 zero."""
+    f = np.zeros(lmax + 1)
+    f[2:] = np.random.default_rng(seed).uniform(0.5, 1.5, lmax - 1)
+    return f * np.where(np.arange(lmax + 1) >= 2, loading_factors(g, radius, lmax), 0.0)
 
 
 def plmbar(L: int, z: float) -> np.ndarray:

@@ -11,7 +11,11 @@ import pytest
 ROOT = Path(__file__).resolve().parent.parent
 sys.path.insert(0, str(ROOT))
 
-REF_INPUT = Path("/root/reference/input_files")   # present only where the reference is mounted
+# A GeodesicODIS checkout (its shipped grids and input.in serve as fixtures), named by the
+# environment variable ODIS_REFERENCE_ROOT; the tests that read it skip when it is not set.
+REF_ROOT = Path(os.environ["ODIS_REFERENCE_ROOT"]) if os.environ.get("ODIS_REFERENCE_ROOT") else None
+REF_INPUT = (REF_ROOT / "input_files") if REF_ROOT else Path("__no_reference_checkout__")
+REF_SKIP = "set ODIS_REFERENCE_ROOT to a GeodesicODIS checkout to run the tests on its shipped files"
 
 # Enceladus-like body of the benchmark configurations
 RADIUS = 252.1e3
@@ -59,7 +63,7 @@ def config0_params(**over):
     from oracle import pyoracle as O
     angvel, P, dt, n = O.derive_time(ANGVEL_IN, 59.197)
     p = dict(radius=RADIUS, g=GRAV, angvel=angvel, h=1e4, alpha=1e-5, ecc=0.0047, obliq=0.0, love_reduct=1.0,
-             dt=dt, potential=1, init_load=0)
+             dt=dt, potential=O.ECC, init_load=0)
     p.update(over)
     return p
 

@@ -49,7 +49,7 @@ def test_closed_form_matches_oracle(grid_dir, level, alpha):
 
 def test_closed_form_only_for_obliq_west(grid_dir):
     import geodesicodis_gb300 as g
-    p, _ = _params(potential=1)
+    p, _ = _params(potential=g.POT_ECC)
     with pytest.raises(g.OdisError) as ei:
         g.analytical_state(g.make_params(**p), g.Mesh.from_file(grid_dir / "grid_2.txt", RADIUS))
     assert ei.value.code == g.ERR_ARG

@@ -90,9 +90,10 @@ def test_input_in_bad_enum_and_missing_file(built, tmp_path):
 def test_reference_input_in_parses(built):
     """The reference's own input.in (OBLIQ_WEST, advection true) parses with its documented values."""
     import geodesicodis_gb300 as g
-    src = Path("/root/reference/input.in")
-    if not src.exists():
-        pytest.skip("reference not mounted")
+    from conftest import REF_ROOT, REF_SKIP
+    if REF_ROOT is None or not (REF_ROOT / "input.in").exists():
+        pytest.skip(REF_SKIP)
+    src = REF_ROOT / "input.in"
     inp = g.read_input(src)
     assert inp.params.potential == g.POT_OBLIQ_WEST
     assert inp.advection == 1 and inp.params.advection == 1 and inp.grid_level == 6
@@ -106,3 +107,30 @@ def test_derive_time_rejects_bad_args(built):
         g.derive_time(-1.0, 10.0)
     a, P, dt, n = g.derive_time(ANGVEL_IN, 29.5985)
     assert n == 4000 and dt == P / 4000
+
+
+@pytest.mark.gpu
+def test_forcing_takes_the_reference_enum(tmp_path, built):
+    """odis_forcing bound with plain ctypes, called as the reference's time loop calls forcing(): the type is
+    globals->tide_type, a value of enum Potential (include/globals.h:60-76: OBLIQ 0, OBLIQ_WEST 1, ECC 5,
+    FULL 8, FULL2 9), and the eccentricity and obliquity are explicit arguments."""
+    import geodesicodis_gb300 as g
+    from oracle import pyoracle as O
+    L = C.CDLL(str(g.LIB_PATH))
+    L.odis_forcing.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]
+    path = tmp_path / "grid_3.txt"
+    g.generate_grid_file(3, path)
+    angvel, P, dt, n = g.derive_time(ANGVEL_IN, 59.197)
+    sol = g.Solver(g.make_params(radius=252.1e3, g=0.113, angvel=angvel, h=1e4, alpha=1e-5, ecc=0.0,
+                                 obliq=0.0, dt=dt, potential=5), g.Mesh.from_file(path, 252.1e3))
+    orc = O.OracleSolver(O.OracleMesh(path, 252.1e3), radius=252.1e3, g=0.113, angvel=angvel, h=1e4,
+                         alpha=1e-5, dt=dt)
+    for tide_type in (5, 0, 1, 8, 9):                 # ECC, OBLIQ, OBLIQ_WEST, FULL, FULL2
+        U = np.zeros(orc.N)
+        st = L.odis_forcing(sol._h, U.ctypes.data, tide_type, 4321.0, 0.0047, 0.0087, g.MEM_HOST)
+        assert st == 0
+        ref = orc.forcing(tide_type, 4321.0, 0.0047, 0.0087)
+        assert np.max(np.abs(ref)) > 0
+        assert np.max(np.abs(U - ref)) <= 1e-12 * np.max(np.abs(ref)), tide_type
+    assert L.odis_forcing(sol._h, U.ctypes.data, 17, 0.0, 0.0, 0.0, g.MEM_HOST) == g.ERR_ARG
+    sol.close()

@@ -43,11 +43,54 @@ def test_update_eta(level3):
     assert rel_err(gpu.updateEta(v), orc.updateEta(v)) < 1e-12
 
 
-@pytest.mark.parametrize("ptype", [1, 2, 3, 4])
+@pytest.mark.parametrize("ptype", list(range(17)))
 def test_forcing(level3, ptype):
+    """forcing(..., type, t, ecc, obl) for every value of the reference's Potential enum (0 OBLIQ ... 16 NONE):
+    the seven types with a case match the oracle; the others, and NONE, leave the array untouched."""
+    from oracle import pyoracle as O
     orc, gpu = level3
-    for t in (0.0, 1234.5, 7.7e5):
-        assert rel_err(gpu.forcing(ptype, t), orc.forcing(ptype, t)) < 1e-12
+    live = ptype in (O.ECC, O.OBLIQ, O.OBLIQ_WEST, O.FULL, O.FULL2, O.PLANET, O.GENERAL)
+    for t, ecc, obl in ((0.0, 0.0047, 0.01), (1234.5, 0.01, 0.002), (7.7e5, 0.003, 0.0087)):
+        sentinel = np.full(orc.N, 3.25)
+        a = gpu.forcing(ptype, t, ecc, obl, out=sentinel.copy())
+        b = orc.forcing(ptype, t, ecc, obl, out=sentinel.copy())
+        if live:
+            assert np.max(np.abs(b)) > 0 and not np.any(b == 3.25)
+            assert rel_err(a, b) < 1e-12
+        else:
+            np.testing.assert_array_equal(a, sentinel)
+            np.testing.assert_array_equal(b, sentinel)
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (2, 1e-10), (1, 1e-4)])
+@pytest.mark.parametrize("ptype", ["FULL2", "PLANET", "GENERAL"])
+def test_nodal_forcing_time_loop(grid_dir, ptype, precision, tol):
+    """Forcing types evaluated at the nodes every step (several harmonics of the orbit, or another period):
+    the fused loop against the oracle over 1200 steps at level 3."""
+    from oracle import pyoracle as O
+    over = dict(potential=getattr(O, ptype), obliq=0.01, fourier_freq=2, semimajor_axis=1221.87e6)
+    orc, gpu = _pair(grid_dir / "grid_3.txt", precision=precision, **over)
+    po, pg = orc.run(1200), gpu.run(1200)
+    _, vo, eo, _, _ = orc.get_state()
+    _, vg, eg, _, _ = gpu.get_state()
+    assert po[-1] > 0
+    assert rel_err(pg[-600:], po[-600:]) < tol
+    if precision != 1:
+        assert rel_err(eg, eo) < tol and rel_err(vg, vo) < tol
+
+
+def test_nodal_forcing_with_self_gravity(grid_dir):
+    """FULL2 added to the self-gravity potential in the same node buffer (FP64 and DF64)."""
+    import geodesicodis_gb300 as g
+    from oracle import pyoracle as O
+    fac = g.benchmark_sh_factors(0.113, RADIUS, 8, seed=1)
+    for prec in (0, 2):
+        orc, gpu = _pair(grid_dir / "grid_3.txt", precision=prec, potential=O.FULL2, obliq=0.01, sh_lmax=8,
+                         sh_factors=fac)
+        po, pg = orc.run(1000), gpu.run(1000)
+        _, vo, eo, _, _ = orc.get_state()
+        _, vg, eg, _, _ = gpu.get_state()
+        assert rel_err(pg, po) < 1e-10 and rel_err(eg, eo) < 1e-10 and rel_err(vg, vo) < 1e-10
 
 
 @pytest.mark.parametrize("it", [0, 1, 2, 7])

@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import REF_INPUT, ref_grid
+from conftest import REF_INPUT, REF_SKIP, ref_grid
 
 
 def read_grid(path):
@@ -57,7 +57,7 @@ def test_clockwise_and_circumcentres(grid_dir, level):
             assert max(d) - min(d) < 1e-12
 
 
-@pytest.mark.skipif(not REF_INPUT.exists(), reason="reference grids not mounted")
+@pytest.mark.skipif(not REF_INPUT.exists(), reason=REF_SKIP)
 @pytest.mark.parametrize("level", [2, 3, 4])
 def test_same_layout_as_reference_files(grid_dir, level):
     """Generated and shipped grids agree in size, pentagon count and orientation convention."""
@@ -74,3 +74,43 @@ def test_same_layout_as_reference_files(grid_dir, level):
         P = xyz(lat, lon)
         return np.mean([np.arccos(np.clip(np.dot(P[i], P[fr[i, 0]]), -1, 1)) for i in range(len(lat))])
     assert abs(mean_spacing(lat, lon, fr) / mean_spacing(lat2, lon2, fr2) - 1) < 0.05
+
+
+def _parse_grid(path):
+    """(node (lat, lon) strings, friends [N][6], centroids [N][6][2]) of a grid file."""
+    import re
+    names, fr, cen = [], [], []
+    for line in open(path).read().splitlines()[1:]:
+        a = line.split("{")
+        head = a[0].split()
+        names.append((head[1], head[2]))
+        fr.append([int(x) for x in a[1].split("}")[0].split(",")])
+        cen.append([(float(x), float(y)) for x, y in re.findall(r"\(([^,]+), ([^)]+)\)", a[2])])
+    return names, np.array(fr), np.array(cen)
+
+
+@pytest.mark.parametrize("level", [0, 2, 4, 5])
+def test_oracle_generator_builds_the_same_mesh(grid_dir, tmp_path, level):
+    """The oracle's own icosahedral generator (creation-order numbering) and the product's (depth-first
+    numbering) describe the same mesh: identical node positions, friend cycles and circumcentres, bit for bit
+    once the nodes are matched."""
+    from oracle import pyoracle as O
+    O.generate_grid_file(level, tmp_path / "o.txt")
+    no, fo, co = _parse_grid(tmp_path / "o.txt")
+    npn, fp, cp = _parse_grid(grid_dir / f"grid_{level}.txt")
+    assert len(no) == len(npn) == 10 * 4 ** level + 2
+    where = {n: i for i, n in enumerate(npn)}
+    perm = np.array([where[n] for n in no])            # oracle node -> product node
+    assert len(set(perm.tolist())) == len(no)
+    mapped = np.where(fo >= 0, perm[np.maximum(fo, 0)], -1)
+    np.testing.assert_array_equal(mapped, fp[perm])
+    np.testing.assert_array_equal(co, cp[perm])
+
+
+def test_oracle_loading_factors_match_product(built):
+    import geodesicodis_gb300 as g
+    from oracle import pyoracle as O
+    a, b = O.loading_factors(0.113, 252.1e3, 32), g.loading_factors(0.113, 252.1e3, 32)
+    np.testing.assert_array_equal(a[1:], b[1:])        # l = 0 is unused (the reference divides by l)
+    np.testing.assert_array_equal(O.benchmark_sh_factors(0.113, 252.1e3, 16, 1),
+                                  g.benchmark_sh_factors(0.113, 252.1e3, 16, 1))

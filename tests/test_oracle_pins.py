@@ -10,7 +10,7 @@ self-gravity term (SHTOOLS 4pi normalisation, csphase=-1)."""
 import numpy as np
 import pytest
 
-from conftest import ANGVEL_IN, RADIUS, REF_INPUT, ref_grid
+from conftest import ANGVEL_IN, RADIUS, REF_INPUT, REF_SKIP, ref_grid
 
 
 def spmv(csr, x):
@@ -61,7 +61,7 @@ def _convergence(paths, min_ratio):
     return errs
 
 
-@pytest.mark.skipif(not REF_INPUT.exists(), reason="reference grids not mounted")
+@pytest.mark.skipif(not REF_INPUT.exists(), reason=REF_SKIP)
 def test_operator_convergence_reference_grids(built):
     # the shipped (tweaked) grids: second order for G and D, close to it for C
     _convergence([ref_grid(k) for k in (2, 3, 4, 5)], (3.5, 3.5, 2.5))
@@ -126,10 +126,10 @@ def test_sh_lsq_round_trip(grid_dir):
     m = O.OracleMesh(grid_dir / "grid_3.txt", RADIUS)
     s = O.OracleSolver(m, radius=RADIUS, g=0.113, angvel=1e-5, h=1e3, alpha=1e-6, dt=10.0,
                        sh_lmax=L, sh_factors=np.ones(L + 1))
-    Y = np.zeros((m.n_cells, K))
+    Y = np.zeros((K, m.n_cells))                     # basis rows Y_k(node)
     O.lib().orc_sh_basis(m._h, L, Y.ctypes.data_as(C.POINTER(C.c_double)))
     c = np.random.default_rng(0).standard_normal(K)
-    eta = Y @ c
+    eta = Y.T @ c
     out = np.zeros(K)
     O.lib().orc_sh_analysis(s._s, eta.ctypes.data_as(C.POINTER(C.c_double)), out.ctypes.data_as(C.POINTER(C.c_double)))
     np.testing.assert_allclose(out, c, atol=1e-10)
