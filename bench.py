@@ -8,11 +8,10 @@ loading factors gamma_l scaled per degree by f_l ~ U[0.5, 1.5] (seed 1).
 4200 steps per orbit (dt = 28.189 s): the specified 4000 puts the fastest
 gravity wave of the level-6 mesh at omega*dt = 0.566, beyond the 6/11 limit
 of the reference's forward-backward AB3 loop, and the run diverges.  The
-headline is the fastest method that meets the 1e-10 FP64 parity bar: ODIS_DF64
-(double-float arithmetic on the FP32 pipes, FP64-width storage).  The native
-FP64 method, the FP32-state variant and the runs without the self-gravity
-term are reported beside it, with their errors against FP64 after the same
-number of orbits from rest.
+headline (`value`, `e2e`) is the FP64 method, the reference's arithmetic.  The
+double-float method (ODIS_DF64, FP64-parity arithmetic on the FP32 pipes), the
+FP32-state variant and the runs without the self-gravity term are reported
+beside it, with their errors against FP64 after the same number of orbits.
 
 A bench "step" is one orbit of the time loop (4200 LTE steps); L2 is flushed
 (256 MB write) before every timed orbit.  Inputs are synthetic (the reference
@@ -22,7 +21,8 @@ has no dataset): the state starts from rest, forcing is the analytic tide.
 
 --impl reference times the reference algorithm's CPU implementation (the FP64
 C restatement in oracle/, built with OpenMP, all host cores) on bounded samples
-of the same workload.
+of the same workload; it loads only the oracle (its own grid generator and
+loading factors), never the product library.
 """
 from __future__ import annotations
 
@@ -54,6 +54,16 @@ def sh_factors(lmax: int, seed: int = 1) -> np.ndarray:
     return g.benchmark_sh_factors(GRAV, RADIUS, lmax, seed)
 
 
+def oracle_setup(O):
+    """The workload for the oracle alone: its own level-6 grid and loading factors (no product code)."""
+    angvel, P, dt, n = O.derive_time(ANGVEL_IN, DT_TARGET)
+    with tempfile.TemporaryDirectory() as d:
+        grid = os.path.join(d, f"grid_{LEVEL}.txt")
+        O.generate_grid_file(LEVEL, grid)
+        mesh = O.OracleMesh(grid, RADIUS)
+    return angvel, P, dt, n, mesh
+
+
 @contextlib.contextmanager
 def sh_path(tc):
     """ODIS_SH_TC around a context creation: "1" tensor-core SH transforms, "0" CUDA-core, None timed choice."""
@@ -70,11 +80,13 @@ def sh_path(tc):
                 os.environ["ODIS_SH_TC"] = old
 
 
-def workload_config(steps_per_orbit: int, n_cells: int, n_faces: int) -> dict:
+def workload_config(steps_per_orbit: int, n_cells: int, n_faces: int, world: int) -> dict:
+    """The workload, identical in both arms' lines."""
     return {"workload": f"LTE time loop, icosahedral level {LEVEL} ({n_cells} cells, {n_faces} faces), "
                         f"ECC tide + SH self-gravity l_max={LMAX}, one orbit = {steps_per_orbit} steps per bench step",
             "level": LEVEL, "cells": n_cells, "faces": n_faces, "steps_per_orbit": steps_per_orbit,
-            "sh_lmax": LMAX, "h_m": H, "alpha": ALPHA, "ecc": ECC,
+            "sh_lmax": LMAX, "h_m": H, "alpha": ALPHA, "ecc": ECC, "global_batch": world,
+            "parallelism": "single instance" if world == 1 else f"{world} independent replicas",
             "l2": "flushed (256 MB write) before each timed orbit; within an orbit the per-step working set "
                   "stays L2-resident as in the real run"}
 
@@ -139,15 +151,10 @@ def cpu_sample(n_steps: int, threads: int | None, with_sh: bool = True):
         ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(env_threads))
     except OSError:
         pass
-    angvel, P, dt, n = O.derive_time(ANGVEL_IN, DT_TARGET)
-    with tempfile.TemporaryDirectory() as d:
-        grid = os.path.join(d, f"grid_{LEVEL}.txt")
-        import geodesicodis_gb300 as g
-        g.generate_grid_file(LEVEL, grid)
-        mesh = O.OracleMesh(grid, RADIUS)
+    angvel, P, dt, n, mesh = oracle_setup(O)
     kw = dict(radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt, potential=O.ECC)
     if with_sh:
-        kw.update(sh_lmax=LMAX, sh_factors=sh_factors(LMAX))
+        kw.update(sh_lmax=LMAX, sh_factors=O.benchmark_sh_factors(GRAV, RADIUS, LMAX, 1))
     sol = O.OracleSolver(mesh, **kw)
     sol.run(2)
     t = time.perf_counter()
@@ -163,14 +170,9 @@ def run_reference(args) -> dict:
     threads = os.cpu_count()
     os.environ["OMP_NUM_THREADS"] = str(threads)
     from oracle import pyoracle as O
-    import geodesicodis_gb300 as g
-    angvel, P, dt, n = O.derive_time(ANGVEL_IN, DT_TARGET)
-    with tempfile.TemporaryDirectory() as d:
-        grid = os.path.join(d, f"grid_{LEVEL}.txt")
-        g.generate_grid_file(LEVEL, grid)
-        mesh = O.OracleMesh(grid, RADIUS)
+    angvel, P, dt, n, mesh = oracle_setup(O)
     sol = O.OracleSolver(mesh, radius=RADIUS, g=GRAV, angvel=angvel, h=H, alpha=ALPHA, ecc=ECC, dt=dt,
-                         potential=O.ECC, sh_lmax=LMAX, sh_factors=sh_factors(LMAX))
+                         potential=O.ECC, sh_lmax=LMAX, sh_factors=O.benchmark_sh_factors(GRAV, RADIUS, LMAX, 1))
     sample = args.ref_sample_steps
     for _ in range(args.warmup):
         sol.run(sample)
@@ -179,14 +181,13 @@ def run_reference(args) -> dict:
         sol.run(sample)
     el = time.perf_counter() - t
     value = mesh.n_cells * sample * args.steps / el
-    desc = (f"{sample} LTE steps of the level-6 FP64 + l_max=16 workload per bench step, "
-            f"oracle C restatement (the reference build needs Eigen/HDF5, absent), OpenMP {threads} threads")
+    desc = (f"{sample} LTE steps of the level-6 FP64 + l_max=16 workload per bench step (the CPU takes minutes "
+            f"per orbit), oracle C restatement (the reference build needs Eigen/HDF5, absent) with its own grid "
+            f"generator and loading factors, OpenMP {threads} threads")
     return {"metric": METRIC, "value": value, "unit": "cell-steps/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": workload_config(n, mesh.n_cells, mesh.n_edges) | {
-                "parallelism": "cpu-openmp", "ref_sample_steps": sample,
-                "bench_step": f"a {sample}-step sample of the orbit (the CPU takes minutes per orbit)"},
+            "config": workload_config(n, mesh.n_cells, mesh.n_edges, args.gpus),
             "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
                              "sample": desc},
             "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -224,6 +225,23 @@ def _replica_setup(cuda: bool = True):
     # host-side barriers and one scalar max per measurement: gloo over CPU tensors, no GPU collective
     D.init_process_group("gloo")
     return rank, world, D
+
+
+# FP64 instructions per face and per cell of the plain step (k_edge_step<double> / k_cell_step<double>,
+# counted from the source; an FMA, a multiply and an add each take one FP64 issue slot):
+#   face: TRiSK sum 10 FMA; |u|^2 and the dissipation 3; -g G eta + Coriolis 3; forcing gradient 2;
+#         drag 1; AB3 3; v update 2; block power sum 5 (the shuffle tree)          -> 29
+#         with self-gravity or nodal forcing, G (g usg) adds 3                      -> 32
+#   cell: divergence 6 FMA; AB3 3; eta update 1                                     -> 10
+FP64_INST_FACE, FP64_INST_FACE_SG, FP64_INST_CELL = 29, 32, 10
+
+
+def sh_fp64_inst(K: int, cells: int, L: int, tiles: int) -> float:
+    """FP64 instructions of one self-gravity step (analysis + synthesis) over the `cells` the basis covers:
+    each transform is K multiply-adds per cell (two per (l, m > 0), one per (l, 0)); the analysis adds its
+    trig products (4 per cell and tile; 2 with the full basis, counted as 4), the synthesis 4 per cell and
+    order; the pair, fold and K x K solve kernels are below 1 %."""
+    return 2.0 * K * cells + 4.0 * cells * tiles + 4.0 * cells * (L + 1)
 
 
 def run_ours(args) -> dict:
@@ -285,33 +303,48 @@ def run_ours(args) -> dict:
             barrier(collective)
         return total, launches
 
-    # headline: the FP64-parity double-float method (ODIS_DF64) on the level-6 + l_max=16 workload
+    # headline: the FP64 method (the reference's arithmetic) on the level-6 + l_max=16 workload; the
+    # end-to-end number is taken on the same context, so both describe the same kernels and tiles
     clocks = ClockSampler()
     clocks.start()
-    main_sol = solver(g.DF64, LMAX)
+    main_sol = solver(g.FP64, LMAX)
     tiles = dict(zip(("tile_l", "chunks", "lanes"), main_sol.sh_tiles()))
+    layout = main_sol.sh_layout()
     t_main, launches = timed_orbits(main_sol, args.steps, args.warmup)
     clk = clocks.stop()
-    main_sol.close()
     t_main = max_over_ranks(t_main)
     value = world * N * n * args.steps / t_main      # whole job: every replica ran the same orbits
-    e2e_value = run_e2e(g, solver, stream, flush, args, n, N, E, barrier, max_over_ranks, world)
+    e2e_value, h2d, d2h = run_e2e(main_sol, stream, flush, args, n, N, E, barrier, max_over_ranks, world)
     if rank != 0:
+        main_sol.close()
         barrier()
         return {}
+    ms = main_sol.profile_kernels(200)             # per-kernel-group device times of the headline method
+    main_sol.close()
 
     # the other methods, 1 untimed + kv timed orbits each from rest; final states kept for the error report
     kv = max(1, args.steps // 4)
-    results, finals = {"df64_sh16": value}, {}
-    for key, prec, lmax, tc, adv in (("df64_sh16", g.DF64, LMAX, None, 0), ("fp64_sh16", g.FP64, LMAX, None, 0),
+    results, finals, extra = {"fp64_sh16": value}, {}, {}
+    for key, prec, lmax, tc, adv in (("fp64_sh16", g.FP64, LMAX, None, 0), ("df64_sh16", g.DF64, LMAX, None, 0),
                                      ("fp32_sh16", g.FP32, LMAX, None, 0), ("fp32_sh16_tc", g.FP32, LMAX, "1", 0),
                                      ("df64_plain", g.DF64, 0, None, 0), ("fp64_plain", g.FP64, 0, None, 0),
                                      ("fp32_plain", g.FP32, 0, None, 0), ("fp64_advection", g.FP64, 0, None, 1),
                                      ("df64_advection", g.DF64, 0, None, 1)):
         s = solver(prec, lmax, tc, adv)
         t, _ = timed_orbits(s, kv, 1, collective=False)     # rank 0 only
-        if key != "df64_sh16":
+        if key != "fp64_sh16":
             results[key] = N * n * kv / t
+        if lmax:
+            extra[key] = {"sh_tiles": list(s.sh_tiles()), "sh_layout": s.sh_layout()}
+        if key == "df64_sh16":
+            # the double-float method end to end, on its own context as the headline
+            extra[key]["e2e"] = run_e2e(s, stream, flush, args, n, N, E, barrier, max_over_ranks, world,
+                                        collective=False)[0]
+            extra[key]["kernel_ms_per_launch"] = dict(zip(("face_step", "cell_step", "sh_self_gravity"),
+                                                          s.profile_kernels(200).tolist()))
+            s.set_state(0, np.zeros(E), np.zeros(N), np.zeros((E, 3)), np.zeros((N, 3)))
+            for _ in range(1 + kv):
+                s.run_device(n, None)
         _, v, eta, _, _ = s.get_state()
         # the last step's dissipated power from a 1-step run continues the same trajectory for all methods
         pw = s.run(1)
@@ -325,66 +358,80 @@ def run_ours(args) -> dict:
         errors[f"{key}_vs_{ref}"] = {"eta": _rel(ea, eb_), "velocity": _rel(va, vb), "power": abs(pa - pb) / abs(pb),
                                      "orbits": 1 + kv}
 
-    h2d = (E + N + 3 * E + 3 * N) * 8
-    d2h = (E + N + 3 * E + 3 * N) * 8 + n * 8
-
-    # per-kernel device times of the headline method (graphs of back-to-back launches, CUDA events)
-    prof = solver(g.DF64, LMAX)
-    prof.set_stream(stream.cuda_stream)
-    ms = prof.profile_kernels(200)
-    prof.close()
-    s_bytes = 8                                  # one double-float value = 8 bytes, as FP64
-    face_bytes = E * (19 * s_bytes + 48)
-    cell_bytes = N * (13 * s_bytes + 24)
-    K = (LMAX + 1) ** 2
-    sh_bytes = 2 * K * N * s_bytes + 2 * N * s_bytes
-    per_step = {"face_step": ms[0], "cell_step": ms[1], "sh_self_gravity": ms[2]}
-    dominant = max(per_step, key=per_step.get)
-    alg = {"face_step": face_bytes, "cell_step": cell_bytes, "sh_self_gravity": sh_bytes}[dominant]
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
+    fp64_tflops = g.measure_fp64_rate()          # FP64 FMA rate of this GPU, TFLOP/s
+    fp64_inst_rate = fp64_tflops * 1e12 / 2.0    # FP64 instructions per second (FMA = 2 flops, 1 slot)
+
+    # roofline of the dominant kernel group of the headline step
+    K = (LMAX + 1) ** 2
+    per_step = {"face_step": ms[0], "cell_step": ms[1], "sh_self_gravity": ms[2]}
+    dominant = max(per_step, key=per_step.get)
+    face_bytes = E * (19 * 8 + 48)
+    cell_bytes = N * (13 * 8 + 24)
+    # self-gravity: the stored basis read once per transform, plus the node vectors each kernel moves
+    # (half basis: pair kernel eta in, e/o out; analysis e/o in; synthesis usg out -> 4 N values)
+    sh_bytes = 2 * layout["basis_bytes"] + (4 if layout["half"] else 2) * N * 8
+    alg = {"face_step": face_bytes, "cell_step": cell_bytes, "sh_self_gravity": sh_bytes}[dominant]
     achieved = alg / (per_step[dominant] / 1e3) / 1e9
-    step_bytes = face_bytes + cell_bytes
+    ntiles = sum((LMAX - m) // max(1, tiles["tile_l"]) + 1 for m in range(LMAX + 1)) if tiles["tile_l"] else LMAX + 1
+    sh_inst = sh_fp64_inst(K, layout["cells"], LMAX, ntiles)
+    inst = {"face_step": E * FP64_INST_FACE_SG, "cell_step": N * FP64_INST_CELL, "sh_self_gravity": sh_inst}[dominant]
+    fp64_ach = inst * 2.0 / (per_step[dominant] / 1e3) / 1e12
     plain = {}
     for key in ("fp64_plain", "df64_plain", "fp32_plain"):
-        b = step_bytes if key != "fp32_plain" else E * (19 * 4 + 48) + N * (13 * 4 + 24)
+        b = face_bytes + cell_bytes if key != "fp32_plain" else E * (19 * 4 + 48) + N * (13 * 4 + 24)
         gbs = b * results[key] / N / 1e9
         plain[key] = {"achieved_gbs": gbs, "frac": gbs / peak, "bytes_per_step": b}
+    fp64_step_inst = E * FP64_INST_FACE + N * FP64_INST_CELL
+    plain["fp64_plain"]["fp64_pipe"] = {"fp64_instructions_per_step": fp64_step_inst,
+                                        "achieved_tflops": fp64_step_inst * 2 * results["fp64_plain"] / N / 1e12,
+                                        "peak_tflops": fp64_tflops,
+                                        "frac": fp64_step_inst * results["fp64_plain"] / N / fp64_inst_rate}
+    step_inst = E * FP64_INST_FACE_SG + N * FP64_INST_CELL + sh_inst
+    headline_fp64 = {"fp64_instructions_per_step": step_inst, "peak_tflops": fp64_tflops,
+                     "achieved_tflops": step_inst * 2 * value / world / N / 1e12,
+                     "frac": step_inst * value / world / N / fp64_inst_rate,
+                     "peak_source": "odis_measure_fp64_rate (FMA chains on every SM, this run)"}
 
     out = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_main / args.steps * 1e3, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "df64", "data": "synthetic",
-           "config": workload_config(n, N, E) | {"parallelism": "single-gpu" if world == 1 else f"{world} replicas",
-                                                 "global_batch": world,
-                                                 "method": "ODIS_DF64: FP64-parity (1e-10) double-float arithmetic",
-                                                 "sh_tiles_autotuned": tiles},
-           "variants_cell_steps_per_s": results,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": workload_config(n, N, E, world),
+           "method": "ODIS_FP64: the reference's FP64 arithmetic (parity 1e-10 against the FP64 oracle)",
+           "sh_tiles_autotuned": tiles, "sh_layout": layout,
+           "variants_cell_steps_per_s": results, "variants": extra,
            "nonlinear": {"cell_steps_per_s": results["df64_advection"],
                          "fp64_cell_steps_per_s": results["fp64_advection"],
                          "bytes_per_step": nonlinear_bytes(N, E, mesh.n_vertices),
                          "roofline_frac": {k: nonlinear_bytes(N, E, mesh.n_vertices) * results[k] / N / 1e9
                                            / peak
                                            for k in ("df64_advection", "fp64_advection")},
-                         "method": "ODIS_DF64 (FP64 parity), advection true: momentum advection + LSQ thickness "
-                                   "flux, 7 kernels per step, AB3 steps replayed from a 64-step CUDA graph",
+                         "method": "advection true: momentum advection + LSQ thickness flux, 7 kernels per step, "
+                                   "AB3 steps replayed from a 64-step CUDA graph",
                          "eta_gap_vs_linear": _rel(finals["fp64_advection"][1], finals["fp64_plain"][1]),
                          "power_gap_vs_linear": abs(finals["fp64_advection"][2] - finals["fp64_plain"][2])
                          / abs(finals["fp64_plain"][2])},
            "errors_vs_fp64": errors,
            "kernel_ms_per_launch": per_step,
            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": profiled_traffic(dominant),
+                        "frac": achieved / peak, "traffic": profiled_traffic(f"{dominant}_fp64"),
                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)" if peaks else "fallback 6800",
                         "algorithmic_bytes": alg,
-                        "note": "sh_self_gravity: Legendre and trig rows (2*K*N values) streamed twice per step; "
-                                "they stay L2-resident at level 6, and the kernel is FP32-pipe bound"
+                        "note": "sh_self_gravity: the stored basis (Legendre + trig rows of the cells it covers) "
+                                "read once per transform plus the node vectors; at level 6 the rows stay "
+                                "L2-resident between steps, and the FP64 kernels are FP64-issue bound (fp64_pipe)"
                                 if dominant == "sh_self_gravity" else ""},
+           "fp64_pipe": {"kernel": dominant, "fp64_instructions": inst, "achieved_tflops": fp64_ach,
+                         "peak_tflops": fp64_tflops, "frac": fp64_ach / fp64_tflops,
+                         "whole_step": headline_fp64},
            "plain_step_roofline": plain,
            "clocks": clk, "gpu_launches": launches * world,
            "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                    "d2h_bytes_per_step": d2h,
-                   "how": f"per orbit: odis_set_state from pinned host buffers, odis_run_steps({n}) with the "
-                          "power series copied to host, odis_get_state back to host; wall clock"}}
+                   "how": f"per orbit on the headline context: odis_set_state from pinned host buffers, "
+                          f"odis_run_steps({n}) with the power series copied to host, odis_get_state back to "
+                          "host; wall clock"}}
     if not args.no_sweep:
         out["sweep"] = run_sweep(args, results["fp64_plain"], peak)
     if not args.no_cpu_baseline:
@@ -402,24 +449,22 @@ def run_ours(args) -> dict:
     return out
 
 
-def run_e2e(g, solver, stream, flush, args, n, N, E, barrier, max_over_ranks, world) -> float:
-    """The headline orbits end to end through the C ABI with pinned host buffers: per orbit
+def run_e2e(sol, stream, flush, args, n, N, E, barrier, max_over_ranks, world, collective=True):
+    """Orbits end to end through the C ABI on an existing context, with pinned host buffers: per orbit
     odis_set_state from host, odis_run_steps with the power series copied to host, odis_get_state back;
-    host wall clock; whole-job cell-steps/s (max over replicas)."""
+    host wall clock; whole-job cell-steps/s (max over replicas).  Returns (value, h2d, d2h bytes per step)."""
     import torch
     hv = torch.zeros(E, dtype=torch.float64).pin_memory()
     he = torch.zeros(N, dtype=torch.float64).pin_memory()
     hdv = torch.zeros(E * 3, dtype=torch.float64).pin_memory()
     hde = torch.zeros(N * 3, dtype=torch.float64).pin_memory()
     hp = torch.zeros(n, dtype=torch.float64).pin_memory()
-    sol = solver(g.DF64, LMAX)
-    sol.set_stream(stream.cuda_stream)
     it = 0
     for _ in range(args.warmup):
         sol.set_state_ptrs(it, hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
         sol.run_host_ptr(n, hp.data_ptr())
         it = sol.get_state_ptrs(hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
-    barrier()
+    barrier(collective)
     total = 0.0
     for _ in range(args.steps):
         flush.fill_(1.0)
@@ -430,9 +475,11 @@ def run_e2e(g, solver, stream, flush, args, n, N, E, barrier, max_over_ranks, wo
         sol.run_host_ptr(n, hp.data_ptr())
         it = sol.get_state_ptrs(hv.data_ptr(), he.data_ptr(), hdv.data_ptr(), hde.data_ptr())
         total += time.perf_counter() - ta
-    sol.close()
-    barrier()
-    return world * N * n * args.steps / max_over_ranks(total)
+    barrier(collective)
+    h2d = (E + N + 3 * E + 3 * N) * 8
+    d2h = (E + N + 3 * E + 3 * N) * 8 + n * 8
+    tmax = max_over_ranks(total) if collective else total
+    return (world if collective else 1) * N * n * args.steps / tmax, h2d, d2h
 
 
 def run_sweep(args, fp64_plain: float, peak: float) -> dict:

@@ -108,9 +108,13 @@ _SIGS = {
     "odis_get_state": ([_V, _I, _D, _D, _D, _D], C.c_int),
     "odis_set_state": ([_V, C.c_int, _D, _D, _D, _D], C.c_int),
     "odis_launch_count": ([_V, C.POINTER(C.c_longlong)], C.c_int),
+    "odis_set_wait_limit": ([_V, C.c_uint, C.c_int], C.c_int),
+    "odis_measure_fp64_rate": ([_D], C.c_int),
+    "odis_batch_set_wait_limit": ([_V, C.c_uint, C.c_int], C.c_int),
     "odis_profile_kernels": ([_V, C.c_int, _D], C.c_int),
     "odis_set_persistent": ([_V, C.c_int, _I], C.c_int),
     "odis_sh_tiles": ([_V, _I, _I, _I], C.c_int),
+    "odis_sh_layout": ([_V, _I, _I, C.POINTER(C.c_longlong)], C.c_int),
     "odis_batch_create": ([C.POINTER(Params), C.POINTER(_V), C.c_int, _V, C.c_int, C.POINTER(_V)], C.c_int),
     "odis_batch_destroy": ([_V], None),
     "odis_batch_run": ([_V, C.c_double, C.c_int, _D, C.c_int, _D, C.c_int, C.c_int], C.c_int),
@@ -253,6 +257,13 @@ def benchmark_sh_factors(g: float, radius: float, lmax: int, seed: int = 1) -> n
     f = np.zeros(lmax + 1)
     f[2:] = np.random.default_rng(seed).uniform(0.5, 1.5, lmax - 1)
     return f * loading_factors(g, radius, lmax)
+
+
+def measure_fp64_rate() -> float:
+    """FP64 FMA rate of this GPU in TFLOP/s (odis_measure_fp64_rate)."""
+    t = C.c_double()
+    _ck(lib().odis_measure_fp64_rate(C.byref(t)), "odis_measure_fp64_rate")
+    return t.value
 
 
 def read_input(path: str | os.PathLike) -> Input:
@@ -459,10 +470,21 @@ class Solver:
         _ck(lib().odis_sh_tiles(self._h, C.byref(a), C.byref(b), C.byref(c)), "odis_sh_tiles")
         return a.value, b.value, c.value
 
+    def sh_layout(self) -> dict:
+        """Self-gravity basis storage: antipodal half basis or full, cells covered, bytes per transform."""
+        a, b, c = C.c_int(), C.c_int(), C.c_longlong()
+        _ck(lib().odis_sh_layout(self._h, C.byref(a), C.byref(b), C.byref(c)), "odis_sh_layout")
+        return {"half": bool(a.value), "cells": b.value, "basis_bytes": c.value}
+
     def launch_count(self) -> int:
         n = C.c_longlong()
         _ck(lib().odis_launch_count(self._h, C.byref(n)), "odis_launch_count")
         return n.value
+
+    def set_wait_limit(self, polls: int = 0, withhold: int = -1) -> None:
+        """Bound the persistent loop's neighbour waits to `polls` polls (0: default); withhold >= 0 makes that
+        CTA publish no step flags (failure-detection test hook)."""
+        _ck(lib().odis_set_wait_limit(self._h, int(polls), int(withhold)), "odis_set_wait_limit")
 
     def profile_kernels(self, reps: int = 200):
         ms = np.zeros(3)
@@ -576,6 +598,11 @@ class Batch:
         _ck(lib().odis_batch_project(self._h, int(mesh), C.c_void_p(bv.ctypes.data), kv, C.c_void_p(be.ctypes.data), ke,
                                      _dp(out), kv + ke), "odis_batch_project")
         return out[self.mesh_members(mesh)]
+
+    def set_wait_limit(self, polls: int = 0, withhold: int = -1) -> None:
+        """Bound each grid-barrier wait to `polls` polls (0: default); withhold >= 0 makes that CTA never
+        arrive (failure-detection test hook)."""
+        _ck(lib().odis_batch_set_wait_limit(self._h, int(polls), int(withhold)), "odis_batch_set_wait_limit")
 
     def info(self) -> dict:
         g, p, gr, n, r = C.c_int(), C.c_int(), C.c_int(), C.c_longlong(), C.c_int()

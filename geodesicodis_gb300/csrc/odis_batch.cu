@@ -104,6 +104,8 @@ struct BatchArgs {
     int* status;
     int init_load;
     float ab3a, ab3b, ab3c;
+    unsigned spin_limit;               // polls of one barrier wait before it gives up
+    int withhold;                      // >= 0: this CTA never arrives at a barrier (failure-detection test hook)
 };
 
 __device__ __forceinline__ float4 f4(float s) { return make_float4(s, s, s, s); }
@@ -173,15 +175,15 @@ __device__ bool grid_barrier(const BatchArgs& a, int* s_ok)
         int ok = 1;
         const unsigned gen = ld_acquire(a.bar_gen);
         __threadfence();
-        const unsigned arrived = atomicAdd(a.bar_count, 1u);
-        if (arrived == gridDim.x - 1) {
+        const unsigned arrived = (int)blockIdx.x == a.withhold ? 0u : atomicAdd(a.bar_count, 1u);
+        if ((int)blockIdx.x != a.withhold && arrived == gridDim.x - 1) {
             atomicExch(a.bar_count, 0u);
             __threadfence();
             st_release(a.bar_gen, gen + 1);
         } else {
             unsigned spins = 0;
             while (ld_acquire(a.bar_gen) == gen) {
-                if (++spins > kBarrierSpins) { ok = 0; atomicOr(a.status, 1 << ODIS_ERR_TIMEOUT); break; }
+                if (++spins > a.spin_limit) { ok = 0; atomicOr(a.status, 1 << ODIS_ERR_TIMEOUT); break; }
                 __nanosleep(32);
             }
         }
@@ -518,6 +520,8 @@ struct odis_batch {
     int* d_base = nullptr;
     double* d_part = nullptr;
     unsigned* d_bar = nullptr;           // [0] count, [1] generation
+    unsigned spin_limit = 0;             // odis_batch_set_wait_limit: polls of a barrier wait (0: kBarrierSpins)
+    int withhold = -1;                   // odis_batch_set_wait_limit: CTA that never arrives (-1: none)
     int* d_status = nullptr;
     int grid = 0;                        // CTAs of the chosen variant
     int variant = 2;                     // index into kRowChoices
@@ -874,6 +878,8 @@ extern "C" odis_status odis_batch_run(odis_batch* b, double orbits, int steps, d
         a.ab3a = (float)(23. / 12.);
         a.ab3b = (float)(-16. / 12.);
         a.ab3c = (float)(5. / 12.);
+        a.spin_limit = b->spin_limit ? b->spin_limit : kBarrierSpins;
+        a.withhold = b->withhold;
         const size_t smem = (sizeof(double) + 2 * sizeof(float)) * (size_t)b->P;
         // steps j = 0 .. smax: the last one only records the power of the final state
         for (int j0 = 0; j0 <= smax && st == ODIS_OK; j0 += chunk) {
@@ -1138,5 +1144,13 @@ extern "C" odis_status odis_batch_set_mesh_members(odis_batch* b, int mesh, cons
         }
         for (int k : here) b->base[b->slot_of[mem[k]]] = 0;
     }
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_batch_set_wait_limit(odis_batch* b, unsigned polls, int withhold)
+{
+    if (!b || withhold < -1) return ODIS_ERR_ARG;
+    b->spin_limit = polls;
+    b->withhold = withhold;
     return ODIS_OK;
 }

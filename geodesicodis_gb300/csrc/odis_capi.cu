@@ -1320,6 +1320,14 @@ static int choose_exec_path(odis_ctx* c)
 // ---------------------------------------------------------------------------
 // measurement helpers
 // ---------------------------------------------------------------------------
+extern "C" odis_status odis_set_wait_limit(odis_ctx* c, unsigned polls, int withhold)
+{
+    if (!c || withhold < -1 || (c->persist_ok && withhold >= c->plan.P)) return ODIS_ERR_ARG;
+    c->plan.spin_limit = polls;
+    c->plan.withhold = withhold;
+    return ODIS_OK;
+}
+
 extern "C" odis_status odis_launch_count(odis_ctx* c, long long* n)
 {
     if (!c || !n) return ODIS_ERR_ARG;
@@ -1396,6 +1404,18 @@ extern "C" odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks
     if (tile_l) *tile_l = a;
     if (chunks) *chunks = b;
     if (lanes) *lanes = d;
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_sh_layout(const odis_ctx* c, int* half, int* cells, long long* basis_bytes)
+{
+    if (!c) return ODIS_ERR_ARG;
+    int a = 0, b = 0;
+    long long by = 0;
+    if (c->sh) sh_layout(c->sh, &a, &b, &by);
+    if (half) *half = a;
+    if (cells) *cells = b;
+    if (basis_bytes) *basis_bytes = by;
     return ODIS_OK;
 }
 

@@ -20,7 +20,7 @@
 //     boundary cells for flag_e >= s+1 of set C (owners of its cells' faces).
 // The same sets cover the write-after-read hazards on the double-buffered v
 // and the in-place eta, because the read relations are symmetric.  Every wait
-// is bounded: after kSpinLimit polls the CTA records ODIS_ERR_TIMEOUT and
+// is bounded: after kSpinLimitDefault polls (or the plan's spin_limit) the CTA records ODIS_ERR_TIMEOUT and
 // leaves the loop, so no CTA waits forever.  Values other CTAs write during the
 // run are read with ld.global.cg (L2, never a stale L1 line).
 #include "../../include/odis_gpu.h"
@@ -33,7 +33,7 @@ namespace odis {
 
 namespace {
 
-constexpr unsigned kSpinLimit = 1u << 22;     // polls of one wait (about a second with the back-off)
+constexpr unsigned kSpinLimitDefault = 1u << 22;   // polls of one wait (about a second with the back-off)
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p)
 {
@@ -48,14 +48,16 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v)
 }
 
 // Wait until flags[dep[q]] >= target for every dependency q; false on timeout.
-__device__ bool wait_deps(const unsigned* flags, const int* dep, int nd, unsigned target, int* status)
+__device__ bool wait_deps(const unsigned* flags, const int* dep, int nd, unsigned target, int* status,
+                          unsigned limit)
 {
+    const unsigned lim = limit ? limit : kSpinLimitDefault;
     bool ok = true;
     for (int q = threadIdx.x; q < nd; q += blockDim.x) {
         const unsigned* f = flags + dep[q];
         unsigned spins = 0;
         while (ld_acquire_u32(f) < target) {
-            if (++spins > kSpinLimit) {
+            if (++spins > lim) {
                 atomicOr(status, 1 << ODIS_ERR_TIMEOUT);
                 ok = false;
                 break;
@@ -67,11 +69,12 @@ __device__ bool wait_deps(const unsigned* flags, const int* dep, int nd, unsigne
 }
 
 // CTA barrier, then one thread publishes v with a GPU-scope release: the barrier
-// orders the CTA's writes before it, and the release is cumulative over them
-__device__ __forceinline__ void signal(unsigned* flag, unsigned v)
+// orders the CTA's writes before it, and the release is cumulative over them.
+// A withheld CTA (test hook) skips the store, so the waits on it run out.
+__device__ __forceinline__ void signal(unsigned* flag, unsigned v, bool withheld)
 {
     __syncthreads();
-    if (threadIdx.x == 0) st_release_u32(flag, v);
+    if (threadIdx.x == 0 && !withheld) st_release_u32(flag, v);
 }
 
 template <class T>
@@ -263,23 +266,23 @@ __global__ void __launch_bounds__(kPersistThreads) k_persistent(FaceCoef<T> fc, 
         fx.cosM = cosM; fx.sinM = sinM; fx.malpha = malpha; fx.ca = ca; fx.cb = cb; fx.cc3 = cc3; fx.dt = dt;
         fx.NF = NF; fx.nfi = nfi; fx.quad = sc.quad; fx.ab3 = ab3; fx.status = st.status;
         for (int lf = threadIdx.x; lf < nfi; lf += blockDim.x) face_update<T>(fx, lf, pw);
-        if (s > 0 && !wait_deps(pl.flag_c, depA, ndA, (unsigned)s, st.status)) { ok = false; break; }
+        if (s > 0 && !wait_deps(pl.flag_c, depA, ndA, (unsigned)s, st.status, pl.spin_limit)) { ok = false; break; }
         for (int lf = nfi + threadIdx.x; lf < nf; lf += blockDim.x) face_update<T>(fx, lf, pw);
         const T bs = block_sum_t<T>(pw, red);
         if (threadIdx.x == 0) part[(size_t)s * P + b] = bs;
-        signal(&pl.flag_e[b], (unsigned)(s + 1));
+        signal(&pl.flag_e[b], (unsigned)(s + 1), b == pl.withhold);
 
         CellCtx<T> cx;
         cx.shw = shw; cx.svo = svo; cx.ho = she + bo * NC; cx.hc = she + bi * NC; cx.seta = seta;
         cx.sedge = sedge; cx.scell = scell; cx.vout = vout; cx.eta = st.eta;
         cx.ca = ca; cx.cb = cb; cx.cc3 = cc3; cx.dt = dt; cx.NC = NC; cx.nci = nci; cx.ab3 = ab3;
         for (int lc = threadIdx.x; lc < nci; lc += blockDim.x) cell_update<T>(cx, lc);
-        if (!wait_deps(pl.flag_e, depC, ndC, (unsigned)(s + 1), st.status)) { ok = false; break; }
+        if (!wait_deps(pl.flag_e, depC, ndC, (unsigned)(s + 1), st.status, pl.spin_limit)) { ok = false; break; }
         for (int lc = nci + threadIdx.x; lc < nc; lc += blockDim.x) cell_update<T>(cx, lc);
-        signal(&pl.flag_c[b], (unsigned)(s + 1));
+        signal(&pl.flag_c[b], (unsigned)(s + 1), b == pl.withhold);
     }
     // dissipation of the final state (power of the run's last step)
-    if (ok && wait_deps(pl.flag_e, depA, ndA, (unsigned)n, st.status)) {
+    if (ok && wait_deps(pl.flag_e, depA, ndA, (unsigned)n, st.status, pl.spin_limit)) {
         const int bf = (int)((first + n) & 1);
         const T* vin = (bf ? st.v[1] : st.v[0]);
         const T* svi = sv + bf * NF;

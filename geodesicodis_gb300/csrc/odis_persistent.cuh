@@ -34,6 +34,8 @@ struct PersistPlan {
     unsigned* flag_e = nullptr;   // [P] face phases completed in the current run
     unsigned* flag_c = nullptr;   // [P] cell phases completed in the current run
     void* part = nullptr;         // [(n+1)][P] dissipation partials of a run (method type)
+    unsigned spin_limit = 0;      // polls of one wait before it gives up (0: kSpinLimit, about a second)
+    int withhold = -1;            // >= 0: this CTA publishes no step flags (failure-detection test hook)
 };
 
 size_t persist_smem_bytes(int value_bytes, int nf_max, int nc_max);

@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 namespace odis {
@@ -68,8 +69,12 @@ void plm_bar(int L, double z, std::vector<double>& P)
 // arithmetic of each method: Ar<T> (odis_arith.cuh)
 
 // partial[k][chunk] = sum over the chunk's cells of Pbar_lm (cos|sin)(m lon) eta,
-// for the degrees l0 .. l0+nl-1 of order m of this block's tile
-template <class T, int kTileL>
+// for the degrees l0 .. l0+nl-1 of order m of this block's tile.
+// kHalf: the basis is stored for one cell of each antipodal pair (N of them,
+// row stride Np), and `eta` holds e = eta_a + eta_b in [0, Np) and
+// o = eta_a - eta_b in [Np, 2 Np); since Y_lm(-x) = (-1)^l Y_lm(x), even
+// degrees sum Y_lm e and odd degrees Y_lm o over the half set.
+template <class T, int kTileL, bool kHalf>
 __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict__ P, const T* __restrict__ trig,
                                                             const T* __restrict__ eta, int N, int Np, int L,
                                                             const int* __restrict__ tiles, int nchunk,
@@ -101,15 +106,23 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
             A::ld2(sm + i, s1, s2);
             const T ec = A::mul(c1, e), es = A::mul(s1, e);
             const T ec2 = A::mul(c2, e2), es2 = A::mul(s2, e2);
+            T oc = ec, os = es, oc2 = ec2, os2 = es2;
+            if constexpr (kHalf) {
+                T o, o2;
+                A::ld2(eta + Np + i, o, o2);
+                oc = A::mul(c1, o); os = A::mul(s1, o);
+                oc2 = A::mul(c2, o2); os2 = A::mul(s2, o2);
+            }
 #pragma unroll
             for (int j = 0; j < kTileL; j++) {
                 if (j < nl) {
                     T p, p2;
                     A::ld2(prow + (size_t)j * Np + i, p, p2);
-                    ac[j] = A::fma_acc(p, ec, ac[j]);
-                    as[j] = A::fma_acc(p, es, as[j]);
-                    bc[j] = A::fma_acc(p2, ec2, bc[j]);
-                    bs[j] = A::fma_acc(p2, es2, bs[j]);
+                    const bool odd = kHalf && ((l0 + j) & 1);
+                    ac[j] = A::fma_acc(p, odd ? oc : ec, ac[j]);
+                    as[j] = A::fma_acc(p, odd ? os : es, as[j]);
+                    bc[j] = A::fma_acc(p2, odd ? oc2 : ec2, bc[j]);
+                    bs[j] = A::fma_acc(p2, odd ? os2 : es2, bs[j]);
                 }
             }
         }
@@ -118,12 +131,18 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
         {
             const T e = eta[i];
             const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
+            T oc = ec, os = es;
+            if constexpr (kHalf) {
+                const T o = eta[Np + i];
+                oc = A::mul(cm[i], o); os = A::mul(sm[i], o);
+            }
 #pragma unroll
             for (int j = 0; j < kTileL; j++) {
                 if (j < nl) {
                     const T p = prow[(size_t)j * Np + i];
-                    ac[j] = A::fma_acc(p, ec, ac[j]);
-                    as[j] = A::fma_acc(p, es, as[j]);
+                    const bool odd = kHalf && ((l0 + j) & 1);
+                    ac[j] = A::fma_acc(p, odd ? oc : ec, ac[j]);
+                    as[j] = A::fma_acc(p, odd ? os : es, as[j]);
                 }
             }
         }
@@ -150,6 +169,26 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
         const int j = threadIdx.x >> 1, is_sin = threadIdx.x & 1;
         if (m > 0 || !is_sin) part[(size_t)sh_col(l0 + j, m, is_sin) * nchunk + chunk] = s;
     }
+}
+
+// e and o of the antipodal pairs (kHalf transforms): eo[h] = eta[ia[h]] + eta[ib[h]],
+// eo[Np + h] = eta[ia[h]] - eta[ib[h]]; zero on the padding h >= N
+template <class T>
+__global__ void __launch_bounds__(256) k_sh_pair(const T* __restrict__ eta, const int* __restrict__ ia,
+                                                 const int* __restrict__ ib, int N, int Np, T* __restrict__ eo)
+{
+    pdl_wait();
+    using A = Ar<T>;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Np) return;
+    T e = A::zero(), o = A::zero();
+    if (h < N) {
+        const T a = eta[ia[h]], b = eta[ib[h]];
+        e = A::add(a, b);
+        o = A::sub(a, b);
+    }
+    eo[h] = e;
+    eo[Np + h] = o;
 }
 
 // t_k = sum over the chunk partials of coefficient k in FP64, one warp per
@@ -188,9 +227,14 @@ __global__ void __launch_bounds__(32) k_sh_coef(const double* __restrict__ t, in
 // kSynthLanes consecutive threads share a cell and split the orders m between
 // them (m = j, j + kSynthLanes, ...); their sums meet by shuffles in a fixed
 // order.  Two independent accumulator pairs keep two loads in flight per lane.
-template <class T, int kSynthLanes, int kCells>
+// kHalf: the basis covers one cell h of each antipodal pair (N of them); the
+// even- and odd-degree sums E and O are kept apart (consecutive degrees go to
+// the two accumulator sets in turn) and the pair's cells receive E + O
+// (ia[h]) and E - O (ib[h]), since Y_lm(-x) = (-1)^l Y_lm(x).
+template <class T, int kSynthLanes, int kCells, bool kHalf>
 __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict__ P, const T* __restrict__ trig,
                                                             const T* __restrict__ coef, int N, int Np, int L, int K,
+                                                            const int* __restrict__ ia, const int* __restrict__ ib,
                                                             T* __restrict__ usg)
 {
     pdl_wait();
@@ -205,10 +249,13 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
     const int q = gt / kSynthLanes, j = gt % kSynthLanes;
     const int i = kCells * q, i2 = kCells == 2 ? min(2 * q + 1, N - 1) : i;
     const bool pair = kCells == 2 && i2 == i + 1;   // i is even, so (i, i+1) is one aligned vector
-    T u = A::zero(), u2 = A::zero();
+    T u = A::zero(), u2 = A::zero();     // full basis: the sums; kHalf: the even-degree sums E
+    T w = A::zero(), w2 = A::zero();     // kHalf: the odd-degree sums O
     if (i < N) {
         for (int m = j; m <= L; m += kSynthLanes) {
-            T a0 = A::zero(), b0 = A::zero(), a1 = A::zero(), b1 = A::zero();
+            // set X takes degrees lstart, lstart + 2, ...; set Y lstart + 1, lstart + 3, ...
+            T xa0 = A::zero(), xb0 = A::zero(), xa1 = A::zero(), xb1 = A::zero();
+            T ya0 = A::zero(), yb0 = A::zero(), ya1 = A::zero(), yb1 = A::zero();
             const int lstart = m < 2 ? 2 : m;
             const T* prow = P + (size_t)p_row(L, lstart, m) * Np;
             // the order's trig values are loaded first and are in flight during the degree loop
@@ -217,7 +264,7 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
             T c0, c1, s0, s1;
             if (pair) { A::ld2(cr + i, c0, c1); A::ld2(sr + i, s0, s1); }
             else { c0 = cr[i]; c1 = cr[i2]; s0 = sr[i]; s1 = sr[i2]; }
-            auto step = [&](int l, T p0, T p1) {
+            auto stepx = [&](int l, T p0, T p1, T& a0, T& b0, T& a1, T& b1) {
                 const T cc = c[sh_col(l, m, 0)];
                 a0 = A::fma_acc(p0, cc, a0);
                 if (kCells == 2) a1 = A::fma_acc(p1, cc, a1);
@@ -237,28 +284,61 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
                     if (pair) A::ld2(pr + i, p0[q], p1[q]);
                     else { p0[q] = pr[i]; p1[q] = kCells == 2 ? pr[i2] : p0[q]; }
                 }
+                if constexpr (kHalf) {
+                    stepx(l, p0[0], p1[0], xa0, xb0, xa1, xb1);
+                    stepx(l + 1, p0[1], p1[1], ya0, yb0, ya1, yb1);
+                    stepx(l + 2, p0[2], p1[2], xa0, xb0, xa1, xb1);
+                    stepx(l + 3, p0[3], p1[3], ya0, yb0, ya1, yb1);
+                } else {
 #pragma unroll
-                for (int q = 0; q < 4; q++) step(l + q, p0[q], p1[q]);
+                    for (int q = 0; q < 4; q++) stepx(l + q, p0[q], p1[q], xa0, xb0, xa1, xb1);
+                }
             }
             for (; l <= L; l++) {
                 const T* pr = prow + (size_t)(l - lstart) * Np;
                 T p0, p1;
                 if (pair) A::ld2(pr + i, p0, p1);
                 else { p0 = pr[i]; p1 = kCells == 2 ? pr[i2] : p0; }
-                step(l, p0, p1);
+                if (kHalf && ((l - lstart) & 1)) stepx(l, p0, p1, ya0, yb0, ya1, yb1);
+                else stepx(l, p0, p1, xa0, xb0, xa1, xb1);
             }
-            u = A::fma(c0, A::norm(a0), A::fma(s0, A::norm(b0), u));
-            if (kCells == 2) u2 = A::fma(c1, A::norm(a1), A::fma(s1, A::norm(b1), u2));
+            if constexpr (kHalf) {
+                const bool xodd = lstart & 1;             // set X holds the degrees of lstart's parity
+                const T ea0 = xodd ? ya0 : xa0, eb0 = xodd ? yb0 : xb0, oa0 = xodd ? xa0 : ya0, ob0 = xodd ? xb0 : yb0;
+                u = A::fma(c0, A::norm(ea0), A::fma(s0, A::norm(eb0), u));
+                w = A::fma(c0, A::norm(oa0), A::fma(s0, A::norm(ob0), w));
+                if (kCells == 2) {
+                    const T ea1 = xodd ? ya1 : xa1, eb1 = xodd ? yb1 : xb1, oa1 = xodd ? xa1 : ya1, ob1 = xodd ? xb1 : yb1;
+                    u2 = A::fma(c1, A::norm(ea1), A::fma(s1, A::norm(eb1), u2));
+                    w2 = A::fma(c1, A::norm(oa1), A::fma(s1, A::norm(ob1), w2));
+                }
+            } else {
+                u = A::fma(c0, A::norm(xa0), A::fma(s0, A::norm(xb0), u));
+                if (kCells == 2) u2 = A::fma(c1, A::norm(xa1), A::fma(s1, A::norm(xb1), u2));
+            }
         }
     }
 #pragma unroll
     for (int o = kSynthLanes / 2; o > 0; o >>= 1) {
         u = A::add(u, A::shfl(u, o));
         if (kCells == 2) u2 = A::add(u2, A::shfl(u2, o));
+        if (kHalf) {
+            w = A::add(w, A::shfl(w, o));
+            if (kCells == 2) w2 = A::add(w2, A::shfl(w2, o));
+        }
     }
     if (i < N && j == 0) {
-        usg[i] = u;
-        if (kCells == 2 && 2 * q + 1 < N) usg[2 * q + 1] = u2;
+        if constexpr (kHalf) {
+            usg[ia[i]] = A::add(u, w);
+            usg[ib[i]] = A::sub(u, w);
+            if (kCells == 2 && 2 * q + 1 < N) {
+                usg[ia[2 * q + 1]] = A::add(u2, w2);
+                usg[ib[2 * q + 1]] = A::sub(u2, w2);
+            }
+        } else {
+            usg[i] = u;
+            if (kCells == 2 && 2 * q + 1 < N) usg[2 * q + 1] = u2;
+        }
     }
 }
 
@@ -309,7 +389,62 @@ struct ShLoading {
     ShTc* tc = nullptr;          // tensor-core transforms (FP32 method), when they fit
     bool use_tc = false;         // setup-time choice between the tc and CUDA-core transforms
     int* status = nullptr;       // context status word (device)
+    // antipodal half basis: P and trig hold the Nh cells ia[h] (one of each pair
+    // {ia[h], ib[h]} of antipodal cells), rows of stride Nhp
+    bool half = false;
+    int Nh = 0, Nhp = 0;
+    int* ia = nullptr;           // [Nhp] (padding repeats the last pair)
+    int* ib = nullptr;
+    void* eo = nullptr;          // [2][Nhp] e = eta_a + eta_b, o = eta_a - eta_b, method type
+    // cells and row stride of the stored basis
+    int bn() const { return half ? Nh : N; }
+    int bp() const { return half ? Nhp : Np; }
 };
+
+// Antipodal pairing of the mesh's cells: b = a(i) with x_b = -x_i to within
+// `tol` (unit vectors), a(a(i)) = i, a(i) != i, for every cell; false if the
+// mesh has no such symmetry.  The icosahedral grids are centrally symmetric.
+static bool antipodal_pairs(const Mesh& m, double tol, std::vector<int>& partner)
+{
+    const int N = m.N;
+    partner.assign(N, -1);
+    std::vector<double> x((size_t)3 * N);
+    for (int i = 0; i < N; i++) {
+        const double lat = m.node_sph[(size_t)i * 2], lon = m.node_sph[(size_t)i * 2 + 1];
+        x[3 * i] = std::cos(lat) * std::cos(lon);
+        x[3 * i + 1] = std::cos(lat) * std::sin(lon);
+        x[3 * i + 2] = std::sin(lat);
+    }
+    // cells bucketed on a grid of spacing q; a partner lies in the bucket of -x or a neighbour of it
+    const double q = 1e-4;
+    auto key = [](long long a, long long b, long long c) {
+        return (unsigned long long)((a & 0x1fffff) | ((b & 0x1fffff) << 21) | ((c & 0x1fffff) << 42));
+    };
+    std::unordered_map<unsigned long long, std::vector<int>> grid;
+    grid.reserve((size_t)N * 2);
+    for (int i = 0; i < N; i++)
+        grid[key(std::llround(x[3 * i] / q), std::llround(x[3 * i + 1] / q), std::llround(x[3 * i + 2] / q))].push_back(i);
+    for (int i = 0; i < N; i++) {
+        const long long k0 = std::llround(-x[3 * i] / q), k1 = std::llround(-x[3 * i + 1] / q),
+                        k2 = std::llround(-x[3 * i + 2] / q);
+        double best = tol;
+        for (int d0 = -1; d0 <= 1; d0++)
+            for (int d1 = -1; d1 <= 1; d1++)
+                for (int d2 = -1; d2 <= 1; d2++) {
+                    auto it = grid.find(key(k0 + d0, k1 + d1, k2 + d2));
+                    if (it == grid.end()) continue;
+                    for (int j : it->second) {
+                        const double d = std::fabs(x[3 * j] + x[3 * i]) + std::fabs(x[3 * j + 1] + x[3 * i + 1]) +
+                                         std::fabs(x[3 * j + 2] + x[3 * i + 2]);
+                        if (d <= best) { best = d; partner[i] = j; }
+                    }
+                }
+        if (partner[i] < 0 || partner[i] == i) return false;
+    }
+    for (int i = 0; i < N; i++)
+        if (partner[partner[i]] != i) return false;
+    return true;
+}
 
 void sh_basis_host(const Mesh& m, int L, std::vector<double>& Y)
 {
@@ -438,9 +573,40 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
     ShLoading* s = new ShLoading;
     s->L = L; s->K = K; s->MP = MP; s->N = N; s->Np = Np; s->precision = precision; s->status = status;
     bool ok = true;
-    if (precision == ODIS_FP64) ok = upload_rows<double>(&s->P, P) && upload_rows<double>(&s->trig, trig);
-    else if (precision == ODIS_DF64) ok = upload_rows<df64>(&s->P, P) && upload_rows<df64>(&s->trig, trig);
-    else ok = upload_rows<float>(&s->P, P) && upload_rows<float>(&s->trig, trig);
+    // Antipodal half basis (ODIS_SH_HALF=0 keeps the full one; the FP32 method's
+    // tensor-core transforms, when forced with ODIS_SH_TC=1, need the full one)
+    std::vector<int> partner;
+    {
+        const char* eh = std::getenv("ODIS_SH_HALF");
+        const char* et = std::getenv("ODIS_SH_TC");
+        const bool want = !(eh && eh[0] == '0') && !(precision == ODIS_FP32 && et && et[0] == '1');
+        s->half = want && (N % 2 == 0) && antipodal_pairs(m, 1e-9, partner);
+    }
+    if (s->half) {
+        s->Nh = N / 2;
+        s->Nhp = (s->Nh + 127) / 128 * 128;
+        std::vector<int> ha(s->Nhp), hb(s->Nhp);
+        int h = 0;
+        for (int i = 0; i < N; i++)
+            if (i < partner[i]) { ha[h] = i; hb[h] = partner[i]; h++; }
+        for (int k = h; k < s->Nhp; k++) { ha[k] = ha[h - 1]; hb[k] = hb[h - 1]; }
+        std::vector<double> Ph((size_t)MP * s->Nhp, 0.0), th((size_t)2 * (L + 1) * s->Nhp, 0.0);
+        for (int r = 0; r < MP; r++)
+            for (int k = 0; k < s->Nh; k++) Ph[(size_t)r * s->Nhp + k] = P[(size_t)r * Np + ha[k]];
+        for (int r = 0; r < 2 * (L + 1); r++)
+            for (int k = 0; k < s->Nh; k++) th[(size_t)r * s->Nhp + k] = trig[(size_t)r * Np + ha[k]];
+        P.swap(Ph);
+        trig.swap(th);
+        ok = cudaMalloc(&s->ia, sizeof(int) * s->Nhp) == cudaSuccess &&
+             cudaMemcpy(s->ia, ha.data(), sizeof(int) * s->Nhp, cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMalloc(&s->ib, sizeof(int) * s->Nhp) == cudaSuccess &&
+             cudaMemcpy(s->ib, hb.data(), sizeof(int) * s->Nhp, cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMalloc(&s->eo, 2 * 8 * (size_t)s->Nhp) == cudaSuccess &&
+             cudaMemset(s->eo, 0, 2 * 8 * (size_t)s->Nhp) == cudaSuccess;
+    }
+    if (precision == ODIS_FP64) ok = ok && upload_rows<double>(&s->P, P) && upload_rows<double>(&s->trig, trig);
+    else if (precision == ODIS_DF64) ok = ok && upload_rows<df64>(&s->P, P) && upload_rows<df64>(&s->trig, trig);
+    else ok = ok && upload_rows<float>(&s->P, P) && upload_rows<float>(&s->trig, trig);
     const size_t esz = precision == ODIS_FP32 ? sizeof(float) : sizeof(double);
     ok = ok && cudaMalloc(&s->usg, esz * Np) == cudaSuccess && cudaMemset(s->usg, 0, esz * Np) == cudaSuccess;
     ok = ok && cudaMalloc(&s->part, 8 * (size_t)K * kMaxChunks) == cudaSuccess &&
@@ -449,7 +615,7 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
          cudaMemcpy(s->FGinv, G.data(), sizeof(double) * G.size(), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMalloc(&s->t, sizeof(double) * K) == cudaSuccess && cudaMalloc(&s->coef, 8 * (size_t)K) == cudaSuccess;
     if (!ok) { sh_destroy(s); return ODIS_ERR_NOMEM; }
-    if (precision == ODIS_FP32) {
+    if (precision == ODIS_FP32 && !s->half) {
         double pmax = 0.0;
         for (double x : P) pmax = std::fmax(pmax, std::fabs(x));
         const int tst = shtc_create(&s->tc, (const float*)s->P, (const float*)s->trig, pmax, L, N, Np, status);
@@ -466,6 +632,7 @@ void sh_destroy(ShLoading* s)
     if (!s) return;
     cudaFree(s->P); cudaFree(s->trig); cudaFree(s->tiles); cudaFree(s->part); cudaFree(s->FGinv);
     cudaFree(s->t); cudaFree(s->coef); cudaFree(s->usg);
+    cudaFree(s->ia); cudaFree(s->ib); cudaFree(s->eo);
     shtc_destroy(s->tc);
     delete s;
 }
@@ -494,28 +661,46 @@ static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int nt
     const dim3 grid(ntiles, nchunk);
     const T* P = (const T*)s->P;
     const T* trig = (const T*)s->trig;
-    const T* e = (const T*)eta;
     T* part = (T*)s->part;
-    if (tl == 2) pdl_launch(k_sh_analysis<T, 2>, grid, kShThreads, 0, st, P, trig, e, s->N, s->Np, s->L, tiles, nchunk, part);
-    else if (tl == 4) pdl_launch(k_sh_analysis<T, 4>, grid, kShThreads, 0, st, P, trig, e, s->N, s->Np, s->L, tiles, nchunk, part);
-    else pdl_launch(k_sh_analysis<T, 8>, grid, kShThreads, 0, st, P, trig, e, s->N, s->Np, s->L, tiles, nchunk, part);
+    const int n = s->bn(), np = s->bp();
+    if (s->half) {
+        T* eo = (T*)s->eo;
+        pdl_launch(k_sh_pair<T>, (np + 255) / 256, 256, 0, st, (const T*)eta, (const int*)s->ia, (const int*)s->ib, n,
+                   np, eo);
+        const T* e = eo;
+        if (tl == 2) pdl_launch(k_sh_analysis<T, 2, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
+        else if (tl == 4) pdl_launch(k_sh_analysis<T, 4, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
+        else pdl_launch(k_sh_analysis<T, 8, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
+        return;
+    }
+    const T* e = (const T*)eta;
+    if (tl == 2) pdl_launch(k_sh_analysis<T, 2, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
+    else if (tl == 4) pdl_launch(k_sh_analysis<T, 4, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
+    else pdl_launch(k_sh_analysis<T, 8, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
 }
 
 template <class T>
 static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t st)
 {
-    const int sb = ((s->N + cells - 1) / cells * lanes + kSynthThreads - 1) / kSynthThreads;
+    const int n = s->bn(), np = s->bp();
+    const int sb = ((n + cells - 1) / cells * lanes + kSynthThreads - 1) / kSynthThreads;
     const size_t sm = sizeof(T) * s->K;
     const T* P = (const T*)s->P;
     const T* trig = (const T*)s->trig;
     const T* c = (const T*)s->coef;
+    const int* ia = s->ia;
+    const int* ib = s->ib;
     T* u = (T*)s->usg;
-#define ODIS_SYNTH(LN, CL) pdl_launch(k_sh_synth<T, LN, CL>, sb, kSynthThreads, sm, st, P, trig, c, s->N, s->Np, s->L, s->K, u)
-    if (cells == 2) {
-        if (lanes == 1) ODIS_SYNTH(1, 2); else if (lanes == 2) ODIS_SYNTH(2, 2); else if (lanes == 4) ODIS_SYNTH(4, 2); else ODIS_SYNTH(8, 2);
+#define ODIS_SYNTH(LN, CL, H) pdl_launch(k_sh_synth<T, LN, CL, H>, sb, kSynthThreads, sm, st, P, trig, c, n, np, s->L, s->K, ia, ib, u)
+#define ODIS_SYNTH_LANES(CL, H) \
+    do { if (lanes == 1) ODIS_SYNTH(1, CL, H); else if (lanes == 2) ODIS_SYNTH(2, CL, H); \
+         else if (lanes == 4) ODIS_SYNTH(4, CL, H); else ODIS_SYNTH(8, CL, H); } while (0)
+    if (s->half) {
+        if (cells == 2) ODIS_SYNTH_LANES(2, true); else ODIS_SYNTH_LANES(1, true);
     } else {
-        if (lanes == 1) ODIS_SYNTH(1, 1); else if (lanes == 2) ODIS_SYNTH(2, 1); else if (lanes == 4) ODIS_SYNTH(4, 1); else ODIS_SYNTH(8, 1);
+        if (cells == 2) ODIS_SYNTH_LANES(2, false); else ODIS_SYNTH_LANES(1, false);
     }
+#undef ODIS_SYNTH_LANES
 #undef ODIS_SYNTH
 }
 
@@ -676,6 +861,14 @@ void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)
     else enqueue_t<float>(s, eta, st);
 }
 
-int sh_kernels_per_step(const ShLoading* s) { return s && s->use_tc ? shtc_kernels_per_step() : 4; }
+int sh_kernels_per_step(const ShLoading* s) { return s && s->use_tc ? shtc_kernels_per_step() : (s && s->half ? 5 : 4); }
+
+void sh_layout(const ShLoading* s, int* half, int* cells, long long* basis_bytes)
+{
+    const size_t esz = s->precision == ODIS_FP32 ? 4 : 8;
+    if (half) *half = s->half ? 1 : 0;
+    if (cells) *cells = s->bn();
+    if (basis_bytes) *basis_bytes = (long long)((size_t)(s->MP + 2 * (s->L + 1)) * s->bn() * esz);
+}
 
 }  // namespace odis

@@ -40,6 +40,9 @@ int sh_kernels_per_step(const ShLoading* s);
 // tile shapes chosen by the setup-time autotuner; tl = 0 for the tensor-core
 // transforms (nchunk = analysis chunks, lanes = cell tiles per synthesis pass)
 void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes);
+// the stored basis: half = 1 for the antipodal half basis, the cells it covers,
+// and its bytes (Legendre rows + trig rows in the method's type)
+void sh_layout(const ShLoading* s, int* half, int* cells, long long* basis_bytes);
 // host helpers for checks: real SH basis at the nodes, [N][K]
 void sh_basis_host(const Mesh& m, int lmax, std::vector<double>& Y);
 

@@ -318,7 +318,23 @@ odis_status odis_update_energy_noalloc(const double* uv, const double* area, int
  * reports whether runs will use the persistent loop. */
 odis_status odis_set_persistent(odis_ctx* c, int enable, int* active);
 
+/* ---- failure detection ------------------------------------------------- */
+/* No reference counterpart (the reference is one single-threaded process).
+ * Every wait of the persistent loop on a neighbour CTA's step flag is bounded:
+ * after `polls` polls (0: the default, about a second) the CTA records
+ * ODIS_ERR_TIMEOUT, leaves the loop, and odis_run_steps returns
+ * ODIS_ERR_TIMEOUT; the state of that run is then undefined, the context stays
+ * usable (odis_set_state, then run again).  withhold >= 0 makes that CTA of
+ * the persistent launch skip its step-flag publications, so the waits on it
+ * run out: the test hook that shows the timeout path ends cleanly.  -1 off. */
+odis_status odis_set_wait_limit(odis_ctx* c, unsigned polls, int withhold);
+
 /* ---- measurement ------------------------------------------------------- */
+/* The FP64 FMA rate this GPU sustains (TFLOP/s, an FMA = 2 flops), measured
+ * by a kernel of independent FMA chains on every SM: the FP64 method's second
+ * ceiling beside HBM bandwidth.  Takes some tens of milliseconds; no context
+ * needed. */
+odis_status odis_measure_fp64_rate(double* tflops);
 /* Number of this library's kernels launched so far by the context. */
 odis_status odis_launch_count(odis_ctx* c, long long* n);
 /* Average device time (ms) per launch of each kernel group, each launched
@@ -337,6 +353,17 @@ odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms);
  * cores) fixes the choice.  With the tensor-core transforms tile_l = 0, chunks
  * = analysis chunks and lanes = 128-cell tiles per synthesis pass. */
 odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes);
+
+/* Storage of the self-gravity basis (0s without self-gravity).  On a centrally
+ * symmetric mesh (every cell has an antipodal partner; the icosahedral grids
+ * do) Y_lm(-x) = (-1)^l Y_lm(x), so the basis is stored for one cell of each
+ * pair and both transforms run over half the cells: the analysis sums even
+ * degrees against eta_a + eta_b and odd degrees against eta_a - eta_b, the
+ * synthesis gives the pair E + O and E - O (E, O: the even- and odd-degree
+ * sums).  *half = 1 then, *cells = N/2.  ODIS_SH_HALF=0 in the environment at
+ * odis_create keeps the full basis.  *basis_bytes = the Legendre and trig rows
+ * one transform reads. */
+odis_status odis_sh_layout(const odis_ctx* c, int* half, int* cells, long long* basis_bytes);
 
 /* ---- batched sweep ----------------------------------------------------- */
 /* Many configurations of the LTE time loop (src/timeIntegrator.cpp:57-322,
@@ -393,6 +420,11 @@ odis_status odis_batch_set_mesh_members(odis_batch* b, int mesh, const double* v
  * sums, FP64 across slices.  Members on other meshes are left untouched. */
 odis_status odis_batch_project(odis_batch* b, int mesh, const float* basis_v, int kv, const float* basis_eta, int ke,
                                double* out, int out_stride);
+
+/* The batch kernel's grid barriers, as odis_set_wait_limit: each wait gives
+ * up after `polls` polls (0: the default, about a second) and odis_batch_run
+ * returns ODIS_ERR_TIMEOUT; withhold >= 0 makes that CTA never arrive. */
+odis_status odis_batch_set_wait_limit(odis_batch* b, unsigned polls, int withhold);
 
 /* ---- warm-start surrogate network -------------------------------------- */
 /* No reference counterpart.  MLP n_in -> width (GELU) x depth -> n_mix * n_out,

@@ -106,6 +106,30 @@ def test_level6_sh_tile_paths(level6, monkeypatch, precision, tiles):
     sol.close()
 
 
+@pytest.mark.parametrize("precision", [0, 2, 1])
+def test_level6_half_and_full_basis(level6, monkeypatch, precision):
+    """The antipodal half basis (the default on these centrally symmetric meshes) and the full basis
+    (ODIS_SH_HALF=0) give the same run: to rounding in FP64/DF64, and both against the oracle."""
+    import geodesicodis_gb300 as g
+    half = _solver(level6, precision)
+    lay = half.sh_layout()
+    assert lay["half"] and lay["cells"] == 40962 // 2
+    monkeypatch.setenv("ODIS_SH_HALF", "0")
+    full = _solver(level6, precision)
+    assert not full.sh_layout()["half"] and full.sh_layout()["cells"] == 40962
+    assert full.sh_layout()["basis_bytes"] == 2 * lay["basis_bytes"]
+    ph, pf = half.run(L6_SHORT), full.run(L6_SHORT)
+    po, so = level6["short"]
+    tol = 1e-4 if precision == 1 else 1e-12
+    assert rel_err(ph, pf) < tol
+    for x, y in zip(half.get_state()[1:], full.get_state()[1:]):
+        assert rel_err(x, y) < (1e-3 if precision == 1 else 1e-12)
+    if precision != 1:
+        _cmp(full.get_state(), so, 1e-10)
+    half.close()
+    full.close()
+
+
 def test_level6_sh16_tensor_core_path(level6, monkeypatch):
     """The FP32 method's tcgen05 transforms at the benchmark size."""
     monkeypatch.setenv("ODIS_SH_TC", "1")

@@ -283,3 +283,29 @@ def test_oracle_quadratic_energy_branch(grid_dir):
         np.testing.assert_allclose(e, e_ref, rtol=1e-15)
         out[fric] = avg
     assert out[0] > 0 and out[1] > 0 and out[1] < 1e-6 * out[0]
+
+
+@pytest.mark.parametrize("level", [2, 4, 5])
+def test_generated_grids_are_centrally_symmetric(grid_dir, level):
+    """Every cell of the icosahedral grids has an antipodal partner (x_b = -x_a to 1e-12), and the real
+    harmonics obey Y_lm(-x) = (-1)^l Y_lm(x) there: the precondition of the half-basis self-gravity
+    transforms (analysis over e = eta_a + eta_b for even l, o = eta_a - eta_b for odd l)."""
+    import ctypes as C
+    from oracle import pyoracle as O
+    m = O.OracleMesh(grid_dir / f"grid_{level}.txt", RADIUS)
+    lat, lon = m.field(12), m.field(13)
+    x = np.stack([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], 1)
+    order = np.lexsort(np.round(x, 8).T)
+    anti = np.lexsort(np.round(-x, 8).T)
+    partner = np.empty(len(x), int)
+    partner[order] = anti                  # the cell whose rounded position is the negated one
+    assert np.max(np.abs(x[partner] + x)) < 1e-12
+    assert np.all(partner[partner] == np.arange(len(x))) and np.all(partner != np.arange(len(x)))
+    L = 8
+    K = (L + 1) ** 2
+    s = O.OracleSolver(m, radius=RADIUS, g=0.113, angvel=1e-5, h=1e3, alpha=1e-6, dt=10.0, sh_lmax=L,
+                       sh_factors=np.ones(L + 1))
+    Y = np.zeros((K, m.n_cells))
+    O.lib().orc_sh_basis(m._h, L, Y.ctypes.data_as(C.POINTER(C.c_double)))
+    parity = np.array([(-1) ** l for l in range(L + 1) for _ in range(2 * l + 1)])
+    np.testing.assert_allclose(Y[:, partner], parity[:, None] * Y, atol=1e-12)
