@@ -484,8 +484,8 @@ def run_e2e(sol, stream, flush, args, n, N, E, barrier, max_over_ranks, world, c
 
 def run_sweep(args, fp64_plain: float, peak: float) -> dict:
     """Batched sweep: 256 seeded configurations (levels 4-6, thickness, drag, eccentricity, obliquity;
-    FULL tide), FP32 state with double-float accumulation, `args.sweep_orbits` orbits each, in one
-    persistent cooperative launch per chunk of steps (odis_batch_run)."""
+    FULL tide), FP32 state with double-float accumulation, `args.sweep_orbits` orbits each: one CUDA graph
+    of persistent cooperative launches, one per chunk of steps (odis_batch_run)."""
     from geodesicodis_gb300 import sweep as S
     t0 = time.perf_counter()
     batch, members, meshes, period = S.make_sweep(256, 2, (4, 5, 6))
@@ -493,7 +493,8 @@ def run_sweep(args, fp64_plain: float, peak: float) -> dict:
     batch.run(steps=200)                                   # warm-up (then the members restart from rest)
     for mesh in range(len(meshes.levels)):
         batch.set_mesh_members(mesh)
-    l0 = batch.info()["launches"]
+    info0 = batch.info()
+    l0, g0 = info0["launches"], info0["graph_runs"]
     t = time.perf_counter()
     op, _ = batch.run(orbits=args.sweep_orbits)            # synchronous: returns when the device is done
     el = time.perf_counter() - t
@@ -515,7 +516,8 @@ def run_sweep(args, fp64_plain: float, peak: float) -> dict:
             "vs_fp64_plain_single_instance": cs / el / fp64_plain,
             "steps_per_orbit_range": [int(spo.min()), int(spo.max())], "members_at_2000": int(np.sum(spo == 2000)),
             "nonfinite_members": int(np.sum(~np.isfinite(op).all(axis=1))),
-            "launches": info["launches"] - l0, "grid": info["grid"], "padded_members": info["padded_members"],
+            "launches": info["launches"] - l0, "graph_launches": info["graph_runs"] - g0 - 1,
+            "grid": info["grid"], "padded_members": info["padded_members"],
             "rows_per_thread": info["rows_per_thread"],
             "create_seconds": t_create,
             "hbm_roofline_uniform": {"bytes_per_cell_step": bytes_per_cell_step,

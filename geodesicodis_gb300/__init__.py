@@ -111,6 +111,7 @@ _SIGS = {
     "odis_set_wait_limit": ([_V, C.c_uint, C.c_int], C.c_int),
     "odis_measure_fp64_rate": ([_D], C.c_int),
     "odis_batch_set_wait_limit": ([_V, C.c_uint, C.c_int], C.c_int),
+    "odis_batch_graph_runs": ([_V, C.POINTER(C.c_longlong)], C.c_int),
     "odis_profile_kernels": ([_V, C.c_int, _D], C.c_int),
     "odis_set_persistent": ([_V, C.c_int, _I], C.c_int),
     "odis_sh_tiles": ([_V, _I, _I, _I], C.c_int),
@@ -608,8 +609,10 @@ class Batch:
         g, p, gr, n, r = C.c_int(), C.c_int(), C.c_int(), C.c_longlong(), C.c_int()
         _ck(lib().odis_batch_info(self._h, C.byref(g), C.byref(p), C.byref(gr), C.byref(n), C.byref(r)),
             "odis_batch_info")
+        gr_runs = C.c_longlong()
+        _ck(lib().odis_batch_graph_runs(self._h, C.byref(gr_runs)), "odis_batch_graph_runs")
         return {"groups": g.value, "padded_members": p.value, "grid": gr.value, "launches": n.value,
-                "rows_per_thread": r.value}
+                "rows_per_thread": r.value, "graph_runs": gr_runs.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value and _lib is not None:

@@ -15,24 +15,86 @@
 // src/outFiles.cpp:138-823): float32 datasets [dumps][faces or nodes], one row
 // per dump, for the outputs input.in switches on.
 //
-//   odis_run [--dir D] [--grid FILE | --level N] [--precision fp64|df64|fp32] [--orbits X]
+// SIGINT, as in the reference (CatchExit and the loop's flag check,
+// src/timeIntegrator.cpp:32-37, 120, 307-316): the handler prints "Caught
+// Terminate Signal...", the loop stops after the step chunk in flight (at most
+// kCheckSteps steps), writes "Terminate signal caught..." to OUTPUT.txt, saves
+// the state and exits with status 1.  Besides the reference's %1.6E text files
+// (rounded to 7 digits), the state is saved exactly as
+// InitialConditions/state.bin (FP64, with the step count); --resume continues
+// from it to the same bits as an uninterrupted run.
+//
+//   odis_run [--dir D] [--grid FILE | --level N] [--precision fp64|df64|fp32] [--orbits X] [--resume]
 //
 // --level is the number of subdivisions (10*4^N+2 cells); without --grid or
 // --level the grid is generated for input.in's "geodesic grid level", whose
 // count the reference's grid files give as 10*4^(level-1)+2 cells.
 #include "odis_gpu.h"
 
+#include <csignal>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
 #include <sys/stat.h>
+#include <unistd.h>
 #include <vector>
 
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;
+constexpr int kCheckSteps = 512;      // steps between two looks at the terminate flag
+
+volatile std::sig_atomic_t g_terminate = 0;
+
+extern "C" void catch_exit(int)
+{
+    static const char msg[] = "Caught Terminate Signal...\n";
+    ssize_t w = write(STDOUT_FILENO, msg, sizeof msg - 1);
+    (void)w;
+    g_terminate = 1;
+}
+
+// Exact checkpoint: "ODISCKP1", int64 steps taken, int32 faces, int32 cells,
+// then v[E], eta[N], dvdt[E][3], detadt[N][3] as little-endian FP64.
+bool write_checkpoint(const std::string& path, long long iter, int E, int N, const std::vector<double>& v,
+                      const std::vector<double>& eta, const std::vector<double>& dv, const std::vector<double>& de)
+{
+    const std::string tmp = path + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return false;
+    const int64_t it = iter;
+    const int32_t e = E, n = N;
+    bool ok = std::fwrite("ODISCKP1", 1, 8, f) == 8 && std::fwrite(&it, 8, 1, f) == 1 && std::fwrite(&e, 4, 1, f) == 1 &&
+              std::fwrite(&n, 4, 1, f) == 1 && std::fwrite(v.data(), 8, E, f) == (size_t)E &&
+              std::fwrite(eta.data(), 8, N, f) == (size_t)N && std::fwrite(dv.data(), 8, (size_t)3 * E, f) == (size_t)3 * E &&
+              std::fwrite(de.data(), 8, (size_t)3 * N, f) == (size_t)3 * N;
+    ok = std::fclose(f) == 0 && ok;
+    return ok && std::rename(tmp.c_str(), path.c_str()) == 0;      // a reader never sees half a file
+}
+
+bool read_checkpoint(const std::string& path, long long* iter, int E, int N, std::vector<double>& v,
+                     std::vector<double>& eta, std::vector<double>& dv, std::vector<double>& de)
+{
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    char magic[8];
+    int64_t it = 0;
+    int32_t e = 0, n = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "ODISCKP1", 8) == 0 && std::fread(&it, 8, 1, f) == 1 &&
+              std::fread(&e, 4, 1, f) == 1 && std::fread(&n, 4, 1, f) == 1 && e == E && n == N && it >= 0;
+    if (ok) {
+        v.resize(E); eta.resize(N); dv.resize((size_t)3 * E); de.resize((size_t)3 * N);
+        ok = std::fread(v.data(), 8, E, f) == (size_t)E && std::fread(eta.data(), 8, N, f) == (size_t)N &&
+             std::fread(dv.data(), 8, (size_t)3 * E, f) == (size_t)3 * E &&
+             std::fread(de.data(), 8, (size_t)3 * N, f) == (size_t)3 * N;
+    }
+    std::fclose(f);
+    *iter = it;
+    return ok;
+}
 
 bool read_state(const std::string& path, int n, std::vector<double>& x, std::vector<double>& hist)
 {
@@ -163,6 +225,7 @@ int main(int argc, char** argv)
     std::string dir = ".", grid, prec = "fp64";
     int level = -1;
     double orbits = -1.0;
+    bool resume = false;
     for (int a = 1; a < argc; a++) {
         const std::string k = argv[a];
         auto next = [&]() -> std::string { return a + 1 < argc ? argv[++a] : std::string(); };
@@ -171,9 +234,10 @@ int main(int argc, char** argv)
         else if (k == "--level") level = std::atoi(next().c_str());
         else if (k == "--precision") prec = next();
         else if (k == "--orbits") orbits = std::atof(next().c_str());
+        else if (k == "--resume") resume = true;
         else {
             std::fprintf(stderr, "usage: odis_run [--dir D] [--grid FILE | --level N] [--precision fp64|df64|fp32] "
-                                 "[--orbits X]\n");
+                                 "[--orbits X] [--resume]\n");
             return 2;
         }
     }
@@ -204,7 +268,13 @@ int main(int argc, char** argv)
     st = odis_create(&p, mesh, &ctx);
     if (st != ODIS_OK) return fail("odis_create", st);
     std::vector<double> v, eta, dv, de;
-    if (in.init_kind == 1) {
+    long long start = 0;          // steps already taken (--resume)
+    if (resume) {
+        if (!read_checkpoint(dir + "/InitialConditions/state.bin", &start, E, N, v, eta, dv, de))
+            return fail("reading InitialConditions/state.bin", ODIS_ERR_IO);
+        st = odis_set_state(ctx, (int)start, v.data(), eta.data(), dv.data(), de.data());
+        if (st != ODIS_OK) return fail("odis_set_state", st);
+    } else if (in.init_kind == 1) {
         if (!read_state(dir + "/InitialConditions/vel_init.txt", E, v, dv) ||
             !read_state(dir + "/InitialConditions/pres_init.txt", N, eta, de))
             return fail("reading InitialConditions", ODIS_ERR_IO);
@@ -222,6 +292,7 @@ int main(int argc, char** argv)
     const double total_orbits = orbits > 0 ? orbits : in.end_time;
     const int out_every = std::max(1, in.steps_per_orbit / std::max(1, in.output_time));
     const long long total_steps = (long long)std::llround(total_orbits * in.steps_per_orbit);
+    std::signal(SIGINT, catch_exit);
     mkdir((dir + "/DATA").c_str(), 0755);
     FILE* out = std::fopen((dir + "/OUTPUT.txt").c_str(), "a");
     FILE* pw = std::fopen((dir + "/DATA/power.txt").c_str(), "w");
@@ -245,10 +316,19 @@ int main(int argc, char** argv)
         std::printf("%s\n", line);
         if (out) std::fprintf(out, "%s\n", line);
     }
-    int rc = 0, count = 2;
-    for (long long done = 0; done < total_steps; done += out_every, count++) {
-        const int n = (int)std::min<long long>(out_every, total_steps - done);
-        st = odis_run_steps(ctx, n, power.data(), ODIS_MEM_HOST);
+    int rc = 0, count = 2 + (int)(start / out_every);
+    bool terminated = false;
+    // output intervals end where the step count is a multiple of out_every (the reference's
+    // iter % out_freq == 0), also after a resume from a mid-interval checkpoint
+    for (long long done = start, n = 0; done < total_steps; done += n, count++) {
+        n = std::min<long long>(out_every - done % out_every, total_steps - done);
+        int ran = 0;
+        for (st = ODIS_OK; ran < n && st == ODIS_OK && !g_terminate; ran += (int)std::min<long long>(kCheckSteps, n - ran))
+            st = odis_run_steps(ctx, (int)std::min<long long>(kCheckSteps, n - ran), power.data() + ran, ODIS_MEM_HOST);
+        if (g_terminate && ran < n) {          // stopped inside the output interval: no dump for it
+            terminated = true;
+            break;
+        }
         double avg = 0.0;
         for (int k = 0; k < n; k++) avg += power[k];
         avg /= n;
@@ -266,6 +346,12 @@ int main(int argc, char** argv)
         if (st != ODIS_OK) { rc = fail("odis_run_steps", st); break; }
         st = data.dump(ctx, count - 1, p.dt * (double)(done + n));
         if (st != ODIS_OK) { rc = fail("writing DATA/data.h5", st); break; }
+        if (g_terminate) { terminated = true; break; }
+    }
+    if (terminated) {                         // src/timeIntegrator.cpp:307-316
+        std::printf("Terminate signal caught...\n");
+        if (out) std::fprintf(out, "Terminate signal caught...\n");
+        rc = 1;
     }
     if (data.close() != ODIS_OK && rc == 0) rc = fail("closing DATA/data.h5", ODIS_ERR_IO);
     if (out) std::fclose(out);
@@ -276,6 +362,8 @@ int main(int argc, char** argv)
         mkdir((dir + "/InitialConditions").c_str(), 0755);
         write_state(dir + "/InitialConditions/vel_init.txt", E, v, dv);
         write_state(dir + "/InitialConditions/pres_init.txt", N, eta, de);
+        if (!write_checkpoint(dir + "/InitialConditions/state.bin", iter, E, N, v, eta, dv, de) && rc == 0)
+            rc = fail("writing InitialConditions/state.bin", ODIS_ERR_IO);
         // final displacement and Cartesian velocity at the nodes (the "displacement" and
         // "x/y/z velocity" fields of the reference's output)
         std::vector<double> uxyz((size_t)3 * N);

@@ -377,6 +377,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(BatchArgs a, int j0, in
     __shared__ int s_ok, s_bad;
     const int tid = threadIdx.x;
     const int ng = a.ngroups;
+    // a previous chunk of this run gave up on a barrier: the run is over
+    if (*(volatile const int*)a.status & (1 << ODIS_ERR_TIMEOUT)) return;
     if (tid == 0) s_bad = 0;
     for (int j = j0; j < j1; j++) {
         // ---- per-step tables: forcing phase of every member, active quads and tiles of every group ----
@@ -520,6 +522,8 @@ struct odis_batch {
     int* d_base = nullptr;
     double* d_part = nullptr;
     unsigned* d_bar = nullptr;           // [0] count, [1] generation
+    bool use_graph = true;               // runs replay their chunk launches from one CUDA graph
+    long long graph_runs = 0;            // runs executed as one graph launch
     unsigned spin_limit = 0;             // odis_batch_set_wait_limit: polls of a barrier wait (0: kBarrierSpins)
     int withhold = -1;                   // odis_batch_set_wait_limit: CTA that never arrives (-1: none)
     int* d_status = nullptr;
@@ -543,6 +547,11 @@ struct odis_batch {
 static const void* batch_kernel(int v)
 {
     return v == 0 ? (const void*)k_batch<1> : v == 1 ? (const void*)k_batch<2> : (const void*)k_batch<4>;
+}
+
+static void (*batch_kernel_fn(int v))(BatchArgs, int, int)
+{
+    return v == 0 ? k_batch<1> : v == 1 ? k_batch<2> : k_batch<4>;
 }
 
 static int zero_state(odis_batch* b)
@@ -881,21 +890,53 @@ extern "C" odis_status odis_batch_run(odis_batch* b, double orbits, int steps, d
         a.spin_limit = b->spin_limit ? b->spin_limit : kBarrierSpins;
         a.withhold = b->withhold;
         const size_t smem = (sizeof(double) + 2 * sizeof(float)) * (size_t)b->P;
-        // steps j = 0 .. smax: the last one only records the power of the final state
-        for (int j0 = 0; j0 <= smax && st == ODIS_OK; j0 += chunk) {
-            int j1 = std::min(smax + 1, j0 + chunk);
-            void* args[] = {&a, &j0, &j1};
-            if (cudaLaunchCooperativeKernel(batch_kernel(b->variant), dim3(b->grid), dim3(kBatchThreads), args, smem, s) !=
-                cudaSuccess) { st = ODIS_ERR_CUDA; break; }
-            b->launches++;
-            int h = 0;
-            // stop at the first chunk that gave up on a barrier; a member that went
-            // non-finite is reported at the end while the others run on
-            if (cudaMemcpyAsync(&h, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-                cudaStreamSynchronize(s) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
-            if (h & (1 << ODIS_ERR_TIMEOUT)) st = ODIS_ERR_TIMEOUT;
-            else if (h & (1 << ODIS_ERR_NONFINITE)) nonfinite = true;
+        // steps j = 0 .. smax (the last one only records the power of the final state), in
+        // cooperative launches of `chunk` steps.  The whole run is one CUDA graph: the chunks'
+        // launches are captured in stream order and replayed by one cudaGraphLaunch; a chunk
+        // that starts after a barrier wait ran out returns at once (the kernel reads the status
+        // word on entry), and a member that went non-finite is reported while the others run on.
+        void (*kern)(BatchArgs, int, int) = batch_kernel_fn(b->variant);
+        auto launch_chunk = [&](int j0, int j1) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(b->grid);
+            cfg.blockDim = dim3(kBatchThreads);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeCooperative;
+            attr[0].val.cooperative = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            return cudaLaunchKernelEx(&cfg, kern, a, j0, j1);
+        };
+        int nchunks = 0;
+        for (int j0 = 0; j0 <= smax; j0 += chunk) nchunks++;
+        bool graphed = false;
+        if (b->use_graph) {
+            cudaGraph_t gr = nullptr;
+            cudaGraphExec_t ge = nullptr;
+            bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (ok) {
+                for (int j0 = 0; j0 <= smax; j0 += chunk) ok = launch_chunk(j0, std::min(smax + 1, j0 + chunk)) == cudaSuccess && ok;
+                ok = cudaStreamEndCapture(s, &gr) == cudaSuccess && ok;
+            }
+            ok = ok && cudaGraphInstantiate(&ge, gr, 0) == cudaSuccess;
+            ok = ok && cudaGraphLaunch(ge, s) == cudaSuccess;
+            if (ge) cudaGraphExecDestroy(ge);       // freed once the launch completes
+            if (gr) cudaGraphDestroy(gr);
+            if (ok) { graphed = true; b->graph_runs++; }
+            else { (void)cudaGetLastError(); b->use_graph = false; }   // plain launches from now on
         }
+        if (!graphed)
+            for (int j0 = 0; j0 <= smax; j0 += chunk)
+                if (launch_chunk(j0, std::min(smax + 1, j0 + chunk)) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
+        if (st != ODIS_OK) break;
+        b->launches += nchunks;
+        int h = 0;
+        if (cudaMemcpyAsync(&h, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
+        if (h & (1 << ODIS_ERR_TIMEOUT)) st = ODIS_ERR_TIMEOUT;
+        else if (h & (1 << ODIS_ERR_NONFINITE)) nonfinite = true;
         if (st != ODIS_OK) break;
         if (step_power && cudaMemcpyAsync(step_power, d_sp, sp_n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
         if (orbit_power && cudaMemcpyAsync(orbit_power, d_op, op_n * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) { st = ODIS_ERR_CUDA; break; }
@@ -1144,6 +1185,13 @@ extern "C" odis_status odis_batch_set_mesh_members(odis_batch* b, int mesh, cons
         }
         for (int k : here) b->base[b->slot_of[mem[k]]] = 0;
     }
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_batch_graph_runs(const odis_batch* b, long long* runs)
+{
+    if (!b || !runs) return ODIS_ERR_ARG;
+    *runs = b->graph_runs;
     return ODIS_OK;
 }
 

@@ -421,6 +421,10 @@ odis_status odis_batch_set_mesh_members(odis_batch* b, int mesh, const double* v
 odis_status odis_batch_project(odis_batch* b, int mesh, const float* basis_v, int kv, const float* basis_eta, int ke,
                                double* out, int out_stride);
 
+/* Runs so far that executed as one CUDA graph launch (every run captures its
+ * chunks' cooperative launches in one graph and replays it; a device that
+ * refuses the capture gets plain launches). */
+odis_status odis_batch_graph_runs(const odis_batch* b, long long* runs);
 /* The batch kernel's grid barriers, as odis_set_wait_limit: each wait gives
  * up after `polls` polls (0: the default, about a second) and odis_batch_run
  * returns ODIS_ERR_TIMEOUT; withhold >= 0 makes that CTA never arrive. */

@@ -166,3 +166,41 @@ def test_cli_nonlinear_run(built, tmp_path, precision):
     assert ds["displacement"].shape == (2, mesh.n_cells)
     last = ds["displacement"].read()[1]
     assert np.max(np.abs(last - eta.astype(np.float32))) <= 1e-6 * np.max(np.abs(eta))
+
+
+@pytest.mark.gpu
+def test_cli_sigint_checkpoint_and_exact_resume(built, tmp_path):
+    """SIGINT (CatchExit, src/timeIntegrator.cpp:32-37, 307-316): the run stops within one step chunk, writes
+    "Terminate signal caught..." to OUTPUT.txt, saves InitialConditions (the reference's text files and the
+    exact FP64 state.bin) and exits with status 1.  --resume continues from state.bin and ends on the same
+    state bits as an uninterrupted run of the same length."""
+    import signal
+    import struct
+    orbits = "100"
+    a = _rundir(tmp_path / "a")
+    r = subprocess.run([str(CLI), "--dir", str(a), "--orbits", orbits], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    b = _rundir(tmp_path / "b")
+    p = subprocess.Popen([str(CLI), "--dir", str(b), "--orbits", orbits], stdout=subprocess.PIPE,
+                         stderr=subprocess.PIPE, text=True)
+    seen = 0
+    for line in p.stdout:
+        seen += line.startswith("DUMPING DATA AT")
+        if seen == 4:                         # the initial dump and three orbits
+            p.send_signal(signal.SIGINT)
+            break
+    out, err = p.communicate(timeout=600)
+    assert p.returncode == 1, err
+    assert "Caught Terminate Signal..." in out and "Terminate signal caught..." in out
+    assert "Terminate signal caught..." in (b / "OUTPUT.txt").read_text()
+    ckp = (b / "InitialConditions" / "state.bin").read_bytes()
+    assert ckp[:8] == b"ODISCKP1"
+    steps_done = struct.unpack("<q", ckp[8:16])[0]
+    assert 0 < steps_done < 100 * 2000
+    assert (b / "InitialConditions" / "vel_init.txt").exists()
+    r = subprocess.run([str(CLI), "--dir", str(b), "--orbits", orbits, "--resume"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    ca = (a / "InitialConditions" / "state.bin").read_bytes()
+    cb = (b / "InitialConditions" / "state.bin").read_bytes()
+    assert struct.unpack("<q", ca[8:16])[0] == struct.unpack("<q", cb[8:16])[0] == 100 * 2000
+    assert ca == cb

@@ -155,3 +155,18 @@ def test_batch_bulk_state_and_projection(grid_dir):
         assert rel_err(v2, 2 * v) < 1e-12 and rel_err(eta2, 3 * eta) < 1e-12
         assert all(b.get_member(int(i))[0] == 0 for i in idx)
     b.close()
+
+
+def test_batch_run_is_one_graph_launch(grid_dir):
+    """Every run replays its chunks' cooperative launches from one CUDA graph; chunking changes nothing."""
+    g, O, angvel, P, paths, meshes, members, common = _setup(grid_dir, count=6, seed=9)
+    b = g.Batch(common, meshes, members)
+    b.run(steps=500, chunk=64)                     # 8 chunks
+    info = b.info()
+    assert info["graph_runs"] == 1 and info["launches"] == 8
+    c = g.Batch(common, meshes, members)
+    c.run(steps=500, chunk=1000)
+    for i in range(len(members)):
+        np.testing.assert_array_equal(b.get_member(i)[1], c.get_member(i)[1])
+    b.close()
+    c.close()
