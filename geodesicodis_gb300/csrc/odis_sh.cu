@@ -3,22 +3,31 @@
 // Storage: the real harmonic Y_lm(cos|sin) = Pbar_lm(sin lat) * (cos|sin)(m lon)
 // is never stored.  Each cell keeps the (L+1)(L+2)/2 normalised Legendre values
 // Pbar_lm in rows ordered by order m (P[row(l,m)][Np]) plus cos(m lon) and
-// sin(m lon) rows; at level 6 with L = 16 that is 187 rows (61 MB in FP64/DF64)
-// instead of 289 rows of Y, small enough to stay L2-resident next to the
-// stencil data across steps.
+// sin(m lon) rows: 187 rows at L = 16 instead of 289 rows of Y.
+//
+// Half basis.  On a centrally symmetric mesh every cell a has an antipodal
+// partner b (x_b = -x_a: lat -> -lat, lon -> lon + pi), and there
+// Pbar_lm(-z) cos|sin(m (lon + pi)) = (-1)^(l+m) (-1)^m Y_lm = (-1)^l Y_lm.
+// The rows are then stored for one cell of each pair only (half the bytes:
+// 31 MB in FP64/DF64 at level 6), and
+//   analysis  t_lm = sum_a Y_lm(a) (eta_a + (-1)^l eta_b)
+//   synthesis usg_a = E + O, usg_b = E - O  (E, O: the even- and odd-degree sums at a)
+// halve the multiply-adds of both transforms.  Without the symmetry (or with
+// ODIS_SH_HALF=0) the full basis is used.
 //
 // Per step:
+//   k_sh_pair:     e = eta_a + eta_b, o = eta_a - eta_b per pair (half basis only)
 //   k_sh_analysis: blocks of (order m, up to 8 degrees, chunk of cells);
-//                  partial sums of Pbar_lm * (cos|sin)(m lon) * eta per chunk
-//   k_sh_fold:     t_k = fixed-order sum of the chunk partials
+//                  partial sums of Pbar_lm * (cos|sin)(m lon) * eta (or e / o) per
+//                  chunk; the last block of each tile folds its chunk partials
 //   k_sh_coef:     c = F (Y^T Y)^-1 t  (least squares as SHExpandLSQ, factors F)
 //   k_sh_synth:    usg_i = sum_m cos(m lon) sum_l Pbar_lm c_lm,cos + sin(m lon) sum_l Pbar_lm c_lm,sin
-//                  with cos/sin(m lon) advanced by angle addition in registers
 // The Legendre values are computed in FP64 on the host (three-term recurrences
 // of the fully normalised functions, Holmes & Featherstone 2002), the Gram
-// matrix Y^T Y in FP64 on the device, its inverse in FP64 (Cholesky) on the
-// host.  The arithmetic of the per-step transforms follows the method: FP64,
-// double-float (DF64) or FP32 (FP32-state variant; block sums in FP64).
+// matrix Y^T Y in FP64 on the device over all cells, its inverse in FP64
+// (Cholesky) on the host.  The arithmetic of the per-step transforms follows
+// the method: FP64, double-float (DF64) or FP32 (FP32-state variant; block sums
+// in FP64).
 #include "odis_sh.cuh"
 #include "odis_sh_tc.cuh"
 #include "odis_df64.cuh"
@@ -74,11 +83,17 @@ void plm_bar(int L, double z, std::vector<double>& P)
 // row stride Np), and `eta` holds e = eta_a + eta_b in [0, Np) and
 // o = eta_a - eta_b in [Np, 2 Np); since Y_lm(-x) = (-1)^l Y_lm(x), even
 // degrees sum Y_lm e and odd degrees Y_lm o over the half set.
+//
+// The last of a tile's nchunk blocks to finish (a per-tile arrival counter,
+// reset by that block for the next step) folds the tile's coefficients over
+// the chunks into t in FP64, in the fixed order of k_sh_fold: the result does
+// not depend on which block comes last, and the step needs no fold launch.
 template <class T, int kTileL, bool kHalf>
 __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict__ P, const T* __restrict__ trig,
                                                             const T* __restrict__ eta, int N, int Np, int L,
                                                             const int* __restrict__ tiles, int nchunk,
-                                                            T* __restrict__ part)
+                                                            T* __restrict__ part, unsigned* __restrict__ arrivals,
+                                                            double* __restrict__ t)
 {
     pdl_wait();
     using A = Ar<T>;
@@ -169,6 +184,25 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
         const int j = threadIdx.x >> 1, is_sin = threadIdx.x & 1;
         if (m > 0 || !is_sin) part[(size_t)sh_col(l0 + j, m, is_sin) * nchunk + chunk] = s;
     }
+    // publish the partials, then count this block in
+    __threadfence();
+    __syncthreads();
+    __shared__ bool s_last;
+    if (threadIdx.x == 0) s_last = atomicAdd(&arrivals[blockIdx.x], 1u) == (unsigned)(nchunk - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int q = wid; q < 2 * nl; q += kShThreads / 32) {       // one warp per coefficient of the tile
+        const int j = q >> 1, is_sin = q & 1;
+        if (m == 0 && is_sin) continue;
+        const int k = sh_col(l0 + j, m, is_sin);
+        double x = 0.0;
+        for (int c = lane; c < nchunk; c += 32) x += A::to(A::ldcg(&part[(size_t)k * nchunk + c]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) t[k] = x;
+    }
+    if (threadIdx.x == 0) arrivals[blockIdx.x] = 0u;             // ready for the next step
 }
 
 // e and o of the antipodal pairs (kHalf transforms): eo[h] = eta[ia[h]] + eta[ib[h]],
@@ -396,6 +430,7 @@ struct ShLoading {
     int* ia = nullptr;           // [Nhp] (padding repeats the last pair)
     int* ib = nullptr;
     void* eo = nullptr;          // [2][Nhp] e = eta_a + eta_b, o = eta_a - eta_b, method type
+    unsigned* arrivals = nullptr; // [analysis tiles] blocks of a tile that finished this step (reset by the last)
     // cells and row stride of the stored basis
     int bn() const { return half ? Nh : N; }
     int bp() const { return half ? Nhp : Np; }
@@ -614,6 +649,9 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
     ok = ok && cudaMalloc(&s->FGinv, sizeof(double) * G.size()) == cudaSuccess &&
          cudaMemcpy(s->FGinv, G.data(), sizeof(double) * G.size(), cudaMemcpyHostToDevice) == cudaSuccess;
     ok = ok && cudaMalloc(&s->t, sizeof(double) * K) == cudaSuccess && cudaMalloc(&s->coef, 8 * (size_t)K) == cudaSuccess;
+    // arrival counters: one per analysis tile, at most (L+1)^2 tiles (one degree per tile)
+    ok = ok && cudaMalloc(&s->arrivals, sizeof(unsigned) * (size_t)K) == cudaSuccess &&
+         cudaMemset(s->arrivals, 0, sizeof(unsigned) * (size_t)K) == cudaSuccess;
     if (!ok) { sh_destroy(s); return ODIS_ERR_NOMEM; }
     if (precision == ODIS_FP32 && !s->half) {
         double pmax = 0.0;
@@ -632,7 +670,7 @@ void sh_destroy(ShLoading* s)
     if (!s) return;
     cudaFree(s->P); cudaFree(s->trig); cudaFree(s->tiles); cudaFree(s->part); cudaFree(s->FGinv);
     cudaFree(s->t); cudaFree(s->coef); cudaFree(s->usg);
-    cudaFree(s->ia); cudaFree(s->ib); cudaFree(s->eo);
+    cudaFree(s->ia); cudaFree(s->ib); cudaFree(s->eo); cudaFree(s->arrivals);
     shtc_destroy(s->tc);
     delete s;
 }
@@ -662,21 +700,23 @@ static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int nt
     const T* P = (const T*)s->P;
     const T* trig = (const T*)s->trig;
     T* part = (T*)s->part;
+    unsigned* arr = s->arrivals;
+    double* tt = s->t;
     const int n = s->bn(), np = s->bp();
     if (s->half) {
         T* eo = (T*)s->eo;
         pdl_launch(k_sh_pair<T>, (np + 255) / 256, 256, 0, st, (const T*)eta, (const int*)s->ia, (const int*)s->ib, n,
                    np, eo);
         const T* e = eo;
-        if (tl == 2) pdl_launch(k_sh_analysis<T, 2, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
-        else if (tl == 4) pdl_launch(k_sh_analysis<T, 4, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
-        else pdl_launch(k_sh_analysis<T, 8, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
+        if (tl == 2) pdl_launch(k_sh_analysis<T, 2, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
+        else if (tl == 4) pdl_launch(k_sh_analysis<T, 4, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
+        else pdl_launch(k_sh_analysis<T, 8, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
         return;
     }
     const T* e = (const T*)eta;
-    if (tl == 2) pdl_launch(k_sh_analysis<T, 2, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
-    else if (tl == 4) pdl_launch(k_sh_analysis<T, 4, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
-    else pdl_launch(k_sh_analysis<T, 8, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part);
+    if (tl == 2) pdl_launch(k_sh_analysis<T, 2, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
+    else if (tl == 4) pdl_launch(k_sh_analysis<T, 4, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
+    else pdl_launch(k_sh_analysis<T, 8, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
 }
 
 template <class T>
@@ -848,8 +888,7 @@ static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st)
             return;
         }
     }
-    launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, eta, st);
-    pdl_launch(k_sh_fold<T>, (s->K + 3) / 4, 128, 0, st, (const T*)s->part, s->K, s->nchunk, s->t);
+    launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, eta, st);      // partials and their fold
     pdl_launch(k_sh_coef<T>, s->K, 32, 0, st, s->t, s->K, s->FGinv, (T*)s->coef);
     launch_synth<T>(s, s->lanes, s->cells, st);
 }
@@ -861,7 +900,7 @@ void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)
     else enqueue_t<float>(s, eta, st);
 }
 
-int sh_kernels_per_step(const ShLoading* s) { return s && s->use_tc ? shtc_kernels_per_step() : (s && s->half ? 5 : 4); }
+int sh_kernels_per_step(const ShLoading* s) { return s && s->use_tc ? shtc_kernels_per_step() : (s && s->half ? 4 : 3); }
 
 void sh_layout(const ShLoading* s, int* half, int* cells, long long* basis_bytes)
 {
