@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
 {
     pdl_wait();
     using A = Ar<T>;
-    __shared__ T red[kShThreads / 32][2 * kTileL];
+    // per-thread sums of the block's tile, [coefficient][thread]: 32 KB for 8 degrees in FP64
+    __shared__ T red[2 * kTileL][kShThreads];
     const int m = tiles[3 * blockIdx.x], l0 = tiles[3 * blockIdx.x + 1], nl = tiles[3 * blockIdx.x + 2];
     const int chunk = blockIdx.y;
     // chunk bounds are even, so cell pairs (i, i+1) stay inside one chunk and are 2-aligned
@@ -168,21 +169,22 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
         as[j] = A::add(A::norm(as[j]), A::norm(bs[j]));
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // block sum of each of the tile's 2 nl coefficients: every thread parks its sums in shared
+    // memory, then one warp per coefficient adds eight values per lane and a shuffle tree --
+    // a fixed order, and a third of the additions of a per-warp shuffle tree of every sum
 #pragma unroll
     for (int j = 0; j < kTileL; j++) {
-        if (j < nl) {
-            T c = ac[j], s = as[j];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) { c = A::add(c, A::shfl(c, o)); s = A::add(s, A::shfl(s, o)); }
-            if (lane == 0) { red[wid][2 * j] = c; red[wid][2 * j + 1] = s; }
-        }
+        if (j < nl) { red[2 * j][threadIdx.x] = ac[j]; red[2 * j + 1][threadIdx.x] = as[j]; }
     }
     __syncthreads();
-    if (threadIdx.x < 2 * nl) {
-        T s = A::zero();
-        for (int w = 0; w < kShThreads / 32; w++) s = A::add(s, red[w][threadIdx.x]);
-        const int j = threadIdx.x >> 1, is_sin = threadIdx.x & 1;
-        if (m > 0 || !is_sin) part[(size_t)sh_col(l0 + j, m, is_sin) * nchunk + chunk] = s;
+    for (int q = wid; q < 2 * nl; q += kShThreads / 32) {
+        T x = red[q][lane];
+#pragma unroll
+        for (int r = 1; r < kShThreads / 32; r++) x = A::add(x, red[q][lane + 32 * r]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x = A::add(x, A::shfl(x, o));
+        const int j = q >> 1, is_sin = q & 1;
+        if (lane == 0 && (m > 0 || !is_sin)) part[(size_t)sh_col(l0 + j, m, is_sin) * nchunk + chunk] = x;
     }
     // publish the partials, then count this block in
     __threadfence();
