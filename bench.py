@@ -308,7 +308,7 @@ def run_ours(args) -> dict:
     clocks = ClockSampler()
     clocks.start()
     main_sol = solver(g.FP64, LMAX)
-    tiles = dict(zip(("tile_l", "chunks", "lanes"), main_sol.sh_tiles()))
+    tiles = dict(zip(("tile_l", "chunks", "lanes", "cells", "pre"), main_sol.sh_tuning()))
     layout = main_sol.sh_layout()
     t_main, launches = timed_orbits(main_sol, args.steps, args.warmup)
     clk = clocks.stop()
@@ -335,7 +335,7 @@ def run_ours(args) -> dict:
         if key != "fp64_sh16":
             results[key] = N * n * kv / t
         if lmax:
-            extra[key] = {"sh_tiles": list(s.sh_tiles()), "sh_layout": s.sh_layout()}
+            extra[key] = {"sh_tiles": list(s.sh_tuning()), "sh_layout": s.sh_layout()}
         if key == "df64_sh16":
             # the double-float method end to end, on its own context as the headline
             extra[key]["e2e"] = run_e2e(s, stream, flush, args, n, N, E, barrier, max_over_ranks, world,
@@ -595,7 +595,7 @@ def run_level8(args) -> dict:
             "us_per_step": el / args.case_steps * 1e6, "cell_steps_per_s": N * args.case_steps / el,
             "face_us": ms[0] * 1e3, "cell_us": ms[1] * 1e3, "sh_us": ms[2] * 1e3,
             "face_hbm_frac": fb / (ms[0] * 1e-3) / 1e9 / peak, "cell_hbm_frac": cb / (ms[1] * 1e-3) / 1e9 / peak,
-            "sh_tiles": list(s.sh_tiles()) if lmax else None}
+            "sh_tiles": list(s.sh_tuning()) if lmax else None}
         s.close()
     for a, b in (("fp32_sh32", "fp64_sh32"), ("fp32_sh32_tc", "fp64_sh32"), ("df64_sh32", "fp64_sh32"),
                  ("fp32_plain", "fp64_plain"), ("df64_advection", "fp64_advection")):

@@ -114,7 +114,7 @@ _SIGS = {
     "odis_batch_graph_runs": ([_V, C.POINTER(C.c_longlong)], C.c_int),
     "odis_profile_kernels": ([_V, C.c_int, _D], C.c_int),
     "odis_set_persistent": ([_V, C.c_int, _I], C.c_int),
-    "odis_sh_tiles": ([_V, _I, _I, _I], C.c_int),
+    "odis_sh_tiles": ([_V, _I, _I, _I, _I, _I], C.c_int),
     "odis_sh_layout": ([_V, _I, _I, C.POINTER(C.c_longlong)], C.c_int),
     "odis_batch_create": ([C.POINTER(Params), C.POINTER(_V), C.c_int, _V, C.c_int, C.POINTER(_V)], C.c_int),
     "odis_batch_destroy": ([_V], None),
@@ -467,9 +467,13 @@ class Solver:
 
     def sh_tiles(self) -> tuple:
         """(tile_l, chunks, lanes) of the self-gravity transforms chosen at creation."""
-        a, b, c = C.c_int(), C.c_int(), C.c_int()
-        _ck(lib().odis_sh_tiles(self._h, C.byref(a), C.byref(b), C.byref(c)), "odis_sh_tiles")
-        return a.value, b.value, c.value
+        return self.sh_tuning()[:3]
+
+    def sh_tuning(self) -> tuple:
+        """(tile_l, chunks, lanes, cells, pre) of the self-gravity transforms chosen at creation."""
+        a, b, c, d, e = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _ck(lib().odis_sh_tiles(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d), C.byref(e)), "odis_sh_tiles")
+        return a.value, b.value, c.value, d.value, e.value
 
     def sh_layout(self) -> dict:
         """Self-gravity basis storage: antipodal half basis or full, cells covered, bytes per transform."""

@@ -1396,14 +1396,16 @@ extern "C" odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms)
     return st;
 }
 
-extern "C" odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes)
+extern "C" odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes, int* cells, int* pre)
 {
     if (!c) return ODIS_ERR_ARG;
-    int a = 0, b = 0, d = 0;
-    if (c->sh) sh_tuning(c->sh, &a, &b, &d);
+    int a = 0, b = 0, d = 0, e = 0, f = 0;
+    if (c->sh) sh_tuning(c->sh, &a, &b, &d, &e, &f);
     if (tile_l) *tile_l = a;
     if (chunks) *chunks = b;
     if (lanes) *lanes = d;
+    if (cells) *cells = e;
+    if (pre) *pre = f;
     return ODIS_OK;
 }
 

@@ -49,6 +49,8 @@ namespace {
 constexpr double kPi = 3.1415926535897932384626433832795028841971693993751058;
 constexpr int kShThreads = 256;
 constexpr int kSynthThreads = 128;
+constexpr int kSynthPairs = 16;    // "lanes" value that selects the warp-per-order-pair synthesis
+constexpr int kSynthMaxWarps = 17; // its warps per block (l_max 32 has 17 order pairs; more pairs share warps)
 constexpr int kMaxChunks = 64;     // largest cell-chunk count the autotuner tries
 
 // fully normalised (4pi) associated Legendre functions with the Condon-Shortley
@@ -83,12 +85,16 @@ void plm_bar(int L, double z, std::vector<double>& P)
 // row stride Np), and `eta` holds e = eta_a + eta_b in [0, Np) and
 // o = eta_a - eta_b in [Np, 2 Np); since Y_lm(-x) = (-1)^l Y_lm(x), even
 // degrees sum Y_lm e and odd degrees Y_lm o over the half set.
+// kPre: `eta` holds the trig-weighted values of every order, written once per
+// step by k_sh_prep (rows 4m..4m+3: cos e, sin e, cos o, sin o with the half
+// basis; rows 2m, 2m+1: cos eta, sin eta with the full one), so the loop is
+// multiply-adds only; otherwise each tile forms those products itself.
 //
 // The last of a tile's nchunk blocks to finish (a per-tile arrival counter,
 // reset by that block for the next step) folds the tile's coefficients over
 // the chunks into t in FP64, in the fixed order of k_sh_fold: the result does
 // not depend on which block comes last, and the step needs no fold launch.
-template <class T, int kTileL, bool kHalf>
+template <class T, int kTileL, bool kHalf, bool kPre>
 __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict__ P, const T* __restrict__ trig,
                                                             const T* __restrict__ eta, int N, int Np, int L,
                                                             const int* __restrict__ tiles, int nchunk,
@@ -116,18 +122,31 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
 #pragma unroll 2
     for (; i + 1 < i1; i += 2 * kShThreads) {
         {
-            T e, e2, c1, c2, s1, s2;
-            A::ld2(eta + i, e, e2);
-            A::ld2(cm + i, c1, c2);
-            A::ld2(sm + i, s1, s2);
-            const T ec = A::mul(c1, e), es = A::mul(s1, e);
-            const T ec2 = A::mul(c2, e2), es2 = A::mul(s2, e2);
-            T oc = ec, os = es, oc2 = ec2, os2 = es2;
-            if constexpr (kHalf) {
-                T o, o2;
-                A::ld2(eta + Np + i, o, o2);
-                oc = A::mul(c1, o); os = A::mul(s1, o);
-                oc2 = A::mul(c2, o2); os2 = A::mul(s2, o2);
+            T ec, es, ec2, es2, oc, os, oc2, os2;
+            if constexpr (kPre) {
+                const T* xm = eta + (size_t)(kHalf ? 4 * m : 2 * m) * Np;
+                A::ld2(xm + i, ec, ec2);
+                A::ld2(xm + Np + i, es, es2);
+                if constexpr (kHalf) {
+                    A::ld2(xm + 2 * (size_t)Np + i, oc, oc2);
+                    A::ld2(xm + 3 * (size_t)Np + i, os, os2);
+                } else {
+                    oc = ec; os = es; oc2 = ec2; os2 = es2;
+                }
+            } else {
+                T e, e2, c1, c2, s1, s2;
+                A::ld2(eta + i, e, e2);
+                A::ld2(cm + i, c1, c2);
+                A::ld2(sm + i, s1, s2);
+                ec = A::mul(c1, e); es = A::mul(s1, e);
+                ec2 = A::mul(c2, e2); es2 = A::mul(s2, e2);
+                oc = ec; os = es; oc2 = ec2; os2 = es2;
+                if constexpr (kHalf) {
+                    T o, o2;
+                    A::ld2(eta + Np + i, o, o2);
+                    oc = A::mul(c1, o); os = A::mul(s1, o);
+                    oc2 = A::mul(c2, o2); os2 = A::mul(s2, o2);
+                }
             }
 #pragma unroll
             for (int j = 0; j < kTileL; j++) {
@@ -145,12 +164,20 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
     }
     if (i < i1) {           // the last cell of an odd-length final chunk
         {
-            const T e = eta[i];
-            const T ec = A::mul(cm[i], e), es = A::mul(sm[i], e);
-            T oc = ec, os = es;
-            if constexpr (kHalf) {
-                const T o = eta[Np + i];
-                oc = A::mul(cm[i], o); os = A::mul(sm[i], o);
+            T ec, es, oc, os;
+            if constexpr (kPre) {
+                const T* xm = eta + (size_t)(kHalf ? 4 * m : 2 * m) * Np;
+                ec = xm[i]; es = xm[Np + i];
+                oc = ec; os = es;
+                if constexpr (kHalf) { oc = xm[2 * (size_t)Np + i]; os = xm[3 * (size_t)Np + i]; }
+            } else {
+                const T e = eta[i];
+                ec = A::mul(cm[i], e); es = A::mul(sm[i], e);
+                oc = ec; os = es;
+                if constexpr (kHalf) {
+                    const T o = eta[Np + i];
+                    oc = A::mul(cm[i], o); os = A::mul(sm[i], o);
+                }
             }
 #pragma unroll
             for (int j = 0; j < kTileL; j++) {
@@ -225,6 +252,45 @@ __global__ void __launch_bounds__(256) k_sh_pair(const T* __restrict__ eta, cons
     }
     eo[h] = e;
     eo[Np + h] = o;
+}
+
+// trig-weighted values of every order for the kPre analysis, one cell per thread:
+// half basis x[4m..4m+3][h] = (cos e, sin e, cos o, sin o)(m lon_h) with
+// e, o = eta_a +- eta_b; full basis x[2m], x[2m+1] = (cos, sin)(m lon_i) eta_i;
+// zero on the padding
+template <class T, bool kHalf>
+__global__ void __launch_bounds__(256) k_sh_prep(const T* __restrict__ eta, const int* __restrict__ ia,
+                                                 const int* __restrict__ ib, const T* __restrict__ trig, int N,
+                                                 int Np, int L, T* __restrict__ x)
+{
+    pdl_wait();
+    using A = Ar<T>;
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= Np) return;
+    T e = A::zero(), o = A::zero();
+    if (h < N) {
+        if constexpr (kHalf) {
+            const T a = eta[ia[h]], b = eta[ib[h]];
+            e = A::add(a, b);
+            o = A::sub(a, b);
+        } else {
+            e = eta[h];
+        }
+    }
+    for (int m = 0; m <= L; m++) {
+        const T c = trig[(size_t)(2 * m) * Np + h], sn = trig[(size_t)(2 * m + 1) * Np + h];
+        if constexpr (kHalf) {
+            T* xm = x + (size_t)(4 * m) * Np + h;
+            xm[0] = A::mul(c, e);
+            xm[(size_t)Np] = A::mul(sn, e);
+            xm[2 * (size_t)Np] = A::mul(c, o);
+            xm[3 * (size_t)Np] = A::mul(sn, o);
+        } else {
+            T* xm = x + (size_t)(2 * m) * Np + h;
+            xm[0] = A::mul(c, e);
+            xm[(size_t)Np] = A::mul(sn, e);
+        }
+    }
 }
 
 // t_k = sum over the chunk partials of coefficient k in FP64, one warp per
@@ -378,6 +444,124 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
     }
 }
 
+// Synthesis with one warp per pair of orders (m, L - m) (the middle order alone
+// for even L): the degree counts of a pair add up to L + 2, so the warps of a
+// block are balanced without splitting an order's degree sum.  A block covers
+// 32 kCells consecutive basis cells (lanes: cells, kCells adjacent cells per
+// lane with one vector load per row); every warp sums its orders for every cell
+// of the block, and the warps' sums meet in shared memory in warp order.  With
+// (L + 2) / 2 warps per block this keeps several times more warps resident than
+// the lane-per-order kernel, whose per-cell thread count the half basis halves.
+template <class T, int kCells, bool kHalf>
+__global__ void __launch_bounds__(kSynthMaxWarps * 32) k_sh_synth_m(const T* __restrict__ P, const T* __restrict__ trig,
+                                                     const T* __restrict__ coef, int N, int Np, int L, int K,
+                                                     const int* __restrict__ ia, const int* __restrict__ ib,
+                                                     T* __restrict__ usg)
+{
+    pdl_wait();
+    using A = Ar<T>;
+    extern __shared__ unsigned char c_raw[];
+    T* c = reinterpret_cast<T*>(c_raw);
+    T* red = c + ((K + 1) & ~1);               // [warps][32][4]: u, u2, w, w2 of every lane
+    for (int k = threadIdx.x; k < K; k += blockDim.x) c[k] = coef[k];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int i = (blockIdx.x * 32 + lane) * kCells;
+    const int i2 = kCells == 2 ? min(i + 1, N - 1) : i;
+    const bool pair = kCells == 2 && i2 == i + 1;
+    T u = A::zero(), u2 = A::zero();     // full basis: the sums; kHalf: the even-degree sums E
+    T w = A::zero(), w2 = A::zero();     // kHalf: the odd-degree sums O
+    const int npairs = L / 2 + 1;
+    if (i < N) {
+        for (int pr = wid; pr < npairs; pr += nw)
+            for (int side = 0; side < 2; side++) {
+                const int m = side == 0 ? pr : L - pr;
+                if (side == 1 && m == pr) break;
+                T xa0 = A::zero(), xb0 = A::zero(), xa1 = A::zero(), xb1 = A::zero();
+                T ya0 = A::zero(), yb0 = A::zero(), ya1 = A::zero(), yb1 = A::zero();
+                const int lstart = m < 2 ? 2 : m;
+                const T* prow = P + (size_t)p_row(L, lstart, m) * Np;
+                const T* cr = trig + (size_t)(2 * m) * Np;
+                const T* sr = trig + (size_t)(2 * m + 1) * Np;
+                T c0, c1, s0, s1;
+                if (pair) { A::ld2(cr + i, c0, c1); A::ld2(sr + i, s0, s1); }
+                else { c0 = cr[i]; c1 = cr[i2]; s0 = sr[i]; s1 = sr[i2]; }
+                auto stepx = [&](int l, T p0, T p1, T& a0, T& b0, T& a1, T& b1) {
+                    const T cc = c[sh_col(l, m, 0)];
+                    a0 = A::fma_acc(p0, cc, a0);
+                    if (kCells == 2) a1 = A::fma_acc(p1, cc, a1);
+                    if (m > 0) {
+                        const T cs = c[sh_col(l, m, 1)];
+                        b0 = A::fma_acc(p0, cs, b0);
+                        if (kCells == 2) b1 = A::fma_acc(p1, cs, b1);
+                    }
+                };
+                int l = lstart;
+                for (; l + 3 <= L; l += 4) {            // four rows' loads in flight
+                    T p0[4], p1[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const T* prq = prow + (size_t)(l + q - lstart) * Np;
+                        if (pair) A::ld2(prq + i, p0[q], p1[q]);
+                        else { p0[q] = prq[i]; p1[q] = kCells == 2 ? prq[i2] : p0[q]; }
+                    }
+                    if constexpr (kHalf) {
+                        stepx(l, p0[0], p1[0], xa0, xb0, xa1, xb1);
+                        stepx(l + 1, p0[1], p1[1], ya0, yb0, ya1, yb1);
+                        stepx(l + 2, p0[2], p1[2], xa0, xb0, xa1, xb1);
+                        stepx(l + 3, p0[3], p1[3], ya0, yb0, ya1, yb1);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 4; q++) stepx(l + q, p0[q], p1[q], xa0, xb0, xa1, xb1);
+                    }
+                }
+                for (; l <= L; l++) {
+                    const T* prq = prow + (size_t)(l - lstart) * Np;
+                    T p0, p1;
+                    if (pair) A::ld2(prq + i, p0, p1);
+                    else { p0 = prq[i]; p1 = kCells == 2 ? prq[i2] : p0; }
+                    if (kHalf && ((l - lstart) & 1)) stepx(l, p0, p1, ya0, yb0, ya1, yb1);
+                    else stepx(l, p0, p1, xa0, xb0, xa1, xb1);
+                }
+                if constexpr (kHalf) {
+                    const bool xodd = lstart & 1;
+                    const T ea0 = xodd ? ya0 : xa0, eb0 = xodd ? yb0 : xb0, oa0 = xodd ? xa0 : ya0, ob0 = xodd ? xb0 : yb0;
+                    u = A::fma(c0, A::norm(ea0), A::fma(s0, A::norm(eb0), u));
+                    w = A::fma(c0, A::norm(oa0), A::fma(s0, A::norm(ob0), w));
+                    if (kCells == 2) {
+                        const T ea1 = xodd ? ya1 : xa1, eb1 = xodd ? yb1 : xb1, oa1 = xodd ? xa1 : ya1, ob1 = xodd ? xb1 : yb1;
+                        u2 = A::fma(c1, A::norm(ea1), A::fma(s1, A::norm(eb1), u2));
+                        w2 = A::fma(c1, A::norm(oa1), A::fma(s1, A::norm(ob1), w2));
+                    }
+                } else {
+                    u = A::fma(c0, A::norm(xa0), A::fma(s0, A::norm(xb0), u));
+                    if (kCells == 2) u2 = A::fma(c1, A::norm(xa1), A::fma(s1, A::norm(xb1), u2));
+                }
+            }
+    }
+    T* r = red + (size_t)(wid * 32 + lane) * 4;
+    r[0] = u; r[1] = u2; r[2] = w; r[3] = w2;
+    __syncthreads();
+    if (wid == 0 && i < N) {
+        T su = A::zero(), su2 = A::zero(), sw = A::zero(), sw2 = A::zero();
+        for (int v = 0; v < nw; v++) {
+            const T* x = red + (size_t)(v * 32 + lane) * 4;
+            su = A::add(su, x[0]); su2 = A::add(su2, x[1]); sw = A::add(sw, x[2]); sw2 = A::add(sw2, x[3]);
+        }
+        if constexpr (kHalf) {
+            usg[ia[i]] = A::add(su, sw);
+            usg[ib[i]] = A::sub(su, sw);
+            if (kCells == 2 && i + 1 < N) {
+                usg[ia[i + 1]] = A::add(su2, sw2);
+                usg[ib[i + 1]] = A::sub(su2, sw2);
+            }
+        } else {
+            usg[i] = su;
+            if (kCells == 2 && i + 1 < N) usg[i + 1] = su2;
+        }
+    }
+}
+
 // Gram matrix G = Y^T Y in FP64 (setup only): 32x32 output tiles, lower triangle
 __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ Y, int K, int N, int Np, double* __restrict__ G)
 {
@@ -413,6 +597,7 @@ int sh_autotune(ShLoading* s);
 struct ShLoading {
     int L = 0, K = 0, MP = 0, N = 0, Np = 0, precision = ODIS_FP64, ntiles = 0;
     int tl = 8, nchunk = 16, lanes = 4;   // tile shapes chosen by the autotuner
+    bool pre = false;                     // analysis from trig-weighted values formed once per step
     int cells = 2;                        // synthesis cells per thread
     void* P = nullptr;           // [MP][Np] Legendre rows, method type
     void* trig = nullptr;        // [2(L+1)][Np] cos(m lon), sin(m lon), method type
@@ -431,7 +616,8 @@ struct ShLoading {
     int Nh = 0, Nhp = 0;
     int* ia = nullptr;           // [Nhp] (padding repeats the last pair)
     int* ib = nullptr;
-    void* eo = nullptr;          // [2][Nhp] e = eta_a + eta_b, o = eta_a - eta_b, method type
+    void* eo = nullptr;          // [2][Nhp] e = eta_a + eta_b, o = eta_a - eta_b, or the trig-weighted values
+                                 // [4(L+1)][Nhp] (half) / [2(L+1)][Np] (full) of the pre analysis; method type
     unsigned* arrivals = nullptr; // [analysis tiles] blocks of a tile that finished this step (reset by the last)
     // cells and row stride of the stored basis
     int bn() const { return half ? Nh : N; }
@@ -637,9 +823,11 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
         ok = cudaMalloc(&s->ia, sizeof(int) * s->Nhp) == cudaSuccess &&
              cudaMemcpy(s->ia, ha.data(), sizeof(int) * s->Nhp, cudaMemcpyHostToDevice) == cudaSuccess &&
              cudaMalloc(&s->ib, sizeof(int) * s->Nhp) == cudaSuccess &&
-             cudaMemcpy(s->ib, hb.data(), sizeof(int) * s->Nhp, cudaMemcpyHostToDevice) == cudaSuccess &&
-             cudaMalloc(&s->eo, 2 * 8 * (size_t)s->Nhp) == cudaSuccess &&
-             cudaMemset(s->eo, 0, 2 * 8 * (size_t)s->Nhp) == cudaSuccess;
+             cudaMemcpy(s->ib, hb.data(), sizeof(int) * s->Nhp, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    {   // e/o (half basis) or the pre analysis's trig-weighted values: (4 | 2) (L+1) rows of the basis stride
+        const size_t eo_bytes = (size_t)(s->half ? 4 : 2) * (L + 1) * (s->half ? s->Nhp : Np) * 8;
+        ok = ok && cudaMalloc(&s->eo, eo_bytes) == cudaSuccess && cudaMemset(s->eo, 0, eo_bytes) == cudaSuccess;
     }
     if (precision == ODIS_FP64) ok = ok && upload_rows<double>(&s->P, P) && upload_rows<double>(&s->trig, trig);
     else if (precision == ODIS_DF64) ok = ok && upload_rows<df64>(&s->P, P) && upload_rows<df64>(&s->trig, trig);
@@ -695,8 +883,8 @@ static std::vector<int> make_tiles(int L, int tl)
 }
 
 template <class T>
-static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int ntiles, int nchunk, const void* eta,
-                            cudaStream_t st)
+static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int ntiles, int nchunk, bool pre,
+                            const void* eta, cudaStream_t st)
 {
     const dim3 grid(ntiles, nchunk);
     const T* P = (const T*)s->P;
@@ -705,20 +893,23 @@ static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int nt
     unsigned* arr = s->arrivals;
     double* tt = s->t;
     const int n = s->bn(), np = s->bp();
-    if (s->half) {
-        T* eo = (T*)s->eo;
-        pdl_launch(k_sh_pair<T>, (np + 255) / 256, 256, 0, st, (const T*)eta, (const int*)s->ia, (const int*)s->ib, n,
-                   np, eo);
-        const T* e = eo;
-        if (tl == 2) pdl_launch(k_sh_analysis<T, 2, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
-        else if (tl == 4) pdl_launch(k_sh_analysis<T, 4, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
-        else pdl_launch(k_sh_analysis<T, 8, true>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
-        return;
-    }
     const T* e = (const T*)eta;
-    if (tl == 2) pdl_launch(k_sh_analysis<T, 2, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
-    else if (tl == 4) pdl_launch(k_sh_analysis<T, 4, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
-    else pdl_launch(k_sh_analysis<T, 8, false>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt);
+    if (pre) {            // trig-weighted values of every order, then multiply-adds only
+        T* x = (T*)s->eo;
+        if (s->half) pdl_launch(k_sh_prep<T, true>, (np + 255) / 256, 256, 0, st, e, (const int*)s->ia, (const int*)s->ib, trig, n, np, s->L, x);
+        else pdl_launch(k_sh_prep<T, false>, (np + 255) / 256, 256, 0, st, e, (const int*)s->ia, (const int*)s->ib, trig, n, np, s->L, x);
+        e = x;
+    } else if (s->half) {
+        T* eo = (T*)s->eo;
+        pdl_launch(k_sh_pair<T>, (np + 255) / 256, 256, 0, st, e, (const int*)s->ia, (const int*)s->ib, n, np, eo);
+        e = eo;
+    }
+#define ODIS_ANA(TL, H, PRE) pdl_launch(k_sh_analysis<T, TL, H, PRE>, grid, kShThreads, 0, st, P, trig, e, n, np, s->L, tiles, nchunk, part, arr, tt)
+#define ODIS_ANA_TL(H, PRE) do { if (tl == 2) ODIS_ANA(2, H, PRE); else if (tl == 4) ODIS_ANA(4, H, PRE); else ODIS_ANA(8, H, PRE); } while (0)
+    if (s->half) { if (pre) ODIS_ANA_TL(true, true); else ODIS_ANA_TL(true, false); }
+    else { if (pre) ODIS_ANA_TL(false, true); else ODIS_ANA_TL(false, false); }
+#undef ODIS_ANA_TL
+#undef ODIS_ANA
 }
 
 template <class T>
@@ -737,7 +928,15 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
 #define ODIS_SYNTH_LANES(CL, H) \
     do { if (lanes == 1) ODIS_SYNTH(1, CL, H); else if (lanes == 2) ODIS_SYNTH(2, CL, H); \
          else if (lanes == 4) ODIS_SYNTH(4, CL, H); else ODIS_SYNTH(8, CL, H); } while (0)
-    if (s->half) {
+    if (lanes == kSynthPairs) {            // one warp per pair of orders, 32 * cells cells per block
+        const int nw = std::min(s->L / 2 + 1, kSynthMaxWarps);
+        const int nb = (n + 32 * cells - 1) / (32 * cells);
+        const size_t smp = sizeof(T) * ((size_t)((s->K + 1) & ~1) + (size_t)nw * 32 * 4);
+#define ODIS_SYNTH_M(CL, H) pdl_launch(k_sh_synth_m<T, CL, H>, nb, nw * 32, smp, st, P, trig, c, n, np, s->L, s->K, ia, ib, u)
+        if (s->half) { if (cells == 2) ODIS_SYNTH_M(2, true); else ODIS_SYNTH_M(1, true); }
+        else { if (cells == 2) ODIS_SYNTH_M(2, false); else ODIS_SYNTH_M(1, false); }
+#undef ODIS_SYNTH_M
+    } else if (s->half) {
         if (cells == 2) ODIS_SYNTH_LANES(2, true); else ODIS_SYNTH_LANES(1, true);
     } else {
         if (cells == 2) ODIS_SYNTH_LANES(2, false); else ODIS_SYNTH_LANES(1, false);
@@ -751,20 +950,23 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
 // and the fastest is kept.  Results do not depend on the choice of the
 // synthesis lanes; the analysis's chunking changes only the order of the
 // partial sums.
-// ODIS_SH_TILES="tile_l,chunks,lanes[,cells]" (tile_l in {2,4,8}, chunks in
-// {8,16,32,64}, lanes in {1,2,4,8}, synthesis cells per thread in {1,2}, default
-// 2) fixes the tiles instead of timing them, e.g. to reproduce a run bit for bit
-// or to profile a given variant.  Anything else is ignored.
+// ODIS_SH_TILES="tile_l,chunks,lanes[,cells[,pre]]" (tile_l in {2,4,8}, chunks in
+// {8,16,32,64}, lanes in {1,2,4,8} threads per cell splitting the orders, or 16
+// for one warp per pair of orders (k_sh_synth_m), synthesis cells per thread in
+// {1,2}, default 2, pre = 1 for the analysis from trig-weighted values formed
+// once per step, default 0) fixes the tiles instead of timing them, e.g. to
+// reproduce a run bit for bit or to profile a given variant.  Anything else is
+// ignored.
 static bool forced_tiles(int* f)
 {
     const char* e = std::getenv("ODIS_SH_TILES");
     if (!e) return false;
-    int a = 0, b = 0, c = 0, d = 2;
-    const int n = std::sscanf(e, "%d,%d,%d,%d", &a, &b, &c, &d);
-    if (n != 3 && n != 4) return false;
+    int a = 0, b = 0, c = 0, d = 2, pre = 0;
+    const int n = std::sscanf(e, "%d,%d,%d,%d,%d", &a, &b, &c, &d, &pre);
+    if (n < 3 || n > 5 || (pre != 0 && pre != 1)) return false;
     const bool ok = (a == 2 || a == 4 || a == 8) && (b == 8 || b == 16 || b == 32 || b == 64) &&
-                    (c == 1 || c == 2 || c == 4 || c == 8) && (d == 1 || d == 2);
-    if (ok) { f[0] = a; f[1] = b; f[2] = c; f[3] = d; }
+                    (c == 1 || c == 2 || c == 4 || c == 8 || c == kSynthPairs) && (d == 1 || d == 2);
+    if (ok) { f[0] = a; f[1] = b; f[2] = c; f[3] = d; f[4] = pre; }
     return ok;
 }
 
@@ -797,20 +999,23 @@ static int autotune_t(ShLoading* s)
     float best = 1e30f;
     int best_tl = 8, best_ch = 16;
     std::vector<int> best_tiles;
-    int forced[4] = {0, 0, 0, 2};
+    int forced[5] = {0, 0, 0, 2, 0};
     const bool force = forced_tiles(forced);
     int* dt = nullptr;
     cudaMalloc(&dt, sizeof(int) * 3 * (size_t)(s->L + 1) * (s->L + 1));
+    bool best_pre = false;
     for (int tl : {2, 4, 8}) {
         if (force && tl != forced[0]) continue;
         const std::vector<int> tiles = make_tiles(s->L, tl);
         cudaMemcpy(dt, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice);
-        for (int ch : {8, 16, 32, 64}) {
-            if (force && ch != forced[1]) continue;
-            const float ms = force ? 0.f : timeit([&] { launch_analysis<T>(s, tl, dt, (int)tiles.size() / 3, ch, eta, 0); });
-            if (ms < best) { best = ms; best_tl = tl; best_ch = ch; best_tiles = tiles; }
-        }
+        for (int ch : {8, 16, 32, 64})
+            for (bool pre : {false, true}) {
+                if (force && (ch != forced[1] || (int)pre != forced[4])) continue;
+                const float ms = force ? 0.f : timeit([&] { launch_analysis<T>(s, tl, dt, (int)tiles.size() / 3, ch, pre, eta, 0); });
+                if (ms < best) { best = ms; best_tl = tl; best_ch = ch; best_tiles = tiles; best_pre = pre; }
+            }
     }
+    s->pre = best_pre;
     cudaFree(dt);
     s->tl = best_tl;
     s->nchunk = best_ch;
@@ -821,7 +1026,7 @@ static int autotune_t(ShLoading* s)
         st = ODIS_ERR_NOMEM;
     best = 1e30f;
     for (int cells : {2, 1})
-        for (int lanes : {1, 2, 4, 8}) {
+        for (int lanes : {1, 2, 4, 8, kSynthPairs}) {
             if (force && (lanes != forced[2] || cells != forced[3])) continue;
             const float ms = force ? 0.f : timeit([&] { launch_synth<T>(s, lanes, cells, 0); });
             if (ms < best) { best = ms; s->lanes = lanes; s->cells = cells; }
@@ -870,11 +1075,13 @@ int sh_autotune(ShLoading* s)
     return autotune_t<float>(s);
 }
 
-void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes)
+void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes, int* cells, int* pre)
 {
     if (tl) *tl = s->use_tc ? 0 : s->tl;
     if (nchunk) *nchunk = s->use_tc ? shtc_chunks(s->tc) : s->nchunk;
     if (lanes) *lanes = s->use_tc ? shtc_tiles_per_pass(s->tc) : s->lanes;
+    if (cells) *cells = s->use_tc ? 0 : s->cells;
+    if (pre) *pre = s->use_tc ? 0 : (s->pre ? 1 : 0);
 }
 
 template <class T>
@@ -890,7 +1097,7 @@ static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st)
             return;
         }
     }
-    launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, eta, st);      // partials and their fold
+    launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, s->pre, eta, st);   // partials and their fold
     pdl_launch(k_sh_coef<T>, s->K, 32, 0, st, s->t, s->K, s->FGinv, (T*)s->coef);
     launch_synth<T>(s, s->lanes, s->cells, st);
 }
@@ -902,7 +1109,10 @@ void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)
     else enqueue_t<float>(s, eta, st);
 }
 
-int sh_kernels_per_step(const ShLoading* s) { return s && s->use_tc ? shtc_kernels_per_step() : (s && s->half ? 4 : 3); }
+int sh_kernels_per_step(const ShLoading* s)
+{
+    return s && s->use_tc ? shtc_kernels_per_step() : (s && (s->half || s->pre) ? 4 : 3);
+}
 
 void sh_layout(const ShLoading* s, int* half, int* cells, long long* basis_bytes)
 {

@@ -39,7 +39,8 @@ void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t stream);
 int sh_kernels_per_step(const ShLoading* s);
 // tile shapes chosen by the setup-time autotuner; tl = 0 for the tensor-core
 // transforms (nchunk = analysis chunks, lanes = cell tiles per synthesis pass)
-void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes);
+// (cells = synthesis cells per thread, pre = 1 for the analysis from trig-weighted values)
+void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes, int* cells, int* pre);
 // the stored basis: half = 1 for the antipodal half basis, the cells it covers,
 // and its bytes (Legendre rows + trig rows in the method's type)
 void sh_layout(const ShLoading* s, int* half, int* cells, long long* basis_bytes);

@@ -343,16 +343,21 @@ odis_status odis_launch_count(odis_ctx* c, long long* n);
  * analysis+solve+synthesis (0 if off).  Leaves the state undefined. */
 odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms);
 /* Tiles of the self-gravity transforms (0 without self-gravity): the analysis
- * covers tile_l degrees per block with the cells split in `chunks`, the
- * synthesis gives each cell `lanes` threads.  odis_create times every
- * combination on this device and keeps the fastest, unless the environment
- * variable ODIS_SH_TILES="tile_l,chunks,lanes" names one.
+ * covers tile_l degrees per block with the cells split in `chunks`, and with
+ * pre = 1 reads the trig-weighted values of every order formed once per step
+ * (else each tile forms them); the synthesis gives each cell `lanes` threads
+ * splitting the orders, or with lanes = 16 one warp per pair of orders
+ * (m, l_max - m) for 32 x `cells` cells per block; each synthesis thread covers
+ * `cells` adjacent cells.  odis_create times every combination on this device
+ * and keeps the fastest, unless the environment variable
+ * ODIS_SH_TILES="tile_l,chunks,lanes[,cells[,pre]]" names one.  Any pointer
+ * may be NULL.
  * ODIS_FP32 also has tensor-core transforms (tcgen05, fp16 hi/lo operand pairs,
  * FP32 accumulation); odis_create times them against the CUDA-core ones and
  * keeps the faster, unless ODIS_SH_TC=1 (tensor cores) or ODIS_SH_TC=0 (CUDA
  * cores) fixes the choice.  With the tensor-core transforms tile_l = 0, chunks
  * = analysis chunks and lanes = 128-cell tiles per synthesis pass. */
-odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes);
+odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes, int* cells, int* pre);
 
 /* Storage of the self-gravity basis (0s without self-gravity).  On a centrally
  * symmetric mesh (every cell has an antipodal partner; the icosahedral grids

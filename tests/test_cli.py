@@ -177,6 +177,8 @@ def test_cli_sigint_checkpoint_and_exact_resume(built, tmp_path):
     import signal
     import struct
     orbits = "100"
+    (tmp_path / "a").mkdir()
+    (tmp_path / "b").mkdir()
     a = _rundir(tmp_path / "a")
     r = subprocess.run([str(CLI), "--dir", str(a), "--orbits", orbits], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr

@@ -161,9 +161,10 @@ def test_batch_run_is_one_graph_launch(grid_dir):
     """Every run replays its chunks' cooperative launches from one CUDA graph; chunking changes nothing."""
     g, O, angvel, P, paths, meshes, members, common = _setup(grid_dir, count=6, seed=9)
     b = g.Batch(common, meshes, members)
+    i0 = b.info()                                  # creation times the row variants with short runs
     b.run(steps=500, chunk=64)                     # 8 chunks
     info = b.info()
-    assert info["graph_runs"] == 1 and info["launches"] == 8
+    assert info["graph_runs"] - i0["graph_runs"] == 1 and info["launches"] - i0["launches"] == 8
     c = g.Batch(common, meshes, members)
     c.run(steps=500, chunk=1000)
     for i in range(len(members)):

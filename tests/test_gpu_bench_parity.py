@@ -83,9 +83,10 @@ def test_level6_sh16_fp32_variant(level6):
     sol.close()
 
 
-# (degrees per analysis tile, cell chunks, synthesis lanes, cells per synthesis thread): every value of
-# each parameter appears at least once
-TILES = [(2, 8, 1, 1), (4, 16, 2, 2), (8, 32, 4, 1), (2, 64, 8, 2), (4, 8, 8, 1), (8, 64, 1, 2)]
+# (degrees per analysis tile, cell chunks, synthesis lanes (16: a warp per order pair), cells per synthesis
+# thread, analysis from precomputed trig-weighted values): every value of each parameter appears
+TILES = [(2, 8, 1, 1, 0), (4, 16, 2, 2, 1), (8, 32, 4, 1, 0), (2, 64, 8, 2, 1), (4, 8, 16, 1, 1),
+         (8, 64, 16, 2, 0), (2, 16, 16, 2, 1)]
 
 
 @pytest.mark.parametrize("precision", [0, 2, 1])
@@ -94,7 +95,7 @@ def test_level6_sh_tile_paths(level6, monkeypatch, precision, tiles):
     monkeypatch.setenv("ODIS_SH_TILES", ",".join(map(str, tiles)))
     monkeypatch.setenv("ODIS_SH_TC", "0")
     sol = _solver(level6, precision)
-    assert tuple(sol.sh_tiles()) == tiles[:3]
+    assert tuple(sol.sh_tuning()) == tiles
     pg = sol.run(L6_SHORT)
     po, so = level6["short"]
     if precision == 1:
@@ -110,7 +111,6 @@ def test_level6_sh_tile_paths(level6, monkeypatch, precision, tiles):
 def test_level6_half_and_full_basis(level6, monkeypatch, precision):
     """The antipodal half basis (the default on these centrally symmetric meshes) and the full basis
     (ODIS_SH_HALF=0) give the same run: to rounding in FP64/DF64, and both against the oracle."""
-    import geodesicodis_gb300 as g
     half = _solver(level6, precision)
     lay = half.sh_layout()
     assert lay["half"] and lay["cells"] == 40962 // 2
@@ -120,10 +120,11 @@ def test_level6_half_and_full_basis(level6, monkeypatch, precision):
     assert full.sh_layout()["basis_bytes"] == 2 * lay["basis_bytes"]
     ph, pf = half.run(L6_SHORT), full.run(L6_SHORT)
     po, so = level6["short"]
-    tol = 1e-4 if precision == 1 else 1e-12
+    # FP64: the two bases differ by rounding only; double-float carries its 48-bit rounding along
+    tol = {0: 1e-12, 2: 1e-11, 1: 1e-4}[precision]
     assert rel_err(ph, pf) < tol
     for x, y in zip(half.get_state()[1:], full.get_state()[1:]):
-        assert rel_err(x, y) < (1e-3 if precision == 1 else 1e-12)
+        assert rel_err(x, y) < (1e-3 if precision == 1 else tol)
     if precision != 1:
         _cmp(full.get_state(), so, 1e-10)
     half.close()
