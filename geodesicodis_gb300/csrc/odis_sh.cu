@@ -84,7 +84,8 @@ void plm_bar(int L, double z, std::vector<double>& P)
 // kHalf: the basis is stored for one cell of each antipodal pair (N of them,
 // row stride Np), and `eta` holds e = eta_a + eta_b in [0, Np) and
 // o = eta_a - eta_b in [Np, 2 Np); since Y_lm(-x) = (-1)^l Y_lm(x), even
-// degrees sum Y_lm e and odd degrees Y_lm o over the half set.
+// degrees sum Y_lm e and odd degrees Y_lm o over the half set.  The tiles then
+// hold one parity each (degrees l0, l0 + 2, ...), so a block reads only e or o.
 // kPre: `eta` holds the trig-weighted values of every order, written once per
 // step by k_sh_prep (rows 4m..4m+3: cos e, sin e, cos o, sin o with the half
 // basis; rows 2m, 2m+1: cos eta, sin eta with the full one), so the loop is
@@ -116,77 +117,54 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
     const T* cm = trig + (size_t)(2 * m) * Np;
     const T* sm = trig + (size_t)(2 * m + 1) * Np;
     const T* prow = P + (size_t)p_row(L, l0, m) * Np;
+    // kHalf: a tile's degrees share one parity (l0, l0 + 2, ...), so it needs only e or only o
+    constexpr int kStride = kHalf ? 2 : 1;
+    const bool odd = kHalf && (l0 & 1);
+    const T* xm = eta + (size_t)(kHalf ? 4 * m + (odd ? 2 : 0) : 2 * m) * Np;   // kPre: cos x, sin x rows
+    const T* ev = eta + (odd ? (size_t)Np : 0);                                 // otherwise: e or o
     // two adjacent cells per thread and iteration, each row read with one vector load;
     // two iterations unrolled so their loads are in flight together
     int i = i0 + 2 * threadIdx.x;
 #pragma unroll 2
     for (; i + 1 < i1; i += 2 * kShThreads) {
-        {
-            T ec, es, ec2, es2, oc, os, oc2, os2;
-            if constexpr (kPre) {
-                const T* xm = eta + (size_t)(kHalf ? 4 * m : 2 * m) * Np;
-                A::ld2(xm + i, ec, ec2);
-                A::ld2(xm + Np + i, es, es2);
-                if constexpr (kHalf) {
-                    A::ld2(xm + 2 * (size_t)Np + i, oc, oc2);
-                    A::ld2(xm + 3 * (size_t)Np + i, os, os2);
-                } else {
-                    oc = ec; os = es; oc2 = ec2; os2 = es2;
-                }
-            } else {
-                T e, e2, c1, c2, s1, s2;
-                A::ld2(eta + i, e, e2);
-                A::ld2(cm + i, c1, c2);
-                A::ld2(sm + i, s1, s2);
-                ec = A::mul(c1, e); es = A::mul(s1, e);
-                ec2 = A::mul(c2, e2); es2 = A::mul(s2, e2);
-                oc = ec; os = es; oc2 = ec2; os2 = es2;
-                if constexpr (kHalf) {
-                    T o, o2;
-                    A::ld2(eta + Np + i, o, o2);
-                    oc = A::mul(c1, o); os = A::mul(s1, o);
-                    oc2 = A::mul(c2, o2); os2 = A::mul(s2, o2);
-                }
-            }
+        T ec, es, ec2, es2;
+        if constexpr (kPre) {
+            A::ld2(xm + i, ec, ec2);
+            A::ld2(xm + Np + i, es, es2);
+        } else {
+            T e, e2, c1, c2, s1, s2;
+            A::ld2(ev + i, e, e2);
+            A::ld2(cm + i, c1, c2);
+            A::ld2(sm + i, s1, s2);
+            ec = A::mul(c1, e); es = A::mul(s1, e);
+            ec2 = A::mul(c2, e2); es2 = A::mul(s2, e2);
+        }
 #pragma unroll
-            for (int j = 0; j < kTileL; j++) {
-                if (j < nl) {
-                    T p, p2;
-                    A::ld2(prow + (size_t)j * Np + i, p, p2);
-                    const bool odd = kHalf && ((l0 + j) & 1);
-                    ac[j] = A::fma_acc(p, odd ? oc : ec, ac[j]);
-                    as[j] = A::fma_acc(p, odd ? os : es, as[j]);
-                    bc[j] = A::fma_acc(p2, odd ? oc2 : ec2, bc[j]);
-                    bs[j] = A::fma_acc(p2, odd ? os2 : es2, bs[j]);
-                }
+        for (int j = 0; j < kTileL; j++) {
+            if (j < nl) {
+                T p, p2;
+                A::ld2(prow + (size_t)(kStride * j) * Np + i, p, p2);
+                ac[j] = A::fma_acc(p, ec, ac[j]);
+                as[j] = A::fma_acc(p, es, as[j]);
+                bc[j] = A::fma_acc(p2, ec2, bc[j]);
+                bs[j] = A::fma_acc(p2, es2, bs[j]);
             }
         }
     }
     if (i < i1) {           // the last cell of an odd-length final chunk
-        {
-            T ec, es, oc, os;
-            if constexpr (kPre) {
-                const T* xm = eta + (size_t)(kHalf ? 4 * m : 2 * m) * Np;
-                ec = xm[i]; es = xm[Np + i];
-                oc = ec; os = es;
-                if constexpr (kHalf) { oc = xm[2 * (size_t)Np + i]; os = xm[3 * (size_t)Np + i]; }
-            } else {
-                const T e = eta[i];
-                ec = A::mul(cm[i], e); es = A::mul(sm[i], e);
-                oc = ec; os = es;
-                if constexpr (kHalf) {
-                    const T o = eta[Np + i];
-                    oc = A::mul(cm[i], o); os = A::mul(sm[i], o);
-                }
-            }
+        T ec, es;
+        if constexpr (kPre) {
+            ec = xm[i]; es = xm[Np + i];
+        } else {
+            const T e = ev[i];
+            ec = A::mul(cm[i], e); es = A::mul(sm[i], e);
+        }
 #pragma unroll
-            for (int j = 0; j < kTileL; j++) {
-                if (j < nl) {
-                    const T p = prow[(size_t)j * Np + i];
-                    const bool odd = kHalf && ((l0 + j) & 1);
-                    ac[j] = A::fma_acc(p, odd ? oc : ec, ac[j]);
-                    as[j] = A::fma_acc(p, odd ? os : es, as[j]);
-                }
+        for (int j = 0; j < kTileL; j++) {
+            if (j < nl) {
+                const T p = prow[(size_t)(kStride * j) * Np + i];
+                ac[j] = A::fma_acc(p, ec, ac[j]);
+                as[j] = A::fma_acc(p, es, as[j]);
             }
         }
     }
@@ -211,7 +189,7 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x = A::add(x, A::shfl(x, o));
         const int j = q >> 1, is_sin = q & 1;
-        if (lane == 0 && (m > 0 || !is_sin)) part[(size_t)sh_col(l0 + j, m, is_sin) * nchunk + chunk] = x;
+        if (lane == 0 && (m > 0 || !is_sin)) part[(size_t)sh_col(l0 + kStride * j, m, is_sin) * nchunk + chunk] = x;
     }
     // publish the partials, then count this block in
     __threadfence();
@@ -224,7 +202,7 @@ __global__ void __launch_bounds__(kShThreads) k_sh_analysis(const T* __restrict_
     for (int q = wid; q < 2 * nl; q += kShThreads / 32) {       // one warp per coefficient of the tile
         const int j = q >> 1, is_sin = q & 1;
         if (m == 0 && is_sin) continue;
-        const int k = sh_col(l0 + j, m, is_sin);
+        const int k = sh_col(l0 + kStride * j, m, is_sin);
         double x = 0.0;
         for (int c = lane; c < nchunk; c += 32) x += A::to(A::ldcg(&part[(size_t)k * nchunk + c]));
 #pragma unroll
@@ -254,10 +232,10 @@ __global__ void __launch_bounds__(256) k_sh_pair(const T* __restrict__ eta, cons
     eo[Np + h] = o;
 }
 
-// trig-weighted values of every order for the kPre analysis, one cell per thread:
-// half basis x[4m..4m+3][h] = (cos e, sin e, cos o, sin o)(m lon_h) with
-// e, o = eta_a +- eta_b; full basis x[2m], x[2m+1] = (cos, sin)(m lon_i) eta_i;
-// zero on the padding
+// trig-weighted values of every order for the kPre analysis, one (cell, order)
+// per thread (grid.y = order): half basis x[4m..4m+3][h] = (cos e, sin e, cos o,
+// sin o)(m lon_h) with e, o = eta_a +- eta_b; full basis x[2m], x[2m+1] =
+// (cos, sin)(m lon_i) eta_i; zero on the padding
 template <class T, bool kHalf>
 __global__ void __launch_bounds__(256) k_sh_prep(const T* __restrict__ eta, const int* __restrict__ ia,
                                                  const int* __restrict__ ib, const T* __restrict__ trig, int N,
@@ -266,30 +244,29 @@ __global__ void __launch_bounds__(256) k_sh_prep(const T* __restrict__ eta, cons
     pdl_wait();
     using A = Ar<T>;
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y;
     if (h >= Np) return;
     T e = A::zero(), o = A::zero();
     if (h < N) {
         if constexpr (kHalf) {
-            const T a = eta[ia[h]], b = eta[ib[h]];
+            const T a = eta[__ldg(&ia[h])], b = eta[__ldg(&ib[h])];
             e = A::add(a, b);
             o = A::sub(a, b);
         } else {
             e = eta[h];
         }
     }
-    for (int m = 0; m <= L; m++) {
-        const T c = trig[(size_t)(2 * m) * Np + h], sn = trig[(size_t)(2 * m + 1) * Np + h];
-        if constexpr (kHalf) {
-            T* xm = x + (size_t)(4 * m) * Np + h;
-            xm[0] = A::mul(c, e);
-            xm[(size_t)Np] = A::mul(sn, e);
-            xm[2 * (size_t)Np] = A::mul(c, o);
-            xm[3 * (size_t)Np] = A::mul(sn, o);
-        } else {
-            T* xm = x + (size_t)(2 * m) * Np + h;
-            xm[0] = A::mul(c, e);
-            xm[(size_t)Np] = A::mul(sn, e);
-        }
+    const T c = trig[(size_t)(2 * m) * Np + h], sn = trig[(size_t)(2 * m + 1) * Np + h];
+    if constexpr (kHalf) {
+        T* xm = x + (size_t)(4 * m) * Np + h;
+        xm[0] = A::mul(c, e);
+        xm[(size_t)Np] = A::mul(sn, e);
+        xm[2 * (size_t)Np] = A::mul(c, o);
+        xm[3 * (size_t)Np] = A::mul(sn, o);
+    } else {
+        T* xm = x + (size_t)(2 * m) * Np + h;
+        xm[0] = A::mul(c, e);
+        xm[(size_t)Np] = A::mul(sn, e);
     }
 }
 
@@ -869,16 +846,27 @@ const double* sh_usg64(ShLoading* s) { return s && s->precision == ODIS_FP64 ? (
 const float* sh_usg32(ShLoading* s) { return s && s->precision == ODIS_FP32 ? (const float*)s->usg : nullptr; }
 const float2* sh_usgdf(ShLoading* s) { return s && s->precision == ODIS_DF64 ? (const float2*)s->usg : nullptr; }
 
-// analysis tiles (m, l0, nl) with nl <= tl
-static std::vector<int> make_tiles(int L, int tl)
+// analysis tiles (m, l0, nl) with nl <= tl: degrees l0 .. l0 + nl - 1, or with the
+// half basis l0, l0 + 2, ..., l0 + 2 (nl - 1) (one parity per tile)
+static std::vector<int> make_tiles(int L, int tl, bool half)
 {
     std::vector<int> tiles;
-    for (int mm = 0; mm <= L; mm++)
-        for (int l0 = mm; l0 <= L; l0 += tl) {
-            tiles.push_back(mm);
-            tiles.push_back(l0);
-            tiles.push_back(std::min(tl, L - l0 + 1));
+    for (int mm = 0; mm <= L; mm++) {
+        if (!half) {
+            for (int l0 = mm; l0 <= L; l0 += tl) {
+                tiles.push_back(mm);
+                tiles.push_back(l0);
+                tiles.push_back(std::min(tl, L - l0 + 1));
+            }
+            continue;
         }
+        for (int start = mm; start <= std::min(L, mm + 1); start++)
+            for (int l0 = start; l0 <= L; l0 += 2 * tl) {
+                tiles.push_back(mm);
+                tiles.push_back(l0);
+                tiles.push_back(std::min(tl, (L - l0) / 2 + 1));
+            }
+    }
     return tiles;
 }
 
@@ -896,8 +884,9 @@ static void launch_analysis(const ShLoading* s, int tl, const int* tiles, int nt
     const T* e = (const T*)eta;
     if (pre) {            // trig-weighted values of every order, then multiply-adds only
         T* x = (T*)s->eo;
-        if (s->half) pdl_launch(k_sh_prep<T, true>, (np + 255) / 256, 256, 0, st, e, (const int*)s->ia, (const int*)s->ib, trig, n, np, s->L, x);
-        else pdl_launch(k_sh_prep<T, false>, (np + 255) / 256, 256, 0, st, e, (const int*)s->ia, (const int*)s->ib, trig, n, np, s->L, x);
+        const dim3 pg((np + 255) / 256, s->L + 1);
+        if (s->half) pdl_launch(k_sh_prep<T, true>, pg, 256, 0, st, e, (const int*)s->ia, (const int*)s->ib, trig, n, np, s->L, x);
+        else pdl_launch(k_sh_prep<T, false>, pg, 256, 0, st, e, (const int*)s->ia, (const int*)s->ib, trig, n, np, s->L, x);
         e = x;
     } else if (s->half) {
         T* eo = (T*)s->eo;
@@ -1006,7 +995,7 @@ static int autotune_t(ShLoading* s)
     bool best_pre = false;
     for (int tl : {2, 4, 8}) {
         if (force && tl != forced[0]) continue;
-        const std::vector<int> tiles = make_tiles(s->L, tl);
+        const std::vector<int> tiles = make_tiles(s->L, tl, s->half);
         cudaMemcpy(dt, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice);
         for (int ch : {8, 16, 32, 64})
             for (bool pre : {false, true}) {

@@ -117,7 +117,7 @@ def converged_at(history: list[float], tol: float = TOL) -> int:
 
 
 def run_to_convergence(common, mesh, members, basis: MeshBasis | None, v0=None, eta0=None, round_orbits: int = 10,
-                       max_orbits: int = 400, log=None):
+                       max_orbits: int = 400, log=None, tol: float = TOL):
     """Run every member (all on `mesh`) from (v0, eta0) (None: rest) until its orbit-mean power converges.
 
     Members still running are re-batched after every round of `round_orbits`
@@ -166,7 +166,7 @@ def run_to_convergence(common, mesh, members, basis: MeshBasis | None, v0=None, 
         for k, i in enumerate(active):
             hist[i].extend(op_all[k].tolist())
             v_cur[i], e_cur[i] = v[k], e[k]
-            c = converged_at(hist[i])
+            c = converged_at(hist[i], tol)
             if c > 0:
                 orbits[i] = c
                 v_fin[i], e_fin[i] = v[k], e[k]
@@ -249,7 +249,7 @@ def relative_coef_error(pred: np.ndarray, true: np.ndarray) -> np.ndarray:
 
 
 def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epochs=800, batch=128, lr=1e-3,
-               round_orbits=10, max_orbits=400, log=print, save=None) -> dict:
+               round_orbits=10, max_orbits=400, log=print, save=None, tol: float = TOL) -> dict:
     """Train on solver runs, then compare orbits to convergence from rest and from the warm start."""
     t0 = time.time()
     common, period = S.common_params()
@@ -262,7 +262,7 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
     mte = members_from(pte, meshes, period)
     log(f"setup {time.time() - t0:.1f} s; training runs ({n_train})")
     t1 = time.time()
-    tr = run_to_convergence(common, mesh, mtr, basis, round_orbits=round_orbits, max_orbits=max_orbits, log=log)
+    tr = run_to_convergence(common, mesh, mtr, basis, round_orbits=round_orbits, max_orbits=max_orbits, log=log, tol=tol)
     t_data = time.time() - t1
     log(f"training data {t_data:.1f} s, {tr['cell_steps']:.3e} cell-steps")
     sur = Surrogate(basis)
@@ -272,17 +272,17 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
     log(f"training {t_fit:.1f} s, loss {losses[0]:.3e} -> {losses[-1]:.3e}")
     # held-out: zero start (also gives the true converged coefficients) and warm start
     t3 = time.time()
-    zero = run_to_convergence(common, mesh, mte, basis, round_orbits=round_orbits, max_orbits=max_orbits, log=log)
+    zero = run_to_convergence(common, mesh, mte, basis, round_orbits=round_orbits, max_orbits=max_orbits, log=log, tol=tol)
     t_zero = time.time() - t3
     v_w, e_w = sur.warm_state(pte)
     t4 = time.time()
     warm = run_to_convergence(common, mesh, mte, None, v0=v_w, eta0=e_w, round_orbits=round_orbits,
-                              max_orbits=max_orbits, log=log)
+                              max_orbits=max_orbits, log=log, tol=tol)
     t_warm = time.time() - t4
     # the best a degree-8 warm start can do: start from the projection of the converged state itself
     v_t, e_t = basis.state(zero["coef"][:, 0, :])
     best = run_to_convergence(common, mesh, mte, None, v0=v_t, eta0=e_t, round_orbits=round_orbits,
-                              max_orbits=max_orbits, log=log)
+                              max_orbits=max_orbits, log=log, tol=tol)
     pred = sur.predict_coef(pte)
     err = relative_coef_error(pred, zero["coef"])
     if save:
@@ -314,6 +314,6 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
         "seconds": {"data": t_data, "train": t_fit, "zero": t_zero, "warm": t_warm},
         "epochs": epochs, "batch": batch, "lr": lr, "round_orbits": round_orbits,
         "cell_steps": {"data": tr["cell_steps"], "zero": zero["cell_steps"], "warm": warm["cell_steps"]},
-        "max_orbits": max_orbits, "tol": TOL,
+        "max_orbits": max_orbits, "tol": tol,
     }
     return res
