@@ -90,22 +90,39 @@ __device__ __forceinline__ void df_accumulate(float& hi, float& lo, float x)
 // finiteness from the exponent bits (integer pipe, no FP64 compare)
 __device__ __forceinline__ bool finite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
 
-// Block sum of the per-thread dissipation: FP64 shuffles in the FP64 method;
-// in the FP32 variant FP32 within a warp (32 terms) and FP64 across warps.
+// Block sum of the per-thread dissipation, valid in thread 0.  FP64 method:
+// every thread parks its term in shared memory (smem: kStepThreads doubles) and
+// warp 0 adds them, eight per lane then a shuffle tree -- 12 FP64 additions a
+// block instead of a 5-step shuffle tree in every warp (the FP64 pipe is the
+// face kernel's bound).  FP32 variant: FP32 within a warp (32 terms) and FP64
+// across warps.
 template <class T>
 __device__ __forceinline__ double block_power(T pw, double* smem)
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if constexpr (std::is_same<T, double>::value) {
+        smem[threadIdx.x] = pw;
+        __syncthreads();
+        double s = 0.0;
+        if (wid == 0) {
+            s = smem[lane];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pw += __shfl_down_sync(0xffffffffu, pw, o);
-    if (lane == 0) smem[wid] = (double)pw;
-    __syncthreads();
-    double s = 0.0;
-    if (wid == 0) {
-        s = lane < kStepThreads / 32 ? smem[lane] : 0.0;
-        s = warp_sum(s);
+            for (int r = 1; r < kStepThreads / 32; r++) s += smem[lane + 32 * r];
+            s = warp_sum(s);
+        }
+        return s;
+    } else {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) pw += __shfl_down_sync(0xffffffffu, pw, o);
+        if (lane == 0) smem[wid] = (double)pw;
+        __syncthreads();
+        double s = 0.0;
+        if (wid == 0) {
+            s = lane < kStepThreads / 32 ? smem[lane] : 0.0;
+            s = warp_sum(s);
+        }
+        return s;
     }
-    return s;
 }
 
 }  // namespace
@@ -120,7 +137,7 @@ template <class T, bool kMaster, bool kQuad>
 __global__ void __launch_bounds__(kStepThreads) k_edge_step(FaceCoef<T> fc, State<T> st, StepConst sc, int offset)
 {
     pdl_wait();
-    __shared__ double s_red[kStepThreads / 32];
+    __shared__ double s_red[kStepThreads];
     const long long it = *st.iter + offset;
     // forcing phase at t^{n+1} (precomputed per run by k_phase)
     const long long kstep = it - *st.run_first;
@@ -186,7 +203,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_f32x2(FaceCoef<float
                                                                      int offset)
 {
     pdl_wait();
-    __shared__ double s_red[kStepThreads / 32];
+    __shared__ double s_red[kStepThreads];
     const long long it = *st.iter + offset;
     const long long kstep = it - *st.run_first;
     const float cosM = st.phase[2 * kstep], sinM = st.phase[2 * kstep + 1];
@@ -247,7 +264,7 @@ __global__ void __launch_bounds__(kStepThreads) k_edge_step_f32x2(FaceCoef<float
 __global__ void __launch_bounds__(kStepThreads) k_power_partial_f32x2(FaceCoef<float> fc, State<float> st,
                                                                       StepConst sc)
 {
-    __shared__ double s_red[kStepThreads / 32];
+    __shared__ double s_red[kStepThreads];
     const long long it = *st.iter;
     const int e = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     const int Ep = sc.Ep;
@@ -305,7 +322,7 @@ __global__ void __launch_bounds__(kStepThreads) k_cell_step(CellCoef<T> cc, Stat
 template <class T>
 __global__ void __launch_bounds__(kStepThreads) k_power_partial(FaceCoef<T> fc, State<T> st, StepConst sc)
 {
-    __shared__ double s_red[kStepThreads / 32];
+    __shared__ double s_red[kStepThreads];
     const long long it = *st.iter;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int Ep = sc.Ep;
@@ -478,7 +495,7 @@ __global__ void k_interp(FaceCoef<double> fc, const double* nrm, int E, int Ep, 
 __global__ void __launch_bounds__(kStepThreads) k_energy_partial(const double* area, int E, double coef, int quad,
                                                                  const double* uv, double* e_out, double* partial)
 {
-    __shared__ double s_red[kStepThreads / 32];
+    __shared__ double s_red[kStepThreads];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double x = 0.0;
     if (i < E) {

@@ -15,17 +15,20 @@ namespace odis {
 
 namespace {
 
-// block sum of a df64 per thread; the result (as FP64) is valid in thread 0
+// block sum of a df64 per thread; the result (as FP64) is valid in thread 0.
+// Every thread parks its term in shared memory (smem: kStepThreads values) and
+// warp 0 adds them, eight per lane then a shuffle tree: 12 double-float
+// additions a block instead of a 5-step shuffle tree in every warp.
 __device__ __forceinline__ double block_sum_df(df64 x, df64* smem)
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x = df_add(x, df_shfl_down(x, o));
-    if (lane == 0) smem[wid] = x;
+    smem[threadIdx.x] = x;
     __syncthreads();
     df64 s = df_make(0.f, 0.f);
     if (wid == 0) {
-        s = lane < kStepThreads / 32 ? smem[lane] : df_make(0.f, 0.f);
+        s = smem[lane];
+#pragma unroll
+        for (int r = 1; r < kStepThreads / 32; r++) s = df_add(s, smem[lane + 32 * r]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_down(s, o));
     }
@@ -40,7 +43,7 @@ template <bool kQuad>   // QUADRATIC friction, a compile-time switch as in k_edg
 __global__ void __launch_bounds__(kStepThreads) k_edge_step_df(FaceCoef<df64> fc, State<df64> st, StepConst sc, int offset)
 {
     pdl_wait();
-    __shared__ df64 s_red[kStepThreads / 32];
+    __shared__ df64 s_red[kStepThreads];
     const long long it = *st.iter + offset;
     const long long kstep = it - *st.run_first;        // forcing phase at t^{n+1}, precomputed per run
     const df64 cosM = st.phase[2 * kstep], sinM = st.phase[2 * kstep + 1];
@@ -103,7 +106,7 @@ __global__ void __launch_bounds__(kStepThreads) k_cell_step_df(CellCoef<df64> cc
 
 __global__ void __launch_bounds__(kStepThreads) k_power_partial_df(FaceCoef<df64> fc, State<df64> st, StepConst sc)
 {
-    __shared__ df64 s_red[kStepThreads / 32];
+    __shared__ df64 s_red[kStepThreads];
     const long long it = *st.iter;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int Ep = sc.Ep;
