@@ -236,12 +236,16 @@ def _replica_setup(cuda: bool = True):
 FP64_INST_FACE, FP64_INST_FACE_SG, FP64_INST_CELL = 29, 32, 10
 
 
-def sh_fp64_inst(K: int, cells: int, L: int, tiles: int) -> float:
-    """FP64 instructions of one self-gravity step (analysis + synthesis) over the `cells` the basis covers:
-    each transform is K multiply-adds per cell (two per (l, m > 0), one per (l, 0)); the analysis adds its
-    trig products (4 per cell and tile; 2 with the full basis, counted as 4), the synthesis 4 per cell and
-    order; the pair, fold and K x K solve kernels are below 1 %."""
-    return 2.0 * K * cells + 4.0 * cells * tiles + 4.0 * cells * (L + 1)
+def sh_fp64_inst(K: int, cells: int, L: int, half: bool, pre: bool, ntiles: int) -> float:
+    """FP64 instructions of one self-gravity step over the `cells` the basis covers, for the variant the
+    setup chose: each transform does K multiply-adds per cell (two per (l, m > 0), one per (l, 0)); the
+    trig-weighted values cost 4 (half basis: cos e, sin e, cos o, sin o) or 2 multiplies per cell and
+    order when formed once per step (pre), or 2 per cell and analysis tile otherwise; the synthesis
+    combines each order's sums with its trig values in 4 (half) or 2 multiply-adds per cell.  The pair,
+    fold and K x K solve work is below 1 %."""
+    per_order = 4 if half else 2
+    trig = per_order * cells * (L + 1) if pre else 2 * cells * ntiles
+    return 2.0 * K * cells + trig + per_order * cells * (L + 1)
 
 
 def run_ours(args) -> dict:
@@ -374,8 +378,12 @@ def run_ours(args) -> dict:
     sh_bytes = 2 * layout["basis_bytes"] + (4 if layout["half"] else 2) * N * 8
     alg = {"face_step": face_bytes, "cell_step": cell_bytes, "sh_self_gravity": sh_bytes}[dominant]
     achieved = alg / (per_step[dominant] / 1e3) / 1e9
-    ntiles = sum((LMAX - m) // max(1, tiles["tile_l"]) + 1 for m in range(LMAX + 1)) if tiles["tile_l"] else LMAX + 1
-    sh_inst = sh_fp64_inst(K, layout["cells"], LMAX, ntiles)
+    tl = max(1, tiles["tile_l"])
+    if layout["half"]:       # one degree parity per tile
+        ntiles = sum(((LMAX - st) // 2) // tl + 1 for m in range(LMAX + 1) for st in (m, m + 1) if st <= LMAX)
+    else:
+        ntiles = sum((LMAX - m) // tl + 1 for m in range(LMAX + 1))
+    sh_inst = sh_fp64_inst(K, layout["cells"], LMAX, layout["half"], bool(tiles["pre"]), ntiles)
     inst = {"face_step": E * FP64_INST_FACE_SG, "cell_step": N * FP64_INST_CELL, "sh_self_gravity": sh_inst}[dominant]
     fp64_ach = inst * 2.0 / (per_step[dominant] / 1e3) / 1e12
     plain = {}
