@@ -50,7 +50,8 @@ constexpr double kPi = 3.1415926535897932384626433832795028841971693993751058;
 constexpr int kShThreads = 256;
 constexpr int kSynthThreads = 128;
 constexpr int kSynthPairs = 16;    // "lanes" value that selects the warp-per-order-pair synthesis
-constexpr int kSynthMaxWarps = 17; // its warps per block (l_max 32 has 17 order pairs; more pairs share warps)
+constexpr int kSynthMaxWarps = 17; // its warps per cell group (l_max 32 has 17 order pairs; more pairs share warps)
+constexpr int kSynthMaxThreads = 1024;
 constexpr int kMaxChunks = 64;     // largest cell-chunk count the autotuner tries
 
 // fully normalised (4pi) associated Legendre functions with the Condon-Shortley
@@ -429,8 +430,11 @@ __global__ void __launch_bounds__(kSynthThreads) k_sh_synth(const T* __restrict_
 // of the block, and the warps' sums meet in shared memory in warp order.  With
 // (L + 2) / 2 warps per block this keeps several times more warps resident than
 // the lane-per-order kernel, whose per-cell thread count the half basis halves.
-template <class T, int kCells, bool kHalf>
-__global__ void __launch_bounds__(kSynthMaxWarps * 32) k_sh_synth_m(const T* __restrict__ P, const T* __restrict__ trig,
+// kGroups: cell groups of 32 kCells cells per block (warp w: order pair w % nw,
+// cell group w / nw), so the coefficients are staged once for kGroups groups.
+template <class T, int kCells, bool kHalf, int kGroups>
+__global__ void __launch_bounds__(kGroups * kSynthMaxWarps * 32 < kSynthMaxThreads ? kGroups * kSynthMaxWarps * 32
+                                                                                    : kSynthMaxThreads) k_sh_synth_m(const T* __restrict__ P, const T* __restrict__ trig,
                                                      const T* __restrict__ coef, int N, int Np, int L, int K,
                                                      const int* __restrict__ ia, const int* __restrict__ ib,
                                                      T* __restrict__ usg)
@@ -442,8 +446,9 @@ __global__ void __launch_bounds__(kSynthMaxWarps * 32) k_sh_synth_m(const T* __r
     T* red = c + ((K + 1) & ~1);               // [warps][32][4]: u, u2, w, w2 of every lane
     for (int k = threadIdx.x; k < K; k += blockDim.x) c[k] = coef[k];
     __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int i = (blockIdx.x * 32 + lane) * kCells;
+    const int lane = threadIdx.x & 31, nw = (blockDim.x >> 5) / kGroups;
+    const int grp = (threadIdx.x >> 5) / nw, wid = (threadIdx.x >> 5) % nw;
+    const int i = ((blockIdx.x * kGroups + grp) * 32 + lane) * kCells;
     const int i2 = kCells == 2 ? min(i + 1, N - 1) : i;
     const bool pair = kCells == 2 && i2 == i + 1;
     T u = A::zero(), u2 = A::zero();     // full basis: the sums; kHalf: the even-degree sums E
@@ -516,13 +521,13 @@ __global__ void __launch_bounds__(kSynthMaxWarps * 32) k_sh_synth_m(const T* __r
                 }
             }
     }
-    T* r = red + (size_t)(wid * 32 + lane) * 4;
+    T* r = red + (size_t)(threadIdx.x) * 4;
     r[0] = u; r[1] = u2; r[2] = w; r[3] = w2;
     __syncthreads();
     if (wid == 0 && i < N) {
         T su = A::zero(), su2 = A::zero(), sw = A::zero(), sw2 = A::zero();
         for (int v = 0; v < nw; v++) {
-            const T* x = red + (size_t)(v * 32 + lane) * 4;
+            const T* x = red + (size_t)((grp * nw + v) * 32 + lane) * 4;
             su = A::add(su, x[0]); su2 = A::add(su2, x[1]); sw = A::add(sw, x[2]); sw2 = A::add(sw2, x[3]);
         }
         if constexpr (kHalf) {
@@ -917,13 +922,17 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
 #define ODIS_SYNTH_LANES(CL, H) \
     do { if (lanes == 1) ODIS_SYNTH(1, CL, H); else if (lanes == 2) ODIS_SYNTH(2, CL, H); \
          else if (lanes == 4) ODIS_SYNTH(4, CL, H); else ODIS_SYNTH(8, CL, H); } while (0)
-    if (lanes == kSynthPairs) {            // one warp per pair of orders, 32 * cells cells per block
+    if (lanes % kSynthPairs == 0) {      // one warp per pair of orders; lanes / 16 groups of 32 * cells cells
+        const int groups = lanes / kSynthPairs;
         const int nw = std::min(s->L / 2 + 1, kSynthMaxWarps);
-        const int nb = (n + 32 * cells - 1) / (32 * cells);
-        const size_t smp = sizeof(T) * ((size_t)((s->K + 1) & ~1) + (size_t)nw * 32 * 4);
-#define ODIS_SYNTH_M(CL, H) pdl_launch(k_sh_synth_m<T, CL, H>, nb, nw * 32, smp, st, P, trig, c, n, np, s->L, s->K, ia, ib, u)
-        if (s->half) { if (cells == 2) ODIS_SYNTH_M(2, true); else ODIS_SYNTH_M(1, true); }
-        else { if (cells == 2) ODIS_SYNTH_M(2, false); else ODIS_SYNTH_M(1, false); }
+        const int nb = (n + 32 * cells * groups - 1) / (32 * cells * groups);
+        const size_t smp = sizeof(T) * ((size_t)((s->K + 1) & ~1) + (size_t)groups * nw * 32 * 4);
+#define ODIS_SYNTH_M(CL, H, G) pdl_launch(k_sh_synth_m<T, CL, H, G>, nb, G * nw * 32, smp, st, P, trig, c, n, np, s->L, s->K, ia, ib, u)
+#define ODIS_SYNTH_MG(CL, H) do { if (groups == 1) ODIS_SYNTH_M(CL, H, 1); else if (groups == 2) ODIS_SYNTH_M(CL, H, 2); \
+                                 else ODIS_SYNTH_M(CL, H, 3); } while (0)
+        if (s->half) { if (cells == 2) ODIS_SYNTH_MG(2, true); else ODIS_SYNTH_MG(1, true); }
+        else { if (cells == 2) ODIS_SYNTH_MG(2, false); else ODIS_SYNTH_MG(1, false); }
+#undef ODIS_SYNTH_MG
 #undef ODIS_SYNTH_M
     } else if (s->half) {
         if (cells == 2) ODIS_SYNTH_LANES(2, true); else ODIS_SYNTH_LANES(1, true);
@@ -940,8 +949,9 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
 // synthesis lanes; the analysis's chunking changes only the order of the
 // partial sums.
 // ODIS_SH_TILES="tile_l,chunks,lanes[,cells[,pre]]" (tile_l in {2,4,8}, chunks in
-// {8,16,32,64}, lanes in {1,2,4,8} threads per cell splitting the orders, or 16
-// for one warp per pair of orders (k_sh_synth_m), synthesis cells per thread in
+// {2,4,8,16,32,64}, lanes in {1,2,4,8} threads per cell splitting the orders, or
+// 16, 32, 48 for one warp per pair of orders (k_sh_synth_m) and 1, 2, 3 cell
+// groups per block, synthesis cells per thread in
 // {1,2}, default 2, pre = 1 for the analysis from trig-weighted values formed
 // once per step, default 0) fixes the tiles instead of timing them, e.g. to
 // reproduce a run bit for bit or to profile a given variant.  Anything else is
@@ -953,8 +963,9 @@ static bool forced_tiles(int* f)
     int a = 0, b = 0, c = 0, d = 2, pre = 0;
     const int n = std::sscanf(e, "%d,%d,%d,%d,%d", &a, &b, &c, &d, &pre);
     if (n < 3 || n > 5 || (pre != 0 && pre != 1)) return false;
-    const bool ok = (a == 2 || a == 4 || a == 8) && (b == 8 || b == 16 || b == 32 || b == 64) &&
-                    (c == 1 || c == 2 || c == 4 || c == 8 || c == kSynthPairs) && (d == 1 || d == 2);
+    const bool ok = (a == 2 || a == 4 || a == 8) && (b == 2 || b == 4 || b == 8 || b == 16 || b == 32 || b == 64) &&
+                    (c == 1 || c == 2 || c == 4 || c == 8 || c == kSynthPairs || c == 2 * kSynthPairs ||
+                     c == 3 * kSynthPairs) && (d == 1 || d == 2);
     if (ok) { f[0] = a; f[1] = b; f[2] = c; f[3] = d; f[4] = pre; }
     return ok;
 }
@@ -997,7 +1008,7 @@ static int autotune_t(ShLoading* s)
         if (force && tl != forced[0]) continue;
         const std::vector<int> tiles = make_tiles(s->L, tl, s->half);
         cudaMemcpy(dt, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice);
-        for (int ch : {8, 16, 32, 64})
+        for (int ch : {2, 4, 8, 16, 32, 64})
             for (bool pre : {false, true}) {
                 if (force && (ch != forced[1] || (int)pre != forced[4])) continue;
                 const float ms = force ? 0.f : timeit([&] { launch_analysis<T>(s, tl, dt, (int)tiles.size() / 3, ch, pre, eta, 0); });
@@ -1015,7 +1026,9 @@ static int autotune_t(ShLoading* s)
         st = ODIS_ERR_NOMEM;
     best = 1e30f;
     for (int cells : {2, 1})
-        for (int lanes : {1, 2, 4, 8, kSynthPairs}) {
+        for (int lanes : {1, 2, 4, 8, kSynthPairs, 2 * kSynthPairs, 3 * kSynthPairs}) {
+            // three groups of the widest order-pair blocks exceed 1024 threads
+            if (lanes == 3 * kSynthPairs && 3 * std::min(s->L / 2 + 1, kSynthMaxWarps) * 32 > kSynthMaxThreads) continue;
             if (force && (lanes != forced[2] || cells != forced[3])) continue;
             const float ms = force ? 0.f : timeit([&] { launch_synth<T>(s, lanes, cells, 0); });
             if (ms < best) { best = ms; s->lanes = lanes; s->cells = cells; }

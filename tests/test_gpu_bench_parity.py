@@ -83,10 +83,11 @@ def test_level6_sh16_fp32_variant(level6):
     sol.close()
 
 
-# (degrees per analysis tile, cell chunks, synthesis lanes (16: a warp per order pair), cells per synthesis
-# thread, analysis from precomputed trig-weighted values): every value of each parameter appears
+# (degrees per analysis tile, cell chunks, synthesis lanes (16, 32, 48: a warp per order pair, 1-3 cell
+# groups per block), cells per synthesis thread, analysis from precomputed trig-weighted values): every
+# value of each parameter appears
 TILES = [(2, 8, 1, 1, 0), (4, 16, 2, 2, 1), (8, 32, 4, 1, 0), (2, 64, 8, 2, 1), (4, 8, 16, 1, 1),
-         (8, 64, 16, 2, 0), (2, 16, 16, 2, 1)]
+         (8, 64, 16, 2, 0), (2, 16, 16, 2, 1), (4, 4, 32, 1, 1), (2, 2, 48, 2, 0)]
 
 
 @pytest.mark.parametrize("precision", [0, 2, 1])
