@@ -327,15 +327,17 @@ __global__ void __launch_bounds__(kStepThreads) k_power_partial(FaceCoef<T> fc, 
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int Ep = sc.Ep;
     const T* __restrict__ vin = ((it & 1) ? st.v[1] : st.v[0]);
-    double pw = 0.0;
+    T pw = T(0);
     if (e < sc.E) {
         T tsum = T(0);
 #pragma unroll
         for (int k = 0; k < kTrisk; k++) tsum = fmaT<T>(__ldg(&fc.w[k * Ep + e]), vin[__ldg(&fc.nbr[k * Ep + e])], tsum);
         const T ve = vin[e];
-        pw = (double)face_diss(__ldg(&fc.diss[e]), fmaT<T>(ve, ve, tsum * tsum), sc.quad);
+        pw = face_diss(__ldg(&fc.diss[e]), fmaT<T>(ve, ve, tsum * tsum), sc.quad);
     }
-    const double bs = block_sum<kStepThreads>(pw, s_red);
+    // the face kernel's block reduction, so that a run's last power value has the
+    // bits it would have inside a longer run
+    const double bs = block_power<T>(pw, s_red);
     if (threadIdx.x == 0) st.partial[(it - *st.run_first) * gridDim.x + blockIdx.x] = bs;
 }
 

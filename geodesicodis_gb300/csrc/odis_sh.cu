@@ -955,7 +955,8 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
 // {1,2}, default 2, pre = 1 for the analysis from trig-weighted values formed
 // once per step, default 0) fixes the tiles instead of timing them, e.g. to
 // reproduce a run bit for bit or to profile a given variant.  Anything else is
-// ignored.
+// ignored, and so are synthesis lanes whose blocks would exceed 1024 threads at
+// this degree (two or three cell groups of 17 order-pair warps at l_max 32).
 static bool forced_tiles(int* f)
 {
     const char* e = std::getenv("ODIS_SH_TILES");
@@ -982,9 +983,12 @@ static int autotune_t(ShLoading* s)
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
+    // a candidate whose launch the driver refuses is never chosen
     auto timeit = [&](auto&& body) {
         float best = 1e30f;
+        (void)cudaGetLastError();
         body();
+        if (cudaGetLastError() != cudaSuccess) return best;
         for (int r = 0; r < 3; r++) {
             cudaEventRecord(a);
             for (int q = 0; q < 10; q++) body();
@@ -1025,12 +1029,17 @@ static int autotune_t(ShLoading* s)
         cudaMemcpy(s->tiles, best_tiles.data(), sizeof(int) * best_tiles.size(), cudaMemcpyHostToDevice) != cudaSuccess)
         st = ODIS_ERR_NOMEM;
     best = 1e30f;
+    // order-pair blocks hold groups x (warps per group) x 32 threads, at most 1024
+    auto synth_fits = [&](int lanes) {
+        return lanes % kSynthPairs != 0 ||
+               (lanes / kSynthPairs) * std::min(s->L / 2 + 1, kSynthMaxWarps) * 32 <= kSynthMaxThreads;
+    };
+    const bool force_synth = force && synth_fits(forced[2]);
     for (int cells : {2, 1})
         for (int lanes : {1, 2, 4, 8, kSynthPairs, 2 * kSynthPairs, 3 * kSynthPairs}) {
-            // three groups of the widest order-pair blocks exceed 1024 threads
-            if (lanes == 3 * kSynthPairs && 3 * std::min(s->L / 2 + 1, kSynthMaxWarps) * 32 > kSynthMaxThreads) continue;
-            if (force && (lanes != forced[2] || cells != forced[3])) continue;
-            const float ms = force ? 0.f : timeit([&] { launch_synth<T>(s, lanes, cells, 0); });
+            if (!synth_fits(lanes)) continue;
+            if (force_synth && (lanes != forced[2] || cells != forced[3])) continue;
+            const float ms = force_synth ? 0.f : timeit([&] { launch_synth<T>(s, lanes, cells, 0); });
             if (ms < best) { best = ms; s->lanes = lanes; s->cells = cells; }
         }
     if constexpr (std::is_same<T, float>::value) {
