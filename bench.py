@@ -560,13 +560,21 @@ def run_level8(args) -> dict:
     t = time.perf_counter()
     mesh = g.Mesh.generate(8, RADIUS)
     t_mesh = time.perf_counter() - t
+    g.Mesh.generate(2, RADIUS, device=True)          # context and module load outside the timing
+    t = time.perf_counter()
+    mesh_dev = g.Mesh.generate(8, RADIUS, device=True)
+    t_mesh_dev = time.perf_counter() - t
+    dev_rel, dev_bad = mesh_dev.compare(mesh)
+    del mesh_dev
     angvel, P, _, _ = g.derive_time(ANGVEL_IN, 118394.0 / 8000)
     w = mesh.gravity_wave_omega(GRAV, h)
     n = g.stable_steps_per_orbit(P, w, 0.95)
     fac = sh_factors(32)
     E, N = mesh.n_edges, mesh.n_cells
     out = {"workload": "level 8, FULL tide (e 0.0047, obliquity 0.2 deg), h 20 km, drag 1e-6, SH l_max 32",
-           "cells": N, "faces": E, "mesh_seconds": t_mesh, "steps_per_orbit_stable": n,
+           "cells": N, "faces": E, "mesh_seconds": t_mesh, "mesh_seconds_device": t_mesh_dev,
+           "mesh_device_vs_host": {"integer_mismatches": dev_bad, "geometry_rel": dev_rel},
+           "steps_per_orbit_stable": n,
            "omega_dt_at_8000_steps_per_orbit": w * P / 8000, "timed_steps": args.case_steps, "methods": {}}
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))

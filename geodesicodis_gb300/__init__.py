@@ -78,6 +78,12 @@ _SIGS = {
     "odis_grid_generate_file": ([C.c_int, C.c_char_p], C.c_int),
     "odis_mesh_from_file": ([C.c_char_p, C.c_double, C.POINTER(_V)], C.c_int),
     "odis_mesh_generate": ([C.c_int, C.c_double, C.POINTER(_V)], C.c_int),
+    "odis_mesh_generate_device": ([C.c_int, C.c_double, C.POINTER(_V)], C.c_int),
+    "odis_mesh_from_file_device": ([C.c_char_p, C.c_double, C.POINTER(_V)], C.c_int),
+    "odis_mesh_from_arrays_device": ([C.c_int, _D, _I, _D, C.c_double, C.POINTER(_V)], C.c_int),
+    "odis_mesh_from_arrays": ([C.c_int, _D, _I, _D, C.c_double, C.POINTER(_V)], C.c_int),
+    "odis_grid_generate_arrays": ([C.c_int, C.c_int, _D, _I, _D], C.c_int),
+    "odis_mesh_compare": ([_V, _V, _D, C.POINTER(C.c_longlong)], C.c_int),
     "odis_mesh_from_arrays": ([C.c_int, _D, _I, _D, C.c_double, C.POINTER(_V)], C.c_int),
     "odis_mesh_sizes": ([_V, _I, _I, _I], C.c_int),
     "odis_mesh_field": ([_V, C.c_int, _D], C.c_int),
@@ -171,6 +177,16 @@ def _vp(a: np.ndarray):
 def generate_grid_file(level: int, path: str | os.PathLike) -> None:
     """Icosahedral grid at `level` (10*4^level+2 cells) in the reference grid-file format."""
     _ck(lib().odis_grid_generate_file(int(level), os.fsencode(str(path))), "odis_grid_generate_file")
+
+
+def generate_grid(level: int, device: bool = False):
+    """The level-n icosahedral grid as arrays (node_deg [N,2], friends [N,6], cent_deg [N,6,2], degrees), the
+    contents of generate_grid_file; device=True generates it with kernels on the current GPU."""
+    n = 10 * 4 ** int(level) + 2
+    nd, fr, cd = np.zeros((n, 2)), np.zeros((n, 6), np.int32), np.zeros((n, 6, 2))
+    _ck(lib().odis_grid_generate_arrays(int(level), int(bool(device)), _dp(nd), fr.ctypes.data_as(_I), _dp(cd)),
+        "odis_grid_generate_arrays")
+    return nd, fr, cd
 
 
 def analytical_state(params: Params, mesh: "Mesh", t: float = 0.0):
@@ -282,17 +298,40 @@ class Mesh:
         _ck(lib().odis_mesh_sizes(self._h, C.byref(n), C.byref(e), C.byref(v)), "odis_mesh_sizes")
         self.n_cells, self.n_edges, self.n_vertices = n.value, e.value, v.value
 
+    # device=True: geometry and TRiSK weights built by kernels on the current GPU (and the grid generated
+    # there); integer arrays identical to the host build, geometry to the device's transcendental rounding
+
     @classmethod
-    def from_file(cls, path: str | os.PathLike, radius: float) -> "Mesh":
+    def from_file(cls, path: str | os.PathLike, radius: float, device: bool = False) -> "Mesh":
         h = C.c_void_p()
-        _ck(lib().odis_mesh_from_file(os.fsencode(str(path)), radius, C.byref(h)), "odis_mesh_from_file")
+        fn = "odis_mesh_from_file_device" if device else "odis_mesh_from_file"
+        _ck(getattr(lib(), fn)(os.fsencode(str(path)), radius, C.byref(h)), fn)
         return cls(h.value)
 
     @classmethod
-    def generate(cls, level: int, radius: float) -> "Mesh":
+    def generate(cls, level: int, radius: float, device: bool = False) -> "Mesh":
         h = C.c_void_p()
-        _ck(lib().odis_mesh_generate(int(level), radius, C.byref(h)), "odis_mesh_generate")
+        fn = "odis_mesh_generate_device" if device else "odis_mesh_generate"
+        _ck(getattr(lib(), fn)(int(level), radius, C.byref(h)), fn)
         return cls(h.value)
+
+    @classmethod
+    def from_arrays(cls, node_sph: np.ndarray, friends: np.ndarray, cent_sph: np.ndarray, radius: float,
+                    device: bool = False) -> "Mesh":
+        """node_sph [N,2] and cent_sph [N,6,2] in radians, friends [N,6] (-1 in slot 5 for pentagons)."""
+        ns = np.ascontiguousarray(node_sph, np.float64)
+        fr = np.ascontiguousarray(friends, np.int32)
+        cs = np.ascontiguousarray(cent_sph, np.float64)
+        h = C.c_void_p()
+        fn = "odis_mesh_from_arrays_device" if device else "odis_mesh_from_arrays"
+        _ck(getattr(lib(), fn)(len(ns), _dp(ns), fr.ctypes.data_as(_I), _dp(cs), radius, C.byref(h)), fn)
+        return cls(h.value)
+
+    def compare(self, other: "Mesh"):
+        """(largest max|a-b|/max|b| over the floating-point arrays, differing integer entries) against other."""
+        rel, bad = C.c_double(), C.c_longlong()
+        _ck(lib().odis_mesh_compare(self._h, other._h, C.byref(rel), C.byref(bad)), "odis_mesh_compare")
+        return rel.value, bad.value
 
     def field(self, which: int) -> np.ndarray:
         n = self.n_cells if which in (3, 12, 13) else self.n_edges

@@ -39,13 +39,19 @@ def sources() -> list[Path]:
     return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
 
 
+# Per-file device flags.  The setup kernels (grid generation, mesh build) run
+# with unfused multiply-adds, as the host code does, so that their sums and
+# products round as the host's.
+FILE_FLAGS = {"odis_mesh_dev.cu": ["-fmad=false"]}
+
+
 def _compile(src: Path, nvcc: str, extra: list[str]) -> Path:
     obj = BUILD / (src.name + ".o")
     deps = [src] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "odis_gpu.h"]
     if obj.exists() and obj.stat().st_mtime > max(d.stat().st_mtime for d in deps):
         return obj
     lang = [] if src.suffix == ".cu" else ["-x", "cu"]
-    cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, *lang, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), *extra, *lang, "-c", str(src), "-o", str(obj)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src.name}:\n{res.stdout}\n{res.stderr}")

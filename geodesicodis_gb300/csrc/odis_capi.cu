@@ -149,13 +149,110 @@ extern "C" odis_status odis_grid_generate_file(int level, const char* path)
     return write_grid(g, path);
 }
 
-static odis_status mesh_from_grid(const GridArrays& g, double radius, odis_mesh** out)
+static odis_status mesh_from_grid(const GridArrays& g, double radius, odis_mesh** out, bool device = false)
 {
     const double rc = kPi / 180.0;
     std::vector<double> ns(g.node_deg.size()), cs(g.cent_deg.size());
     for (size_t k = 0; k < ns.size(); k++) ns[k] = g.node_deg[k] * rc;
     for (size_t k = 0; k < cs.size(); k++) cs[k] = g.cent_deg[k] * rc;
-    return odis_mesh_from_arrays(g.N, ns.data(), g.friends.data(), cs.data(), radius, out);
+    return device ? odis_mesh_from_arrays_device(g.N, ns.data(), g.friends.data(), cs.data(), radius, out)
+                  : odis_mesh_from_arrays(g.N, ns.data(), g.friends.data(), cs.data(), radius, out);
+}
+
+extern "C" odis_status odis_grid_generate_arrays(int level, int on_device, double* node_deg, int* friends,
+                                                 double* cent_deg)
+{
+    if (!node_deg || !friends || !cent_deg) return ODIS_ERR_ARG;
+    GridArrays g;
+    const int st = on_device ? generate_grid_device(level, g) : generate_grid(level, g);
+    if (st != ODIS_OK) return st;
+    std::memcpy(node_deg, g.node_deg.data(), sizeof(double) * g.node_deg.size());
+    std::memcpy(friends, g.friends.data(), sizeof(int) * g.friends.size());
+    std::memcpy(cent_deg, g.cent_deg.data(), sizeof(double) * g.cent_deg.size());
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_mesh_from_arrays_device(int n_nodes, const double* node_sph, const int* friends,
+                                                    const double* cent_sph, double radius, odis_mesh** out)
+{
+    if (!out) return ODIS_ERR_ARG;
+    *out = nullptr;
+    odis_mesh* m = new (std::nothrow) odis_mesh;
+    if (!m) return ODIS_ERR_NOMEM;
+    int st = build_mesh_device(n_nodes, node_sph, friends, cent_sph, radius, m->m);
+    if (st != ODIS_OK) { delete m; return st; }
+    *out = m;
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_mesh_from_file_device(const char* path, double radius, odis_mesh** out)
+{
+    if (!path || !out) return ODIS_ERR_ARG;
+    GridArrays g;
+    int st = read_grid(path, g);
+    if (st != ODIS_OK) return st;
+    return mesh_from_grid(g, radius, out, true);
+}
+
+extern "C" odis_status odis_mesh_generate_device(int level, double radius, odis_mesh** out)
+{
+    if (!out) return ODIS_ERR_ARG;
+    GridArrays g;
+    int st = generate_grid_device(level, g);
+    if (st != ODIS_OK) return st;
+    return mesh_from_grid(g, radius, out, true);
+}
+
+// largest |a - b| of one array over its largest |b|, and integer mismatches;
+// lonlat: (lat, lon) pairs, longitudes compared modulo 2 pi (a point at lon 0
+// may come out at 2 pi)
+template <class T>
+static void cmp_array(const std::vector<T>& a, const std::vector<T>& b, double* rel, long long* bad,
+                      bool lonlat = false)
+{
+    if (a.size() != b.size()) { *bad += (long long)std::max(a.size(), b.size()) + 1; return; }
+    if constexpr (std::is_integral<T>::value) {
+        for (size_t k = 0; k < a.size(); k++) *bad += a[k] != b[k];
+    } else {
+        double d = 0.0, s = 0.0;
+        for (size_t k = 0; k < a.size(); k++) {
+            double dk = std::fabs(a[k] - b[k]);
+            if (lonlat && (k & 1)) dk = std::min(dk, std::fabs(dk - 2 * kPi));
+            d = std::max(d, dk);
+            s = std::max(s, std::fabs(b[k]));
+        }
+        if (d > 0.0) *rel = std::max(*rel, s > 0.0 ? d / s : INFINITY);
+    }
+}
+
+extern "C" odis_status odis_mesh_compare(const odis_mesh* ap, const odis_mesh* bp, double* max_rel, long long* int_mismatches)
+{
+    if (!ap || !bp || !max_rel || !int_mismatches) return ODIS_ERR_ARG;
+    const Mesh &a = ap->m, &b = bp->m;
+    double rel = 0.0;
+    long long bad = (a.N != b.N) + (a.E != b.E) + (a.V != b.V);
+    if (!bad) {
+        for (auto pr : {std::make_pair(&a.friends, &b.friends), std::make_pair(&a.vertexes, &b.vertexes),
+                        std::make_pair(&a.faces, &b.faces), std::make_pair(&a.node_face_dir, &b.node_face_dir),
+                        std::make_pair(&a.face_nodes, &b.face_nodes), std::make_pair(&a.interp_friends, &b.interp_friends),
+                        std::make_pair(&a.interp_n, &b.interp_n), std::make_pair(&a.vert_nodes, &b.vert_nodes),
+                        std::make_pair(&a.face_verts, &b.face_verts), std::make_pair(&a.vert_faces, &b.vert_faces),
+                        std::make_pair(&a.vert_face_dir, &b.vert_face_dir)})
+            cmp_array(*pr.first, *pr.second, &rel, &bad);
+        for (auto pr : {std::make_pair(&a.node_sph, &b.node_sph), std::make_pair(&a.cent_sph, &b.cent_sph),
+                        std::make_pair(&a.vert_sph, &b.vert_sph), std::make_pair(&a.face_centre, &b.face_centre),
+                        std::make_pair(&a.face_int, &b.face_int)})
+            cmp_array(*pr.first, *pr.second, &rel, &bad, true);
+        for (auto pr : {std::make_pair(&a.cv_area, &b.cv_area), std::make_pair(&a.face_len, &b.face_len),
+                        std::make_pair(&a.face_dist, &b.face_dist), std::make_pair(&a.face_area, &b.face_area),
+                        std::make_pair(&a.face_m, &b.face_m), std::make_pair(&a.face_normal, &b.face_normal),
+                        std::make_pair(&a.face_nxyz, &b.face_nxyz), std::make_pair(&a.interp_w, &b.interp_w),
+                        std::make_pair(&a.vert_R, &b.vert_R), std::make_pair(&a.vert_area, &b.vert_area)})
+            cmp_array(*pr.first, *pr.second, &rel, &bad);
+    }
+    *max_rel = rel;
+    *int_mismatches = bad;
+    return ODIS_OK;
 }
 
 extern "C" odis_status odis_mesh_from_arrays(int n_nodes, const double* node_sph, const int* friends,

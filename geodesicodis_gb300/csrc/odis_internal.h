@@ -56,6 +56,12 @@ struct Mesh {
 
 int build_mesh(int N, const double* node_sph, const int* friends, const double* cent_sph,
                double radius, Mesh& m);
+// The same grid and mesh computed by kernels on the current device
+// (odis_mesh_dev.cu): integers identical to the host's, geometry to the last
+// bit of CUDA's transcendental functions.
+int generate_grid_device(int level, GridArrays& g);
+int build_mesh_device(int N, const double* node_sph, const int* friends, const double* cent_sph,
+                      double radius, Mesh& m);
 
 // Forcing as a single-frequency pair: U_i(t) = cos(M) Ua_i + sin(M) Ub_i with
 // M = angvel * t, for the ECC / OBLIQ / OBLIQ_WEST / FULL potentials; zero for

@@ -191,6 +191,29 @@ odis_status odis_mesh_vertex_field(const odis_mesh* m, int which, double* out);
 odis_status odis_mesh_vertex_topology(const odis_mesh* m, int* vert_nodes, int* vert_faces, int* vert_face_dir,
                                       int* face_verts);
 void odis_mesh_destroy(odis_mesh* m);
+
+/* ---- grid generation and mesh build on the GPU ------------------------- */
+/* The same steps as odis_grid_generate_file / odis_mesh_from_arrays
+ * (ReadMeshFile + AssignFaces + the geometry and TRiSK weights of
+ * src/mesh.cpp:436-1154), one kernel per step over nodes, faces, vertices and
+ * lattice points of the current device; the result is an ordinary odis_mesh
+ * (host arrays).  Numbering, friends, stencils and every other integer array
+ * are identical to the host build's; the geometry agrees with it to the last
+ * bit of the device's transcendental functions (odis_mesh_compare reports by
+ * how much).  Temporary device memory only, freed before return; level 8 needs
+ * about 0.5 GB. */
+odis_status odis_mesh_generate_device(int level, double radius, odis_mesh** out);
+odis_status odis_mesh_from_file_device(const char* path, double radius, odis_mesh** out);
+odis_status odis_mesh_from_arrays_device(int n_nodes, const double* node_sph, const int* friends,
+                                         const double* cent_sph, double radius, odis_mesh** out);
+/* The level-n icosahedral grid as arrays (what odis_grid_generate_file
+ * writes): node_deg [N][2], friends [N][6] and cent_deg [N][6][2] in degrees,
+ * N = 10*4^n+2, generated on the host (on_device = 0) or the current device. */
+odis_status odis_grid_generate_arrays(int level, int on_device, double* node_deg, int* friends, double* cent_deg);
+/* Compare two meshes array by array: *int_mismatches counts differing entries
+ * of the integer arrays (sizes included), *max_rel is the largest
+ * max|a - b| / max|b| over the floating-point arrays (longitudes modulo 2 pi). */
+odis_status odis_mesh_compare(const odis_mesh* a, const odis_mesh* b, double* max_rel, long long* int_mismatches);
 /* Largest gravity-wave frequency (rad/s) of the discrete operator: sqrt of the
  * largest eigenvalue of -g h D G, by `iters` power iterations (host).  The
  * reference's time loop (AB3 momentum with the old eta, then AB3 continuity

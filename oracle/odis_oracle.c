@@ -1717,14 +1717,17 @@ int orc_generate_grid_file(int level, const char *path)
                 }
             }
             if (st != 0 || (k != 5 && k != 6)) { st = -5; break; }
-            /* clockwise seen from outside: descending angle in the local east/north plane */
+            /* clockwise seen from outside: descending angle in the local east/north plane; a
+             * neighbour due west (on atan2's branch cut, where a rounding-level north component
+             * decides between +pi and -pi) is put at +pi, first */
             double lr = atan2(p.y, p.x);
             orc_v3 east = {-sin(lr), cos(lr), 0.0};
             orc_v3 north = {p.y * east.z - p.z * east.y, p.z * east.x - p.x * east.z, p.x * east.y - p.y * east.x};
             orc_nbr_ang ang[6];
             for (int j = 0; j < k; j++) {
                 orc_v3 d = {pos[nb[j]].x - p.x, pos[nb[j]].y - p.y, pos[nb[j]].z - p.z};
-                ang[j].ang = atan2(d.x * north.x + d.y * north.y + d.z * north.z, d.x * east.x + d.y * east.y + d.z * east.z);
+                double dn = d.x * north.x + d.y * north.y + d.z * north.z, de = d.x * east.x + d.y * east.y + d.z * east.z;
+                ang[j].ang = (de < 0.0 && fabs(dn) <= 1e-12 * fabs(de)) ? 3.14159265358979323846 : atan2(dn, de);
                 ang[j].node = nb[j];
             }
             qsort(ang, k, sizeof(orc_nbr_ang), ang_desc);
