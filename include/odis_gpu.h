@@ -376,10 +376,12 @@ odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms);
  * ODIS_SH_TILES="tile_l,chunks,lanes[,cells[,pre]]" names one.  Any pointer
  * may be NULL.
  * ODIS_FP32 also has tensor-core transforms (tcgen05, fp16 hi/lo operand pairs,
- * FP32 accumulation); odis_create times them against the CUDA-core ones and
- * keeps the faster, unless ODIS_SH_TC=1 (tensor cores) or ODIS_SH_TC=0 (CUDA
- * cores) fixes the choice.  With the tensor-core transforms tile_l = 0, chunks
- * = analysis chunks and lanes = 128-cell tiles per synthesis pass. */
+ * FP32 accumulation), retired from the default path because they are slower.
+ * They need the full basis, so they are built only with ODIS_SH_TC=1 (which
+ * selects them) or on a mesh without antipodal pairs, where odis_create times
+ * them against the CUDA-core transforms and keeps the faster (ODIS_SH_TC=0
+ * keeps the CUDA cores).  With the tensor-core transforms tile_l = 0, chunks =
+ * analysis chunks and lanes = 128-cell tiles per synthesis pass. */
 odis_status odis_sh_tiles(const odis_ctx* c, int* tile_l, int* chunks, int* lanes, int* cells, int* pre);
 
 /* Storage of the self-gravity basis (0s without self-gravity).  On a centrally
