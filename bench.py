@@ -236,16 +236,16 @@ def _replica_setup(cuda: bool = True):
 FP64_INST_FACE, FP64_INST_FACE_SG, FP64_INST_CELL = 29, 32, 10
 
 
-def sh_fp64_inst(K: int, cells: int, L: int, half: bool, pre: bool, ntiles: int) -> float:
+def sh_fp64_inst(K: int, cells: int, L: int, half: bool, pre: bool, ntiles: int, dense: bool = False) -> float:
     """FP64 instructions of one self-gravity step over the `cells` the basis covers, for the variant the
     setup chose: each transform does K multiply-adds per cell (two per (l, m > 0), one per (l, 0)); the
     trig-weighted values cost 4 (half basis: cos e, sin e, cos o, sin o) or 2 multiplies per cell and
-    order when formed once per step (pre), or 2 per cell and analysis tile otherwise; the synthesis
-    combines each order's sums with its trig values in 4 (half) or 2 multiply-adds per cell.  The pair,
-    fold and K x K solve work is below 1 %."""
+    order when formed once per step (pre), or 2 per cell and analysis tile otherwise; the factored
+    synthesis combines each order's sums with its trig values in 4 (half) or 2 multiply-adds per cell,
+    the dense synthesis (Z t) has no such step.  The pair, fold and K x K solve work is below 1 %."""
     per_order = 4 if half else 2
     trig = per_order * cells * (L + 1) if pre else 2 * cells * ntiles
-    return 2.0 * K * cells + trig + per_order * cells * (L + 1)
+    return 2.0 * K * cells + trig + (0 if dense else per_order * cells * (L + 1))
 
 
 def run_ours(args) -> dict:
@@ -373,9 +373,12 @@ def run_ours(args) -> dict:
     dominant = max(per_step, key=per_step.get)
     face_bytes = E * (19 * 8 + 48)
     cell_bytes = N * (13 * 8 + 24)
-    # self-gravity: the stored basis read once per transform, plus the node vectors each kernel moves
+    # self-gravity: the stored basis read by the analysis and the factored synthesis, or the dense
+    # synthesis matrix Z (K rows of the basis's cells, lanes < 0), plus the node vectors each kernel moves
     # (half basis: pair kernel eta in, e/o out; analysis e/o in; synthesis usg out -> 4 N values)
-    sh_bytes = 2 * layout["basis_bytes"] + (4 if layout["half"] else 2) * N * 8
+    dense = tiles["lanes"] < 0
+    z_bytes = K * layout["cells"] * 8
+    sh_bytes = layout["basis_bytes"] + (z_bytes if dense else layout["basis_bytes"]) + (4 if layout["half"] else 2) * N * 8
     alg = {"face_step": face_bytes, "cell_step": cell_bytes, "sh_self_gravity": sh_bytes}[dominant]
     achieved = alg / (per_step[dominant] / 1e3) / 1e9
     tl = max(1, tiles["tile_l"])
@@ -383,7 +386,7 @@ def run_ours(args) -> dict:
         ntiles = sum(((LMAX - st) // 2) // tl + 1 for m in range(LMAX + 1) for st in (m, m + 1) if st <= LMAX)
     else:
         ntiles = sum((LMAX - m) // tl + 1 for m in range(LMAX + 1))
-    sh_inst = sh_fp64_inst(K, layout["cells"], LMAX, layout["half"], bool(tiles["pre"]), ntiles)
+    sh_inst = sh_fp64_inst(K, layout["cells"], LMAX, layout["half"], bool(tiles["pre"]), ntiles, dense)
     inst = {"face_step": E * FP64_INST_FACE_SG, "cell_step": N * FP64_INST_CELL, "sh_self_gravity": sh_inst}[dominant]
     fp64_ach = inst * 2.0 / (per_step[dominant] / 1e3) / 1e12
     plain = {}

@@ -627,6 +627,7 @@ static int build_persist_plan(odis_ctx* c, const Mesh& m)
 }
 
 static int choose_exec_path(odis_ctx* c);
+static int choose_sh_synthesis(odis_ctx* c);
 
 extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, odis_ctx** out)
 {
@@ -790,7 +791,8 @@ extern "C" odis_status odis_create(const odis_params* p, const odis_mesh* mp, od
         if (st == ODIS_OK) st = adv_state_alloc(c->adv, p->precision, p->h, Ua, Ub);
         if (st != ODIS_OK) return st;
     } else {
-        st = choose_exec_path(c.get());
+        st = choose_sh_synthesis(c.get());
+        if (st == ODIS_OK) st = choose_exec_path(c.get());
         if (st != ODIS_OK) return st;
     }
     *out = c.release();
@@ -1410,6 +1412,33 @@ static int choose_exec_path(odis_ctx* c)
     c->exec_ms[1] = best[1];
     c->persist_auto = c->persist_ok && best[1] < best[0];
     c->persist_on = c->persist_auto;
+    c->launches = 0;
+    return odis_set_state(c, 0, nullptr, nullptr, nullptr, nullptr);
+}
+
+// The dense self-gravity synthesis against the factored one over whole
+// graph-replayed steps (its matrix competes for L2 with the step's other
+// arrays, which the transforms' own timing does not see): best of two runs of
+// 3 graph chunks each way after a warm-up, the graph captured again for each
+// choice; keeps the faster and puts the context back in its fresh state.
+static int choose_sh_synthesis(odis_ctx* c)
+{
+    if (!c->sh || !sh_dense_candidate(c->sh)) return ODIS_OK;
+    const int n = 3 * kGraphSteps;
+    double best[2] = {1e300, 1e300};
+    for (int rep = 0; rep < 3; rep++) {
+        for (int mode = 0; mode < 2; mode++) {
+            sh_try_dense(c->sh, mode == 1);
+            if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+            const auto t0 = std::chrono::steady_clock::now();
+            const int st = odis_run_steps(c, n, nullptr, ODIS_MEM_DEVICE);
+            const auto t1 = std::chrono::steady_clock::now();
+            if (st != ODIS_OK && st != ODIS_ERR_NONFINITE) return st;
+            if (rep > 0) best[mode] = std::min(best[mode], std::chrono::duration<double, std::milli>(t1 - t0).count() / n);
+        }
+    }
+    sh_set_dense(c->sh, best[1] < best[0]);
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     c->launches = 0;
     return odis_set_state(c, 0, nullptr, nullptr, nullptr, nullptr);
 }

@@ -572,6 +572,137 @@ __global__ void __launch_bounds__(256) k_gram(const double* __restrict__ Y, int 
     }
 }
 
+// (l, m, sin) of coefficient k = sh_col(l, m, sin)
+__host__ __device__ inline void sh_lms(int k, int& l, int& m, int& s)
+{
+    l = 0;
+    while ((l + 1) * (l + 1) <= k) l++;
+    const int r = k - l * l;
+    m = (r + 1) >> 1;
+    s = r == 0 ? 0 : ((r + 1) & 1);
+}
+
+// Dense synthesis matrix Z[k][h] = sum_j Y_j(h) M[j][k] (setup only, FP64):
+// usg = Y c = Y M t = Z t, so the per-step synthesis reads t directly and the
+// K x K product disappears from the step.  Y_j(h) = P[row(j)][h] trig[2m+s][h]
+// is formed while the tile is staged.  64 x 64 output tiles, 16 j per stage,
+// 4 x 4 outputs per thread.  Rows k of Z are written in the method's type.
+template <class T>
+__global__ void __launch_bounds__(256) k_sh_zmat(const double* __restrict__ P, const double* __restrict__ trig,
+                                                 const double* __restrict__ M, int L, int K, int np,
+                                                 T* __restrict__ Z)
+{
+    __shared__ double ys[16][64 + 1], ms[16][64 + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int h0 = blockIdx.x * 64, k0 = blockIdx.y * 64;
+    double acc[4][4] = {};
+    for (int j0 = 0; j0 < K; j0 += 16) {
+        for (int q = threadIdx.x; q < 16 * 64; q += 256) {
+            const int jj = q >> 6, c = q & 63, j = j0 + jj;
+            double y = 0.0, mv = 0.0;
+            if (j < K) {
+                int l, m, s;
+                sh_lms(j, l, m, s);
+                y = P[(size_t)p_row(L, l, m) * np + h0 + c] * trig[(size_t)(2 * m + s) * np + h0 + c];
+                if (k0 + c < K) mv = M[(size_t)j * K + k0 + c];
+            }
+            ys[jj][c] = y;
+            ms[jj][c] = mv;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++)
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = fma(ys[jj][tx + 16 * a], ms[jj][ty + 16 * b], acc[a][b]);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+        const int k = k0 + ty + 16 * b;
+        if (k >= K) continue;
+#pragma unroll
+        for (int a = 0; a < 4; a++) Z[(size_t)k * np + h0 + tx + 16 * a] = Ar<T>::from(acc[a][b]);
+    }
+}
+
+// Dense synthesis usg = Z t: kW warps split the K rows (warp w takes rows w, w + kW,
+// ...), each lane owns kC cells (h = base + lane + 32 c, so every row load of a warp
+// is one coalesced line), t is staged once per block in the method's type.  Rows are
+// taken four at a time, so each lane has 4 kC loads in flight.  kHalf: rows of even
+// degree add to E, odd to O (a per-row flag in shared memory), and the pair's cells
+// receive E + O and E - O.  The warps' partial sums meet in shared memory in warp
+// order (a fixed order).
+template <class T, bool kHalf, int kW, int kC>
+__global__ void __launch_bounds__(32 * kW) k_sh_synth_z(const T* __restrict__ Z, const double* __restrict__ t, int n,
+                                                        int np, int K, const int* __restrict__ ia,
+                                                        const int* __restrict__ ib, T* __restrict__ usg)
+{
+    pdl_wait();
+    using A = Ar<T>;
+    constexpr int kU = 4;
+    extern __shared__ unsigned char z_raw[];
+    T* tk = reinterpret_cast<T*>(z_raw);                                     // [K]
+    T* se = tk + ((K + 1) & ~1);                                             // [kW][32 kC]
+    T* so = se + kW * 32 * kC;
+    unsigned char* odd = reinterpret_cast<unsigned char*>(so + kW * 32 * kC); // [K] degree parity of row k
+    for (int k = threadIdx.x; k < K; k += 32 * kW) {
+        tk[k] = A::from(t[k]);
+        int l = 0;
+        while ((l + 1) * (l + 1) <= k) l++;
+        odd[k] = (unsigned char)(kHalf && (l & 1));
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int base = blockIdx.x * 32 * kC;
+    T e[kC], o[kC];
+#pragma unroll
+    for (int c = 0; c < kC; c++) { e[c] = A::zero(); o[c] = A::zero(); }
+    const T* zc = Z + base + lane;
+    for (int k0 = w; k0 < K; k0 += kU * kW) {
+        T z[kU][kC];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int k = k0 + u * kW;
+#pragma unroll
+            for (int c = 0; c < kC; c++) z[u][c] = k < K ? zc[(size_t)k * np + 32 * c] : A::zero();
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int k = k0 + u * kW;
+            if (k >= K) break;
+            const T tv = tk[k];
+            if (odd[k]) {
+#pragma unroll
+                for (int c = 0; c < kC; c++) o[c] = A::fma_acc(z[u][c], tv, o[c]);
+            } else {
+#pragma unroll
+                for (int c = 0; c < kC; c++) e[c] = A::fma_acc(z[u][c], tv, e[c]);
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kC; c++) {
+        se[w * 32 * kC + 32 * c + lane] = A::norm(e[c]);
+        so[w * 32 * kC + 32 * c + lane] = A::norm(o[c]);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < 32 * kC; q += 32 * kW) {
+        T E = se[q], O = so[q];
+#pragma unroll
+        for (int v = 1; v < kW; v++) { E = A::add(E, se[v * 32 * kC + q]); O = A::add(O, so[v * 32 * kC + q]); }
+        const int h = base + q;
+        if (h >= n) continue;
+        if constexpr (kHalf) {
+            usg[__ldg(&ia[h])] = A::add(E, O);
+            usg[__ldg(&ib[h])] = A::sub(E, O);
+        } else {
+            usg[h] = E;
+        }
+    }
+}
+
 }  // namespace
 
 int sh_autotune(ShLoading* s);
@@ -601,6 +732,12 @@ struct ShLoading {
     void* eo = nullptr;          // [2][Nhp] e = eta_a + eta_b, o = eta_a - eta_b, or the trig-weighted values
                                  // [4(L+1)][Nhp] (half) / [2(L+1)][Np] (full) of the pre analysis; method type
     unsigned* arrivals = nullptr; // [analysis tiles] blocks of a tile that finished this step (reset by the last)
+    // dense synthesis usg = Z t (Z = Y F G^-1, [K][bp], method type), chosen by the timing when faster than the
+    // K x K product plus the factored synthesis: zw warps per block (0: factored), zc cells per lane
+    void* Z = nullptr;
+    int zw = 0, zc = 1;
+    int zw_cand = 0, zc_cand = 1;   // the fastest dense variant in isolation, offered to the whole-step timing
+    bool zforced = false;           // ODIS_SH_TILES named the synthesis
     // cells and row stride of the stored basis
     int bn() const { return half ? Nh : N; }
     int bp() const { return half ? Nhp : Np; }
@@ -724,6 +861,8 @@ static bool upload_rows(void** d, const std::vector<double>& h)
     return cudaMemcpy(*d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice) == cudaSuccess;
 }
 
+static bool forced_tiles(int* f);
+
 int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int precision, int Np, int* status)
 {
     *out = nullptr;
@@ -820,11 +959,47 @@ int sh_create(ShLoading** out, const Mesh& m, int L, const double* factors, int 
          cudaMemset(s->part, 0, 8 * (size_t)K * kMaxChunks) == cudaSuccess;
     ok = ok && cudaMalloc(&s->FGinv, sizeof(double) * G.size()) == cudaSuccess &&
          cudaMemcpy(s->FGinv, G.data(), sizeof(double) * G.size(), cudaMemcpyHostToDevice) == cudaSuccess;
-    ok = ok && cudaMalloc(&s->t, sizeof(double) * K) == cudaSuccess && cudaMalloc(&s->coef, 8 * (size_t)K) == cudaSuccess;
+    ok = ok && cudaMalloc(&s->t, sizeof(double) * K) == cudaSuccess && cudaMalloc(&s->coef, 8 * (size_t)K) == cudaSuccess &&
+         cudaMemset(s->t, 0, sizeof(double) * K) == cudaSuccess;
     // arrival counters: one per analysis tile, at most (L+1)^2 tiles (one degree per tile)
     ok = ok && cudaMalloc(&s->arrivals, sizeof(unsigned) * (size_t)K) == cudaSuccess &&
          cudaMemset(s->arrivals, 0, sizeof(unsigned) * (size_t)K) == cudaSuccess;
     if (!ok) { sh_destroy(s); return ODIS_ERR_NOMEM; }
+    // dense synthesis matrix, from the FP64 rows and F G^-1.  It pays only while it stays in L2 with the
+    // rest of the step (measured: FP32 at level 6, 24 MB; FP64 and DF64 at level 6, 48 MB, and every
+    // method at level 8 ran slower with it), so it is built up to 32 MB, or when ODIS_SH_TILES names the
+    // dense synthesis or ODIS_SH_DENSE=1 asks for it (ODIS_SH_DENSE=0: never).
+    {
+        const char* ed = std::getenv("ODIS_SH_DENSE");
+        const char* et = std::getenv("ODIS_SH_TILES");
+        int f[5] = {0, 0, 0, 2, 0};
+        const bool named = et && forced_tiles(f) && f[2] < 0;
+        const int np = s->bp();
+        const size_t zb = (precision == ODIS_FP32 ? sizeof(float) : sizeof(double)) * (size_t)K * np;
+        const bool want = !(ed && ed[0] == '0') && (named || (ed && ed[0] == '1') || zb <= ((size_t)32 << 20));
+        if (want) {
+            double *dP = nullptr, *dT = nullptr;
+            bool zok = cudaMalloc(&dP, sizeof(double) * P.size()) == cudaSuccess &&
+                       cudaMalloc(&dT, sizeof(double) * trig.size()) == cudaSuccess &&
+                       cudaMalloc(&s->Z, zb) == cudaSuccess &&
+                       cudaMemcpy(dP, P.data(), sizeof(double) * P.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+                       cudaMemcpy(dT, trig.data(), sizeof(double) * trig.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+            if (zok) {
+                const dim3 zg(np / 64, (K + 63) / 64);
+                if (precision == ODIS_FP64) k_sh_zmat<double><<<zg, 256>>>(dP, dT, s->FGinv, L, K, np, (double*)s->Z);
+                else if (precision == ODIS_DF64) k_sh_zmat<df64><<<zg, 256>>>(dP, dT, s->FGinv, L, K, np, (df64*)s->Z);
+                else k_sh_zmat<float><<<zg, 256>>>(dP, dT, s->FGinv, L, K, np, (float*)s->Z);
+                zok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+            }
+            cudaFree(dP);
+            cudaFree(dT);
+            if (!zok) {
+                (void)cudaGetLastError();
+                cudaFree(s->Z);
+                s->Z = nullptr;                          // the factored synthesis still works
+            }
+        }
+    }
     if (precision == ODIS_FP32 && !s->half) {
         double pmax = 0.0;
         for (double x : P) pmax = std::fmax(pmax, std::fabs(x));
@@ -842,7 +1017,7 @@ void sh_destroy(ShLoading* s)
     if (!s) return;
     cudaFree(s->P); cudaFree(s->trig); cudaFree(s->tiles); cudaFree(s->part); cudaFree(s->FGinv);
     cudaFree(s->t); cudaFree(s->coef); cudaFree(s->usg);
-    cudaFree(s->ia); cudaFree(s->ib); cudaFree(s->eo); cudaFree(s->arrivals);
+    cudaFree(s->ia); cudaFree(s->ib); cudaFree(s->eo); cudaFree(s->arrivals); cudaFree(s->Z);
     shtc_destroy(s->tc);
     delete s;
 }
@@ -943,6 +1118,24 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
 #undef ODIS_SYNTH
 }
 
+// dense synthesis usg = Z t with zw warps per block and zc cells per lane
+template <class T>
+static cudaError_t launch_synth_z(const ShLoading* s, int zw, int zc, cudaStream_t st)
+{
+    const int n = s->bn(), np = s->bp(), K = s->K;
+    const int nb = (n + 32 * zc - 1) / (32 * zc);
+    const size_t sm = sizeof(T) * ((size_t)((K + 1) & ~1) + 2 * (size_t)zw * 32 * zc) + (size_t)K;
+    const T* Z = (const T*)s->Z;
+    T* u = (T*)s->usg;
+#define ODIS_SZ(H, W, C) return pdl_launch(k_sh_synth_z<T, H, W, C>, nb, 32 * W, sm, st, Z, (const double*)s->t, n, np, K, \
+                                           (const int*)s->ia, (const int*)s->ib, u)
+#define ODIS_SZ_W(H, C) do { if (zw == 4) ODIS_SZ(H, 4, C); if (zw == 8) ODIS_SZ(H, 8, C); ODIS_SZ(H, 16, C); } while (0)
+    if (s->half) { if (zc == 2) ODIS_SZ_W(true, 2); ODIS_SZ_W(true, 1); }
+    else { if (zc == 2) ODIS_SZ_W(false, 2); ODIS_SZ_W(false, 1); }
+#undef ODIS_SZ_W
+#undef ODIS_SZ
+}
+
 // Self-tuning of the transform tiles: every candidate is timed on this mesh
 // and this device (CUDA events, warm L2, median of three runs of 10 launches)
 // and the fastest is kept.  Results do not depend on the choice of the
@@ -951,7 +1144,8 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
 // ODIS_SH_TILES="tile_l,chunks,lanes[,cells[,pre]]" (tile_l in {2,4,8}, chunks in
 // {2,4,8,16,32,64}, lanes in {1,2,4,8} threads per cell splitting the orders, or
 // 16, 32, 48 for one warp per pair of orders (k_sh_synth_m) and 1, 2, 3 cell
-// groups per block, synthesis cells per thread in
+// groups per block, or -4, -8, -16 for the dense synthesis with that many warps
+// per block, synthesis cells per thread in
 // {1,2}, default 2, pre = 1 for the analysis from trig-weighted values formed
 // once per step, default 0) fixes the tiles instead of timing them, e.g. to
 // reproduce a run bit for bit or to profile a given variant.  Anything else is
@@ -966,7 +1160,7 @@ static bool forced_tiles(int* f)
     if (n < 3 || n > 5 || (pre != 0 && pre != 1)) return false;
     const bool ok = (a == 2 || a == 4 || a == 8) && (b == 2 || b == 4 || b == 8 || b == 16 || b == 32 || b == 64) &&
                     (c == 1 || c == 2 || c == 4 || c == 8 || c == kSynthPairs || c == 2 * kSynthPairs ||
-                     c == 3 * kSynthPairs) && (d == 1 || d == 2);
+                     c == 3 * kSynthPairs || c == -4 || c == -8 || c == -16) && (d == 1 || d == 2);
     if (ok) { f[0] = a; f[1] = b; f[2] = c; f[3] = d; f[4] = pre; }
     return ok;
 }
@@ -1034,14 +1228,41 @@ static int autotune_t(ShLoading* s)
         return lanes % kSynthPairs != 0 ||
                (lanes / kSynthPairs) * std::min(s->L / 2 + 1, kSynthMaxWarps) * 32 <= kSynthMaxThreads;
     };
-    const bool force_synth = force && synth_fits(forced[2]);
+    const bool force_dense = force && forced[2] < 0 && s->Z;
+    const bool force_synth = force && !force_dense && forced[2] > 0 && synth_fits(forced[2]);
     for (int cells : {2, 1})
         for (int lanes : {1, 2, 4, 8, kSynthPairs, 2 * kSynthPairs, 3 * kSynthPairs}) {
-            if (!synth_fits(lanes)) continue;
+            if (!synth_fits(lanes) || force_dense) continue;
             if (force_synth && (lanes != forced[2] || cells != forced[3])) continue;
             const float ms = force_synth ? 0.f : timeit([&] { launch_synth<T>(s, lanes, cells, 0); });
             if (ms < best) { best = ms; s->lanes = lanes; s->cells = cells; }
         }
+    // the dense synthesis against the K x K product plus the chosen factored synthesis, in isolation.
+    // Z's bytes compete for L2 with the rest of the step, so a dense variant within 5 % is only a
+    // candidate: odis_create times whole steps both ways (sh_dense_candidate / sh_set_dense).
+    s->zw = 0;
+    s->zw_cand = 0;
+    s->zforced = force_synth || force_dense;
+    if (s->Z && !force_synth) {
+        const float fact = force_dense ? 1e30f : timeit([&] {
+            pdl_launch(k_sh_coef<T>, s->K, 32, 0, (cudaStream_t)0, s->t, s->K, s->FGinv, (T*)s->coef);
+            launch_synth<T>(s, s->lanes, s->cells, 0);
+        });
+        float bz = 1e30f;
+        for (int zc : {1, 2})
+            for (int zw : {4, 8, 16}) {
+                if (force_dense && (zw != -forced[2] || zc != forced[3])) continue;
+                const float ms = force_dense ? 0.f : timeit([&] { launch_synth_z<T>(s, zw, zc, 0); });
+                if (ms < bz) { bz = ms; s->zw_cand = zw; s->zc_cand = zc; }
+            }
+        if (force_dense) { s->zw = s->zw_cand; s->zc = s->zc_cand; }
+        else if (!(bz <= 1.05f * fact)) s->zw_cand = 0;
+    }
+    if (s->zw == 0 && s->zw_cand == 0 && s->Z) {       // the factored synthesis stays: Z is not kept
+        cudaDeviceSynchronize();
+        cudaFree(s->Z);
+        s->Z = nullptr;
+    }
     if constexpr (std::is_same<T, float>::value) {
         // tensor-core transforms against the CUDA-core ones, whole per-step sequence;
         // ODIS_SH_TC=1 or 0 fixes the choice
@@ -1086,12 +1307,34 @@ int sh_autotune(ShLoading* s)
     return autotune_t<float>(s);
 }
 
+bool sh_dense_candidate(const ShLoading* s) { return s && !s->use_tc && !s->zforced && s->Z && s->zw_cand > 0; }
+
+void sh_set_dense(ShLoading* s, bool on)
+{
+    if (!sh_dense_candidate(s)) return;
+    s->zw = on ? s->zw_cand : 0;
+    s->zc = on ? s->zc_cand : 1;
+    if (!on) {                                         // the factored synthesis is kept: free Z
+        cudaDeviceSynchronize();
+        cudaFree(s->Z);
+        s->Z = nullptr;
+        s->zw_cand = 0;
+    }
+}
+
+void sh_try_dense(ShLoading* s, bool on)
+{
+    if (!sh_dense_candidate(s)) return;
+    s->zw = on ? s->zw_cand : 0;
+    s->zc = on ? s->zc_cand : 1;
+}
+
 void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes, int* cells, int* pre)
 {
     if (tl) *tl = s->use_tc ? 0 : s->tl;
     if (nchunk) *nchunk = s->use_tc ? shtc_chunks(s->tc) : s->nchunk;
-    if (lanes) *lanes = s->use_tc ? shtc_tiles_per_pass(s->tc) : s->lanes;
-    if (cells) *cells = s->use_tc ? 0 : s->cells;
+    if (lanes) *lanes = s->use_tc ? shtc_tiles_per_pass(s->tc) : (s->zw ? -s->zw : s->lanes);
+    if (cells) *cells = s->use_tc ? 0 : (s->zw ? s->zc : s->cells);
     if (pre) *pre = s->use_tc ? 0 : (s->pre ? 1 : 0);
 }
 
@@ -1109,6 +1352,10 @@ static void enqueue_t(ShLoading* s, const void* eta, cudaStream_t st)
         }
     }
     launch_analysis<T>(s, s->tl, s->tiles, s->ntiles, s->nchunk, s->pre, eta, st);   // partials and their fold
+    if (s->zw) {
+        launch_synth_z<T>(s, s->zw, s->zc, st);
+        return;
+    }
     pdl_launch(k_sh_coef<T>, s->K, 32, 0, st, s->t, s->K, s->FGinv, (T*)s->coef);
     launch_synth<T>(s, s->lanes, s->cells, st);
 }
@@ -1122,7 +1369,9 @@ void sh_enqueue(ShLoading* s, const void* eta, cudaStream_t st)
 
 int sh_kernels_per_step(const ShLoading* s)
 {
-    return s && s->use_tc ? shtc_kernels_per_step() : (s && (s->half || s->pre) ? 4 : 3);
+    if (!s) return 0;
+    if (s->use_tc) return shtc_kernels_per_step();
+    return ((s->half || s->pre) ? 4 : 3) - (s->zw ? 1 : 0);
 }
 
 void sh_layout(const ShLoading* s, int* half, int* cells, long long* basis_bytes)

@@ -41,6 +41,12 @@ int sh_kernels_per_step(const ShLoading* s);
 // transforms (nchunk = analysis chunks, lanes = cell tiles per synthesis pass)
 // (cells = synthesis cells per thread, pre = 1 for the analysis from trig-weighted values)
 void sh_tuning(const ShLoading* s, int* tl, int* nchunk, int* lanes, int* cells, int* pre);
+// Dense synthesis (usg = Z t, Z = Y F G^-1) offered by the setup timing for a
+// whole-step comparison: sh_try_dense switches between it and the factored
+// synthesis; sh_set_dense makes the choice final (off frees Z).
+bool sh_dense_candidate(const ShLoading* s);
+void sh_try_dense(ShLoading* s, bool on);
+void sh_set_dense(ShLoading* s, bool on);
 // the stored basis: half = 1 for the antipodal half basis, the cells it covers,
 // and its bytes (Legendre rows + trig rows in the method's type)
 void sh_layout(const ShLoading* s, int* half, int* cells, long long* basis_bytes);

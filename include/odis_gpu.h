@@ -369,12 +369,17 @@ odis_status odis_profile_kernels(odis_ctx* c, int reps, double* ms);
  * covers tile_l degrees per block with the cells split in `chunks`, and with
  * pre = 1 reads the trig-weighted values of every order formed once per step
  * (else each tile forms them); the synthesis gives each cell `lanes` threads
- * splitting the orders, or with lanes = 16 one warp per pair of orders
- * (m, l_max - m) for 32 x `cells` cells per block; each synthesis thread covers
- * `cells` adjacent cells.  odis_create times every combination on this device
- * and keeps the fastest, unless the environment variable
- * ODIS_SH_TILES="tile_l,chunks,lanes[,cells[,pre]]" names one.  Any pointer
- * may be NULL.
+ * splitting the orders, or with lanes = 16 (32, 48) one warp per pair of
+ * orders (m, l_max - m) for 32 x `cells` cells (1, 2, 3 groups of them) per
+ * block; each synthesis thread covers `cells` adjacent cells.  lanes = -W is
+ * the dense synthesis usg = Z t with Z = Y F (Y^T Y)^-1 precomputed (K rows of
+ * the basis's cells, no K x K product per step): W warps per block split the
+ * rows, each lane covers `cells` cells.  odis_create times every combination
+ * on this device and keeps the fastest; the dense synthesis, whose matrix
+ * competes for L2 with the rest of the step, is kept only if whole steps run
+ * faster with it.  The environment variable
+ * ODIS_SH_TILES="tile_l,chunks,lanes[,cells[,pre]]" names a combination
+ * instead.  Any pointer may be NULL.
  * ODIS_FP32 also has tensor-core transforms (tcgen05, fp16 hi/lo operand pairs,
  * FP32 accumulation), retired from the default path because they are slower.
  * They need the full basis, so they are built only with ODIS_SH_TC=1 (which

@@ -4,7 +4,8 @@
   in FP64 and DF64 within 1e-10 (max-abs normalised) on eta, v, both AB3 histories and the power series; the
   FP32-state variant's power within 1e-4, its per-field errors printed.
 * Every tile shape of the self-gravity transforms (ODIS_SH_TILES: degrees per analysis tile, cell chunks,
-  synthesis lanes, cells per synthesis thread), each a different code path, over 300 steps.
+  synthesis lanes or the dense synthesis's warps, cells per synthesis thread), each a different code path,
+  over 300 steps.
 * Level 8 (655362 cells), FULL tide, l_max = 32, h = 20 km, drag 1e-6: 200 steps at the stable step.
 * Batch members on levels 4, 5 and 6, thick oceans included at their stable step counts.
 """
@@ -84,10 +85,11 @@ def test_level6_sh16_fp32_variant(level6):
 
 
 # (degrees per analysis tile, cell chunks, synthesis lanes (16, 32, 48: a warp per order pair, 1-3 cell
-# groups per block), cells per synthesis thread, analysis from precomputed trig-weighted values): every
-# value of each parameter appears
+# groups per block; -4, -8, -16: the dense synthesis Z t with that many warps per block), cells per
+# synthesis thread, analysis from precomputed trig-weighted values): every value of each parameter appears
 TILES = [(2, 8, 1, 1, 0), (4, 16, 2, 2, 1), (8, 32, 4, 1, 0), (2, 64, 8, 2, 1), (4, 8, 16, 1, 1),
-         (8, 64, 16, 2, 0), (2, 16, 16, 2, 1), (4, 4, 32, 1, 1), (2, 2, 48, 2, 0)]
+         (8, 64, 16, 2, 0), (2, 16, 16, 2, 1), (4, 4, 32, 1, 1), (2, 2, 48, 2, 0),
+         (2, 8, -8, 1, 1), (4, 16, -16, 2, 0), (8, 32, -4, 2, 1), (2, 4, -4, 1, 0)]
 
 
 @pytest.mark.parametrize("precision", [0, 2, 1])

@@ -321,7 +321,7 @@ def test_fp32_self_gravity_transform_paths(grid_dir, monkeypatch, tc):
     fac = g.benchmark_sh_factors(0.113, RADIUS, 8, seed=1)
     orc, gpu = _pair(grid_dir / "grid_3.txt", precision=1, sh_lmax=8, sh_factors=fac)
     tl, chunks, lanes = gpu.sh_tiles()
-    assert (tl == 0) == (tc == "1") and chunks > 0 and lanes > 0
+    assert (tl == 0) == (tc == "1") and chunks > 0 and lanes != 0     # lanes < 0: the dense synthesis
     po, pg = orc.run(1500), gpu.run(1500)
     _, vo, eo, _, _ = orc.get_state()
     _, vg, eg, _, _ = gpu.get_state()
