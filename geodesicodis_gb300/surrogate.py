@@ -1,10 +1,13 @@
 """Learned warm start of the tidal time loop.
 
-A network maps the ocean parameters (log thickness, log drag, eccentricity,
-obliquity) to the spherical-harmonic coefficients, to degree 8, of the
-converged tidal state at 8 orbital phases: eta, and the velocity potential chi
-and stream function psi of the edge-normal velocity (v_e = n_e . grad chi +
-n_e . (k x grad psi)).  The predicted phase-0 state is loaded into the batched
+A network maps the ocean parameters to the spherical-harmonic coefficients, to
+degree 8, of the converged tidal state at the start of an orbit and a quarter
+orbit later: eta, and the velocity potential chi and stream function psi of the
+edge-normal velocity (v_e = n_e . grad chi + n_e . (k x grad psi)).  The LTE is
+linear and the FULL tide is linear in eccentricity and obliquity, so the
+network's input is (log thickness, log drag) only and its output is two
+response heads, per unit eccentricity and per unit obliquity, mixed by the
+member's amplitudes.  The predicted phase-0 state is loaded into the batched
 integrator, which runs on from it until the orbit-mean dissipated power
 converges: the plain integrator judges the result, and a zero start is the
 fallback and the reference for the number of orbits.
@@ -29,7 +32,8 @@ from . import MLP, Batch
 from . import sweep as S
 
 LMAX = 8
-PHASES = 8
+PHASES = 8                 # parts of the last orbit of a round at which the state is projected
+MODEL_PHASES = (0, 2)      # the phases the network predicts: the orbit start and a quarter orbit later
 TOL = 1e-4
 
 
@@ -186,8 +190,8 @@ def run_to_convergence(common, mesh, members, basis: MeshBasis | None, v0=None, 
 # features, targets and the network
 # ---------------------------------------------------------------------------
 def features(prm: dict) -> np.ndarray:
-    return np.stack([np.log10(prm["h"]), np.log10(prm["alpha"]), prm["ecc"] / 0.01,
-                     np.rad2deg(prm["obliq"]) / 0.5], axis=1)
+    """Network input: the response per unit forcing depends on thickness and drag only."""
+    return np.stack([np.log10(prm["h"]), np.log10(prm["alpha"])], axis=1)
 
 
 def mixing(prm: dict) -> np.ndarray:
@@ -198,24 +202,29 @@ def mixing(prm: dict) -> np.ndarray:
 class Surrogate:
     """Network + the scalings between its units and the harmonic coefficients."""
 
-    def __init__(self, basis: MeshBasis, width=256, depth=3, seed=0):
+    def __init__(self, basis: MeshBasis, width=512, depth=3, seed=0):
         self.basis = basis
-        self.n_out = PHASES * basis.n_coef
-        self.net = MLP(4, width, depth, self.n_out, 2, seed=seed)
+        self.n_out = len(MODEL_PHASES) * basis.n_coef
+        self.net = MLP(2, width, depth, self.n_out, 2, seed=seed)
         self.mu = self.sd = self.scale = None
 
     def _targets(self, coef: np.ndarray, prm: dict) -> np.ndarray:
-        """coef [n, PHASES, KV+K] -> network units: velocity coefficients times h (transport), per-output scale."""
-        t = coef.copy()
+        """coef [n, PHASES, KV+K] -> network units (the MODEL_PHASES rows): velocity coefficients times h
+        (transport), per-output scale."""
+        t = coef[:, list(MODEL_PHASES)].copy()
         t[:, :, :self.basis.KV] *= prm["h"][:, None, None]
         return t.reshape(t.shape[0], -1)
 
     def _coef(self, t: np.ndarray, prm: dict) -> np.ndarray:
-        c = t.reshape(t.shape[0], PHASES, self.basis.n_coef).copy()
+        """Network units -> coef [n, len(MODEL_PHASES), KV+K]."""
+        c = t.reshape(t.shape[0], len(MODEL_PHASES), self.basis.n_coef).copy()
         c[:, :, :self.basis.KV] /= prm["h"][:, None, None]
         return c
 
-    def fit(self, prm: dict, coef: np.ndarray, epochs=800, batch=128, lr=1e-3, seed=0):
+    def fit(self, prm: dict, coef: np.ndarray, epochs=800, batch=128, lr=1e-3, seed=0, orbits=None):
+        """Train on converged coefficients.  Each sample's loss is its relative squared error, weighted by
+        sqrt(orbits) when the zero-start orbit counts are given: the slowly converging (low-drag) members
+        are where a warm start saves orbits."""
         x = features(prm)
         self.mu, self.sd = x.mean(axis=0), x.std(axis=0) + 1e-12
         t = self._targets(coef, prm)
@@ -224,6 +233,9 @@ class Surrogate:
         self.scale = np.median(np.abs(t), axis=0) / np.median(np.abs(mix).sum(axis=1)) + 1e-30
         tn = t / self.scale
         w = 1.0 / np.maximum(np.sum(tn ** 2, axis=1), 1e-30) * tn.shape[1]
+        if orbits is not None:
+            cost = np.sqrt(np.maximum(np.asarray(orbits, np.float64), 1.0))
+            w = w * cost / cost.mean()
         losses = self.net.train((x - self.mu) / self.sd, tn, mix, w, epochs=epochs, batch=batch, lr=lr, seed=seed)
         return losses
 
@@ -248,9 +260,27 @@ def relative_coef_error(pred: np.ndarray, true: np.ndarray) -> np.ndarray:
     return np.linalg.norm(d, axis=1) / np.maximum(np.linalg.norm(t, axis=1), 1e-300)
 
 
+def refine_parameters(prm: dict, err: np.ndarray, orbits: np.ndarray, count: int, seed: int) -> dict:
+    """Extra training draws around the members the network predicts worst, weighted by their orbit cost:
+    the top count/4 by err * sqrt(orbits), four draws each, thickness within +-2.3 % (resonances are a few
+    per mille wide at low drag) and drag within a factor 1.6, fresh eccentricity and obliquity."""
+    rng = np.random.default_rng(seed)
+    score = err * np.sqrt(np.maximum(orbits, 1.0))
+    pick = np.argsort(score)[::-1][:max(1, count // 4)]
+    src = np.repeat(pick, 4)[:count]
+    n = src.size
+    h = np.clip(prm["h"][src] * 10.0 ** rng.uniform(-0.01, 0.01, n), 100.0, 1e5)
+    alpha = np.clip(prm["alpha"][src] * 10.0 ** rng.uniform(-0.2, 0.2, n), 1e-7, 1e-4)
+    return {"level": prm["level"][src], "h": h, "alpha": alpha, "ecc": rng.uniform(0.001, 0.01, n),
+            "obliq": np.deg2rad(rng.uniform(0.0, 0.5, n))}
+
+
 def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epochs=800, batch=128, lr=1e-3,
-               round_orbits=10, max_orbits=400, log=print, save=None, tol: float = TOL) -> dict:
-    """Train on solver runs, then compare orbits to convergence from rest and from the warm start."""
+               round_orbits=10, max_orbits=400, log=print, save=None, tol: float = TOL, refine: int = 0) -> dict:
+    """Train on solver runs, then compare orbits to convergence from rest and from the warm start.
+    refine > 0: after the first fit, `refine` more training members are drawn around the worst-predicted
+    costly ones (refine_parameters), run to convergence from the network's own warm start, and the
+    network is trained again on all of them."""
     t0 = time.time()
     common, period = S.common_params()
     meshes = S.SweepMeshes((level,))
@@ -267,9 +297,29 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
     log(f"training data {t_data:.1f} s, {tr['cell_steps']:.3e} cell-steps")
     sur = Surrogate(basis)
     t2 = time.time()
-    losses = sur.fit(ptr, tr["coef"], epochs=epochs, batch=batch, lr=lr)
+    orb_tr = np.where(tr["orbits"] > 0, tr["orbits"], max_orbits + 1)
+    losses = sur.fit(ptr, tr["coef"], epochs=epochs, batch=batch, lr=lr, orbits=orb_tr)
     t_fit = time.time() - t2
     log(f"training {t_fit:.1f} s, loss {losses[0]:.3e} -> {losses[-1]:.3e}")
+    t_refine = 0.0
+    if refine > 0:
+        t5 = time.time()
+        err_tr = relative_coef_error(sur.predict_coef(ptr)[:, 0], tr["coef"][:, 0])
+        pre = refine_parameters(ptr, err_tr, orb_tr, refine, seed_train + 1000)
+        mre = members_from(pre, meshes, period)
+        v_r, e_r = sur.warm_state(pre)
+        rr = run_to_convergence(common, mesh, mre, basis, v0=v_r, eta0=e_r, round_orbits=round_orbits,
+                                max_orbits=max_orbits, log=log, tol=tol)
+        ptr = {k: np.concatenate([ptr[k], pre[k]]) for k in ptr}
+        tr["coef"] = np.concatenate([tr["coef"], rr["coef"]])
+        tr["cell_steps"] += rr["cell_steps"]
+        # their orbit cost from rest is unknown: the source member's stands in
+        src_orbits = orb_tr[np.argsort(err_tr * np.sqrt(np.maximum(orb_tr, 1.0)))[::-1][:max(1, refine // 4)]]
+        orb_tr = np.concatenate([orb_tr, np.repeat(src_orbits, 4)[:refine]])
+        sur = Surrogate(basis)
+        losses = sur.fit(ptr, tr["coef"], epochs=epochs, batch=batch, lr=lr, orbits=orb_tr)
+        t_refine = time.time() - t5
+        log(f"refinement: {refine} members around the worst-predicted, {t_refine:.1f} s, loss -> {losses[-1]:.3e}")
     # held-out: zero start (also gives the true converged coefficients) and warm start
     t3 = time.time()
     zero = run_to_convergence(common, mesh, mte, basis, round_orbits=round_orbits, max_orbits=max_orbits, log=log, tol=tol)
@@ -284,12 +334,12 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
     best = run_to_convergence(common, mesh, mte, None, v0=v_t, eta0=e_t, round_orbits=round_orbits,
                               max_orbits=max_orbits, log=log, tol=tol)
     pred = sur.predict_coef(pte)
-    err = relative_coef_error(pred, zero["coef"])
-    if save:
+    err = relative_coef_error(pred[:, 0], zero["coef"][:, 0])         # the phase-0 state the warm start loads
+    if save:        # per member: parameters, orbit counts, prediction error (no coefficient arrays: a few hundred kB)
         np.savez_compressed(save, ptr_h=ptr["h"], ptr_alpha=ptr["alpha"], ptr_ecc=ptr["ecc"], ptr_obliq=ptr["obliq"],
                             pte_h=pte["h"], pte_alpha=pte["alpha"], pte_ecc=pte["ecc"], pte_obliq=pte["obliq"],
-                            coef_train=tr["coef"], coef_test=zero["coef"], pred=pred, orbits_train=tr["orbits"],
-                            orbits_zero=zero["orbits"], orbits_warm=warm["orbits"], orbits_best=best["orbits"], losses=losses,
+                            err_test=err, orbits_train=tr["orbits"], orbits_zero=zero["orbits"],
+                            orbits_warm=warm["orbits"], orbits_best=best["orbits"], losses=losses,
                             power_zero=zero["power"], power_warm=warm["power"])
     oz = np.where(zero["orbits"] > 0, zero["orbits"], max_orbits + 1)
     ow = np.where(warm["orbits"] > 0, warm["orbits"], max_orbits + 1)
@@ -311,7 +361,8 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
         "converged_power_rel_diff_max": float(np.max(pdiff[both])) if both.any() else None,
         "coef_rel_err_median": float(np.median(err)), "coef_rel_err_p90": float(np.quantile(err, 0.9)),
         "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
-        "seconds": {"data": t_data, "train": t_fit, "zero": t_zero, "warm": t_warm},
+        "seconds": {"data": t_data, "train": t_fit, "refine": t_refine, "zero": t_zero, "warm": t_warm},
+        "refine": refine, "loss_weight": "relative squared error x sqrt(zero-start orbits)",
         "epochs": epochs, "batch": batch, "lr": lr, "round_orbits": round_orbits,
         "cell_steps": {"data": tr["cell_steps"], "zero": zero["cell_steps"], "warm": warm["cell_steps"]},
         "max_orbits": max_orbits, "tol": tol,
