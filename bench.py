@@ -340,6 +340,11 @@ def run_ours(args) -> dict:
             results[key] = N * n * kv / t
         if lmax:
             extra[key] = {"sh_tiles": list(s.sh_tuning()), "sh_layout": s.sh_layout()}
+        if key.startswith("fp32"):
+            extra.setdefault(key, {})["arithmetic"] = (
+                "FP32 state and stencils, AB3 accumulated in double-float; dissipated power summed in FP32 within a "
+                "warp (32 non-negative terms) and FP64 beyond (the FP64 reductions of the FP64 and DF64 methods); "
+                "errors against FP64 in errors_vs_fp64")
         if key == "df64_sh16":
             # the double-float method end to end, on its own context as the headline
             extra[key]["e2e"] = run_e2e(s, stream, flush, args, n, N, E, barrier, max_over_ranks, world,

@@ -34,6 +34,7 @@
 #include "odis_arith.cuh"
 #include "odis_pdl.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <cstdio>
@@ -1118,6 +1119,35 @@ static void launch_synth(const ShLoading* s, int lanes, int cells, cudaStream_t 
 #undef ODIS_SYNTH
 }
 
+// Cell-chunk counts the timing tries for an analysis of nt tiles: the powers of
+// two, and the counts whose tiles x chunks CTAs fill one, two or three whole
+// waves of this kernel's resident CTAs.  The transforms are bound by arithmetic
+// issue, so an SM that runs one CTA more than the others sets the time: 85
+// tiles x 8 chunks = 680 CTAs on 608 slots leaves some SMs 5 CTAs' work
+// against 4.47 on average, 85 x 7 = 595 fits one wave.
+template <class T>
+static std::vector<int> analysis_chunks(const ShLoading* s, int tl, bool pre, int nt)
+{
+    std::vector<int> c = {2, 4, 8, 16, 32, 64};
+    int dev = 0, sms = 0, nb = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const bool h = s->half;
+#define ODIS_AFN(TL) (pre ? (h ? (const void*)k_sh_analysis<T, TL, true, true> : (const void*)k_sh_analysis<T, TL, false, true>) \
+                          : (h ? (const void*)k_sh_analysis<T, TL, true, false> : (const void*)k_sh_analysis<T, TL, false, false>))
+    const void* f = tl == 2 ? ODIS_AFN(2) : tl == 4 ? ODIS_AFN(4) : ODIS_AFN(8);
+#undef ODIS_AFN
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, f, kShThreads, 0) != cudaSuccess || nb <= 0 || sms <= 0 || nt <= 0) {
+        (void)cudaGetLastError();
+        return c;
+    }
+    for (int w = 1; w <= 3; w++) {
+        const int ch = w * nb * sms / nt;
+        if (ch >= 2 && ch <= kMaxChunks && std::find(c.begin(), c.end(), ch) == c.end()) c.push_back(ch);
+    }
+    return c;
+}
+
 // dense synthesis usg = Z t with zw warps per block and zc cells per lane
 template <class T>
 static cudaError_t launch_synth_z(const ShLoading* s, int zw, int zc, cudaStream_t st)
@@ -1142,7 +1172,7 @@ static cudaError_t launch_synth_z(const ShLoading* s, int zw, int zc, cudaStream
 // synthesis lanes; the analysis's chunking changes only the order of the
 // partial sums.
 // ODIS_SH_TILES="tile_l,chunks,lanes[,cells[,pre]]" (tile_l in {2,4,8}, chunks in
-// {2,4,8,16,32,64}, lanes in {1,2,4,8} threads per cell splitting the orders, or
+// 2..64, lanes in {1,2,4,8} threads per cell splitting the orders, or
 // 16, 32, 48 for one warp per pair of orders (k_sh_synth_m) and 1, 2, 3 cell
 // groups per block, or -4, -8, -16 for the dense synthesis with that many warps
 // per block, synthesis cells per thread in
@@ -1158,7 +1188,7 @@ static bool forced_tiles(int* f)
     int a = 0, b = 0, c = 0, d = 2, pre = 0;
     const int n = std::sscanf(e, "%d,%d,%d,%d,%d", &a, &b, &c, &d, &pre);
     if (n < 3 || n > 5 || (pre != 0 && pre != 1)) return false;
-    const bool ok = (a == 2 || a == 4 || a == 8) && (b == 2 || b == 4 || b == 8 || b == 16 || b == 32 || b == 64) &&
+    const bool ok = (a == 2 || a == 4 || a == 8) && b >= 2 && b <= kMaxChunks &&
                     (c == 1 || c == 2 || c == 4 || c == 8 || c == kSynthPairs || c == 2 * kSynthPairs ||
                      c == 3 * kSynthPairs || c == -4 || c == -8 || c == -16) && (d == 1 || d == 2);
     if (ok) { f[0] = a; f[1] = b; f[2] = c; f[3] = d; f[4] = pre; }
@@ -1206,10 +1236,11 @@ static int autotune_t(ShLoading* s)
         if (force && tl != forced[0]) continue;
         const std::vector<int> tiles = make_tiles(s->L, tl, s->half);
         cudaMemcpy(dt, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice);
-        for (int ch : {2, 4, 8, 16, 32, 64})
-            for (bool pre : {false, true}) {
+        const int nt = (int)tiles.size() / 3;
+        for (bool pre : {false, true})
+            for (int ch : analysis_chunks<T>(s, tl, pre, nt)) {
                 if (force && (ch != forced[1] || (int)pre != forced[4])) continue;
-                const float ms = force ? 0.f : timeit([&] { launch_analysis<T>(s, tl, dt, (int)tiles.size() / 3, ch, pre, eta, 0); });
+                const float ms = force ? 0.f : timeit([&] { launch_analysis<T>(s, tl, dt, nt, ch, pre, eta, 0); });
                 if (ms < best) { best = ms; best_tl = tl; best_ch = ch; best_tiles = tiles; best_pre = pre; }
             }
     }

@@ -89,7 +89,8 @@ def test_level6_sh16_fp32_variant(level6):
 # synthesis thread, analysis from precomputed trig-weighted values): every value of each parameter appears
 TILES = [(2, 8, 1, 1, 0), (4, 16, 2, 2, 1), (8, 32, 4, 1, 0), (2, 64, 8, 2, 1), (4, 8, 16, 1, 1),
          (8, 64, 16, 2, 0), (2, 16, 16, 2, 1), (4, 4, 32, 1, 1), (2, 2, 48, 2, 0),
-         (2, 8, -8, 1, 1), (4, 16, -16, 2, 0), (8, 32, -4, 2, 1), (2, 4, -4, 1, 0)]
+         (2, 8, -8, 1, 1), (4, 16, -16, 2, 0), (8, 32, -4, 2, 1), (2, 4, -4, 1, 0),
+         (2, 7, 16, 1, 1), (4, 13, -8, 1, 0)]          # chunk counts that fill whole waves are not powers of two
 
 
 @pytest.mark.parametrize("precision", [0, 2, 1])
