@@ -1238,11 +1238,17 @@ static int autotune_t(ShLoading* s)
         cudaMemcpy(dt, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice);
         const int nt = (int)tiles.size() / 3;
         for (bool pre : {false, true})
-            for (int ch : analysis_chunks<T>(s, tl, pre, nt)) {
+            for (int ch : force ? std::vector<int>{forced[1]} : analysis_chunks<T>(s, tl, pre, nt)) {
                 if (force && (ch != forced[1] || (int)pre != forced[4])) continue;
                 const float ms = force ? 0.f : timeit([&] { launch_analysis<T>(s, tl, dt, nt, ch, pre, eta, 0); });
                 if (ms < best) { best = ms; best_tl = tl; best_ch = ch; best_tiles = tiles; best_pre = pre; }
             }
+    }
+    if (best_tiles.empty()) {                          // nothing ran (a refused launch in every candidate)
+        best_tl = 8;
+        best_ch = 16;
+        best_pre = false;
+        best_tiles = make_tiles(s->L, best_tl, s->half);
     }
     s->pre = best_pre;
     cudaFree(dt);
