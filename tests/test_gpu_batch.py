@@ -55,6 +55,27 @@ def test_batch_members_match_oracle(grid_dir):
     b.close()
 
 
+@pytest.mark.parametrize("rows", ["1", "2", "4"])
+def test_batch_kernel_variants_match_oracle(grid_dir, monkeypatch, rows):
+    """Each kernel variant forced by ODIS_BATCH_ROWS (face/cell rows per thread and tile): the same members
+    against the FP64 oracle."""
+    monkeypatch.setenv("ODIS_BATCH_ROWS", rows)
+    g, O, angvel, P, paths, meshes, members, common = _setup(grid_dir, count=6, seed=11)
+    b = g.Batch(common, meshes, members)
+    assert b.info()["rows_per_thread"] == int(rows)
+    steps = 400
+    _, sp = b.run(steps=steps, step_power=True)
+    for i, m in enumerate(members):
+        orc = _oracle(O, paths[m["mesh"]], angvel, P, m)
+        po = orc.run(steps)
+        _, vo, eo, _, _ = orc.get_state()
+        it, vg, eg = b.get_member(i)
+        assert it == steps
+        assert rel_err(sp[i, steps // 2:], po[steps // 2:]) < 1e-4, i
+        assert rel_err(eg, eo) < 1e-3 and rel_err(vg, vo) < 1e-3, i
+    b.close()
+
+
 def test_batch_orbit_power_and_retirement(grid_dir):
     """Members with fewer steps per orbit stop first; nothing about them depends on the others."""
     g, O, angvel, P, paths, meshes, members, common = _setup(grid_dir, count=9, seed=3)
