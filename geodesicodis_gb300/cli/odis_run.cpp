@@ -25,10 +25,14 @@
 // from it to the same bits as an uninterrupted run.
 //
 //   odis_run [--dir D] [--grid FILE | --level N] [--precision fp64|df64|fp32] [--orbits X] [--resume]
+//            [--device-mesh]
 //
 // --level is the number of subdivisions (10*4^N+2 cells); without --grid or
 // --level the grid is generated for input.in's "geodesic grid level", whose
 // count the reference's grid files give as 10*4^(level-1)+2 cells.
+// --device-mesh generates the grid and builds the mesh geometry and TRiSK
+// weights on the GPU (the same integers; the geometry to the conditioning of
+// the reference's formulas), which is faster at fine levels.
 #include "odis_gpu.h"
 
 #include <csignal>
@@ -225,7 +229,7 @@ int main(int argc, char** argv)
     std::string dir = ".", grid, prec = "fp64";
     int level = -1;
     double orbits = -1.0;
-    bool resume = false;
+    bool resume = false, device_mesh = false;
     for (int a = 1; a < argc; a++) {
         const std::string k = argv[a];
         auto next = [&]() -> std::string { return a + 1 < argc ? argv[++a] : std::string(); };
@@ -235,9 +239,10 @@ int main(int argc, char** argv)
         else if (k == "--precision") prec = next();
         else if (k == "--orbits") orbits = std::atof(next().c_str());
         else if (k == "--resume") resume = true;
+        else if (k == "--device-mesh") device_mesh = true;
         else {
             std::fprintf(stderr, "usage: odis_run [--dir D] [--grid FILE | --level N] [--precision fp64|df64|fp32] "
-                                 "[--orbits X] [--resume]\n");
+                                 "[--orbits X] [--resume] [--device-mesh]\n");
             return 2;
         }
     }
@@ -251,8 +256,13 @@ int main(int argc, char** argv)
         p.precision = ODIS_FP64;
     }
     odis_mesh* mesh = nullptr;
-    if (!grid.empty()) st = odis_mesh_from_file(grid.c_str(), p.radius, &mesh);
-    else st = odis_mesh_generate(level >= 0 ? level : in.grid_level - 1, p.radius, &mesh);
+    const int gen_level = level >= 0 ? level : in.grid_level - 1;
+    if (!grid.empty())
+        st = device_mesh ? odis_mesh_from_file_device(grid.c_str(), p.radius, &mesh)
+                         : odis_mesh_from_file(grid.c_str(), p.radius, &mesh);
+    else
+        st = device_mesh ? odis_mesh_generate_device(gen_level, p.radius, &mesh)
+                         : odis_mesh_generate(gen_level, p.radius, &mesh);
     if (st != ODIS_OK) return fail("building the mesh", st);
     int N = 0, E = 0;
     odis_mesh_sizes(mesh, &N, &E, nullptr);

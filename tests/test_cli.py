@@ -91,6 +91,21 @@ dummy1 output;                true;                  div;
 
 
 @pytest.mark.gpu
+def test_cli_device_mesh(built, tmp_path):
+    """--device-mesh builds the grid and mesh on the GPU: the same run as the host-built mesh, power to the
+    geometry's conditioning at this level (grid level 3 of input.in, 642 cells)."""
+    outs = []
+    for extra, name in (([], "host"), (["--device-mesh"], "device")):
+        (tmp_path / name).mkdir()
+        d = _rundir(tmp_path / name)
+        r = subprocess.run([str(CLI), "--dir", str(d), "--orbits", "0.1", *extra], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        outs.append(np.loadtxt(d / "DATA" / "power.txt", ndmin=2))
+    assert outs[0].shape == outs[1].shape
+    assert np.max(np.abs(outs[1][:, 1] - outs[0][:, 1])) <= 1e-10 * np.max(np.abs(outs[0][:, 1]))
+
+
+@pytest.mark.gpu
 def test_cli_writes_data_h5(built, tmp_path):
     """DATA/data.h5 in the reference's layout (src/outFiles.cpp:138-823), read back with the
     specification reader: one row per dump (the initial state, then every output interval), each
