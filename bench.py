@@ -1,6 +1,6 @@
 """Benchmark: cell-steps/s of the GeodesicODIS LTE time loop on one GB300.
 
-Workload (configs[1] of the benchmark set): icosahedral mesh level 6 (40962 cells,
+Workload (the headline case of the benchmark set): icosahedral mesh level 6 (40962 cells,
 122880 faces), Enceladus-like body (r = 252.1 km, g = 0.113 m/s^2, rotation
 5.307e-5 rad/s -> P = 118394 s), h = 10 km, linear drag 1e-5 1/s, eccentricity
 tide e = 0.0047, self-gravity/loading to l_max = 16 with the reference's
@@ -560,7 +560,7 @@ def nonlinear_bytes(N: int, E: int, V: int, s: int = 8) -> int:
 
 
 def run_level8(args) -> dict:
-    """configs[4]: level 8 (655362 cells), eccentricity + obliquity tide, h = 20 km, drag 1e-6, self-gravity
+    """The level-8 case: 655362 cells, eccentricity + obliquity tide, h = 20 km, drag 1e-6, self-gravity
     l_max = 32; every method with and without self-gravity, `args.case_steps` timed steps each, errors of
     FP32 and DF64 against FP64 after the same steps from rest."""
     import geodesicodis_gb300 as g

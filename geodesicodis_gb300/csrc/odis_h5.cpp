@@ -1,5 +1,5 @@
 // The run's DATA/data.h5 container (src/outFiles.cpp:138-823) written without
-// the HDF5 library, which this build does not have.
+// the HDF5 library, which this library does not depend on.
 //
 // The file has the structure that the HDF5 library writes with default property
 // lists (H5Fcreate / H5Dcreate with H5P_DEFAULT, as the reference calls them),

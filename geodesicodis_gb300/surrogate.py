@@ -9,7 +9,7 @@ network's input is (log thickness, log drag) only and its output is two
 response heads, per unit eccentricity and per unit obliquity, mixed by the
 member's amplitudes.  The predicted phase-0 state is loaded into the batched
 integrator, which runs on from it until the orbit-mean dissipated power
-converges: the plain integrator judges the result, and a zero start is the
+converges: the plain integrator decides convergence, and a zero start is the
 fallback and the reference for the number of orbits.
 
 Everything that computes runs in this library's kernels: the integrator

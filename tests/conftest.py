@@ -59,7 +59,7 @@ def rel_err(a, b) -> float:
 
 
 def config0_params(**over):
-    """configs[0]: h = 10 km, alpha = 1e-5, ECC e = 0.0047, 2000 steps/orbit."""
+    """The reference's own CPU-sized case: h = 10 km, alpha = 1e-5, ECC e = 0.0047, 2000 steps/orbit."""
     from oracle import pyoracle as O
     angvel, P, dt, n = O.derive_time(ANGVEL_IN, 59.197)
     p = dict(radius=RADIUS, g=GRAV, angvel=angvel, h=1e4, alpha=1e-5, ecc=0.0047, obliq=0.0, love_reduct=1.0,

@@ -148,7 +148,7 @@ def test_level6_sh16_tensor_core_path(level6, monkeypatch):
 
 
 def test_level8_sh32_sample(tmp_path, built):
-    """configs[4]'s workload: level 8, FULL tide (e 0.0047, obliquity 0.2 deg), h 20 km, drag 1e-6,
+    """The level-8 workload: FULL tide (e 0.0047, obliquity 0.2 deg), h 20 km, drag 1e-6,
     l_max 32, at the stable step count; 200 steps in FP64 and DF64 (1e-10) and FP32 (power 1e-4)."""
     import geodesicodis_gb300 as g
     from oracle import pyoracle as O

@@ -222,7 +222,8 @@ def test_fused_fp64_parity(grid_dir, level, steps):
 
 
 def test_config0_full_run_parity(grid_dir):
-    """configs[0]: level 4 (2562 cells), ECC e=0.0047, h=10 km, alpha=1e-5, 10 orbits x 2000 steps."""
+    """The reference's own CPU-sized case: level 4 (2562 cells), ECC e=0.0047, h=10 km, alpha=1e-5,
+    10 orbits x 2000 steps."""
     orc, gpu = _pair(grid_dir / "grid_4.txt")
     po = orc.run(20000)
     pg = gpu.run(20000)
