@@ -76,8 +76,9 @@ def test_batch_kernel_variants_match_oracle(grid_dir, monkeypatch, rows):
     b.close()
 
 
-def test_batch_orbit_power_and_retirement(grid_dir):
+def test_batch_orbit_power_and_retirement(grid_dir, monkeypatch):
     """Members with fewer steps per orbit stop first; nothing about them depends on the others."""
+    monkeypatch.setenv("ODIS_BATCH_ROWS", "2")      # both batches run the same kernel variant
     g, O, angvel, P, paths, meshes, members, common = _setup(grid_dir, count=9, seed=3)
     a = g.Batch(common, meshes, members)
     op, sp = a.run(orbits=1, step_power=True)
@@ -100,7 +101,8 @@ def test_batch_orbit_power_and_retirement(grid_dir):
     b.close()
 
 
-def test_batch_chunking_and_split_runs_are_bitwise(grid_dir):
+def test_batch_chunking_and_split_runs_are_bitwise(grid_dir, monkeypatch):
+    monkeypatch.setenv("ODIS_BATCH_ROWS", "2")      # both batches run the same kernel variant
     g, O, angvel, P, paths, meshes, members, common = _setup(grid_dir, count=6, seed=5)
     a = g.Batch(common, meshes, members)
     b = g.Batch(common, meshes, members)
@@ -178,8 +180,9 @@ def test_batch_bulk_state_and_projection(grid_dir):
     b.close()
 
 
-def test_batch_run_is_one_graph_launch(grid_dir):
+def test_batch_run_is_one_graph_launch(grid_dir, monkeypatch):
     """Every run replays its chunks' cooperative launches from one CUDA graph; chunking changes nothing."""
+    monkeypatch.setenv("ODIS_BATCH_ROWS", "2")      # both batches run the same kernel variant
     g, O, angvel, P, paths, meshes, members, common = _setup(grid_dir, count=6, seed=9)
     b = g.Batch(common, meshes, members)
     i0 = b.info()                                  # creation times the row variants with short runs

@@ -251,6 +251,8 @@ def test_graph_and_eager_paths_agree(grid_dir):
     """Chunks replayed from the CUDA graph and eager launches give identical bits; runs are deterministic."""
     _, a = _pair(grid_dir / "grid_2.txt")
     _, b = _pair(grid_dir / "grid_2.txt")
+    a.set_persistent(False)                                  # the graph-replayed path in both (creation times
+    b.set_persistent(False)                                  # it against the persistent loop per context)
     pa = a.run(64 * 3 + 5)                                   # 3 graph chunks + 5 eager steps
     pb = np.concatenate([b.run(10), b.run(63), b.run(64 * 2 - 5), b.run(1)])   # mixed chunking, 197 steps
     assert pa.shape == pb.shape

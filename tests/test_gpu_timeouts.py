@@ -46,8 +46,9 @@ def test_persistent_loop_wait_runs_out(grid_dir, precision):
     b.close()
 
 
-def test_batch_barrier_wait_runs_out(grid_dir):
+def test_batch_barrier_wait_runs_out(grid_dir, monkeypatch):
     import geodesicodis_gb300 as g
+    monkeypatch.setenv("ODIS_BATCH_ROWS", "2")      # both batches run the same kernel variant
     from oracle import pyoracle as O
     angvel, P, _, _ = O.derive_time(ANGVEL_IN, 59.197)
     meshes = [g.Mesh.from_file(grid_dir / f"grid_{lv}.txt", RADIUS) for lv in (2, 3)]
