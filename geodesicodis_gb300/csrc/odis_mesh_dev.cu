@@ -102,7 +102,10 @@ struct DevExec {
     template <class T> const T* in(const T* h, size_t n)
     {
         T* p = alloc<T>(n);
-        if (p && cudaMemcpyAsync(p, h, sizeof(T) * n, cudaMemcpyHostToDevice, s) != cudaSuccess) check();
+        if (p && cudaMemcpyAsync(p, h, sizeof(T) * n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            (void)cudaGetLastError();
+            if (st == ODIS_OK) st = ODIS_ERR_CUDA;
+        }
         return p;
     }
     template <class F> void run(long long n, const F& f)
