@@ -157,8 +157,25 @@ ODIS_HD inline double sph_tri_area(LL p1, LL p2, LL p3, double r)
     return pow2(r) * fabs((A + B + C) - kGeoPi);
 }
 
-// an id ranked by its angle (degrees) about a node
-struct Ranked { int id; double deg; };
+// an id (and its slot at the node) ranked by its angle (degrees) about a node
+struct Ranked { int id; int slot; double deg; };
+
+// the absolute angle of q in c's stereographic plane, as angle_about forms it
+ODIS_HD inline double angle_in_plane(LL q, LL c)
+{
+    double m, x, y;
+    stereo(c, q, 1.0, m, x, y);
+    return atan2(y - 0.0, x - 0.0);
+}
+
+// angle_about(q1, q2, c) from the two absolute angles angle_in_plane(q1, c) and angle_in_plane(q2, c)
+ODIS_HD inline double angle_between(double t1, double t2)
+{
+    double a = t1 - t2;
+    if (a > kGeoPi) a -= 2 * kGeoPi;
+    else if (a < -kGeoPi) a += 2 * kGeoPi;
+    return a;
+}
 
 // descending insertion sort of k <= 6 entries (stable)
 ODIS_HD inline void sort_desc(Ranked* r, int k)

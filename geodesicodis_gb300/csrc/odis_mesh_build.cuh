@@ -51,6 +51,10 @@ struct MeshView {
     int* vert_faces = nullptr;          // [V][3]
     int* vert_face_dir = nullptr;       // [V][3]
     double* vert_area = nullptr;        // [V]
+    // per node slot: the absolute angles, about the node, of the slot's face intercept and vertex, and
+    // the kite areas of the slot's vertex with its cyclic successor vertex (cv) and with the faces
+    // before (a1) and after (a2) it, computed once per node for every ranking about it
+    double *th_f = nullptr, *th_v = nullptr, *kcv = nullptr, *ka1 = nullptr, *ka2 = nullptr;   // [N][6]
     int* err = nullptr;                 // nonzero: the arrays do not describe a valid mesh
 
     ODIS_HD int nfriends(int i) const { return friends[i * 6 + 5] < 0 ? 5 : 6; }
@@ -210,32 +214,70 @@ struct StepFaceGeometry {
 };
 
 // faces and vertices about node nd ranked anticlockwise from face e (degrees,
-// wrapped to (-360, 1e-8]), the control-volume area from the ranked vertices
+// wrapped to (-360, 1e-8]), and the control-volume area summed over the
+// ranked vertices, from the node's absolute angles (StepNodeAngles): the same
+// subtraction, wrap and scaling as angle_about, so the same ranking bits
 struct Ranking {
     geo::Ranked fr[6], vr[6];
     double area_cv;
 };
 
+ODIS_HD inline void rank_angles(const MeshView& m, int nd, double te, geo::Ranked* fr, geo::Ranked* vr)
+{
+    const int k = m.nfriends(nd);
+    for (int j = 0; j < k; j++) {
+        double a = geo::angle_between(te, m.th_f[nd * 6 + j]) * 180. / geo::kGeoPi;
+        if (a > 0.0 + 1e-8) a -= 360.0;
+        fr[j] = {m.faces[nd * 6 + j], j, a};
+        double b = geo::angle_between(te, m.th_v[nd * 6 + j]) * 180. / geo::kGeoPi;
+        if (b > 0.0 + 1e-8) b -= 360.0;
+        vr[j] = {m.vertexes[nd * 6 + j], j, b};
+    }
+    geo::sort_desc(fr, k);
+    geo::sort_desc(vr, k);
+}
+
 ODIS_HD inline void rank_about(const MeshView& m, int nd, int e, Ranking& o)
 {
     const int k = m.nfriends(nd);
-    const geo::LL ie = m.ipos(e), c = m.node(nd);
-    for (int j = 0; j < k; j++) {
-        const int id = m.faces[nd * 6 + j];
-        double a = geo::angle_about(ie, m.ipos(id), c) * 180. / geo::kGeoPi;
-        if (a > 0.0 + 1e-8) a -= 360.0;
-        o.fr[j] = {id, a};
-        const int vid = m.vertexes[nd * 6 + j];
-        double b = geo::angle_about(ie, m.vpos(vid), c) * 180. / geo::kGeoPi;
-        if (b > 0.0 + 1e-8) b -= 360.0;
-        o.vr[j] = {vid, b};
-    }
-    geo::sort_desc(o.fr, k);
-    geo::sort_desc(o.vr, k);
+    int je = -1;
+    for (int j = 0; j < k; j++)
+        if (m.faces[nd * 6 + j] == e) je = j;
+    if (je < 0) m.fail();
+    const double te = je < 0 ? 0.0 : m.th_f[nd * 6 + je];
+    rank_angles(m, nd, te, o.fr, o.vr);
     double area_cv = 0.0;
-    for (int j = 0; j < k; j++) area_cv += geo::sph_tri_area(c, m.vpos(o.vr[j].id), m.vpos(o.vr[(j + 1) % k].id), m.r);
+    for (int j = 0; j < k; j++) area_cv += m.kcv[nd * 6 + o.vr[j].slot];
     o.area_cv = area_cv;
 }
+
+// node nd: absolute angles of its faces' intercepts and vertices, and the kite
+// areas (src/mesh.cpp:680-907: the control volume's triangles of consecutive
+// vertices, the two triangles of each vertex with its neighbouring faces'
+// intercepts).  A vertex lies between the faces ranked just before and after
+// it, whatever face the ranking starts from, so these areas serve every
+// ranking about the node; each face's ranking sums them in its own order.
+struct StepNodeAngles {
+    MeshView m;
+    ODIS_HD void operator()(int nd) const
+    {
+        const int k = m.nfriends(nd);
+        const geo::LL c = m.node(nd);
+        for (int j = 0; j < k; j++) {
+            m.th_f[nd * 6 + j] = geo::angle_in_plane(m.ipos(m.faces[nd * 6 + j]), c);
+            m.th_v[nd * 6 + j] = geo::angle_in_plane(m.vpos(m.vertexes[nd * 6 + j]), c);
+        }
+        geo::Ranked fr[6], vr[6];
+        rank_angles(m, nd, m.th_f[nd * 6], fr, vr);
+        for (int j = 0; j < k; j++) {
+            const geo::LL v = m.vpos(vr[j].id);
+            const int q = nd * 6 + vr[j].slot;
+            m.kcv[q] = geo::sph_tri_area(c, v, m.vpos(vr[(j + 1) % k].id), m.r);
+            m.ka1[q] = geo::sph_tri_area(c, v, m.ipos(fr[j].id), m.r);
+            m.ka2[q] = geo::sph_tri_area(c, v, m.ipos(fr[(j + 1) % k].id), m.r);
+        }
+    }
+};
 
 // TRiSK weights of face e (src/mesh.cpp:680-907): w = (sum_{j'<j} R_j' - 1/2) n_{e',node} t_{e,node}
 struct StepTrisk {
@@ -246,15 +288,12 @@ struct StepTrisk {
         for (int side = 0; side < 2; side++) {
             const int nd = m.face_nodes[e * 2 + side];
             const int k = m.nfriends(nd);
-            const geo::LL c = m.node(nd);
             Ranking rk;
             rank_about(m, nd, e, rk);
             double R[6];
             for (int j = 0; j < k; j++) {
-                const geo::LL v = m.vpos(rk.vr[j].id);
-                const double a1 = geo::sph_tri_area(c, v, m.ipos(rk.fr[j].id), m.r);
-                const double a2 = geo::sph_tri_area(c, v, m.ipos(rk.fr[(j + 1) % k].id), m.r);
-                R[j] = (a1 + a2) / rk.area_cv;
+                const int q = nd * 6 + rk.vr[j].slot;
+                R[j] = (m.ka1[q] + m.ka2[q]) / rk.area_cv;
             }
             const int tev = (m.face_nodes[e * 2] == nd) ? 1 : -1;
             for (int j = 0; j < k; j++) {
@@ -289,14 +328,12 @@ struct StepVertexR {
         const int k = m.nfriends(nd);
         int e = -1;
         for (int j = 0; j < k; j++) e = m.faces[nd * 6 + j] > e ? m.faces[nd * 6 + j] : e;
-        const geo::LL c = m.node(nd);
         Ranking rk;
         rank_about(m, nd, e, rk);
         for (int j = 0; j < k; j++) {
             const int vid = rk.vr[j].id;
-            const geo::LL v = m.vpos(vid);
-            const double a1 = geo::sph_tri_area(c, v, m.ipos(rk.fr[j].id), m.r);
-            const double a2 = geo::sph_tri_area(c, v, m.ipos(rk.fr[(j + 1) % k].id), m.r);
+            const int q = nd * 6 + rk.vr[j].slot;
+            const double a1 = m.ka1[q], a2 = m.ka2[q];
             int slot = -1;
             for (int q = 0; q < 3; q++)
                 if (m.vert_nodes[vid * 3 + q] == nd) { slot = q; break; }
@@ -433,6 +470,15 @@ int build_mesh_steps(X& x, int N, const double* node_sph, const int* friends, co
     x.run(E, StepFaceGeometry{v});
     if (x.failed(err.ptr)) return x.status() ? x.status() : ODIS_ERR_MESH;
 
+    auto th_f = x.template tmp<double>((size_t)N * 6, 0.0), th_v = x.template tmp<double>((size_t)N * 6, 0.0);
+    auto kcv = x.template tmp<double>((size_t)N * 6, 0.0), ka1 = x.template tmp<double>((size_t)N * 6, 0.0);
+    auto ka2 = x.template tmp<double>((size_t)N * 6, 0.0);
+    v.th_f = th_f.ptr;
+    v.th_v = th_v.ptr;
+    v.kcv = kcv.ptr;
+    v.ka1 = ka1.ptr;
+    v.ka2 = ka2.ptr;
+    x.run(N, StepNodeAngles{v});
     v.interp_friends = x.out(m.interp_friends, (size_t)E * 10, 0);
     v.interp_w = x.out(m.interp_w, (size_t)E * 10, 0.0);
     v.interp_n = x.out(m.interp_n, E, 0);
