@@ -12,10 +12,13 @@ ROOT = Path(__file__).resolve().parent.parent
 sys.path.insert(0, str(ROOT))
 
 # A GeodesicODIS checkout (its shipped grids and input.in serve as fixtures), named by the
-# environment variable ODIS_REFERENCE_ROOT; the tests that read it skip when it is not set.
+# environment variable ODIS_REFERENCE_ROOT.  Without it the tests use the byte-exact copies of
+# the smallest shipped files in tests/golden (make_reference_fixtures.py) and skip the rest.
 REF_ROOT = Path(os.environ["ODIS_REFERENCE_ROOT"]) if os.environ.get("ODIS_REFERENCE_ROOT") else None
 REF_INPUT = (REF_ROOT / "input_files") if REF_ROOT else Path("__no_reference_checkout__")
 REF_SKIP = "set ODIS_REFERENCE_ROOT to a GeodesicODIS checkout to run the tests on its shipped files"
+GOLDEN = ROOT / "tests" / "golden"
+_unpacked: dict[str, Path] = {}
 
 # Enceladus-like body of the benchmark configurations
 RADIUS = 252.1e3
@@ -46,9 +49,46 @@ def grid_dir(tmp_path_factory, built):
     return d
 
 
+def _golden_copy(rel: str) -> Path | None:
+    """The fixture copy of the reference file `rel`, unpacked once per process and checked against the
+    SHA-256 of the shipped file; None when tests/golden holds no copy of it."""
+    import atexit
+    import gzip
+    import hashlib
+    import shutil
+    import tempfile
+    if rel in _unpacked:
+        return _unpacked[rel]
+    gz = GOLDEN / (Path(rel).name + ".gz")
+    if not gz.exists():
+        return None
+    sums = dict(line.split()[::-1] for line in (GOLDEN / "MANIFEST.txt").read_text().splitlines() if line.strip())
+    data = gzip.decompress(gz.read_bytes())
+    assert hashlib.sha256(data).hexdigest() == sums[rel], f"{gz} does not match the shipped {rel}"
+    if "dir" not in _unpacked:
+        d = Path(tempfile.mkdtemp(prefix="odis_ref_"))
+        atexit.register(shutil.rmtree, d, True)
+        _unpacked["dir"] = d
+    out = _unpacked["dir"] / Path(rel).name
+    out.write_bytes(data)
+    _unpacked[rel] = out
+    return out
+
+
+def ref_file(rel: str) -> Path:
+    """A file of the reference checkout (path relative to its root), else its fixture copy; skips the
+    calling test when neither exists."""
+    if REF_ROOT is not None and (REF_ROOT / rel).exists():
+        return REF_ROOT / rel
+    p = _golden_copy(rel)
+    if p is None:
+        pytest.skip(REF_SKIP)
+    return p
+
+
 def ref_grid(level_baseline: int) -> Path:
     """The reference's shipped grid with 10*4^level+2 cells (its file is named one level higher)."""
-    return REF_INPUT / f"grid_l{level_baseline + 1}.txt"
+    return ref_file(f"input_files/grid_l{level_baseline + 1}.txt")
 
 
 def rel_err(a, b) -> float:

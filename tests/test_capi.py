@@ -90,10 +90,8 @@ def test_input_in_bad_enum_and_missing_file(built, tmp_path):
 def test_reference_input_in_parses(built):
     """The reference's own input.in (OBLIQ_WEST, advection true) parses with its documented values."""
     import geodesicodis_gb300 as g
-    from conftest import REF_ROOT, REF_SKIP
-    if REF_ROOT is None or not (REF_ROOT / "input.in").exists():
-        pytest.skip(REF_SKIP)
-    src = REF_ROOT / "input.in"
+    from conftest import ref_file
+    src = ref_file("input.in")
     inp = g.read_input(src)
     assert inp.params.potential == g.POT_OBLIQ_WEST
     assert inp.advection == 1 and inp.params.advection == 1 and inp.grid_level == 6

@@ -235,6 +235,22 @@ def test_config0_full_run_parity(grid_dir):
     assert po[-1] > 0
 
 
+@pytest.mark.parametrize("precision", [0, 2])
+def test_reference_grid_run_parity(precision):
+    """The configuration-0 physics on the reference's own shipped grid (input_files/grid_l4.txt, 642
+    cells), FP64 and DF64: 4000 steps (two orbits) within 1e-10 of the oracle."""
+    from conftest import ref_grid
+    orc, gpu = _pair(ref_grid(3), precision=precision)
+    po = orc.run(4000)
+    pg = gpu.run(4000)
+    _, vo, eo, _, _ = orc.get_state()
+    _, vg, eg, _, _ = gpu.get_state()
+    assert rel_err(eg, eo) < 1e-10
+    assert rel_err(vg, vo) < 1e-10
+    assert rel_err(pg, po) < 1e-10
+    assert po[-1] > 0
+
+
 def test_fp32_variant_power(grid_dir):
     """FP32 state and stencils, FP64 time accumulation and reductions: power within 1e-4 of FP64."""
     orc, gpu = _pair(grid_dir / "grid_3.txt", precision=1)

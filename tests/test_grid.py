@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import REF_INPUT, REF_SKIP, ref_grid
+from conftest import ref_grid
 
 
 def read_grid(path):
@@ -57,7 +57,6 @@ def test_clockwise_and_circumcentres(grid_dir, level):
             assert max(d) - min(d) < 1e-12
 
 
-@pytest.mark.skipif(not REF_INPUT.exists(), reason=REF_SKIP)
 @pytest.mark.parametrize("level", [2, 3, 4])
 def test_same_layout_as_reference_files(grid_dir, level):
     """Generated and shipped grids agree in size, pentagon count and orientation convention."""

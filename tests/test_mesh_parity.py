@@ -3,7 +3,7 @@ geometry and TRiSK weights must be bit-identical, since both follow the referenc
 import numpy as np
 import pytest
 
-from conftest import RADIUS, REF_INPUT, REF_SKIP, ref_grid
+from conftest import RADIUS, ref_grid
 from test_grid import read_grid
 
 
@@ -35,7 +35,6 @@ def test_generated_grids(grid_dir, level):
     _compare(grid_dir / f"grid_{level}.txt")
 
 
-@pytest.mark.skipif(not REF_INPUT.exists(), reason=REF_SKIP)
 @pytest.mark.parametrize("level", [2, 3, 4, 5])
 def test_reference_grids(built, level):
     _compare(ref_grid(level))

@@ -10,7 +10,7 @@ self-gravity term (SHTOOLS 4pi normalisation, csphase=-1)."""
 import numpy as np
 import pytest
 
-from conftest import ANGVEL_IN, RADIUS, REF_INPUT, REF_SKIP, ref_grid
+from conftest import ANGVEL_IN, RADIUS, ref_grid
 
 
 def spmv(csr, x):
@@ -61,7 +61,6 @@ def _convergence(paths, min_ratio):
     return errs
 
 
-@pytest.mark.skipif(not REF_INPUT.exists(), reason=REF_SKIP)
 def test_operator_convergence_reference_grids(built):
     # the shipped (tweaked) grids: second order for G and D, close to it for C
     _convergence([ref_grid(k) for k in (2, 3, 4, 5)], (3.5, 3.5, 2.5))
