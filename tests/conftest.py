@@ -98,7 +98,7 @@ def rel_err(a, b) -> float:
     return float(np.max(np.abs(a - b)) / s)
 
 
-def config0_params(**over):
+def ecc_case_params(**over):
     """The reference's own CPU-sized case: h = 10 km, alpha = 1e-5, ECC e = 0.0047, 2000 steps/orbit."""
     from oracle import pyoracle as O
     angvel, P, dt, n = O.derive_time(ANGVEL_IN, 59.197)

@@ -12,7 +12,7 @@ FP32-state method's power.
 import numpy as np
 import pytest
 
-from conftest import RADIUS, config0_params, rel_err
+from conftest import RADIUS, ecc_case_params, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 def _pair(path, precision=0, **over):
     import geodesicodis_gb300 as g
     from oracle import pyoracle as O
-    p = config0_params(**over)
+    p = ecc_case_params(**over)
     orc = O.OracleSolver(O.OracleMesh(path, RADIUS), **p)
     gp = g.make_params(precision=precision, **p)
     return orc, g.Solver(gp, g.Mesh.from_file(path, RADIUS))
@@ -35,7 +35,7 @@ def test_quadratic_update_energy(grid_dir):
     assert abs(a_g - a_o) / abs(a_o) < 1e-12
     # the |u|^3 branch, not the |u|^2 one: alpha / h |u|^3 per face
     q = (uv ** 2).sum(axis=1)
-    p = config0_params()
+    p = ecc_case_params()
     np.testing.assert_allclose(e_g, p["alpha"] / p["h"] * np.sqrt(q) * q, rtol=1e-14)
 
 

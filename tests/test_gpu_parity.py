@@ -9,7 +9,7 @@ Tolerances:
 import numpy as np
 import pytest
 
-from conftest import RADIUS, config0_params, rel_err
+from conftest import RADIUS, ecc_case_params, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 def _pair(path, precision=0, **over):
     import geodesicodis_gb300 as g
     from oracle import pyoracle as O
-    p = config0_params(**over)
+    p = ecc_case_params(**over)
     om = O.OracleMesh(path, RADIUS)
     orc = O.OracleSolver(om, **p)
     gm = g.Mesh.from_file(path, RADIUS)
@@ -192,7 +192,7 @@ def test_advection_options_are_checked(grid_dir):
     m = g.Mesh.from_file(grid_dir / "grid_2.txt", RADIUS)
     for over in (dict(precision=g.FP32), dict(sh_lmax=4, sh_factors=np.ones(5))):
         with pytest.raises(g.OdisError) as ei:
-            g.Solver(g.make_params(**config0_params(), advection=1, **over), m)
+            g.Solver(g.make_params(**ecc_case_params(), advection=1, **over), m)
         assert ei.value.code == g.ERR_ARG
 
 
@@ -221,7 +221,7 @@ def test_fused_fp64_parity(grid_dir, level, steps):
     assert rel_err(dvg, dvo) < 1e-10 and rel_err(deg, deo) < 1e-10
 
 
-def test_config0_full_run_parity(grid_dir):
+def test_ecc_case_full_run_parity(grid_dir):
     """The reference's own CPU-sized case: level 4 (2562 cells), ECC e=0.0047, h=10 km, alpha=1e-5,
     10 orbits x 2000 steps."""
     orc, gpu = _pair(grid_dir / "grid_4.txt")
@@ -237,8 +237,9 @@ def test_config0_full_run_parity(grid_dir):
 
 @pytest.mark.parametrize("precision", [0, 2])
 def test_reference_grid_run_parity(precision):
-    """The configuration-0 physics on the reference's own shipped grid (input_files/grid_l4.txt, 642
-    cells), FP64 and DF64: 4000 steps (two orbits) within 1e-10 of the oracle."""
+    """The ECC-tide case (e 0.0047, h 10 km, alpha 1e-5, 2000 steps per orbit) on the reference's own
+    shipped grid (input_files/grid_l4.txt, 642 cells), FP64 and DF64: 4000 steps (two orbits) within 1e-10
+    of the oracle."""
     from conftest import ref_grid
     orc, gpu = _pair(ref_grid(3), precision=precision)
     po = orc.run(4000)
@@ -359,7 +360,7 @@ def test_df64_parity(grid_dir, level, steps):
     assert rel_err(dvg, dvo) < 1e-10 and rel_err(deg, deo) < 1e-10
 
 
-def test_df64_config0_full_run(grid_dir):
+def test_df64_ecc_case_full_run(grid_dir):
     orc, gpu = _pair(grid_dir / "grid_4.txt", precision=2)
     po, pg = orc.run(20000), gpu.run(20000)
     _, vo, eo, _, _ = orc.get_state()

@@ -19,11 +19,11 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("precision", [0, 2])
 def test_persistent_loop_wait_runs_out(grid_dir, precision):
     import geodesicodis_gb300 as g
-    from conftest import config0_params
+    from conftest import ecc_case_params
     path = grid_dir / "grid_4.txt"
     mesh = g.Mesh.from_file(path, RADIUS)
-    a = g.Solver(g.make_params(precision=precision, **config0_params()), mesh)
-    b = g.Solver(g.make_params(precision=precision, **config0_params()), mesh)
+    a = g.Solver(g.make_params(precision=precision, **ecc_case_params()), mesh)
+    b = g.Solver(g.make_params(precision=precision, **ecc_case_params()), mesh)
     assert a.set_persistent(True) and b.set_persistent(True)
     a.run(50)
     state = a.get_state()

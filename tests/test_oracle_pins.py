@@ -137,13 +137,13 @@ def test_sh_lsq_round_trip(grid_dir):
 def test_oracle_rest_state_and_linearity(grid_dir):
     """No forcing and a zero state stay at rest; doubling the forcing doubles the response."""
     from oracle import pyoracle as O
-    from conftest import config0_params
+    from conftest import ecc_case_params
     m = O.OracleMesh(grid_dir / "grid_2.txt", RADIUS)
-    s0 = O.OracleSolver(m, **config0_params(potential=O.NONE))
+    s0 = O.OracleSolver(m, **ecc_case_params(potential=O.NONE))
     p = s0.run(50)
     assert np.all(p == 0.0)
-    a = O.OracleSolver(m, **config0_params())
-    b = O.OracleSolver(m, **config0_params(ecc=2 * 0.0047))
+    a = O.OracleSolver(m, **ecc_case_params())
+    b = O.OracleSolver(m, **ecc_case_params(ecc=2 * 0.0047))
     a.run(200); b.run(200)
     _, va, ea, _, _ = a.get_state()
     _, vb, eb, _, _ = b.get_state()
@@ -248,16 +248,16 @@ def test_lsq_flux_constant_and_smooth_fields(grid_dir):
 
 
 def test_advective_loop_stays_near_linear_at_small_amplitude(grid_dir):
-    """ab3Explicit with advection true (momentum advection + LSQ thickness flux): at the config-0
-    tide (eta / h ~ 2e-3) the nonlinear run stays within a fraction of a percent of the linear one,
+    """ab3Explicit with advection true (momentum advection + LSQ thickness flux): at the ECC tide of the
+    level-4 CPU-sized case (e 0.0047, h 10 km; eta / h ~ 2e-3) the nonlinear run stays within a fraction of a percent of the linear one,
     and the gap (discretisation differences of the PV-flux Coriolis term) shrinks with level."""
-    from conftest import config0_params
+    from conftest import ecc_case_params
     from oracle import pyoracle as O
     gaps = []
     for lv in (2, 3):
         om = O.OracleMesh(grid_dir / f"grid_{lv}.txt", RADIUS)
-        lin = O.OracleSolver(om, **config0_params())
-        adv = O.OracleSolver(om, **config0_params(), advection=1)
+        lin = O.OracleSolver(om, **ecc_case_params())
+        adv = O.OracleSolver(om, **ecc_case_params(), advection=1)
         pl, pa = lin.run(1500), adv.run(1500)
         _, vl, el, _, _ = lin.get_state()
         _, va, ea, _, _ = adv.get_state()
@@ -271,14 +271,14 @@ def test_oracle_quadratic_energy_branch(grid_dir):
     """updateEnergy QUADRATIC (src/energy.cpp:45-53): e_e = alpha / h sqrt(u^2 + v^2) (u^2 + v^2),
     restated here in numpy; LINEAR stays alpha 1000 h |u|^2.  Both means weight e_e by the same
     face areas, so their ratio is the area-weighted ratio of the two fields."""
-    from conftest import config0_params
+    from conftest import ecc_case_params
     from oracle import pyoracle as O
     om = O.OracleMesh(grid_dir / "grid_3.txt", RADIUS)
     uv = np.random.default_rng(5).standard_normal((om.n_edges, 2)) * 0.05
     q = uv[:, 0] * uv[:, 0] + uv[:, 1] * uv[:, 1]
     out = {}
     for fric, e_ref in ((1, 1e-5 / 1e4 * np.sqrt(q) * q), (0, 1e-5 * 1000.0 * 1e4 * q)):
-        avg, e = O.OracleSolver(om, **config0_params(friction=fric)).updateEnergy(uv)
+        avg, e = O.OracleSolver(om, **ecc_case_params(friction=fric)).updateEnergy(uv)
         np.testing.assert_allclose(e, e_ref, rtol=1e-15)
         out[fric] = avg
     assert out[0] > 0 and out[1] > 0 and out[1] < 1e-6 * out[0]

@@ -9,7 +9,7 @@ the smallest stable step count."""
 import numpy as np
 import pytest
 
-from conftest import RADIUS, config0_params
+from conftest import RADIUS, ecc_case_params
 
 A, B, Cc = 23 / 12, -16 / 12, 5 / 12
 
@@ -54,7 +54,7 @@ def test_oracle_run_follows_the_limit(grid_dir, ratio, grows):
     import geodesicodis_gb300 as g
     from oracle import pyoracle as O
     path = grid_dir / "grid_3.txt"
-    p = config0_params()
+    p = ecc_case_params()
     w = g.Mesh.from_file(path, RADIUS).gravity_wave_omega(p["g"], p["h"], 2000)
     p["dt"] = ratio * (6 / 11) / w
     s = O.OracleSolver(O.OracleMesh(path, RADIUS), **p)

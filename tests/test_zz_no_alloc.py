@@ -12,7 +12,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import RADIUS, config0_params
+from conftest import RADIUS, ecc_case_params
 
 pytestmark = pytest.mark.gpu
 
@@ -32,7 +32,7 @@ def test_noalloc_energy_matches_context_path(grid_dir):
     f = _entry()
     dev = torch.device("cuda:0")
     mesh = g.Mesh.from_file(grid_dir / "grid_4.txt", RADIUS)
-    p = config0_params()
+    p = ecc_case_params()
     sol = g.Solver(g.make_params(**p), mesh)
     E = mesh.n_edges
     area = torch.tensor(mesh.field(2), dtype=torch.float64, device=dev)
