@@ -675,6 +675,8 @@ def main():
     ap.add_argument("--sur-save", default=None, help="surrogate: write parameters, coefficients and orbit counts (npz)")
     ap.add_argument("--sur-refine", type=int, default=0,
                     help="surrogate: extra training members drawn around the worst-predicted costly ones")
+    ap.add_argument("--sur-ensemble", type=int, default=1,
+                    help="surrogate: networks averaged for the warm start (>1 also runs the first one alone)")
     ap.add_argument("--case-steps", type=int, default=30)
     ap.add_argument("--case-graph", action="store_true", help="--profile-case: force the graph-replayed kernels")
     args = ap.parse_args()
@@ -688,7 +690,7 @@ def main():
         build_ext.build()
         res = surrogate.experiment(n_train=args.sur_train, n_test=args.sur_test, level=args.sur_level,
                                    epochs=args.sur_epochs, log=lambda m: print(m, file=sys.stderr, flush=True),
-                                   save=args.sur_save, refine=args.sur_refine)
+                                   save=args.sur_save, refine=args.sur_refine, ensemble=args.sur_ensemble)
         print(json.dumps(res))
         return
     if args.profile_case == "batch":

@@ -200,12 +200,19 @@ def mixing(prm: dict) -> np.ndarray:
 
 
 class Surrogate:
-    """Network + the scalings between its units and the harmonic coefficients."""
+    """Network(s) + the scalings between their units and the harmonic coefficients.
 
-    def __init__(self, basis: MeshBasis, width=512, depth=3, seed=0):
+    ensemble > 1 trains that many networks of the same shape on the same data, each from its own
+    initialisation and minibatch order (seeds seed, seed + 1, ...), and predicts their mean.  The
+    prediction error of one network is dominated by its variance between fits (it grows with more
+    epochs), which the mean reduces."""
+
+    def __init__(self, basis: MeshBasis, width=512, depth=3, seed=0, ensemble: int = 1):
         self.basis = basis
         self.n_out = len(MODEL_PHASES) * basis.n_coef
-        self.net = MLP(2, width, depth, self.n_out, 2, seed=seed)
+        self.seed = seed
+        self.nets = [MLP(2, width, depth, self.n_out, 2, seed=seed + k) for k in range(max(1, int(ensemble)))]
+        self.net = self.nets[0]
         self.mu = self.sd = self.scale = None
 
     def _targets(self, coef: np.ndarray, prm: dict) -> np.ndarray:
@@ -224,7 +231,7 @@ class Surrogate:
     def fit(self, prm: dict, coef: np.ndarray, epochs=800, batch=128, lr=1e-3, seed=0, orbits=None):
         """Train on converged coefficients.  Each sample's loss is its relative squared error, weighted by
         sqrt(orbits) when the zero-start orbit counts are given: the slowly converging (low-drag) members
-        are where a warm start saves orbits."""
+        are where a warm start saves orbits.  Returns the first network's loss per epoch."""
         x = features(prm)
         self.mu, self.sd = x.mean(axis=0), x.std(axis=0) + 1e-12
         t = self._targets(coef, prm)
@@ -236,17 +243,24 @@ class Surrogate:
         if orbits is not None:
             cost = np.sqrt(np.maximum(np.asarray(orbits, np.float64), 1.0))
             w = w * cost / cost.mean()
-        losses = self.net.train((x - self.mu) / self.sd, tn, mix, w, epochs=epochs, batch=batch, lr=lr, seed=seed)
+        xn = (x - self.mu) / self.sd
+        losses = None
+        for k, net in enumerate(self.nets):
+            lk = net.train(xn, tn, mix, w, epochs=epochs, batch=batch, lr=lr, seed=seed + k)
+            losses = lk if losses is None else losses
         return losses
 
-    def predict_coef(self, prm: dict) -> np.ndarray:
+    def predict_coef(self, prm: dict, members: int | None = None) -> np.ndarray:
+        """Predicted coefficients: the mean of the first `members` networks (all by default)."""
         x = (features(prm) - self.mu) / self.sd
-        tn = self.net.predict(x, mixing(prm)).astype(np.float64)
+        mix = mixing(prm)
+        nets = self.nets[:members] if members else self.nets
+        tn = np.mean([net.predict(x, mix).astype(np.float64) for net in nets], axis=0)
         return self._coef(tn * self.scale, prm)
 
-    def warm_state(self, prm: dict):
+    def warm_state(self, prm: dict, members: int | None = None):
         """Predicted phase-0 (v, eta) for each parameter set."""
-        c = self.predict_coef(prm)[:, 0, :]
+        c = self.predict_coef(prm, members)[:, 0, :]
         return self.basis.state(c)
 
 
@@ -276,11 +290,14 @@ def refine_parameters(prm: dict, err: np.ndarray, orbits: np.ndarray, count: int
 
 
 def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epochs=800, batch=128, lr=1e-3,
-               round_orbits=10, max_orbits=400, log=print, save=None, tol: float = TOL, refine: int = 0) -> dict:
+               round_orbits=10, max_orbits=400, log=print, save=None, tol: float = TOL, refine: int = 0,
+               ensemble: int = 1) -> dict:
     """Train on solver runs, then compare orbits to convergence from rest and from the warm start.
     refine > 0: after the first fit, `refine` more training members are drawn around the worst-predicted
     costly ones (refine_parameters), run to convergence from the network's own warm start, and the
-    network is trained again on all of them."""
+    network is trained again on all of them.  ensemble > 1: the warm start is the mean of that many
+    networks (Surrogate), and the held-out members also run from the first network alone, on the same
+    data, for comparison."""
     t0 = time.time()
     common, period = S.common_params()
     meshes = S.SweepMeshes((level,))
@@ -295,7 +312,7 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
     tr = run_to_convergence(common, mesh, mtr, basis, round_orbits=round_orbits, max_orbits=max_orbits, log=log, tol=tol)
     t_data = time.time() - t1
     log(f"training data {t_data:.1f} s, {tr['cell_steps']:.3e} cell-steps")
-    sur = Surrogate(basis)
+    sur = Surrogate(basis, ensemble=ensemble)
     t2 = time.time()
     orb_tr = np.where(tr["orbits"] > 0, tr["orbits"], max_orbits + 1)
     losses = sur.fit(ptr, tr["coef"], epochs=epochs, batch=batch, lr=lr, orbits=orb_tr)
@@ -316,7 +333,7 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
         # their orbit cost from rest is unknown: the source member's stands in
         src_orbits = orb_tr[np.argsort(err_tr * np.sqrt(np.maximum(orb_tr, 1.0)))[::-1][:max(1, refine // 4)]]
         orb_tr = np.concatenate([orb_tr, np.repeat(src_orbits, 4)[:refine]])
-        sur = Surrogate(basis)
+        sur = Surrogate(basis, ensemble=ensemble)
         losses = sur.fit(ptr, tr["coef"], epochs=epochs, batch=batch, lr=lr, orbits=orb_tr)
         t_refine = time.time() - t5
         log(f"refinement: {refine} members around the worst-predicted, {t_refine:.1f} s, loss -> {losses[-1]:.3e}")
@@ -329,18 +346,25 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
     warm = run_to_convergence(common, mesh, mte, None, v0=v_w, eta0=e_w, round_orbits=round_orbits,
                               max_orbits=max_orbits, log=log, tol=tol)
     t_warm = time.time() - t4
+    single = None
+    if len(sur.nets) > 1:           # the first network alone, for comparison
+        v_s, e_s = sur.warm_state(pte, members=1)
+        single = run_to_convergence(common, mesh, mte, None, v0=v_s, eta0=e_s, round_orbits=round_orbits,
+                                    max_orbits=max_orbits, log=log, tol=tol)
     # the best a degree-8 warm start can do: start from the projection of the converged state itself
     v_t, e_t = basis.state(zero["coef"][:, 0, :])
     best = run_to_convergence(common, mesh, mte, None, v0=v_t, eta0=e_t, round_orbits=round_orbits,
                               max_orbits=max_orbits, log=log, tol=tol)
     pred = sur.predict_coef(pte)
     err = relative_coef_error(pred[:, 0], zero["coef"][:, 0])         # the phase-0 state the warm start loads
+    err1 = relative_coef_error(sur.predict_coef(pte, members=1)[:, 0], zero["coef"][:, 0]) if single else err
     if save:        # per member: parameters, orbit counts, prediction error (no coefficient arrays: a few hundred kB)
         np.savez_compressed(save, ptr_h=ptr["h"], ptr_alpha=ptr["alpha"], ptr_ecc=ptr["ecc"], ptr_obliq=ptr["obliq"],
                             pte_h=pte["h"], pte_alpha=pte["alpha"], pte_ecc=pte["ecc"], pte_obliq=pte["obliq"],
                             err_test=err, orbits_train=tr["orbits"], orbits_zero=zero["orbits"],
                             orbits_warm=warm["orbits"], orbits_best=best["orbits"], losses=losses,
-                            power_zero=zero["power"], power_warm=warm["power"])
+                            power_zero=zero["power"], power_warm=warm["power"], err_test_single=err1,
+                            orbits_warm_single=single["orbits"] if single else warm["orbits"])
     oz = np.where(zero["orbits"] > 0, zero["orbits"], max_orbits + 1)
     ow = np.where(warm["orbits"] > 0, warm["orbits"], max_orbits + 1)
     ob = np.where(best["orbits"] > 0, best["orbits"], max_orbits + 1)
@@ -362,9 +386,17 @@ def experiment(n_train=4096, n_test=512, level=5, seed_train=3, seed_test=4, epo
         "coef_rel_err_median": float(np.median(err)), "coef_rel_err_p90": float(np.quantile(err, 0.9)),
         "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
         "seconds": {"data": t_data, "train": t_fit, "refine": t_refine, "zero": t_zero, "warm": t_warm},
-        "refine": refine, "loss_weight": "relative squared error x sqrt(zero-start orbits)",
+        "refine": refine, "ensemble": len(sur.nets),
+        "loss_weight": "relative squared error x sqrt(zero-start orbits)",
         "epochs": epochs, "batch": batch, "lr": lr, "round_orbits": round_orbits,
         "cell_steps": {"data": tr["cell_steps"], "zero": zero["cell_steps"], "warm": warm["cell_steps"]},
         "max_orbits": max_orbits, "tol": tol,
     }
+    if single is not None:
+        os1 = np.where(single["orbits"] > 0, single["orbits"], max_orbits + 1)
+        res["single_network"] = {"orbits_ratio_total": float(np.sum(oz) / np.sum(os1)),
+                                 "orbits_warm_mean": float(np.mean(os1)),
+                                 "warm_not_converged": int(np.sum(single["orbits"] <= 0)),
+                                 "coef_rel_err_median": float(np.median(err1)),
+                                 "coef_rel_err_p90": float(np.quantile(err1, 0.9))}
     return res

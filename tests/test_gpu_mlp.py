@@ -74,6 +74,29 @@ def test_training_learns_a_smooth_map():
     net.close()
 
 
+def test_surrogate_ensemble_is_the_mean_of_its_networks(built):
+    """Surrogate(ensemble=3): three networks from different seeds, trained on the same data; the warm
+    start is their mean prediction, and members=1 gives the first network alone."""
+    from geodesicodis_gb300 import surrogate as SU
+    from geodesicodis_gb300 import sweep as S
+    meshes = S.SweepMeshes((2,))
+    basis = SU.MeshBasis(meshes.meshes[2], S.RADIUS, lmax=4)
+    prm = S.draw_parameters(96, 5, (2,))
+    coef = np.random.default_rng(0).standard_normal((96, SU.PHASES, basis.n_coef))
+    sur = SU.Surrogate(basis, width=64, depth=2, ensemble=3)
+    sur.fit(prm, coef, epochs=4, batch=32)
+    x = (SU.features(prm) - sur.mu) / sur.sd
+    each = [net.predict(x, SU.mixing(prm)).astype(np.float64) for net in sur.nets]
+    assert np.max(np.abs(each[0] - each[1])) > 1e-3 and np.max(np.abs(each[1] - each[2])) > 1e-3
+    np.testing.assert_allclose(sur.predict_coef(prm), sur._coef(np.mean(each, axis=0) * sur.scale, prm),
+                               rtol=1e-12, atol=0)
+    np.testing.assert_array_equal(sur.predict_coef(prm, members=1), sur._coef(each[0] * sur.scale, prm))
+    v, eta = sur.warm_state(prm)
+    assert v.shape == (96, meshes.meshes[2].n_edges) and eta.shape == (96, meshes.meshes[2].n_cells)
+    for net in sur.nets:
+        net.close()
+
+
 def test_warm_start_gains_on_the_solver(built):
     """The learned warm start, end to end at a small size: solver runs of 512 level-3 oceans from the sweep's
     parameter distribution train the network (the library's forward/backward/Adam kernels); 48 held-out
