@@ -66,6 +66,15 @@ def test_operator_convergence_reference_grids(built):
     _convergence([ref_grid(k) for k in (2, 3, 4, 5)], (3.5, 3.5, 2.5))
 
 
+def test_operator_convergence_reference_fixture_grids(built):
+    # the two smallest shipped grids (162 and 642 cells; fixtures when no checkout is named): the
+    # same orders between them, and the level-3 error norms of the shipped grid
+    errs = np.array([operator_errors(ref_grid(k)) for k in (2, 3)])
+    ratios = errs[0] / errs[1]
+    assert np.all(ratios > np.array([3.5, 3.5, 2.5])), ratios
+    assert errs[1, 0] < 5e-4 and errs[1, 1] < 3e-3 and errs[1, 2] < 3e-3, errs
+
+
 def test_operator_convergence_generated_grids(grid_dir):
     # plain recursive bisection: G second order, D a little below, C first order
     _convergence([grid_dir / f"grid_{k}.txt" for k in (2, 3, 4, 5)], (3.5, 3.0, 1.4))
