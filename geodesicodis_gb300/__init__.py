@@ -84,6 +84,7 @@ _SIGS = {
     "odis_mesh_from_arrays": ([C.c_int, _D, _I, _D, C.c_double, C.POINTER(_V)], C.c_int),
     "odis_grid_generate_arrays": ([C.c_int, C.c_int, _D, _I, _D], C.c_int),
     "odis_mesh_compare": ([_V, _V, _D, C.POINTER(C.c_longlong)], C.c_int),
+    "odis_text_round16": ([_D, _D, C.c_longlong], C.c_int),
     "odis_mesh_from_arrays": ([C.c_int, _D, _I, _D, C.c_double, C.POINTER(_V)], C.c_int),
     "odis_mesh_sizes": ([_V, _I, _I, _I], C.c_int),
     "odis_mesh_field": ([_V, C.c_int, _D], C.c_int),
@@ -187,6 +188,13 @@ def generate_grid(level: int, device: bool = False):
     _ck(lib().odis_grid_generate_arrays(int(level), int(bool(device)), _dp(nd), fr.ctypes.data_as(_I), _dp(cd)),
         "odis_grid_generate_arrays")
     return nd, fr, cd
+
+
+def text_round16(values) -> np.ndarray:
+    """Each value through the grid file's text form: float("%.16f" % v), as the generators store coordinates."""
+    x = np.ascontiguousarray(values, np.float64).ravel().copy()
+    _ck(lib().odis_text_round16(_dp(x), _dp(x), x.size), "odis_text_round16")
+    return x.reshape(np.shape(values))
 
 
 def analytical_state(params: Params, mesh: "Mesh", t: float = 0.0):

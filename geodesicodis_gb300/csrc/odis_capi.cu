@@ -13,6 +13,7 @@
 #include "odis_advection.cuh"
 #include "odis_df64.cuh"
 #include "odis_persistent.cuh"
+#include "odis_text_round.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -169,6 +170,13 @@ extern "C" odis_status odis_grid_generate_arrays(int level, int on_device, doubl
     std::memcpy(node_deg, g.node_deg.data(), sizeof(double) * g.node_deg.size());
     std::memcpy(friends, g.friends.data(), sizeof(int) * g.friends.size());
     std::memcpy(cent_deg, g.cent_deg.data(), sizeof(double) * g.cent_deg.size());
+    return ODIS_OK;
+}
+
+extern "C" odis_status odis_text_round16(const double* in, double* out, long long n)
+{
+    if (n < 0 || (n > 0 && (!in || !out))) return ODIS_ERR_ARG;
+    for (long long i = 0; i < n; i++) out[i] = text_round16(in[i]);
     return ODIS_OK;
 }
 

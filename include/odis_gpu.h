@@ -210,6 +210,12 @@ odis_status odis_mesh_from_arrays_device(int n_nodes, const double* node_sph, co
  * writes): node_deg [N][2], friends [N][6] and cent_deg [N][6][2] in degrees,
  * N = 10*4^n+2, generated on the host (on_device = 0) or the current device. */
 odis_status odis_grid_generate_arrays(int level, int on_device, double* node_deg, int* friends, double* cent_deg);
+/* out[i] = the double that strtod returns for printf("%.16f", in[i]): the
+ * coordinates' round trip through the reference's grid-file text
+ * (src/mesh.cpp:4016-4089), which the grid generators apply to every node and
+ * circumcentre coordinate they store, computed in exact integer arithmetic
+ * (host; in and out may be the same array). */
+odis_status odis_text_round16(const double* in, double* out, long long n);
 /* Compare two meshes array by array: *int_mismatches counts differing entries
  * of the integer arrays (sizes included), *max_rel is the largest
  * max|a - b| / max|b| over the floating-point arrays (longitudes modulo 2 pi). */

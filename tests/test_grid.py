@@ -113,3 +113,24 @@ def test_oracle_loading_factors_match_product(built):
     np.testing.assert_array_equal(a[1:], b[1:])        # l = 0 is unused (the reference divides by l)
     np.testing.assert_array_equal(O.benchmark_sh_factors(0.113, 252.1e3, 16, 1),
                                   g.benchmark_sh_factors(0.113, 252.1e3, 16, 1))
+
+
+def test_text_round16_is_printf_then_strtod(built):
+    """odis_text_round16 (exact integer arithmetic, shared by the host and device generators) against
+    float("%.16f" % v): Python's formatting and parsing round correctly, as glibc's printf and strtod do.
+    Random values at every scale the generators meet, and values within a few ulps of a tie of the 16th
+    decimal, where a one-ulp slip in the arithmetic would show."""
+    import geodesicodis_gb300 as g
+    rng = np.random.default_rng(2024)
+    parts = [rng.uniform(-1, 1, 200000), rng.uniform(-360, 360, 50000),
+             np.sign(rng.uniform(-1, 1, 100000)) * 10.0 ** rng.uniform(-25, 0, 100000),
+             np.array([0.0, -0.0, 1.0, -1.0, 0.5, 1e-16, 5e-17, 4.9999999999999999e-17, 1.5e-16, 2.5e-16,
+                       0.9999999999999999, 0.99999999999999995, 89.99999999999999, 1e-300, 5e-324])]
+    k = rng.integers(0, 10 ** 16, 100000)
+    ties = (k + 0.5) * 1e-16                                   # nearest doubles to ties of the 16th decimal
+    parts += [ties, np.nextafter(ties, 0), np.nextafter(ties, 1), -ties]
+    v = np.concatenate(parts)
+    got = g.text_round16(v)
+    want = np.array([float("%.16f" % x) for x in v])
+    bad = np.flatnonzero(got.view(np.int64) != want.view(np.int64))
+    assert bad.size == 0, [(v[i], got[i], want[i]) for i in bad[:5]]
